@@ -1,0 +1,703 @@
+// gkrt_api.cu — host side of the C ABI declared in include/gkrt.h.
+//
+// Mirrors the lifecycle of the reference's path-tracing logic renderer
+// (src/Rendering/PathTracing/PathTracingRenderer.cpp:18-232): create, (re)size images,
+// load a scene, build acceleration structures, then per frame: rt pass -> reproject pass
+// -> compose pass -> history hand-over. Every entry point returns a status code; no
+// exception crosses the boundary.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gk_shade.cuh"
+#include "gkrt_internal.h"
+
+using namespace gk;
+
+struct GkrtContext {
+    int device = 0;
+    uint32_t watchdog_ms = 60000;
+    std::string err;
+    uint32_t W = 0, H = 0;
+    void* img[GKRT_IMG_COUNT] = {};
+
+    bool has_scene = false;
+    std::vector<GkrtMesh> meshes;
+    std::vector<GkrtInstance> inst;
+    std::vector<float> pos_host;      // float4 per vertex (kept for BVH builds)
+    std::vector<uint32_t> idx_host;
+    uint32_t nvert = 0, nidx = 0, nmat = 0;
+    float4* d_pos = nullptr;
+    float4* d_nrm = nullptr;
+    uint32_t* d_slot = nullptr;
+    uint32_t* d_idx = nullptr;
+    GkrtMaterial* d_mat = nullptr;
+    uint32_t* d_inst_mat = nullptr;
+    float* d_inst_prev = nullptr;
+    DevInst* d_inst = nullptr;
+    uint32_t* d_cubes = nullptr;
+    uint32_t* d_voxels = nullptr;
+
+    // acceleration structures
+    std::vector<BvhNode> blas_nodes;
+    std::vector<int> blas_root;
+    std::vector<float> blas_box;      // 6 per mesh
+    BvhNode* d_nodes = nullptr;
+    size_t d_nodes_cap = 0;
+    float4* d_tris = nullptr;
+    int tlas_root = -1;
+    uint32_t tlas_nodes = 0;
+    bool blas_ready = false, tlas_ready = false;
+
+    unsigned long long* d_counters = nullptr;   // see flush_counters: 5 per-pass slots + total rays
+    uint32_t* d_error = nullptr;
+};
+
+namespace {
+
+int fail(GkrtContext* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(GkrtContext* c, cudaError_t e, const char* what) {
+    int code = (e == cudaErrorMemoryAllocation) ? GKRT_ERR_OOM : GKRT_ERR_CUDA;
+    return fail(c, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define GK_CUDA(call)                                             \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+size_t image_bytes_per_px(int id) {
+    switch (id) {
+        case GKRT_IMG_OBJECT_ID: case GKRT_IMG_OBJECT_ID_PREV: case GKRT_IMG_MOTION_MOMENT:
+        case GKRT_IMG_HIT_INST: case GKRT_IMG_HIT_PRIM: case GKRT_IMG_PREV_DEPTH:
+            return 4;
+        case GKRT_IMG_MOTION:
+            return 8;
+        default:
+            return 16;
+    }
+}
+uint32_t image_format(int id) {
+    switch (id) {
+        case GKRT_IMG_OBJECT_ID: case GKRT_IMG_OBJECT_ID_PREV: case GKRT_IMG_MOTION_MOMENT:
+        case GKRT_IMG_HIT_INST: case GKRT_IMG_HIT_PRIM:
+            return GKRT_FMT_U32;
+        case GKRT_IMG_PREV_DEPTH:
+            return GKRT_FMT_F32;
+        case GKRT_IMG_MOTION:
+            return GKRT_FMT_F32X2;
+        default:
+            return GKRT_FMT_F32X4;
+    }
+}
+
+void free_images(GkrtContext* c) {
+    for (auto& p : c->img) dfree(p);
+    c->W = c->H = 0;
+}
+
+void free_scene(GkrtContext* c) {
+    dfree(c->d_pos); dfree(c->d_nrm); dfree(c->d_slot); dfree(c->d_idx); dfree(c->d_mat);
+    dfree(c->d_inst_mat); dfree(c->d_inst_prev); dfree(c->d_inst); dfree(c->d_cubes); dfree(c->d_voxels);
+    dfree(c->d_nodes); dfree(c->d_tris);
+    c->d_nodes_cap = 0;
+    c->has_scene = false;
+    c->blas_ready = c->tlas_ready = false;
+    c->tlas_root = -1;
+    c->meshes.clear(); c->inst.clear(); c->pos_host.clear(); c->idx_host.clear();
+    c->blas_nodes.clear(); c->blas_root.clear(); c->blas_box.clear();
+}
+
+template <class T>
+int upload(GkrtContext* ctx, T*& dst, const void* src, size_t bytes) {
+    dfree(dst);
+    if (bytes == 0) return GKRT_OK;
+    GK_CUDA(cudaMalloc((void**)&dst, bytes));
+    GK_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return GKRT_OK;
+}
+
+bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+int validate_instances(GkrtContext* ctx, const GkrtInstance* in, uint32_t n, uint32_t nmesh, uint32_t nmat) {
+    for (uint32_t i = 0; i < n; ++i) {
+        if (in[i].mesh_id >= nmesh) return fail(ctx, GKRT_ERR_INVALID_ARG, "instance mesh_id out of range");
+        for (int k = 0; k < 16; ++k)
+            if (in[i].mat_id[k] >= nmat && nmat > 0)
+                return fail(ctx, GKRT_ERR_INVALID_ARG, "instance mat_id out of range");
+        for (int k = 0; k < 12; ++k)
+            if (!std::isfinite(in[i].world[k]) || !std::isfinite(in[i].world_inv[k]) ||
+                !std::isfinite(in[i].combined_prev[k]))
+                return fail(ctx, GKRT_ERR_INVALID_ARG, "non-finite instance transform");
+        // world * world_inv must be the identity
+        for (int r = 0; r < 3; ++r)
+            for (int cc = 0; cc < 4; ++cc) {
+                double s = (cc == 3) ? (double)in[i].world[4 * r + 3] : 0.0;
+                for (int k = 0; k < 3; ++k) s += (double)in[i].world[4 * r + k] * (double)in[i].world_inv[4 * k + cc];
+                double want = (r == cc) ? 1.0 : 0.0;
+                double scale = 1.0 + std::fabs((double)in[i].world[4 * r + 3]);
+                if (std::fabs(s - want) > 1e-3 * scale)
+                    return fail(ctx, GKRT_ERR_INVALID_ARG, "world_inv is not the inverse of world");
+            }
+    }
+    return GKRT_OK;
+}
+
+int upload_instances(GkrtContext* ctx) {
+    const uint32_t n = (uint32_t)ctx->inst.size();
+    std::vector<uint32_t> mats(16 * (size_t)n);
+    std::vector<float> prev(12 * (size_t)n);
+    std::vector<DevInst> di(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const GkrtInstance& s = ctx->inst[i];
+        std::memcpy(&mats[16 * (size_t)i], s.mat_id, 64);
+        std::memcpy(&prev[12 * (size_t)i], s.combined_prev, 48);
+        std::memcpy(di[i].winv, s.world_inv, 48);
+        const GkrtMesh& m = ctx->meshes[s.mesh_id];
+        di[i].blas_root = ctx->blas_ready ? ctx->blas_root[s.mesh_id] : -1;
+        di[i].index_offset = m.index_offset;
+        di[i].vertex_offset = m.vertex_offset;
+        di[i].instance_id = s.instance_id;
+    }
+    int rc;
+    if ((rc = upload(ctx, ctx->d_inst_mat, mats.data(), mats.size() * 4)) != GKRT_OK) return rc;
+    if ((rc = upload(ctx, ctx->d_inst_prev, prev.data(), prev.size() * 4)) != GKRT_OK) return rc;
+    if ((rc = upload(ctx, ctx->d_inst, di.data(), di.size() * sizeof(DevInst))) != GKRT_OK) return rc;
+    return GKRT_OK;
+}
+
+int build_blas(GkrtContext* ctx) {
+    const uint32_t nm = (uint32_t)ctx->meshes.size();
+    ctx->blas_nodes.clear();
+    ctx->blas_root.assign(nm, -1);
+    ctx->blas_box.assign(6 * (size_t)nm, 0.0f);
+    std::vector<float4> tris;
+    for (uint32_t mi = 0; mi < nm; ++mi) {
+        const GkrtMesh& m = ctx->meshes[mi];
+        const uint32_t nt = m.index_count / 3;
+        std::vector<float> boxes(6 * (size_t)nt);
+        float rb[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t t = 0; t < nt; ++t) {
+            for (int k = 0; k < 3; ++k) { boxes[6 * t + k] = INFINITY; boxes[6 * t + 3 + k] = -INFINITY; }
+            for (int v = 0; v < 3; ++v) {
+                const float* p = &ctx->pos_host[4 * (size_t)(ctx->idx_host[m.index_offset + 3 * t + v] + m.vertex_offset)];
+                for (int k = 0; k < 3; ++k) {
+                    boxes[6 * t + k] = std::min(boxes[6 * t + k], p[k]);
+                    boxes[6 * t + 3 + k] = std::max(boxes[6 * t + 3 + k], p[k]);
+                }
+            }
+            for (int k = 0; k < 3; ++k) {
+                rb[k] = std::min(rb[k], boxes[6 * t + k]);
+                rb[3 + k] = std::max(rb[3 + k], boxes[6 * t + 3 + k]);
+            }
+        }
+        std::memcpy(&ctx->blas_box[6 * (size_t)mi], rb, sizeof(rb));
+        if (nt == 0) continue;
+        HostBvh hb;
+        build_bvh_host(boxes.data(), nt, 4, (uint32_t)ctx->blas_nodes.size(), (uint32_t)(tris.size() / 3), false, hb);
+        if (hb.depth > kStackSize - 24)
+            return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "mesh BVH deeper than the traversal stack allows");
+        ctx->blas_root[mi] = hb.root;
+        ctx->blas_nodes.insert(ctx->blas_nodes.end(), hb.nodes.begin(), hb.nodes.end());
+        for (uint32_t k = 0; k < nt; ++k) {
+            const uint32_t prim = hb.order[k];
+            for (int v = 0; v < 3; ++v) {
+                const float* p = &ctx->pos_host[4 * (size_t)(ctx->idx_host[m.index_offset + 3 * prim + v] + m.vertex_offset)];
+                float w = 0.0f;
+                if (v == 0) std::memcpy(&w, &prim, 4);
+                tris.push_back(make_float4(p[0], p[1], p[2], w));
+            }
+        }
+    }
+    int rc = upload(ctx, ctx->d_tris, tris.data(), tris.size() * sizeof(float4));
+    if (rc != GKRT_OK) return rc;
+    ctx->blas_ready = true;
+    return GKRT_OK;
+}
+
+int build_tlas(GkrtContext* ctx) {
+    const uint32_t n = (uint32_t)ctx->inst.size();
+    std::vector<float> boxes;
+    std::vector<uint32_t> map;
+    for (uint32_t i = 0; i < n; ++i) {
+        const GkrtInstance& in = ctx->inst[i];
+        if (!in.visible || ctx->blas_root[in.mesh_id] < 0) continue;
+        const float* rb = &ctx->blas_box[6 * (size_t)in.mesh_id];
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int c = 0; c < 8; ++c) {
+            double p[3] = {(c & 1) ? rb[3] : rb[0], (c & 2) ? rb[4] : rb[1], (c & 4) ? rb[5] : rb[2]};
+            for (int r = 0; r < 3; ++r) {
+                double v = (double)in.world[4 * r] * p[0] + (double)in.world[4 * r + 1] * p[1] +
+                           (double)in.world[4 * r + 2] * p[2] + (double)in.world[4 * r + 3];
+                lo[r] = std::min(lo[r], v);
+                hi[r] = std::max(hi[r], v);
+            }
+        }
+        // widen: the mesh level traverses the FP32-transformed ray, whose points sit within
+        // rounding of the world ray's
+        for (int r = 0; r < 3; ++r) {
+            double pad = 1e-5 * (std::fabs(lo[r]) + std::fabs(hi[r]) + (hi[r] - lo[r])) + 1e-7;
+            boxes.push_back((float)(lo[r] - pad));
+        }
+        for (int r = 0; r < 3; ++r) {
+            double pad = 1e-5 * (std::fabs(lo[r]) + std::fabs(hi[r]) + (hi[r] - lo[r])) + 1e-7;
+            boxes.push_back((float)(hi[r] + pad));
+        }
+        map.push_back(i);
+    }
+    // boxes were pushed as lo xyz then hi xyz per instance
+    HostBvh hb;
+    const uint32_t base = (uint32_t)ctx->blas_nodes.size();
+    build_bvh_host(boxes.data(), (uint32_t)map.size(), 1, base, 0, true, hb);
+    // leaf payloads hold positions in `map`; rewrite them to instance indices
+    for (auto& nd : hb.nodes) {
+        int* r[2] = {&nd.d.x, &nd.d.y};
+        for (int k = 0; k < 2; ++k)
+            if (*r[k] < 0 && *r[k] != kRefPop) {
+                uint32_t payload = ~(uint32_t)(*r[k]);
+                uint32_t pos = payload >> 3;
+                *r[k] = (int)(~(map[pos] << 3));
+            }
+    }
+    if (hb.depth > 24 + 8) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "instance BVH too deep");
+    const size_t total = ctx->blas_nodes.size() + hb.nodes.size();
+    if (total > ctx->d_nodes_cap) {
+        dfree(ctx->d_nodes);
+        cudaError_t e = cudaMalloc((void**)&ctx->d_nodes, std::max<size_t>(total, 1) * sizeof(BvhNode));
+        if (e != cudaSuccess) { ctx->d_nodes_cap = 0; return cuda_fail(ctx, e, "cudaMalloc(nodes)"); }
+        ctx->d_nodes_cap = std::max<size_t>(total, 1);
+        if (!ctx->blas_nodes.empty()) {
+            e = cudaMemcpy(ctx->d_nodes, ctx->blas_nodes.data(), ctx->blas_nodes.size() * sizeof(BvhNode),
+                           cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(blas nodes)");
+        }
+    }
+    if (!hb.nodes.empty()) {
+        cudaError_t e = cudaMemcpy(ctx->d_nodes + base, hb.nodes.data(), hb.nodes.size() * sizeof(BvhNode),
+                                   cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(tlas nodes)");
+    }
+    ctx->tlas_root = map.empty() ? -1 : hb.root;
+    ctx->tlas_nodes = (uint32_t)hb.nodes.size();
+    ctx->tlas_ready = true;
+    return upload_instances(ctx);
+}
+
+int ensure_bvh(GkrtContext* ctx, uint32_t flags) {
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    int rc;
+    if ((flags & GKRT_BUILD_BLAS) || !ctx->blas_ready) {
+        if ((rc = build_blas(ctx)) != GKRT_OK) return rc;
+        // nodes must be re-uploaded with the new BLAS part
+        dfree(ctx->d_nodes);
+        ctx->d_nodes_cap = 0;
+        ctx->tlas_ready = false;
+    }
+    if ((flags & GKRT_BUILD_TLAS) || !ctx->tlas_ready) {
+        if ((rc = build_tlas(ctx)) != GKRT_OK) return rc;
+    }
+    return GKRT_OK;
+}
+
+SceneView scene_view(GkrtContext* c) {
+    SceneView S;
+    S.nodes = c->d_nodes;
+    S.tris = c->d_tris;
+    S.inst = c->d_inst;
+    S.tlas_root = c->tlas_root;
+    S.error = c->d_error;
+    return S;
+}
+
+int check_frame(GkrtContext* ctx, const GkrtFrameConstants* fc) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!fc) return fail(ctx, GKRT_ERR_INVALID_ARG, "null frame constants");
+    if (ctx->W == 0 || ctx->H == 0) return fail(ctx, GKRT_ERR_STATE, "gkrt_resize was not called");
+    return GKRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gkrt_abi_version(void) { return GKRT_ABI_VERSION; }
+
+int gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out) {
+    if (!out) return GKRT_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return GKRT_ERR_NO_DEVICE;
+    }
+    GkrtContext* ctx = new (std::nothrow) GkrtContext();
+    if (!ctx) return GKRT_ERR_OOM;
+    ctx->device = desc ? desc->device : 0;
+    if (desc && desc->watchdog_ms) ctx->watchdog_ms = desc->watchdog_ms;
+    if (ctx->device < 0 || ctx->device >= ndev) { delete ctx; return GKRT_ERR_INVALID_ARG; }
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_counters, 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_error, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_counters, 0, 8 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        dfree(ctx->d_counters);
+        dfree(ctx->d_error);
+        delete ctx;
+        return e == cudaErrorMemoryAllocation ? GKRT_ERR_OOM : GKRT_ERR_CUDA;
+    }
+    *out = ctx;
+    return GKRT_OK;
+}
+
+int gkrt_context_destroy(GkrtContext* ctx) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    free_images(ctx);
+    free_scene(ctx);
+    dfree(ctx->d_counters);
+    dfree(ctx->d_error);
+    delete ctx;
+    return GKRT_OK;
+}
+
+const char* gkrt_last_error_message(const GkrtContext* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int gkrt_resize(GkrtContext* ctx, uint32_t width, uint32_t height) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (width == 0 || height == 0 || width > 16384 || height > 16384)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "image size must be 1..16384");
+    cudaSetDevice(ctx->device);
+    free_images(ctx);
+    const size_t px = (size_t)width * height;
+    for (int i = 0; i < GKRT_IMG_COUNT; ++i) {
+        GK_CUDA(cudaMalloc(&ctx->img[i], px * image_bytes_per_px(i)));
+        GK_CUDA(cudaMemset(ctx->img[i], 0, px * image_bytes_per_px(i)));
+    }
+    ctx->W = width;
+    ctx->H = height;
+    return GKRT_OK;
+}
+
+int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!d) return fail(ctx, GKRT_ERR_INVALID_ARG, "null scene");
+    if ((d->vertex_count && (!d->positions || !d->normals || !d->material_slots)) ||
+        (d->index_count && !d->indices) || (d->mesh_count && !d->meshes) || (d->material_count == 0) ||
+        !d->materials || (d->instance_count && !d->instances) || (d->light_count && !d->lights))
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "scene arrays missing for non-zero counts");
+    if (d->instance_count > (1u << 24)) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "too many instances");
+    if ((uint64_t)d->index_count / 3 >= (1u << 28)) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "too many triangles");
+    for (uint32_t i = 0; i < d->vertex_count; ++i)
+        if (!finite3(d->positions + 4 * (size_t)i) || !finite3(d->normals + 4 * (size_t)i))
+            return fail(ctx, GKRT_ERR_INVALID_ARG, "non-finite vertex position or normal");
+    for (uint32_t i = 0; i < d->vertex_count; ++i)
+        if (d->material_slots[i] > 15u) return fail(ctx, GKRT_ERR_INVALID_ARG, "material slot above 15");
+    for (uint32_t m = 0; m < d->mesh_count; ++m) {
+        const GkrtMesh& ms = d->meshes[m];
+        if (ms.index_count % 3 != 0) return fail(ctx, GKRT_ERR_INVALID_ARG, "mesh index_count not a multiple of 3");
+        if ((uint64_t)ms.index_offset + ms.index_count > d->index_count)
+            return fail(ctx, GKRT_ERR_INVALID_ARG, "mesh index range outside the index buffer");
+        if ((uint64_t)ms.vertex_offset + ms.vertex_count > d->vertex_count)
+            return fail(ctx, GKRT_ERR_INVALID_ARG, "mesh vertex range outside the vertex buffer");
+        for (uint32_t k = 0; k < ms.index_count; ++k)
+            if (d->indices[ms.index_offset + k] >= ms.vertex_count)
+                return fail(ctx, GKRT_ERR_INVALID_ARG, "index outside its mesh's vertex range");
+    }
+    for (uint32_t i = 0; i < d->material_count; ++i) {
+        const GkrtMaterial& mt = d->materials[i];
+        if (mt.diffuse_texture_id >= 0 || mt.mra_texture_id >= 0 || mt.normal_texture_id >= 0)
+            return fail(ctx, GKRT_ERR_UNSUPPORTED, "textured materials are outside this pass (texture ids must be -1)");
+        if (mt.material_model > GKRT_MAT_MIXTURE) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown material model");
+    }
+    int rc = validate_instances(ctx, d->instances, d->instance_count, d->mesh_count, d->material_count);
+    if (rc != GKRT_OK) return rc;
+    cudaSetDevice(ctx->device);
+    free_scene(ctx);
+    ctx->meshes.assign(d->meshes, d->meshes + d->mesh_count);
+    ctx->inst.assign(d->instances, d->instances + d->instance_count);
+    ctx->pos_host.assign(d->positions, d->positions + 4 * (size_t)d->vertex_count);
+    ctx->idx_host.assign(d->indices, d->indices + d->index_count);
+    ctx->nvert = d->vertex_count;
+    ctx->nidx = d->index_count;
+    ctx->nmat = d->material_count;
+    if ((rc = upload(ctx, ctx->d_pos, d->positions, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
+    if ((rc = upload(ctx, ctx->d_nrm, d->normals, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
+    if ((rc = upload(ctx, ctx->d_slot, d->material_slots, 4 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
+    if ((rc = upload(ctx, ctx->d_idx, d->indices, 4 * (size_t)d->index_count)) != GKRT_OK) return rc;
+    if ((rc = upload(ctx, ctx->d_mat, d->materials, sizeof(GkrtMaterial) * (size_t)d->material_count)) != GKRT_OK)
+        return rc;
+    if (d->probe_cubes && d->probe_voxels) {
+        const size_t n = (size_t)192 * 192 * 48;
+        if ((rc = upload(ctx, ctx->d_cubes, d->probe_cubes, n * 14 * 4)) != GKRT_OK) return rc;
+        if ((rc = upload(ctx, ctx->d_voxels, d->probe_voxels, n * 4 * 4)) != GKRT_OK) return rc;
+    }
+    ctx->has_scene = true;
+    return ensure_bvh(ctx, GKRT_BUILD_ALL);
+}
+
+int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count, void* stream) {
+    (void)stream;
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    if (!instances || count != ctx->inst.size())
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "instance update must keep the instance count");
+    int rc = validate_instances(ctx, instances, count, (uint32_t)ctx->meshes.size(), ctx->nmat);
+    if (rc != GKRT_OK) return rc;
+    cudaSetDevice(ctx->device);
+    ctx->inst.assign(instances, instances + count);
+    return build_tlas(ctx);
+}
+
+int gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream) {
+    (void)stream;
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    return ensure_bvh(ctx, flags);
+}
+
+int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
+    int rc = check_frame(ctx, fc);
+    if (rc != GKRT_OK) return rc;
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    if (fc->nee_mode != GKRT_NEE_REFERENCE)
+        return fail(ctx, GKRT_ERR_UNSUPPORTED, "nee_mode not supported by this build");
+    cudaSetDevice(ctx->device);
+    if ((rc = ensure_bvh(ctx, 0)) != GKRT_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    ShadeScene sc;
+    sc.S = scene_view(ctx);
+    sc.normals = ctx->d_nrm;
+    sc.slots = ctx->d_slot;
+    sc.indices = ctx->d_idx;
+    sc.inst_mat = ctx->d_inst_mat;
+    sc.inst_prev = ctx->d_inst_prev;
+    sc.mats = ctx->d_mat;
+    sc.nmat = ctx->nmat;
+    sc.cubes = ctx->d_cubes;
+    sc.voxels = ctx->d_voxels;
+    PixelImages im;
+    im.single_diffuse = (float4*)ctx->img[GKRT_IMG_SINGLE_DIFFUSE];
+    im.single_specular = (float4*)ctx->img[GKRT_IMG_SINGLE_SPECULAR];
+    im.albedo = (float4*)ctx->img[GKRT_IMG_ALBEDO];
+    im.normal = (float4*)ctx->img[GKRT_IMG_NORMAL];
+    im.object_id = (uint32_t*)ctx->img[GKRT_IMG_OBJECT_ID];
+    im.motion = (float2*)ctx->img[GKRT_IMG_MOTION];
+    im.prev_depth = (float*)ctx->img[GKRT_IMG_PREV_DEPTH];
+    im.motion_moment = (uint32_t*)ctx->img[GKRT_IMG_MOTION_MOMENT];
+    im.hit_inst = (uint32_t*)ctx->img[GKRT_IMG_HIT_INST];
+    im.hit_prim = (uint32_t*)ctx->img[GKRT_IMG_HIT_PRIM];
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, im, ctx->d_counters, st));
+    return GKRT_OK;
+}
+
+int gkrt_reproject_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
+    int rc = check_frame(ctx, fc);
+    if (rc != GKRT_OK) return rc;
+    cudaSetDevice(ctx->device);
+    ReprojectArgs a;
+    a.W = (int)ctx->W; a.H = (int)ctx->H;
+    a.progressive = fc->progressive_render;
+    a.temporal_frames = fc->temporal_frames;
+    a.src_d = (const float4*)ctx->img[GKRT_IMG_SINGLE_DIFFUSE];
+    a.src_s = (const float4*)ctx->img[GKRT_IMG_SINGLE_SPECULAR];
+    a.src_a = (const float4*)ctx->img[GKRT_IMG_ALBEDO];
+    a.prev_d = (const float4*)ctx->img[GKRT_IMG_PREV_DIFFUSE];
+    a.prev_s = (const float4*)ctx->img[GKRT_IMG_PREV_SPECULAR];
+    a.prev_a = (const float4*)ctx->img[GKRT_IMG_PREV_ALBEDO];
+    a.normal = (const float4*)ctx->img[GKRT_IMG_NORMAL];
+    a.motion = (const float2*)ctx->img[GKRT_IMG_MOTION];
+    a.id0 = (const uint32_t*)ctx->img[GKRT_IMG_OBJECT_ID];
+    a.id1 = (const uint32_t*)ctx->img[GKRT_IMG_OBJECT_ID_PREV];
+    a.moment = (const uint32_t*)ctx->img[GKRT_IMG_MOTION_MOMENT];
+    a.acc_d = (float4*)ctx->img[GKRT_IMG_ACCUM_DIFFUSE];
+    a.acc_s = (float4*)ctx->img[GKRT_IMG_ACCUM_SPECULAR];
+    a.acc_a = (float4*)ctx->img[GKRT_IMG_ACCUM_ALBEDO];
+    GK_CUDA(gkrt_launch_reproject(a, (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
+int gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
+    int rc = check_frame(ctx, fc);
+    if (rc != GKRT_OK) return rc;
+    if (fc->denoiser != GKRT_DENOISE_JBF) return fail(ctx, GKRT_ERR_UNSUPPORTED, "denoiser not supported by this build");
+    cudaSetDevice(ctx->device);
+    ComposeArgs a;
+    a.W = (int)ctx->W; a.H = (int)ctx->H;
+    a.bf_size = fc->bf_size;
+    a.hdr = fc->hdr;
+    a.bf_sigma = fc->bf_sigma;
+    a.bf_sigma_lum = fc->bf_sigma_lum;
+    a.paper_white_nit = fc->paper_white_nit;
+    a.pad = 0.0f;
+    a.acc_d = (const float4*)ctx->img[GKRT_IMG_ACCUM_DIFFUSE];
+    a.acc_s = (const float4*)ctx->img[GKRT_IMG_ACCUM_SPECULAR];
+    a.acc_a = (const float4*)ctx->img[GKRT_IMG_ACCUM_ALBEDO];
+    a.out = (float4*)ctx->img[GKRT_IMG_DENOISED];
+    a.out_linear = (float4*)ctx->img[GKRT_IMG_DENOISED_LINEAR];
+    GK_CUDA(gkrt_launch_compose(a, (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
+int gkrt_end_frame(GkrtContext* ctx, void* stream) {
+    (void)stream;
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (ctx->W == 0) return fail(ctx, GKRT_ERR_STATE, "gkrt_resize was not called");
+    const int pairs[4][2] = {{GKRT_IMG_ACCUM_DIFFUSE, GKRT_IMG_PREV_DIFFUSE},
+                             {GKRT_IMG_ACCUM_SPECULAR, GKRT_IMG_PREV_SPECULAR},
+                             {GKRT_IMG_ACCUM_ALBEDO, GKRT_IMG_PREV_ALBEDO},
+                             {GKRT_IMG_OBJECT_ID, GKRT_IMG_OBJECT_ID_PREV}};
+    for (auto& p : pairs) std::swap(ctx->img[p[0]], ctx->img[p[1]]);
+    return GKRT_OK;
+}
+
+int gkrt_render_frame(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
+    int rc;
+    if ((rc = gkrt_trace_pass(ctx, fc, stream)) != GKRT_OK) return rc;
+    if ((rc = gkrt_reproject_pass(ctx, fc, stream)) != GKRT_OK) return rc;
+    if ((rc = gkrt_denoise_pass(ctx, fc, stream)) != GKRT_OK) return rc;
+    return gkrt_end_frame(ctx, stream);
+}
+
+int gkrt_get_image(GkrtContext* ctx, int id, GkrtImageView* out) {
+    if (!ctx || !out) return GKRT_ERR_INVALID_ARG;
+    if (id < 0 || id >= GKRT_IMG_COUNT) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown image id");
+    if (ctx->W == 0) return fail(ctx, GKRT_ERR_STATE, "gkrt_resize was not called");
+    out->device_ptr = ctx->img[id];
+    out->width = ctx->W;
+    out->height = ctx->H;
+    out->pitch_bytes = (uint32_t)(ctx->W * image_bytes_per_px(id));
+    out->format = image_format(id);
+    return GKRT_OK;
+}
+
+int gkrt_synchronize(GkrtContext* ctx, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return cuda_fail(ctx, e, "cudaStreamQuery");
+        auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+        if ((uint64_t)ms > ctx->watchdog_ms) return fail(ctx, GKRT_ERR_TIMEOUT, "stream did not drain before the watchdog");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    uint32_t errw = 0;
+    GK_CUDA(cudaMemcpy(&errw, ctx->d_error, 4, cudaMemcpyDeviceToHost));
+    if (errw) {
+        cudaMemset(ctx->d_error, 0, 4);
+        return fail(ctx, GKRT_ERR_DEVICE_LIMIT,
+                    (errw & kErrStack) ? "traversal stack overflow" : "traversal iteration cap reached");
+    }
+    return GKRT_OK;
+}
+
+int gkrt_copy_image_to_host(GkrtContext* ctx, int id, void* dst, size_t dst_bytes, void* stream) {
+    GkrtImageView v;
+    int rc = gkrt_get_image(ctx, id, &v);
+    if (rc != GKRT_OK) return rc;
+    const size_t bytes = (size_t)v.pitch_bytes * v.height;
+    if (!dst || dst_bytes < bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
+    cudaSetDevice(ctx->device);
+    GK_CUDA(cudaMemcpyAsync(dst, v.device_ptr, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    return gkrt_synchronize(ctx, stream);
+}
+
+int gkrt_upload_image(GkrtContext* ctx, int id, const void* src, size_t src_bytes, void* stream) {
+    GkrtImageView v;
+    int rc = gkrt_get_image(ctx, id, &v);
+    if (rc != GKRT_OK) return rc;
+    const size_t bytes = (size_t)v.pitch_bytes * v.height;
+    if (!src || src_bytes != bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "source size differs from the image");
+    cudaSetDevice(ctx->device);
+    GK_CUDA(cudaMemcpyAsync(v.device_ptr, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    return gkrt_synchronize(ctx, stream);
+}
+
+int gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32_t count, uint32_t mode, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (count && (!rays || !hits)) return fail(ctx, GKRT_ERR_INVALID_ARG, "null ray or hit buffer");
+    if (mode > GKRT_TRACE_ANY) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown trace mode");
+    cudaSetDevice(ctx->device);
+    int rc = ensure_bvh(ctx, 0);
+    if (rc != GKRT_OK) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(gkrt_launch_trace_rays(scene_view(ctx), rays, hits, count, mode, ctx->d_counters, st));
+    return GKRT_OK;
+}
+
+int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
+    if (!ctx || !out) return GKRT_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    std::memset(out, 0, sizeof(*out));
+    unsigned long long c[6] = {0, 0, 0, 0, 0, 0};
+    GK_CUDA(cudaDeviceSynchronize());
+    GK_CUDA(cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
+    uint32_t errw = 0;
+    GK_CUDA(cudaMemcpy(&errw, ctx->d_error, 4, cudaMemcpyDeviceToHost));
+    out->rays_traced = c[0];
+    out->exact_fallbacks = c[1];
+    out->exact_retraces = c[2];
+    out->node_visits = c[3];
+    out->triangle_tests = c[4];
+    out->rays_total = c[5];
+    out->device_error = errw;
+    out->bvh_nodes = (uint32_t)ctx->blas_nodes.size();
+    out->tlas_nodes = ctx->tlas_nodes;
+    out->bvh_leaf_tris = ctx->nidx / 3;
+    return GKRT_OK;
+}
+
+int gkrt_affine_inverse(const float w[12], float winv[12]) {
+    if (!w || !winv) return GKRT_ERR_INVALID_ARG;
+    double a[3][3], t[3];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) a[r][c] = w[4 * r + c];
+        t[r] = w[4 * r + 3];
+    }
+    double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                 a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+    if (!(std::fabs(det) > 1e-30)) return GKRT_ERR_INVALID_ARG;
+    double inv[3][3];
+    inv[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / det;
+    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+    inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
+    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+    inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / det;
+    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+    for (int r = 0; r < 3; ++r) {
+        double tt = 0.0;
+        for (int c = 0; c < 3; ++c) {
+            winv[4 * r + c] = (float)inv[r][c];
+            tt -= inv[r][c] * t[c];
+        }
+        winv[4 * r + 3] = (float)tt;
+    }
+    return GKRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+// gkrt_internal.h — declarations shared by the host side of libgkrt and its kernels.
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "../../include/gkrt.h"
+
+namespace gk {
+struct ShadeScene;
+struct PixelImages;
+struct SceneView;
+struct BvhNode;
+
+struct ReprojectArgs {
+    int W, H;
+    uint32_t progressive, temporal_frames;
+    const float4 *src_d, *src_s, *src_a, *prev_d, *prev_s, *prev_a, *normal;
+    const float2* motion;
+    const uint32_t *id0, *id1, *moment;
+    float4 *acc_d, *acc_s, *acc_a;
+};
+
+struct ComposeArgs {
+    int W, H;
+    uint32_t bf_size, hdr;
+    float bf_sigma, bf_sigma_lum, paper_white_nit, pad;
+    const float4 *acc_d, *acc_s, *acc_a;
+    float4 *out, *out_linear;
+};
+
+// Host-side BVH build (binned SAH over boxes). Returns nodes in device layout and the leaf
+// order of the primitives; refs follow the encoding of gk_trace.cuh.
+struct HostBvh {
+    std::vector<BvhNode> nodes;
+    std::vector<uint32_t> order;
+    int root = -1;
+    int depth = 0;
+};
+// boxes: 6 floats per primitive (lo xyz, hi xyz). node_base: index of nodes[0] in the
+// global node array; prim_base: global index of order[0] (leaf refs are global).
+void build_bvh_host(const float* boxes, uint32_t n, uint32_t max_leaf, uint32_t node_base, uint32_t prim_base,
+                    bool leaf_is_instance, HostBvh& out);
+}  // namespace gk
+
+cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H,
+                                   const gk::PixelImages& im, unsigned long long* counters, cudaStream_t st);
+cudaError_t gkrt_launch_trace_rays(const gk::SceneView& S, const GkrtRay* rays, GkrtHit* hits, uint32_t n,
+                                   uint32_t mode, unsigned long long* counters, cudaStream_t st);
+cudaError_t gkrt_launch_reproject(const gk::ReprojectArgs& a, cudaStream_t st);
+cudaError_t gkrt_launch_compose(const gk::ComposeArgs& a, cudaStream_t st);

@@ -1,0 +1,67 @@
+"""ctypes binding of libgkrt.so (the C ABI of include/gkrt.h).
+
+The product path is this library and nothing else: if the shared object is missing or
+fails to load, every call raises. There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgkrt.so")
+
+_lib = None
+
+
+class GkrtError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path: str | None = None):
+    """Load libgkrt.so; raises if it is absent (build it with gknextengine_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libgkrt.so not found at {p}: run __graft_entry__.build() first")
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    L.gkrt_abi_version.restype = C.c_int
+    L.gkrt_context_create.argtypes = [C.POINTER(abi.GkrtDeviceDesc), C.POINTER(vp)]
+    L.gkrt_context_destroy.argtypes = [vp]
+    L.gkrt_last_error_message.restype = C.c_char_p
+    L.gkrt_last_error_message.argtypes = [vp]
+    L.gkrt_resize.argtypes = [vp, C.c_uint32, C.c_uint32]
+    L.gkrt_scene_upload.argtypes = [vp, C.POINTER(abi.GkrtSceneDesc)]
+    L.gkrt_scene_update_instances.argtypes = [vp, vp, C.c_uint32, vp]
+    L.gkrt_build_bvh.argtypes = [vp, C.c_uint32, vp]
+    for n in ("gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_render_frame"):
+        getattr(L, n).argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), vp]
+    L.gkrt_end_frame.argtypes = [vp, vp]
+    L.gkrt_get_image.argtypes = [vp, C.c_int, C.POINTER(abi.GkrtImageView)]
+    L.gkrt_copy_image_to_host.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
+    L.gkrt_upload_image.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
+    L.gkrt_trace_rays.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
+    L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
+    L.gkrt_synchronize.argtypes = [vp, vp]
+    L.gkrt_affine_inverse.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    if L.gkrt_abi_version() != 1:
+        raise RuntimeError("libgkrt ABI version mismatch")
+    _lib = L
+    return L
+
+
+# every function include/gkrt.h declares (checked by the CPU test suite)
+EXPORTED = [
+    "gkrt_context_create", "gkrt_context_destroy", "gkrt_last_error_message", "gkrt_abi_version",
+    "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_build_bvh",
+    "gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_end_frame", "gkrt_render_frame",
+    "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_get_stats",
+    "gkrt_synchronize", "gkrt_affine_inverse",
+]

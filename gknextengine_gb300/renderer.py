@@ -1,0 +1,139 @@
+"""PathTracingRenderer: the host-side mirror of the reference's logic renderer.
+
+The reference drives its path tracer through LogicRendererBase
+(src/Rendering/VulkanBaseRenderer.hpp:213-243): OnDeviceSet, CreateSwapChain(extent),
+DeleteSwapChain, Render(commandBuffer, imageIndex), BeforeNextFrame; the path-tracing
+implementation records "rt pass", "reproject pass", "compose pass" and "copy pass"
+(src/Rendering/PathTracing/PathTracingRenderer.cpp:104-218). This class keeps those names
+and that order over the C ABI, with CUDA streams in place of command buffers. Errors are
+raised as GkrtError, carrying the library's status code and message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi, native
+
+
+class PathTracingRenderer:
+    def __init__(self, device: int = 0, watchdog_ms: int = 0):
+        self._lib = native.load()
+        d = abi.GkrtDeviceDesc()
+        d.device = device
+        d.watchdog_ms = watchdog_ms
+        h = C.c_void_p()
+        rc = self._lib.gkrt_context_create(C.byref(d), C.byref(h))
+        if rc != abi.GKRT_OK:
+            raise native.GkrtError(rc, "gkrt_context_create failed")
+        self._h = h
+        self.width = self.height = 0
+        self._scene = None
+
+    # -- helpers ---------------------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc != abi.GKRT_OK:
+            msg = self._lib.gkrt_last_error_message(self._h)
+            raise native.GkrtError(rc, msg.decode() if msg else "")
+
+    @staticmethod
+    def _stream(stream):
+        if stream is None:
+            return None
+        if isinstance(stream, int):
+            return C.c_void_p(stream)
+        return C.c_void_p(int(stream.cuda_stream))   # torch.cuda.Stream
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gkrt_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- LogicRendererBase ---------------------------------------------------------------
+    def create_swap_chain(self, width: int, height: int):
+        """CreateSwapChain(extent): (re)allocates the image set."""
+        self._check(self._lib.gkrt_resize(self._h, width, height))
+        self.width, self.height = int(width), int(height)
+
+    resize = create_swap_chain
+
+    def load_scene(self, scene: abi.SceneArrays):
+        """Scene::RebuildMeshBuffer + RayTraceBaseRenderer::CreateAccelerationStructures."""
+        self._scene = scene
+        desc = scene.desc()
+        self._check(self._lib.gkrt_scene_upload(self._h, C.byref(desc)))
+
+    def update_instances(self, instances: np.ndarray, stream=None):
+        """Per-frame NodeProxy upload + TLAS rebuild (Scene::UpdateNodesGpuDriven, AfterUpdateScene)."""
+        inst = np.ascontiguousarray(instances, dtype=abi.INSTANCE_DTYPE)
+        self._check(self._lib.gkrt_scene_update_instances(self._h, inst.ctypes.data, inst.shape[0],
+                                                          self._stream(stream)))
+
+    def build_bvh(self, flags: int = abi.BUILD_ALL, stream=None):
+        self._check(self._lib.gkrt_build_bvh(self._h, flags, self._stream(stream)))
+
+    def trace_pass(self, fc, stream=None):
+        self._check(self._lib.gkrt_trace_pass(self._h, C.byref(fc), self._stream(stream)))
+
+    def reproject_pass(self, fc, stream=None):
+        self._check(self._lib.gkrt_reproject_pass(self._h, C.byref(fc), self._stream(stream)))
+
+    def denoise_pass(self, fc, stream=None):
+        self._check(self._lib.gkrt_denoise_pass(self._h, C.byref(fc), self._stream(stream)))
+
+    def end_frame(self, stream=None):
+        self._check(self._lib.gkrt_end_frame(self._h, self._stream(stream)))
+
+    def render(self, fc, stream=None):
+        """Render(): rt pass -> reproject pass -> compose pass -> copy pass."""
+        self._check(self._lib.gkrt_render_frame(self._h, C.byref(fc), self._stream(stream)))
+
+    def synchronize(self, stream=None):
+        self._check(self._lib.gkrt_synchronize(self._h, self._stream(stream)))
+
+    # -- outputs ---------------------------------------------------------------------------
+    def image_view(self, image_id: int) -> abi.GkrtImageView:
+        v = abi.GkrtImageView()
+        self._check(self._lib.gkrt_get_image(self._h, image_id, C.byref(v)))
+        return v
+
+    def read_image(self, image_id: int, stream=None, out: np.ndarray | None = None) -> np.ndarray:
+        dt, ch = abi.IMAGE_FORMATS[image_id]
+        shape = (self.height, self.width) if ch == 1 else (self.height, self.width, ch)
+        if out is None:
+            out = np.empty(shape, dt)
+        self._check(self._lib.gkrt_copy_image_to_host(self._h, image_id, out.ctypes.data, out.nbytes,
+                                                      self._stream(stream)))
+        return out
+
+    def write_image(self, image_id: int, data: np.ndarray, stream=None):
+        dt, ch = abi.IMAGE_FORMATS[image_id]
+        a = np.ascontiguousarray(data, dtype=dt)
+        self._check(self._lib.gkrt_upload_image(self._h, image_id, a.ctypes.data, a.nbytes, self._stream(stream)))
+
+    def images(self, ids=None) -> dict:
+        ids = range(abi.IMG_COUNT) if ids is None else ids
+        return {i: self.read_image(i) for i in ids}
+
+    def trace_rays_device(self, rays_ptr: int, hits_ptr: int, count: int, mode=abi.TRACE_CLOSEST, stream=None):
+        """Ray queries on device buffers (GkrtRay / GkrtHit layouts)."""
+        self._check(self._lib.gkrt_trace_rays(self._h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr), count, mode,
+                                              self._stream(stream)))
+
+    def stats(self) -> abi.GkrtStats:
+        s = abi.GkrtStats()
+        self._check(self._lib.gkrt_get_stats(self._h, C.byref(s)))
+        return s

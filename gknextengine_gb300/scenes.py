@@ -1,0 +1,272 @@
+"""Seeded synthetic scenes for the path-tracing pass.
+
+The reference ships procedural scene templates (FProcModel::CreateCornellBox / CreateBox,
+src/Assets/FProcModel.cpp:16-176; SceneList::CornellBox, src/Runtime/SceneList.cpp:180-226).
+The workloads here follow those templates with the sizes and value distributions of the
+benchmark configurations:
+
+* cornell():  5 axis-aligned wall quads + 2 boxes rotated about Y (34 tris) and one
+  0.25 x 0.25 emissive quad (2 tris, radiance 15); Lambertian albedo U(0.2, 0.9)^3 per
+  object; 256 x 256, 40 deg FOV, pinhole, 1 spp, 4 bounces.
+* bricks():   one studded-brick mesh (252 tris) instanced 4096 times on a 64 x 64 grid with
+  integer heights 1..8 (1.03 M tris); GGX materials with roughness U(0.05, 1),
+  metallic Bernoulli(0.3), base colour U(0, 1)^3; 64 emissive bricks, radiance U(5, 20);
+  1920 x 1080, 1 spp, 8 bounces, camera orbiting 0.5 deg per frame.
+
+Every array is produced with numpy's seeded generators, so the oracle and the GPU see the
+same floats. The scene data is synthetic: the reference's .glb scenes are not used.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import abi
+from .camera import Camera, Settings
+
+
+def affine_inverse(m12: np.ndarray) -> np.ndarray:
+    """world->object for a row-major 3x4 object->world transform, in float64."""
+    m = np.eye(4)
+    m[:3, :] = np.asarray(m12, np.float64).reshape(3, 4)
+    return np.linalg.inv(m)[:3, :].reshape(-1).astype(np.float32)
+
+
+def trs(translate=(0, 0, 0), rot_y_deg=0.0, scale=(1, 1, 1)) -> np.ndarray:
+    a = math.radians(rot_y_deg)
+    c, s = math.cos(a), math.sin(a)
+    r = np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]])
+    m = np.zeros((3, 4))
+    m[:, :3] = r @ np.diag(scale)
+    m[:, 3] = translate
+    return m.reshape(-1)
+
+
+def make_instance(mesh_id, world12, mat_ids, instance_id, prev_world12=None, visible=1):
+    inst = np.zeros((), abi.INSTANCE_DTYPE)
+    inst["instance_id"] = instance_id
+    inst["mesh_id"] = mesh_id
+    inst["visible"] = visible
+    inst["world"] = np.asarray(world12, np.float32)
+    inst["world_inv"] = affine_inverse(world12)
+    inst["combined_prev"] = combined_prev(world12, world12 if prev_world12 is None else prev_world12)
+    mids = np.zeros(16, np.uint32)
+    mids[: len(mat_ids)] = mat_ids
+    inst["mat_id"] = mids
+    return inst
+
+
+def combined_prev(world12, prev_world12) -> np.ndarray:
+    """prevTransform * inverse(transform) (Node::TickVelocity, src/Assets/Node.cpp:94):
+    maps a world position on the instance this frame to where it was last frame."""
+    w = np.eye(4)
+    w[:3, :] = np.asarray(world12, np.float64).reshape(3, 4)
+    p = np.eye(4)
+    p[:3, :] = np.asarray(prev_world12, np.float64).reshape(3, 4)
+    return (p @ np.linalg.inv(w))[:3, :].reshape(-1).astype(np.float32)
+
+
+def material(diffuse, model, fuzziness=1.0, ri=1.0, metalness=0.0, ri2=0.0):
+    m = np.zeros((), abi.MATERIAL_DTYPE)
+    m["diffuse"] = list(diffuse) + [1.0] if len(diffuse) == 3 else list(diffuse)
+    m["diffuse_texture_id"] = -1
+    m["mra_texture_id"] = -1
+    m["normal_texture_id"] = -1
+    m["fuzziness"] = fuzziness
+    m["refraction_index"] = ri
+    m["material_model"] = model
+    m["metalness"] = metalness
+    m["refraction_index2"] = ri2
+    return m
+
+
+# Material factories of src/Assets/Material.hpp:10-38.
+def lambertian(rgb):
+    return material(rgb, abi.MAT_LAMBERTIAN, fuzziness=1.0, ri=1.0, metalness=0.0)
+
+
+def metallic(rgb, fuzz):
+    return material(rgb, abi.MAT_METALLIC, fuzziness=fuzz, ri=1.45, metalness=1.0)
+
+
+def mixture(rgb, fuzz):
+    return material(rgb, abi.MAT_MIXTURE, fuzziness=fuzz, ri=1.45, metalness=0.0)
+
+
+def diffuse_light(rgb):
+    return material(rgb, abi.MAT_DIFFUSE_LIGHT, fuzziness=0.0, ri=0.0, metalness=0.0)
+
+
+class MeshBuilder:
+    def __init__(self):
+        self.pos, self.nrm, self.slot, self.idx = [], [], [], []
+
+    def quad(self, p0, p1, p2, p3, n, slot):
+        """Two triangles (p0,p1,p2), (p0,p2,p3) with a flat normal, like AddTriangle."""
+        b = len(self.pos)
+        for p in (p0, p1, p2, p3):
+            self.pos.append(list(p) + [1.0])
+            self.nrm.append(list(n) + [0.0])
+            self.slot.append(slot)
+        self.idx += [b, b + 1, b + 2, b, b + 2, b + 3]
+
+    def tri(self, p0, p1, p2, n0, n1, n2, slot):
+        b = len(self.pos)
+        for p, n in ((p0, n0), (p1, n1), (p2, n2)):
+            self.pos.append(list(p) + [1.0])
+            self.nrm.append(list(n) + [0.0])
+            self.slot.append(slot)
+        self.idx += [b, b + 1, b + 2]
+
+    def box(self, lo, hi, slot=0, bottom=True):
+        """Axis-aligned box with outward normals (FProcModel::CreateBox winding)."""
+        (x0, y0, z0), (x1, y1, z1) = lo, hi
+        self.quad((x0, y0, z0), (x0, y0, z1), (x0, y1, z1), (x0, y1, z0), (-1, 0, 0), slot)
+        self.quad((x1, y0, z1), (x1, y0, z0), (x1, y1, z0), (x1, y1, z1), (1, 0, 0), slot)
+        self.quad((x1, y0, z0), (x0, y0, z0), (x0, y1, z0), (x1, y1, z0), (0, 0, -1), slot)
+        self.quad((x0, y0, z1), (x1, y0, z1), (x1, y1, z1), (x0, y1, z1), (0, 0, 1), slot)
+        if bottom:
+            self.quad((x0, y0, z0), (x1, y0, z0), (x1, y0, z1), (x0, y0, z1), (0, -1, 0), slot)
+        self.quad((x1, y1, z0), (x0, y1, z0), (x0, y1, z1), (x1, y1, z1), (0, 1, 0), slot)
+
+    def arrays(self):
+        return (np.asarray(self.pos, np.float32), np.asarray(self.nrm, np.float32),
+                np.asarray(self.slot, np.uint32), np.asarray(self.idx, np.uint32))
+
+
+def _concat_meshes(builders):
+    pos, nrm, slot, idx, meshes = [], [], [], [], []
+    voff = ioff = 0
+    for b in builders:
+        p, n, s, i = b.arrays()
+        meshes.append((ioff, len(i), voff, len(p)))
+        pos.append(p); nrm.append(n); slot.append(s); idx.append(i)
+        voff += len(p)
+        ioff += len(i)
+    return (np.concatenate(pos), np.concatenate(nrm), np.concatenate(slot), np.concatenate(idx),
+            np.array(meshes, dtype=abi.MESH_DTYPE))
+
+
+# ---------------------------------------------------------------------------------------
+def cornell(seed: int = 1, width: int = 256, height: int = 256):
+    """Config C1. Returns (SceneArrays, Camera, Settings)."""
+    rng = np.random.default_rng(seed)
+    room = MeshBuilder()
+    # unit room x in [-0.5, 0.5], y in [0, 1], z in [-0.5, 0.5]; front open (CreateCornellBox, scale 1)
+    l0, l1, l2, l3 = (-0.5, 0, 0.5), (-0.5, 0, -0.5), (-0.5, 1, -0.5), (-0.5, 1, 0.5)
+    r0, r1, r2, r3 = (0.5, 0, 0.5), (0.5, 0, -0.5), (0.5, 1, -0.5), (0.5, 1, 0.5)
+    room.quad(l0, l1, l2, l3, (1, 0, 0), 0)          # left
+    room.quad(r2, r1, r0, r3, (-1, 0, 0), 1)         # right (AddTriangle 2,1,0 / 3,2,0)
+    room.quad(l1, r1, r2, l2, (0, 0, 1), 2)          # back
+    room.quad(l0, r0, r1, l1, (0, 1, 0), 3)          # floor
+    room.quad(l2, r2, r3, l3, (0, -1, 0), 4)         # ceiling
+    y = 0.999
+    room.quad((-0.125, y, 0.125), (0.125, y, 0.125), (0.125, y, -0.125), (-0.125, y, -0.125), (0, -1, 0), 5)
+    box = MeshBuilder()
+    box.box((-0.5, 0.0, -0.5), (0.5, 1.0, 0.5), slot=0)
+    pos, nrm, slot, idx, meshes = _concat_meshes([room, box])
+    albedo = rng.uniform(0.2, 0.9, size=(7, 3))
+    mats = [lambertian(albedo[i]) for i in range(7)] + [diffuse_light((15.0, 15.0, 15.0))]
+    materials = np.array(mats, dtype=abi.MATERIAL_DTYPE)
+    insts = [
+        make_instance(0, trs(), [0, 1, 2, 3, 4, 7], instance_id=0),
+        make_instance(1, trs((-0.17, 0.0, -0.15), rot_y_deg=18.0, scale=(0.3, 0.6, 0.3)), [5], instance_id=1),
+        make_instance(1, trs((0.18, 0.0, 0.17), rot_y_deg=-17.0, scale=(0.3, 0.3, 0.3)), [6], instance_id=2),
+    ]
+    instances = np.array(insts, dtype=abi.INSTANCE_DTYPE)
+    light = np.zeros(1, abi.LIGHT_DTYPE)
+    light["p0"] = [-0.125, y, 0.125, 1]
+    light["p1"] = [-0.125, y, -0.125, 1]
+    light["p3"] = [0.125, y, 0.125, 1]
+    light["normal_area"] = [0, -1, 0, 0.0625]
+    light["light_mat_idx"] = 7
+    scene = abi.SceneArrays(pos, nrm, slot, idx, meshes, materials, instances, lights=light, name="cornell")
+    cam = Camera(eye=(0.0, 0.5, 1.94), center=(0.0, 0.5, 0.0), fov_deg=40.0)
+    settings = Settings(samples=1, bounces=4, max_bounces=4, taa=False)
+    return scene, cam, settings
+
+
+def brick_mesh(studs_x=4, studs_z=2, pitch=0.5, height=0.6, stud_r=0.15, stud_h=0.17, segments=10):
+    """A studded brick: a box (12 tris) plus studs_x*studs_z capped cylinders of
+    3*segments tris each (4 x 2 studs, 10 segments: 252 tris)."""
+    b = MeshBuilder()
+    sx, sz = studs_x * pitch, studs_z * pitch
+    b.box((0.0, 0.0, 0.0), (sx, height, sz), slot=0)
+    for i in range(studs_x):
+        for j in range(studs_z):
+            cx, cz = (i + 0.5) * pitch, (j + 0.5) * pitch
+            y0, y1 = height, height + stud_h
+            ang = [2 * math.pi * k / segments for k in range(segments + 1)]
+            for k in range(segments):
+                a0, a1 = ang[k], ang[k + 1]
+                p00 = (cx + stud_r * math.cos(a0), y0, cz + stud_r * math.sin(a0))
+                p01 = (cx + stud_r * math.cos(a1), y0, cz + stud_r * math.sin(a1))
+                p10 = (cx + stud_r * math.cos(a0), y1, cz + stud_r * math.sin(a0))
+                p11 = (cx + stud_r * math.cos(a1), y1, cz + stud_r * math.sin(a1))
+                n0 = (math.cos(a0), 0.0, math.sin(a0))
+                n1 = (math.cos(a1), 0.0, math.sin(a1))
+                b.tri(p00, p11, p01, n0, n1, n1, 0)
+                b.tri(p00, p10, p11, n0, n0, n1, 0)
+                b.tri((cx, y1, cz), p11, p10, (0, 1, 0), (0, 1, 0), (0, 1, 0), 0)
+    return b
+
+
+def bricks(seed: int = 2, width: int = 1920, height: int = 1080, grid: int = 64, emissive: int = 64):
+    """Config C2. Returns (SceneArrays, Camera, Settings)."""
+    rng = np.random.default_rng(seed)
+    brick = brick_mesh()
+    ground = MeshBuilder()
+    pitch_x, pitch_z = 2.2, 1.2
+    ext_x, ext_z = grid * pitch_x, grid * pitch_z
+    ground.quad((-2.0, 0.0, -2.0), (-2.0, 0.0, ext_z + 2.0), (ext_x + 2.0, 0.0, ext_z + 2.0),
+                (ext_x + 2.0, 0.0, -2.0), (0, 1, 0), 0)
+    pos, nrm, slot, idx, meshes = _concat_meshes([brick, ground])
+    n = grid * grid
+    heights = rng.integers(1, 9, size=n)
+    rough = rng.uniform(0.05, 1.0, size=n)
+    metal = rng.random(n) < 0.3
+    base = rng.uniform(0.0, 1.0, size=(n, 3))
+    emit_ids = rng.choice(n, size=emissive, replace=False)
+    radiance = rng.uniform(5.0, 20.0, size=emissive)
+    mats = []
+    for i in range(n):
+        mats.append(metallic(base[i], rough[i]) if metal[i] else mixture(base[i], rough[i]))
+    for k, i in enumerate(emit_ids):
+        mats[i] = diffuse_light((radiance[k], radiance[k], radiance[k]))
+    mats.append(lambertian((0.5, 0.5, 0.5)))
+    materials = np.array(mats, dtype=abi.MATERIAL_DTYPE)
+    insts = np.zeros(n + 1, abi.INSTANCE_DTYPE)
+    gi, gj = np.meshgrid(np.arange(grid), np.arange(grid), indexing="ij")
+    gi, gj = gi.reshape(-1), gj.reshape(-1)
+    worlds = np.zeros((n, 12))
+    worlds[:, 0] = 1.0
+    worlds[:, 5] = heights
+    worlds[:, 10] = 1.0
+    worlds[:, 3] = gi * pitch_x
+    worlds[:, 11] = gj * pitch_z
+    invs = np.zeros((n, 12))
+    invs[:, 0] = 1.0
+    invs[:, 5] = 1.0 / heights
+    invs[:, 10] = 1.0
+    invs[:, 3] = -worlds[:, 3]
+    invs[:, 11] = -worlds[:, 11]
+    ident = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
+    insts["instance_id"][:n] = np.arange(n)
+    insts["mesh_id"][:n] = 0
+    insts["visible"] = 1
+    insts["world"][:n] = worlds.astype(np.float32)
+    insts["world_inv"][:n] = invs.astype(np.float32)
+    insts["combined_prev"][:] = ident
+    insts["mat_id"][:n, 0] = np.arange(n)
+    insts["instance_id"][n] = n
+    insts["mesh_id"][n] = 1
+    insts["world"][n] = ident
+    insts["world_inv"][n] = ident
+    insts["mat_id"][n, 0] = n
+    lights = np.zeros(0, abi.LIGHT_DTYPE)
+    scene = abi.SceneArrays(pos, nrm, slot, idx, meshes, materials, insts, lights=lights, name="bricks")
+    center = np.array([ext_x * 0.5, 0.0, ext_z * 0.5])
+    cam = Camera(eye=center + np.array([0.0, 40.0, 90.0]), center=center + np.array([0.0, 2.0, 0.0]), fov_deg=40.0)
+    settings = Settings(samples=1, bounces=8, max_bounces=8, temporal_frames=16, taa=True)
+    return scene, cam, settings

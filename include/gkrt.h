@@ -1,0 +1,303 @@
+/*
+ * gkrt.h — C ABI of the GB300-native ray-tracing pass.
+ *
+ * This is the drop-in boundary for gkNextRenderer's path-tracing logic renderer.
+ * The reference plugs a "logic renderer" into its Vulkan frame loop
+ * (class LogicRendererBase, src/Rendering/VulkanBaseRenderer.hpp:213-243), and the
+ * path tracer implements it (src/Rendering/PathTracing/PathTracingRenderer.cpp:66-232).
+ * Its inputs are the scene buffers addressed through the GPUScene push constant
+ * (assets/shaders/common/BasicTypes.slang:261-291, filled by Scene::FetchGPUScene,
+ * src/Assets/Scene.cpp:291-314) and the per-frame UniformBufferObject
+ * (BasicTypes.slang:22-84, built by NextEngine::GetUniformBufferObject,
+ * src/Runtime/Engine.cpp:736-849). Its outputs are bindless storage images
+ * (assets/shaders/common/BindlessTexture.slang:8-40).
+ *
+ * Here the same pass is exposed as plain C: host pointers and sizes in, device images
+ * out, every call returns a status code, no exceptions cross the boundary, and all GPU
+ * work is ordered on the caller's CUDA stream (passed as void* so that this header
+ * needs no CUDA include). One context is used by one host thread at a time.
+ */
+#ifndef GKRT_H
+#define GKRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GKRT_ABI_VERSION 1
+
+/* ---- status codes (the reference throws instead: src/Utilities/Exception.hpp:10) ---- */
+#define GKRT_OK                0
+#define GKRT_ERR_INVALID_ARG   1  /* bad pointer, size, id, NaN vertex, ...            */
+#define GKRT_ERR_OOM           2  /* device allocation failed                           */
+#define GKRT_ERR_CUDA          3  /* a CUDA runtime call failed                         */
+#define GKRT_ERR_TIMEOUT       4  /* a bounded wait ran out (host watchdog)             */
+#define GKRT_ERR_DEVICE_LIMIT  5  /* a device loop hit its iteration cap                */
+#define GKRT_ERR_UNSUPPORTED   6  /* feature outside this pass (textures, ...)          */
+#define GKRT_ERR_STATE         7  /* call order: render before scene/resize, ...        */
+#define GKRT_ERR_NO_DEVICE     8  /* no CUDA device / the kernels are not loadable      */
+
+/* ---- material models (BasicTypes.slang:183-188) ---- */
+#define GKRT_MAT_LAMBERTIAN    0u
+#define GKRT_MAT_METALLIC      1u
+#define GKRT_MAT_DIELECTRIC    2u
+#define GKRT_MAT_ISOTROPIC     3u
+#define GKRT_MAT_DIFFUSE_LIGHT 4u
+#define GKRT_MAT_MIXTURE       5u
+
+/* Material: byte-for-byte the reference's 64-byte Material (BasicTypes.slang:218-236).
+ * Texture ids must be -1: bindless textures are outside this pass. */
+typedef struct GkrtMaterial {
+    float    diffuse[4];
+    int32_t  diffuse_texture_id;
+    int32_t  mra_texture_id;
+    int32_t  normal_texture_id;
+    float    fuzziness;
+    float    refraction_index;
+    uint32_t material_model;
+    float    metalness;
+    float    refraction_index2;
+    float    normal_texture_scale;
+    float    reserved[3];
+} GkrtMaterial;
+
+/* Emissive quad: the reference's 80-byte LightObject (BasicTypes.slang:171-182). */
+typedef struct GkrtLight {
+    float    p0[4];
+    float    p1[4];
+    float    p3[4];
+    float    normal_area[4];
+    uint32_t light_mat_idx;
+    uint32_t reserved[3];
+} GkrtLight;
+
+/* Mesh ranges: the first four words of the reference's ModelData (BasicTypes.slang:97-111).
+ * index_offset/index_count address GkrtSceneDesc.indices; indices are relative to vertex_offset. */
+typedef struct GkrtMesh {
+    uint32_t index_offset;
+    uint32_t index_count;
+    uint32_t vertex_offset;
+    uint32_t vertex_count;
+} GkrtMesh;
+
+/* Instance: the reference's NodeProxy (BasicTypes.slang:86-95) with affine 3x4 row-major
+ * transforms instead of 4x4 ones, plus the world->object inverse that RayQuery derives
+ * internally (CommittedRayWorldToObject, Shading.slang:808). Supplying the inverse keeps
+ * the object-space ray identical for every consumer; gkrt_affine_inverse() computes it.
+ * combined_prev maps this frame's world position to last frame's (Node::TickVelocity,
+ * src/Assets/Node.cpp:82-106: prevTransform * inverse(transform)). */
+typedef struct GkrtInstance {
+    uint32_t instance_id;   /* custom index: written to the object-id image             */
+    uint32_t mesh_id;       /* index into GkrtSceneDesc.meshes (NodeProxy.modelId)     */
+    uint32_t visible;       /* 0: left out of the top-level BVH (instance mask 0)      */
+    uint32_t reserved;
+    float    world[12];
+    float    world_inv[12];
+    float    combined_prev[12];
+    uint32_t mat_id[16];    /* per-vertex material slot -> material index              */
+} GkrtInstance;
+
+/* Scene: what Scene::RebuildMeshBuffer uploads (src/Assets/Scene.cpp:102-289) in FP32.
+ * All arrays are host memory and are copied; the caller keeps ownership. */
+typedef struct GkrtSceneDesc {
+    const float*        positions;      /* float4 per vertex, w ignored                */
+    const float*        normals;        /* float4 per vertex, w ignored                */
+    const uint32_t*     material_slots; /* per vertex, 0..15 (packed in Vertex.hpp:97) */
+    uint32_t            vertex_count;
+    const uint32_t*     indices;
+    uint32_t            index_count;
+    const GkrtMesh*     meshes;
+    uint32_t            mesh_count;
+    const GkrtMaterial* materials;
+    uint32_t            material_count;
+    const GkrtInstance* instances;
+    uint32_t            instance_count;
+    const GkrtLight*    lights;
+    uint32_t            light_count;
+    /* Optional ambient-cube probe grid (AmbientCube.slang:12-15; 192*48*192 entries):
+     * 14 u32 per AmbientCube and 4 u32 per VoxelData, or NULL for all-zero probes. */
+    const uint32_t*     probe_cubes;
+    const uint32_t*     probe_voxels;
+} GkrtSceneDesc;
+
+/* Frame constants: the fields of UniformBufferObject (BasicTypes.slang:22-84) the pass
+ * reads, plus the reprojection push constants (PathTracingRenderer.cpp:127-128).
+ * Matrices are column-major float[16] (glm's memory layout). */
+typedef struct GkrtFrameConstants {
+    float    model_view[16];
+    float    projection[16];
+    float    model_view_inverse[16];
+    float    projection_inverse[16];
+    float    view_projection[16];
+    float    prev_view_projection[16];
+    float    view_projection_unjit[16];
+    float    prev_view_projection_unjit[16];
+    float    sun_direction[4];
+    float    sun_color[4];
+    float    sky_color[4];          /* constant sky radiance (stands in for the HDR map) */
+    float    aperture;
+    float    focus_distance;
+    float    paper_white_nit;
+    float    sky_intensity;
+    uint32_t total_frames;
+    uint32_t number_of_samples;
+    uint32_t number_of_bounces;
+    uint32_t max_number_of_bounces;
+    uint32_t temporal_frames;
+    uint32_t has_sky;
+    uint32_t has_sun;
+    uint32_t taa;
+    uint32_t fast_gather;
+    uint32_t progressive_render;
+    uint32_t bf_size;              /* 0: no bilateral filter                           */
+    uint32_t hdr;
+    float    bf_sigma;
+    float    bf_sigma_lum;
+    float    bf_sigma_normal;
+    uint32_t denoiser;             /* GKRT_DENOISE_*                                    */
+    uint32_t nee_mode;             /* GKRT_NEE_*                                        */
+    uint32_t flags;                /* GKRT_FRAME_*                                      */
+    uint32_t reserved[2];
+} GkrtFrameConstants;
+
+#define GKRT_DENOISE_JBF     0u    /* reference single-pass joint bilateral filter      */
+#define GKRT_DENOISE_ATROUS  1u    /* 5x5 edge-aware a-trous, 3 passes (no reference)   */
+
+#define GKRT_NEE_REFERENCE   0u    /* sun-cone NEE only, as the built Slang path        */
+#define GKRT_NEE_EMISSIVE    1u    /* + emissive-triangle NEE via an alias table (new)  */
+
+#define GKRT_FRAME_PRIMARY_IDS  1u /* also write HIT_INST / HIT_PRIM of the camera ray  */
+
+/* Images owned by the context (formats: FP32x4 unless stated). */
+#define GKRT_IMG_SINGLE_DIFFUSE    0
+#define GKRT_IMG_SINGLE_SPECULAR   1
+#define GKRT_IMG_ALBEDO            2
+#define GKRT_IMG_NORMAL            3   /* xyz normal, w roughness                        */
+#define GKRT_IMG_OBJECT_ID         4   /* u32, 65535 on a miss                           */
+#define GKRT_IMG_OBJECT_ID_PREV    5   /* u32                                            */
+#define GKRT_IMG_MOTION            6   /* FP32x2 pixel motion                            */
+#define GKRT_IMG_PREV_DEPTH        7   /* FP32                                           */
+#define GKRT_IMG_MOTION_MOMENT     8   /* u32                                            */
+#define GKRT_IMG_ACCUM_DIFFUSE     9
+#define GKRT_IMG_ACCUM_SPECULAR    10
+#define GKRT_IMG_ACCUM_ALBEDO      11
+#define GKRT_IMG_PREV_DIFFUSE      12
+#define GKRT_IMG_PREV_SPECULAR     13
+#define GKRT_IMG_PREV_ALBEDO       14
+#define GKRT_IMG_DENOISED          15  /* tonemapped, as RT_DENOISED                     */
+#define GKRT_IMG_DENOISED_LINEAR   16  /* same pixel before the tonemap                  */
+#define GKRT_IMG_HIT_INST          17  /* u32 instance index of the camera-ray hit       */
+#define GKRT_IMG_HIT_PRIM          18  /* u32 primitive index within the mesh            */
+#define GKRT_IMG_COUNT             19
+
+#define GKRT_FMT_F32X4  0
+#define GKRT_FMT_F32X2  1
+#define GKRT_FMT_F32    2
+#define GKRT_FMT_U32    3
+
+typedef struct GkrtImageView {
+    void*    device_ptr;
+    uint32_t width;
+    uint32_t height;
+    uint32_t pitch_bytes;
+    uint32_t format;
+} GkrtImageView;
+
+/* Ray query records for gkrt_trace_rays (device memory). */
+typedef struct GkrtRay {
+    float origin[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} GkrtRay;
+
+typedef struct GkrtHit {
+    float    t;          /* hit distance; -1 on a miss                                  */
+    float    b1, b2;     /* barycentrics of vertex 1 and 2                              */
+    uint32_t inst;       /* instance index, 0xFFFFFFFF on a miss                        */
+    uint32_t prim;       /* triangle index within the instance's mesh                   */
+    uint32_t pad[3];
+} GkrtHit;
+
+#define GKRT_TRACE_CLOSEST 0u
+#define GKRT_TRACE_ANY     1u
+
+typedef struct GkrtDeviceDesc {
+    int32_t  device;            /* CUDA ordinal                                          */
+    uint32_t flags;
+    uint32_t watchdog_ms;       /* 0: default bounded wait for gkrt_synchronize          */
+    uint32_t reserved;
+} GkrtDeviceDesc;
+
+typedef struct GkrtStats {
+    uint64_t rays_traced;       /* camera + bounce + shadow rays of the last trace pass   */
+    uint64_t exact_fallbacks;   /* triangle tests decided in FP64, last pass              */
+    uint64_t exact_retraces;    /* rays re-traversed in exact mode (t-ambiguous)          */
+    uint64_t node_visits;       /* BVH nodes visited, last pass                           */
+    uint64_t triangle_tests;    /* ray/triangle tests, last pass                          */
+    uint64_t rays_total;        /* rays traced since the context was created              */
+    uint32_t device_error;      /* device error word (iteration caps hit)                 */
+    uint32_t bvh_nodes;
+    uint32_t bvh_leaf_tris;
+    uint32_t tlas_nodes;
+} GkrtStats;
+
+typedef struct GkrtContext GkrtContext;
+
+/* Context lifetime (LogicRendererBase ctor/OnDeviceSet, VulkanBaseRenderer.hpp:216-219). */
+int  gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out);
+int  gkrt_context_destroy(GkrtContext* ctx);
+const char* gkrt_last_error_message(const GkrtContext* ctx);
+int  gkrt_abi_version(void);
+
+/* Image set (CreateSwapChain/DeleteSwapChain, PathTracingRenderer.cpp:66-102;
+ * formats of VulkanBaseRenderer::CreateRenderImages, VulkanBaseRenderer.cpp:429-463). */
+int  gkrt_resize(GkrtContext* ctx, uint32_t width, uint32_t height);
+
+/* Scene upload (Scene::RebuildMeshBuffer, Scene.cpp:102-289) and per-frame instance
+ * update (Scene::UpdateNodesGpuDriven, Scene.cpp:443-492, with AfterUpdateScene,
+ * RayTraceBaseRenderer.cpp:165-191). Instance updates keep mesh ids and count. */
+int  gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* scene);
+int  gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
+                                 uint32_t count, void* stream);
+
+/* Acceleration structures (RayTraceBaseRenderer::CreateBottomLevelStructures /
+ * CreateTopLevelStructures, RayTraceBaseRenderer.cpp:276-386; TLAS update :205-218).
+ * flags: GKRT_BUILD_* */
+#define GKRT_BUILD_BLAS 1u
+#define GKRT_BUILD_TLAS 2u
+#define GKRT_BUILD_ALL  3u
+int  gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream);
+
+/* Passes (PathTracingRenderer::Render, PathTracingRenderer.cpp:104-218). */
+int  gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream);     /* "rt pass"        */
+int  gkrt_reproject_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream); /* "reproject pass" */
+int  gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream);   /* "compose pass"   */
+int  gkrt_end_frame(GkrtContext* ctx, void* stream);                                    /* "copy pass"      */
+/* All four in order: the whole Render() of the path-tracing logic renderer. */
+int  gkrt_render_frame(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream);
+
+/* Outputs (bindless storage images, BindlessTexture.slang:8-40). */
+int  gkrt_get_image(GkrtContext* ctx, int image_id, GkrtImageView* out);
+int  gkrt_copy_image_to_host(GkrtContext* ctx, int image_id, void* dst, size_t dst_bytes, void* stream);
+int  gkrt_upload_image(GkrtContext* ctx, int image_id, const void* src, size_t src_bytes, void* stream);
+
+/* Ray queries on the scene's BVH (FHardwareRayTracerV2::TraceRay / TraceOcclusion,
+ * assets/shaders/common/Shading.slang:737-826). rays/hits are device pointers. */
+int  gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32_t count,
+                     uint32_t mode, void* stream);
+
+int  gkrt_get_stats(GkrtContext* ctx, GkrtStats* out);
+int  gkrt_synchronize(GkrtContext* ctx, void* stream);
+
+/* Helper: world->object inverse of an affine 3x4 row-major transform, in FP64. */
+int  gkrt_affine_inverse(const float world[12], float world_inv[12]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GKRT_H */

@@ -1,0 +1,1068 @@
+// gk_oracle.cpp — CPU restatement of gkNextRenderer's ray-tracing pass.
+//
+// TEST INFRASTRUCTURE ONLY: this library is the oracle the GB300 kernels are checked
+// against (tests/, __graft_entry__.smoke(), and the CPU-baseline leg of bench.py). The
+// product library never links, loads or calls it.
+//
+// What it restates (reference files, paths within gkNextEngine):
+//   RNG ................ assets/shaders/common/Const_Func.slang:227-258 (pcg4d, uint_to_float)
+//   samplers ........... Const_Func.slang:8-49 (Schlick, ONB, AlignWithNormal), 260-340
+//                        (concentric disk, cone, cosine hemisphere, bounded VNDF GGX)
+//   camera ray ......... assets/shaders/common/Shading.slang:283-334 (FHardwarePrimaryRayCaster)
+//   closest/any hit .... Shading.slang:737-826 (FHardwareRayTracerV2) with the FP64 closest-hit
+//                        definition of oracle_isect.h in place of RT-core RayQuery
+//   bounce/shading ..... Shading.slang:1003-1082 (GetRayColor), 1084-1184 (Render)
+//   primary outputs .... Shading.slang:1186-1241 (PrimaryHit, Init), 50-72 (motion vector),
+//                        82-112 (FetchGBufferV2), Util.BufferClear.comp.slang:6-13 (clears)
+//   sun NEE ............ Shading.slang:886-908, 1135-1144
+//   probe termination .. assets/shaders/common/AmbientCube.slang:71-78, 178-223, 290-382
+//   sample multiplier .. assets/shaders/Core.PathTracing.comp.slang:16-30
+//   reprojection ....... assets/shaders/Process.ReProject.comp.slang:32-223
+//   bilateral denoise .. assets/shaders/Process.DenoiseJBF.comp.slang:14-184, tonemap
+//                        Const_Func.slang:51-126
+// Deviations that both sides share (documented with the product): FP32 vertices instead of
+// FP16; sin/cos of 2*pi*u and of |x|<=pi/4 from the polynomial in oracle_math.h; a constant
+// sky colour instead of the HDR texture; out-of-range image reads return zero; the
+// accumulation alpha keeps last frame's value (the reference writes only .rgb).
+#include "oracle_math.h"
+#include "oracle_isect.h"
+#include "../include/gkrt.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <limits>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace gko;
+
+namespace {
+
+const float kEPS = 1e-3f;                 // PreProcessor.slang:13
+const float kPT_MAX = 1000.0f;            // Shading.slang:15
+const float kM_1_PI = 0.318309886183790671538f;
+const float kCosQuarterDeg = 0.999990482f;  // cos(0.25 deg), Shading.slang:897
+const float kHalton[8][2] = {{0.5f, 0.3333f}, {0.25f, 0.6667f}, {0.75f, 0.1111f}, {0.125f, 0.4444f},
+                             {0.625f, 0.7778f}, {0.375f, 0.2222f}, {0.875f, 0.5556f}, {0.0625f, 0.8889f}};
+const int kCubeXY = 192, kCubeZ = 48;
+const float kCubeUnit = 0.25f;
+const float kCubeOff[3] = {-24.0f, -0.34375f, -24.0f};
+
+struct BNode {
+    float lo[3], hi[3];
+    int left;    // interior: left child; leaf: first prim
+    int count;   // 0 interior (right = left + 1 is not assumed; right stored below)
+    int right;
+};
+
+struct Bvh {
+    std::vector<BNode> nodes;
+    std::vector<uint32_t> prims;
+};
+
+struct Box { float lo[3], hi[3]; };
+
+void build_rec(Bvh& bvh, std::vector<Box>& boxes, std::vector<float>& cent, uint32_t* idx, int n, int node) {
+    Box b{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+    float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = 0; i < n; ++i) {
+        const Box& p = boxes[idx[i]];
+        for (int k = 0; k < 3; ++k) {
+            b.lo[k] = std::min(b.lo[k], p.lo[k]);
+            b.hi[k] = std::max(b.hi[k], p.hi[k]);
+            clo[k] = std::min(clo[k], cent[idx[i] * 3 + k]);
+            chi[k] = std::max(chi[k], cent[idx[i] * 3 + k]);
+        }
+    }
+    for (int k = 0; k < 3; ++k) { bvh.nodes[node].lo[k] = b.lo[k]; bvh.nodes[node].hi[k] = b.hi[k]; }
+    if (n <= 4) {
+        bvh.nodes[node].left = (int)(idx - bvh.prims.data());
+        bvh.nodes[node].count = n;
+        return;
+    }
+    int axis = 0;
+    float ext = chi[0] - clo[0];
+    for (int k = 1; k < 3; ++k) if (chi[k] - clo[k] > ext) { ext = chi[k] - clo[k]; axis = k; }
+    int mid = n / 2;
+    std::nth_element(idx, idx + mid, idx + n, [&](uint32_t a, uint32_t c) {
+        float ca = cent[a * 3 + axis], cc = cent[c * 3 + axis];
+        return ca < cc || (ca == cc && a < c);
+    });
+    int l = (int)bvh.nodes.size();
+    bvh.nodes.push_back(BNode{});
+    bvh.nodes.push_back(BNode{});
+    bvh.nodes[node].left = l;
+    bvh.nodes[node].right = l + 1;
+    bvh.nodes[node].count = 0;
+    build_rec(bvh, boxes, cent, idx, mid, l);
+    build_rec(bvh, boxes, cent, idx + mid, n - mid, l + 1);
+}
+
+void build_bvh(Bvh& bvh, std::vector<Box>& boxes) {
+    int n = (int)boxes.size();
+    bvh.nodes.clear();
+    bvh.prims.resize(n);
+    for (int i = 0; i < n; ++i) bvh.prims[i] = (uint32_t)i;
+    std::vector<float> cent(3 * (size_t)std::max(n, 1));
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) cent[i * 3 + k] = 0.5f * (boxes[i].lo[k] + boxes[i].hi[k]);
+    bvh.nodes.push_back(BNode{});
+    if (n == 0) {
+        for (int k = 0; k < 3; ++k) { bvh.nodes[0].lo[k] = 1.0f; bvh.nodes[0].hi[k] = -1.0f; }
+        bvh.nodes[0].left = 0; bvh.nodes[0].count = 0; bvh.nodes[0].right = -1;
+        return;
+    }
+    build_rec(bvh, boxes, cent, bvh.prims.data(), n, 0);
+}
+
+// Conservative double slab test (culling only; the triangle test decides hits).
+bool box_hit(const float lo[3], const float hi[3], const double o[3], const double invd[3], const bool zero[3],
+             double tmin, double tmax) {
+    double tn = -INFINITY, tf = INFINITY;
+    for (int k = 0; k < 3; ++k) {
+        if (zero[k]) {
+            double pad = 1e-9 * (std::fabs((double)lo[k]) + std::fabs((double)hi[k]) + 1e-30);
+            if (o[k] < (double)lo[k] - pad || o[k] > (double)hi[k] + pad) return false;
+            continue;
+        }
+        double t0 = ((double)lo[k] - o[k]) * invd[k];
+        double t1 = ((double)hi[k] - o[k]) * invd[k];
+        if (t0 > t1) std::swap(t0, t1);
+        tn = std::max(tn, t0);
+        tf = std::min(tf, t1);
+    }
+    double m = 1e-9 * (std::fabs(tn) + std::fabs(tf)) + 1e-12;
+    if (tn > tf + m) return false;
+    if (tf < tmin - m) return false;
+    if (tn > tmax + m) return false;
+    return true;
+}
+
+struct OScene {
+    std::vector<f3> pos, nrm;
+    std::vector<uint32_t> slot, idx;
+    std::vector<GkrtMesh> meshes;
+    std::vector<GkrtMaterial> mats;
+    std::vector<GkrtInstance> inst;
+    std::vector<GkrtLight> lights;
+    std::vector<uint32_t> cubes, voxels;
+    bool has_probes = false;
+    std::vector<Bvh> blas;
+    Bvh tlas;
+};
+
+// 0: every candidate triangle is decided by the FP64 test (the definition itself).
+// 1: the FP32 test with certified bounds rejects certain misses first; the outcome is the
+//    same, only faster (used for the timed CPU baseline).
+int g_fast = 0;
+
+struct HitRec {
+    bool hit;
+    uint32_t inst, prim;
+    double td;
+};
+
+struct LocalRay {
+    f3 o, d;
+    RayShear s;
+};
+
+LocalRay to_object(const GkrtInstance& in, f3 o, f3 d) {
+    LocalRay r;
+    r.o = xform_point(in.world_inv, o);
+    r.d = xform_vector(in.world_inv, d);
+    r.s = make_shear(r.d);
+    return r;
+}
+
+void tri_verts(const OScene& S, const GkrtMesh& m, uint32_t prim, f3& v0, f3& v1, f3& v2, uint32_t* vi = nullptr) {
+    uint32_t i0 = S.idx[m.index_offset + 3 * prim + 0] + m.vertex_offset;
+    uint32_t i1 = S.idx[m.index_offset + 3 * prim + 1] + m.vertex_offset;
+    uint32_t i2 = S.idx[m.index_offset + 3 * prim + 2] + m.vertex_offset;
+    v0 = S.pos[i0]; v1 = S.pos[i1]; v2 = S.pos[i2];
+    if (vi) { vi[0] = i0; vi[1] = i1; vi[2] = i2; }
+}
+
+inline bool key_less(double t, uint32_t inst, uint32_t prim, const HitRec& b) {
+    if (!b.hit) return true;
+    if (t != b.td) return t < b.td;
+    if (inst != b.inst) return inst < b.inst;
+    return prim < b.prim;
+}
+
+// Closest (any=false) or any (any=true) hit of a world ray under the FP64 definition.
+HitRec trace(const OScene& S, f3 o, f3 d, float tminf, float tmaxf, bool any, bool brute, uint64_t* tests) {
+    HitRec best{false, 0xFFFFFFFFu, 0xFFFFFFFFu, INFINITY};
+    const double tmin = tminf, tmax0 = tmaxf;
+    auto do_instance = [&](uint32_t ii) -> bool {
+        const GkrtInstance& in = S.inst[ii];
+        if (!in.visible) return false;
+        const GkrtMesh& m = S.meshes[in.mesh_id];
+        LocalRay lr = to_object(in, o, d);
+        double od[3] = {lr.o.x, lr.o.y, lr.o.z};
+        double dd[3] = {lr.d.x, lr.d.y, lr.d.z};
+        double inv[3];
+        bool zero[3];
+        for (int k = 0; k < 3; ++k) { zero[k] = dd[k] == 0.0; inv[k] = zero[k] ? 0.0 : 1.0 / dd[k]; }
+        auto test_tri = [&](uint32_t prim) -> bool {
+            f3 v0, v1, v2;
+            tri_verts(S, m, prim, v0, v1, v2);
+            if (tests) ++*tests;
+            if (g_fast && fp32_test(lr.o, lr.s, v0, v1, v2).kind == 0) return false;
+            ExactHit x = exact_test(lr.o, lr.s, v0, v1, v2);
+            if (!x.hit || !(x.t >= tmin && x.t <= tmax0)) return false;
+            if (any) { best = HitRec{true, ii, prim, x.t}; return true; }
+            if (key_less(x.t, ii, prim, best)) best = HitRec{true, ii, prim, x.t};
+            return false;
+        };
+        uint32_t ntri = m.index_count / 3;
+        if (brute) {
+            for (uint32_t p = 0; p < ntri; ++p) if (test_tri(p)) return true;
+            return false;
+        }
+        const Bvh& bv = S.blas[in.mesh_id];
+        int stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp) {
+            const BNode& nd = bv.nodes[stack[--sp]];
+            double tcut = best.hit ? best.td : tmax0;
+            if (!box_hit(nd.lo, nd.hi, od, inv, zero, tmin, tcut)) continue;
+            if (nd.count > 0) {
+                for (int i = 0; i < nd.count; ++i)
+                    if (test_tri(bv.prims[nd.left + i])) return true;
+            } else if (nd.right >= 0) {
+                stack[sp++] = nd.left;
+                stack[sp++] = nd.right;
+            }
+        }
+        return false;
+    };
+    if (brute) {
+        for (uint32_t ii = 0; ii < S.inst.size(); ++ii)
+            if (do_instance(ii)) return best;
+        return best;
+    }
+    double od[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z}, inv[3];
+    bool zero[3];
+    for (int k = 0; k < 3; ++k) { zero[k] = dd[k] == 0.0; inv[k] = zero[k] ? 0.0 : 1.0 / dd[k]; }
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const BNode& nd = S.tlas.nodes[stack[--sp]];
+        double tcut = best.hit ? best.td : tmax0;
+        if (!box_hit(nd.lo, nd.hi, od, inv, zero, tmin, tcut)) continue;
+        if (nd.count > 0) {
+            for (int i = 0; i < nd.count; ++i)
+                if (do_instance(S.tlas.prims[nd.left + i])) return best;
+        } else if (nd.right >= 0) {
+            stack[sp++] = nd.left;
+            stack[sp++] = nd.right;
+        }
+    }
+    return best;
+}
+
+struct Vtx {
+    f3 P, N;
+    uint32_t mat;
+    uint32_t inst;   // instance index
+};
+
+const GkrtMaterial& get_mat(const OScene& S, uint32_t i) {
+    uint32_t n = (uint32_t)S.mats.size();
+    return S.mats[i < n ? i : n - 1];
+}
+
+// FHardwareRayTracerV2::TraceRay (Shading.slang:784-826) on top of trace().
+bool trace_ray(const OScene& S, f3 o, f3 d, float tmax, Vtx& out, uint32_t* out_prim, uint64_t* rays) {
+    if (rays) ++*rays;
+    HitRec h = trace(S, o, d, kEPS, tmax, false, false, nullptr);
+    if (!h.hit) return false;
+    const GkrtInstance& in = S.inst[h.inst];
+    const GkrtMesh& m = S.meshes[in.mesh_id];
+    LocalRay lr = to_object(in, o, d);
+    f3 v0, v1, v2;
+    uint32_t vi[3];
+    tri_verts(S, m, h.prim, v0, v1, v2, vi);
+    HybridHit hh = hybrid_eval(lr.o, lr.s, v0, v1, v2);
+    f3 n0 = S.nrm[vi[0]], n1 = S.nrm[vi[1]], n2 = S.nrm[vi[2]];
+    // Mix(n0, n1, n2, bary) = n0 + (n1 - n0) b1 + (n2 - n0) b2
+    f3 e1 = sub(n1, n0), e2 = sub(n2, n0);
+    f3 nobj = f3{fma_(e2.x, hh.b2, fma_(e1.x, hh.b1, n0.x)), fma_(e2.y, hh.b2, fma_(e1.y, hh.b1, n0.y)),
+                 fma_(e2.z, hh.b2, fma_(e1.z, hh.b1, n0.z))};
+    out.N = normalize3(xform_normal(in.world_inv, nobj));
+    out.P = fma3(d, hh.t, o);
+    out.mat = in.mat_id[S.slot[vi[0]] & 15u];
+    out.inst = h.inst;
+    if (out_prim) *out_prim = h.prim;
+    return true;
+}
+
+bool trace_occlusion(const OScene& S, f3 o, f3 d, uint64_t* rays) {
+    if (rays) ++*rays;
+    return trace(S, o, d, kEPS, kPT_MAX, true, false, nullptr).hit;
+}
+
+// ---- samplers (Const_Func.slang) ----
+void onb(f3 n, f3& b1, f3& b2) {
+    float signZ = n.z < 0.0f ? -1.0f : 1.0f;
+    float a = -1.0f / (signZ + n.z);
+    b2 = f3{(n.x * n.y) * a, fma_(n.y * n.y, a, signZ), -n.y};
+    b1 = f3{fma_((signZ * n.x) * n.x, a, 1.0f), signZ * b2.x, -signZ * n.x};
+}
+// to_world(v, T, B, N) = v.x T + v.y B + v.z N
+f3 to_world(f3 v, f3 T, f3 B, f3 N) {
+    return f3{fma_(v.z, N.x, fma_(v.y, B.x, v.x * T.x)), fma_(v.z, N.y, fma_(v.y, B.y, v.x * T.y)),
+              fma_(v.z, N.z, fma_(v.y, B.z, v.x * T.z))};
+}
+f3 align_with_normal(f3 ray, f3 n) {
+    f3 T, B;
+    onb(n, T, B);
+    return to_world(ray, T, B, n);
+}
+f3 hemi1(uint32_t seed[4]) {
+    f2 u = rand2(seed);
+    float s, c;
+    sincos_2pi(u.x, &s, &c);
+    float r = std::sqrt(u.y);
+    return f3{r * c, r * s, std::sqrt(1.0f - u.y)};
+}
+f3 cone(uint32_t seed[4], float cos_theta) {
+    f2 u = rand2(seed);
+    float s, c;
+    sincos_2pi(u.x, &s, &c);
+    float ct = fma_(u.y, cos_theta - 1.0f, 1.0f);
+    float r = std::sqrt(fma_(-ct, ct, 1.0f));
+    return f3{r * c, r * s, ct};
+}
+f2 unit_disk(uint32_t seed[4]) {
+    f2 u = rand2(seed);
+    float ox = u.x + (u.x - 1.0f), oy = u.y + (u.y - 1.0f);
+    const float nz = 1e-35f;
+    if ((ox > -nz && ox < nz) && (oy > -nz && oy < nz)) return f2{0.0f, 0.0f};
+    const float pi4 = 0.785398163397448309616f;
+    float s, c;
+    if (std::fabs(ox) > std::fabs(oy)) {
+        float th = (pi4 * oy) / ox;
+        sincos_poly(th, &s, &c);
+        return f2{ox * c, ox * s};
+    }
+    float th = (pi4 * ox) / oy;
+    sincos_poly(th, &s, &c);
+    float ct = s;
+    return f2{oy * ct, oy * std::sqrt(fma_(-ct, ct, 1.0f))};
+}
+f3 ggx_vndf(float alpha, f3 wi_, f2 uv) {
+    f3 wi = normalize3(f3{wi_.x * alpha, wi_.y * alpha, wi_.z});
+    float b = wi.z;
+    if (wi_.z > 0.0f) {
+        float a = saturate(alpha);
+        float lxy = std::sqrt(fma_(wi_.y, wi_.y, wi_.x * wi_.x));
+        float awiz_s = (a * wi_.z) / (1.0f + lxy);
+        b = b * ((fma_(-a, a, 1.0f)) / fma_(awiz_s, awiz_s, 1.0f));
+    }
+    float z = fma_(1.0f - uv.y, 1.0f + b, -b);
+    float s, c;
+    sincos_2pi(uv.x, &s, &c);
+    float r = std::sqrt(saturate(fma_(-z, z, 1.0f)));
+    f3 o_std = f3{r * c, r * s, z};
+    f3 m = add(wi, o_std);
+    return normalize3(f3{m.x * alpha, m.y * alpha, m.z});
+}
+f3 ggx_sampling(uint32_t seed[4], float roughness, f3 n) {
+    f3 T, B;
+    onb(n, T, B);
+    f3 loc = f3{dot3(T, n), dot3(B, n), dot3(n, n)};
+    f2 uv = rand2(seed);
+    f3 wm = ggx_vndf(roughness * roughness, loc, uv);
+    return to_world(wm, T, B, n);
+}
+float schlick(float cosine, float ri) {
+    float r0 = (1.0f - ri) / (1.0f + ri);
+    r0 = r0 * r0;
+    float x = 1.0f - cosine;
+    float p5 = (((x * x) * x) * x) * x;
+    return fma_(1.0f - r0, p5, r0);
+}
+
+// ---- ambient cube probes (AmbientCube.slang) ----
+f4 unpack_rgb10a2(uint32_t p) {
+    float r = (float)(p & 0x3FFu) / 1023.0f;
+    float g = (float)((p >> 10) & 0x3FFu) / 1023.0f;
+    float b = (float)((p >> 20) & 0x3FFu) / 1023.0f;
+    return f4{r * 512.0f, g * 512.0f, b * 512.0f, 0.0f * 512.0f};
+}
+f4 sample_cube_full(const uint32_t* cube, f3 n) {
+    float wx = fmax_(n.x, 0.0f), wnx = fmax_(-n.x, 0.0f);
+    float wy = fmax_(n.y, 0.0f), wny = fmax_(-n.y, 0.0f);
+    float wz = fmax_(n.z, 0.0f), wnz = fmax_(-n.z, 0.0f);
+    float sum = ((((wx + wnx) + wy) + wny) + wz) + wnz;
+    uint32_t s0 = cube[12], s1 = cube[13];
+    float sky = 0.0f;
+    sky = sky + (float)(s0 & 0xFFu) * wz;
+    sky = sky + (float)((s0 >> 8) & 0xFFu) * wnz;
+    sky = sky + (float)((s0 >> 16) & 0xFFu) * wy;
+    sky = sky + (float)((s0 >> 24) & 0xFFu) * wny;
+    sky = sky + (float)(s1 & 0xFFu) * wx;
+    sky = sky + (float)((s1 >> 8) & 0xFFu) * wnx;
+    f4 col{0.0f, 0.0f, 0.0f, 0.0f};
+    const int order[12] = {10, 11, 8, 9, 6, 7, 4, 5, 2, 3, 0, 1};
+    const float w[12] = {wx, wnx, wy, wny, wz, wnz, wx, wnx, wy, wny, wz, wnz};
+    for (int i = 0; i < 12; ++i) col = add4(col, scale4(unpack_rgb10a2(cube[order[i]]), w[i]));
+    float k = sum > 0.0f ? 1.0f / sum : 1.0f;
+    col.x = col.x * k; col.y = col.y * k; col.z = col.z * k;
+    sky = sky * k;
+    col.w = sky / 255.0f;
+    return col;
+}
+f4 probe_term(const OScene& S, f3 p, f3 n) {
+    float npx = (p.x - kCubeOff[0]) / kCubeUnit;
+    float npy = (p.y - kCubeOff[1]) / kCubeUnit;
+    float npz = (p.z - kCubeOff[2]) / kCubeUnit;
+    // !(>=): a NaN position takes the early out (the shader would read undefined probes)
+    if (!(npx >= 0.0f) || !(npy >= 0.0f) || !(npz >= 0.0f) || npx > (float)(kCubeXY - 2) || npy > (float)(kCubeZ - 2) ||
+        npz > (float)(kCubeXY - 2))
+        return f4{0.0f, 0.0f, 0.0f, 1.0f};
+    if (!S.has_probes) return f4{0.0f, 0.0f, 0.0f, 0.0f};
+    float fx = std::floor(npx), fy = std::floor(npy), fz = std::floor(npz);
+    int bx = (int)fx, by = (int)fy, bz = (int)fz;
+    float frx = npx - fx, fry = npy - fy, frz = npz - fz;
+    float tw = 0.0f;
+    f4 res{0.0f, 0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < 8; ++i) {
+        int ox = i & 1, oy = (i >> 1) & 1, oz = (i >> 2) & 1;
+        int px = bx + ox, py = by + oy, pz = bz + oz;
+        size_t id = (size_t)py * kCubeXY * kCubeXY + (size_t)pz * kCubeXY + (size_t)px;
+        const uint32_t* cube = &S.cubes[id * 14];
+        const uint32_t* vox = &S.voxels[id * 4];
+        uint32_t u0 = vox[2], u1 = vox[3];
+        float d0y = (float)((u0 >> 8) & 0xFFu) / 255.0f;
+        float d0z = (float)((u0 >> 16) & 0xFFu) / 255.0f;
+        float d0w = (float)((u0 >> 24) & 0xFFu) / 255.0f;
+        float d1x = (float)(u1 & 0xFFu) / 255.0f;
+        float d1y = (float)((u1 >> 8) & 0xFFu) / 255.0f;
+        float d1z = (float)((u1 >> 16) & 0xFFu) / 255.0f;
+        float d1w = (float)((u1 >> 24) & 0xFFu) / 255.0f;
+        if (d0y < 0.01f) continue;
+        f3 pl = f3{frx - (float)ox, fry - (float)oy, frz - (float)oz};
+        float dist = length3(pl);
+        f3 dir = normalize3(pl);
+        float wxp = std::sqrt(fmax_(dir.x, 0.0f)), wxn = std::sqrt(fmax_(-dir.x, 0.0f));
+        float wyp = std::sqrt(fmax_(dir.y, 0.0f)), wyn = std::sqrt(fmax_(-dir.y, 0.0f));
+        float wzp = std::sqrt(fmax_(dir.z, 0.0f)), wzn = std::sqrt(fmax_(-dir.z, 0.0f));
+        float hl = wxp * d1x;
+        hl = hl + wxn * d1y;
+        hl = hl + wyp * d1z;
+        hl = hl + wyn * d1w;
+        hl = hl + wzp * d0z;
+        hl = hl + wzn * d0w;
+        if (dist > hl + 0.05f) continue;
+        float wx = ox == 0 ? 1.0f - frx : frx;
+        float wy = oy == 0 ? 1.0f - fry : fry;
+        float wz = oz == 0 ? 1.0f - frz : frz;
+        float wgt = (wx * wy) * wz;
+        f4 sc = sample_cube_full(cube, n);
+        res = add4(res, scale4(sc, wgt));
+        tw = tw + wgt;
+    }
+    if (tw > 0.0f) return f4{res.x / tw, res.y / tw, res.z / tw, res.w / tw};
+    return f4{0.0f, 0.0f, 0.0f, 0.0f};
+}
+
+f4 sky_color(const GkrtFrameConstants& fc) {
+    if (!fc.has_sky) return f4{0.0f, 0.0f, 0.0f, 0.0f};
+    f4 c{fmin_(10.0f, fc.sky_color[0]), fmin_(10.0f, fc.sky_color[1]), fmin_(10.0f, fc.sky_color[2]),
+         fmin_(1.0f, fc.sky_color[3])};
+    return scale4(c, fc.sky_intensity);
+}
+
+// FPathTracingRendererV2::GetRayColor (Shading.slang:1003-1082)
+bool get_ray_color(const OScene& S, const GkrtFrameConstants& fc, Vtx& v, f3& dir, f4& color, uint32_t seed[4],
+                   bool& hitReflect, bool& hitMetal, uint64_t* rays) {
+    const GkrtMaterial& mat = get_mat(S, v.mat);
+    const bool diel = mat.material_model == GKRT_MAT_DIELECTRIC;
+    const float startPosOffset = diel ? 0.0f : 1.0f;
+    const float roughness = mat.fuzziness;
+    const float dotValue = dot3(dir, v.N);
+    const bool back = dotValue > 0.0f;
+    const f3 outward = back ? neg(v.N) : v.N;
+    const float niOverNt = back ? mat.refraction_index2 : (1.0f / mat.refraction_index2);
+    const float cosine = dotValue > 0.0f ? mat.refraction_index * dotValue : -dotValue;
+    const float reflectProb = schlick(cosine, mat.refraction_index);
+    const float metalProb = mat.metalness;
+    bool chanceReflect = rand1(seed) < reflectProb;
+    bool chanceMetal = rand1(seed) < metalProb;
+    bool chanceGGX = chanceReflect || chanceMetal;
+    f3 next = chanceGGX ? reflect3(dir, outward) : outward;
+    f3 tdir = chanceGGX ? ggx_sampling(seed, std::sqrt(roughness), next) : align_with_normal(hemi1(seed), next);
+    hitReflect = chanceGGX;
+    hitMetal = chanceMetal;
+    if (diel && !chanceReflect) tdir = refract3(dir, outward, niOverNt);
+    dir = tdir;
+    f3 org = fma3(v.N, 0.001f * startPosOffset, v.P);
+    Vtx nv;
+    if (trace_ray(S, org, tdir, kPT_MAX, nv, nullptr, rays)) {
+        v = nv;
+        const GkrtMaterial& hm = get_mat(S, v.mat);
+        f4 alb{hm.diffuse[0], hm.diffuse[1], hm.diffuse[2], hm.diffuse[3]};
+        if (hm.material_model == GKRT_MAT_DIFFUSE_LIGHT || !chanceReflect) color = mul4(color, alb);
+        if (back && !diel) {
+            color = f4{0.5f, 0.5f, 0.5f, 0.0f};
+            return true;
+        }
+        if (hm.material_model == GKRT_MAT_DIFFUSE_LIGHT) return true;
+        return false;
+    }
+    color = mul4(color, sky_color(fc));
+    return true;
+}
+
+inline float* img_f4(void** im, int id, size_t i) { return ((float*)im[id]) + 4 * i; }
+
+struct PixelOut {
+    uint64_t rays;
+};
+
+// One pixel of Core.PathTracing (Core.PathTracing.comp.slang:7-31).
+void shade_pixel(const OScene& S, const GkrtFrameConstants& fc, int W, int H, int x, int y, void** im,
+                 uint64_t* rays) {
+    const size_t pix = (size_t)y * W + x;
+    uint32_t seed[4] = {(uint32_t)x, (uint32_t)y, fc.total_frames, 0u};
+    // Util.BufferClear: single-frame targets start at 0 / 100000
+    float* sd = img_f4(im, GKRT_IMG_SINGLE_DIFFUSE, pix);
+    float* ss = img_f4(im, GKRT_IMG_SINGLE_SPECULAR, pix);
+    ss[0] = ss[1] = ss[2] = ss[3] = 0.0f;
+    ((float*)im[GKRT_IMG_PREV_DEPTH])[pix] = 100000.0f;
+    if (im[GKRT_IMG_HIT_INST]) ((uint32_t*)im[GKRT_IMG_HIT_INST])[pix] = 0xFFFFFFFFu;
+    if (im[GKRT_IMG_HIT_PRIM]) ((uint32_t*)im[GKRT_IMG_HIT_PRIM])[pix] = 0xFFFFFFFFu;
+
+    // FHardwarePrimaryRayCaster::TracePrimaryRay
+    float uvx = fma_((float)x / (float)W, 2.0f, -1.0f);
+    float uvy = fma_((float)y / (float)H, 2.0f, -1.0f);
+    if (fc.taa) {
+        const float* h = kHalton[fc.total_frames % 8];
+        uvx = uvx + (h[0] - 0.5f) / (float)W;
+        uvy = uvy + (h[1] - 0.5f) / (float)H;
+    }
+    f2 disk = unit_disk(seed);
+    float ha = fc.aperture / 2.0f;
+    f2 off{ha * disk.x, ha * disk.y};
+    f4 origin = mat4_mul(fc.model_view_inverse, f4{off.x, off.y, 0.0f, 1.0f});
+    f4 target = mat4_mul(fc.projection_inverse, f4{uvx, uvy, 1.0f, 1.0f});
+    f3 tv = f3{fma_(target.x, fc.focus_distance, -off.x), fma_(target.y, fc.focus_distance, -off.y),
+               target.z * fc.focus_distance};
+    f3 tn = normalize3(tv);
+    f4 direction = mat4_mul(fc.model_view_inverse, f4{tn.x, tn.y, tn.z, 0.0f});
+    f3 o3 = xyz(origin), d3 = xyz(direction);
+    f3 primDir = normalize3(d3);
+    Vtx pv;
+    uint32_t pprim = 0;
+    bool hit = trace_ray(S, o3, d3, kPT_MAX, pv, &pprim, rays);
+
+    float* alb = img_f4(im, GKRT_IMG_ALBEDO, pix);
+    float* nrm = img_f4(im, GKRT_IMG_NORMAL, pix);
+    float* mot = ((float*)im[GKRT_IMG_MOTION]) + 2 * pix;
+    uint32_t* oid = (uint32_t*)im[GKRT_IMG_OBJECT_ID];
+    uint32_t* mom = (uint32_t*)im[GKRT_IMG_MOTION_MOMENT];
+    if (!hit) {
+        f4 sky = sky_color(fc);
+        sd[0] = sky.x; sd[1] = sky.y; sd[2] = sky.z; sd[3] = sky.w;
+        mot[0] = 0.0f; mot[1] = 0.0f;
+        alb[0] = alb[1] = alb[2] = alb[3] = 1.0f;
+        nrm[0] = 0.0f; nrm[1] = 1.0f; nrm[2] = 0.0f; nrm[3] = 1.0f;
+        oid[pix] = 65535u;
+        return;
+    }
+    if (im[GKRT_IMG_HIT_INST]) ((uint32_t*)im[GKRT_IMG_HIT_INST])[pix] = pv.inst;
+    if (im[GKRT_IMG_HIT_PRIM]) ((uint32_t*)im[GKRT_IMG_HIT_PRIM])[pix] = pprim;
+    const GkrtInstance& pin = S.inst[pv.inst];
+    // PrimaryHit (Shading.slang:1204-1220)
+    f4 P4{pv.P.x, pv.P.y, pv.P.z, 1.0f};
+    f4 clip = mat4_mul(fc.view_projection, P4);
+    float ndcDepth = clip.z / clip.w;
+    // CalculateMotionVectorV2 (Shading.slang:50-72)
+    f4 ch = mat4_mul(fc.view_projection_unjit, P4);
+    float cfx = (ch.x / ch.w) * 0.5f, cfy = (ch.y / ch.w) * 0.5f;
+    f3 prevP = xform_point(pin.combined_prev, pv.P);
+    f4 ph = mat4_mul(fc.prev_view_projection_unjit, f4{prevP.x, prevP.y, prevP.z, 1.0f});
+    float pfx = (ph.x / ph.w) * 0.5f, pfy = (ph.y / ph.w) * 0.5f;
+    if (length3(sub(pv.P, prevP)) > 0.02f) mom[pix] = fc.temporal_frames;
+    else mom[pix] = mom[pix] > 0u ? mom[pix] - 1u : 0u;
+    float mx = pfx - cfx, my = pfy - cfy;
+    const GkrtMaterial& pmat = get_mat(S, pv.mat);
+    f4 primaryAlbedo{pmat.diffuse[0], pmat.diffuse[1], pmat.diffuse[2], pmat.diffuse[3]};
+    alb[0] = primaryAlbedo.x; alb[1] = primaryAlbedo.y; alb[2] = primaryAlbedo.z; alb[3] = primaryAlbedo.w;
+    nrm[0] = pv.N.x; nrm[1] = pv.N.y; nrm[2] = pv.N.z; nrm[3] = pmat.fuzziness;
+    oid[pix] = pin.instance_id;
+    mot[0] = mx * (float)W; mot[1] = my * (float)H;
+    ((float*)im[GKRT_IMG_PREV_DEPTH])[pix] = ndcDepth;
+    if (pmat.material_model != GKRT_MAT_DIELECTRIC) pv.P = fma3(primDir, -0.03f, pv.P);
+
+    // Render (Shading.slang:1084-1184)
+    const int mult = mom[pix] > 0u ? 4 : 1;
+    f4 fcol{0.0f, 0.0f, 0.0f, 0.0f}, frefl{0.0f, 0.0f, 0.0f, 0.0f};
+    if (pmat.material_model == GKRT_MAT_DIFFUSE_LIGHT) {
+        sd[0] = pmat.diffuse[0]; sd[1] = pmat.diffuse[1]; sd[2] = pmat.diffuse[2]; sd[3] = pmat.diffuse[3];
+        return;
+    }
+    const bool pdiel = pmat.material_model == GKRT_MAT_DIELECTRIC;
+    int samples = (int)fc.number_of_samples * mult;
+    if (samples < 1) samples = 1;
+    f4 eye = mat4_mul(fc.model_view_inverse, f4{0.0f, 0.0f, 0.0f, 1.0f});
+    const uint32_t maxB = pdiel ? fc.max_number_of_bounces : fc.number_of_bounces;
+    for (int i = 0; i < samples; ++i) {
+        f4 rc{1.0f, 1.0f, 1.0f, 1.0f};
+        f3 dir = normalize3(sub(pv.P, xyz(eye)));
+        Vtx vs = pv;
+        bool hitReflect = false, hitMetal = false;
+        bool exitFirst = get_ray_color(S, fc, vs, dir, rc, seed, hitReflect, hitMetal, rays);
+        if (!exitFirst) {
+            if (fc.fast_gather && !pdiel) {
+                rc = mul4(rc, probe_term(S, vs.P, vs.N));
+            } else {
+                for (uint32_t b = 1; b < maxB; ++b) {
+                    bool dc = false;
+                    if (get_ray_color(S, fc, vs, dir, rc, seed, dc, dc, rays)) break;
+                    if (fc.has_sun && rand1(seed) < 0.5f) {
+                        f3 sun = f3{fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]};
+                        f3 cd = align_with_normal(cone(seed, kCosQuarterDeg), sun);
+                        if (!trace_occlusion(S, vs.P, cd, rays)) {
+                            rc = mul4(rc, f4{fc.sun_color[0], fc.sun_color[1], fc.sun_color[2], fc.sun_color[3]});
+                            break;
+                        }
+                    }
+                    const bool early = !pdiel && rand1(seed) < 0.5f;
+                    if (b == maxB - 1 || early) {
+                        rc = mul4(rc, probe_term(S, vs.P, vs.N));
+                        break;
+                    }
+                }
+            }
+        }
+        if (hitMetal) rc = mul4(rc, primaryAlbedo);
+        if (hitReflect) frefl = add4(frefl, rc);
+        else fcol = add4(fcol, rc);
+    }
+    const float fs = (float)samples;
+    fcol = f4{fcol.x / fs, fcol.y / fs, fcol.z / fs, fcol.w / fs};
+    frefl = f4{frefl.x / fs, frefl.y / fs, frefl.z / fs, frefl.w / fs};
+    // FHardwareDirectIlluminatorV2 (Shading.slang:886-908)
+    f3 sun = f3{fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]};
+    float dd = fmax_(dot3(sun, normalize3(pv.N)), 0.0f) * kM_1_PI;
+    float shadow = 0.0f;
+    if (fc.has_sun) {
+        f3 cd = align_with_normal(cone(seed, kCosQuarterDeg), sun);
+        shadow = 1.0f;
+        if (trace_occlusion(S, pv.P, cd, rays)) shadow = 0.0f;
+    }
+    f4 dc{(fc.sun_color[0] * dd) * shadow, (fc.sun_color[1] * dd) * shadow, (fc.sun_color[2] * dd) * shadow,
+          (fc.sun_color[3] * dd) * shadow};
+    fcol = add4(fcol, dc);
+    sd[0] = fcol.x; sd[1] = fcol.y; sd[2] = fcol.z; sd[3] = fcol.w;
+    ss[0] = frefl.x; ss[1] = frefl.y; ss[2] = frefl.z; ss[3] = frefl.w;
+}
+
+// ---- reprojection (Process.ReProject.comp.slang) ----
+struct Img {
+    int W, H;
+    bool in(int x, int y) const { return x >= 0 && y >= 0 && x < W && y < H; }
+};
+inline f4 ld4(const float* p, const Img& g, int x, int y) {
+    if (!g.in(x, y)) return f4{0.0f, 0.0f, 0.0f, 0.0f};
+    const float* q = p + 4 * ((size_t)y * g.W + x);
+    return f4{q[0], q[1], q[2], q[3]};
+}
+inline f2 ld2(const float* p, const Img& g, int x, int y) {
+    if (!g.in(x, y)) return f2{0.0f, 0.0f};
+    const float* q = p + 2 * ((size_t)y * g.W + x);
+    return f2{q[0], q[1]};
+}
+inline uint32_t ldu(const uint32_t* p, const Img& g, int x, int y) {
+    if (!g.in(x, y)) return 0u;
+    return p[(size_t)y * g.W + x];
+}
+inline float lerp_(float a, float b, float t) { return fma_(t, b - a, a); }
+inline f3 lerp3(f3 a, f3 b, float t) { return f3{lerp_(a.x, b.x, t), lerp_(a.y, b.y, t), lerp_(a.z, b.z, t)}; }
+inline f4 lerp4(f4 a, f4 b, float t) {
+    return f4{lerp_(a.x, b.x, t), lerp_(a.y, b.y, t), lerp_(a.z, b.z, t), lerp_(a.w, b.w, t)};
+}
+
+float calc_weight(float cd, bool same, bool center, f3 n, f3 cn) {
+    if (center) return 0.4f;
+    if (!same) return 0.0f;
+    float nd = saturate(dot3(n, cn));
+    const float th = 0.98f;
+    if (nd < th) return 0.0f;
+    float nw = (nd - th) / (1.0f - th);
+    return (nw * 2.0f) / fma_(cd, 1.5f, 4.0f);
+}
+
+f3 filter_history(const float* prev, const Img& g, f2 sub, int px, int py, uint32_t cur, uint32_t p0, uint32_t p1,
+                  uint32_t p2, uint32_t p3, f4 cs) {
+    f3 c = xyz(cs);
+    f3 h0 = cur == p0 ? xyz(ld4(prev, g, px, py)) : c;
+    f3 h1 = cur == p1 ? xyz(ld4(prev, g, px + 1, py)) : c;
+    f3 h2 = cur == p2 ? xyz(ld4(prev, g, px, py + 1)) : c;
+    f3 h3 = cur == p3 ? xyz(ld4(prev, g, px + 1, py + 1)) : c;
+    f3 h = lerp3(lerp3(h0, h1, sub.x), lerp3(h2, h3, sub.x), sub.y);
+    auto cl = [](float v) { return v < 0.0f ? 0.0f : (v > 1600.0f ? 1600.0f : v); };
+    return f3{cl(h.x), cl(h.y), cl(h.z)};
+}
+
+void reproject_pixel(const GkrtFrameConstants& fc, int W, int H, int x, int y, void** im) {
+    Img g{W, H};
+    const size_t pix = (size_t)y * W + x;
+    const float* SD = (const float*)im[GKRT_IMG_SINGLE_DIFFUSE];
+    const float* SS = (const float*)im[GKRT_IMG_SINGLE_SPECULAR];
+    const float* SA = (const float*)im[GKRT_IMG_ALBEDO];
+    const float* PD = (const float*)im[GKRT_IMG_PREV_DIFFUSE];
+    const float* PS = (const float*)im[GKRT_IMG_PREV_SPECULAR];
+    const float* PA = (const float*)im[GKRT_IMG_PREV_ALBEDO];
+    float* AD = (float*)im[GKRT_IMG_ACCUM_DIFFUSE];
+    float* AS = (float*)im[GKRT_IMG_ACCUM_SPECULAR];
+    float* AA = (float*)im[GKRT_IMG_ACCUM_ALBEDO];
+    const uint32_t* ID0 = (const uint32_t*)im[GKRT_IMG_OBJECT_ID];
+    const uint32_t* ID1 = (const uint32_t*)im[GKRT_IMG_OBJECT_ID_PREV];
+    const float* MV = (const float*)im[GKRT_IMG_MOTION];
+    const float* NB = (const float*)im[GKRT_IMG_NORMAL];
+    const uint32_t* MM = (const uint32_t*)im[GKRT_IMG_MOTION_MOMENT];
+    auto st = [&](float* dst, f4 v) { float* q = dst + 4 * pix; q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w; };
+    if (fc.progressive_render) {
+        const float k = 1.0f / 512.0f;
+        st(AD, lerp4(ld4(PD, g, x, y), ld4(SD, g, x, y), k));
+        st(AS, lerp4(ld4(PS, g, x, y), ld4(SS, g, x, y), k));
+        st(AA, lerp4(ld4(PA, g, x, y), ld4(SA, g, x, y), k));
+        return;
+    }
+    f4 cd = ld4(SD, g, x, y), cs = ld4(SS, g, x, y), ca = ld4(SA, g, x, y);
+    f2 mv = ld2(MV, g, x, y);
+    float fxm = (float)x + mv.x, fym = (float)y + mv.y;
+    float flx = std::floor(fxm), fly = std::floor(fym);
+    int px = (int)flx, py = (int)fly;
+    bool inside = px < W && py < H && px >= -1 && py >= -1;
+    uint32_t cur = ldu(ID0, g, x, y);
+    uint32_t p0 = ldu(ID1, g, px, py);
+    bool miss = cur == 65535u;
+    uint32_t moment = ldu(MM, g, x, y);
+    bool use = !(miss || !inside || moment > 0u);
+    if (!use) {
+        st(AD, cd); st(AS, cs); st(AA, ca);
+        return;
+    }
+    f3 cn = xyz(ld4(NB, g, x, y));
+    f4 sdiff{0, 0, 0, 0}, sspec{0, 0, 0, 0};
+    float tw = 0.0f, mir = 0.0f;
+    for (int oy = -2; oy <= 2; ++oy) {
+        for (int ox = -2; ox <= 2; ++ox) {
+            int sx = x + ox, sy = y + oy;
+            uint32_t pid = ldu(ID0, g, sx, sy);
+            f3 wn = xyz(ld4(NB, g, sx, sy));
+            bool center = ox == 0 && oy == 0;
+            bool same = pid == cur;
+            float fox = (float)ox, foy = (float)oy;
+            float cdist = std::sqrt(fma_(foy, foy, fox * fox));
+            float w = calc_weight(cdist, same, center, wn, cn);
+            sdiff = add4(sdiff, scale4(ld4(SD, g, sx, sy), w));
+            sspec = add4(sspec, scale4(ld4(SS, g, sx, sy), w));
+            tw = tw + w;
+            f2 m2 = ld2(MV, g, x + 2 * ox, y + 2 * oy);
+            mir = mir + std::sqrt(fma_(m2.y, m2.y, m2.x * m2.x));
+        }
+    }
+    sdiff = f4{sdiff.x / tw, sdiff.y / tw, sdiff.z / tw, sdiff.w / tw};
+    sspec = f4{sspec.x / tw, sspec.y / tw, sspec.z / tw, sspec.w / tw};
+    uint32_t p1 = ldu(ID1, g, px + 1, py), p2 = ldu(ID1, g, px, py + 1), p3 = ldu(ID1, g, px + 1, py + 1);
+    if (std::fabs(mir) < 0.1f) { p0 = cur; p1 = cur; p2 = cur; p3 = cur; }
+    f2 sub{fxm - flx, fym - fly};
+    f3 hd = filter_history(PD, g, sub, px, py, cur, p0, p1, p2, p3, sdiff);
+    f3 hs = filter_history(PS, g, sub, px, py, cur, p0, p1, p2, p3, sspec);
+    f3 ha = filter_history(PA, g, sub, px, py, cur, p0, p1, p2, p3, ca);
+    float tf = (float)(fc.temporal_frames > 1u ? fc.temporal_frames : 1u);
+    float keep = saturate(1.0f / tf);
+    f3 od = lerp3(hd, xyz(cd), keep), os = lerp3(hs, xyz(cs), keep), oa = lerp3(ha, xyz(ca), keep);
+    st(AD, f4{od.x, od.y, od.z, ld4(PD, g, x, y).w});
+    st(AS, f4{os.x, os.y, os.z, ld4(PS, g, x, y).w});
+    st(AA, f4{oa.x, oa.y, oa.z, ld4(PA, g, x, y).w});
+}
+
+// ---- compose / denoise (Process.DenoiseJBF.comp.slang, tonemaps Const_Func.slang:51-126) ----
+float gt_tonemap(float x) {
+    const float P = 1.0f, a = 0.7f, m = 0.22f, l = 0.4f, c = 1.33f, b = 0.0f;
+    const float e = 2.71828f;
+    float l0 = ((P - m) * l) / a;
+    float L0 = m - m / a;
+    (void)L0;
+    float L_x = m + a * (x - m);
+    float T_x = m * std::pow(x / m, c) + b;
+    float S0 = m + l0;
+    float S1 = m + a * l0;
+    float C2 = (a * P) / (P - S1);
+    float S_x = P - (P - S1) * std::pow(e, -((C2 * (x - S0)) / P));
+    auto Wf = [](float v, float e0, float e1) {
+        if (v <= e0) return 0.0f;
+        if (v >= e1) return 1.0f;
+        float q = (v - e0) / (e1 - e0);
+        return (q * q) * (3.0f - 2.0f * q);
+    };
+    auto Hf = [](float v, float e0, float e1) {
+        if (v <= e0) return 0.0f;
+        if (v >= e1) return 1.0f;
+        return (v - e0) / (e1 - e0);
+    };
+    float w0 = 1.0f - Wf(x, 0.0f, m);
+    float w2 = Hf(x, m + l0, m + l0);
+    float w1 = (1.0f - w0) - w2;
+    return (T_x * w0 + L_x * w1) + S_x * w2;
+}
+f3 pq_encode(f3 lin) {
+    const float m1 = 0.1593017578125f, m2 = 78.84375f, c1 = 0.8359375f, c2 = 18.8515625f, c3 = 18.6875f;
+    const float C = 10000.0f;
+    float in[3] = {lin.x / C, lin.y / C, lin.z / C}, out[3];
+    for (int k = 0; k < 3; ++k) {
+        float Lm = std::pow(in[k], m1);
+        float N1 = c1 + c2 * Lm;
+        float N2 = 1.0f + c3 * Lm;
+        float N = N1 * (1.0f / N2);
+        out[k] = std::pow(N, m2);
+    }
+    return f3{out[0], out[1], out[2]};
+}
+
+const f3 kLumW{0.212671f, 0.715160f, 0.072169f};
+
+void denoise_pixel(const GkrtFrameConstants& fc, int W, int H, int x, int y, void** im) {
+    Img g{W, H};
+    const size_t pix = (size_t)y * W + x;
+    const float* AD = (const float*)im[GKRT_IMG_ACCUM_DIFFUSE];
+    const float* AS = (const float*)im[GKRT_IMG_ACCUM_SPECULAR];
+    const float* AA = (const float*)im[GKRT_IMG_ACCUM_ALBEDO];
+    f3 total{0, 0, 0};
+    const f3 eps{0.001f, 0.001f, 0.001f};
+    if (fc.bf_size > 0u) {
+        f3 cc = add(xyz(ld4(AD, g, x, y)), eps);
+        f3 cspec = add(xyz(ld4(AS, g, x, y)), eps);
+        float clum = dot3(cc, kLumW);
+        const float sigma = fc.bf_sigma, sigmaL = fc.bf_sigma_lum * 100.0f;
+        const float den_s = (2.0f * sigma) * sigma, den_l = (2.0f * sigmaL) * sigmaL;
+        float wsum = 0.0f;
+        for (int i = -5; i <= 5; i += 2) {
+            for (int j = -5; j <= 5; j += 2) {
+                f3 ci = add(xyz(ld4(AD, g, x + j, y + i)), eps);
+                float lumi = dot3(ci, kLumW);
+                float dist = saturate((float)(i * i + j * j) / 25.0f);
+                float dl = (clum - lumi) * (clum - lumi);
+                float Fi = std::exp(-(dist * dist) / den_s);
+                float Li = std::exp(-(dl * dl) / den_l);
+                total = add(total, mul(mul(ci, Fi), Li));
+                wsum = wsum + Fi * Li;
+            }
+        }
+        total = f3{total.x / wsum, total.y / wsum, total.z / wsum};
+        f3 a = xyz(ld4(AA, g, x, y));
+        total = f3{fma_(total.x, a.x, cspec.x), fma_(total.y, a.y, cspec.y), fma_(total.z, a.z, cspec.z)};
+    } else {
+        f3 d = xyz(ld4(AD, g, x, y)), s = xyz(ld4(AS, g, x, y)), a = xyz(ld4(AA, g, x, y));
+        total = f3{fma_(d.x, a.x, s.x), fma_(d.y, a.y, s.y), fma_(d.z, a.z, s.z)};
+    }
+    float* lin = img_f4(im, GKRT_IMG_DENOISED_LINEAR, pix);
+    lin[0] = total.x; lin[1] = total.y; lin[2] = total.z; lin[3] = 1.0f;
+    float* out = img_f4(im, GKRT_IMG_DENOISED, pix);
+    if (fc.hdr) {
+        f3 t = f3{total.x / 2000.0f, total.y / 2000.0f, total.z / 2000.0f};
+        t = f3{gt_tonemap(t.x) * 2000.0f, gt_tonemap(t.y) * 2000.0f, gt_tonemap(t.z) * 2000.0f};
+        float k = fc.paper_white_nit / 230.0f;
+        f3 pq = pq_encode(f3{t.x * k, t.y * k, t.z * k});
+        out[0] = pq.x; out[1] = pq.y; out[2] = pq.z; out[3] = 1.0f;
+    } else {
+        float k = fc.paper_white_nit / 40000.0f;
+        out[0] = gt_tonemap(total.x * k);
+        out[1] = gt_tonemap(total.y * k);
+        out[2] = gt_tonemap(total.z * k);
+        out[3] = 1.0f;
+    }
+}
+
+}  // namespace
+
+// ===================================== C API ==========================================
+extern "C" {
+
+void* gko_scene_create(const GkrtSceneDesc* d) {
+    OScene* S = new OScene();
+    S->pos.resize(d->vertex_count);
+    S->nrm.resize(d->vertex_count);
+    S->slot.assign(d->material_slots, d->material_slots + d->vertex_count);
+    for (uint32_t i = 0; i < d->vertex_count; ++i) {
+        S->pos[i] = f3{d->positions[4 * i], d->positions[4 * i + 1], d->positions[4 * i + 2]};
+        S->nrm[i] = f3{d->normals[4 * i], d->normals[4 * i + 1], d->normals[4 * i + 2]};
+    }
+    S->idx.assign(d->indices, d->indices + d->index_count);
+    S->meshes.assign(d->meshes, d->meshes + d->mesh_count);
+    S->mats.assign(d->materials, d->materials + d->material_count);
+    S->inst.assign(d->instances, d->instances + d->instance_count);
+    if (d->lights && d->light_count) S->lights.assign(d->lights, d->lights + d->light_count);
+    if (d->probe_cubes && d->probe_voxels) {
+        size_t n = (size_t)kCubeXY * kCubeXY * kCubeZ;
+        S->cubes.assign(d->probe_cubes, d->probe_cubes + n * 14);
+        S->voxels.assign(d->probe_voxels, d->probe_voxels + n * 4);
+        S->has_probes = true;
+    }
+    // BLAS per mesh over triangle boxes (float min/max of the vertices: exact).
+    S->blas.resize(S->meshes.size());
+    std::vector<Box> rootbox(S->meshes.size());
+    for (size_t mi = 0; mi < S->meshes.size(); ++mi) {
+        const GkrtMesh& m = S->meshes[mi];
+        uint32_t nt = m.index_count / 3;
+        std::vector<Box> boxes(nt);
+        Box rb{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+        for (uint32_t t = 0; t < nt; ++t) {
+            f3 v[3];
+            tri_verts(*S, m, t, v[0], v[1], v[2]);
+            for (int k = 0; k < 3; ++k) {
+                float a = comp(v[0], k), b = comp(v[1], k), c = comp(v[2], k);
+                boxes[t].lo[k] = std::min(a, std::min(b, c));
+                boxes[t].hi[k] = std::max(a, std::max(b, c));
+                rb.lo[k] = std::min(rb.lo[k], boxes[t].lo[k]);
+                rb.hi[k] = std::max(rb.hi[k], boxes[t].hi[k]);
+            }
+        }
+        build_bvh(S->blas[mi], boxes);
+        rootbox[mi] = rb;
+    }
+    // TLAS over instance world boxes (corners transformed in double, padded).
+    std::vector<Box> ib;
+    std::vector<uint32_t> map;
+    for (size_t ii = 0; ii < S->inst.size(); ++ii) {
+        const GkrtInstance& in = S->inst[ii];
+        if (!in.visible) continue;
+        const Box& rb = rootbox[in.mesh_id];
+        Box w{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+        for (int c = 0; c < 8; ++c) {
+            double p[3] = {(c & 1) ? rb.hi[0] : rb.lo[0], (c & 2) ? rb.hi[1] : rb.lo[1], (c & 4) ? rb.hi[2] : rb.lo[2]};
+            for (int r = 0; r < 3; ++r) {
+                double v = (double)in.world[4 * r] * p[0] + (double)in.world[4 * r + 1] * p[1] +
+                           (double)in.world[4 * r + 2] * p[2] + (double)in.world[4 * r + 3];
+                w.lo[r] = std::min(w.lo[r], (float)v);
+                w.hi[r] = std::max(w.hi[r], (float)v);
+            }
+        }
+        for (int r = 0; r < 3; ++r) {
+            float pad = 1e-4f * (std::fabs(w.lo[r]) + std::fabs(w.hi[r]) + (w.hi[r] - w.lo[r])) + 1e-6f;
+            w.lo[r] -= pad;
+            w.hi[r] += pad;
+        }
+        ib.push_back(w);
+        map.push_back((uint32_t)ii);
+    }
+    build_bvh(S->tlas, ib);
+    for (auto& p : S->tlas.prims) p = map[p];
+    return S;
+}
+
+void gko_scene_destroy(void* s) { delete (OScene*)s; }
+
+// Closest (mode 0) or any (mode 1) hit of device-layout rays, FP64 definition.
+// brute != 0 tests every triangle of every instance. Fills GkrtHit like the GPU.
+void gko_trace_rays(void* s, const GkrtRay* rays, GkrtHit* hits, uint32_t n, uint32_t mode, int brute,
+                    int threads) {
+    const OScene& S = *(const OScene*)s;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        const GkrtRay& r = rays[i];
+        f3 o{r.origin[0], r.origin[1], r.origin[2]}, d{r.dir[0], r.dir[1], r.dir[2]};
+        HitRec h = trace(S, o, d, r.tmin, r.tmax, mode == GKRT_TRACE_ANY, brute != 0, nullptr);
+        GkrtHit& H = hits[i];
+        std::memset(&H, 0, sizeof(H));
+        if (!h.hit) {
+            H.t = -1.0f; H.inst = 0xFFFFFFFFu; H.prim = 0xFFFFFFFFu;
+            continue;
+        }
+        H.inst = h.inst;
+        H.prim = h.prim;
+        if (mode == GKRT_TRACE_ANY) { H.t = (float)h.td; continue; }
+        const GkrtInstance& in = S.inst[h.inst];
+        LocalRay lr = to_object(in, o, d);
+        f3 v0, v1, v2;
+        tri_verts(S, S.meshes[in.mesh_id], h.prim, v0, v1, v2);
+        HybridHit hh = hybrid_eval(lr.o, lr.s, v0, v1, v2);
+        H.t = hh.t; H.b1 = hh.b1; H.b2 = hh.b2;
+    }
+}
+
+// The "rt pass" over rows [y0, y1) (or every pixel when y1 <= y0). images: GKRT_IMG_COUNT
+// host pointers laid out like the product's images (NULL allowed for HIT_*).
+// Returns the number of rays traced (camera + bounce + shadow).
+uint64_t gko_trace_pass(void* s, const GkrtFrameConstants* fc, int W, int H, void** images, int y0, int y1,
+                        int threads) {
+    const OScene& S = *(const OScene*)s;
+    if (y1 <= y0) { y0 = 0; y1 = H; }
+    std::atomic<uint64_t> total{0};
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel
+#endif
+    {
+        uint64_t local = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64) nowait
+#endif
+        for (int64_t p = (int64_t)y0 * W; p < (int64_t)y1 * W; ++p)
+            shade_pixel(S, *fc, W, H, (int)(p % W), (int)(p / W), images, &local);
+        total += local;
+    }
+    return total.load();
+}
+
+void gko_reproject_pass(const GkrtFrameConstants* fc, int W, int H, void** images, int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t p = 0; p < (int64_t)W * H; ++p) reproject_pixel(*fc, W, H, (int)(p % W), (int)(p / W), images);
+}
+
+void gko_denoise_pass(const GkrtFrameConstants* fc, int W, int H, void** images, int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t p = 0; p < (int64_t)W * H; ++p) denoise_pixel(*fc, W, H, (int)(p % W), (int)(p / W), images);
+}
+
+void gko_set_fast(int on) { g_fast = on; }
+
+// Small known-answer hooks for the unit tests.
+void gko_pcg4d(uint32_t v[4]) { pcg4d(v); }
+float gko_uint_to_float(uint32_t x) { return u2f(x); }
+void gko_sincos_2pi(float u, float* s, float* c) { sincos_2pi(u, s, c); }
+void gko_sample_hemi(uint32_t seed[4], float out[3]) { f3 v = hemi1(seed); out[0] = v.x; out[1] = v.y; out[2] = v.z; }
+void gko_sample_ggx(uint32_t seed[4], float roughness, const float n[3], float out[3]) {
+    f3 v = ggx_sampling(seed, roughness, f3{n[0], n[1], n[2]});
+    out[0] = v.x; out[1] = v.y; out[2] = v.z;
+}
+float gko_schlick(float c, float ri) { return schlick(c, ri); }
+float gko_gt_tonemap(float x) { return gt_tonemap(x); }
+int gko_exact_tri(const float o[3], const float d[3], const float v[9], double out[3]) {
+    RayShear sh = make_shear(f3{d[0], d[1], d[2]});
+    ExactHit x = exact_test(f3{o[0], o[1], o[2]}, sh, f3{v[0], v[1], v[2]}, f3{v[3], v[4], v[5]}, f3{v[6], v[7], v[8]});
+    out[0] = x.t; out[1] = x.b1; out[2] = x.b2;
+    return x.hit ? 1 : 0;
+}
+int gko_fp32_tri(const float o[3], const float d[3], const float v[9], float out[4]) {
+    RayShear sh = make_shear(f3{d[0], d[1], d[2]});
+    Fp32Result r = fp32_test(f3{o[0], o[1], o[2]}, sh, f3{v[0], v[1], v[2]}, f3{v[3], v[4], v[5]}, f3{v[6], v[7], v[8]});
+    out[0] = r.t; out[1] = r.e; out[2] = r.b1; out[3] = r.b2;
+    return r.kind;
+}
+
+}  // extern "C"

@@ -1,0 +1,207 @@
+"""Python front end of the CPU oracle (test infrastructure only).
+
+The oracle is the checker of the GB300 kernels: a C++ restatement of the reference's
+path-tracing pass (gk_oracle.cpp, with its file:line citations) and the FP64 closest-hit
+definition (oracle_isect.h). Only the tests, __graft_entry__.smoke() and the CPU-baseline
+leg of bench.py use it; the product package never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+import subprocess
+
+import numpy as np
+
+from gknextengine_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libgkoracle.so")
+SOURCES = ["gk_oracle.cpp", "oracle_math.h", "oracle_isect.h", os.path.join("..", "include", "gkrt.h")]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with contraction off (see oracle_math.h)."""
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs)):
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           os.path.join(HERE, "gk_oracle.cpp"), "-o", LIB_PATH + ".tmp"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        cmd.insert(1, "-mfma")
+    subprocess.check_call(cmd)
+    os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(build())
+        L.gko_scene_create.restype = C.c_void_p
+        L.gko_scene_create.argtypes = [C.POINTER(abi.GkrtSceneDesc)]
+        L.gko_scene_destroy.argtypes = [C.c_void_p]
+        L.gko_trace_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_int]
+        L.gko_trace_pass.restype = C.c_uint64
+        L.gko_trace_pass.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_int, C.c_int,
+                                     C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
+        L.gko_reproject_pass.argtypes = [C.POINTER(abi.GkrtFrameConstants), C.c_int, C.c_int,
+                                         C.POINTER(C.c_void_p), C.c_int]
+        L.gko_denoise_pass.argtypes = [C.POINTER(abi.GkrtFrameConstants), C.c_int, C.c_int,
+                                       C.POINTER(C.c_void_p), C.c_int]
+        L.gko_uint_to_float.restype = C.c_float
+        L.gko_uint_to_float.argtypes = [C.c_uint32]
+        L.gko_sincos_2pi.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.gko_schlick.restype = C.c_float
+        L.gko_schlick.argtypes = [C.c_float, C.c_float]
+        L.gko_gt_tonemap.restype = C.c_float
+        L.gko_gt_tonemap.argtypes = [C.c_float]
+        L.gko_set_fast.argtypes = [C.c_int]
+        L.gko_exact_tri.restype = C.c_int
+        L.gko_fp32_tri.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def new_images(width: int, height: int) -> dict:
+    """Host images in the product's layouts (abi.IMAGE_FORMATS), zero-initialised."""
+    out = {}
+    for k, (dt, ch) in abi.IMAGE_FORMATS.items():
+        shape = (height, width) if ch == 1 else (height, width, ch)
+        out[k] = np.zeros(shape, dt)
+    return out
+
+
+def _ptrs(images: dict):
+    arr = (C.c_void_p * abi.IMG_COUNT)()
+    for k in range(abi.IMG_COUNT):
+        a = images.get(k)
+        arr[k] = a.ctypes.data if a is not None else None
+    return arr
+
+
+class OracleScene:
+    def __init__(self, scene: abi.SceneArrays):
+        self.scene = scene
+        self._desc = scene.desc()
+        self.h = lib().gko_scene_create(C.byref(self._desc))
+
+    def close(self):
+        if self.h:
+            lib().gko_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace_rays(self, rays: np.ndarray, mode: int = abi.TRACE_CLOSEST, brute: bool = False,
+                   threads: int = 0) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=abi.RAY_DTYPE)
+        hits = np.zeros(rays.shape[0], abi.HIT_DTYPE)
+        lib().gko_trace_rays(self.h, rays.ctypes.data, hits.ctypes.data, rays.shape[0], mode, int(brute), threads)
+        return hits
+
+    def trace_pass(self, fc, width, height, images, y0=0, y1=0, threads=0) -> int:
+        return int(lib().gko_trace_pass(self.h, C.byref(fc), width, height, _ptrs(images), y0, y1, threads))
+
+
+def reproject_pass(fc, width, height, images, threads=0):
+    lib().gko_reproject_pass(C.byref(fc), width, height, _ptrs(images), threads)
+
+
+def denoise_pass(fc, width, height, images, threads=0):
+    lib().gko_denoise_pass(C.byref(fc), width, height, _ptrs(images), threads)
+
+
+def end_frame(images):
+    """History hand-over of the copy pass (PathTracingRenderer.cpp:159-182 and the
+    object-id copy, VulkanBaseRenderer.cpp:1136-1152) as the buffer swap the library does."""
+    for a, b in ((abi.IMG_ACCUM_DIFFUSE, abi.IMG_PREV_DIFFUSE), (abi.IMG_ACCUM_SPECULAR, abi.IMG_PREV_SPECULAR),
+                 (abi.IMG_ACCUM_ALBEDO, abi.IMG_PREV_ALBEDO), (abi.IMG_OBJECT_ID, abi.IMG_OBJECT_ID_PREV)):
+        images[a], images[b] = images[b], images[a]
+
+
+def render_frame(oscene: OracleScene, fc, width, height, images, threads=0) -> int:
+    rays = oscene.trace_pass(fc, width, height, images, threads=threads)
+    reproject_pass(fc, width, height, images, threads)
+    denoise_pass(fc, width, height, images, threads)
+    end_frame(images)
+    return rays
+
+
+def pcg4d(v):
+    a = (C.c_uint32 * 4)(*[int(x) & 0xFFFFFFFF for x in v])
+    lib().gko_pcg4d(a)
+    return [int(x) for x in a]
+
+
+def sincos_2pi(u: float):
+    s, c = C.c_float(), C.c_float()
+    lib().gko_sincos_2pi(C.c_float(u), C.byref(s), C.byref(c))
+    return s.value, c.value
+
+
+# ---- the reference's own CPU BVH (tinybvh, vendored in gkNextEngine), test use only ----
+REF_DIR = os.path.join(HERE, "_ref")
+REF_LIB = os.path.join(REF_DIR, "libtinybvh_ref.so")
+REFERENCE_TINYBVH = "/root/reference/src/ThirdParty/tinybvh"
+
+
+def build_ref(force: bool = False):
+    """Compile ref_tinybvh.cpp against tiny_bvh.h where it lies in the reference tree.
+    Returns the library path, or None when the reference tree is not present (the GPU machine)
+    or the header does not build on this host."""
+    src = os.path.join(HERE, "ref_tinybvh.cpp")
+    if not force and os.path.exists(REF_LIB) and os.path.getmtime(REF_LIB) >= os.path.getmtime(src):
+        return REF_LIB
+    if not os.path.isdir(REFERENCE_TINYBVH):
+        return None
+    os.makedirs(REF_DIR, exist_ok=True)
+    cmd = ["g++", "-O2", "-std=c++20", "-fopenmp", "-fPIC", "-shared", "-w", "-I" + REFERENCE_TINYBVH, src,
+           "-o", REF_LIB + ".tmp"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        cmd[1:1] = ["-mavx2", "-mfma"]   # tiny_bvh.h uses SSE4/AVX intrinsics unconditionally on x86
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return None
+    os.replace(REF_LIB + ".tmp", REF_LIB)
+    return REF_LIB
+
+
+_ref = None
+
+
+def ref_lib():
+    """ctypes handle of the tinybvh shim, or None when it is unavailable."""
+    global _ref
+    if _ref is None:
+        p = REF_LIB if os.path.exists(REF_LIB) else build_ref()
+        if not p:
+            return None
+        L = C.CDLL(p)
+        L.gkref_closest_double.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.gkref_closest_float.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.gkref_closest_float.restype = C.c_int64
+        _ref = L
+    return _ref
+
+
+def ref_closest_double(tri_verts: np.ndarray, origins: np.ndarray, dirs: np.ndarray):
+    """tinybvh BVH_Double closest hits: tri_verts (n,3,3) float64; returns (t, prim)."""
+    L = ref_lib()
+    v = np.ascontiguousarray(tri_verts, np.float64).reshape(-1, 9)
+    r = np.ascontiguousarray(np.concatenate([origins, dirs], axis=1), np.float64)
+    t = np.zeros(r.shape[0], np.float64)
+    p = np.zeros(r.shape[0], np.int64)
+    L.gkref_closest_double(v.ctypes.data, v.shape[0], r.ctypes.data, r.shape[0], t.ctypes.data, p.ctypes.data)
+    return t, p
