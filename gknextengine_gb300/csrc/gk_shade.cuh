@@ -50,36 +50,27 @@ GK_D MatV load_mat(const ShadeScene& sc, uint32_t i) {
     return m;
 }
 
-// FHardwareRayTracerV2::TraceRay: closest hit -> position, shading normal, material.
-GK_D bool trace_ray(const ShadeScene& sc, f3 o, f3 d, float tmax, Vtx& out, uint32_t* prim_out, uint32_t* stk,
-                    int stride, Counters& cn) {
-    ++cn.rays;
-    TraceOut r = trace_closest(sc.S, o, d, 1e-3f, tmax, stk, stride, cn);
-    if (!r.hit) return false;
-    HitShade h = hit_shade(sc.S, o, d, r.inst, r.tri);
-    const DevInst* ip = sc.S.inst + r.inst;
-    const uint32_t ioff = __ldg(&ip->index_offset) + 3u * r.prim, voff = __ldg(&ip->vertex_offset);
+// FHardwareRayTracerV2::TraceRay after the query (Shading.slang:801-823): position,
+// interpolated shading normal through WorldToObject, and the material of vertex 0's slot.
+static __device__ __noinline__ Vtx hit_vertex(const ShadeScene& sc, f3 o, f3 d, uint32_t inst, uint32_t prim, uint32_t tri) {
+    const HitShade h = hit_shade(sc.S, o, d, inst, tri);
+    const DevInst* ip = sc.S.inst + inst;
+    const uint32_t ioff = __ldg(&ip->index_offset) + 3u * prim, voff = __ldg(&ip->vertex_offset);
     const uint32_t i0 = __ldg(&sc.indices[ioff]) + voff, i1 = __ldg(&sc.indices[ioff + 1]) + voff,
                    i2 = __ldg(&sc.indices[ioff + 2]) + voff;
-    float4 a = __ldg(&sc.normals[i0]), b = __ldg(&sc.normals[i1]), c = __ldg(&sc.normals[i2]);
-    f3 n0 = F3(a.x, a.y, a.z), e1 = F3(b.x, b.y, b.z) - n0, e2 = F3(c.x, c.y, c.z) - n0;
-    f3 nobj = F3(fmaf_(e2.x, h.b2, fmaf_(e1.x, h.b1, n0.x)), fmaf_(e2.y, h.b2, fmaf_(e1.y, h.b1, n0.y)),
-                 fmaf_(e2.z, h.b2, fmaf_(e1.z, h.b1, n0.z)));
+    const float4 a = __ldg(&sc.normals[i0]), b = __ldg(&sc.normals[i1]), c = __ldg(&sc.normals[i2]);
+    const f3 n0 = F3(a.x, a.y, a.z), e1 = F3(b.x, b.y, b.z) - n0, e2 = F3(c.x, c.y, c.z) - n0;
+    const f3 nobj = F3(fmaf_(e2.x, h.b2, fmaf_(e1.x, h.b1, n0.x)), fmaf_(e2.y, h.b2, fmaf_(e1.y, h.b1, n0.y)),
+                       fmaf_(e2.z, h.b2, fmaf_(e1.z, h.b1, n0.z)));
     float w[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) w[k] = __ldg(&ip->winv[k]);
+    Vtx out;
     out.N = normalize3(xnormal(w, nobj));
     out.P = fma3(d, h.t, o);
-    out.mat = __ldg(&sc.inst_mat[16u * r.inst + (__ldg(&sc.slots[i0]) & 15u)]);
-    out.inst = r.inst;
-    if (prim_out) *prim_out = r.prim;
-    return true;
-}
-
-GK_D bool trace_occlusion(const ShadeScene& sc, f3 o, f3 d, uint32_t* stk, int stride, Counters& cn) {
-    ++cn.rays;
-    TraceOut r = traverse<kAny>(sc.S, o, d, 1e-3f, 1000.0f, stk, stride, cn);
-    return r.hit;
+    out.mat = __ldg(&sc.inst_mat[16u * inst + (__ldg(&sc.slots[i0]) & 15u)]);
+    out.inst = inst;
+    return out;
 }
 
 GK_D f4 sky(const GkrtFrameConstants& fc) {
@@ -117,12 +108,17 @@ GK_D f4 cube_sample(const uint32_t* cube, f3 n) {
     col.w = div_(sk, 255.0f);
     return col;
 }
+static __device__ __noinline__ f4 probe_grid(const ShadeScene& sc, float npx, float npy, float npz, f3 n);
 GK_D f4 probe_term(const ShadeScene& sc, f3 p, f3 n) {
     float npx = div_(p.x - -24.0f, 0.25f), npy = div_(p.y - -0.34375f, 0.25f), npz = div_(p.z - -24.0f, 0.25f);
     // written as !(>=) so that a NaN position takes the early out
     if (!(npx >= 0.0f) || !(npy >= 0.0f) || !(npz >= 0.0f) || npx > 190.0f || npy > 46.0f || npz > 190.0f)
         return F4(0.0f, 0.0f, 0.0f, 1.0f);
     if (!sc.cubes) return F4(0.0f, 0.0f, 0.0f, 0.0f);
+    return probe_grid(sc, npx, npy, npz, n);
+}
+// The 8-probe interpolation itself (only reached when a probe grid was uploaded).
+static __device__ __noinline__ f4 probe_grid(const ShadeScene& sc, float npx, float npy, float npz, f3 n) {
     float fx = floorf(npx), fy = floorf(npy), fz = floorf(npz);
     int bx = (int)fx, by = (int)fy, bz = (int)fz;
     float frx = npx - fx, fry = npy - fy, frz = npz - fz;
@@ -156,41 +152,6 @@ GK_D f4 probe_term(const ShadeScene& sc, f3 p, f3 n) {
     return F4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
-// GetRayColor (Shading.slang:1003-1082)
-GK_D bool ray_color(const ShadeScene& sc, const GkrtFrameConstants& fc, Vtx& v, f3& dir, f4& color, Rng& seed,
-                    bool& hitReflect, bool& hitMetal, uint32_t* stk, int stride, Counters& cn) {
-    const MatV mat = load_mat(sc, v.mat);
-    const bool diel = mat.model == GKRT_MAT_DIELECTRIC;
-    const float startPosOffset = diel ? 0.0f : 1.0f;
-    const float dotValue = dot3(dir, v.N);
-    const bool back = dotValue > 0.0f;
-    const f3 outward = back ? -v.N : v.N;
-    const float niOverNt = back ? mat.ri2 : div_(1.0f, mat.ri2);
-    const float cosine = dotValue > 0.0f ? mat.ri * dotValue : -dotValue;
-    const float reflectProb = schlick(cosine, mat.ri);
-    const bool chanceReflect = rnd1(seed) < reflectProb;
-    const bool chanceMetal = rnd1(seed) < mat.metal;
-    const bool chanceGGX = chanceReflect || chanceMetal;
-    f3 tdir;
-    if (chanceGGX) tdir = ggx_sample(seed, sqrt_(mat.fuzz), reflect3(dir, outward));
-    else tdir = align_normal(hemisphere_cos(seed), outward);
-    hitReflect = chanceGGX;
-    hitMetal = chanceMetal;
-    if (diel && !chanceReflect) tdir = refract3(dir, outward, niOverNt);
-    dir = tdir;
-    f3 org = fma3(v.N, 0.001f * startPosOffset, v.P);
-    Vtx nv;
-    if (trace_ray(sc, org, tdir, 1000.0f, nv, nullptr, stk, stride, cn)) {
-        v = nv;
-        const MatV hm = load_mat(sc, v.mat);
-        if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !chanceReflect) color = color * hm.diffuse;
-        if (back && !diel) { color = F4(0.5f, 0.5f, 0.5f, 0.0f); return true; }
-        return hm.model == GKRT_MAT_DIFFUSE_LIGHT;
-    }
-    color = color * sky(fc);
-    return true;
-}
-
 struct PixelImages {
     float4* single_diffuse;
     float4* single_specular;
@@ -206,120 +167,5 @@ struct PixelImages {
 
 __constant__ float c_halton[16] = {0.5f, 0.3333f, 0.25f, 0.6667f, 0.75f, 0.1111f, 0.125f, 0.4444f,
                                    0.625f, 0.7778f, 0.375f, 0.2222f, 0.875f, 0.5556f, 0.0625f, 0.8889f};
-
-// One pixel of Core.PathTracing (PrimaryHit + Render + DirectIlluminate).
-GK_D void shade_pixel(const ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int x, int y,
-                      const PixelImages& im, uint32_t* stk, int stride, Counters& cn) {
-    const size_t pix = (size_t)y * W + x;
-    Rng seed;
-    seed.v[0] = (uint32_t)x; seed.v[1] = (uint32_t)y; seed.v[2] = fc.total_frames; seed.v[3] = 0u;
-    const bool want_ids = (fc.flags & GKRT_FRAME_PRIMARY_IDS) != 0u;
-    float uvx = fmaf_(div_((float)x, (float)W), 2.0f, -1.0f);
-    float uvy = fmaf_(div_((float)y, (float)H), 2.0f, -1.0f);
-    if (fc.taa) {
-        const uint32_t hi = fc.total_frames % 8u;
-        uvx = uvx + div_(c_halton[2 * hi] - 0.5f, (float)W);
-        uvy = uvy + div_(c_halton[2 * hi + 1] - 0.5f, (float)H);
-    }
-    f2 disk = unit_disk(seed);
-    const float ha = div_(fc.aperture, 2.0f);
-    const float offx = ha * disk.x, offy = ha * disk.y;
-    f4 origin = mat4v(fc.model_view_inverse, F4(offx, offy, 0.0f, 1.0f));
-    f4 target = mat4v(fc.projection_inverse, F4(uvx, uvy, 1.0f, 1.0f));
-    f3 tn = normalize3(F3(fmaf_(target.x, fc.focus_distance, -offx), fmaf_(target.y, fc.focus_distance, -offy),
-                          target.z * fc.focus_distance));
-    f4 direction = mat4v(fc.model_view_inverse, F4(tn.x, tn.y, tn.z, 0.0f));
-    const f3 o3 = xyz(origin), d3 = xyz(direction);
-    const f3 primDir = normalize3(d3);
-    Vtx pv;
-    uint32_t pprim = 0;
-    const bool hit = trace_ray(sc, o3, d3, 1000.0f, pv, &pprim, stk, stride, cn);
-    im.single_specular[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (!hit) {
-        f4 s = sky(fc);
-        im.single_diffuse[pix] = make_float4(s.x, s.y, s.z, s.w);
-        im.motion[pix] = make_float2(0.0f, 0.0f);
-        im.albedo[pix] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-        im.normal[pix] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
-        im.object_id[pix] = 65535u;
-        im.prev_depth[pix] = 100000.0f;
-        if (want_ids) { im.hit_inst[pix] = 0xFFFFFFFFu; im.hit_prim[pix] = 0xFFFFFFFFu; }
-        return;
-    }
-    if (want_ids) { im.hit_inst[pix] = pv.inst; im.hit_prim[pix] = pprim; }
-    const f4 P4 = F4(pv.P.x, pv.P.y, pv.P.z, 1.0f);
-    const f4 clip = mat4v(fc.view_projection, P4);
-    const f4 ch = mat4v(fc.view_projection_unjit, P4);
-    const float cfx = div_(ch.x, ch.w) * 0.5f, cfy = div_(ch.y, ch.w) * 0.5f;
-    float cp[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) cp[k] = __ldg(&sc.inst_prev[12u * pv.inst + k]);
-    const f3 prevP = xpoint(cp, pv.P);
-    const f4 ph = mat4v(fc.prev_view_projection_unjit, F4(prevP.x, prevP.y, prevP.z, 1.0f));
-    const float pfx = div_(ph.x, ph.w) * 0.5f, pfy = div_(ph.y, ph.w) * 0.5f;
-    uint32_t mom = im.motion_moment[pix];
-    if (len3(pv.P - prevP) > 0.02f) mom = fc.temporal_frames;
-    else mom = mom > 0u ? mom - 1u : 0u;
-    im.motion_moment[pix] = mom;
-    const MatV pm = load_mat(sc, pv.mat);
-    im.albedo[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
-    im.normal[pix] = make_float4(pv.N.x, pv.N.y, pv.N.z, pm.fuzz);
-    im.object_id[pix] = __ldg(&sc.S.inst[pv.inst].instance_id);
-    im.motion[pix] = make_float2((pfx - cfx) * (float)W, (pfy - cfy) * (float)H);
-    im.prev_depth[pix] = div_(clip.z, clip.w);
-    if (pm.model != GKRT_MAT_DIELECTRIC) pv.P = fma3(primDir, -0.03f, pv.P);
-    if (pm.model == GKRT_MAT_DIFFUSE_LIGHT) {
-        im.single_diffuse[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
-        return;
-    }
-    const bool pdiel = pm.model == GKRT_MAT_DIELECTRIC;
-    int samples = (int)fc.number_of_samples * (mom > 0u ? 4 : 1);
-    if (samples < 1) samples = 1;
-    const f4 eye = mat4v(fc.model_view_inverse, F4(0.0f, 0.0f, 0.0f, 1.0f));
-    const uint32_t maxB = pdiel ? fc.max_number_of_bounces : fc.number_of_bounces;
-    const f3 sunDir = F3(fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]);
-    const f4 sunCol = F4(fc.sun_color[0], fc.sun_color[1], fc.sun_color[2], fc.sun_color[3]);
-    const float kCosCone = 0.999990482f;
-    f4 fcol = F4(0.0f, 0.0f, 0.0f, 0.0f), frefl = F4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (int i = 0; i < samples; ++i) {
-        f4 rc = F4(1.0f, 1.0f, 1.0f, 1.0f);
-        f3 dir = normalize3(pv.P - xyz(eye));
-        Vtx vs = pv;
-        bool hitReflect = false, hitMetal = false;
-        const bool exitFirst = ray_color(sc, fc, vs, dir, rc, seed, hitReflect, hitMetal, stk, stride, cn);
-        if (!exitFirst) {
-            if (fc.fast_gather && !pdiel) {
-                rc = rc * probe_term(sc, vs.P, vs.N);
-            } else {
-                for (uint32_t b = 1; b < maxB; ++b) {
-                    bool dc = false, dc2 = false;
-                    if (ray_color(sc, fc, vs, dir, rc, seed, dc, dc2, stk, stride, cn)) break;
-                    if (fc.has_sun && rnd1(seed) < 0.5f) {
-                        const f3 cd = align_normal(cone(seed, kCosCone), sunDir);
-                        if (!trace_occlusion(sc, vs.P, cd, stk, stride, cn)) { rc = rc * sunCol; break; }
-                    }
-                    const bool early = !pdiel && rnd1(seed) < 0.5f;
-                    if (b == maxB - 1u || early) { rc = rc * probe_term(sc, vs.P, vs.N); break; }
-                }
-            }
-        }
-        if (hitMetal) rc = rc * pm.diffuse;
-        if (hitReflect) frefl = frefl + rc;
-        else fcol = fcol + rc;
-    }
-    const float fs = (float)samples;
-    fcol = F4(div_(fcol.x, fs), div_(fcol.y, fs), div_(fcol.z, fs), div_(fcol.w, fs));
-    frefl = F4(div_(frefl.x, fs), div_(frefl.y, fs), div_(frefl.z, fs), div_(frefl.w, fs));
-    const float dd = mx(dot3(sunDir, normalize3(pv.N)), 0.0f) * 0.318309886183790671538f;
-    float shadow = 0.0f;
-    if (fc.has_sun) {
-        const f3 cd = align_normal(cone(seed, kCosCone), sunDir);
-        shadow = trace_occlusion(sc, pv.P, cd, stk, stride, cn) ? 0.0f : 1.0f;
-    }
-    fcol = fcol + F4((sunCol.x * dd) * shadow, (sunCol.y * dd) * shadow, (sunCol.z * dd) * shadow,
-                     (sunCol.w * dd) * shadow);
-    im.single_diffuse[pix] = make_float4(fcol.x, fcol.y, fcol.z, fcol.w);
-    im.single_specular[pix] = make_float4(frefl.x, frefl.y, frefl.z, frefl.w);
-}
 
 }  // namespace gk

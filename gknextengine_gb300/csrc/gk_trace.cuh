@@ -12,8 +12,8 @@
 // error bounds and uses FP64 only where the bounds do not decide:
 //   * edge functions U, V, W within their error bound of zero -> FP64 test;
 //   * t within its error bound of tmin/tmax -> FP64 t;
-//   * two hits whose t-intervals overlap -> the ray is traced again with every candidate
-//     decided in FP64 (exact mode).
+//   * two hits whose t-intervals overlap -> both are decided in FP64 (the incumbent's
+//     triangle is fetched again) and the key is compared exactly.
 // Box tests widen the slab interval by 1e-6 relative (> 2.5 gamma_3), so no box holding
 // the FP64 winner is culled. The float t and barycentrics used for shading are those of
 // the FP32 test when it is certain, else the rounded FP64 values.
@@ -59,7 +59,6 @@ struct SceneView {
 struct Shear {
     int kx, ky, kz;
     float Sx, Sy, Sz;
-    double Sxd, Syd, Szd;
 };
 
 GK_D float pick(f3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
@@ -80,26 +79,36 @@ GK_D Shear make_shear(f3 d) {
     s.Sx = div_(dx, dz);
     s.Sy = div_(dy, dz);
     s.Sz = rcp_(dz);
-    s.Sxd = (double)dx / (double)dz;
-    s.Syd = (double)dy / (double)dz;
-    s.Szd = 1.0 / (double)dz;
     return s;
+}
+
+// FP64 shear constants, computed only when an FP64 decision is needed.
+struct ShearD { double Sxd, Syd, Szd; };
+GK_D ShearD shear_d(f3 d, const Shear& s) {
+    const double dz = (double)pick(d, s.kz);
+    ShearD r;
+    r.Sxd = (double)pick(d, s.kx) / dz;
+    r.Syd = (double)pick(d, s.ky) / dz;
+    r.Szd = 1.0 / dz;
+    return r;
 }
 
 struct ExactHit { bool hit; double t, b1, b2; };
 
 // FP64 watertight test; products and sums rounded in double, nothing fused.
-GK_D ExactHit exact_test(f3 o, const Shear& s, f3 v0, f3 v1, f3 v2) {
+// Out of line: taken rarely, and inlining it at every call site bloats the hot kernel.
+static __device__ __noinline__ ExactHit exact_test(f3 o, f3 d, Shear s, f3 v0, f3 v1, f3 v2) {
     ExactHit r; r.hit = false; r.t = 0.0; r.b1 = 0.0; r.b2 = 0.0;
+    const ShearD sd = shear_d(d, s);
     double Ak = (double)pick(v0, s.kz) - (double)pick(o, s.kz);
     double Bk = (double)pick(v1, s.kz) - (double)pick(o, s.kz);
     double Ck = (double)pick(v2, s.kz) - (double)pick(o, s.kz);
-    double Ax = ((double)pick(v0, s.kx) - (double)pick(o, s.kx)) - s.Sxd * Ak;
-    double Ay = ((double)pick(v0, s.ky) - (double)pick(o, s.ky)) - s.Syd * Ak;
-    double Bx = ((double)pick(v1, s.kx) - (double)pick(o, s.kx)) - s.Sxd * Bk;
-    double By = ((double)pick(v1, s.ky) - (double)pick(o, s.ky)) - s.Syd * Bk;
-    double Cx = ((double)pick(v2, s.kx) - (double)pick(o, s.kx)) - s.Sxd * Ck;
-    double Cy = ((double)pick(v2, s.ky) - (double)pick(o, s.ky)) - s.Syd * Ck;
+    double Ax = ((double)pick(v0, s.kx) - (double)pick(o, s.kx)) - sd.Sxd * Ak;
+    double Ay = ((double)pick(v0, s.ky) - (double)pick(o, s.ky)) - sd.Syd * Ak;
+    double Bx = ((double)pick(v1, s.kx) - (double)pick(o, s.kx)) - sd.Sxd * Bk;
+    double By = ((double)pick(v1, s.ky) - (double)pick(o, s.ky)) - sd.Syd * Bk;
+    double Cx = ((double)pick(v2, s.kx) - (double)pick(o, s.kx)) - sd.Sxd * Ck;
+    double Cy = ((double)pick(v2, s.ky) - (double)pick(o, s.ky)) - sd.Syd * Ck;
     double U = Cx * By - Cy * Bx;
     double V = Ax * Cy - Ay * Cx;
     double W = Bx * Ay - By * Ax;
@@ -107,7 +116,7 @@ GK_D ExactHit exact_test(f3 o, const Shear& s, f3 v0, f3 v1, f3 v2) {
     if (!in) return r;
     double det = U + V + W;
     if (det == 0.0) return r;
-    double T = U * (s.Szd * Ak) + V * (s.Szd * Bk) + W * (s.Szd * Ck);
+    double T = U * (sd.Szd * Ak) + V * (sd.Szd * Bk) + W * (sd.Szd * Ck);
     r.hit = true;
     r.t = T / det;
     r.b1 = V / det;
@@ -172,6 +181,40 @@ GK_D Fp32Hit fp32_test(f3 o, const Shear& s, f3 v0, f3 v1, f3 v2) {
     return r;
 }
 
+// Certified interval for the exact hit distance, from the plane of the triangle:
+// t = dot(n, v0 - o) / dot(n, d), n = (v1 - v0) x (v2 - v0). Its error grows like
+// u |t| / cos(theta), while the bound carried by the sheared edge functions grows like
+// u |t| * distance / size, far too wide for small distant triangles. Used only to order
+// candidates and to check [tmin, tmax]; the shading t stays the sheared FP32 value.
+// e_woop (the sheared bound) scaled by 2^-28 covers the FP64 evaluation's own error.
+// Returns false when dot(n, d) is not bounded away from zero (grazing).
+GK_D bool plane_interval(f3 o, f3 d, f3 v0, f3 v1, f3 v2, float e_woop, float& tp, float& ep) {
+    const float kU = 5.9604645e-08f;
+    const f3 e1 = v1 - v0, e2 = v2 - v0, w = v0 - o;
+    const float nx = fmaf_(e1.y, e2.z, -(e1.z * e2.y));
+    const float ny = fmaf_(e1.z, e2.x, -(e1.x * e2.z));
+    const float nz = fmaf_(e1.x, e2.y, -(e1.y * e2.x));
+    // |n_i - n_i*| <= 3u (|a b| + |c d|) + u |n_i|, rounded up to 4u and 2u
+    const float enx = fmaf_(4.0f * kU, fabsf(e1.y * e2.z) + fabsf(e1.z * e2.y), (2.0f * kU) * fabsf(nx));
+    const float eny = fmaf_(4.0f * kU, fabsf(e1.z * e2.x) + fabsf(e1.x * e2.z), (2.0f * kU) * fabsf(ny));
+    const float enz = fmaf_(4.0f * kU, fabsf(e1.x * e2.y) + fabsf(e1.y * e2.x), (2.0f * kU) * fabsf(nz));
+    const float num = fmaf_(nz, w.z, fmaf_(ny, w.y, nx * w.x));
+    const float den = fmaf_(nz, d.z, fmaf_(ny, d.y, nx * d.x));
+    const float anx = fabsf(nx), any_ = fabsf(ny), anz = fabsf(nz);
+    const float awx = fabsf(w.x), awy = fabsf(w.y), awz = fabsf(w.z);
+    const float adx = fabsf(d.x), ady = fabsf(d.y), adz = fabsf(d.z);
+    const float enum_ = fmaf_(5.0f * kU, fmaf_(anz, awz, fmaf_(any_, awy, anx * awx)),
+                              fmaf_(enz, awz, fmaf_(eny, awy, enx * awx)));
+    const float eden = fmaf_(4.0f * kU, fmaf_(anz, adz, fmaf_(any_, ady, anx * adx)),
+                             fmaf_(enz, adz, fmaf_(eny, ady, enx * adx)));
+    const float aden = fabsf(den);
+    if (!(aden > 2.0f * eden)) return false;
+    tp = div_(num, den);
+    const float atp = fabsf(tp);
+    ep = fmaf_(1.25f, div_(fmaf_(atp, eden, enum_), aden - eden), fmaf_(4.0f * kU, atp, 3.7252903e-09f * e_woop));
+    return true;
+}
+
 GK_D f3 safe_inv(f3 d) {
     float x = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
     float y = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
@@ -205,140 +248,222 @@ GK_D f3 tri_v(const float4* tris, uint32_t ti, int k, uint32_t* prim = nullptr) 
     return F3(v.x, v.y, v.z);
 }
 
-// MODE kClosest: interval bookkeeping, returns ambiguous on overlapping candidates.
-// MODE kAny:     first valid hit.
-// MODE kExact:   every candidate decided in FP64, key (t, inst, prim).
+// Resumable traversal state of one ray. The stack lives in shared memory (caller-owned,
+// strided); everything else is here, so a ray can be advanced one step at a time and a
+// lane can leave the traversal loop and come back.
+struct Trav {
+    f3 wo, wd;            // world ray
+    f3 o, d, inv;         // ray in the current space (world or instance)
+    Shear sh;
+    float tmax, tcull, best_lo, best_hi;
+    double best_td;
+    uint32_t inst, prim, tri;   // current best
+    uint32_t cur;               // instance being traversed
+    int ref, sp, iter;
+    int mode;                   // kClosest / kAny / kExact
+    bool hit, best_exact, inblas, done, ambiguous;
+};
+
+constexpr float kTmin = 1e-3f;   // EPS, assets/shaders/common/PreProcessor.slang:13
+
+GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int mode) {
+    T.wo = wo; T.wd = wd; T.o = wo; T.d = wd;
+    T.inv = safe_inv(wd);
+    T.sh = make_shear(wd);
+    T.tmax = tmax;
+    T.tcull = tmax * 1.000001f;
+    T.best_lo = 0.0f; T.best_hi = 0.0f; T.best_td = 0.0;
+    T.inst = 0xFFFFFFFFu; T.prim = 0xFFFFFFFFu; T.tri = 0xFFFFFFFFu;
+    T.cur = 0; T.sp = 0; T.iter = 0;
+    T.mode = mode;
+    T.hit = false; T.best_exact = false; T.inblas = false; T.ambiguous = false;
+    T.ref = S.tlas_root;
+    T.done = S.tlas_root < 0;
+}
+
+// FP64 t of the current best candidate: its triangle against its instance's
+// object-space ray (recomputed with the same FP32 operations as during traversal).
+GK_D double exact_t_of(const Trav& T, const SceneView& S) {
+    f3 o = T.o, d = T.d;
+    Shear sh = T.sh;
+    if (!T.inblas || T.inst != T.cur) {
+        const DevInst* ip = S.inst + T.inst;
+        float w[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) w[k] = __ldg(&ip->winv[k]);
+        o = xpoint(w, T.wo);
+        d = xvector(w, T.wd);
+        sh = make_shear(d);
+    }
+    const f3 v0 = tri_v(S.tris, T.tri, 0), v1 = tri_v(S.tris, T.tri, 1), v2 = tri_v(S.tris, T.tri, 2);
+    return exact_test(o, d, sh, v0, v1, v2).t;
+}
+
+// Test the triangles of one leaf against the current best. Returns true when the ray is
+// finished early (any-hit found).
+GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, Counters& cn) {
+    const double tmind = (double)kTmin, tmaxd = (double)T.tmax;
+    for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t ti = first + k;
+        uint32_t prim;
+        const f3 v0 = tri_v(S.tris, ti, 0, &prim), v1 = tri_v(S.tris, ti, 1), v2 = tri_v(S.tris, ti, 2);
+        ++cn.tris;
+        const Fp32Hit f = fp32_test(T.o, T.sh, v0, v1, v2);
+        if (f.kind == 0) continue;
+        if (T.mode == kExact) {
+            const ExactHit x = exact_test(T.o, T.d, T.sh, v0, v1, v2);
+            ++cn.fallbacks;
+            if (!x.hit || !(x.t >= tmind && x.t <= tmaxd)) continue;
+            const bool better = !T.hit || x.t < T.best_td ||
+                                (x.t == T.best_td && (T.cur < T.inst || (T.cur == T.inst && prim < T.prim)));
+            if (better) {
+                T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
+                T.best_td = x.t;
+                T.tcull = (float)x.t * 1.000001f;
+            }
+            continue;
+        }
+        float t, e;
+        double td = 0.0;
+        bool have_td = false;
+        if (f.kind == 1 && plane_interval(T.o, T.d, v0, v1, v2, f.e, t, e)) {
+            // certified interval from the plane equation
+        } else {
+            const ExactHit x = exact_test(T.o, T.d, T.sh, v0, v1, v2);
+            ++cn.fallbacks;
+            if (!x.hit) continue;
+            td = x.t; have_td = true;
+            t = (float)x.t;
+            e = 2.384185791e-07f * fabsf(t);   // 4u |t|
+        }
+        if (t + e < kTmin || t - e > T.tmax) continue;
+        if (t - e < kTmin || t + e > T.tmax) {
+            if (!have_td) {
+                const ExactHit x = exact_test(T.o, T.d, T.sh, v0, v1, v2);
+                ++cn.fallbacks;
+                td = x.t; have_td = true;
+                t = (float)x.t;
+                e = 2.384185791e-07f * fabsf(t);
+            }
+            if (!(td >= tmind && td <= tmaxd)) continue;
+        }
+        if (T.mode == kAny) {
+            T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
+            return true;
+        }
+        const float lo = t - e, hi = t + e;
+        if (T.hit) {
+            if (have_td && T.best_exact) {
+                // both FP64: compare the key (t, instance, primitive) exactly
+                const bool closer = td < T.best_td ||
+                                    (td == T.best_td && (T.cur < T.inst || (T.cur == T.inst && prim < T.prim)));
+                if (!closer) continue;
+            } else {
+                if (lo > T.best_hi) continue;
+                if (!(hi < T.best_lo)) {
+                    // intervals overlap: decide both in FP64 and compare the key exactly
+                    ++cn.retraces;
+                    if (!have_td) {
+                        const ExactHit x = exact_test(T.o, T.d, T.sh, v0, v1, v2);
+                        ++cn.fallbacks;
+                        td = x.t; have_td = true;
+                        t = (float)x.t;
+                        e = 2.384185791e-07f * fabsf(t);
+                    }
+                    if (!T.best_exact) {
+                        T.best_td = exact_t_of(T, S);
+                        T.best_exact = true;
+                        ++cn.fallbacks;
+                    }
+                    const bool closer = td < T.best_td ||
+                                        (td == T.best_td && (T.cur < T.inst || (T.cur == T.inst && prim < T.prim)));
+                    if (!closer) continue;
+                }
+            }
+        }
+        T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
+        T.best_lo = lo; T.best_hi = hi;
+        T.best_exact = have_td;
+        T.best_td = td;
+        T.tcull = hi * 1.000001f;
+    }
+    return false;
+}
+
+// One traversal step: an interior node, a leaf, a stack pop or the return to the instance
+// level. Sets T.done at the end of the ray; an ambiguous fast closest-hit query restarts
+// itself in exact mode.
+GK_D void trav_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn) {
+    if (++T.iter > kIterCap) { atomicOr(S.error, kErrIter); T.done = true; return; }
+    int ref = T.ref;
+    if (ref == kRefPop) {
+        if (T.sp == 0) { T.done = true; return; }
+        --T.sp;
+        T.ref = (int)stk[T.sp * stride];
+        return;
+    }
+    if (ref == kRefMarker) {
+        T.o = T.wo; T.d = T.wd; T.inv = safe_inv(T.wd);
+        T.inblas = false;
+        T.ref = kRefPop;
+        return;
+    }
+    if (ref >= 0) {
+        ++cn.nodes;
+        const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
+        const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+        const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
+        float tn0, tn1;
+        const bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, T.o, T.inv, kTmin, T.tcull, tn0);
+        const bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, T.o, T.inv, kTmin, T.tcull, tn1);
+        if (h0 && h1) {
+            int nearr = nd.x, farr = nd.y;
+            if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
+            if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return; }
+            stk[T.sp * stride] = (uint32_t)farr;
+            ++T.sp;
+            T.ref = nearr;
+        } else if (h0) {
+            T.ref = nd.x;
+        } else if (h1) {
+            T.ref = nd.y;
+        } else {
+            T.ref = kRefPop;
+        }
+        return;
+    }
+    const uint32_t payload = ~(uint32_t)ref;
+    if (!T.inblas) {
+        T.cur = payload >> 3;
+        const DevInst* ip = S.inst + T.cur;
+        float w[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) w[k] = __ldg(&ip->winv[k]);
+        T.o = xpoint(w, T.wo);
+        T.d = xvector(w, T.wd);
+        T.inv = safe_inv(T.d);
+        T.sh = make_shear(T.d);
+        if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return; }
+        stk[T.sp * stride] = (uint32_t)kRefMarker;
+        ++T.sp;
+        T.inblas = true;
+        T.ref = __ldg(&ip->blas_root);
+        return;
+    }
+    T.ref = kRefPop;
+    if (trav_leaf(T, S, payload >> 3, (payload & 7u) + 1u, cn)) T.done = true;
+}
+
+// Whole-ray traversal on top of the stepper.
 template <int MODE>
 GK_D TraceOut traverse(const SceneView& S, f3 wo, f3 wd, float tmin, float tmax, uint32_t* stk, int stride,
                        Counters& cn) {
+    (void)tmin;
+    Trav T;
+    trav_init(T, S, wo, wd, tmax, MODE);
+    while (!T.done) trav_step(T, S, stk, stride, cn);
     TraceOut R;
-    R.hit = false; R.ambiguous = false; R.inst = 0xFFFFFFFFu; R.prim = 0xFFFFFFFFu; R.tri = 0xFFFFFFFFu;
-    if (S.tlas_root < 0) return R;
-    float best_lo = 0.0f, best_hi = 0.0f;
-    double best_td = 0.0;
-    float tcull = tmax * 1.000001f;
-    const double tmind = (double)tmin, tmaxd = (double)tmax;
-    const f3 winv = safe_inv(wd);
-    f3 o = wo, d = wd, inv = winv;
-    Shear sh = make_shear(wd);
-    int level = 0;
-    uint32_t cur = 0;
-    int sp = 0;
-    int ref = S.tlas_root;
-    int iter = 0;
-    for (;;) {
-        if (++iter > kIterCap) { atomicOr(S.error, kErrIter); break; }
-        if (ref == kRefPop) {
-            if (sp == 0) break;
-            --sp;
-            ref = (int)stk[sp * stride];
-            continue;
-        }
-        if (ref == kRefMarker) {
-            o = wo; d = wd; inv = winv; level = 0;
-            ref = kRefPop;
-            continue;
-        }
-        if (ref >= 0) {
-            ++cn.nodes;
-            const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
-            float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
-            int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
-            float tn0, tn1;
-            bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, o, inv, tmin, tcull, tn0);
-            bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, o, inv, tmin, tcull, tn1);
-            if (h0 && h1) {
-                int nearr = nd.x, farr = nd.y;
-                if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
-                if (sp >= kStackSize) { atomicOr(S.error, kErrStack); break; }
-                stk[sp * stride] = (uint32_t)farr;
-                ++sp;
-                ref = nearr;
-            } else if (h0) {
-                ref = nd.x;
-            } else if (h1) {
-                ref = nd.y;
-            } else {
-                ref = kRefPop;
-            }
-            continue;
-        }
-        const uint32_t payload = ~(uint32_t)ref;
-        if (level == 0) {
-            cur = payload >> 3;
-            const DevInst* ip = S.inst + cur;
-            float w[12];
-#pragma unroll
-            for (int k = 0; k < 12; ++k) w[k] = __ldg(&ip->winv[k]);
-            o = xpoint(w, wo);
-            d = xvector(w, wd);
-            inv = safe_inv(d);
-            sh = make_shear(d);
-            if (sp >= kStackSize) { atomicOr(S.error, kErrStack); break; }
-            stk[sp * stride] = (uint32_t)kRefMarker;
-            ++sp;
-            level = 1;
-            ref = __ldg(&ip->blas_root);
-            continue;
-        }
-        const uint32_t first = payload >> 3, cnt = (payload & 7u) + 1u;
-        ref = kRefPop;
-        for (uint32_t k = 0; k < cnt; ++k) {
-            const uint32_t ti = first + k;
-            uint32_t prim;
-            f3 v0 = tri_v(S.tris, ti, 0, &prim), v1 = tri_v(S.tris, ti, 1), v2 = tri_v(S.tris, ti, 2);
-            ++cn.tris;
-            Fp32Hit f = fp32_test(o, sh, v0, v1, v2);
-            if (f.kind == 0) continue;
-            if (MODE == kExact) {
-                ExactHit x = exact_test(o, sh, v0, v1, v2);
-                ++cn.fallbacks;
-                if (!x.hit || !(x.t >= tmind && x.t <= tmaxd)) continue;
-                bool better = !R.hit || x.t < best_td ||
-                              (x.t == best_td && (cur < R.inst || (cur == R.inst && prim < R.prim)));
-                if (better) {
-                    R.hit = true; R.inst = cur; R.prim = prim; R.tri = ti;
-                    best_td = x.t;
-                    tcull = (float)x.t * 1.000001f;
-                }
-                continue;
-            }
-            float t, e;
-            double td = 0.0;
-            bool have_td = false;
-            if (f.kind == 2) {
-                ExactHit x = exact_test(o, sh, v0, v1, v2);
-                ++cn.fallbacks;
-                if (!x.hit) continue;
-                td = x.t; have_td = true;
-                t = (float)x.t;
-                e = 2.384185791e-07f * fabsf(t);   // 4u |t|
-            } else {
-                t = f.t; e = f.e;
-            }
-            if (t + e < tmin || t - e > tmax) continue;
-            if (t - e < tmin || t + e > tmax) {
-                if (!have_td) {
-                    ExactHit x = exact_test(o, sh, v0, v1, v2);
-                    ++cn.fallbacks;
-                    td = x.t;
-                }
-                if (!(td >= tmind && td <= tmaxd)) continue;
-            }
-            if (MODE == kAny) {
-                R.hit = true; R.inst = cur; R.prim = prim; R.tri = ti;
-                return R;
-            }
-            const float lo = t - e, hi = t + e;
-            if (R.hit) {
-                if (lo > best_hi) continue;
-                if (!(hi < best_lo)) { R.ambiguous = true; return R; }
-            }
-            R.hit = true; R.inst = cur; R.prim = prim; R.tri = ti;
-            best_lo = lo; best_hi = hi;
-            tcull = hi * 1.000001f;
-        }
-    }
+    R.hit = T.hit; R.ambiguous = false; R.inst = T.inst; R.prim = T.prim; R.tri = T.tri;
     return R;
 }
 
@@ -355,20 +480,15 @@ GK_D HitShade hit_shade(const SceneView& S, f3 wo, f3 wd, uint32_t inst, uint32_
     Fp32Hit f = fp32_test(o, sh, v0, v1, v2);
     HitShade h;
     if (f.kind == 1) { h.t = f.t; h.b1 = f.b1; h.b2 = f.b2; return h; }
-    ExactHit x = exact_test(o, sh, v0, v1, v2);
+    ExactHit x = exact_test(o, d, sh, v0, v1, v2);
     h.t = (float)x.t; h.b1 = (float)x.b1; h.b2 = (float)x.b2;
     return h;
 }
 
-// Closest hit under the contract: fast pass, exact re-trace when t-ambiguous.
+// Closest hit under the contract.
 GK_D TraceOut trace_closest(const SceneView& S, f3 wo, f3 wd, float tmin, float tmax, uint32_t* stk, int stride,
                             Counters& cn) {
-    TraceOut r = traverse<kClosest>(S, wo, wd, tmin, tmax, stk, stride, cn);
-    if (r.ambiguous) {
-        ++cn.retraces;
-        r = traverse<kExact>(S, wo, wd, tmin, tmax, stk, stride, cn);
-    }
-    return r;
+    return traverse<kClosest>(S, wo, wd, tmin, tmax, stk, stride, cn);
 }
 
 }  // namespace gk

@@ -56,6 +56,8 @@ struct GkrtContext {
 
     unsigned long long* d_counters = nullptr;   // see flush_counters: 5 per-pass slots + total rays
     uint32_t* d_error = nullptr;
+    unsigned int* d_work = nullptr;             // pixel counter of the persistent trace kernel
+    int num_sms = 1;
 };
 
 namespace {
@@ -354,11 +356,14 @@ int gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out) {
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_counters, 8 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_error, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_work, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
     if (e == cudaSuccess) e = cudaMemset(ctx->d_counters, 0, 8 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
     if (e != cudaSuccess) {
         dfree(ctx->d_counters);
         dfree(ctx->d_error);
+        dfree(ctx->d_work);
         delete ctx;
         return e == cudaErrorMemoryAllocation ? GKRT_ERR_OOM : GKRT_ERR_CUDA;
     }
@@ -374,6 +379,7 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     free_scene(ctx);
     dfree(ctx->d_counters);
     dfree(ctx->d_error);
+    dfree(ctx->d_work);
     delete ctx;
     return GKRT_OK;
 }
@@ -505,7 +511,7 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     im.hit_inst = (uint32_t*)ctx->img[GKRT_IMG_HIT_INST];
     im.hit_prim = (uint32_t*)ctx->img[GKRT_IMG_HIT_PRIM];
     GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
-    GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, im, ctx->d_counters, st));
+    GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, im, ctx->d_counters, ctx->d_work, ctx->num_sms, st));
     return GKRT_OK;
 }
 

@@ -44,7 +44,8 @@ void build_bvh_host(const float* boxes, uint32_t n, uint32_t max_leaf, uint32_t 
 }  // namespace gk
 
 cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H,
-                                   const gk::PixelImages& im, unsigned long long* counters, cudaStream_t st);
+                                   const gk::PixelImages& im, unsigned long long* counters, unsigned int* work,
+                                   int num_sms, cudaStream_t st);
 cudaError_t gkrt_launch_trace_rays(const gk::SceneView& S, const GkrtRay* rays, GkrtHit* hits, uint32_t n,
                                    uint32_t mode, unsigned long long* counters, cudaStream_t st);
 cudaError_t gkrt_launch_reproject(const gk::ReprojectArgs& a, cudaStream_t st);

@@ -1,10 +1,25 @@
 // k_pathtrace.cu — the "rt pass" (Core.PathTracing) and ray-query kernels for sm_103a.
+//
+// The rt pass is one persistent kernel: every lane runs the per-pixel logic of
+// FPathTracingRendererV2 (assets/shaders/common/Shading.slang:1084-1241, with the traced
+// camera ray of FHardwarePrimaryRayCaster, :283-334) as a state machine that stops
+// whenever it needs a ray traced. The warp alternates two phases: all lanes advance their
+// rays through the BVH until every ray of the warp is finished, then every lane runs its
+// state machine to its next ray, or takes the next pixel from a global counter
+// (warp-aggregated atomics, 8 x 4 pixel tiles) when its path has ended. A lane whose path
+// ends early thus refills instead of idling until the longest path of its warp is done.
+// (Refilling in the middle of the traversal phase was measured slower: shading is the
+// divergent, expensive part, and is best run for all lanes at once.) Each path keeps its
+// own RNG stream, so results do not depend on the schedule.
 #include "gk_shade.cuh"
 #include "gkrt_internal.h"
 
 namespace gk {
 
-constexpr int kPtBlockX = 16, kPtBlockY = 8, kPtThreads = kPtBlockX * kPtBlockY;
+constexpr int kPtThreads = 128;
+constexpr int kPtMinBlocks = 4;   // resident blocks per SM (128 registers): measured best of 3..6
+constexpr int kRefillBelow = 1;    // shade and refill once every lane of the warp has finished its ray
+constexpr float kCosCone = 0.999990482f;   // cos(0.25 deg), Shading.slang:897
 
 // Warp-aggregated flush: one atomic per counter per warp. Slots 0-4 are per pass
 // (rays, FP64 fallbacks, exact re-traces, node visits, triangle tests); slot 5 counts rays
@@ -23,15 +38,347 @@ __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long 
     }
 }
 
-__global__ void __launch_bounds__(kPtThreads) k_trace_pass(ShadeScene sc, GkrtFrameConstants fc, int W, int H,
-                                                           PixelImages im, unsigned long long* counters) {
+enum Stage : uint32_t { ST_PRIMARY = 0, ST_FIRST = 1, ST_BOUNCE = 2, ST_SUN = 3, ST_DIRECT = 4 };
+
+// Per-thread slots in shared memory (strided by the block size): the primary vertex,
+// the per-pixel loop bounds and the two accumulators. Read at sample boundaries only.
+enum Slot { SL_PX = 0, SL_PY, SL_PZ, SL_NX, SL_NY, SL_NZ, SL_MAT, SL_LOOP, SL_FC, SL_FR = SL_FC + 4, SL_COUNT = SL_FR + 4 };
+
+struct Lane {
+    int pix;          // pixel index, -1 when the lane holds no pixel
+    Rng seed;
+    uint32_t stage;
+    uint32_t i, b;    // sample and bounce indices
+    bool chanceReflect, back, diel, hitReflect, hitMetal;
+    f4 rc;            // throughput of the current sample (RayColor)
+    Vtx vs;           // current path vertex
+    f3 dir;           // current path direction
+};
+
+struct Ctx {
+    const ShadeScene& sc;
+    const GkrtFrameConstants& fc;
+    const PixelImages& im;
+    int W, H;
+    float* ps;        // this thread's first shared slot
+    int stride;
+    Counters& cn;
+    __device__ float& slot(int k) const { return ps[k * stride]; }
+};
+
+__device__ __forceinline__ void emit(Trav& T, const Ctx& c, f3 o, f3 d, int mode) {
+    ++c.cn.rays;
+    trav_init(T, c.sc.S, o, d, 1000.0f, mode);
+}
+
+__device__ __forceinline__ f3 pv_pos(const Ctx& c) { return F3(c.slot(SL_PX), c.slot(SL_PY), c.slot(SL_PZ)); }
+__device__ __forceinline__ f3 pv_nrm(const Ctx& c) { return F3(c.slot(SL_NX), c.slot(SL_NY), c.slot(SL_NZ)); }
+
+// Micro-steps of the per-pixel logic; each piece of code appears once in advance().
+enum Step : uint32_t {
+    K_PRIMARY_DONE, K_BEGIN_SAMPLE, K_PRE_FIRST, K_PRE_BOUNCE, K_FIRST_DONE, K_BOUNCE_DONE, K_SUN_DONE,
+    K_AFTER_SUN, K_END_SAMPLE, K_DIRECT_DONE, K_FINISH
+};
+
+// Run the lane's state machine on the ray that just finished, up to the next ray
+// (returns true) or the end of the pixel (returns false). Follows FPathTracingRendererV2:
+// PrimaryHit (Shading.slang:1186-1223), Render (:1084-1184) with GetRayColor
+// (:1003-1082) split at its trace, the sun test of the bounce loop (:1135-1144), early exit
+// and probe termination (:1146-1154), and DirectIlluminate (:886-908).
+__device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
+    const GkrtFrameConstants& fc = c.fc;
+    const f3 sunDir = F3(fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]);
+    uint32_t k;
+    switch (L.stage) {
+        case ST_PRIMARY: k = K_PRIMARY_DONE; break;
+        case ST_FIRST: k = K_FIRST_DONE; break;
+        case ST_BOUNCE: k = K_BOUNCE_DONE; break;
+        case ST_SUN: k = K_SUN_DONE; break;
+        default: k = K_DIRECT_DONE; break;
+    }
+    float shadow = 0.0f;
+    for (;;) {
+        switch (k) {
+            case K_PRIMARY_DONE: {
+                const int pix = L.pix;
+                const bool want_ids = (fc.flags & GKRT_FRAME_PRIMARY_IDS) != 0u;
+                c.im.single_specular[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (!T.hit) {
+                    const f4 s = sky(fc);
+                    c.im.single_diffuse[pix] = make_float4(s.x, s.y, s.z, s.w);
+                    c.im.motion[pix] = make_float2(0.0f, 0.0f);
+                    c.im.albedo[pix] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+                    c.im.normal[pix] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
+                    c.im.object_id[pix] = 65535u;
+                    c.im.prev_depth[pix] = 100000.0f;
+                    if (want_ids) { c.im.hit_inst[pix] = 0xFFFFFFFFu; c.im.hit_prim[pix] = 0xFFFFFFFFu; }
+                    L.pix = -1;
+                    return false;
+                }
+                Vtx pv = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
+                if (want_ids) { c.im.hit_inst[pix] = T.inst; c.im.hit_prim[pix] = T.prim; }
+                const f4 P4 = F4(pv.P.x, pv.P.y, pv.P.z, 1.0f);
+                const f4 clip = mat4v(fc.view_projection, P4);
+                const f4 ch = mat4v(fc.view_projection_unjit, P4);
+                const float cfx = div_(ch.x, ch.w) * 0.5f, cfy = div_(ch.y, ch.w) * 0.5f;
+                float cp[12];
+#pragma unroll
+                for (int q = 0; q < 12; ++q) cp[q] = __ldg(&c.sc.inst_prev[12u * pv.inst + q]);
+                const f3 prevP = xpoint(cp, pv.P);
+                const f4 ph = mat4v(fc.prev_view_projection_unjit, F4(prevP.x, prevP.y, prevP.z, 1.0f));
+                const float pfx = div_(ph.x, ph.w) * 0.5f, pfy = div_(ph.y, ph.w) * 0.5f;
+                uint32_t mom = c.im.motion_moment[pix];
+                if (len3(pv.P - prevP) > 0.02f) mom = fc.temporal_frames;
+                else mom = mom > 0u ? mom - 1u : 0u;
+                c.im.motion_moment[pix] = mom;
+                const MatV pm = load_mat(c.sc, pv.mat);
+                c.im.albedo[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
+                c.im.normal[pix] = make_float4(pv.N.x, pv.N.y, pv.N.z, pm.fuzz);
+                c.im.object_id[pix] = __ldg(&c.sc.S.inst[pv.inst].instance_id);
+                c.im.motion[pix] = make_float2((pfx - cfx) * (float)c.W, (pfy - cfy) * (float)c.H);
+                c.im.prev_depth[pix] = div_(clip.z, clip.w);
+                if (pm.model != GKRT_MAT_DIELECTRIC) pv.P = fma3(normalize3(T.wd), -0.03f, pv.P);
+                if (pm.model == GKRT_MAT_DIFFUSE_LIGHT) {
+                    c.im.single_diffuse[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
+                    L.pix = -1;
+                    return false;
+                }
+                const bool pdiel = pm.model == GKRT_MAT_DIELECTRIC;
+                int samples = (int)fc.number_of_samples * (mom > 0u ? 4 : 1);
+                if (samples < 1) samples = 1;
+                if (samples > 0xFFFF) samples = 0xFFFF;
+                uint32_t maxB = pdiel ? fc.max_number_of_bounces : fc.number_of_bounces;
+                if (maxB > 0x7FFFu) maxB = 0x7FFFu;
+                c.slot(SL_PX) = pv.P.x; c.slot(SL_PY) = pv.P.y; c.slot(SL_PZ) = pv.P.z;
+                c.slot(SL_NX) = pv.N.x; c.slot(SL_NY) = pv.N.y; c.slot(SL_NZ) = pv.N.z;
+                c.slot(SL_MAT) = __uint_as_float(pv.mat);
+                c.slot(SL_LOOP) = __uint_as_float((uint32_t)samples | (maxB << 16) | (pdiel ? 0x80000000u : 0u));
+#pragma unroll
+                for (int q = 0; q < 4; ++q) { c.slot(SL_FC + q) = 0.0f; c.slot(SL_FR + q) = 0.0f; }
+                L.i = 0;
+                k = K_BEGIN_SAMPLE;
+                break;
+            }
+            case K_BEGIN_SAMPLE: {
+                const f4 eye = mat4v(fc.model_view_inverse, F4(0.0f, 0.0f, 0.0f, 1.0f));
+                L.rc = F4(1.0f, 1.0f, 1.0f, 1.0f);
+                L.vs.P = pv_pos(c);
+                L.vs.N = pv_nrm(c);
+                L.vs.mat = __float_as_uint(c.slot(SL_MAT));
+                L.dir = normalize3(L.vs.P - xyz(eye));
+                L.hitReflect = false;
+                L.hitMetal = false;
+                k = K_PRE_FIRST;
+                break;
+            }
+            case K_PRE_FIRST:
+            case K_PRE_BOUNCE: {
+                // GetRayColor up to the trace (Shading.slang:1007-1039)
+                const bool first = k == K_PRE_FIRST;
+                const MatV mat = load_mat(c.sc, L.vs.mat);
+                const bool diel = mat.model == GKRT_MAT_DIELECTRIC;
+                const float startPosOffset = diel ? 0.0f : 1.0f;
+                const float dotValue = dot3(L.dir, L.vs.N);
+                const bool back = dotValue > 0.0f;
+                const f3 outward = back ? -L.vs.N : L.vs.N;
+                const float niOverNt = back ? mat.ri2 : div_(1.0f, mat.ri2);
+                const float cosine = dotValue > 0.0f ? mat.ri * dotValue : -dotValue;
+                const float reflectProb = schlick(cosine, mat.ri);
+                const bool chanceReflect = rnd1(L.seed) < reflectProb;
+                const bool chanceMetal = rnd1(L.seed) < mat.metal;
+                const bool chanceGGX = chanceReflect || chanceMetal;
+                f3 tdir;
+                if (chanceGGX) tdir = ggx_sample(L.seed, sqrt_(mat.fuzz), reflect3(L.dir, outward));
+                else tdir = align_normal(hemisphere_cos(L.seed), outward);
+                if (first) { L.hitReflect = chanceGGX; L.hitMetal = chanceMetal; }
+                if (diel && !chanceReflect) tdir = refract3(L.dir, outward, niOverNt);
+                L.dir = tdir;
+                L.chanceReflect = chanceReflect;
+                L.back = back;
+                L.diel = diel;
+                L.stage = first ? ST_FIRST : ST_BOUNCE;
+                emit(T, c, fma3(L.vs.N, 0.001f * startPosOffset, L.vs.P), tdir, kClosest);
+                return true;
+            }
+            case K_FIRST_DONE:
+            case K_BOUNCE_DONE: {
+                // GetRayColor after the trace (Shading.slang:1039-1081)
+                bool term;
+                if (T.hit) {
+                    L.vs = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
+                    const MatV hm = load_mat(c.sc, L.vs.mat);
+                    if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !L.chanceReflect) L.rc = L.rc * hm.diffuse;
+                    if (L.back && !L.diel) { L.rc = F4(0.5f, 0.5f, 0.5f, 0.0f); term = true; }
+                    else term = hm.model == GKRT_MAT_DIFFUSE_LIGHT;
+                } else {
+                    L.rc = L.rc * sky(fc);
+                    term = true;
+                }
+                if (term) { k = K_END_SAMPLE; break; }
+                const uint32_t loop = __float_as_uint(c.slot(SL_LOOP));
+                if (k == K_FIRST_DONE) {
+                    const uint32_t maxB = (loop >> 16) & 0x7FFFu;
+                    const bool pdiel = (loop >> 31) != 0u;
+                    if (fc.fast_gather && !pdiel) {
+                        L.rc = L.rc * probe_term(c.sc, L.vs.P, L.vs.N);
+                        k = K_END_SAMPLE;
+                        break;
+                    }
+                    L.b = 1;
+                    k = L.b < maxB ? K_PRE_BOUNCE : K_END_SAMPLE;
+                    break;
+                }
+                if (fc.has_sun && rnd1(L.seed) < 0.5f) {
+                    const f3 cd = align_normal(cone(L.seed, kCosCone), sunDir);
+                    L.stage = ST_SUN;
+                    emit(T, c, L.vs.P, cd, kAny);
+                    return true;
+                }
+                k = K_AFTER_SUN;
+                break;
+            }
+            case K_SUN_DONE: {
+                if (!T.hit) {
+                    L.rc = L.rc * F4(fc.sun_color[0], fc.sun_color[1], fc.sun_color[2], fc.sun_color[3]);
+                    k = K_END_SAMPLE;
+                } else {
+                    k = K_AFTER_SUN;
+                }
+                break;
+            }
+            case K_AFTER_SUN: {
+                const uint32_t loop = __float_as_uint(c.slot(SL_LOOP));
+                const uint32_t maxB = (loop >> 16) & 0x7FFFu;
+                const bool pdiel = (loop >> 31) != 0u;
+                const bool early = !pdiel && rnd1(L.seed) < 0.5f;
+                if (L.b == maxB - 1u || early) {
+                    L.rc = L.rc * probe_term(c.sc, L.vs.P, L.vs.N);
+                    k = K_END_SAMPLE;
+                } else {
+                    ++L.b;
+                    k = K_PRE_BOUNCE;
+                }
+                break;
+            }
+            case K_END_SAMPLE: {
+                // end of a sample (Shading.slang:1159-1172)
+                if (L.hitMetal) L.rc = L.rc * load_mat(c.sc, __float_as_uint(c.slot(SL_MAT))).diffuse;
+                const int acc = L.hitReflect ? SL_FR : SL_FC;
+                c.slot(acc) = c.slot(acc) + L.rc.x;
+                c.slot(acc + 1) = c.slot(acc + 1) + L.rc.y;
+                c.slot(acc + 2) = c.slot(acc + 2) + L.rc.z;
+                c.slot(acc + 3) = c.slot(acc + 3) + L.rc.w;
+                const uint32_t samples = __float_as_uint(c.slot(SL_LOOP)) & 0xFFFFu;
+                if (++L.i < samples) { k = K_BEGIN_SAMPLE; break; }
+                const float fs = (float)samples;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    c.slot(SL_FC + q) = div_(c.slot(SL_FC + q), fs);
+                    c.slot(SL_FR + q) = div_(c.slot(SL_FR + q), fs);
+                }
+                if (fc.has_sun) {
+                    const f3 cd = align_normal(cone(L.seed, kCosCone), sunDir);
+                    L.stage = ST_DIRECT;
+                    emit(T, c, pv_pos(c), cd, kAny);
+                    return true;
+                }
+                shadow = 0.0f;
+                k = K_FINISH;
+                break;
+            }
+            case K_DIRECT_DONE: {
+                shadow = T.hit ? 0.0f : 1.0f;
+                k = K_FINISH;
+                break;
+            }
+            default: {   // K_FINISH: DirectIlluminate's contribution and the two outputs
+                const float dd = mx(dot3(sunDir, normalize3(pv_nrm(c))), 0.0f) * 0.318309886183790671538f;
+                f4 fcol = F4(c.slot(SL_FC), c.slot(SL_FC + 1), c.slot(SL_FC + 2), c.slot(SL_FC + 3));
+                const f4 frefl = F4(c.slot(SL_FR), c.slot(SL_FR + 1), c.slot(SL_FR + 2), c.slot(SL_FR + 3));
+                fcol = fcol + F4((fc.sun_color[0] * dd) * shadow, (fc.sun_color[1] * dd) * shadow,
+                                 (fc.sun_color[2] * dd) * shadow, (fc.sun_color[3] * dd) * shadow);
+                c.im.single_diffuse[L.pix] = make_float4(fcol.x, fcol.y, fcol.z, fcol.w);
+                c.im.single_specular[L.pix] = make_float4(frefl.x, frefl.y, frefl.z, frefl.w);
+                L.pix = -1;
+                return false;
+            }
+        }
+    }
+}
+
+// Camera ray of FHardwarePrimaryRayCaster (Shading.slang:286-304) for pixel index pix.
+__device__ void start_pixel(Lane& L, Trav& T, const Ctx& c, int x, int y) {
+    const GkrtFrameConstants& fc = c.fc;
+    L.pix = y * c.W + x;
+    L.seed.v[0] = (uint32_t)x; L.seed.v[1] = (uint32_t)y; L.seed.v[2] = fc.total_frames; L.seed.v[3] = 0u;
+    float uvx = fmaf_(div_((float)x, (float)c.W), 2.0f, -1.0f);
+    float uvy = fmaf_(div_((float)y, (float)c.H), 2.0f, -1.0f);
+    if (fc.taa) {
+        const uint32_t hi = fc.total_frames % 8u;
+        uvx = uvx + div_(c_halton[2 * hi] - 0.5f, (float)c.W);
+        uvy = uvy + div_(c_halton[2 * hi + 1] - 0.5f, (float)c.H);
+    }
+    const f2 disk = unit_disk(L.seed);
+    const float ha = div_(fc.aperture, 2.0f);
+    const float offx = ha * disk.x, offy = ha * disk.y;
+    const f4 origin = mat4v(fc.model_view_inverse, F4(offx, offy, 0.0f, 1.0f));
+    const f4 target = mat4v(fc.projection_inverse, F4(uvx, uvy, 1.0f, 1.0f));
+    const f3 tn = normalize3(F3(fmaf_(target.x, fc.focus_distance, -offx), fmaf_(target.y, fc.focus_distance, -offy),
+                                target.z * fc.focus_distance));
+    const f4 direction = mat4v(fc.model_view_inverse, F4(tn.x, tn.y, tn.z, 0.0f));
+    L.stage = ST_PRIMARY;
+    emit(T, c, xyz(origin), xyz(direction), kClosest);
+}
+
+__global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeScene sc, GkrtFrameConstants fc, int W, int H,
+                                                           PixelImages im, unsigned long long* counters,
+                                                           unsigned int* work) {
     __shared__ uint32_t stack[kStackSize * kPtThreads];
+    __shared__ float pslots[SL_COUNT * kPtThreads];
     const int tid = threadIdx.x;
-    const int x = blockIdx.x * kPtBlockX + (tid % kPtBlockX);
-    const int y = blockIdx.y * kPtBlockY + (tid / kPtBlockX);
+    const unsigned lane = tid & 31u;
     Counters cn;
     cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0;
-    if (x < W && y < H) shade_pixel(sc, fc, W, H, x, y, im, stack + tid, kPtThreads, cn);
+    const Ctx c{sc, fc, im, W, H, pslots + tid, kPtThreads, cn};
+    const int tiles_x = (W + 7) / 8, tiles_y = (H + 3) / 4;
+    const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
+    Lane L;
+    L.pix = -1;
+    L.stage = ST_PRIMARY;
+    Trav T;
+    T.done = true;
+    bool tracing = false, exhausted = false;
+    for (;;) {
+        if (!tracing) {
+            if (L.pix >= 0) tracing = advance(L, T, c);
+            while (!tracing && !exhausted) {
+                // next pixel: warp-aggregated fetch over 8 x 4 tiles
+                const unsigned m = __activemask();
+                const int leader = __ffs(m) - 1;
+                const unsigned rank = __popc(m & ((1u << lane) - 1u));
+                unsigned base = 0;
+                if ((int)lane == leader) base = atomicAdd(work, (unsigned)__popc(m));
+                base = __shfl_sync(m, base, leader);
+                const unsigned k = base + rank;
+                if (k >= total) { exhausted = true; break; }
+                const unsigned tile = k >> 5, in = k & 31u;
+                const int x = (int)((tile % (unsigned)tiles_x) * 8u + (in & 7u));
+                const int y = (int)((tile / (unsigned)tiles_x) * 4u + (in >> 3));
+                if (x >= W || y >= H) continue;
+                start_pixel(L, T, c, x, y);
+                tracing = true;
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, tracing) == 0u) break;
+        // advance all tracing lanes until enough of them are done to be worth a refill
+        for (;;) {
+            if (tracing) {
+                if (!T.done) trav_step(T, sc.S, stack + tid, kPtThreads, cn);
+                if (T.done) tracing = false;
+            }
+            if (__popc(__ballot_sync(0xFFFFFFFFu, tracing)) < kRefillBelow) break;
+        }
+    }
     flush_counters(cn, counters);
 }
 
@@ -51,18 +398,14 @@ __global__ void __launch_bounds__(kRqThreads) k_trace_rays(SceneView S, const Gk
         h.t = -1.0f; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = 0xFFFFFFFFu; h.prim = 0xFFFFFFFFu;
         h.pad[0] = h.pad[1] = h.pad[2] = 0u;
         cn.rays = 1;
-        if (mode == GKRT_TRACE_ANY) {
-            TraceOut t = traverse<kAny>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn);
-            if (t.hit) {
-                HitShade s = hit_shade(S, o, d, t.inst, t.tri);
-                h.t = s.t; h.inst = t.inst; h.prim = t.prim;
-            }
-        } else {
-            TraceOut t = trace_closest(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn);
-            if (t.hit) {
-                HitShade s = hit_shade(S, o, d, t.inst, t.tri);
-                h.t = s.t; h.b1 = s.b1; h.b2 = s.b2; h.inst = t.inst; h.prim = t.prim;
-            }
+        // tmin of the query is fixed at EPS like the reference's TraceRay/TraceOcclusion
+        const TraceOut t = mode == GKRT_TRACE_ANY
+                               ? traverse<kAny>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn)
+                               : traverse<kClosest>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn);
+        if (t.hit) {
+            const HitShade s = hit_shade(S, o, d, t.inst, t.tri);
+            h.t = s.t; h.inst = t.inst; h.prim = t.prim;
+            if (mode != GKRT_TRACE_ANY) { h.b1 = s.b1; h.b2 = s.b2; }
         }
         hits[i] = h;
     }
@@ -74,9 +417,19 @@ __global__ void __launch_bounds__(kRqThreads) k_trace_rays(SceneView S, const Gk
 using namespace gk;
 
 cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H,
-                                   const PixelImages& im, unsigned long long* counters, cudaStream_t st) {
-    dim3 grid((W + kPtBlockX - 1) / kPtBlockX, (H + kPtBlockY - 1) / kPtBlockY);
-    k_trace_pass<<<grid, kPtThreads, 0, st>>>(sc, fc, W, H, im, counters);
+                                   const PixelImages& im, unsigned long long* counters, unsigned int* work,
+                                   int num_sms, cudaStream_t st) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pass, kPtThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const int pixels = W * H;
+    int blocks = num_sms * per_sm;
+    const int need = (pixels + kPtThreads - 1) / kPtThreads;
+    if (blocks > need) blocks = need;
+    e = cudaMemsetAsync(work, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    k_trace_pass<<<blocks, kPtThreads, 0, st>>>(sc, fc, W, H, im, counters, work);
     return cudaGetLastError();
 }
 

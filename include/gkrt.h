@@ -235,7 +235,7 @@ typedef struct GkrtDeviceDesc {
 typedef struct GkrtStats {
     uint64_t rays_traced;       /* camera + bounce + shadow rays of the last trace pass   */
     uint64_t exact_fallbacks;   /* triangle tests decided in FP64, last pass              */
-    uint64_t exact_retraces;    /* rays re-traversed in exact mode (t-ambiguous)          */
+    uint64_t exact_retraces;    /* t-ambiguous candidate pairs resolved in FP64           */
     uint64_t node_visits;       /* BVH nodes visited, last pass                           */
     uint64_t triangle_tests;    /* ray/triangle tests, last pass                          */
     uint64_t rays_total;        /* rays traced since the context was created              */

@@ -1058,10 +1058,15 @@ int gko_exact_tri(const float o[3], const float d[3], const float v[9], double o
     out[0] = x.t; out[1] = x.b1; out[2] = x.b2;
     return x.hit ? 1 : 0;
 }
-int gko_fp32_tri(const float o[3], const float d[3], const float v[9], float out[4]) {
+// out: t, e (sheared bound), b1, b2, plane t, plane e, plane ok
+int gko_fp32_tri(const float o[3], const float d[3], const float v[9], float out[7]) {
     RayShear sh = make_shear(f3{d[0], d[1], d[2]});
-    Fp32Result r = fp32_test(f3{o[0], o[1], o[2]}, sh, f3{v[0], v[1], v[2]}, f3{v[3], v[4], v[5]}, f3{v[6], v[7], v[8]});
+    f3 O{o[0], o[1], o[2]}, D{d[0], d[1], d[2]}, V0{v[0], v[1], v[2]}, V1{v[3], v[4], v[5]}, V2{v[6], v[7], v[8]};
+    Fp32Result r = fp32_test(O, sh, V0, V1, V2);
     out[0] = r.t; out[1] = r.e; out[2] = r.b1; out[3] = r.b2;
+    float tp = 0.0f, ep = 0.0f;
+    bool ok = r.kind == 1 && plane_interval(O, D, V0, V1, V2, r.e, &tp, &ep);
+    out[4] = tp; out[5] = ep; out[6] = ok ? 1.0f : 0.0f;
     return r.kind;
 }
 

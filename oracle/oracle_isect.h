@@ -143,6 +143,33 @@ static inline Fp32Result fp32_test(f3 o, const RayShear& s, f3 v0, f3 v1, f3 v2)
     return r;
 }
 
+// Certified interval for the exact hit distance from the plane equation
+// t = dot(n, v0 - o) / dot(n, d), n = (v1 - v0) x (v2 - v0); false when dot(n, d) is not
+// bounded away from zero. e_woop (the sheared FP32 bound) scaled by 2^-28 covers the
+// FP64 evaluation's own rounding.
+static inline bool plane_interval(f3 o, f3 d, f3 v0, f3 v1, f3 v2, float e_woop, float* tp, float* ep) {
+    f3 e1 = sub(v1, v0), e2 = sub(v2, v0), w = sub(v0, o);
+    float nx = fma_(e1.y, e2.z, -(e1.z * e2.y));
+    float ny = fma_(e1.z, e2.x, -(e1.x * e2.z));
+    float nz = fma_(e1.x, e2.y, -(e1.y * e2.x));
+    float enx = fma_(4.0f * kU, std::fabs(e1.y * e2.z) + std::fabs(e1.z * e2.y), (2.0f * kU) * std::fabs(nx));
+    float eny = fma_(4.0f * kU, std::fabs(e1.z * e2.x) + std::fabs(e1.x * e2.z), (2.0f * kU) * std::fabs(ny));
+    float enz = fma_(4.0f * kU, std::fabs(e1.x * e2.y) + std::fabs(e1.y * e2.x), (2.0f * kU) * std::fabs(nz));
+    float num = fma_(nz, w.z, fma_(ny, w.y, nx * w.x));
+    float den = fma_(nz, d.z, fma_(ny, d.y, nx * d.x));
+    float anx = std::fabs(nx), any_ = std::fabs(ny), anz = std::fabs(nz);
+    float awx = std::fabs(w.x), awy = std::fabs(w.y), awz = std::fabs(w.z);
+    float adx = std::fabs(d.x), ady = std::fabs(d.y), adz = std::fabs(d.z);
+    float enum_ = fma_(5.0f * kU, fma_(anz, awz, fma_(any_, awy, anx * awx)), fma_(enz, awz, fma_(eny, awy, enx * awx)));
+    float eden = fma_(4.0f * kU, fma_(anz, adz, fma_(any_, ady, anx * adx)), fma_(enz, adz, fma_(eny, ady, enx * adx)));
+    float aden = std::fabs(den);
+    if (!(aden > 2.0f * eden)) return false;
+    *tp = num / den;
+    float atp = std::fabs(*tp);
+    *ep = fma_(1.25f, fma_(atp, eden, enum_) / (aden - eden), fma_(4.0f * kU, atp, 3.7252903e-09f * e_woop));
+    return true;
+}
+
 // Shading values of a triangle known (by the FP64 definition) to be the closest hit:
 // float t and barycentrics from the FP32 path when it is certain, else from FP64.
 struct HybridHit { float t, b1, b2; bool used_fp64; };

@@ -211,7 +211,8 @@ def test_bricks_full_size_properties(bricks_env):
     hit = ids != 0xFFFFFFFF
     assert (ids[hit] < sc.instances.shape[0]).all()
     assert s1.rays_traced >= W * H
-    assert s1.exact_fallbacks < 0.01 * s1.rays_traced
+    assert s1.exact_fallbacks < 0.05 * s1.triangle_tests
+    assert s1.exact_retraces < 0.01 * s1.rays_traced   # t-ambiguous pairs decided in FP64
     assert s1.device_error == 0
     # a sampled band of rows against the oracle
     oim = O.new_images(W, H)

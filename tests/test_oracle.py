@@ -61,7 +61,7 @@ def test_fp32_bounds_are_conservative():
         if i % 3 == 0:   # rays through vertices and edges
             d = (tris[i][i % 3] + (tris[i][(i + 1) % 3] - tris[i][i % 3]) * rng.random() - o).astype(np.float32)
         ex = np.zeros(3)
-        f = np.zeros(4, np.float32)
+        f = np.zeros(7, np.float32)
         hit = L.gko_exact_tri(o.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p),
                               v.ctypes.data_as(C.c_void_p), ex.ctypes.data_as(C.c_void_p))
         kind = L.gko_fp32_tri(o.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p),
@@ -72,6 +72,8 @@ def test_fp32_bounds_are_conservative():
         elif kind == 1:
             assert hit == 1
             assert abs(ex[0] - f[0]) <= f[1]
+            if f[6]:
+                assert abs(ex[0] - f[4]) <= f[5]
             certain += 1
         else:
             undecided += 1
@@ -224,7 +226,7 @@ def test_fp32_bounds_far_small_triangles():
         d = (tgt - o).astype(np.float32)
         v = np.ascontiguousarray(tri.reshape(-1))
         ex = np.zeros(3)
-        f = np.zeros(4, np.float32)
+        f = np.zeros(7, np.float32)
         hit = L.gko_exact_tri(o.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p),
                               v.ctypes.data_as(C.c_void_p), ex.ctypes.data_as(C.c_void_p))
         kind = L.gko_fp32_tri(o.ctypes.data_as(C.c_void_p), d.ctypes.data_as(C.c_void_p),
@@ -233,5 +235,8 @@ def test_fp32_bounds_far_small_triangles():
             assert hit == 0
         elif kind == 1:
             assert hit == 1 and abs(ex[0] - f[0]) <= f[1]
+            assert f[6] and abs(ex[0] - f[4]) <= f[5]
+            # the plane interval is far tighter than the sheared one
+            assert f[5] <= f[1]
         certain += kind != 2
     assert certain > 0.95 * n
