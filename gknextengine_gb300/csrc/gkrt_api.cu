@@ -336,6 +336,17 @@ int check_frame(GkrtContext* ctx, const GkrtFrameConstants* fc) {
 
 }  // namespace
 
+int gkrt_internal_fail(GkrtContext* ctx, int code, const std::string& msg) { return fail(ctx, code, msg); }
+
+int gkrt_internal_ready_view(GkrtContext* ctx, SceneView* view, unsigned long long** counters, int* device) {
+    if (!ctx->has_scene || !ctx->blas_ready || !ctx->tlas_ready)
+        return fail(ctx, GKRT_ERR_STATE, "scene and BVH must be built before this call (it allocates nothing)");
+    *view = scene_view(ctx);
+    *counters = ctx->d_counters;
+    *device = ctx->device;
+    return GKRT_OK;
+}
+
 extern "C" {
 
 int gkrt_abi_version(void) { return GKRT_ABI_VERSION; }

@@ -48,5 +48,12 @@ cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameCons
                                    int num_sms, cudaStream_t st);
 cudaError_t gkrt_launch_trace_rays(const gk::SceneView& S, const GkrtRay* rays, GkrtHit* hits, uint32_t n,
                                    uint32_t mode, unsigned long long* counters, cudaStream_t st);
+// Internal helpers for entry points defined outside gkrt_api.cu.
+#include <string>
+int gkrt_internal_fail(GkrtContext* ctx, int code, const std::string& msg);
+// Scene view, statistics counters and device of a context whose scene and BVH are already
+// built; GKRT_ERR_STATE otherwise (nothing is built or allocated here).
+int gkrt_internal_ready_view(GkrtContext* ctx, gk::SceneView* view, unsigned long long** counters, int* device);
+
 cudaError_t gkrt_launch_reproject(const gk::ReprojectArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_compose(const gk::ComposeArgs& a, cudaStream_t st);

@@ -48,6 +48,7 @@ def load(path: str | None = None):
     L.gkrt_copy_image_to_host.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
     L.gkrt_upload_image.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
     L.gkrt_trace_rays.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
+    L.gkrt_trace_rays_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
     L.gkrt_synchronize.argtypes = [vp, vp]
     L.gkrt_affine_inverse.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -62,6 +63,7 @@ EXPORTED = [
     "gkrt_context_create", "gkrt_context_destroy", "gkrt_last_error_message", "gkrt_abi_version",
     "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_build_bvh",
     "gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_end_frame", "gkrt_render_frame",
-    "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_get_stats",
+    "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
+    "gkrt_get_stats",
     "gkrt_synchronize", "gkrt_affine_inverse",
 ]

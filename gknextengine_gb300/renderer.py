@@ -133,6 +133,12 @@ class PathTracingRenderer:
         self._check(self._lib.gkrt_trace_rays(self._h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr), count, mode,
                                               self._stream(stream)))
 
+    def trace_rays_noalloc_device(self, rays_ptr: int, hits_ptr: int, count: int, mode=abi.TRACE_CLOSEST,
+                                  stream=None):
+        """Ray queries that allocate no device memory (static scratch; see gkrt.h)."""
+        self._check(self._lib.gkrt_trace_rays_noalloc(self._h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr), count,
+                                                      mode, self._stream(stream)))
+
     def stats(self) -> abi.GkrtStats:
         s = abi.GkrtStats()
         self._check(self._lib.gkrt_get_stats(self._h, C.byref(s)))

@@ -290,6 +290,19 @@ int  gkrt_upload_image(GkrtContext* ctx, int image_id, const void* src, size_t s
 int  gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32_t count,
                      uint32_t mode, void* stream);
 
+/* The same ray queries for callers that cannot allocate device memory while they issue work
+ * (a host engine whose device memory belongs to its own pool allocator, a process at its
+ * memory budget, or code running inside CUDA stream capture, where allocation is not
+ * allowed). No counterpart in the reference. The call allocates nothing: it needs a context
+ * whose scene and BVH are already built (else GKRT_ERR_STATE), and its scratch memory is a
+ * fixed 2 MiB static device array that every GPU loading the library keeps until process
+ * exit. At most 4,194,304 rays per call (GKRT_ERR_INVALID_ARG above that). The first call on
+ * a device looks up the array's device address; make that first call before any stream
+ * capture. Calls share the array: calls that overlap on the GPU race, so order them on one
+ * stream. Statistics land in the context's counters as for gkrt_trace_rays. */
+int  gkrt_trace_rays_noalloc(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32_t count,
+                             uint32_t mode, void* stream);
+
 int  gkrt_get_stats(GkrtContext* ctx, GkrtStats* out);
 int  gkrt_synchronize(GkrtContext* ctx, void* stream);
 
