@@ -294,9 +294,13 @@ def main():
     ap.add_argument("--impl", default="gkrt", choices=["gkrt", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--size", default=None, help="WxH override for profiling small cases (default 1920x1080)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.size:
+        global W_, H_
+        W_, H_ = (int(v) for v in args.size.lower().split("x"))
     if args.impl == "reference":
         return run_reference(args)
     return run_gkrt(args)

@@ -74,75 +74,67 @@ __device__ __forceinline__ void emit(Trav& T, const Ctx& c, f3 o, f3 d, int mode
 __device__ __forceinline__ f3 pv_pos(const Ctx& c) { return F3(c.slot(SL_PX), c.slot(SL_PY), c.slot(SL_PZ)); }
 __device__ __forceinline__ f3 pv_nrm(const Ctx& c) { return F3(c.slot(SL_NX), c.slot(SL_NY), c.slot(SL_NZ)); }
 
-// Micro-steps of the per-pixel logic; each piece of code appears once in advance().
-enum Step : uint32_t {
-    K_PRIMARY_DONE, K_BEGIN_SAMPLE, K_PRE_FIRST, K_PRE_BOUNCE, K_FIRST_DONE, K_BOUNCE_DONE, K_SUN_DONE,
-    K_AFTER_SUN, K_END_SAMPLE, K_DIRECT_DONE, K_FINISH
-};
-
 // Run the lane's state machine on the ray that just finished, up to the next ray
 // (returns true) or the end of the pixel (returns false). Follows FPathTracingRendererV2:
 // PrimaryHit (Shading.slang:1186-1223), Render (:1084-1184) with GetRayColor
 // (:1003-1082) split at its trace, the sun test of the bounce loop (:1135-1144), early exit
 // and probe termination (:1146-1154), and DirectIlluminate (:886-908).
+//
+// The logic is laid out as guarded sections in one fixed order; every lane passes each
+// section at most once per call, so lanes in different states re-converge after each
+// section and the expensive ones (the sampling before a trace, the hit reconstruction
+// after it) run once per warp for all the lanes that need them.
 __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
     const GkrtFrameConstants& fc = c.fc;
     const f3 sunDir = F3(fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]);
-    uint32_t k;
-    switch (L.stage) {
-        case ST_PRIMARY: k = K_PRIMARY_DONE; break;
-        case ST_FIRST: k = K_FIRST_DONE; break;
-        case ST_BOUNCE: k = K_BOUNCE_DONE; break;
-        case ST_SUN: k = K_SUN_DONE; break;
-        default: k = K_DIRECT_DONE; break;
-    }
+    const uint32_t stage = L.stage;
+    bool emitted = false, need_begin = false, need_pre = false, pre_first = false;
+    bool need_end = false, need_after_sun = false, need_finish = false;
     float shadow = 0.0f;
-    for (;;) {
-        switch (k) {
-            case K_PRIMARY_DONE: {
-                const int pix = L.pix;
-                const bool want_ids = (fc.flags & GKRT_FRAME_PRIMARY_IDS) != 0u;
-                c.im.single_specular[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                if (!T.hit) {
-                    const f4 s = sky(fc);
-                    c.im.single_diffuse[pix] = make_float4(s.x, s.y, s.z, s.w);
-                    c.im.motion[pix] = make_float2(0.0f, 0.0f);
-                    c.im.albedo[pix] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-                    c.im.normal[pix] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
-                    c.im.object_id[pix] = 65535u;
-                    c.im.prev_depth[pix] = 100000.0f;
-                    if (want_ids) { c.im.hit_inst[pix] = 0xFFFFFFFFu; c.im.hit_prim[pix] = 0xFFFFFFFFu; }
-                    L.pix = -1;
-                    return false;
-                }
-                Vtx pv = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
-                if (want_ids) { c.im.hit_inst[pix] = T.inst; c.im.hit_prim[pix] = T.prim; }
-                const f4 P4 = F4(pv.P.x, pv.P.y, pv.P.z, 1.0f);
-                const f4 clip = mat4v(fc.view_projection, P4);
-                const f4 ch = mat4v(fc.view_projection_unjit, P4);
-                const float cfx = div_(ch.x, ch.w) * 0.5f, cfy = div_(ch.y, ch.w) * 0.5f;
-                float cp[12];
+
+    // 1. the camera ray's hit: G-buffer outputs, motion, sample set-up
+    if (stage == ST_PRIMARY) {
+        const int pix = L.pix;
+        const bool want_ids = (fc.flags & GKRT_FRAME_PRIMARY_IDS) != 0u;
+        c.im.single_specular[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!T.hit) {
+            const f4 s = sky(fc);
+            c.im.single_diffuse[pix] = make_float4(s.x, s.y, s.z, s.w);
+            c.im.motion[pix] = make_float2(0.0f, 0.0f);
+            c.im.albedo[pix] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+            c.im.normal[pix] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
+            c.im.object_id[pix] = 65535u;
+            c.im.prev_depth[pix] = 100000.0f;
+            if (want_ids) { c.im.hit_inst[pix] = 0xFFFFFFFFu; c.im.hit_prim[pix] = 0xFFFFFFFFu; }
+            L.pix = -1;
+        } else {
+            Vtx pv = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
+            if (want_ids) { c.im.hit_inst[pix] = T.inst; c.im.hit_prim[pix] = T.prim; }
+            const f4 P4 = F4(pv.P.x, pv.P.y, pv.P.z, 1.0f);
+            const f4 clip = mat4v(fc.view_projection, P4);
+            const f4 ch = mat4v(fc.view_projection_unjit, P4);
+            const float cfx = div_(ch.x, ch.w) * 0.5f, cfy = div_(ch.y, ch.w) * 0.5f;
+            float cp[12];
 #pragma unroll
-                for (int q = 0; q < 12; ++q) cp[q] = __ldg(&c.sc.inst_prev[12u * pv.inst + q]);
-                const f3 prevP = xpoint(cp, pv.P);
-                const f4 ph = mat4v(fc.prev_view_projection_unjit, F4(prevP.x, prevP.y, prevP.z, 1.0f));
-                const float pfx = div_(ph.x, ph.w) * 0.5f, pfy = div_(ph.y, ph.w) * 0.5f;
-                uint32_t mom = c.im.motion_moment[pix];
-                if (len3(pv.P - prevP) > 0.02f) mom = fc.temporal_frames;
-                else mom = mom > 0u ? mom - 1u : 0u;
-                c.im.motion_moment[pix] = mom;
-                const MatV pm = load_mat(c.sc, pv.mat);
-                c.im.albedo[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
-                c.im.normal[pix] = make_float4(pv.N.x, pv.N.y, pv.N.z, pm.fuzz);
-                c.im.object_id[pix] = __ldg(&c.sc.S.inst[pv.inst].instance_id);
-                c.im.motion[pix] = make_float2((pfx - cfx) * (float)c.W, (pfy - cfy) * (float)c.H);
-                c.im.prev_depth[pix] = div_(clip.z, clip.w);
-                if (pm.model != GKRT_MAT_DIELECTRIC) pv.P = fma3(normalize3(T.wd), -0.03f, pv.P);
-                if (pm.model == GKRT_MAT_DIFFUSE_LIGHT) {
-                    c.im.single_diffuse[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
-                    L.pix = -1;
-                    return false;
-                }
+            for (int q = 0; q < 12; ++q) cp[q] = __ldg(&c.sc.inst_prev[12u * pv.inst + q]);
+            const f3 prevP = xpoint(cp, pv.P);
+            const f4 ph = mat4v(fc.prev_view_projection_unjit, F4(prevP.x, prevP.y, prevP.z, 1.0f));
+            const float pfx = div_(ph.x, ph.w) * 0.5f, pfy = div_(ph.y, ph.w) * 0.5f;
+            uint32_t mom = c.im.motion_moment[pix];
+            if (len3(pv.P - prevP) > 0.02f) mom = fc.temporal_frames;
+            else mom = mom > 0u ? mom - 1u : 0u;
+            c.im.motion_moment[pix] = mom;
+            const MatV pm = load_mat(c.sc, pv.mat);
+            c.im.albedo[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
+            c.im.normal[pix] = make_float4(pv.N.x, pv.N.y, pv.N.z, pm.fuzz);
+            c.im.object_id[pix] = __ldg(&c.sc.S.inst[pv.inst].instance_id);
+            c.im.motion[pix] = make_float2((pfx - cfx) * (float)c.W, (pfy - cfy) * (float)c.H);
+            c.im.prev_depth[pix] = div_(clip.z, clip.w);
+            if (pm.model != GKRT_MAT_DIELECTRIC) pv.P = fma3(normalize3(T.wd), -0.03f, pv.P);
+            if (pm.model == GKRT_MAT_DIFFUSE_LIGHT) {
+                c.im.single_diffuse[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
+                L.pix = -1;
+            } else {
                 const bool pdiel = pm.model == GKRT_MAT_DIELECTRIC;
                 int samples = (int)fc.number_of_samples * (mom > 0u ? 4 : 1);
                 if (samples < 1) samples = 1;
@@ -156,154 +148,163 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) { c.slot(SL_FC + q) = 0.0f; c.slot(SL_FR + q) = 0.0f; }
                 L.i = 0;
-                k = K_BEGIN_SAMPLE;
-                break;
-            }
-            case K_BEGIN_SAMPLE: {
-                const f4 eye = mat4v(fc.model_view_inverse, F4(0.0f, 0.0f, 0.0f, 1.0f));
-                L.rc = F4(1.0f, 1.0f, 1.0f, 1.0f);
-                L.vs.P = pv_pos(c);
-                L.vs.N = pv_nrm(c);
-                L.vs.mat = __float_as_uint(c.slot(SL_MAT));
-                L.dir = normalize3(L.vs.P - xyz(eye));
-                L.hitReflect = false;
-                L.hitMetal = false;
-                k = K_PRE_FIRST;
-                break;
-            }
-            case K_PRE_FIRST:
-            case K_PRE_BOUNCE: {
-                // GetRayColor up to the trace (Shading.slang:1007-1039)
-                const bool first = k == K_PRE_FIRST;
-                const MatV mat = load_mat(c.sc, L.vs.mat);
-                const bool diel = mat.model == GKRT_MAT_DIELECTRIC;
-                const float startPosOffset = diel ? 0.0f : 1.0f;
-                const float dotValue = dot3(L.dir, L.vs.N);
-                const bool back = dotValue > 0.0f;
-                const f3 outward = back ? -L.vs.N : L.vs.N;
-                const float niOverNt = back ? mat.ri2 : div_(1.0f, mat.ri2);
-                const float cosine = dotValue > 0.0f ? mat.ri * dotValue : -dotValue;
-                const float reflectProb = schlick(cosine, mat.ri);
-                const bool chanceReflect = rnd1(L.seed) < reflectProb;
-                const bool chanceMetal = rnd1(L.seed) < mat.metal;
-                const bool chanceGGX = chanceReflect || chanceMetal;
-                f3 tdir;
-                if (chanceGGX) tdir = ggx_sample(L.seed, sqrt_(mat.fuzz), reflect3(L.dir, outward));
-                else tdir = align_normal(hemisphere_cos(L.seed), outward);
-                if (first) { L.hitReflect = chanceGGX; L.hitMetal = chanceMetal; }
-                if (diel && !chanceReflect) tdir = refract3(L.dir, outward, niOverNt);
-                L.dir = tdir;
-                L.chanceReflect = chanceReflect;
-                L.back = back;
-                L.diel = diel;
-                L.stage = first ? ST_FIRST : ST_BOUNCE;
-                emit(T, c, fma3(L.vs.N, 0.001f * startPosOffset, L.vs.P), tdir, kClosest);
-                return true;
-            }
-            case K_FIRST_DONE:
-            case K_BOUNCE_DONE: {
-                // GetRayColor after the trace (Shading.slang:1039-1081)
-                bool term;
-                if (T.hit) {
-                    L.vs = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
-                    const MatV hm = load_mat(c.sc, L.vs.mat);
-                    if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !L.chanceReflect) L.rc = L.rc * hm.diffuse;
-                    if (L.back && !L.diel) { L.rc = F4(0.5f, 0.5f, 0.5f, 0.0f); term = true; }
-                    else term = hm.model == GKRT_MAT_DIFFUSE_LIGHT;
-                } else {
-                    L.rc = L.rc * sky(fc);
-                    term = true;
-                }
-                if (term) { k = K_END_SAMPLE; break; }
-                const uint32_t loop = __float_as_uint(c.slot(SL_LOOP));
-                if (k == K_FIRST_DONE) {
-                    const uint32_t maxB = (loop >> 16) & 0x7FFFu;
-                    const bool pdiel = (loop >> 31) != 0u;
-                    if (fc.fast_gather && !pdiel) {
-                        L.rc = L.rc * probe_term(c.sc, L.vs.P, L.vs.N);
-                        k = K_END_SAMPLE;
-                        break;
-                    }
-                    L.b = 1;
-                    k = L.b < maxB ? K_PRE_BOUNCE : K_END_SAMPLE;
-                    break;
-                }
-                if (fc.has_sun && rnd1(L.seed) < 0.5f) {
-                    const f3 cd = align_normal(cone(L.seed, kCosCone), sunDir);
-                    L.stage = ST_SUN;
-                    emit(T, c, L.vs.P, cd, kAny);
-                    return true;
-                }
-                k = K_AFTER_SUN;
-                break;
-            }
-            case K_SUN_DONE: {
-                if (!T.hit) {
-                    L.rc = L.rc * F4(fc.sun_color[0], fc.sun_color[1], fc.sun_color[2], fc.sun_color[3]);
-                    k = K_END_SAMPLE;
-                } else {
-                    k = K_AFTER_SUN;
-                }
-                break;
-            }
-            case K_AFTER_SUN: {
-                const uint32_t loop = __float_as_uint(c.slot(SL_LOOP));
-                const uint32_t maxB = (loop >> 16) & 0x7FFFu;
-                const bool pdiel = (loop >> 31) != 0u;
-                const bool early = !pdiel && rnd1(L.seed) < 0.5f;
-                if (L.b == maxB - 1u || early) {
-                    L.rc = L.rc * probe_term(c.sc, L.vs.P, L.vs.N);
-                    k = K_END_SAMPLE;
-                } else {
-                    ++L.b;
-                    k = K_PRE_BOUNCE;
-                }
-                break;
-            }
-            case K_END_SAMPLE: {
-                // end of a sample (Shading.slang:1159-1172)
-                if (L.hitMetal) L.rc = L.rc * load_mat(c.sc, __float_as_uint(c.slot(SL_MAT))).diffuse;
-                const int acc = L.hitReflect ? SL_FR : SL_FC;
-                c.slot(acc) = c.slot(acc) + L.rc.x;
-                c.slot(acc + 1) = c.slot(acc + 1) + L.rc.y;
-                c.slot(acc + 2) = c.slot(acc + 2) + L.rc.z;
-                c.slot(acc + 3) = c.slot(acc + 3) + L.rc.w;
-                const uint32_t samples = __float_as_uint(c.slot(SL_LOOP)) & 0xFFFFu;
-                if (++L.i < samples) { k = K_BEGIN_SAMPLE; break; }
-                const float fs = (float)samples;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    c.slot(SL_FC + q) = div_(c.slot(SL_FC + q), fs);
-                    c.slot(SL_FR + q) = div_(c.slot(SL_FR + q), fs);
-                }
-                if (fc.has_sun) {
-                    const f3 cd = align_normal(cone(L.seed, kCosCone), sunDir);
-                    L.stage = ST_DIRECT;
-                    emit(T, c, pv_pos(c), cd, kAny);
-                    return true;
-                }
-                shadow = 0.0f;
-                k = K_FINISH;
-                break;
-            }
-            case K_DIRECT_DONE: {
-                shadow = T.hit ? 0.0f : 1.0f;
-                k = K_FINISH;
-                break;
-            }
-            default: {   // K_FINISH: DirectIlluminate's contribution and the two outputs
-                const float dd = mx(dot3(sunDir, normalize3(pv_nrm(c))), 0.0f) * 0.318309886183790671538f;
-                f4 fcol = F4(c.slot(SL_FC), c.slot(SL_FC + 1), c.slot(SL_FC + 2), c.slot(SL_FC + 3));
-                const f4 frefl = F4(c.slot(SL_FR), c.slot(SL_FR + 1), c.slot(SL_FR + 2), c.slot(SL_FR + 3));
-                fcol = fcol + F4((fc.sun_color[0] * dd) * shadow, (fc.sun_color[1] * dd) * shadow,
-                                 (fc.sun_color[2] * dd) * shadow, (fc.sun_color[3] * dd) * shadow);
-                c.im.single_diffuse[L.pix] = make_float4(fcol.x, fcol.y, fcol.z, fcol.w);
-                c.im.single_specular[L.pix] = make_float4(frefl.x, frefl.y, frefl.z, frefl.w);
-                L.pix = -1;
-                return false;
+                need_begin = true;
             }
         }
     }
+
+    // 2. GetRayColor after its trace (Shading.slang:1039-1081), then the bounce loop's sun test
+    if (stage == ST_FIRST || stage == ST_BOUNCE) {
+        bool term;
+        if (T.hit) {
+            L.vs = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
+            const MatV hm = load_mat(c.sc, L.vs.mat);
+            if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !L.chanceReflect) L.rc = L.rc * hm.diffuse;
+            if (L.back && !L.diel) { L.rc = F4(0.5f, 0.5f, 0.5f, 0.0f); term = true; }
+            else term = hm.model == GKRT_MAT_DIFFUSE_LIGHT;
+        } else {
+            L.rc = L.rc * sky(fc);
+            term = true;
+        }
+        const uint32_t loop = __float_as_uint(c.slot(SL_LOOP));
+        if (term) {
+            need_end = true;
+        } else if (stage == ST_FIRST) {
+            const uint32_t maxB = (loop >> 16) & 0x7FFFu;
+            const bool pdiel = (loop >> 31) != 0u;
+            if (fc.fast_gather && !pdiel) {
+                L.rc = L.rc * probe_term(c.sc, L.vs.P, L.vs.N);
+                need_end = true;
+            } else {
+                L.b = 1;
+                if (L.b < maxB) need_pre = true;
+                else need_end = true;
+            }
+        } else if (fc.has_sun && rnd1(L.seed) < 0.5f) {
+            const f3 cd = align_normal(cone(L.seed, kCosCone), sunDir);
+            L.stage = ST_SUN;
+            emit(T, c, L.vs.P, cd, kAny);
+            emitted = true;
+        } else {
+            need_after_sun = true;
+        }
+    }
+
+    // 3. the sun test's answer
+    if (stage == ST_SUN) {
+        if (!T.hit) {
+            L.rc = L.rc * F4(fc.sun_color[0], fc.sun_color[1], fc.sun_color[2], fc.sun_color[3]);
+            need_end = true;
+        } else {
+            need_after_sun = true;
+        }
+    }
+
+    // 4. early exit or last bounce: probe termination, else the next bounce
+    if (need_after_sun) {
+        const uint32_t loop = __float_as_uint(c.slot(SL_LOOP));
+        const uint32_t maxB = (loop >> 16) & 0x7FFFu;
+        const bool pdiel = (loop >> 31) != 0u;
+        const bool early = !pdiel && rnd1(L.seed) < 0.5f;
+        if (L.b == maxB - 1u || early) {
+            L.rc = L.rc * probe_term(c.sc, L.vs.P, L.vs.N);
+            need_end = true;
+        } else {
+            ++L.b;
+            need_pre = true;
+        }
+    }
+
+    // 5. end of a sample (Shading.slang:1159-1176), then the next sample or DirectIlluminate
+    if (need_end) {
+        if (L.hitMetal) L.rc = L.rc * load_mat(c.sc, __float_as_uint(c.slot(SL_MAT))).diffuse;
+        const int acc = L.hitReflect ? SL_FR : SL_FC;
+        c.slot(acc) = c.slot(acc) + L.rc.x;
+        c.slot(acc + 1) = c.slot(acc + 1) + L.rc.y;
+        c.slot(acc + 2) = c.slot(acc + 2) + L.rc.z;
+        c.slot(acc + 3) = c.slot(acc + 3) + L.rc.w;
+        const uint32_t samples = __float_as_uint(c.slot(SL_LOOP)) & 0xFFFFu;
+        if (++L.i < samples) {
+            need_begin = true;
+        } else {
+            const float fs = (float)samples;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                c.slot(SL_FC + q) = div_(c.slot(SL_FC + q), fs);
+                c.slot(SL_FR + q) = div_(c.slot(SL_FR + q), fs);
+            }
+            if (fc.has_sun) {
+                const f3 cd = align_normal(cone(L.seed, kCosCone), sunDir);
+                L.stage = ST_DIRECT;
+                emit(T, c, pv_pos(c), cd, kAny);
+                emitted = true;
+            } else {
+                shadow = 0.0f;
+                need_finish = true;
+            }
+        }
+    }
+
+    // 6. DirectIlluminate's answer
+    if (stage == ST_DIRECT) {
+        shadow = T.hit ? 0.0f : 1.0f;
+        need_finish = true;
+    }
+
+    // 7. the pixel's outputs (Shading.slang:1175-1183)
+    if (need_finish) {
+        const float dd = mx(dot3(sunDir, normalize3(pv_nrm(c))), 0.0f) * 0.318309886183790671538f;
+        f4 fcol = F4(c.slot(SL_FC), c.slot(SL_FC + 1), c.slot(SL_FC + 2), c.slot(SL_FC + 3));
+        const f4 frefl = F4(c.slot(SL_FR), c.slot(SL_FR + 1), c.slot(SL_FR + 2), c.slot(SL_FR + 3));
+        fcol = fcol + F4((fc.sun_color[0] * dd) * shadow, (fc.sun_color[1] * dd) * shadow,
+                         (fc.sun_color[2] * dd) * shadow, (fc.sun_color[3] * dd) * shadow);
+        c.im.single_diffuse[L.pix] = make_float4(fcol.x, fcol.y, fcol.z, fcol.w);
+        c.im.single_specular[L.pix] = make_float4(frefl.x, frefl.y, frefl.z, frefl.w);
+        L.pix = -1;
+    }
+
+    // 8. start of a sample (Shading.slang:1103-1117)
+    if (need_begin) {
+        const f4 eye = mat4v(fc.model_view_inverse, F4(0.0f, 0.0f, 0.0f, 1.0f));
+        L.rc = F4(1.0f, 1.0f, 1.0f, 1.0f);
+        L.vs.P = pv_pos(c);
+        L.vs.N = pv_nrm(c);
+        L.vs.mat = __float_as_uint(c.slot(SL_MAT));
+        L.dir = normalize3(L.vs.P - xyz(eye));
+        L.hitReflect = false;
+        L.hitMetal = false;
+        need_pre = true;
+        pre_first = true;
+    }
+
+    // 9. GetRayColor up to its trace (Shading.slang:1007-1039)
+    if (need_pre) {
+        const MatV mat = load_mat(c.sc, L.vs.mat);
+        const bool diel = mat.model == GKRT_MAT_DIELECTRIC;
+        const float startPosOffset = diel ? 0.0f : 1.0f;
+        const float dotValue = dot3(L.dir, L.vs.N);
+        const bool back = dotValue > 0.0f;
+        const f3 outward = back ? -L.vs.N : L.vs.N;
+        const float niOverNt = back ? mat.ri2 : div_(1.0f, mat.ri2);
+        const float cosine = dotValue > 0.0f ? mat.ri * dotValue : -dotValue;
+        const float reflectProb = schlick(cosine, mat.ri);
+        const bool chanceReflect = rnd1(L.seed) < reflectProb;
+        const bool chanceMetal = rnd1(L.seed) < mat.metal;
+        const bool chanceGGX = chanceReflect || chanceMetal;
+        f3 tdir;
+        if (chanceGGX) tdir = ggx_sample(L.seed, sqrt_(mat.fuzz), reflect3(L.dir, outward));
+        else tdir = align_normal(hemisphere_cos(L.seed), outward);
+        if (pre_first) { L.hitReflect = chanceGGX; L.hitMetal = chanceMetal; }
+        if (diel && !chanceReflect) tdir = refract3(L.dir, outward, niOverNt);
+        L.dir = tdir;
+        L.chanceReflect = chanceReflect;
+        L.back = back;
+        L.diel = diel;
+        L.stage = pre_first ? ST_FIRST : ST_BOUNCE;
+        emit(T, c, fma3(L.vs.N, 0.001f * startPosOffset, L.vs.P), tdir, kClosest);
+        emitted = true;
+    }
+    return emitted;
 }
 
 // Camera ray of FHardwarePrimaryRayCaster (Shading.slang:286-304) for pixel index pix.
@@ -370,11 +371,16 @@ __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeSc
             }
         }
         if (__ballot_sync(0xFFFFFFFFu, tracing) == 0u) break;
-        // advance all tracing lanes until enough of them are done to be worth a refill
+        // traversal phase: node steps while any lane can take one, then the postponed leaves
+        // of all lanes together, until every ray of the warp is finished
         for (;;) {
+            bool can = tracing && !T.done;
+            while (__any_sync(0xFFFFFFFFu, can)) {
+                if (can) can = trav_node_step(T, sc.S, stack + tid, kPtThreads, cn);
+            }
             if (tracing) {
-                if (!T.done) trav_step(T, sc.S, stack + tid, kPtThreads, cn);
-                if (T.done) tracing = false;
+                trav_leaf_step(T, sc.S, cn);
+                if (trav_finished(T)) tracing = false;
             }
             if (__popc(__ballot_sync(0xFFFFFFFFu, tracing)) < kRefillBelow) break;
         }
