@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "gk_shade.cuh"
+#include "gk_tma.cuh"
 #include "gkrt_internal.h"
 
 using namespace gk;
@@ -23,8 +24,9 @@ struct GkrtContext {
     int device = 0;
     uint32_t watchdog_ms = 60000;
     std::string err;
-    uint32_t W = 0, H = 0;
+    uint32_t W = 0, H = 0, P = 0;     // P: row pitch in pixels (W rounded up to 4: 16-byte rows)
     void* img[GKRT_IMG_COUNT] = {};
+    float4* atrous_tmp[2] = {nullptr, nullptr};   // ping-pong of the a-trous passes
 
     bool has_scene = false;
     std::vector<GkrtMesh> meshes;
@@ -111,7 +113,9 @@ uint32_t image_format(int id) {
 
 void free_images(GkrtContext* c) {
     for (auto& p : c->img) dfree(p);
-    c->W = c->H = 0;
+    dfree(c->atrous_tmp[0]);
+    dfree(c->atrous_tmp[1]);
+    c->W = c->H = c->P = 0;
 }
 
 void free_scene(GkrtContext* c) {
@@ -338,6 +342,34 @@ int check_frame(GkrtContext* ctx, const GkrtFrameConstants* fc) {
 
 int gkrt_internal_fail(GkrtContext* ctx, int code, const std::string& msg) { return fail(ctx, code, msg); }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link needed).
+cudaError_t gkrt_encode_tmap_2d(CUtensorMap* map, const void* base, uint32_t elems_x, uint32_t rows,
+                                uint32_t row_bytes, uint32_t box_x, uint32_t box_y, bool is_float) {
+    typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
+        fn = (EncodeFn)p;
+    }
+    if (((uintptr_t)base & 15u) || (row_bytes & 15u) || box_x == 0 || box_x > 256 || box_y == 0 || box_y > 256 ||
+        ((box_x * 4u) & 15u))
+        return cudaErrorInvalidValue;
+    const cuuint64_t dims[2] = {elems_x, rows};
+    const cuuint64_t strides[1] = {row_bytes};
+    const cuuint32_t box[2] = {box_x, box_y};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, is_float ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 2,
+                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 int gkrt_internal_ready_view(GkrtContext* ctx, SceneView* view, unsigned long long** counters, int* device) {
     if (!ctx->has_scene || !ctx->blas_ready || !ctx->tlas_ready)
         return fail(ctx, GKRT_ERR_STATE, "scene and BVH must be built before this call (it allocates nothing)");
@@ -403,13 +435,19 @@ int gkrt_resize(GkrtContext* ctx, uint32_t width, uint32_t height) {
         return fail(ctx, GKRT_ERR_INVALID_ARG, "image size must be 1..16384");
     cudaSetDevice(ctx->device);
     free_images(ctx);
-    const size_t px = (size_t)width * height;
+    const uint32_t pitch = (width + 3u) & ~3u;
+    const size_t px = (size_t)pitch * height;
     for (int i = 0; i < GKRT_IMG_COUNT; ++i) {
         GK_CUDA(cudaMalloc(&ctx->img[i], px * image_bytes_per_px(i)));
         GK_CUDA(cudaMemset(ctx->img[i], 0, px * image_bytes_per_px(i)));
     }
+    for (auto& t : ctx->atrous_tmp) {
+        GK_CUDA(cudaMalloc((void**)&t, px * sizeof(float4)));
+        GK_CUDA(cudaMemset(t, 0, px * sizeof(float4)));
+    }
     ctx->W = width;
     ctx->H = height;
+    ctx->P = pitch;
     return GKRT_OK;
 }
 
@@ -522,7 +560,7 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     im.hit_inst = (uint32_t*)ctx->img[GKRT_IMG_HIT_INST];
     im.hit_prim = (uint32_t*)ctx->img[GKRT_IMG_HIT_PRIM];
     GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
-    GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, im, ctx->d_counters, ctx->d_work, ctx->num_sms, st));
+    GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, (int)ctx->P, im, ctx->d_counters, ctx->d_work, ctx->num_sms, st));
     return GKRT_OK;
 }
 
@@ -531,7 +569,8 @@ int gkrt_reproject_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* st
     if (rc != GKRT_OK) return rc;
     cudaSetDevice(ctx->device);
     ReprojectArgs a;
-    a.W = (int)ctx->W; a.H = (int)ctx->H;
+    a.W = (int)ctx->W; a.H = (int)ctx->H; a.P = (int)ctx->P;
+    a.err = ctx->d_error;
     a.progressive = fc->progressive_render;
     a.temporal_frames = fc->temporal_frames;
     a.src_d = (const float4*)ctx->img[GKRT_IMG_SINGLE_DIFFUSE];
@@ -555,16 +594,35 @@ int gkrt_reproject_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* st
 int gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
     int rc = check_frame(ctx, fc);
     if (rc != GKRT_OK) return rc;
-    if (fc->denoiser != GKRT_DENOISE_JBF) return fail(ctx, GKRT_ERR_UNSUPPORTED, "denoiser not supported by this build");
+    if (fc->denoiser > GKRT_DENOISE_ATROUS) return fail(ctx, GKRT_ERR_UNSUPPORTED, "unknown denoiser");
     cudaSetDevice(ctx->device);
+    if (fc->denoiser == GKRT_DENOISE_ATROUS && fc->bf_size > 0u) {
+        AtrousArgs a;
+        a.W = (int)ctx->W; a.H = (int)ctx->H; a.P = (int)ctx->P;
+        a.step = 1; a.last = 0; a.hdr = fc->hdr;
+        a.sigma_lum = fc->bf_sigma_lum;
+        a.paper_white_nit = fc->paper_white_nit;
+        a.err = ctx->d_error;
+        a.normal = (const float4*)ctx->img[GKRT_IMG_NORMAL];
+        a.albedo = (const float4*)ctx->img[GKRT_IMG_ACCUM_ALBEDO];
+        a.spec = (const float4*)ctx->img[GKRT_IMG_ACCUM_SPECULAR];
+        a.id0 = (const uint32_t*)ctx->img[GKRT_IMG_OBJECT_ID];
+        a.out = nullptr;
+        a.final_out = (float4*)ctx->img[GKRT_IMG_DENOISED];
+        a.final_linear = (float4*)ctx->img[GKRT_IMG_DENOISED_LINEAR];
+        GK_CUDA(gkrt_launch_atrous(a, (const float4*)ctx->img[GKRT_IMG_ACCUM_DIFFUSE], ctx->atrous_tmp[0],
+                                   ctx->atrous_tmp[1], (cudaStream_t)stream));
+        return GKRT_OK;
+    }
     ComposeArgs a;
-    a.W = (int)ctx->W; a.H = (int)ctx->H;
+    a.W = (int)ctx->W; a.H = (int)ctx->H; a.P = (int)ctx->P;
     a.bf_size = fc->bf_size;
     a.hdr = fc->hdr;
     a.bf_sigma = fc->bf_sigma;
     a.bf_sigma_lum = fc->bf_sigma_lum;
     a.paper_white_nit = fc->paper_white_nit;
     a.pad = 0.0f;
+    a.err = ctx->d_error;
     a.acc_d = (const float4*)ctx->img[GKRT_IMG_ACCUM_DIFFUSE];
     a.acc_s = (const float4*)ctx->img[GKRT_IMG_ACCUM_SPECULAR];
     a.acc_a = (const float4*)ctx->img[GKRT_IMG_ACCUM_ALBEDO];
@@ -601,7 +659,7 @@ int gkrt_get_image(GkrtContext* ctx, int id, GkrtImageView* out) {
     out->device_ptr = ctx->img[id];
     out->width = ctx->W;
     out->height = ctx->H;
-    out->pitch_bytes = (uint32_t)(ctx->W * image_bytes_per_px(id));
+    out->pitch_bytes = (uint32_t)(ctx->P * image_bytes_per_px(id));
     out->format = image_format(id);
     return GKRT_OK;
 }
@@ -624,7 +682,9 @@ int gkrt_synchronize(GkrtContext* ctx, void* stream) {
     if (errw) {
         cudaMemset(ctx->d_error, 0, 4);
         return fail(ctx, GKRT_ERR_DEVICE_LIMIT,
-                    (errw & kErrStack) ? "traversal stack overflow" : "traversal iteration cap reached");
+                    (errw & kErrStack) ? "traversal stack overflow"
+                    : (errw & kErrIter) ? "traversal iteration cap reached"
+                                        : "a tile load did not complete within its wait limit");
     }
     return GKRT_OK;
 }
@@ -633,10 +693,12 @@ int gkrt_copy_image_to_host(GkrtContext* ctx, int id, void* dst, size_t dst_byte
     GkrtImageView v;
     int rc = gkrt_get_image(ctx, id, &v);
     if (rc != GKRT_OK) return rc;
-    const size_t bytes = (size_t)v.pitch_bytes * v.height;
-    if (!dst || dst_bytes < bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
+    const size_t row = (size_t)v.width * image_bytes_per_px(id);
+    if (!dst || dst_bytes < row * v.height) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
     cudaSetDevice(ctx->device);
-    GK_CUDA(cudaMemcpyAsync(dst, v.device_ptr, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    // the host copy is dense (width x height); the device rows are padded
+    GK_CUDA(cudaMemcpy2DAsync(dst, row, v.device_ptr, v.pitch_bytes, row, v.height, cudaMemcpyDeviceToHost,
+                              (cudaStream_t)stream));
     return gkrt_synchronize(ctx, stream);
 }
 
@@ -644,10 +706,11 @@ int gkrt_upload_image(GkrtContext* ctx, int id, const void* src, size_t src_byte
     GkrtImageView v;
     int rc = gkrt_get_image(ctx, id, &v);
     if (rc != GKRT_OK) return rc;
-    const size_t bytes = (size_t)v.pitch_bytes * v.height;
-    if (!src || src_bytes != bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "source size differs from the image");
+    const size_t row = (size_t)v.width * image_bytes_per_px(id);
+    if (!src || src_bytes != row * v.height) return fail(ctx, GKRT_ERR_INVALID_ARG, "source size differs from the image");
     cudaSetDevice(ctx->device);
-    GK_CUDA(cudaMemcpyAsync(v.device_ptr, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    GK_CUDA(cudaMemcpy2DAsync(v.device_ptr, v.pitch_bytes, src, row, row, v.height, cudaMemcpyHostToDevice,
+                              (cudaStream_t)stream));
     return gkrt_synchronize(ctx, stream);
 }
 

@@ -13,8 +13,9 @@ struct SceneView;
 struct BvhNode;
 
 struct ReprojectArgs {
-    int W, H;
+    int W, H, P;                   // P: row pitch in pixels (a multiple of 4)
     uint32_t progressive, temporal_frames;
+    uint32_t* err;
     const float4 *src_d, *src_s, *src_a, *prev_d, *prev_s, *prev_a, *normal;
     const float2* motion;
     const uint32_t *id0, *id1, *moment;
@@ -22,11 +23,24 @@ struct ReprojectArgs {
 };
 
 struct ComposeArgs {
-    int W, H;
+    int W, H, P;
     uint32_t bf_size, hdr;
     float bf_sigma, bf_sigma_lum, paper_white_nit, pad;
+    uint32_t* err;
     const float4 *acc_d, *acc_s, *acc_a;
     float4 *out, *out_linear;
+};
+
+struct AtrousArgs {
+    int W, H, P;
+    int step;                      // 1, 2, 4
+    uint32_t last, hdr;            // last pass remodulates and tone maps
+    float sigma_lum, paper_white_nit;
+    uint32_t* err;
+    const float4 *normal, *albedo, *spec;
+    const uint32_t* id0;
+    float4* out;                   // this pass's output (scratch)
+    float4 *final_out, *final_linear;
 };
 
 // Host-side BVH build (binned SAH over boxes). Returns nodes in device layout and the leaf
@@ -43,7 +57,7 @@ void build_bvh_host(const float* boxes, uint32_t n, uint32_t max_leaf, uint32_t 
                     bool leaf_is_instance, HostBvh& out);
 }  // namespace gk
 
-cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H,
+cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,
                                    const gk::PixelImages& im, unsigned long long* counters, unsigned int* work,
                                    int num_sms, cudaStream_t st);
 cudaError_t gkrt_launch_trace_rays(const gk::SceneView& S, const GkrtRay* rays, GkrtHit* hits, uint32_t n,
@@ -57,3 +71,4 @@ int gkrt_internal_ready_view(GkrtContext* ctx, gk::SceneView* view, unsigned lon
 
 cudaError_t gkrt_launch_reproject(const gk::ReprojectArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_compose(const gk::ComposeArgs& a, cudaStream_t st);
+cudaError_t gkrt_launch_atrous(const gk::AtrousArgs& a, const float4* in, float4* tmp0, float4* tmp1, cudaStream_t st);

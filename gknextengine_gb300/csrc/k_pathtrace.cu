@@ -59,7 +59,7 @@ struct Ctx {
     const ShadeScene& sc;
     const GkrtFrameConstants& fc;
     const PixelImages& im;
-    int W, H;
+    int W, H, P;      // P: image row pitch in pixels
     float* ps;        // this thread's first shared slot
     int stride;
     Counters& cn;
@@ -310,7 +310,7 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
 // Camera ray of FHardwarePrimaryRayCaster (Shading.slang:286-304) for pixel index pix.
 __device__ void start_pixel(Lane& L, Trav& T, const Ctx& c, int x, int y) {
     const GkrtFrameConstants& fc = c.fc;
-    L.pix = y * c.W + x;
+    L.pix = y * c.P + x;
     L.seed.v[0] = (uint32_t)x; L.seed.v[1] = (uint32_t)y; L.seed.v[2] = fc.total_frames; L.seed.v[3] = 0u;
     float uvx = fmaf_(div_((float)x, (float)c.W), 2.0f, -1.0f);
     float uvy = fmaf_(div_((float)y, (float)c.H), 2.0f, -1.0f);
@@ -332,7 +332,7 @@ __device__ void start_pixel(Lane& L, Trav& T, const Ctx& c, int x, int y) {
 }
 
 __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeScene sc, GkrtFrameConstants fc, int W, int H,
-                                                           PixelImages im, unsigned long long* counters,
+                                                           int P, PixelImages im, unsigned long long* counters,
                                                            unsigned int* work) {
     __shared__ uint32_t stack[kStackSize * kPtThreads];
     __shared__ float pslots[SL_COUNT * kPtThreads];
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeSc
     const unsigned lane = tid & 31u;
     Counters cn;
     cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0;
-    const Ctx c{sc, fc, im, W, H, pslots + tid, kPtThreads, cn};
+    const Ctx c{sc, fc, im, W, H, P, pslots + tid, kPtThreads, cn};
     const int tiles_x = (W + 7) / 8, tiles_y = (H + 3) / 4;
     const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
     Lane L;
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(kRqThreads) k_trace_rays(SceneView S, const Gk
 
 using namespace gk;
 
-cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H,
+cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,
                                    const PixelImages& im, unsigned long long* counters, unsigned int* work,
                                    int num_sms, cudaStream_t st) {
     int per_sm = 0;
@@ -435,7 +435,7 @@ cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstant
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(work, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    k_trace_pass<<<blocks, kPtThreads, 0, st>>>(sc, fc, W, H, im, counters, work);
+    k_trace_pass<<<blocks, kPtThreads, 0, st>>>(sc, fc, W, H, P, im, counters, work);
     return cudaGetLastError();
 }
 

@@ -2,31 +2,33 @@
 //
 // Reprojection follows assets/shaders/Process.ReProject.comp.slang:19-223; the compose
 // pass follows assets/shaders/Process.DenoiseJBF.comp.slang:4-184 with the tone mappers of
-// assets/shaders/common/Const_Func.slang:51-126. Both are HBM-bound stencils. Images are
-// dense FP32 arrays (pitch = width); a read outside the image returns zero.
+// assets/shaders/common/Const_Func.slang:51-126. The edge-aware a-trous filter (5 x 5, three
+// passes with steps 1, 2, 4) has no counterpart in the reference.
+//
+// All three are HBM-bound stencils over FP32 images (rows padded to a multiple of 4 pixels).
+// Each 16 x 16 block stages the neighbourhoods it reads (image tile plus halo) into shared
+// memory with 2D TMA loads (gk_tma.cuh), one mbarrier per block, then computes from shared
+// memory; data-dependent reads (history at the reprojected position) go through L2. Reads
+// outside the image are zero, as the TMA fill and the ld* helpers both give.
 #include "gk_device.cuh"
+#include "gk_tma.cuh"
 #include "gkrt_internal.h"
 
 namespace gk {
 
-struct ImgDims { int W, H; };
+constexpr int kTile = 16;
+
+struct ImgDims { int W, H, P; };   // width, height, pitch in pixels
 
 GK_D bool inb(const ImgDims& g, int x, int y) { return x >= 0 && y >= 0 && x < g.W && y < g.H; }
 GK_D f4 ld4(const float4* p, const ImgDims& g, int x, int y) {
     if (!inb(g, x, y)) return F4(0.0f, 0.0f, 0.0f, 0.0f);
-    float4 v = __ldg(&p[(size_t)y * g.W + x]);
+    float4 v = __ldg(&p[(size_t)y * g.P + x]);
     return F4(v.x, v.y, v.z, v.w);
-}
-GK_D f2 ld2(const float2* p, const ImgDims& g, int x, int y) {
-    f2 r; r.x = 0.0f; r.y = 0.0f;
-    if (!inb(g, x, y)) return r;
-    float2 v = __ldg(&p[(size_t)y * g.W + x]);
-    r.x = v.x; r.y = v.y;
-    return r;
 }
 GK_D uint32_t ldu(const uint32_t* p, const ImgDims& g, int x, int y) {
     if (!inb(g, x, y)) return 0u;
-    return __ldg(&p[(size_t)y * g.W + x]);
+    return __ldg(&p[(size_t)y * g.P + x]);
 }
 GK_D float lerpf(float a, float b, float t) { return fmaf_(t, b - a, a); }
 GK_D f3 lerp3(f3 a, f3 b, float t) { return F3(lerpf(a.x, b.x, t), lerpf(a.y, b.y, t), lerpf(a.z, b.z, t)); }
@@ -34,6 +36,23 @@ GK_D f4 lerp4(f4 a, f4 b, float t) {
     return F4(lerpf(a.x, b.x, t), lerpf(a.y, b.y, t), lerpf(a.z, b.z, t), lerpf(a.w, b.w, t));
 }
 GK_D float4 st4(f4 v) { return make_float4(v.x, v.y, v.z, v.w); }
+GK_D f4 tf4(const float4* t, int stride, int x, int y) {
+    float4 v = t[y * stride + x];
+    return F4(v.x, v.y, v.z, v.w);
+}
+
+// Arm the block's barrier (thread 0), then all threads wait. Returns false on a timeout.
+struct TileLoad {
+    uint64_t* bar;
+    GK_D void begin() {
+        if (threadIdx.x == 0) { mbar_init(bar, 1); mbar_fence_init(); }
+        __syncthreads();
+    }
+    GK_D bool wait(uint32_t* err) { return mbar_wait_bounded(bar, 0u, err); }
+};
+
+// ---------------------------------------------------------------------------------------
+// reprojection (Process.ReProject.comp.slang:71-223)
 
 // calculateWeight (Process.ReProject.comp.slang:32-47)
 GK_D float reproj_weight(float cd, bool same, bool center, f3 n, f3 cn) {
@@ -56,25 +75,61 @@ GK_D f3 history(const float4* prev, const ImgDims& g, f2 sub, int px, int py, ui
     return F3(fminf(fmaxf(h.x, 0.0f), 1600.0f), fminf(fmaxf(h.y, 0.0f), 1600.0f), fminf(fmaxf(h.z, 0.0f), 1600.0f));
 }
 
-__global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a) {
-    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
-    const ImgDims g{a.W, a.H};
-    if (x >= a.W || y >= a.H) return;
-    const size_t pix = (size_t)y * a.W + x;
+// staged neighbourhoods of one 16 x 16 block
+constexpr int kRpHalo = 2;                          // 5 x 5 spatial fill
+constexpr int kRpT = kTile + 2 * kRpHalo;           // 20 pixels
+constexpr int kRpIdX = kTile + 8;                   // id tile starts 4 left (16-byte aligned x)
+constexpr int kRpMv = kTile + 8;                    // motion read at 2x offsets: halo 4
+
+__global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid_constant__ CUtensorMap m_sd,
+                                                   const __grid_constant__ CUtensorMap m_ss,
+                                                   const __grid_constant__ CUtensorMap m_nrm,
+                                                   const __grid_constant__ CUtensorMap m_id,
+                                                   const __grid_constant__ CUtensorMap m_mv) {
+    __shared__ __align__(128) float4 t_sd[kRpT * kRpT];
+    __shared__ __align__(128) float4 t_ss[kRpT * kRpT];
+    __shared__ __align__(128) float4 t_nrm[kRpT * kRpT];
+    __shared__ __align__(128) uint32_t t_id[kRpT * kRpIdX];
+    __shared__ __align__(128) float2 t_mv[kRpMv * kRpMv];
+    __shared__ __align__(8) uint64_t bar;
+    const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int x = x0 + tx, y = y0 + ty;
+    const ImgDims g{a.W, a.H, a.P};
     if (a.progressive) {
-        const float k = 1.0f / 512.0f;
-        a.acc_d[pix] = st4(lerp4(ld4(a.prev_d, g, x, y), ld4(a.src_d, g, x, y), k));
-        a.acc_s[pix] = st4(lerp4(ld4(a.prev_s, g, x, y), ld4(a.src_s, g, x, y), k));
-        a.acc_a[pix] = st4(lerp4(ld4(a.prev_a, g, x, y), ld4(a.src_a, g, x, y), k));
+        if (x < a.W && y < a.H) {
+            const size_t pix = (size_t)y * a.P + x;
+            const float k = 1.0f / 512.0f;
+            a.acc_d[pix] = st4(lerp4(ld4(a.prev_d, g, x, y), ld4(a.src_d, g, x, y), k));
+            a.acc_s[pix] = st4(lerp4(ld4(a.prev_s, g, x, y), ld4(a.src_s, g, x, y), k));
+            a.acc_a[pix] = st4(lerp4(ld4(a.prev_a, g, x, y), ld4(a.src_a, g, x, y), k));
+        }
         return;
     }
-    const f4 cd = ld4(a.src_d, g, x, y), cs = ld4(a.src_s, g, x, y), ca = ld4(a.src_a, g, x, y);
-    const f2 mv = ld2(a.motion, g, x, y);
-    const float fxm = (float)x + mv.x, fym = (float)y + mv.y;
+    TileLoad tl{&bar};
+    tl.begin();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = 3u * kRpT * kRpT * 16u + kRpT * kRpIdX * 4u + kRpMv * kRpMv * 8u;
+        mbar_expect_tx(&bar, bytes);
+        tma_load_2d(t_sd, &m_sd, 4 * (x0 - kRpHalo), y0 - kRpHalo, &bar);
+        tma_load_2d(t_ss, &m_ss, 4 * (x0 - kRpHalo), y0 - kRpHalo, &bar);
+        tma_load_2d(t_nrm, &m_nrm, 4 * (x0 - kRpHalo), y0 - kRpHalo, &bar);
+        tma_load_2d(t_id, &m_id, x0 - 4, y0 - kRpHalo, &bar);
+        tma_load_2d(t_mv, &m_mv, 2 * (x0 - 4), y0 - 4, &bar);
+    }
+    if (!tl.wait(a.err)) return;
+    if (x >= a.W || y >= a.H) return;
+    const size_t pix = (size_t)y * a.P + x;
+    // tile-local coordinates of (x, y)
+    const int cx = tx + kRpHalo, cy = ty + kRpHalo;      // colour/normal tiles
+    const int ix = tx + 4;                               // id tile (starts 4 left)
+    const f4 cd = tf4(t_sd, kRpT, cx, cy), cs = tf4(t_ss, kRpT, cx, cy), ca = ld4(a.src_a, g, x, y);
+    const float2 mv2 = t_mv[(ty + 4) * kRpMv + (tx + 4)];
+    const float fxm = (float)x + mv2.x, fym = (float)y + mv2.y;
     const float flx = floorf(fxm), fly = floorf(fym);
     const int px = (int)flx, py = (int)fly;
     const bool inside = px < a.W && py < a.H && px >= -1 && py >= -1;
-    const uint32_t cur = ldu(a.id0, g, x, y);
+    const uint32_t cur = t_id[cy * kRpIdX + ix];
     uint32_t p0 = ldu(a.id1, g, px, py);
     const bool miss = cur == 65535u;
     const uint32_t moment = ldu(a.moment, g, x, y);
@@ -84,20 +139,19 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a) {
         a.acc_a[pix] = st4(ca);
         return;
     }
-    const f3 cn = xyz(ld4(a.normal, g, x, y));
+    const f3 cn = xyz(tf4(t_nrm, kRpT, cx, cy));
     f4 sd = F4(0.0f, 0.0f, 0.0f, 0.0f), ss = F4(0.0f, 0.0f, 0.0f, 0.0f);
     float tw = 0.0f, mir = 0.0f;
     for (int oy = -2; oy <= 2; ++oy) {
         for (int ox = -2; ox <= 2; ++ox) {
-            const int sx = x + ox, sy = y + oy;
-            const uint32_t pid = ldu(a.id0, g, sx, sy);
-            const f3 wn = xyz(ld4(a.normal, g, sx, sy));
+            const uint32_t pid = t_id[(cy + oy) * kRpIdX + (ix + ox)];
+            const f3 wn = xyz(tf4(t_nrm, kRpT, cx + ox, cy + oy));
             const float fox = (float)ox, foy = (float)oy;
             const float w = reproj_weight(sqrt_(fmaf_(foy, foy, fox * fox)), pid == cur, ox == 0 && oy == 0, wn, cn);
-            sd = sd + ld4(a.src_d, g, sx, sy) * w;
-            ss = ss + ld4(a.src_s, g, sx, sy) * w;
+            sd = sd + tf4(t_sd, kRpT, cx + ox, cy + oy) * w;
+            ss = ss + tf4(t_ss, kRpT, cx + ox, cy + oy) * w;
             tw = tw + w;
-            const f2 m2 = ld2(a.motion, g, x + 2 * ox, y + 2 * oy);
+            const float2 m2 = t_mv[(ty + 4 + 2 * oy) * kRpMv + (tx + 4 + 2 * ox)];
             mir = mir + sqrt_(fmaf_(m2.y, m2.y, m2.x * m2.x));
         }
     }
@@ -115,6 +169,9 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a) {
     a.acc_s[pix] = make_float4(os.x, os.y, os.z, ld4(a.prev_s, g, x, y).w);
     a.acc_a[pix] = make_float4(oa.x, oa.y, oa.z, ld4(a.prev_a, g, x, y).w);
 }
+
+// ---------------------------------------------------------------------------------------
+// compose: remodulation and tone map (Process.DenoiseJBF.comp.slang:145-181)
 
 // GranTurismoTonemapper (Const_Func.slang:100-121)
 GK_D float gt_tonemap(float x) {
@@ -139,17 +196,48 @@ GK_D float pq_encode(float v) {
     float N = (c1 + c2 * Lm) * div_(1.0f, 1.0f + c3 * Lm);
     return powf(N, m2);
 }
+GK_D void write_composed(const ComposeArgs& a, size_t pix, f3 total) {
+    a.out_linear[pix] = make_float4(total.x, total.y, total.z, 1.0f);
+    if (a.hdr) {
+        const float k = div_(a.paper_white_nit, 230.0f);
+        float r = gt_tonemap(div_(total.x, 2000.0f)) * 2000.0f, gg = gt_tonemap(div_(total.y, 2000.0f)) * 2000.0f,
+              bb = gt_tonemap(div_(total.z, 2000.0f)) * 2000.0f;
+        a.out[pix] = make_float4(pq_encode(r * k), pq_encode(gg * k), pq_encode(bb * k), 1.0f);
+    } else {
+        const float k = div_(a.paper_white_nit, 40000.0f);
+        a.out[pix] = make_float4(gt_tonemap(total.x * k), gt_tonemap(total.y * k), gt_tonemap(total.z * k), 1.0f);
+    }
+}
 
-__global__ void __launch_bounds__(256) k_compose(ComposeArgs a) {
-    const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+// joint bilateral filter (Process.DenoiseJBF.comp.slang:49-148): 36 taps at stride 2 over
+// 11 x 11; the 26 x 26 diffuse neighbourhood of the block is staged by TMA.
+constexpr int kJbfHalo = 5;
+constexpr int kJbfT = kTile + 2 * kJbfHalo;   // 26
+
+__global__ void __launch_bounds__(256) k_compose_jbf(ComposeArgs a, const __grid_constant__ CUtensorMap m_d) {
+    __shared__ __align__(128) float4 t_d[kJbfT * kJbfT];
+    __shared__ __align__(8) uint64_t bar;
+    const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int x = x0 + tx, y = y0 + ty;
+    const ImgDims g{a.W, a.H, a.P};
+    if (a.bf_size > 0u) {
+        TileLoad tl{&bar};
+        tl.begin();
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&bar, kJbfT * kJbfT * 16u);
+            tma_load_2d(t_d, &m_d, 4 * (x0 - kJbfHalo), y0 - kJbfHalo, &bar);
+        }
+        if (!tl.wait(a.err)) return;
+    }
     if (x >= a.W || y >= a.H) return;
-    const ImgDims g{a.W, a.H};
-    const size_t pix = (size_t)y * a.W + x;
+    const size_t pix = (size_t)y * a.P + x;
     f3 total;
     if (a.bf_size > 0u) {
         const f3 eps = F3(0.001f, 0.001f, 0.001f);
         const f3 lw = F3(0.212671f, 0.715160f, 0.072169f);
-        const f3 cc = xyz(ld4(a.acc_d, g, x, y)) + eps;
+        const int cx = tx + kJbfHalo, cy = ty + kJbfHalo;
+        const f3 cc = xyz(tf4(t_d, kJbfT, cx, cy)) + eps;
         const f3 cspec = xyz(ld4(a.acc_s, g, x, y)) + eps;
         const float clum = dot3(cc, lw);
         const float sigmaL = a.bf_sigma_lum * 100.0f;
@@ -158,7 +246,7 @@ __global__ void __launch_bounds__(256) k_compose(ComposeArgs a) {
         float wsum = 0.0f;
         for (int i = -5; i <= 5; i += 2) {
             for (int j = -5; j <= 5; j += 2) {
-                const f3 ci = xyz(ld4(a.acc_d, g, x + j, y + i)) + eps;
+                const f3 ci = xyz(tf4(t_d, kJbfT, cx + j, cy + i)) + eps;
                 const float lumi = dot3(ci, lw);
                 const float dist = sat(div_((float)(i * i + j * j), 25.0f));
                 const float dl = (clum - lumi) * (clum - lumi);
@@ -175,30 +263,142 @@ __global__ void __launch_bounds__(256) k_compose(ComposeArgs a) {
         const f3 d = xyz(ld4(a.acc_d, g, x, y)), s = xyz(ld4(a.acc_s, g, x, y)), al = xyz(ld4(a.acc_a, g, x, y));
         total = F3(fmaf_(d.x, al.x, s.x), fmaf_(d.y, al.y, s.y), fmaf_(d.z, al.z, s.z));
     }
-    a.out_linear[pix] = make_float4(total.x, total.y, total.z, 1.0f);
-    if (a.hdr) {
-        const float k = div_(a.paper_white_nit, 230.0f);
-        float r = gt_tonemap(div_(total.x, 2000.0f)) * 2000.0f, gg = gt_tonemap(div_(total.y, 2000.0f)) * 2000.0f,
-              bb = gt_tonemap(div_(total.z, 2000.0f)) * 2000.0f;
-        a.out[pix] = make_float4(pq_encode(r * k), pq_encode(gg * k), pq_encode(bb * k), 1.0f);
-    } else {
-        const float k = div_(a.paper_white_nit, 40000.0f);
-        a.out[pix] = make_float4(gt_tonemap(total.x * k), gt_tonemap(total.y * k), gt_tonemap(total.z * k), 1.0f);
+    write_composed(a, pix, total);
+}
+
+// ---------------------------------------------------------------------------------------
+// edge-aware a-trous filter (no counterpart in the reference)
+//
+// Pass with step s over the demodulated diffuse: 5 x 5 taps at offsets s * (-2..2) with the
+// B3-spline weights h = (1/16, 1/4, 3/8, 1/4, 1/16) per axis, multiplied by
+//   normal weight  max(0, n_p . n_q)^16,
+//   luminance weight  exp(-|L_p - L_q| / sigma_L)  (sigma_L = bf_sigma_lum),
+//   0 when the object ids differ or q lies outside the image.
+// Three passes with s = 1, 2, 4; the last one remodulates (x albedo + specular) and tone maps.
+constexpr int kAtMaxHalo = 8;
+constexpr int kAtT = kTile + 2 * kAtMaxHalo;   // 32
+
+GK_D float b3(int k) { return k == 0 ? 0.375f : (k == 1 ? 0.25f : 0.0625f); }
+GK_D float pow16(float v) { float a = v * v; a = a * a; a = a * a; return a * a; }
+
+__global__ void __launch_bounds__(256) k_atrous(AtrousArgs a, const __grid_constant__ CUtensorMap m_in,
+                                                const __grid_constant__ CUtensorMap m_nrm,
+                                                const __grid_constant__ CUtensorMap m_id) {
+    __shared__ __align__(128) float4 t_c[kAtT * kAtT];
+    __shared__ __align__(128) float4 t_n[kAtT * kAtT];
+    __shared__ __align__(128) uint32_t t_id[kAtT * kAtT];
+    __shared__ __align__(8) uint64_t bar;
+    const int s = a.step, halo = 2 * s, T = kTile + 2 * halo;
+    const int hid = (halo + 3) & ~3, Tid = kTile + 2 * hid;   // id tile starts on a 16-byte boundary
+    const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int x = x0 + tx, y = y0 + ty;
+    TileLoad tl{&bar};
+    tl.begin();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, (uint32_t)(T * T) * 32u + (uint32_t)(Tid * T) * 4u);
+        tma_load_2d(t_c, &m_in, 4 * (x0 - halo), y0 - halo, &bar);
+        tma_load_2d(t_n, &m_nrm, 4 * (x0 - halo), y0 - halo, &bar);
+        tma_load_2d(t_id, &m_id, x0 - hid, y0 - halo, &bar);
     }
+    if (!tl.wait(a.err)) return;
+    if (x >= a.W || y >= a.H) return;
+    const size_t pix = (size_t)y * a.P + x;
+    const int cx = tx + halo, cy = ty + halo;
+    const f3 lw = F3(0.212671f, 0.715160f, 0.072169f);
+    const f4 cp = tf4(t_c, T, cx, cy);
+    const f3 np = xyz(tf4(t_n, T, cx, cy));
+    const uint32_t idp = t_id[cy * Tid + tx + hid];
+    const float lp = dot3(xyz(cp), lw);
+    const float inv_sl = div_(1.0f, fmaxf(a.sigma_lum, 1e-4f));
+    f3 sum = F3(0.0f, 0.0f, 0.0f);
+    float wsum = 0.0f;
+    for (int dy = -2; dy <= 2; ++dy) {
+        for (int dx = -2; dx <= 2; ++dx) {
+            const int qx = x + dx * s, qy = y + dy * s;
+            if (qx < 0 || qy < 0 || qx >= a.W || qy >= a.H) continue;
+            const int lx = cx + dx * s, ly = cy + dy * s;
+            if (t_id[ly * Tid + tx + hid + dx * s] != idp) continue;
+            const f4 cq = tf4(t_c, T, lx, ly);
+            const float wn = pow16(fmaxf(dot3(np, xyz(tf4(t_n, T, lx, ly))), 0.0f));
+            const float wl = expf(-(fabsf(lp - dot3(xyz(cq), lw)) * inv_sl));
+            const float w = ((b3(dx < 0 ? -dx : dx) * b3(dy < 0 ? -dy : dy)) * wn) * wl;
+            sum = sum + xyz(cq) * w;
+            wsum = wsum + w;
+        }
+    }
+    // the centre tap always passes (weight 0.140625 > 0)
+    const f3 f = F3(div_(sum.x, wsum), div_(sum.y, wsum), div_(sum.z, wsum));
+    if (!a.last) {
+        a.out[pix] = make_float4(f.x, f.y, f.z, cp.w);
+        return;
+    }
+    const ImgDims g{a.W, a.H, a.P};
+    const f3 al = xyz(ld4(a.albedo, g, x, y)), sp = xyz(ld4(a.spec, g, x, y));
+    ComposeArgs c;
+    c.W = a.W; c.H = a.H; c.P = a.P; c.bf_size = 0u; c.hdr = a.hdr; c.paper_white_nit = a.paper_white_nit;
+    c.out = a.final_out; c.out_linear = a.final_linear;
+    write_composed(c, pix, F3(fmaf_(f.x, al.x, sp.x), fmaf_(f.y, al.y, sp.y), fmaf_(f.z, al.z, sp.z)));
 }
 
 }  // namespace gk
 
 using namespace gk;
 
+namespace {
+// 2D maps over float4 / u32 / float2 images with the given box in pixels.
+cudaError_t map_f4(CUtensorMap* m, const void* base, int W, int H, int P, int bw, int bh) {
+    return gkrt_encode_tmap_2d(m, base, 4u * W, H, 16u * P, 4u * bw, bh, true);
+}
+cudaError_t map_u32(CUtensorMap* m, const void* base, int W, int H, int P, int bw, int bh) {
+    return gkrt_encode_tmap_2d(m, base, W, H, 4u * P, bw, bh, false);
+}
+cudaError_t map_f2(CUtensorMap* m, const void* base, int W, int H, int P, int bw, int bh) {
+    return gkrt_encode_tmap_2d(m, base, 2u * W, H, 8u * P, 2u * bw, bh, true);
+}
+}  // namespace
+
 cudaError_t gkrt_launch_reproject(const ReprojectArgs& a, cudaStream_t st) {
-    dim3 grid((a.W + 15) / 16, (a.H + 15) / 16);
-    k_reproject<<<grid, 256, 0, st>>>(a);
+    CUtensorMap m_sd, m_ss, m_nrm, m_id, m_mv;
+    cudaError_t e;
+    if ((e = map_f4(&m_sd, a.src_d, a.W, a.H, a.P, kRpT, kRpT)) != cudaSuccess) return e;
+    if ((e = map_f4(&m_ss, a.src_s, a.W, a.H, a.P, kRpT, kRpT)) != cudaSuccess) return e;
+    if ((e = map_f4(&m_nrm, a.normal, a.W, a.H, a.P, kRpT, kRpT)) != cudaSuccess) return e;
+    if ((e = map_u32(&m_id, a.id0, a.W, a.H, a.P, kRpIdX, kRpT)) != cudaSuccess) return e;
+    if ((e = map_f2(&m_mv, a.motion, a.W, a.H, a.P, kRpMv, kRpMv)) != cudaSuccess) return e;
+    dim3 grid((a.W + kTile - 1) / kTile, (a.H + kTile - 1) / kTile);
+    k_reproject<<<grid, 256, 0, st>>>(a, m_sd, m_ss, m_nrm, m_id, m_mv);
     return cudaGetLastError();
 }
 
 cudaError_t gkrt_launch_compose(const ComposeArgs& a, cudaStream_t st) {
-    dim3 grid((a.W + 15) / 16, (a.H + 15) / 16);
-    k_compose<<<grid, 256, 0, st>>>(a);
+    CUtensorMap m_d;
+    cudaError_t e;
+    if ((e = map_f4(&m_d, a.acc_d, a.W, a.H, a.P, kJbfT, kJbfT)) != cudaSuccess) return e;
+    dim3 grid((a.W + kTile - 1) / kTile, (a.H + kTile - 1) / kTile);
+    k_compose_jbf<<<grid, 256, 0, st>>>(a, m_d);
     return cudaGetLastError();
+}
+
+cudaError_t gkrt_launch_atrous(const AtrousArgs& base, const float4* in, float4* tmp0, float4* tmp1,
+                               cudaStream_t st) {
+    dim3 grid((base.W + kTile - 1) / kTile, (base.H + kTile - 1) / kTile);
+    const float4* src = in;
+    float4* bufs[2] = {tmp0, tmp1};
+    for (int p = 0; p < 3; ++p) {
+        AtrousArgs a = base;
+        a.step = 1 << p;
+        a.last = p == 2 ? 1u : 0u;
+        a.out = bufs[p & 1];
+        const int T = kTile + 4 * a.step, Tid = kTile + 2 * ((2 * a.step + 3) & ~3);
+        CUtensorMap m_in, m_n, m_id;
+        cudaError_t e;
+        if ((e = map_f4(&m_in, src, a.W, a.H, a.P, T, T)) != cudaSuccess) return e;
+        if ((e = map_f4(&m_n, a.normal, a.W, a.H, a.P, T, T)) != cudaSuccess) return e;
+        if ((e = map_u32(&m_id, a.id0, a.W, a.H, a.P, Tid, T)) != cudaSuccess) return e;
+        k_atrous<<<grid, 256, 0, st>>>(a, m_in, m_n, m_id);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        src = a.out;
+    }
+    return cudaSuccess;
 }

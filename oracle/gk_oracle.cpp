@@ -837,6 +837,70 @@ f3 pq_encode(f3 lin) {
 
 const f3 kLumW{0.212671f, 0.715160f, 0.072169f};
 
+// Compose tail shared by both denoisers: linear output and the tone map
+// (Process.DenoiseJBF.comp.slang:170-181).
+void write_composed(const GkrtFrameConstants& fc, size_t pix, f3 total, void** im) {
+    float* lin = img_f4(im, GKRT_IMG_DENOISED_LINEAR, pix);
+    lin[0] = total.x; lin[1] = total.y; lin[2] = total.z; lin[3] = 1.0f;
+    float* out = img_f4(im, GKRT_IMG_DENOISED, pix);
+    if (fc.hdr) {
+        f3 t = f3{total.x / 2000.0f, total.y / 2000.0f, total.z / 2000.0f};
+        t = f3{gt_tonemap(t.x) * 2000.0f, gt_tonemap(t.y) * 2000.0f, gt_tonemap(t.z) * 2000.0f};
+        float k = fc.paper_white_nit / 230.0f;
+        f3 pq = pq_encode(f3{t.x * k, t.y * k, t.z * k});
+        out[0] = pq.x; out[1] = pq.y; out[2] = pq.z; out[3] = 1.0f;
+    } else {
+        float k = fc.paper_white_nit / 40000.0f;
+        out[0] = gt_tonemap(total.x * k);
+        out[1] = gt_tonemap(total.y * k);
+        out[2] = gt_tonemap(total.z * k);
+        out[3] = 1.0f;
+    }
+}
+
+// Edge-aware a-trous pass (no counterpart in the reference; the definition the GPU filter
+// implements): 5 x 5 taps at step s with B3-spline weights (1/16, 1/4, 3/8, 1/4, 1/16)
+// per axis, times max(0, n_p . n_q)^16, times exp(-|L_p - L_q| / sigma_L); taps outside the
+// image or on another object id get weight 0. The last pass remodulates and tone maps.
+float b3w(int k) { return k == 0 ? 0.375f : (k == 1 ? 0.25f : 0.0625f); }
+float pow16(float v) { float a = v * v; a = a * a; a = a * a; return a * a; }
+void atrous_pixel(const GkrtFrameConstants& fc, int W, int H, int x, int y, int step, const float* in, float* out,
+                  bool last, void** im) {
+    Img g{W, H};
+    const size_t pix = (size_t)y * W + x;
+    const float* NB = (const float*)im[GKRT_IMG_NORMAL];
+    const uint32_t* ID = (const uint32_t*)im[GKRT_IMG_OBJECT_ID];
+    const f3 lw{0.212671f, 0.715160f, 0.072169f};
+    const f4 cp = ld4(in, g, x, y);
+    const f3 np = xyz(ld4(NB, g, x, y));
+    const uint32_t idp = ldu(ID, g, x, y);
+    const float lp = dot3(xyz(cp), lw);
+    const float inv_sl = 1.0f / fmax_(fc.bf_sigma_lum, 1e-4f);
+    f3 sum{0.0f, 0.0f, 0.0f};
+    float wsum = 0.0f;
+    for (int dy = -2; dy <= 2; ++dy)
+        for (int dx = -2; dx <= 2; ++dx) {
+            const int qx = x + dx * step, qy = y + dy * step;
+            if (!g.in(qx, qy)) continue;
+            if (ldu(ID, g, qx, qy) != idp) continue;
+            const f4 cq = ld4(in, g, qx, qy);
+            const float wn = pow16(fmax_(dot3(np, xyz(ld4(NB, g, qx, qy))), 0.0f));
+            const float wl = std::exp(-(std::fabs(lp - dot3(xyz(cq), lw)) * inv_sl));
+            const float w = ((b3w(dx < 0 ? -dx : dx) * b3w(dy < 0 ? -dy : dy)) * wn) * wl;
+            sum = add(sum, mul(xyz(cq), w));
+            wsum = wsum + w;
+        }
+    const f3 f{sum.x / wsum, sum.y / wsum, sum.z / wsum};
+    if (!last) {
+        float* q = out + 4 * pix;
+        q[0] = f.x; q[1] = f.y; q[2] = f.z; q[3] = cp.w;
+        return;
+    }
+    const f3 al = xyz(ld4((const float*)im[GKRT_IMG_ACCUM_ALBEDO], g, x, y));
+    const f3 sp = xyz(ld4((const float*)im[GKRT_IMG_ACCUM_SPECULAR], g, x, y));
+    write_composed(fc, pix, f3{fma_(f.x, al.x, sp.x), fma_(f.y, al.y, sp.y), fma_(f.z, al.z, sp.z)}, im);
+}
+
 void denoise_pixel(const GkrtFrameConstants& fc, int W, int H, int x, int y, void** im) {
     Img g{W, H};
     const size_t pix = (size_t)y * W + x;
@@ -871,22 +935,7 @@ void denoise_pixel(const GkrtFrameConstants& fc, int W, int H, int x, int y, voi
         f3 d = xyz(ld4(AD, g, x, y)), s = xyz(ld4(AS, g, x, y)), a = xyz(ld4(AA, g, x, y));
         total = f3{fma_(d.x, a.x, s.x), fma_(d.y, a.y, s.y), fma_(d.z, a.z, s.z)};
     }
-    float* lin = img_f4(im, GKRT_IMG_DENOISED_LINEAR, pix);
-    lin[0] = total.x; lin[1] = total.y; lin[2] = total.z; lin[3] = 1.0f;
-    float* out = img_f4(im, GKRT_IMG_DENOISED, pix);
-    if (fc.hdr) {
-        f3 t = f3{total.x / 2000.0f, total.y / 2000.0f, total.z / 2000.0f};
-        t = f3{gt_tonemap(t.x) * 2000.0f, gt_tonemap(t.y) * 2000.0f, gt_tonemap(t.z) * 2000.0f};
-        float k = fc.paper_white_nit / 230.0f;
-        f3 pq = pq_encode(f3{t.x * k, t.y * k, t.z * k});
-        out[0] = pq.x; out[1] = pq.y; out[2] = pq.z; out[3] = 1.0f;
-    } else {
-        float k = fc.paper_white_nit / 40000.0f;
-        out[0] = gt_tonemap(total.x * k);
-        out[1] = gt_tonemap(total.y * k);
-        out[2] = gt_tonemap(total.z * k);
-        out[3] = 1.0f;
-    }
+    write_composed(fc, pix, total, im);
 }
 
 }  // namespace
@@ -1034,6 +1083,23 @@ void gko_reproject_pass(const GkrtFrameConstants* fc, int W, int H, void** image
 void gko_denoise_pass(const GkrtFrameConstants* fc, int W, int H, void** images, int threads) {
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
+#endif
+    if (fc->denoiser == GKRT_DENOISE_ATROUS && fc->bf_size > 0u) {
+        std::vector<float> t0((size_t)W * H * 4), t1((size_t)W * H * 4);
+        const float* src = (const float*)images[GKRT_IMG_ACCUM_DIFFUSE];
+        float* bufs[2] = {t0.data(), t1.data()};
+        for (int pass = 0; pass < 3; ++pass) {
+            float* dst = bufs[pass & 1];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+            for (int64_t p = 0; p < (int64_t)W * H; ++p)
+                atrous_pixel(*fc, W, H, (int)(p % W), (int)(p / W), 1 << pass, src, dst, pass == 2, images);
+            src = dst;
+        }
+        return;
+    }
+#ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
     for (int64_t p = 0; p < (int64_t)W * H; ++p) denoise_pixel(*fc, W, H, (int)(p % W), (int)(p / W), images);

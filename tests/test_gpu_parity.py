@@ -122,11 +122,14 @@ def _moving_cornell():
     return sc, cam, st
 
 
-def test_frames_reproject_and_compose():
+@pytest.mark.parametrize("W,H,denoiser", [(160, 120, abi.DENOISE_JBF), (150, 90, abi.DENOISE_ATROUS),
+                                           (97, 61, abi.DENOISE_JBF), (61, 47, abi.DENOISE_ATROUS)])
+def test_frames_reproject_and_compose(W, H, denoiser):
     """Three frames with a moving box and an orbiting camera: every image after each
-    pass matches the oracle (history, motion moment, accumulation, denoised)."""
+    pass matches the oracle (history, motion moment, accumulation, denoised). Odd sizes
+    exercise the padded rows and the zero fill of tile loads outside the image."""
     sc, cam, st = _moving_cornell()
-    W, H = 160, 120
+    st.denoiser = denoiser
     st.taa = True
     st.flags = abi.FRAME_PRIMARY_IDS
     r = PathTracingRenderer(0)
