@@ -76,6 +76,7 @@ IMAGE_FORMATS = {
 TRACE_CLOSEST = 0
 TRACE_ANY = 1
 BUILD_BLAS, BUILD_TLAS, BUILD_ALL = 1, 2, 3
+BUILD_ON_HOST = 4
 
 MATERIAL_DTYPE = np.dtype([
     ("diffuse", np.float32, 4), ("diffuse_texture_id", np.int32), ("mra_texture_id", np.int32),

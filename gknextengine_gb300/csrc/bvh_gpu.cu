@@ -1,0 +1,915 @@
+// bvh_gpu.cu — binned-SAH BVH construction on the GPU (sm_103a).
+//
+// Replaces the Vulkan acceleration-structure builds of the reference
+// (RayTraceBaseRenderer::CreateBottomLevelStructures / CreateTopLevelStructures,
+// src/Rendering/RayTraceBaseRenderer.cpp:276-386, and the per-frame TLAS rebuild of
+// AfterUpdateScene / TLAS Update, :165-218) with the split rule of the host builder
+// (binned SAH, 16 bins per axis, median split when all centroids share a bin).
+//
+// Top-down and breadth first. Every range of more than kSmall primitives is a "big task";
+// one level of big tasks is processed per round:
+//   bounds    per work item (<= 1024 primitives of one task): box and centroid bounds,
+//             reduced in the block and merged with ordered-integer atomics;
+//   bin       per work item: 3 x 16 bins in shared memory, merged into the task's bins;
+//   split     one thread per task: SAH over the 3 x 15 bin boundaries; the task writes its
+//             box and node ref into its parent's node (a node's fields are written by its
+//             two children, so no node is written twice);
+//   partition left counts, exclusive scan over work items, stable scatter, copy back;
+//   emit      children with more than kSmall primitives become the next round's big tasks
+//             (with their work items); the others become small tasks with a reserved run of
+//             m - 1 node slots (the most a subtree of m primitives can use).
+// The host reads back one group of counts per round. Small tasks are finished at the end by
+// one thread each, sequentially and with the host builder's leaf rule (SAH leaf test for
+// up to max_leaf triangles). Node indices are deterministic; reserved slots that a small
+// subtree does not use stay zero and are never referenced.
+// Node layout and leaf encoding are those of gk_trace.cuh.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "gk_trace.cuh"
+#include "gkrt_internal.h"
+
+namespace gk {
+
+namespace {
+
+constexpr int kBins = 16;
+constexpr uint32_t kChunk = 1024;
+constexpr int kBt = 256;
+constexpr uint32_t kSmall = 32;
+constexpr int kSmallStack = 40;
+constexpr int kBinWords = 3 * kBins * 7;   // per task: 3 axes x 16 bins x (6 ordered bounds + count)
+constexpr int kScanB = 1024;
+constexpr float kFar = 1e30f;
+constexpr uint32_t kBuildErrStack = 1u;     // small-task stack full
+constexpr uint32_t kBuildErrRange = 2u;     // a write would leave its task's range or reservation
+
+struct BigTask {
+    int node;       // relative node index of this task
+    int parent;     // relative node index of the parent, or -1 - root for a root task
+    int side;
+    int depth;
+    uint32_t begin, end;
+};
+
+struct SmallTask {
+    int parent, side, depth;
+    int root_node;  // relative node index for a root task, -1 otherwise
+    uint32_t begin, end;
+    uint32_t res0;  // first reserved node slot
+    uint32_t pad;
+};
+
+struct Split {
+    int axis, bin;  // axis -1: split by position
+    uint32_t nleft;
+    float clo, scale;
+};
+
+struct MeshRange {
+    uint32_t tri_base, index_offset, vertex_offset, pad;
+};
+
+struct Geo {
+    const float* box;   // 6 per primitive: lo xyz, hi xyz
+    const float* cent;  // 3 per primitive
+};
+
+__host__ __device__ inline int f2o(float f) {   // order-preserving float -> int
+    int i;
+    memcpy(&i, &f, 4);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__host__ __device__ inline float o2f(int i) {
+    const int j = i >= 0 ? i : i ^ 0x7FFFFFFF;
+    float f;
+    memcpy(&f, &j, 4);
+    return f;
+}
+
+__device__ __forceinline__ float area6(const float* b) {
+    const float dx = b[3] - b[0], dy = b[4] - b[1], dz = b[5] - b[2];
+    if (!(dx >= 0.0f && dy >= 0.0f && dz >= 0.0f)) return 0.0f;
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+__device__ __forceinline__ int bin_of(float c, float clo, float scale) {
+    const int b = (int)((c - clo) * scale);
+    return min(max(b, 0), kBins - 1);
+}
+
+// Child `side` of node `parent` gets box and ref; a root's box goes to root_box instead.
+__device__ void write_child(BvhNode* nodes, float* root_box, int parent, int side, const float* box, int ref) {
+    if (parent < 0) {
+        float* rb = root_box + 6 * (-1 - parent);
+        for (int j = 0; j < 6; ++j) rb[j] = box[j];
+        return;
+    }
+    float* f = reinterpret_cast<float*>(nodes + parent);
+    for (int j = 0; j < 6; ++j) f[6 * side + j] = box[j];
+    reinterpret_cast<int*>(nodes + parent)[12 + side] = ref;
+}
+
+// ---------------------------------------------------------------------------------------------
+// primitive boxes
+
+__device__ __forceinline__ uint32_t find_range(const MeshRange* mr, uint32_t nmr, uint32_t t) {
+    uint32_t lo = 0, hi = nmr;   // last range whose tri_base <= t
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (mr[mid].tri_base <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_tri_boxes(const float4* pos, const uint32_t* ind, const MeshRange* mr, uint32_t nmr, uint32_t ntri,
+                            float* box, float* cent) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const MeshRange m = mr[find_range(mr, nmr, t)];
+    const uint32_t lt = t - m.tri_base;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int v = 0; v < 3; ++v) {
+        const float4 p = pos[ind[m.index_offset + 3u * lt + v] + m.vertex_offset];
+        const float c[3] = {p.x, p.y, p.z};
+        for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], c[k]); hi[k] = fmaxf(hi[k], c[k]); }
+    }
+    for (int k = 0; k < 3; ++k) {
+        box[6 * (size_t)t + k] = lo[k];
+        box[6 * (size_t)t + 3 + k] = hi[k];
+        cent[3 * (size_t)t + k] = 0.5f * (lo[k] + hi[k]);
+    }
+}
+
+// Triangles in leaf order, 3 float4 each; the first vertex's w holds the mesh-local index.
+__global__ void k_gather_tris(const float4* pos, const uint32_t* ind, const MeshRange* mr, uint32_t nmr,
+                              const uint32_t* order, uint32_t ntri, float4* tris) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ntri) return;
+    const uint32_t p = order[k];
+    const MeshRange m = mr[find_range(mr, nmr, p)];
+    const uint32_t lt = p - m.tri_base;
+    for (int v = 0; v < 3; ++v) {
+        const float4 q = pos[ind[m.index_offset + 3u * lt + v] + m.vertex_offset];
+        tris[3 * (size_t)k + v] = make_float4(q.x, q.y, q.z, v == 0 ? __uint_as_float(lt) : 0.0f);
+    }
+}
+
+// World boxes of instances: the mesh box's 8 corners through the 3x4 world matrix in FP64,
+// widened because the mesh level traverses the FP32 object-space ray.
+__global__ void k_inst_boxes(const GpuInstBox* in, uint32_t n, const float* mesh_box, float* box, float* cent) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GpuInstBox I = in[i];
+    const float* rb = mesh_box + 6 * (size_t)I.mesh;
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+        const double p[3] = {(c & 1) ? rb[3] : rb[0], (c & 2) ? rb[4] : rb[1], (c & 4) ? rb[5] : rb[2]};
+        for (int r = 0; r < 3; ++r) {
+            const double v = (double)I.world[4 * r] * p[0] + (double)I.world[4 * r + 1] * p[1] +
+                             (double)I.world[4 * r + 2] * p[2] + (double)I.world[4 * r + 3];
+            lo[r] = fmin(lo[r], v);
+            hi[r] = fmax(hi[r], v);
+        }
+    }
+    for (int r = 0; r < 3; ++r) {
+        const double pad = 1e-5 * (fabs(lo[r]) + fabs(hi[r]) + (hi[r] - lo[r])) + 1e-7;
+        const float l = (float)(lo[r] - pad), h = (float)(hi[r] + pad);
+        box[6 * (size_t)i + r] = l;
+        box[6 * (size_t)i + 3 + r] = h;
+        cent[3 * (size_t)i + r] = 0.5f * (l + h);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// one round of big tasks
+
+__global__ void k_init_idx(uint32_t* idx, uint32_t n) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) idx[t] = t;
+}
+
+__global__ void k_clear(int* bins, int* tb, uint32_t ntask) {
+    const uint32_t nb = ntask * (uint32_t)kBinWords, nt = ntask * 12u;
+    const int pinf = f2o(INFINITY), ninf = f2o(-INFINITY);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb + nt; i += gridDim.x * blockDim.x) {
+        if (i < nb) {
+            const uint32_t q = i % 7u;
+            bins[i] = q == 6u ? 0 : (q < 3u ? pinf : ninf);
+        } else {
+            const uint32_t j = (i - nb) % 6u;
+            tb[i - nb] = j < 3u ? pinf : ninf;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBt) k_bounds(Geo g, const uint32_t* idx, const uint32_t* wtask,
+                                                const uint32_t* wbeg, const uint32_t* wend, int* tb) {
+    __shared__ int s[12];
+    const uint32_t w = blockIdx.x;
+    if (threadIdx.x < 12) s[threadIdx.x] = (threadIdx.x % 6) < 3 ? f2o(INFINITY) : f2o(-INFINITY);
+    __syncthreads();
+    float v[12];
+    for (int k = 0; k < 3; ++k) {
+        v[k] = INFINITY; v[3 + k] = -INFINITY; v[6 + k] = INFINITY; v[9 + k] = -INFINITY;
+    }
+    for (uint32_t i = wbeg[w] + threadIdx.x; i < wend[w]; i += kBt) {
+        const uint32_t p = idx[i];
+        for (int k = 0; k < 3; ++k) {
+            v[k] = fminf(v[k], g.box[6 * (size_t)p + k]);
+            v[3 + k] = fmaxf(v[3 + k], g.box[6 * (size_t)p + 3 + k]);
+            const float c = g.cent[3 * (size_t)p + k];
+            v[6 + k] = fminf(v[6 + k], c);
+            v[9 + k] = fmaxf(v[9 + k], c);
+        }
+    }
+    for (int k = 0; k < 12; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
+            const float u = __shfl_xor_sync(0xFFFFFFFFu, v[k], o);
+            v[k] = (k % 6) < 3 ? fminf(v[k], u) : fmaxf(v[k], u);
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 12; ++k) {
+            if ((k % 6) < 3) atomicMin(&s[k], f2o(v[k]));
+            else atomicMax(&s[k], f2o(v[k]));
+        }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        int* d = &tb[12 * (size_t)wtask[w] + threadIdx.x];
+        if ((threadIdx.x % 6) < 3) atomicMin(d, s[threadIdx.x]);
+        else atomicMax(d, s[threadIdx.x]);
+    }
+}
+
+__device__ __forceinline__ void axis_scale(const int* tbt, int k, float* clo, float* scale) {
+    *clo = o2f(tbt[6 + k]);
+    const float ext = o2f(tbt[9 + k]) - *clo;
+    *scale = ext > 0.0f ? (float)kBins / ext : 0.0f;
+}
+
+__global__ void __launch_bounds__(kBt) k_bin(Geo g, const uint32_t* idx, const int* tb, const uint32_t* wtask,
+                                             const uint32_t* wbeg, const uint32_t* wend, int* bins) {
+    __shared__ int sb[kBinWords];
+    const uint32_t w = blockIdx.x;
+    const uint32_t t = wtask[w];
+    const int pinf = f2o(INFINITY), ninf = f2o(-INFINITY);
+    for (int i = threadIdx.x; i < kBinWords; i += kBt) {
+        const int q = i % 7;
+        sb[i] = q == 6 ? 0 : (q < 3 ? pinf : ninf);
+    }
+    __syncthreads();
+    float clo[3], scale[3];
+    for (int k = 0; k < 3; ++k) axis_scale(tb + 12 * (size_t)t, k, &clo[k], &scale[k]);
+    for (uint32_t i = wbeg[w] + threadIdx.x; i < wend[w]; i += kBt) {
+        const uint32_t p = idx[i];
+        int b6[6];
+        for (int j = 0; j < 6; ++j) b6[j] = f2o(g.box[6 * (size_t)p + j]);
+        for (int k = 0; k < 3; ++k) {
+            int* s = &sb[(k * kBins + bin_of(g.cent[3 * (size_t)p + k], clo[k], scale[k])) * 7];
+            for (int j = 0; j < 3; ++j) {
+                atomicMin(&s[j], b6[j]);
+                atomicMax(&s[3 + j], b6[3 + j]);
+            }
+            atomicAdd(&s[6], 1);
+        }
+    }
+    __syncthreads();
+    int* gb = bins + (size_t)t * kBinWords;
+    for (int i = threadIdx.x; i < kBinWords; i += kBt) {
+        const int q = i % 7;
+        if (sb[i - q + 6] == 0) continue;   // empty bin: nothing to merge
+        if (q == 6) atomicAdd(&gb[i], sb[i]);
+        else if (q < 3) atomicMin(&gb[i], sb[i]);
+        else atomicMax(&gb[i], sb[i]);
+    }
+}
+
+// SAH over one axis's bins (the host builder's sweep): best cost, boundary and left count.
+__device__ void sah_axis(const float (*bb)[6], const uint32_t* bc, int axis, float* best, int* best_axis,
+                         int* best_bin, uint32_t* best_left) {
+    float ra[kBins];
+    uint32_t rc[kBins];
+    float acc[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    uint32_t cnt = 0;
+    for (int i = kBins - 1; i > 0; --i) {
+        for (int j = 0; j < 3; ++j) { acc[j] = fminf(acc[j], bb[i][j]); acc[3 + j] = fmaxf(acc[3 + j], bb[i][3 + j]); }
+        cnt += bc[i];
+        ra[i] = area6(acc);
+        rc[i] = cnt;
+    }
+    for (int j = 0; j < 3; ++j) { acc[j] = INFINITY; acc[3 + j] = -INFINITY; }
+    cnt = 0;
+    for (int i = 0; i < kBins - 1; ++i) {
+        for (int j = 0; j < 3; ++j) { acc[j] = fminf(acc[j], bb[i][j]); acc[3 + j] = fmaxf(acc[3 + j], bb[i][3 + j]); }
+        cnt += bc[i];
+        if (cnt == 0 || rc[i + 1] == 0) continue;
+        const float cost = area6(acc) * (float)cnt + ra[i + 1] * (float)rc[i + 1];
+        if (cost < *best) { *best = cost; *best_axis = axis; *best_bin = i + 1; *best_left = cnt; }
+    }
+}
+
+__global__ void k_split(const BigTask* tasks, uint32_t ntask, const int* bins, const int* tb, Split* split,
+                        BvhNode* nodes, float* root_box, uint32_t node_base) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntask) return;
+    const BigTask T = tasks[t];
+    const int* tbt = tb + 12 * (size_t)t;
+    float box[6];
+    for (int j = 0; j < 6; ++j) box[j] = o2f(tbt[j]);
+    write_child(nodes, root_box, T.parent, T.side, box, (int)node_base + T.node);
+    const int* b = bins + (size_t)t * kBinWords;
+    Split s;
+    s.axis = -1; s.bin = 0; s.nleft = (T.end - T.begin) / 2u; s.clo = 0.0f; s.scale = 0.0f;
+    float best = INFINITY;
+    float clo[3], scale[3];
+    for (int k = 0; k < 3; ++k) {
+        axis_scale(tbt, k, &clo[k], &scale[k]);
+        if (!(scale[k] > 0.0f)) continue;
+        float bb[kBins][6];
+        uint32_t bc[kBins];
+        for (int i = 0; i < kBins; ++i) {
+            const int* q = &b[(k * kBins + i) * 7];
+            for (int j = 0; j < 6; ++j) bb[i][j] = o2f(q[j]);
+            bc[i] = (uint32_t)q[6];
+        }
+        sah_axis(bb, bc, k, &best, &s.axis, &s.bin, &s.nleft);
+    }
+    if (s.axis >= 0) { s.clo = clo[s.axis]; s.scale = scale[s.axis]; }
+    split[t] = s;
+}
+
+__device__ __forceinline__ bool goes_left(const Geo& g, uint32_t p, uint32_t pos, const Split& s, uint32_t begin) {
+    if (s.axis < 0) return pos - begin < s.nleft;
+    return bin_of(g.cent[3 * (size_t)p + s.axis], s.clo, s.scale) < s.bin;
+}
+
+__global__ void __launch_bounds__(kBt) k_count_left(Geo g, const uint32_t* idx, const Split* split,
+                                                    const BigTask* tasks, const uint32_t* wtask, const uint32_t* wbeg,
+                                                    const uint32_t* wend, uint32_t* wleft) {
+    __shared__ uint32_t red[kBt / 32];
+    const uint32_t w = blockIdx.x, t = wtask[w];
+    const Split s = split[t];
+    const uint32_t begin = tasks[t].begin;
+    uint32_t c = 0;
+    for (uint32_t i = wbeg[w] + threadIdx.x; i < wend[w]; i += kBt) c += goes_left(g, idx[i], i, s, begin) ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int i = 0; i < kBt / 32; ++i) tot += red[i];
+        wleft[w] = tot;
+    }
+}
+
+// Stable scatter into tmp: left side first. wleft_scan: exclusive scan of left counts over
+// work items; a task's work items are consecutive, the first being task_w0[t].
+__global__ void __launch_bounds__(kBt) k_scatter(Geo g, const uint32_t* idx, uint32_t* tmp, const Split* split,
+                                                 const BigTask* tasks, const uint32_t* wtask, const uint32_t* wbeg,
+                                                 const uint32_t* wend, const uint32_t* wleft_scan,
+                                                 const uint32_t* task_w0, uint32_t* info) {
+    __shared__ uint32_t wsum[kBt / 32];
+    const uint32_t w = blockIdx.x, t = wtask[w];
+    const BigTask T = tasks[t];
+    const Split s = split[t];
+    const uint32_t left_before = wleft_scan[w] - wleft_scan[task_w0[t]];
+    const uint32_t right_before = (wbeg[w] - T.begin) - left_before;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    uint32_t lrun = 0, rrun = 0;
+    for (uint32_t base = wbeg[w]; base < wend[w]; base += kBt) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < wend[w];
+        uint32_t p = 0;
+        bool left = false;
+        if (valid) {
+            p = idx[i];
+            left = goes_left(g, p, i, s, T.begin);
+        }
+        const unsigned ml = __ballot_sync(0xFFFFFFFFu, valid && left);
+        const unsigned mr = __ballot_sync(0xFFFFFFFFu, valid && !left);
+        if (lane == 0) wsum[wid] = (uint32_t)__popc(ml) | ((uint32_t)__popc(mr) << 16);
+        __syncthreads();
+        uint32_t lw = 0, rw = 0, lt = 0, rt = 0;
+        for (uint32_t j = 0; j < kBt / 32; ++j) {
+            const uint32_t v = wsum[j];
+            if (j < wid) { lw += v & 0xFFFFu; rw += v >> 16; }
+            lt += v & 0xFFFFu;
+            rt += v >> 16;
+        }
+        if (valid) {
+            const uint32_t dst = left ? T.begin + left_before + lrun + lw + (uint32_t)__popc(ml & below)
+                                      : T.begin + s.nleft + right_before + rrun + rw + (uint32_t)__popc(mr & below);
+            if (dst >= T.begin && dst < T.end) tmp[dst] = p;
+            else atomicOr(&info[2], kBuildErrRange);
+        }
+        lrun += lt;
+        rrun += rt;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kBt) k_copy_back(const uint32_t* tmp, uint32_t* idx, const uint32_t* wbeg,
+                                                   const uint32_t* wend) {
+    const uint32_t w = blockIdx.x;
+    for (uint32_t i = wbeg[w] + threadIdx.x; i < wend[w]; i += kBt) idx[i] = tmp[i];
+}
+
+// Per task: (big children, their work items, small children, node slots they reserve).
+__global__ void k_child_counts(const BigTask* tasks, uint32_t ntask, const Split* split, uint4* cc) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntask) return;
+    const BigTask T = tasks[t];
+    const uint32_t m[2] = {split[t].nleft, (T.end - T.begin) - split[t].nleft};
+    uint4 c = make_uint4(0u, 0u, 0u, 0u);
+    for (int k = 0; k < 2; ++k) {
+        if (m[k] > kSmall) { c.x += 1u; c.y += (m[k] + kChunk - 1u) / kChunk; }
+        else { c.z += 1u; c.w += m[k] - 1u; }
+    }
+    cc[t] = c;
+}
+
+__global__ void k_emit(const BigTask* tasks, uint32_t ntask, const Split* split, const uint4* off, uint32_t node0,
+                       uint32_t res0, uint32_t small0, BigTask* next, uint32_t* nwtask, uint32_t* nwbeg,
+                       uint32_t* nwend, uint32_t* next_w0, SmallTask* small) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntask) return;
+    const BigTask T = tasks[t];
+    uint4 o = off[t];
+    const uint32_t mid = T.begin + split[t].nleft;
+    for (int c = 0; c < 2; ++c) {
+        const uint32_t b = c ? mid : T.begin, e = c ? T.end : mid, m = e - b;
+        if (m > kSmall) {
+            const uint32_t j = o.x++;
+            BigTask nt;
+            nt.node = (int)(node0 + j);
+            nt.parent = T.node;
+            nt.side = c;
+            nt.depth = T.depth + 1;
+            nt.begin = b;
+            nt.end = e;
+            next[j] = nt;
+            next_w0[j] = o.y;
+            for (uint32_t cb = b; cb < e; cb += kChunk) {
+                const uint32_t w = o.y++;
+                nwtask[w] = j;
+                nwbeg[w] = cb;
+                nwend[w] = min(cb + kChunk, e);
+            }
+        } else {
+            SmallTask st;
+            st.parent = T.node;
+            st.side = c;
+            st.depth = T.depth + 1;
+            st.root_node = -1;
+            st.begin = b;
+            st.end = e;
+            st.res0 = res0 + o.w;
+            st.pad = 0;
+            small[small0 + o.z++] = st;
+            o.w += m - 1u;
+        }
+    }
+}
+
+// One thread per small task: the rest of the subtree, depth first, with the host builder's
+// rules (triangle ranges of up to 2 are leaves, up to max_leaf when the SAH prefers a leaf;
+// instance leaves hold one instance). info[0] += nodes used, info[1] = max depth, info[2]
+// error bits.
+__global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, BvhNode* nodes, float* root_box,
+                        uint32_t max_leaf, int inst_leaf, const uint32_t* prim_map, uint32_t node_base,
+                        uint32_t* info) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns) return;
+    const SmallTask S = st[i];
+    struct Item {
+        uint32_t b, e;
+        int parent, side, depth;
+    };
+    Item stk[kSmallStack];
+    int sp = 0;
+    stk[sp++] = Item{S.begin, S.end, S.parent, S.side, S.depth};
+    uint32_t res = S.res0, used = 0;
+    int maxd = 0;
+    bool first = true;
+    while (sp > 0) {
+        const Item it = stk[--sp];
+        const uint32_t n = it.e - it.b;
+        float box[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t q = it.b; q < it.e; ++q) {
+            const uint32_t p = idx[q];
+            for (int k = 0; k < 3; ++k) {
+                box[k] = fminf(box[k], g.box[6 * (size_t)p + k]);
+                box[3 + k] = fmaxf(box[3 + k], g.box[6 * (size_t)p + 3 + k]);
+                const float c = g.cent[3 * (size_t)p + k];
+                clo[k] = fminf(clo[k], c);
+                chi[k] = fmaxf(chi[k], c);
+            }
+        }
+        maxd = max(maxd, it.depth);
+        bool leaf = inst_leaf ? n == 1u : n <= 2u;
+        int best_axis = -1, best_bin = 0;
+        uint32_t best_left = 0;
+        float best = INFINITY, bclo = 0.0f, bscale = 0.0f;
+        if (!leaf) {
+            for (int k = 0; k < 3; ++k) {
+                const float ext = chi[k] - clo[k];
+                if (!(ext > 0.0f)) continue;
+                const float scale = (float)kBins / ext;
+                float bb[kBins][6];
+                uint32_t bc[kBins];
+                for (int j = 0; j < kBins; ++j) {
+                    bc[j] = 0;
+                    for (int c = 0; c < 3; ++c) { bb[j][c] = INFINITY; bb[j][3 + c] = -INFINITY; }
+                }
+                for (uint32_t q = it.b; q < it.e; ++q) {
+                    const uint32_t p = idx[q];
+                    const int bi = bin_of(g.cent[3 * (size_t)p + k], clo[k], scale);
+                    bc[bi]++;
+                    for (int c = 0; c < 3; ++c) {
+                        bb[bi][c] = fminf(bb[bi][c], g.box[6 * (size_t)p + c]);
+                        bb[bi][3 + c] = fmaxf(bb[bi][3 + c], g.box[6 * (size_t)p + 3 + c]);
+                    }
+                }
+                const int prev_axis = best_axis;
+                sah_axis(bb, bc, k, &best, &best_axis, &best_bin, &best_left);
+                if (best_axis != prev_axis) { bclo = clo[k]; bscale = scale; }
+            }
+            const float area = area6(box);
+            if (!inst_leaf && n <= max_leaf && (best_axis < 0 || area * (float)n <= best + 1.0f * area)) leaf = true;
+        }
+        if (leaf) {
+            const uint32_t payload = inst_leaf ? (prim_map[idx[it.b]] << 3) : ((it.b << 3) | (n - 1u));
+            const int ref = (int)(~payload);
+            if (it.parent >= 0) {
+                write_child(nodes, root_box, it.parent, it.side, box, ref);
+            } else {
+                // a root that is a single leaf: interior root whose second child never intersects
+                write_child(nodes, root_box, it.parent, it.side, box, 0);
+                BvhNode nd;
+                nd.a = make_float4(box[0], box[1], box[2], box[3]);
+                nd.b = make_float4(box[4], box[5], kFar, kFar);
+                nd.c = make_float4(kFar, kFar, kFar, kFar);
+                nd.d = make_int4(ref, kRefPop, 0, 0);
+                nodes[S.root_node] = nd;
+                ++used;
+            }
+            first = false;
+            continue;
+        }
+        if (!(first && S.root_node >= 0) && res >= S.res0 + (S.end - S.begin - 1u)) {
+            atomicOr(&info[2], kBuildErrRange);
+            break;
+        }
+        const int me = (first && S.root_node >= 0) ? S.root_node : (int)(res++);
+        first = false;
+        ++used;
+        write_child(nodes, root_box, it.parent, it.side, box, (int)node_base + me);
+        uint32_t mid;
+        if (best_axis < 0) {
+            mid = it.b + n / 2u;
+        } else {
+            uint32_t lo = it.b, hi = it.e;   // in-place partition: bins below best_bin first
+            while (lo < hi) {
+                const uint32_t p = idx[lo];
+                if (bin_of(g.cent[3 * (size_t)p + best_axis], bclo, bscale) < best_bin) {
+                    ++lo;
+                } else {
+                    --hi;
+                    idx[lo] = idx[hi];
+                    idx[hi] = p;
+                }
+            }
+            mid = lo;
+            if (mid == it.b || mid == it.e) mid = it.b + n / 2u;
+        }
+        if (sp + 2 > kSmallStack) {
+            atomicOr(&info[2], kBuildErrStack);
+            break;
+        }
+        stk[sp++] = Item{mid, it.e, me, 1, it.depth + 1};
+        stk[sp++] = Item{it.b, mid, me, 0, it.depth + 1};
+    }
+    atomicAdd(&info[0], used);
+    atomicMax(&info[1], (uint32_t)maxd);
+}
+
+// ---------------------------------------------------------------------------------------------
+// exclusive scans of uint32 / uint4: in-block inclusive scans, a scan of the block sums, a fix-up
+
+__device__ __forceinline__ uint32_t add_(uint32_t a, uint32_t b) { return a + b; }
+__device__ __forceinline__ uint4 add_(uint4 a, uint4 b) { return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ uint32_t sub_(uint32_t a, uint32_t b) { return a - b; }
+__device__ __forceinline__ uint4 sub_(uint4 a, uint4 b) { return make_uint4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+template <class T> __device__ __forceinline__ T zero_();
+template <> __device__ __forceinline__ uint32_t zero_<uint32_t>() { return 0u; }
+template <> __device__ __forceinline__ uint4 zero_<uint4>() { return make_uint4(0u, 0u, 0u, 0u); }
+
+template <class T>
+__device__ T block_scan_incl(T v, T* s) {   // inclusive scan over the kScanB threads
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanB; o <<= 1) {
+        const T u = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : zero_<T>();
+        __syncthreads();
+        s[threadIdx.x] = add_(s[threadIdx.x], u);
+        __syncthreads();
+    }
+    return s[threadIdx.x];
+}
+
+template <class T>
+__global__ void __launch_bounds__(kScanB) k_scan_blocks(const T* in, uint32_t n, T* out, T* bsum) {
+    __shared__ T s[kScanB];
+    const uint32_t i = blockIdx.x * kScanB + threadIdx.x;
+    const T incl = block_scan_incl(i < n ? in[i] : zero_<T>(), s);
+    if (i < n) out[i] = incl;
+    if (threadIdx.x == kScanB - 1) bsum[blockIdx.x] = incl;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kScanB) k_scan_sums(T* bsum, uint32_t nb, T* total) {
+    __shared__ T s[kScanB];
+    T carry = zero_<T>();
+    for (uint32_t base = 0; base < nb; base += kScanB) {
+        const uint32_t i = base + threadIdx.x;
+        const T incl = block_scan_incl(i < nb ? bsum[i] : zero_<T>(), s);
+        const T blk = s[kScanB - 1];
+        if (i < nb) bsum[i] = add_(carry, incl);   // inclusive prefix of the block sums
+        __syncthreads();
+        carry = add_(carry, blk);
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kScanB) k_scan_fix(const T* in, uint32_t n, T* out, const T* bsum_incl) {
+    const uint32_t i = blockIdx.x * kScanB + threadIdx.x;
+    if (i >= n) return;
+    const T before = blockIdx.x ? bsum_incl[blockIdx.x - 1] : zero_<T>();
+    out[i] = add_(sub_(out[i], in[i]), before);
+}
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaError_t need(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        release();
+        const size_t want = std::max<size_t>(n + n / 4, 16);
+        cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        else p = nullptr;
+        return e;
+    }
+    // grow keeping the first `keep` entries; the rest is zero
+    cudaError_t grow_keep(size_t n, size_t keep, cudaStream_t st) {
+        if (n <= cap) return cudaSuccess;
+        const size_t want = std::max<size_t>(n + n / 2, 16);
+        T* q = nullptr;
+        cudaError_t e = cudaMalloc((void**)&q, want * sizeof(T));
+        if (e != cudaSuccess) return e;
+        e = cudaMemsetAsync(q, 0, want * sizeof(T), st);
+        if (e == cudaSuccess && keep && p) e = cudaMemcpyAsync(q, p, keep * sizeof(T), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cudaFree(q);
+            return e;
+        }
+        release();
+        p = q;
+        cap = want;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+#define GK_TRY(x)                         \
+    do {                                  \
+        cudaError_t e_ = (x);             \
+        if (e_ != cudaSuccess) return e_; \
+    } while (0)
+
+}  // namespace
+
+struct GpuBvh {
+    DBuf<float> box, cent, root_box;
+    DBuf<uint32_t> idx, tmp, wtask[2], wbeg[2], wend[2], w0[2], wleft, wleft_scan, bsum32, tot32, info, map;
+    DBuf<uint4> cc, cc_scan, bsum4, tot4;
+    DBuf<int> bins, tb;
+    DBuf<BigTask> tasks[2];
+    DBuf<Split> split;
+    DBuf<SmallTask> small;
+    DBuf<BvhNode> nodes;
+    DBuf<MeshRange> ranges;
+    DBuf<GpuInstBox> inst;
+
+    ~GpuBvh() {
+        box.release(); cent.release(); root_box.release(); idx.release(); tmp.release();
+        for (int k = 0; k < 2; ++k) {
+            wtask[k].release(); wbeg[k].release(); wend[k].release(); w0[k].release(); tasks[k].release();
+        }
+        wleft.release(); wleft_scan.release(); bsum32.release(); tot32.release(); info.release(); map.release();
+        cc.release(); cc_scan.release(); bsum4.release(); tot4.release(); bins.release(); tb.release();
+        split.release(); small.release(); nodes.release(); ranges.release(); inst.release();
+    }
+
+    template <class T>
+    cudaError_t scan(const T* in, uint32_t n, T* out, DBuf<T>& bsum, DBuf<T>& tot, cudaStream_t st) {
+        const uint32_t nb = std::max<uint32_t>((n + kScanB - 1) / kScanB, 1u);
+        GK_TRY(bsum.need(nb));
+        GK_TRY(tot.need(1));
+        if (n) k_scan_blocks<T><<<nb, kScanB, 0, st>>>(in, n, out, bsum.p);
+        else GK_TRY(cudaMemsetAsync(bsum.p, 0, sizeof(T), st));
+        k_scan_sums<T><<<1, kScanB, 0, st>>>(bsum.p, nb, tot.p);
+        if (n) k_scan_fix<T><<<nb, kScanB, 0, st>>>(in, n, out, bsum.p);
+        return cudaGetLastError();
+    }
+
+    // Builds over the n primitives whose boxes and centroids are in box/cent, one tree per
+    // root range [root_begin[r], root_end[r]). Triangle leaves hold ranges of the final
+    // order (idx); instance leaves hold prim_map[primitive]. Refs are node_base + relative
+    // node index.
+    cudaError_t build(uint32_t n, const std::vector<uint32_t>& root_begin, const std::vector<uint32_t>& root_end,
+                      uint32_t max_leaf, bool inst_leaf, const uint32_t* prim_map, uint32_t node_base,
+                      GpuBvhResult* out, cudaStream_t st) {
+        const uint32_t nroots = (uint32_t)root_begin.size();
+        out->root_node.assign(nroots, -1);
+        out->node_count = 0;
+        out->nodes_used = 0;
+        out->depth = 0;
+        GK_TRY(idx.need(std::max<uint32_t>(n, 1u)));
+        GK_TRY(tmp.need(std::max<uint32_t>(n, 1u)));
+        GK_TRY(root_box.need(6 * (size_t)std::max<uint32_t>(nroots, 1u)));
+        GK_TRY(info.need(4));
+        GK_TRY(cudaMemsetAsync(info.p, 0, 16, st));
+        if (n) k_init_idx<<<(n + 255) / 256, 256, 0, st>>>(idx.p, n);
+        // roots: node slots [0, nroots); small roots reserve m - 1 slots after them
+        std::vector<float> rbox(6 * (size_t)std::max<uint32_t>(nroots, 1u));
+        for (uint32_t r = 0; r < nroots; ++r)
+            for (int k = 0; k < 3; ++k) { rbox[6 * r + k] = INFINITY; rbox[6 * r + 3 + k] = -INFINITY; }
+        std::vector<BigTask> big;
+        std::vector<SmallTask> smalls;
+        std::vector<uint32_t> hw[3], hw0;
+        uint32_t next_node = nroots;
+        for (uint32_t r = 0; r < nroots; ++r) {
+            const uint32_t b = root_begin[r], e = root_end[r];
+            if (e <= b) continue;
+            out->root_node[r] = (int)(node_base + r);
+            if (e - b > kSmall) {
+                hw0.push_back((uint32_t)hw[0].size());
+                for (uint32_t cb = b; cb < e; cb += kChunk) {
+                    hw[0].push_back((uint32_t)big.size());
+                    hw[1].push_back(cb);
+                    hw[2].push_back(std::min(cb + kChunk, e));
+                }
+                big.push_back(BigTask{(int)r, -1 - (int)r, 0, 0, b, e});
+            } else {
+                smalls.push_back(SmallTask{-1 - (int)r, 0, 0, (int)r, b, e, next_node, 0u});
+                next_node += e - b - 1u;
+            }
+        }
+        uint32_t ntask = (uint32_t)big.size(), nwork = (uint32_t)hw[0].size(), nsmall = (uint32_t)smalls.size();
+        GK_TRY(nodes.grow_keep(std::max<uint32_t>(next_node, 1u), 0, st));
+        GK_TRY(cudaMemsetAsync(nodes.p, 0, nodes.cap * sizeof(BvhNode), st));
+        GK_TRY(small.grow_keep(std::max<uint32_t>(nsmall, 1u), 0, st));
+        GK_TRY(cudaMemcpyAsync(root_box.p, rbox.data(), rbox.size() * 4, cudaMemcpyHostToDevice, st));
+        if (nsmall)
+            GK_TRY(cudaMemcpyAsync(small.p, smalls.data(), nsmall * sizeof(SmallTask), cudaMemcpyHostToDevice, st));
+        int cur = 0;
+        if (ntask) {
+            GK_TRY(tasks[0].need(ntask));
+            GK_TRY(w0[0].need(ntask));
+            GK_TRY(wtask[0].need(nwork));
+            GK_TRY(wbeg[0].need(nwork));
+            GK_TRY(wend[0].need(nwork));
+            GK_TRY(cudaMemcpyAsync(wtask[0].p, hw[0].data(), nwork * 4ull, cudaMemcpyHostToDevice, st));
+            GK_TRY(cudaMemcpyAsync(wbeg[0].p, hw[1].data(), nwork * 4ull, cudaMemcpyHostToDevice, st));
+            GK_TRY(cudaMemcpyAsync(wend[0].p, hw[2].data(), nwork * 4ull, cudaMemcpyHostToDevice, st));
+            GK_TRY(cudaMemcpyAsync(tasks[0].p, big.data(), ntask * sizeof(BigTask), cudaMemcpyHostToDevice, st));
+            GK_TRY(cudaMemcpyAsync(w0[0].p, hw0.data(), ntask * 4ull, cudaMemcpyHostToDevice, st));
+        }
+        GK_TRY(cudaStreamSynchronize(st));   // the host staging vectors are reused below
+        const Geo g{box.p, cent.p};
+        int rounds = 0;
+        while (ntask > 0) {
+            if (++rounds > 64) return cudaErrorInvalidValue;
+            const uint32_t gt = (ntask + 255) / 256;
+            GK_TRY(bins.need((size_t)ntask * kBinWords));
+            GK_TRY(tb.need((size_t)ntask * 12));
+            GK_TRY(split.need(ntask));
+            GK_TRY(wleft.need(nwork));
+            GK_TRY(wleft_scan.need(nwork));
+            GK_TRY(cc.need(ntask));
+            GK_TRY(cc_scan.need(ntask));
+            const uint32_t nclear = ntask * (uint32_t)(kBinWords + 12);
+            k_clear<<<std::min<uint32_t>((nclear + 255) / 256, 4096u), 256, 0, st>>>(bins.p, tb.p, ntask);
+            k_bounds<<<nwork, kBt, 0, st>>>(g, idx.p, wtask[cur].p, wbeg[cur].p, wend[cur].p, tb.p);
+            k_bin<<<nwork, kBt, 0, st>>>(g, idx.p, tb.p, wtask[cur].p, wbeg[cur].p, wend[cur].p, bins.p);
+            k_split<<<gt, 256, 0, st>>>(tasks[cur].p, ntask, bins.p, tb.p, split.p, nodes.p, root_box.p, node_base);
+            k_count_left<<<nwork, kBt, 0, st>>>(g, idx.p, split.p, tasks[cur].p, wtask[cur].p, wbeg[cur].p,
+                                                wend[cur].p, wleft.p);
+            GK_TRY(scan<uint32_t>(wleft.p, nwork, wleft_scan.p, bsum32, tot32, st));
+            k_scatter<<<nwork, kBt, 0, st>>>(g, idx.p, tmp.p, split.p, tasks[cur].p, wtask[cur].p, wbeg[cur].p,
+                                             wend[cur].p, wleft_scan.p, w0[cur].p, info.p);
+            k_copy_back<<<nwork, kBt, 0, st>>>(tmp.p, idx.p, wbeg[cur].p, wend[cur].p);
+            k_child_counts<<<gt, 256, 0, st>>>(tasks[cur].p, ntask, split.p, cc.p);
+            GK_TRY(scan<uint4>(cc.p, ntask, cc_scan.p, bsum4, tot4, st));
+            uint4 tot;
+            GK_TRY(cudaMemcpyAsync(&tot, tot4.p, sizeof(uint4), cudaMemcpyDeviceToHost, st));
+            GK_TRY(cudaStreamSynchronize(st));
+            const uint32_t nbig = tot.x, nwork_next = tot.y, nsm = tot.z, nres = tot.w;
+            const uint32_t node0 = next_node, res0 = next_node + nbig;
+            GK_TRY(nodes.grow_keep(next_node + nbig + nres, next_node, st));
+            next_node += nbig + nres;
+            GK_TRY(small.grow_keep(nsmall + nsm, nsmall, st));
+            const int nx = cur ^ 1;
+            GK_TRY(tasks[nx].need(std::max<uint32_t>(nbig, 1u)));
+            GK_TRY(w0[nx].need(std::max<uint32_t>(nbig, 1u)));
+            GK_TRY(wtask[nx].need(std::max<uint32_t>(nwork_next, 1u)));
+            GK_TRY(wbeg[nx].need(std::max<uint32_t>(nwork_next, 1u)));
+            GK_TRY(wend[nx].need(std::max<uint32_t>(nwork_next, 1u)));
+            k_emit<<<gt, 256, 0, st>>>(tasks[cur].p, ntask, split.p, cc_scan.p, node0, res0, nsmall, tasks[nx].p,
+                                       wtask[nx].p, wbeg[nx].p, wend[nx].p, w0[nx].p, small.p);
+            GK_TRY(cudaGetLastError());
+            out->nodes_used += ntask;
+            nsmall += nsm;
+            ntask = nbig;
+            nwork = nwork_next;
+            cur = nx;
+        }
+        if (nsmall)
+            k_small<<<(nsmall + 127) / 128, 128, 0, st>>>(g, idx.p, small.p, nsmall, nodes.p, root_box.p, max_leaf,
+                                                          inst_leaf ? 1 : 0, prim_map, node_base, info.p);
+        GK_TRY(cudaGetLastError());
+        uint32_t hinfo[4];
+        GK_TRY(cudaMemcpyAsync(hinfo, info.p, 16, cudaMemcpyDeviceToHost, st));
+        GK_TRY(cudaStreamSynchronize(st));
+        if (hinfo[2]) return cudaErrorInvalidValue;
+        out->nodes_used += hinfo[0];
+        out->depth = std::max<int>(rounds, (int)hinfo[1]);
+        out->node_count = next_node;
+        out->nodes = nodes.p;
+        out->order = idx.p;
+        out->root_box = root_box.p;
+        return cudaSuccess;
+    }
+};
+
+GpuBvh* gpu_bvh_new() { return new (std::nothrow) GpuBvh(); }
+void gpu_bvh_free(GpuBvh* b) { delete b; }
+
+cudaError_t gpu_bvh_build_meshes(GpuBvh* B, const float4* pos, const uint32_t* ind, const GkrtMesh* meshes,
+                                 uint32_t nmesh, uint32_t node_base, float4* tris_out, GpuBvhResult* out,
+                                 cudaStream_t st) {
+    std::vector<MeshRange> mr(std::max<uint32_t>(nmesh, 1u), MeshRange{0u, 0u, 0u, 0u});
+    std::vector<uint32_t> rb(nmesh), re(nmesh);
+    uint32_t ntri = 0;
+    for (uint32_t m = 0; m < nmesh; ++m) {
+        mr[m] = MeshRange{ntri, meshes[m].index_offset, meshes[m].vertex_offset, 0u};
+        rb[m] = ntri;
+        ntri += meshes[m].index_count / 3u;
+        re[m] = ntri;
+    }
+    GK_TRY(B->ranges.need(mr.size()));
+    GK_TRY(cudaMemcpyAsync(B->ranges.p, mr.data(), mr.size() * sizeof(MeshRange), cudaMemcpyHostToDevice, st));
+    GK_TRY(B->box.need(6 * (size_t)std::max<uint32_t>(ntri, 1u)));
+    GK_TRY(B->cent.need(3 * (size_t)std::max<uint32_t>(ntri, 1u)));
+    const uint32_t nmr = std::max<uint32_t>(nmesh, 1u);
+    if (ntri) k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(pos, ind, B->ranges.p, nmr, ntri, B->box.p, B->cent.p);
+    GK_TRY(cudaGetLastError());
+    GK_TRY(B->build(ntri, rb, re, 4, false, nullptr, node_base, out, st));
+    if (ntri) k_gather_tris<<<(ntri + 255) / 256, 256, 0, st>>>(pos, ind, B->ranges.p, nmr, B->idx.p, ntri, tris_out);
+    GK_TRY(cudaGetLastError());
+    return cudaStreamSynchronize(st);
+}
+
+cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
+                                    uint32_t node_base, GpuBvhResult* out, cudaStream_t st) {
+    GK_TRY(B->inst.need(std::max<uint32_t>(n, 1u)));
+    GK_TRY(B->map.need(std::max<uint32_t>(n, 1u)));
+    std::vector<uint32_t> map(n);
+    for (uint32_t i = 0; i < n; ++i) map[i] = inst_host[i].inst;
+    if (n) {
+        GK_TRY(cudaMemcpyAsync(B->inst.p, inst_host, n * sizeof(GpuInstBox), cudaMemcpyHostToDevice, st));
+        GK_TRY(cudaMemcpyAsync(B->map.p, map.data(), n * 4ull, cudaMemcpyHostToDevice, st));
+    }
+    GK_TRY(B->box.need(6 * (size_t)std::max<uint32_t>(n, 1u)));
+    GK_TRY(B->cent.need(3 * (size_t)std::max<uint32_t>(n, 1u)));
+    if (n) k_inst_boxes<<<(n + 255) / 256, 256, 0, st>>>(B->inst.p, n, mesh_box, B->box.p, B->cent.p);
+    GK_TRY(cudaGetLastError());
+    const std::vector<uint32_t> rb(1, 0u), re(1, n);
+    GK_TRY(B->build(n, rb, re, 1, true, B->map.p, node_base, out, st));
+    return cudaStreamSynchronize(st);
+}
+
+}  // namespace gk

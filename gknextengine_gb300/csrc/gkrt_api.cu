@@ -5,6 +5,7 @@
 // load a scene, build acceleration structures, then per frame: rt pass -> reproject pass
 // -> compose pass -> history hand-over. Every entry point returns a status code; no
 // exception crosses the boundary.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -45,16 +46,21 @@ struct GkrtContext {
     uint32_t* d_cubes = nullptr;
     uint32_t* d_voxels = nullptr;
 
-    // acceleration structures
-    std::vector<BvhNode> blas_nodes;
+    // acceleration structures: d_nodes holds the mesh-level nodes [0, blas_node_count) and
+    // the instance-level nodes after them
+    bool host_build = false;          // GKRT_BUILD_ON_HOST
+    GpuBvh* builder = nullptr;
+    uint32_t blas_node_count = 0, blas_nodes_used = 0;
     std::vector<int> blas_root;
     std::vector<float> blas_box;      // 6 per mesh
+    float* d_blas_box = nullptr;
     BvhNode* d_nodes = nullptr;
     size_t d_nodes_cap = 0;
     float4* d_tris = nullptr;
     int tlas_root = -1;
     uint32_t tlas_nodes = 0;
     bool blas_ready = false, tlas_ready = false;
+    uint32_t inst_cap = 0;            // instance arrays allocated for this many instances
 
     unsigned long long* d_counters = nullptr;   // see flush_counters: 5 per-pass slots + total rays
     uint32_t* d_error = nullptr;
@@ -121,13 +127,15 @@ void free_images(GkrtContext* c) {
 void free_scene(GkrtContext* c) {
     dfree(c->d_pos); dfree(c->d_nrm); dfree(c->d_slot); dfree(c->d_idx); dfree(c->d_mat);
     dfree(c->d_inst_mat); dfree(c->d_inst_prev); dfree(c->d_inst); dfree(c->d_cubes); dfree(c->d_voxels);
-    dfree(c->d_nodes); dfree(c->d_tris);
+    dfree(c->d_nodes); dfree(c->d_tris); dfree(c->d_blas_box);
     c->d_nodes_cap = 0;
+    c->inst_cap = 0;
     c->has_scene = false;
     c->blas_ready = c->tlas_ready = false;
     c->tlas_root = -1;
+    c->blas_node_count = c->blas_nodes_used = 0;
     c->meshes.clear(); c->inst.clear(); c->pos_host.clear(); c->idx_host.clear();
-    c->blas_nodes.clear(); c->blas_root.clear(); c->blas_box.clear();
+    c->blas_root.clear(); c->blas_box.clear();
 }
 
 template <class T>
@@ -165,6 +173,13 @@ int validate_instances(GkrtContext* ctx, const GkrtInstance* in, uint32_t n, uin
     return GKRT_OK;
 }
 
+template <class T>
+int copy_in(GkrtContext* ctx, T* dst, const void* src, size_t bytes) {
+    if (bytes) GK_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+    return GKRT_OK;
+}
+
+// Instance tables of the kernels; allocated once per scene (updates keep the count).
 int upload_instances(GkrtContext* ctx) {
     const uint32_t n = (uint32_t)ctx->inst.size();
     std::vector<uint32_t> mats(16 * (size_t)n);
@@ -182,15 +197,80 @@ int upload_instances(GkrtContext* ctx) {
         di[i].instance_id = s.instance_id;
     }
     int rc;
-    if ((rc = upload(ctx, ctx->d_inst_mat, mats.data(), mats.size() * 4)) != GKRT_OK) return rc;
-    if ((rc = upload(ctx, ctx->d_inst_prev, prev.data(), prev.size() * 4)) != GKRT_OK) return rc;
-    if ((rc = upload(ctx, ctx->d_inst, di.data(), di.size() * sizeof(DevInst))) != GKRT_OK) return rc;
+    if (ctx->inst_cap < n || !ctx->d_inst) {
+        if ((rc = upload(ctx, ctx->d_inst_mat, mats.data(), mats.size() * 4)) != GKRT_OK) return rc;
+        if ((rc = upload(ctx, ctx->d_inst_prev, prev.data(), prev.size() * 4)) != GKRT_OK) return rc;
+        if ((rc = upload(ctx, ctx->d_inst, di.data(), di.size() * sizeof(DevInst))) != GKRT_OK) return rc;
+        ctx->inst_cap = n;
+        return GKRT_OK;
+    }
+    if ((rc = copy_in(ctx, ctx->d_inst_mat, mats.data(), mats.size() * 4)) != GKRT_OK) return rc;
+    if ((rc = copy_in(ctx, ctx->d_inst_prev, prev.data(), prev.size() * 4)) != GKRT_OK) return rc;
+    return copy_in(ctx, ctx->d_inst, di.data(), di.size() * sizeof(DevInst));
+}
+
+// d_nodes capacity for `total` nodes, keeping the mesh-level part.
+int ensure_node_cap(GkrtContext* ctx, size_t total) {
+    if (total <= ctx->d_nodes_cap && ctx->d_nodes) return GKRT_OK;
+    const size_t cap = std::max<size_t>(total + total / 4, 16);
+    BvhNode* q = nullptr;
+    GK_CUDA(cudaMalloc((void**)&q, cap * sizeof(BvhNode)));
+    cudaError_t e = cudaSuccess;
+    if (ctx->d_nodes && ctx->blas_node_count)
+        e = cudaMemcpy(q, ctx->d_nodes, (size_t)ctx->blas_node_count * sizeof(BvhNode), cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(q);
+        return cuda_fail(ctx, e, "cudaMemcpy(nodes)");
+    }
+    dfree(ctx->d_nodes);
+    ctx->d_nodes = q;
+    ctx->d_nodes_cap = cap;
     return GKRT_OK;
 }
 
-int build_blas(GkrtContext* ctx) {
+int get_builder(GkrtContext* ctx) {
+    if (!ctx->builder) ctx->builder = gpu_bvh_new();
+    return ctx->builder ? GKRT_OK : fail(ctx, GKRT_ERR_OOM, "BVH builder");
+}
+
+int finish_blas(GkrtContext* ctx) {
+    int rc = upload(ctx, ctx->d_blas_box, ctx->blas_box.data(), ctx->blas_box.size() * 4);
+    if (rc != GKRT_OK) return rc;
+    ctx->blas_ready = true;
+    ctx->tlas_ready = false;
+    return GKRT_OK;
+}
+
+// Mesh-level trees on the GPU: one build over every mesh's triangles.
+int build_blas_gpu(GkrtContext* ctx, cudaStream_t st) {
     const uint32_t nm = (uint32_t)ctx->meshes.size();
-    ctx->blas_nodes.clear();
+    ctx->blas_root.assign(nm, -1);
+    ctx->blas_box.assign(6 * (size_t)nm, 0.0f);
+    size_t ntri = 0;
+    for (const GkrtMesh& m : ctx->meshes) ntri += m.index_count / 3;
+    dfree(ctx->d_tris);
+    if (ntri) GK_CUDA(cudaMalloc((void**)&ctx->d_tris, 3 * ntri * sizeof(float4)));
+    int rc;
+    if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
+    GpuBvhResult r;
+    GK_CUDA(gpu_bvh_build_meshes(ctx->builder, ctx->d_pos, ctx->d_idx, ctx->meshes.data(), nm, 0, ctx->d_tris, &r, st));
+    if (r.depth > kStackSize - 24) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "mesh BVH deeper than the traversal stack allows");
+    ctx->blas_root = r.root_node;
+    if (nm) GK_CUDA(cudaMemcpy(ctx->blas_box.data(), r.root_box, 6 * (size_t)nm * 4, cudaMemcpyDeviceToHost));
+    ctx->blas_node_count = r.node_count;
+    ctx->blas_nodes_used = r.nodes_used;
+    dfree(ctx->d_nodes);
+    ctx->d_nodes_cap = 0;
+    if ((rc = ensure_node_cap(ctx, (size_t)r.node_count + 2 * ctx->inst.size() + 2)) != GKRT_OK) return rc;
+    if (r.node_count)
+        GK_CUDA(cudaMemcpy(ctx->d_nodes, r.nodes, (size_t)r.node_count * sizeof(BvhNode), cudaMemcpyDeviceToDevice));
+    return finish_blas(ctx);
+}
+
+// Mesh-level trees on the host (GKRT_BUILD_ON_HOST).
+int build_blas_host(GkrtContext* ctx) {
+    const uint32_t nm = (uint32_t)ctx->meshes.size();
+    std::vector<BvhNode> nodes;
     ctx->blas_root.assign(nm, -1);
     ctx->blas_box.assign(6 * (size_t)nm, 0.0f);
     std::vector<float4> tris;
@@ -216,11 +296,11 @@ int build_blas(GkrtContext* ctx) {
         std::memcpy(&ctx->blas_box[6 * (size_t)mi], rb, sizeof(rb));
         if (nt == 0) continue;
         HostBvh hb;
-        build_bvh_host(boxes.data(), nt, 4, (uint32_t)ctx->blas_nodes.size(), (uint32_t)(tris.size() / 3), false, hb);
+        build_bvh_host(boxes.data(), nt, 4, (uint32_t)nodes.size(), (uint32_t)(tris.size() / 3), false, hb);
         if (hb.depth > kStackSize - 24)
             return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "mesh BVH deeper than the traversal stack allows");
         ctx->blas_root[mi] = hb.root;
-        ctx->blas_nodes.insert(ctx->blas_nodes.end(), hb.nodes.begin(), hb.nodes.end());
+        nodes.insert(nodes.end(), hb.nodes.begin(), hb.nodes.end());
         for (uint32_t k = 0; k < nt; ++k) {
             const uint32_t prim = hb.order[k];
             for (int v = 0; v < 3; ++v) {
@@ -233,12 +313,49 @@ int build_blas(GkrtContext* ctx) {
     }
     int rc = upload(ctx, ctx->d_tris, tris.data(), tris.size() * sizeof(float4));
     if (rc != GKRT_OK) return rc;
-    ctx->blas_ready = true;
-    return GKRT_OK;
+    ctx->blas_node_count = ctx->blas_nodes_used = (uint32_t)nodes.size();
+    dfree(ctx->d_nodes);
+    ctx->d_nodes_cap = 0;
+    if ((rc = ensure_node_cap(ctx, nodes.size() + 2 * ctx->inst.size() + 2)) != GKRT_OK) return rc;
+    if ((rc = copy_in(ctx, ctx->d_nodes, nodes.data(), nodes.size() * sizeof(BvhNode))) != GKRT_OK) return rc;
+    return finish_blas(ctx);
 }
 
-int build_tlas(GkrtContext* ctx) {
+int build_blas(GkrtContext* ctx, cudaStream_t st) {
+    return ctx->host_build ? build_blas_host(ctx) : build_blas_gpu(ctx, st);
+}
+
+int build_tlas(GkrtContext* ctx, cudaStream_t st) {
     const uint32_t n = (uint32_t)ctx->inst.size();
+    const uint32_t base = ctx->blas_node_count;
+    int rc;
+    if (!ctx->host_build) {
+        std::vector<GpuInstBox> ib;
+        ib.reserve(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            const GkrtInstance& in = ctx->inst[i];
+            if (!in.visible || ctx->blas_root[in.mesh_id] < 0) continue;
+            GpuInstBox b;
+            std::memcpy(b.world, in.world, 48);
+            b.mesh = in.mesh_id;
+            b.inst = i;
+            b.pad0 = b.pad1 = 0;
+            ib.push_back(b);
+        }
+        if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
+        GpuBvhResult r;
+        GK_CUDA(gpu_bvh_build_instances(ctx->builder, ib.data(), (uint32_t)ib.size(), ctx->d_blas_box, base, &r, st));
+        if (r.depth > 24 + 8) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "instance BVH too deep");
+        if ((rc = ensure_node_cap(ctx, (size_t)base + r.node_count)) != GKRT_OK) return rc;
+        if (r.node_count)
+            GK_CUDA(cudaMemcpyAsync(ctx->d_nodes + base, r.nodes, (size_t)r.node_count * sizeof(BvhNode),
+                                    cudaMemcpyDeviceToDevice, st));
+        GK_CUDA(cudaStreamSynchronize(st));
+        ctx->tlas_root = ib.empty() ? -1 : r.root_node[0];
+        ctx->tlas_nodes = r.nodes_used;
+        ctx->tlas_ready = true;
+        return upload_instances(ctx);
+    }
     std::vector<float> boxes;
     std::vector<uint32_t> map;
     for (uint32_t i = 0; i < n; ++i) {
@@ -267,9 +384,7 @@ int build_tlas(GkrtContext* ctx) {
         }
         map.push_back(i);
     }
-    // boxes were pushed as lo xyz then hi xyz per instance
     HostBvh hb;
-    const uint32_t base = (uint32_t)ctx->blas_nodes.size();
     build_bvh_host(boxes.data(), (uint32_t)map.size(), 1, base, 0, true, hb);
     // leaf payloads hold positions in `map`; rewrite them to instance indices
     for (auto& nd : hb.nodes) {
@@ -282,41 +397,23 @@ int build_tlas(GkrtContext* ctx) {
             }
     }
     if (hb.depth > 24 + 8) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "instance BVH too deep");
-    const size_t total = ctx->blas_nodes.size() + hb.nodes.size();
-    if (total > ctx->d_nodes_cap) {
-        dfree(ctx->d_nodes);
-        cudaError_t e = cudaMalloc((void**)&ctx->d_nodes, std::max<size_t>(total, 1) * sizeof(BvhNode));
-        if (e != cudaSuccess) { ctx->d_nodes_cap = 0; return cuda_fail(ctx, e, "cudaMalloc(nodes)"); }
-        ctx->d_nodes_cap = std::max<size_t>(total, 1);
-        if (!ctx->blas_nodes.empty()) {
-            e = cudaMemcpy(ctx->d_nodes, ctx->blas_nodes.data(), ctx->blas_nodes.size() * sizeof(BvhNode),
-                           cudaMemcpyHostToDevice);
-            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(blas nodes)");
-        }
-    }
-    if (!hb.nodes.empty()) {
-        cudaError_t e = cudaMemcpy(ctx->d_nodes + base, hb.nodes.data(), hb.nodes.size() * sizeof(BvhNode),
-                                   cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(tlas nodes)");
-    }
+    if ((rc = ensure_node_cap(ctx, (size_t)base + hb.nodes.size())) != GKRT_OK) return rc;
+    if ((rc = copy_in(ctx, ctx->d_nodes + base, hb.nodes.data(), hb.nodes.size() * sizeof(BvhNode))) != GKRT_OK)
+        return rc;
     ctx->tlas_root = map.empty() ? -1 : hb.root;
     ctx->tlas_nodes = (uint32_t)hb.nodes.size();
     ctx->tlas_ready = true;
     return upload_instances(ctx);
 }
 
-int ensure_bvh(GkrtContext* ctx, uint32_t flags) {
+int ensure_bvh(GkrtContext* ctx, uint32_t flags, cudaStream_t st) {
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
     int rc;
     if ((flags & GKRT_BUILD_BLAS) || !ctx->blas_ready) {
-        if ((rc = build_blas(ctx)) != GKRT_OK) return rc;
-        // nodes must be re-uploaded with the new BLAS part
-        dfree(ctx->d_nodes);
-        ctx->d_nodes_cap = 0;
-        ctx->tlas_ready = false;
+        if ((rc = build_blas(ctx, st)) != GKRT_OK) return rc;
     }
     if ((flags & GKRT_BUILD_TLAS) || !ctx->tlas_ready) {
-        if ((rc = build_tlas(ctx)) != GKRT_OK) return rc;
+        if ((rc = build_tlas(ctx, st)) != GKRT_OK) return rc;
     }
     return GKRT_OK;
 }
@@ -420,6 +517,8 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     cudaDeviceSynchronize();
     free_images(ctx);
     free_scene(ctx);
+    gpu_bvh_free(ctx->builder);
+    ctx->builder = nullptr;
     dfree(ctx->d_counters);
     dfree(ctx->d_error);
     dfree(ctx->d_work);
@@ -505,11 +604,10 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
         if ((rc = upload(ctx, ctx->d_voxels, d->probe_voxels, n * 4 * 4)) != GKRT_OK) return rc;
     }
     ctx->has_scene = true;
-    return ensure_bvh(ctx, GKRT_BUILD_ALL);
+    return ensure_bvh(ctx, GKRT_BUILD_ALL, (cudaStream_t)0);
 }
 
 int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count, void* stream) {
-    (void)stream;
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
     if (!instances || count != ctx->inst.size())
@@ -518,14 +616,20 @@ int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
     if (rc != GKRT_OK) return rc;
     cudaSetDevice(ctx->device);
     ctx->inst.assign(instances, instances + count);
-    return build_tlas(ctx);
+    if (!ctx->blas_ready) return ensure_bvh(ctx, 0, (cudaStream_t)stream);
+    return build_tlas(ctx, (cudaStream_t)stream);
 }
 
 int gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream) {
-    (void)stream;
     if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (flags & ~(GKRT_BUILD_ALL | GKRT_BUILD_ON_HOST)) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown build flags");
     cudaSetDevice(ctx->device);
-    return ensure_bvh(ctx, flags);
+    const bool host = (flags & GKRT_BUILD_ON_HOST) != 0;
+    if (host != ctx->host_build) {
+        ctx->host_build = host;
+        flags |= GKRT_BUILD_ALL;   // both levels come from the same builder
+    }
+    return ensure_bvh(ctx, flags, (cudaStream_t)stream);
 }
 
 int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
@@ -535,8 +639,8 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     if (fc->nee_mode != GKRT_NEE_REFERENCE)
         return fail(ctx, GKRT_ERR_UNSUPPORTED, "nee_mode not supported by this build");
     cudaSetDevice(ctx->device);
-    if ((rc = ensure_bvh(ctx, 0)) != GKRT_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
     ShadeScene sc;
     sc.S = scene_view(ctx);
     sc.normals = ctx->d_nrm;
@@ -719,9 +823,9 @@ int gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32
     if (count && (!rays || !hits)) return fail(ctx, GKRT_ERR_INVALID_ARG, "null ray or hit buffer");
     if (mode > GKRT_TRACE_ANY) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown trace mode");
     cudaSetDevice(ctx->device);
-    int rc = ensure_bvh(ctx, 0);
-    if (rc != GKRT_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    int rc = ensure_bvh(ctx, 0, st);
+    if (rc != GKRT_OK) return rc;
     GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
     GK_CUDA(gkrt_launch_trace_rays(scene_view(ctx), rays, hits, count, mode, ctx->d_counters, st));
     return GKRT_OK;
@@ -743,7 +847,7 @@ int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     out->triangle_tests = c[4];
     out->rays_total = c[5];
     out->device_error = errw;
-    out->bvh_nodes = (uint32_t)ctx->blas_nodes.size();
+    out->bvh_nodes = ctx->blas_nodes_used;
     out->tlas_nodes = ctx->tlas_nodes;
     out->bvh_leaf_tris = ctx->nidx / 3;
     return GKRT_OK;

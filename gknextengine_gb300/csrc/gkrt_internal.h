@@ -55,6 +55,33 @@ struct HostBvh {
 // global node array; prim_base: global index of order[0] (leaf refs are global).
 void build_bvh_host(const float* boxes, uint32_t n, uint32_t max_leaf, uint32_t node_base, uint32_t prim_base,
                     bool leaf_is_instance, HostBvh& out);
+
+// GPU builder (bvh_gpu.cu): same split rule and node layout, device scratch reused across
+// builds. Results stay in the builder's memory until its next build.
+struct GpuBvh;
+struct GpuInstBox {                 // one visible instance for the instance-level build
+    float world[12];
+    uint32_t mesh, inst, pad0, pad1;
+};
+struct GpuBvhResult {
+    const BvhNode* nodes = nullptr; // node_count slots; refs already include node_base
+    uint32_t node_count = 0;        // slots, including reserved ones left unused (zero)
+    uint32_t nodes_used = 0;
+    int depth = 0;
+    const uint32_t* order = nullptr;   // leaf order of the primitives
+    const float* root_box = nullptr;   // 6 per root
+    std::vector<int> root_node;        // absolute node index per root, -1 for an empty root
+};
+GpuBvh* gpu_bvh_new();
+void gpu_bvh_free(GpuBvh* b);
+// One tree per mesh over all meshes' triangles; writes the triangles in leaf order to
+// tris_out (3 float4 per triangle).
+cudaError_t gpu_bvh_build_meshes(GpuBvh* b, const float4* pos, const uint32_t* indices, const GkrtMesh* meshes,
+                                 uint32_t nmesh, uint32_t node_base, float4* tris_out, GpuBvhResult* out,
+                                 cudaStream_t st);
+// Instance-level tree; mesh_box: device, 6 floats per mesh.
+cudaError_t gpu_bvh_build_instances(GpuBvh* b, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
+                                    uint32_t node_base, GpuBvhResult* out, cudaStream_t st);
 }  // namespace gk
 
 cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,

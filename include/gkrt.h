@@ -270,6 +270,10 @@ int  gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances
 #define GKRT_BUILD_BLAS 1u
 #define GKRT_BUILD_TLAS 2u
 #define GKRT_BUILD_ALL  3u
+/* Build on the host CPU instead of the GPU builder. The choice sticks for later builds
+ * (including the instance-level rebuild of gkrt_scene_update_instances) until a call
+ * without the flag. Both builders use the same split rule; trace results are identical. */
+#define GKRT_BUILD_ON_HOST 4u
 int  gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream);
 
 /* Passes (PathTracingRenderer::Render, PathTracingRenderer.cpp:104-218). */
