@@ -40,12 +40,34 @@ HIT_FETCH_BYTES = 3 * 4 + 3 * 16 + 64 + 64 + 48   # indices, normals, material, 
 NODE_BYTES, TRI_BYTES, RAY_BYTES = 64, 48, 32
 
 
+WORKLOAD = "bricks"
+
+
 def workload_config():
-    return {"workload": "bricks-1.03M-tris 1920x1080 1spp depth8 orbit0.5deg/frame reproject+JBF",
+    if WORKLOAD == "city":
+        return {"workload": f"city-10.48M-tris {W_}x{H_} 1spp depth8 alias-table-NEE moving-spheres "
+                            "per-frame-instance-rebuild reproject+JBF",
+                "triangles": 10480002, "instances": 25001, "emissive_triangles": 10240, "width": W_, "height": H_,
+                "spp": 1, "max_depth": 8,
+                "l2": "per-frame image working set 2 GB > L2 (129 MB)",
+                "per_frame": "gkrt_scene_update_instances (instance-level BVH rebuild on the GPU + emitter "
+                             "alias table) inside the timed frame",
+                "data": "synthetic seeded scene (numpy default_rng seed 3)"}
+    return {"workload": f"bricks-1.03M-tris {W_}x{H_} 1spp depth8 orbit0.5deg/frame reproject+JBF",
             "triangles": 1032194, "instances": 4097, "width": W_, "height": H_, "spp": 1, "max_depth": 8,
             "l2": "per-frame image working set 0.5 GB > L2 (129 MB); the 0.6 MB BVH stays L2-resident as "
                   "in steady-state rendering",
             "data": "synthetic seeded scene (numpy default_rng seed 2)"}
+
+
+def load_workload():
+    """(scene, camera, settings, per-frame instance function or None)."""
+    from gknextengine_gb300 import scenes
+    if WORKLOAD == "city":
+        sc, cam, st, motion = scenes.city(width=W_, height=H_)
+        return sc, cam, st, motion.instances
+    sc, cam, st = scenes.bricks()
+    return sc, cam, st, None
 
 
 def dist_env():
@@ -175,6 +197,70 @@ def run_reference(args):
     return 0
 
 
+def relmse(x, y):
+    """mean over pixels and RGB of (x - y)^2 / (y^2 + 1e-2), linear radiance."""
+    import numpy as np
+    d = x[..., :3].astype(np.float64) - y[..., :3]
+    return float(np.mean(d * d / (y[..., :3].astype(np.float64) ** 2 + 1e-2)))
+
+
+def relmse_measure(device: int, W: int = 960, H: int = 540, ref_spp: int = 4096, temporal: int = 16):
+    """Denoised RelMSE against a 4096-spp reference on the Cornell scene (static camera,
+    no TAA jitter). The reference is the mean of 4096 independent 1-spp trace passes,
+    remodulated like the compose pass (diffuse x albedo + specular). Compared: the raw
+    1-spp image, the reference's JBF and the a-trous filter on one frame, and the same after
+    `temporal` frames of reprojection."""
+    import numpy as np
+    import torch
+    from gknextengine_gb300 import abi, camera, scenes
+    from gknextengine_gb300.renderer import PathTracingRenderer
+    sc, cam, st = scenes.cornell()
+    st.taa = False
+    out = {"scene": f"cornell {W}x{H}", "reference_spp": ref_spp, "metric": "mean (x-y)^2/(y^2+1e-2) over px, RGB"}
+    with PathTracingRenderer(device) as r:
+        r.load_scene(sc)
+        r.create_swap_chain(W, H)
+        fb = camera.FrameBuilder(W, H, st)
+        t0 = time.perf_counter()
+        acc_d = torch.zeros((H, r.image_view(abi.IMG_SINGLE_DIFFUSE).pitch_bytes // 16, 4), device="cuda")
+        acc_s = torch.zeros_like(acc_d)
+        vd = r.image_view(abi.IMG_SINGLE_DIFFUSE)
+        vs = r.image_view(abi.IMG_SINGLE_SPECULAR)
+        n = H * (vd.pitch_bytes // 16) * 4
+        for f in range(ref_spp):
+            fc = fb.build(cam, 100000 + f)
+            r.trace_pass(fc)
+            d = torch.as_tensor(_device_f32(vd.device_ptr, n)).view(H, -1, 4)
+            s_ = torch.as_tensor(_device_f32(vs.device_ptr, n)).view(H, -1, 4)
+            acc_d += d
+            acc_s += s_
+        torch.cuda.synchronize()
+        out["reference_seconds"] = time.perf_counter() - t0
+        alb = r.read_image(abi.IMG_ALBEDO)
+        ref = (acc_d[:, :W].cpu().numpy() / ref_spp) * alb + acc_s[:, :W].cpu().numpy() / ref_spp
+        for name, den, bf in (("raw", abi.DENOISE_JBF, 0), ("jbf", abi.DENOISE_JBF, 5),
+                              ("atrous", abi.DENOISE_ATROUS, 5)):
+            st.denoiser, st.bf_size = den, bf
+            # one frame on its own (history weight 0), then the steady state of the temporal
+            # blend (1/16 per frame) after 8 x 16 frames, when the zeroed start no longer counts
+            for tf, frames, key in ((1, 1, f"{name}_1spp"), (temporal, 8 * temporal, f"{name}_temporal")):
+                st.temporal_frames = tf
+                fbn = camera.FrameBuilder(W, H, st)
+                r.create_swap_chain(W, H)
+                for f in range(frames):
+                    r.render(fbn.build(cam, f))
+                out[key] = relmse(r.read_image(abi.IMG_DENOISED_LINEAR), ref)
+    return out
+
+
+def _device_f32(ptr, n):
+    """A float32 view of n floats of device memory (no copy)."""
+    import torch
+    class _A:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (ptr, False), "version": 3}
+    return torch.as_tensor(_A(), device="cuda")
+
+
 def run_gkrt(args):
     import numpy as np
     import torch
@@ -187,14 +273,26 @@ def run_gkrt(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    sc, cam, st = scenes.bricks()
+    sc, cam, st, frame_instances = load_workload()
     r = PathTracingRenderer(local)
+    t0 = time.perf_counter()
     r.load_scene(sc)
+    load_s = time.perf_counter() - t0
     r.create_swap_chain(W_, H_)
     stream = torch.cuda.Stream()
+    # BVH build times (GPU builder, host clock around the synchronous calls)
+    r.build_bvh(abi.BUILD_ALL, stream)
+    t0 = time.perf_counter()
+    r.build_bvh(abi.BUILD_ALL, stream)
+    build_all_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    r.update_instances(sc.instances if frame_instances is None else frame_instances(0), stream)
+    build_inst_ms = (time.perf_counter() - t0) * 1e3
+    orbit = 0.5 if frame_instances is None else 0.25
     fb = camera.FrameBuilder(W_, H_, st)
     K, Wm = args.steps, args.warmup
-    fcs = [fb.build(cam.orbit(0.5 * i), i) for i in range(Wm + K)]
+    fcs = [fb.build(cam.orbit(orbit * i), i) for i in range(Wm + K)]
+    insts = [frame_instances(i) for i in range(Wm + K)] if frame_instances is not None else None
 
     def barrier():
         if world > 1:
@@ -202,17 +300,22 @@ def run_gkrt(args):
 
     # ---- warm-up, then K timed frames (device-resident inputs) ----
     for i in range(Wm):
+        if insts is not None:
+            r.update_instances(insts[i], stream)
         r.render(fcs[i], stream)
     r.synchronize(stream)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    rays0 = r.stats().rays_total
+    s0 = r.stats()
+    rays0, bl0 = s0.rays_total, s0.build_launches
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk, torch.cuda.stream(stream):
         start.record(stream)
         for k in range(K):
             fc = fcs[Wm + k]
+            if insts is not None:
+                r.update_instances(insts[Wm + k], stream)
             ev[k][0].record(stream)
             r.trace_pass(fc, stream)
             ev[k][1].record(stream)
@@ -224,6 +327,7 @@ def run_gkrt(args):
     barrier()
     st_last = r.stats()
     rays = st_last.rays_total - rays0
+    build_launches = st_last.build_launches - bl0
     ms_total = start.elapsed_time(end)
     trace_ms = [a.elapsed_time(b) for a, b in ev]
     if world > 1:
@@ -254,7 +358,9 @@ def run_gkrt(args):
     t0 = time.perf_counter()
     e2e_rays0 = r.stats().rays_total
     for k in range(K):
-        fc_host = fb.build(cam.orbit(0.5 * (Wm + k)), Wm + k)   # frame constants built in host memory
+        fc_host = fb.build(cam.orbit(orbit * (Wm + k)), Wm + k)   # frame constants built in host memory
+        if insts is not None:
+            r.update_instances(insts[Wm + k], stream)              # host instance records
         r.render(fc_host, stream)
         r.read_image(abi.IMG_DENOISED, stream, out=out)          # D2H into pinned memory, waits
     e2e_s = time.perf_counter() - t0
@@ -267,7 +373,10 @@ def run_gkrt(args):
                 "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic", "config": workload_config(),
                 "ms_per_frame": ms_total / K, "trace_ms": trace_avg_ms, "rays_per_frame": rays / max(K, 1) / world,
-                "gpu_launches": 3 * K,
+                "gpu_launches": 3 * K + 2 * K * (fcs[0].denoiser == abi.DENOISE_ATROUS) + build_launches,
+                "bvh_build_ms": {"all_levels": build_all_ms, "instance_level": build_inst_ms,
+                                 "scene_load_s": load_s, "triangles": int(sc.triangle_count),
+                                 "instances": int(sc.instances.shape[0])},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ctypes.sizeof(abi.GkrtFrameConstants),
                         "d2h_bytes_per_step": W_ * H_ * 16, "ms_per_frame": e2e_s / K * 1e3},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -277,7 +386,9 @@ def run_gkrt(args):
                              "node_visits": st_last.node_visits, "triangle_tests": st_last.triangle_tests,
                              "exact_fallbacks": st_last.exact_fallbacks, "exact_retraces": st_last.exact_retraces},
                 "clocks": clk.summary()}
-        if world == 1 and not args.no_cpu_baseline:
+        if world == 1 and WORKLOAD == "bricks" and not args.no_relmse:
+            line["relmse"] = relmse_measure(local)
+        if world == 1 and not args.no_cpu_baseline and WORKLOAD == "bricks":
             line["cpu_baseline"] = cpu_baseline_measure(args.cpu_budget)
         print(json.dumps(line))
     r.close()
@@ -294,12 +405,18 @@ def main():
     ap.add_argument("--impl", default="gkrt", choices=["gkrt", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-relmse", action="store_true")
     ap.add_argument("--size", default=None, help="WxH override for profiling small cases (default 1920x1080)")
+    ap.add_argument("--workload", default="bricks", choices=["bricks", "city"],
+                    help="bricks: the 1080p headline workload; city: 10.5M tris at 4K with per-frame rebuild")
     args = ap.parse_args()
+    global WORKLOAD, W_, H_
+    WORKLOAD = args.workload
+    if WORKLOAD == "city":
+        W_, H_ = 3840, 2160
     if args.warmup < 3:
         args.warmup = 3
     if args.size:
-        global W_, H_
         W_, H_ = (int(v) for v in args.size.lower().split("x"))
     if args.impl == "reference":
         return run_reference(args)

@@ -2,8 +2,9 @@
 
 Each .cu translation unit is compiled in parallel with nvcc (one -gencode, sm_103a) and
 linked into gknextengine_gb300/_lib/libgkrt.so, which the ctypes binding loads. Kernels
-are compiled with -fmad=false: fused multiply-adds appear only where the source writes
-them, so float results do not depend on compiler contraction choices.
+are compiled with -fmad=false and host code with -ffp-contract=off: fused multiply-adds
+appear only where the source writes them, so float results do not depend on compiler
+contraction choices (the host-built emitter table must match the oracle's bit for bit).
 """
 from __future__ import annotations
 
@@ -19,7 +20,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(LIB_DIR, "libgkrt.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr", "-Xptxas", "-v"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-Xptxas", "-v"]
 
 
 def nvcc() -> str:

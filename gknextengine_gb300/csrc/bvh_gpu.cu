@@ -712,6 +712,7 @@ struct GpuBvh {
     DBuf<BvhNode> nodes;
     DBuf<MeshRange> ranges;
     DBuf<GpuInstBox> inst;
+    uint32_t launches = 0;   // kernels launched by all builds so far
 
     ~GpuBvh() {
         box.release(); cent.release(); root_box.release(); idx.release(); tmp.release();
@@ -732,6 +733,7 @@ struct GpuBvh {
         else GK_TRY(cudaMemsetAsync(bsum.p, 0, sizeof(T), st));
         k_scan_sums<T><<<1, kScanB, 0, st>>>(bsum.p, nb, tot.p);
         if (n) k_scan_fix<T><<<nb, kScanB, 0, st>>>(in, n, out, bsum.p);
+        launches += n ? 3u : 1u;
         return cudaGetLastError();
     }
 
@@ -752,7 +754,10 @@ struct GpuBvh {
         GK_TRY(root_box.need(6 * (size_t)std::max<uint32_t>(nroots, 1u)));
         GK_TRY(info.need(4));
         GK_TRY(cudaMemsetAsync(info.p, 0, 16, st));
-        if (n) k_init_idx<<<(n + 255) / 256, 256, 0, st>>>(idx.p, n);
+        if (n) {
+            k_init_idx<<<(n + 255) / 256, 256, 0, st>>>(idx.p, n);
+            ++launches;
+        }
         // roots: node slots [0, nroots); small roots reserve m - 1 slots after them
         std::vector<float> rbox(6 * (size_t)std::max<uint32_t>(nroots, 1u));
         for (uint32_t r = 0; r < nroots; ++r)
@@ -841,15 +846,18 @@ struct GpuBvh {
             k_emit<<<gt, 256, 0, st>>>(tasks[cur].p, ntask, split.p, cc_scan.p, node0, res0, nsmall, tasks[nx].p,
                                        wtask[nx].p, wbeg[nx].p, wend[nx].p, w0[nx].p, small.p);
             GK_TRY(cudaGetLastError());
+            launches += 9u;   // clear, bounds, bin, split, count_left, scatter, copy_back, child_counts, emit
             out->nodes_used += ntask;
             nsmall += nsm;
             ntask = nbig;
             nwork = nwork_next;
             cur = nx;
         }
-        if (nsmall)
+        if (nsmall) {
             k_small<<<(nsmall + 127) / 128, 128, 0, st>>>(g, idx.p, small.p, nsmall, nodes.p, root_box.p, max_leaf,
                                                           inst_leaf ? 1 : 0, prim_map, node_base, info.p);
+            ++launches;
+        }
         GK_TRY(cudaGetLastError());
         uint32_t hinfo[4];
         GK_TRY(cudaMemcpyAsync(hinfo, info.p, 16, cudaMemcpyDeviceToHost, st));
@@ -866,6 +874,7 @@ struct GpuBvh {
 };
 
 GpuBvh* gpu_bvh_new() { return new (std::nothrow) GpuBvh(); }
+uint32_t gpu_bvh_launches(const GpuBvh* b) { return b ? b->launches : 0u; }
 void gpu_bvh_free(GpuBvh* b) { delete b; }
 
 cudaError_t gpu_bvh_build_meshes(GpuBvh* B, const float4* pos, const uint32_t* ind, const GkrtMesh* meshes,
@@ -885,10 +894,16 @@ cudaError_t gpu_bvh_build_meshes(GpuBvh* B, const float4* pos, const uint32_t* i
     GK_TRY(B->box.need(6 * (size_t)std::max<uint32_t>(ntri, 1u)));
     GK_TRY(B->cent.need(3 * (size_t)std::max<uint32_t>(ntri, 1u)));
     const uint32_t nmr = std::max<uint32_t>(nmesh, 1u);
-    if (ntri) k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(pos, ind, B->ranges.p, nmr, ntri, B->box.p, B->cent.p);
+    if (ntri) {
+        k_tri_boxes<<<(ntri + 255) / 256, 256, 0, st>>>(pos, ind, B->ranges.p, nmr, ntri, B->box.p, B->cent.p);
+        ++B->launches;
+    }
     GK_TRY(cudaGetLastError());
     GK_TRY(B->build(ntri, rb, re, 4, false, nullptr, node_base, out, st));
-    if (ntri) k_gather_tris<<<(ntri + 255) / 256, 256, 0, st>>>(pos, ind, B->ranges.p, nmr, B->idx.p, ntri, tris_out);
+    if (ntri) {
+        k_gather_tris<<<(ntri + 255) / 256, 256, 0, st>>>(pos, ind, B->ranges.p, nmr, B->idx.p, ntri, tris_out);
+        ++B->launches;
+    }
     GK_TRY(cudaGetLastError());
     return cudaStreamSynchronize(st);
 }
@@ -905,7 +920,10 @@ cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint
     }
     GK_TRY(B->box.need(6 * (size_t)std::max<uint32_t>(n, 1u)));
     GK_TRY(B->cent.need(3 * (size_t)std::max<uint32_t>(n, 1u)));
-    if (n) k_inst_boxes<<<(n + 255) / 256, 256, 0, st>>>(B->inst.p, n, mesh_box, B->box.p, B->cent.p);
+    if (n) {
+        k_inst_boxes<<<(n + 255) / 256, 256, 0, st>>>(B->inst.p, n, mesh_box, B->box.p, B->cent.p);
+        ++B->launches;
+    }
     GK_TRY(cudaGetLastError());
     const std::vector<uint32_t> rb(1, 0u), re(1, n);
     GK_TRY(B->build(n, rb, re, 1, true, B->map.p, node_base, out, st));

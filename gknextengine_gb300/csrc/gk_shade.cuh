@@ -22,6 +22,9 @@ struct ShadeScene {
     uint32_t nmat;
     const uint32_t* cubes;       // optional probe grid
     const uint32_t* voxels;
+    const float4* emit;          // emissive triangles, 5 float4 each (see nee_sample)
+    const float2* emit_alias;    // alias table: (threshold, alias index bits) per entry
+    uint32_t nemit;              // 0: no emissive-triangle NEE
 };
 
 struct Vtx {
@@ -150,6 +153,51 @@ static __device__ __noinline__ f4 probe_grid(const ShadeScene& sc, float npx, fl
     }
     if (tw > 0.0f) return F4(div_(res.x, tw), div_(res.y, tw), div_(res.z, tw), div_(res.w, tw));
     return F4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// Emissive-triangle NEE (GKRT_NEE_EMISSIVE; no counterpart in the built reference path, its
+// math follows the legacy area-light branch of ScatterLambertian,
+// assets/shaders/glsl_legacy/common/Scatter.glsl:55-76, with the light chosen by an alias
+// table over power = area x luminance instead of uniformly). Entry j of sc.emit:
+//   [p0.xyz, w_j = area_j / pick-probability_j], [p1 - p0, 0], [p2 - p0, 0], [unit normal, 0],
+//   [emission rgba].
+// One uniform number picks slot i and tests its threshold (the fraction of u * n), a second
+// pair places a uniform point on the triangle. The sample is the throughput times
+//   Le * cos_s * |cos_l| * w_j / (pi * d^2),
+// tested for visibility over [EPS, d - EPS] from the bounce ray's origin (the segment of
+// TraceSegment, Shading.slang:759-782). Emitters are two-sided, as hits on them are.
+struct NeeSample {
+    f3 o, dir;
+    float tmax;
+    f4 contrib;
+};
+GK_D bool nee_sample(const ShadeScene& sc, Rng& seed, f3 P, f3 N, f4 rc, NeeSample& s) {
+    const uint32_t n = sc.nemit;
+    const float x = rnd1(seed) * (float)n;
+    uint32_t i = (uint32_t)x;
+    if (i > n - 1u) i = n - 1u;
+    const float frac = x - (float)i;
+    const float2 pa = __ldg(&sc.emit_alias[i]);
+    const uint32_t j = frac < pa.x ? i : __float_as_uint(pa.y);
+    const f2 r = rnd2(seed);
+    const float4* g = sc.emit + 5u * j;
+    const float4 g0 = __ldg(g), g1 = __ldg(g + 1), g2 = __ldg(g + 2), g3 = __ldg(g + 3), g4 = __ldg(g + 4);
+    const float su = sqrt_(r.x), bs = su * (1.0f - r.y), bt = su * r.y;
+    const f3 q = F3((g0.x + g1.x * bs) + g2.x * bt, (g0.y + g1.y * bs) + g2.y * bt, (g0.z + g1.z * bs) + g2.z * bt);
+    s.o = fma3(N, 0.001f, P);
+    const f3 lv = q - s.o;
+    const float d2 = dot3(lv, lv);
+    const float dist = sqrt_(d2);
+    if (!(dist > 2e-3f)) return false;
+    s.dir = lv * div_(1.0f, dist);
+    const float cs = dot3(N, s.dir);
+    if (!(cs > 0.0f)) return false;
+    const float cl = fabsf(dot3(F3(g3.x, g3.y, g3.z), s.dir));
+    if (!(cl > 0.0f)) return false;
+    const float gm = div_((cs * cl) * g0.w, d2 * 3.14159265358979323846f);
+    s.contrib = (rc * F4(g4.x, g4.y, g4.z, g4.w)) * gm;
+    s.tmax = dist - 1e-3f;
+    return true;
 }
 
 struct PixelImages {

@@ -34,6 +34,11 @@ struct GkrtContext {
     std::vector<GkrtInstance> inst;
     std::vector<float> pos_host;      // float4 per vertex (kept for BVH builds)
     std::vector<uint32_t> idx_host;
+    std::vector<GkrtMaterial> mat_host;
+    std::vector<std::vector<uint32_t>> slot_tris;   // per mesh and material slot
+    float4* d_emit = nullptr;         // emissive-triangle table (GKRT_NEE_EMISSIVE)
+    float2* d_emit_alias = nullptr;
+    uint32_t nemit = 0, emit_cap = 0;
     uint32_t nvert = 0, nidx = 0, nmat = 0;
     float4* d_pos = nullptr;
     float4* d_nrm = nullptr;
@@ -127,7 +132,9 @@ void free_images(GkrtContext* c) {
 void free_scene(GkrtContext* c) {
     dfree(c->d_pos); dfree(c->d_nrm); dfree(c->d_slot); dfree(c->d_idx); dfree(c->d_mat);
     dfree(c->d_inst_mat); dfree(c->d_inst_prev); dfree(c->d_inst); dfree(c->d_cubes); dfree(c->d_voxels);
-    dfree(c->d_nodes); dfree(c->d_tris); dfree(c->d_blas_box);
+    dfree(c->d_nodes); dfree(c->d_tris); dfree(c->d_blas_box); dfree(c->d_emit); dfree(c->d_emit_alias);
+    c->nemit = c->emit_cap = 0;
+    c->mat_host.clear(); c->slot_tris.clear();
     c->d_nodes_cap = 0;
     c->inst_cap = 0;
     c->has_scene = false;
@@ -406,6 +413,27 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
     return upload_instances(ctx);
 }
 
+// The emissive-triangle table of the current instances (rebuilt with every instance update).
+int build_emitters(GkrtContext* ctx) {
+    EmitterTable t;
+    build_emitter_table(ctx->inst.data(), (uint32_t)ctx->inst.size(), ctx->meshes.data(), ctx->pos_host.data(),
+                        ctx->idx_host.data(), ctx->slot_tris, ctx->mat_host.data(), ctx->nmat, t);
+    const uint32_t n = (uint32_t)t.alias.size();
+    if (n > ctx->emit_cap) {
+        dfree(ctx->d_emit);
+        dfree(ctx->d_emit_alias);
+        ctx->emit_cap = 0;
+        GK_CUDA(cudaMalloc((void**)&ctx->d_emit, (size_t)n * 5 * sizeof(float4)));
+        GK_CUDA(cudaMalloc((void**)&ctx->d_emit_alias, (size_t)n * sizeof(float2)));
+        ctx->emit_cap = n;
+    }
+    int rc;
+    if ((rc = copy_in(ctx, ctx->d_emit, t.geo.data(), t.geo.size() * sizeof(float4))) != GKRT_OK) return rc;
+    if ((rc = copy_in(ctx, ctx->d_emit_alias, t.alias.data(), t.alias.size() * sizeof(float2))) != GKRT_OK) return rc;
+    ctx->nemit = n;
+    return GKRT_OK;
+}
+
 int ensure_bvh(GkrtContext* ctx, uint32_t flags, cudaStream_t st) {
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
     int rc;
@@ -426,6 +454,24 @@ SceneView scene_view(GkrtContext* c) {
     S.tlas_root = c->tlas_root;
     S.error = c->d_error;
     return S;
+}
+
+ShadeScene shade_scene(GkrtContext* ctx) {
+    ShadeScene sc;
+    sc.S = scene_view(ctx);
+    sc.normals = ctx->d_nrm;
+    sc.slots = ctx->d_slot;
+    sc.indices = ctx->d_idx;
+    sc.inst_mat = ctx->d_inst_mat;
+    sc.inst_prev = ctx->d_inst_prev;
+    sc.mats = ctx->d_mat;
+    sc.nmat = ctx->nmat;
+    sc.cubes = ctx->d_cubes;
+    sc.voxels = ctx->d_voxels;
+    sc.emit = ctx->d_emit;
+    sc.emit_alias = ctx->d_emit_alias;
+    sc.nemit = ctx->nemit;
+    return sc;
 }
 
 int check_frame(GkrtContext* ctx, const GkrtFrameConstants* fc) {
@@ -592,6 +638,8 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
     ctx->nvert = d->vertex_count;
     ctx->nidx = d->index_count;
     ctx->nmat = d->material_count;
+    ctx->mat_host.assign(d->materials, d->materials + d->material_count);
+    mesh_slot_triangles(d->meshes, d->mesh_count, d->indices, d->material_slots, ctx->slot_tris);
     if ((rc = upload(ctx, ctx->d_pos, d->positions, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
     if ((rc = upload(ctx, ctx->d_nrm, d->normals, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
     if ((rc = upload(ctx, ctx->d_slot, d->material_slots, 4 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
@@ -604,7 +652,8 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
         if ((rc = upload(ctx, ctx->d_voxels, d->probe_voxels, n * 4 * 4)) != GKRT_OK) return rc;
     }
     ctx->has_scene = true;
-    return ensure_bvh(ctx, GKRT_BUILD_ALL, (cudaStream_t)0);
+    if ((rc = ensure_bvh(ctx, GKRT_BUILD_ALL, (cudaStream_t)0)) != GKRT_OK) return rc;
+    return build_emitters(ctx);
 }
 
 int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count, void* stream) {
@@ -616,8 +665,10 @@ int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
     if (rc != GKRT_OK) return rc;
     cudaSetDevice(ctx->device);
     ctx->inst.assign(instances, instances + count);
-    if (!ctx->blas_ready) return ensure_bvh(ctx, 0, (cudaStream_t)stream);
-    return build_tlas(ctx, (cudaStream_t)stream);
+    if (!ctx->blas_ready) rc = ensure_bvh(ctx, 0, (cudaStream_t)stream);
+    else rc = build_tlas(ctx, (cudaStream_t)stream);
+    if (rc != GKRT_OK) return rc;
+    return build_emitters(ctx);
 }
 
 int gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream) {
@@ -636,22 +687,11 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     int rc = check_frame(ctx, fc);
     if (rc != GKRT_OK) return rc;
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
-    if (fc->nee_mode != GKRT_NEE_REFERENCE)
-        return fail(ctx, GKRT_ERR_UNSUPPORTED, "nee_mode not supported by this build");
+    if (fc->nee_mode > GKRT_NEE_EMISSIVE) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown nee_mode");
     cudaSetDevice(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
-    ShadeScene sc;
-    sc.S = scene_view(ctx);
-    sc.normals = ctx->d_nrm;
-    sc.slots = ctx->d_slot;
-    sc.indices = ctx->d_idx;
-    sc.inst_mat = ctx->d_inst_mat;
-    sc.inst_prev = ctx->d_inst_prev;
-    sc.mats = ctx->d_mat;
-    sc.nmat = ctx->nmat;
-    sc.cubes = ctx->d_cubes;
-    sc.voxels = ctx->d_voxels;
+    const ShadeScene sc = shade_scene(ctx);
     PixelImages im;
     im.single_diffuse = (float4*)ctx->img[GKRT_IMG_SINGLE_DIFFUSE];
     im.single_specular = (float4*)ctx->img[GKRT_IMG_SINGLE_SPECULAR];
@@ -850,6 +890,59 @@ int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     out->bvh_nodes = ctx->blas_nodes_used;
     out->tlas_nodes = ctx->tlas_nodes;
     out->bvh_leaf_tris = ctx->nidx / 3;
+    out->emitters = ctx->nemit;
+    out->build_launches = gpu_bvh_launches(ctx->builder);
+    return GKRT_OK;
+}
+
+int gkrt_set_material_params(GkrtContext* ctx, const float* albedo_rgb, const float* roughness, uint32_t first,
+                             uint32_t count, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    if ((uint64_t)first + count > ctx->nmat) return fail(ctx, GKRT_ERR_INVALID_ARG, "material range outside the scene");
+    cudaSetDevice(ctx->device);
+    GK_CUDA(gkrt_launch_set_params(ctx->d_mat, albedo_rgb, roughness, first, count, (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
+static int adjoint_checks(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t spp) {
+    int rc = check_frame(ctx, fc);
+    if (rc != GKRT_OK) return rc;
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    if (spp == 0 || spp > 4096) return fail(ctx, GKRT_ERR_INVALID_ARG, "spp must be 1..4096");
+    if (fc->has_sun || fc->nee_mode != GKRT_NEE_REFERENCE)
+        return fail(ctx, GKRT_ERR_UNSUPPORTED, "the adjoint covers the reference NEE mode without sun");
+    if (fc->number_of_bounces > 16 || fc->max_number_of_bounces > 16)
+        return fail(ctx, GKRT_ERR_UNSUPPORTED, "the adjoint records at most 16 bounces");
+    if (ctx->nmat > 8192) return fail(ctx, GKRT_ERR_UNSUPPORTED, "the adjoint sums at most 8192 materials per block");
+    return GKRT_OK;
+}
+
+int gkrt_adjoint_forward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t spp, const float* sample_roughness,
+                         float* image, void* stream) {
+    int rc = adjoint_checks(ctx, fc, spp);
+    if (rc != GKRT_OK) return rc;
+    if (!image) return fail(ctx, GKRT_ERR_INVALID_ARG, "null image");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(gkrt_launch_adjoint(shade_scene(ctx), *fc, (int)ctx->W, (int)ctx->H, spp, sample_roughness,
+                                (float4*)image, nullptr, nullptr, nullptr, ctx->d_counters, st));
+    return GKRT_OK;
+}
+
+int gkrt_adjoint_backward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t spp, const float* sample_roughness,
+                          const float* d_image, double* grad_albedo, double* grad_roughness, void* stream) {
+    int rc = adjoint_checks(ctx, fc, spp);
+    if (rc != GKRT_OK) return rc;
+    if (!d_image || !grad_albedo || !grad_roughness) return fail(ctx, GKRT_ERR_INVALID_ARG, "null buffer");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(gkrt_launch_adjoint(shade_scene(ctx), *fc, (int)ctx->W, (int)ctx->H, spp, sample_roughness, nullptr,
+                                (const float4*)d_image, grad_albedo, grad_roughness, ctx->d_counters, st));
     return GKRT_OK;
 }
 

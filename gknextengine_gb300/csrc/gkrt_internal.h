@@ -56,6 +56,20 @@ struct HostBvh {
 void build_bvh_host(const float* boxes, uint32_t n, uint32_t max_leaf, uint32_t node_base, uint32_t prim_base,
                     bool leaf_is_instance, HostBvh& out);
 
+// Emissive-triangle table for GKRT_NEE_EMISSIVE (emitters.cu): 5 float4 per emitter and one
+// alias entry (threshold, alias index bits) per emitter.
+struct EmitterTable {
+    std::vector<float4> geo;
+    std::vector<float2> alias;
+};
+float emitter_luminance(const float* rgb);
+// Triangles of each mesh grouped by the material slot of their vertex 0: out[16 * mesh + slot].
+void mesh_slot_triangles(const GkrtMesh* meshes, uint32_t nmesh, const uint32_t* indices, const uint32_t* slots,
+                         std::vector<std::vector<uint32_t>>& out);
+void build_emitter_table(const GkrtInstance* inst, uint32_t ninst, const GkrtMesh* meshes, const float* pos,
+                         const uint32_t* indices, const std::vector<std::vector<uint32_t>>& slot_tris,
+                         const GkrtMaterial* mats, uint32_t nmat, EmitterTable& out);
+
 // GPU builder (bvh_gpu.cu): same split rule and node layout, device scratch reused across
 // builds. Results stay in the builder's memory until its next build.
 struct GpuBvh;
@@ -74,6 +88,7 @@ struct GpuBvhResult {
 };
 GpuBvh* gpu_bvh_new();
 void gpu_bvh_free(GpuBvh* b);
+uint32_t gpu_bvh_launches(const GpuBvh* b);   // kernels launched by all its builds
 // One tree per mesh over all meshes' triangles; writes the triangles in leaf order to
 // tris_out (3 float4 per triangle).
 cudaError_t gpu_bvh_build_meshes(GpuBvh* b, const float4* pos, const uint32_t* indices, const GkrtMesh* meshes,
@@ -96,6 +111,11 @@ int gkrt_internal_fail(GkrtContext* ctx, int code, const std::string& msg);
 // built; GKRT_ERR_STATE otherwise (nothing is built or allocated here).
 int gkrt_internal_ready_view(GkrtContext* ctx, gk::SceneView* view, unsigned long long** counters, int* device);
 
+cudaError_t gkrt_launch_adjoint(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, uint32_t spp,
+                                const float* sample_rough, float4* image, const float4* dimage, double* g_alb,
+                                double* g_rough, unsigned long long* counters, cudaStream_t st);
+cudaError_t gkrt_launch_set_params(GkrtMaterial* mats, const float* alb, const float* rough, uint32_t first,
+                                   uint32_t count, cudaStream_t st);
 cudaError_t gkrt_launch_reproject(const gk::ReprojectArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_compose(const gk::ComposeArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_atrous(const gk::AtrousArgs& a, const float4* in, float4* tmp0, float4* tmp1, cudaStream_t st);

@@ -38,11 +38,17 @@ __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long 
     }
 }
 
-enum Stage : uint32_t { ST_PRIMARY = 0, ST_FIRST = 1, ST_BOUNCE = 2, ST_SUN = 3, ST_DIRECT = 4 };
+enum Stage : uint32_t {
+    ST_PRIMARY = 0, ST_FIRST = 1, ST_BOUNCE = 2, ST_SUN = 3, ST_DIRECT = 4,
+    ST_NEE_FIRST = 5, ST_NEE_BOUNCE = 6   // emissive-triangle shadow ray before the first / a later bounce
+};
 
 // Per-thread slots in shared memory (strided by the block size): the primary vertex,
-// the per-pixel loop bounds and the two accumulators. Read at sample boundaries only.
-enum Slot { SL_PX = 0, SL_PY, SL_PZ, SL_NX, SL_NY, SL_NZ, SL_MAT, SL_LOOP, SL_FC, SL_FR = SL_FC + 4, SL_COUNT = SL_FR + 4 };
+// the per-pixel loop bounds, the two accumulators and the pending emissive-NEE sample.
+enum Slot {
+    SL_PX = 0, SL_PY, SL_PZ, SL_NX, SL_NY, SL_NZ, SL_MAT, SL_LOOP, SL_FC, SL_FR = SL_FC + 4, SL_NEE = SL_FR + 4,
+    SL_COUNT = SL_NEE + 4
+};
 
 struct Lane {
     int pix;          // pixel index, -1 when the lane holds no pixel
@@ -50,6 +56,7 @@ struct Lane {
     uint32_t stage;
     uint32_t i, b;    // sample and bounce indices
     bool chanceReflect, back, diel, hitReflect, hitMetal;
+    bool neeLobe;     // the bounce in flight was sampled from the diffuse lobe of an emissive-NEE vertex
     f4 rc;            // throughput of the current sample (RayColor)
     Vtx vs;           // current path vertex
     f3 dir;           // current path direction
@@ -66,9 +73,9 @@ struct Ctx {
     __device__ float& slot(int k) const { return ps[k * stride]; }
 };
 
-__device__ __forceinline__ void emit(Trav& T, const Ctx& c, f3 o, f3 d, int mode) {
+__device__ __forceinline__ void emit(Trav& T, const Ctx& c, f3 o, f3 d, int mode, float tmax = 1000.0f) {
     ++c.cn.rays;
-    trav_init(T, c.sc.S, o, d, 1000.0f, mode);
+    trav_init(T, c.sc.S, o, d, tmax, mode);
 }
 
 __device__ __forceinline__ f3 pv_pos(const Ctx& c) { return F3(c.slot(SL_PX), c.slot(SL_PY), c.slot(SL_PZ)); }
@@ -84,6 +91,7 @@ __device__ __forceinline__ f3 pv_nrm(const Ctx& c) { return F3(c.slot(SL_NX), c.
 // section at most once per call, so lanes in different states re-converge after each
 // section and the expensive ones (the sampling before a trace, the hit reconstruction
 // after it) run once per warp for all the lanes that need them.
+template <bool kNee>
 __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
     const GkrtFrameConstants& fc = c.fc;
     const f3 sunDir = F3(fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]);
@@ -159,9 +167,15 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
         if (T.hit) {
             L.vs = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
             const MatV hm = load_mat(c.sc, L.vs.mat);
-            if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !L.chanceReflect) L.rc = L.rc * hm.diffuse;
-            if (L.back && !L.diel) { L.rc = F4(0.5f, 0.5f, 0.5f, 0.0f); term = true; }
-            else term = hm.model == GKRT_MAT_DIFFUSE_LIGHT;
+            if (kNee && L.neeLobe && hm.model == GKRT_MAT_DIFFUSE_LIGHT) {
+                // the emitter this diffuse bounce reached was sampled by the vertex's NEE
+                L.rc = F4(0.0f, 0.0f, 0.0f, 0.0f);
+                term = true;
+            } else {
+                if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !L.chanceReflect) L.rc = L.rc * hm.diffuse;
+                if (L.back && !L.diel) { L.rc = F4(0.5f, 0.5f, 0.5f, 0.0f); term = true; }
+                else term = hm.model == GKRT_MAT_DIFFUSE_LIGHT;
+            }
         } else {
             L.rc = L.rc * sky(fc);
             term = true;
@@ -251,6 +265,18 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
         need_finish = true;
     }
 
+    // 6b. an emissive-NEE shadow ray's answer, then the bounce ray its vertex sampled
+    if (kNee && (stage == ST_NEE_FIRST || stage == ST_NEE_BOUNCE)) {
+        if (!T.hit) {
+            const int acc = L.hitReflect ? SL_FR : SL_FC;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c.slot(acc + q) = c.slot(acc + q) + c.slot(SL_NEE + q);
+        }
+        L.stage = stage == ST_NEE_FIRST ? ST_FIRST : ST_BOUNCE;
+        emit(T, c, fma3(L.vs.N, 0.001f, L.vs.P), L.dir, kClosest);
+        emitted = true;
+    }
+
     // 7. the pixel's outputs (Shading.slang:1175-1183)
     if (need_finish) {
         const float dd = mx(dot3(sunDir, normalize3(pv_nrm(c))), 0.0f) * 0.318309886183790671538f;
@@ -300,8 +326,19 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
         L.chanceReflect = chanceReflect;
         L.back = back;
         L.diel = diel;
-        L.stage = pre_first ? ST_FIRST : ST_BOUNCE;
-        emit(T, c, fma3(L.vs.N, 0.001f * startPosOffset, L.vs.P), tdir, kClosest);
+        L.neeLobe = kNee && !back && !diel && !chanceGGX;
+        NeeSample ns;
+        if (kNee && L.neeLobe && nee_sample(c.sc, L.seed, L.vs.P, L.vs.N, L.rc, ns)) {
+            f4 contrib = ns.contrib;
+            if (L.hitMetal) contrib = contrib * load_mat(c.sc, __float_as_uint(c.slot(SL_MAT))).diffuse;
+            c.slot(SL_NEE) = contrib.x; c.slot(SL_NEE + 1) = contrib.y;
+            c.slot(SL_NEE + 2) = contrib.z; c.slot(SL_NEE + 3) = contrib.w;
+            L.stage = pre_first ? ST_NEE_FIRST : ST_NEE_BOUNCE;
+            emit(T, c, ns.o, ns.dir, kAny, ns.tmax);
+        } else {
+            L.stage = pre_first ? ST_FIRST : ST_BOUNCE;
+            emit(T, c, fma3(L.vs.N, 0.001f * startPosOffset, L.vs.P), tdir, kClosest);
+        }
         emitted = true;
     }
     return emitted;
@@ -331,6 +368,9 @@ __device__ void start_pixel(Lane& L, Trav& T, const Ctx& c, int x, int y) {
     emit(T, c, xyz(origin), xyz(direction), kClosest);
 }
 
+// kNee: emissive-triangle NEE compiled in (GKRT_NEE_EMISSIVE with a non-empty table); the
+// reference mode runs the instantiation without it.
+template <bool kNee>
 __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeScene sc, GkrtFrameConstants fc, int W, int H,
                                                            int P, PixelImages im, unsigned long long* counters,
                                                            unsigned int* work) {
@@ -346,12 +386,13 @@ __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeSc
     Lane L;
     L.pix = -1;
     L.stage = ST_PRIMARY;
+    L.neeLobe = false;
     Trav T;
     T.done = true;
     bool tracing = false, exhausted = false;
     for (;;) {
         if (!tracing) {
-            if (L.pix >= 0) tracing = advance(L, T, c);
+            if (L.pix >= 0) tracing = advance<kNee>(L, T, c);
             while (!tracing && !exhausted) {
                 // next pixel: warp-aggregated fetch over 8 x 4 tiles
                 const unsigned m = __activemask();
@@ -425,8 +466,10 @@ using namespace gk;
 cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,
                                    const PixelImages& im, unsigned long long* counters, unsigned int* work,
                                    int num_sms, cudaStream_t st) {
+    const bool nee = fc.nee_mode == GKRT_NEE_EMISSIVE && sc.nemit > 0u;
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pass, kPtThreads, 0);
+    cudaError_t e = nee ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pass<true>, kPtThreads, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pass<false>, kPtThreads, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const int pixels = W * H;
@@ -435,7 +478,8 @@ cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstant
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(work, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    k_trace_pass<<<blocks, kPtThreads, 0, st>>>(sc, fc, W, H, P, im, counters, work);
+    if (nee) k_trace_pass<true><<<blocks, kPtThreads, 0, st>>>(sc, fc, W, H, P, im, counters, work);
+    else k_trace_pass<false><<<blocks, kPtThreads, 0, st>>>(sc, fc, W, H, P, im, counters, work);
     return cudaGetLastError();
 }
 

@@ -52,6 +52,9 @@ def load(path: str | None = None):
     L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
     L.gkrt_synchronize.argtypes = [vp, vp]
     L.gkrt_affine_inverse.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.gkrt_set_material_params.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
+    L.gkrt_adjoint_forward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp]
+    L.gkrt_adjoint_backward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp, vp, vp]
     if L.gkrt_abi_version() != 1:
         raise RuntimeError("libgkrt ABI version mismatch")
     _lib = L
@@ -66,4 +69,5 @@ EXPORTED = [
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
     "gkrt_get_stats",
     "gkrt_synchronize", "gkrt_affine_inverse",
+    "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward",
 ]

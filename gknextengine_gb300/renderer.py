@@ -76,6 +76,10 @@ class PathTracingRenderer:
         desc = scene.desc()
         self._check(self._lib.gkrt_scene_upload(self._h, C.byref(desc)))
 
+    @property
+    def material_count(self) -> int:
+        return 0 if getattr(self, "_scene", None) is None else int(self._scene.materials.shape[0])
+
     def update_instances(self, instances: np.ndarray, stream=None):
         """Per-frame NodeProxy upload + TLAS rebuild (Scene::UpdateNodesGpuDriven, AfterUpdateScene)."""
         inst = np.ascontiguousarray(instances, dtype=abi.INSTANCE_DTYPE)
@@ -138,6 +142,26 @@ class PathTracingRenderer:
         """Ray queries that allocate no device memory (static scratch; see gkrt.h)."""
         self._check(self._lib.gkrt_trace_rays_noalloc(self._h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr), count,
                                                       mode, self._stream(stream)))
+
+    # ---- differentiable rendering (path-replay adjoint; device pointers) ----
+    def set_material_params(self, albedo_ptr: int | None, rough_ptr: int | None, first: int, count: int,
+                            stream=None):
+        """Overwrite diffuse rgb (3 floats each) and fuzziness of materials [first, first+count)."""
+        self._check(self._lib.gkrt_set_material_params(self._h, C.c_void_p(albedo_ptr or 0),
+                                                       C.c_void_p(rough_ptr or 0), first, count,
+                                                       self._stream(stream)))
+
+    def adjoint_forward(self, fc, spp: int, image_ptr: int, sample_rough_ptr: int | None = None, stream=None):
+        """The estimator's composed radiance (dense width x height float4) with spp samples."""
+        self._check(self._lib.gkrt_adjoint_forward(self._h, C.byref(fc), spp, C.c_void_p(sample_rough_ptr or 0),
+                                                   C.c_void_p(image_ptr), self._stream(stream)))
+
+    def adjoint_backward(self, fc, spp: int, dimage_ptr: int, grad_albedo_ptr: int, grad_rough_ptr: int,
+                         sample_rough_ptr: int | None = None, stream=None):
+        """Adds d loss / d (albedo rgb, roughness) per material (doubles) for d loss / d image."""
+        self._check(self._lib.gkrt_adjoint_backward(self._h, C.byref(fc), spp, C.c_void_p(sample_rough_ptr or 0),
+                                                    C.c_void_p(dimage_ptr), C.c_void_p(grad_albedo_ptr),
+                                                    C.c_void_p(grad_rough_ptr), self._stream(stream)))
 
     def stats(self) -> abi.GkrtStats:
         s = abi.GkrtStats()

@@ -270,3 +270,206 @@ def bricks(seed: int = 2, width: int = 1920, height: int = 1080, grid: int = 64,
     cam = Camera(eye=center + np.array([0.0, 40.0, 90.0]), center=center + np.array([0.0, 2.0, 0.0]), fov_deg=40.0)
     settings = Settings(samples=1, bounces=8, max_bounces=8, temporal_frames=16, taa=True)
     return scene, cam, settings
+
+
+def octa_sphere(levels: int = 4) -> MeshBuilder:
+    """Unit sphere: an octahedron subdivided `levels` times (8 * 4**levels tris; 2048 at 4),
+    vertex normals = positions."""
+    P = [np.array(v, np.float64) for v in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1))]
+    faces = [(0, 2, 4), (2, 1, 4), (1, 3, 4), (3, 0, 4), (2, 0, 5), (1, 2, 5), (3, 1, 5), (0, 3, 5)]
+    tris = [(P[a], P[b], P[c]) for a, b, c in faces]
+    for _ in range(levels):
+        nxt = []
+        for a, b, c in tris:
+            ab, bc, ca = a + b, b + c, c + a
+            ab, bc, ca = ab / np.linalg.norm(ab), bc / np.linalg.norm(bc), ca / np.linalg.norm(ca)
+            nxt += [(a, ab, ca), (ab, b, bc), (ca, bc, c), (ab, bc, ca)]
+        tris = nxt
+    m = MeshBuilder()
+    for a, b, c in tris:
+        m.tri(tuple(a), tuple(b), tuple(c), tuple(a), tuple(b), tuple(c), 0)
+    return m
+
+
+class CityMotion:
+    """Per-frame instance transforms of city(): the spheres circle about fixed centres."""
+
+    def __init__(self, instances, first_sphere, centre, radius, orbit, phase, omega):
+        self.base = instances
+        self.first = first_sphere
+        self.centre, self.radius, self.orbit, self.phase, self.omega = centre, radius, orbit, phase, omega
+
+    def _worlds(self, frame):
+        a = self.phase + self.omega * frame
+        n = self.radius.shape[0]
+        w = np.zeros((n, 12))
+        w[:, 0] = w[:, 5] = w[:, 10] = self.radius
+        w[:, 3] = self.centre[:, 0] + self.orbit * np.cos(a)
+        w[:, 7] = self.centre[:, 1]
+        w[:, 11] = self.centre[:, 2] + self.orbit * np.sin(a)
+        return w
+
+    def instances(self, frame: int) -> np.ndarray:
+        """Instances of `frame`; combined_prev maps this frame's positions to last frame's."""
+        inst = self.base.copy()
+        w = self._worlds(frame)
+        pw = self._worlds(frame - 1 if frame > 0 else 0)
+        s = slice(self.first, self.first + w.shape[0])
+        inst["world"][s] = w.astype(np.float32)
+        inv = np.zeros_like(w)
+        inv[:, 0] = inv[:, 5] = inv[:, 10] = 1.0 / self.radius
+        inv[:, 3] = -w[:, 3] / self.radius
+        inv[:, 7] = -w[:, 7] / self.radius
+        inv[:, 11] = -w[:, 11] / self.radius
+        inst["world_inv"][s] = inv.astype(np.float32)
+        cp = np.zeros_like(w)   # translation only: prev = x + (t_prev - t)
+        cp[:, 0] = cp[:, 5] = cp[:, 10] = 1.0
+        cp[:, 3] = pw[:, 3] - w[:, 3]
+        cp[:, 7] = pw[:, 7] - w[:, 7]
+        cp[:, 11] = pw[:, 11] - w[:, 11]
+        inst["combined_prev"][s] = cp.astype(np.float32)
+        return inst
+
+
+def city(seed: int = 3, width: int = 3840, height: int = 2160, boxes: int = 20000, spheres: int = 5000,
+         emissive_spheres: int = 5, sphere_levels: int = 4):
+    """Config C3: 20k extruded boxes (a unit box mesh of 12 tris, footprints U(2, 5) m,
+    heights LogNormal(3, 0.6)) on a jittered grid, 5k spheres (one 2048-tri octahedral sphere
+    mesh) circling above them, of which 5 are emissive (10,240 emissive tris, sampled through
+    the alias table), GGX roughness U(0.02, 1); 3840 x 2160, 1 spp, 8 bounces, no sky.
+    Returns (SceneArrays, Camera, Settings, CityMotion); the spheres move every frame, so the
+    instance level is rebuilt every frame."""
+    rng = np.random.default_rng(seed)
+    box = MeshBuilder()
+    box.box((-0.5, 0.0, -0.5), (0.5, 1.0, 0.5), slot=0)
+    sph = octa_sphere(sphere_levels)
+    grid = int(math.ceil(math.sqrt(boxes)))
+    pitch = 6.0
+    ext = grid * pitch
+    ground = MeshBuilder()
+    ground.quad((-10.0, 0.0, -10.0), (-10.0, 0.0, ext + 10.0), (ext + 10.0, 0.0, ext + 10.0), (ext + 10.0, 0.0, -10.0),
+                (0, 1, 0), 0)
+    pos, nrm, slot, idx, meshes = _concat_meshes([box, sph, ground])
+    npal = 256
+    rough = rng.uniform(0.02, 1.0, npal)
+    metal = rng.random(npal) < 0.3
+    base = rng.uniform(0.05, 0.95, (npal, 3))
+    mats = [metallic(base[i], rough[i]) if metal[i] else mixture(base[i], rough[i]) for i in range(npal)]
+    rad = rng.uniform(20.0, 60.0, emissive_spheres)
+    tint = rng.uniform(0.6, 1.0, (emissive_spheres, 3))
+    for k in range(emissive_spheres):
+        mats.append(diffuse_light(tuple(rad[k] * tint[k])))
+    mats.append(lambertian((0.4, 0.4, 0.4)))
+    materials = np.array(mats, dtype=abi.MATERIAL_DTYPE)
+    ground_mat = len(mats) - 1
+    n = boxes + spheres + 1
+    insts = np.zeros(n, abi.INSTANCE_DTYPE)
+    ident = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
+    insts["instance_id"] = np.arange(n)
+    insts["visible"] = 1
+    insts["combined_prev"][:] = ident
+    # buildings
+    gi, gj = np.divmod(np.arange(boxes), grid)
+    cx = (gi + 0.5) * pitch + rng.uniform(-0.5, 0.5, boxes)
+    cz = (gj + 0.5) * pitch + rng.uniform(-0.5, 0.5, boxes)
+    sx, sz = rng.uniform(2.0, 5.0, boxes), rng.uniform(2.0, 5.0, boxes)
+    hy = np.clip(rng.lognormal(3.0, 0.6, boxes), 2.0, 200.0)
+    w = np.zeros((boxes, 12))
+    w[:, 0], w[:, 5], w[:, 10] = sx, hy, sz
+    w[:, 3], w[:, 11] = cx, cz
+    inv = np.zeros((boxes, 12))
+    inv[:, 0], inv[:, 5], inv[:, 10] = 1.0 / sx, 1.0 / hy, 1.0 / sz
+    inv[:, 3], inv[:, 11] = -cx / sx, -cz / sz
+    insts["mesh_id"][:boxes] = 0
+    insts["world"][:boxes] = w.astype(np.float32)
+    insts["world_inv"][:boxes] = inv.astype(np.float32)
+    insts["mat_id"][:boxes, 0] = rng.integers(0, npal, boxes)
+    # spheres
+    s0 = boxes
+    centre = np.stack([rng.uniform(0.0, ext, spheres), rng.uniform(60.0, 160.0, spheres),
+                       rng.uniform(0.0, ext, spheres)], 1)
+    radius = rng.uniform(1.0, 3.0, spheres)
+    orbit = rng.uniform(2.0, 12.0, spheres)
+    phase = rng.uniform(0.0, 2 * math.pi, spheres)
+    omega = rng.uniform(0.02, 0.08, spheres) * rng.choice([-1.0, 1.0], spheres)
+    insts["mesh_id"][s0:s0 + spheres] = 1
+    smat = rng.integers(0, npal, spheres)
+    emit_ids = rng.choice(spheres, emissive_spheres, replace=False)
+    smat[emit_ids] = npal + np.arange(emissive_spheres)
+    radius[emit_ids] = 6.0
+    insts["mat_id"][s0:s0 + spheres, 0] = smat
+    # ground
+    insts["mesh_id"][n - 1] = 2
+    insts["world"][n - 1] = ident
+    insts["world_inv"][n - 1] = ident
+    insts["mat_id"][n - 1, 0] = ground_mat
+    motion = CityMotion(insts, s0, centre, radius, orbit, phase, omega)
+    insts = motion.instances(0)
+    motion.base = insts
+    scene = abi.SceneArrays(pos, nrm, slot, idx, meshes, materials, insts, lights=np.zeros(0, abi.LIGHT_DTYPE),
+                            name="city")
+    c = np.array([ext * 0.5, 0.0, ext * 0.5])
+    cam = Camera(eye=c + np.array([0.0, 260.0, 520.0]), center=c + np.array([0.0, 20.0, 0.0]), fov_deg=40.0)
+    settings = Settings(samples=1, bounces=8, max_bounces=8, temporal_frames=16, taa=True,
+                        nee_mode=abi.NEE_EMISSIVE)
+    return scene, cam, settings, motion
+
+
+def cornell_materials(seed: int = 4, tiles: int = 16, width: int = 512, height: int = 512, spp: int = 16):
+    """Config C4: the Cornell box with its walls and both boxes tiled tiles x tiles, tile
+    (i, j) using material tiles * i + j (256 materials: albedo U(0.2, 0.9)^3, roughness
+    U(0.05, 1), metalness 0.25, Schlick index 1.5, drawn from `seed`), plus the 0.25 x 0.25
+    light (material 256, radiance 15). Instances address 16 material slots, so each surface
+    group is split into `tiles` row meshes whose slot j is the tile column.
+    Returns (SceneArrays, Camera, Settings) with settings.samples = spp."""
+    rng = np.random.default_rng(seed)
+    nmat = tiles * tiles
+
+    def tiled_quad(rows, p0, p1, p3, n):
+        # p0 + u (p1 - p0) + v (p3 - p0); row i along v, column j along u
+        p0, p1, p3 = (np.asarray(p, np.float64) for p in (p0, p1, p3))
+        eu, ev = (p1 - p0) / tiles, (p3 - p0) / tiles
+        for i in range(tiles):
+            for j in range(tiles):
+                a = p0 + eu * j + ev * i
+                rows[i].quad(tuple(a), tuple(a + eu), tuple(a + eu + ev), tuple(a + ev), n, j)
+
+    room = [MeshBuilder() for _ in range(tiles)]
+    # the five walls of cornell(), each with outward-facing (into the room) normals
+    tiled_quad(room, (-0.5, 0, 0.5), (-0.5, 0, -0.5), (-0.5, 1, 0.5), (1, 0, 0))      # left
+    tiled_quad(room, (0.5, 0, -0.5), (0.5, 0, 0.5), (0.5, 1, -0.5), (-1, 0, 0))       # right
+    tiled_quad(room, (-0.5, 0, -0.5), (0.5, 0, -0.5), (-0.5, 1, -0.5), (0, 0, 1))     # back
+    tiled_quad(room, (-0.5, 0, 0.5), (0.5, 0, 0.5), (-0.5, 0, -0.5), (0, 1, 0))       # floor
+    tiled_quad(room, (-0.5, 1, -0.5), (0.5, 1, -0.5), (-0.5, 1, 0.5), (0, -1, 0))     # ceiling
+    box = [MeshBuilder() for _ in range(tiles)]
+    x0, y0, z0, x1, y1, z1 = -0.5, 0.0, -0.5, 0.5, 1.0, 0.5
+    tiled_quad(box, (x0, y0, z1), (x0, y0, z0), (x0, y1, z1), (-1, 0, 0))
+    tiled_quad(box, (x1, y0, z0), (x1, y0, z1), (x1, y1, z0), (1, 0, 0))
+    tiled_quad(box, (x0, y0, z0), (x1, y0, z0), (x0, y1, z0), (0, 0, -1))
+    tiled_quad(box, (x1, y0, z1), (x0, y0, z1), (x1, y1, z1), (0, 0, 1))
+    tiled_quad(box, (x0, y0, z0), (x0, y0, z1), (x1, y0, z0), (0, -1, 0))
+    tiled_quad(box, (x0, y1, z1), (x0, y1, z0), (x1, y1, z1), (0, 1, 0))
+    light = MeshBuilder()
+    y = 0.999
+    light.quad((-0.125, y, 0.125), (0.125, y, 0.125), (0.125, y, -0.125), (-0.125, y, -0.125), (0, -1, 0), 0)
+    pos, nrm, slot, idx, meshes = _concat_meshes(room + box + [light])
+    albedo = rng.uniform(0.2, 0.9, (nmat, 3))
+    rough = rng.uniform(0.05, 1.0, nmat)
+    mats = [material(tuple(albedo[k]), abi.MAT_LAMBERTIAN, fuzziness=float(rough[k]), ri=1.5, metalness=0.25)
+            for k in range(nmat)]
+    mats.append(diffuse_light((15.0, 15.0, 15.0)))
+    materials = np.array(mats, dtype=abi.MATERIAL_DTYPE)
+    insts = []
+    row_ids = list(range(tiles))
+    for i in row_ids:
+        insts.append(make_instance(i, trs(), [tiles * i + j for j in range(tiles)], instance_id=0))
+    for k, w in enumerate((trs((-0.17, 0.0, -0.15), rot_y_deg=18.0, scale=(0.3, 0.6, 0.3)),
+                           trs((0.18, 0.0, 0.17), rot_y_deg=-17.0, scale=(0.3, 0.3, 0.3)))):
+        for i in row_ids:
+            insts.append(make_instance(tiles + i, w, [tiles * i + j for j in range(tiles)], instance_id=1 + k))
+    insts.append(make_instance(2 * tiles, trs(), [nmat], instance_id=3))
+    instances = np.array(insts, dtype=abi.INSTANCE_DTYPE)
+    scene = abi.SceneArrays(pos, nrm, slot, idx, meshes, materials, instances, name="cornell-256-materials")
+    cam = Camera(eye=(0.0, 0.5, 1.94), center=(0.0, 0.5, 0.0), fov_deg=40.0)
+    settings = Settings(samples=spp, bounces=4, max_bounces=4, taa=False)
+    return scene, cam, settings

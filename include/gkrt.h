@@ -243,6 +243,8 @@ typedef struct GkrtStats {
     uint32_t bvh_nodes;
     uint32_t bvh_leaf_tris;
     uint32_t tlas_nodes;
+    uint32_t emitters;          /* emissive triangles in the GKRT_NEE_EMISSIVE table      */
+    uint32_t build_launches;    /* kernels launched by GPU BVH builds since creation      */
 } GkrtStats;
 
 typedef struct GkrtContext GkrtContext;
@@ -306,6 +308,27 @@ int  gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint3
  * stream. Statistics land in the context's counters as for gkrt_trace_rays. */
 int  gkrt_trace_rays_noalloc(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32_t count,
                              uint32_t mode, void* stream);
+
+/* Differentiable rendering (no counterpart in the reference): the pass's estimator with
+ * `spp` samples per pixel from the primary hit, composed as the compose pass composes it
+ * (diffuse x primary albedo + specular, no filter), and its path-replay adjoint.
+ * Reference NEE mode without sun (else GKRT_ERR_UNSUPPORTED), at most 16 bounces.
+ * image / d_image: dense width x height float4 device arrays (the context's size).
+ * sample_roughness: per material, the roughness GGX directions are sampled with (detached);
+ * NULL samples with the current roughness. GGX bounces are weighted by the ratio of the
+ * sampler's densities at the current and the sampling roughness, which is 1 when they are
+ * equal. Gradients are ADDED to grad_albedo (3 doubles per material) and grad_roughness
+ * (1 double per material), device arrays the caller zeroes.
+ * gkrt_set_material_params overwrites diffuse rgb (3 floats each) and fuzziness of
+ * materials [first, first + count) from device arrays (either may be NULL); emitter
+ * radiance changes need gkrt_scene_upload. */
+int  gkrt_set_material_params(GkrtContext* ctx, const float* albedo_rgb, const float* roughness,
+                              uint32_t first, uint32_t count, void* stream);
+int  gkrt_adjoint_forward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t spp,
+                          const float* sample_roughness, float* image, void* stream);
+int  gkrt_adjoint_backward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t spp,
+                           const float* sample_roughness, const float* d_image,
+                           double* grad_albedo, double* grad_roughness, void* stream);
 
 int  gkrt_get_stats(GkrtContext* ctx, GkrtStats* out);
 int  gkrt_synchronize(GkrtContext* ctx, void* stream);

@@ -154,6 +154,11 @@ struct OScene {
     bool has_probes = false;
     std::vector<Bvh> blas;
     Bvh tlas;
+    // emissive-triangle table (GKRT_NEE_EMISSIVE): 20 floats per emitter
+    // (p0, w | p1-p0, 0 | p2-p0, 0 | normal, 0 | emission rgba) and its alias table
+    std::vector<float> emit;
+    std::vector<float> emit_thr;
+    std::vector<uint32_t> emit_alias;
 };
 
 // 0: every candidate triangle is decided by the FP64 test (the definition itself).
@@ -308,6 +313,12 @@ bool trace_ray(const OScene& S, f3 o, f3 d, float tmax, Vtx& out, uint32_t* out_
 bool trace_occlusion(const OScene& S, f3 o, f3 d, uint64_t* rays) {
     if (rays) ++*rays;
     return trace(S, o, d, kEPS, kPT_MAX, true, false, nullptr).hit;
+}
+
+// Any hit over [EPS, tmax] (TraceSegment, Shading.slang:759-782).
+bool trace_segment(const OScene& S, f3 o, f3 d, float tmax, uint64_t* rays) {
+    if (rays) ++*rays;
+    return trace(S, o, d, kEPS, tmax, true, false, nullptr).hit;
 }
 
 // ---- samplers (Const_Func.slang) ----
@@ -483,9 +494,52 @@ f4 sky_color(const GkrtFrameConstants& fc) {
     return scale4(c, fc.sky_intensity);
 }
 
-// FPathTracingRendererV2::GetRayColor (Shading.slang:1003-1082)
+// Emissive-triangle NEE (GKRT_NEE_EMISSIVE, no counterpart in the built reference path; the
+// estimator of the legacy area-light branch, Scatter.glsl:55-76, with the alias-table pick
+// of the light). Samples one point for vertex (P, N) with throughput rc; false when the
+// sample cannot contribute (no shadow ray then).
+bool nee_sample(const OScene& S, uint32_t seed[4], f3 P, f3 N, f4 rc, f3& o, f3& dir, float& tmax, f4& contrib) {
+    const uint32_t n = (uint32_t)S.emit_thr.size();
+    const float x = rand1(seed) * (float)n;
+    uint32_t i = (uint32_t)x;
+    if (i > n - 1u) i = n - 1u;
+    const float frac = x - (float)i;
+    const uint32_t j = frac < S.emit_thr[i] ? i : S.emit_alias[i];
+    const f2 r = rand2(seed);
+    const float* g = &S.emit[20 * (size_t)j];
+    const float su = std::sqrt(r.x), bs = su * (1.0f - r.y), bt = su * r.y;
+    const f3 q{(g[0] + g[4] * bs) + g[8] * bt, (g[1] + g[5] * bs) + g[9] * bt, (g[2] + g[6] * bs) + g[10] * bt};
+    o = fma3(N, 0.001f, P);
+    const f3 lv = sub(q, o);
+    const float d2 = dot3(lv, lv);
+    const float dist = std::sqrt(d2);
+    if (!(dist > 2e-3f)) return false;
+    const float inv = 1.0f / dist;
+    dir = f3{lv.x * inv, lv.y * inv, lv.z * inv};
+    const float cs = dot3(N, dir);
+    if (!(cs > 0.0f)) return false;
+    const float cl = std::fabs(dot3(f3{g[12], g[13], g[14]}, dir));
+    if (!(cl > 0.0f)) return false;
+    const float gm = ((cs * cl) * g[3]) / (d2 * 3.14159265358979323846f);
+    const f4 le{g[16], g[17], g[18], g[19]};
+    const f4 c = mul4(rc, le);
+    contrib = f4{c.x * gm, c.y * gm, c.z * gm, c.w * gm};
+    tmax = dist - 1e-3f;
+    return true;
+}
+
+// Where a vertex's NEE samples go: the sample's accumulator, times the primary albedo when
+// the sample's first bounce was metallic (Shading.slang:1159-1171).
+struct NeeAcc {
+    f4* acc;
+    bool metal;
+    f4 palb;
+};
+
+// FPathTracingRendererV2::GetRayColor (Shading.slang:1003-1082), plus the emissive-triangle
+// NEE of its diffuse-lobe vertices when nee is given.
 bool get_ray_color(const OScene& S, const GkrtFrameConstants& fc, Vtx& v, f3& dir, f4& color, uint32_t seed[4],
-                   bool& hitReflect, bool& hitMetal, uint64_t* rays) {
+                   bool& hitReflect, bool& hitMetal, uint64_t* rays, const NeeAcc* nee = nullptr) {
     const GkrtMaterial& mat = get_mat(S, v.mat);
     const bool diel = mat.material_model == GKRT_MAT_DIELECTRIC;
     const float startPosOffset = diel ? 0.0f : 1.0f;
@@ -506,11 +560,25 @@ bool get_ray_color(const OScene& S, const GkrtFrameConstants& fc, Vtx& v, f3& di
     hitMetal = chanceMetal;
     if (diel && !chanceReflect) tdir = refract3(dir, outward, niOverNt);
     dir = tdir;
+    const bool neeLobe = nee && !S.emit_thr.empty() && !back && !diel && !chanceGGX;
+    if (neeLobe) {
+        f3 so, sd;
+        float stmax;
+        f4 contrib;
+        if (nee_sample(S, seed, v.P, v.N, color, so, sd, stmax, contrib)) {
+            if (nee->metal) contrib = mul4(contrib, nee->palb);
+            if (!trace_segment(S, so, sd, stmax, rays)) *nee->acc = add4(*nee->acc, contrib);
+        }
+    }
     f3 org = fma3(v.N, 0.001f * startPosOffset, v.P);
     Vtx nv;
     if (trace_ray(S, org, tdir, kPT_MAX, nv, nullptr, rays)) {
         v = nv;
         const GkrtMaterial& hm = get_mat(S, v.mat);
+        if (neeLobe && hm.material_model == GKRT_MAT_DIFFUSE_LIGHT) {
+            color = f4{0.0f, 0.0f, 0.0f, 0.0f};   // this emitter is the NEE's to count
+            return true;
+        }
         f4 alb{hm.diffuse[0], hm.diffuse[1], hm.diffuse[2], hm.diffuse[3]};
         if (hm.material_model == GKRT_MAT_DIFFUSE_LIGHT || !chanceReflect) color = mul4(color, alb);
         if (back && !diel) {
@@ -622,14 +690,19 @@ void shade_pixel(const OScene& S, const GkrtFrameConstants& fc, int W, int H, in
         f3 dir = normalize3(sub(pv.P, xyz(eye)));
         Vtx vs = pv;
         bool hitReflect = false, hitMetal = false;
-        bool exitFirst = get_ray_color(S, fc, vs, dir, rc, seed, hitReflect, hitMetal, rays);
+        const bool nee_on = fc.nee_mode == GKRT_NEE_EMISSIVE;
+        // a first-vertex NEE sample exists only for a diffuse first bounce: accumulator fcol
+        const NeeAcc nee_first{&fcol, false, primaryAlbedo};
+        bool exitFirst = get_ray_color(S, fc, vs, dir, rc, seed, hitReflect, hitMetal, rays,
+                                       nee_on ? &nee_first : nullptr);
+        const NeeAcc nee_rest{hitReflect ? &frefl : &fcol, hitMetal, primaryAlbedo};
         if (!exitFirst) {
             if (fc.fast_gather && !pdiel) {
                 rc = mul4(rc, probe_term(S, vs.P, vs.N));
             } else {
                 for (uint32_t b = 1; b < maxB; ++b) {
                     bool dc = false;
-                    if (get_ray_color(S, fc, vs, dir, rc, seed, dc, dc, rays)) break;
+                    if (get_ray_color(S, fc, vs, dir, rc, seed, dc, dc, rays, nee_on ? &nee_rest : nullptr)) break;
                     if (fc.has_sun && rand1(seed) < 0.5f) {
                         f3 sun = f3{fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]};
                         f3 cd = align_with_normal(cone(seed, kCosQuarterDeg), sun);
@@ -938,6 +1011,270 @@ void denoise_pixel(const GkrtFrameConstants& fc, int W, int H, int x, int y, voi
     write_composed(fc, pix, total, im);
 }
 
+// Emissive-triangle table and alias table (Walker's method, Vose's construction): entries in
+// the order instance, material slot 0..15, triangle; pick probability power / total with
+// power = area x luminance of the emission; w = area / probability = total / luminance.
+void build_emitters(OScene& S) {
+    std::vector<float> power, lum;
+    for (const GkrtInstance& in : S.inst) {
+        if (!in.visible) continue;
+        const GkrtMesh& m = S.meshes[in.mesh_id];
+        for (int slot = 0; slot < 16; ++slot) {
+            if (in.mat_id[slot] >= S.mats.size()) continue;
+            const GkrtMaterial& mt = S.mats[in.mat_id[slot]];
+            if (mt.material_model != GKRT_MAT_DIFFUSE_LIGHT) continue;
+            const float l = (0.2126f * mt.diffuse[0] + 0.7152f * mt.diffuse[1]) + 0.0722f * mt.diffuse[2];
+            if (!(l > 0.0f)) continue;
+            for (uint32_t t = 0; t < m.index_count / 3; ++t) {
+                if ((S.slot[S.idx[m.index_offset + 3 * t] + m.vertex_offset] & 15u) != (uint32_t)slot) continue;
+                float w[3][3];
+                for (int v = 0; v < 3; ++v) {
+                    const f3 p = S.pos[S.idx[m.index_offset + 3 * t + v] + m.vertex_offset];
+                    for (int r = 0; r < 3; ++r)
+                        w[v][r] = ((in.world[4 * r] * p.x + in.world[4 * r + 1] * p.y) + in.world[4 * r + 2] * p.z) +
+                                  in.world[4 * r + 3];
+                }
+                float e1[3], e2[3];
+                for (int r = 0; r < 3; ++r) { e1[r] = w[1][r] - w[0][r]; e2[r] = w[2][r] - w[0][r]; }
+                const float cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                            cz = e1[0] * e2[1] - e1[1] * e2[0];
+                const float len = std::sqrt((cx * cx + cy * cy) + cz * cz);
+                const float area = 0.5f * len;
+                if (!(area > 0.0f) || !std::isfinite(area)) continue;
+                const float inv = 1.0f / len;
+                const float e[20] = {w[0][0], w[0][1], w[0][2], 0.0f, e1[0], e1[1], e1[2], 0.0f,
+                                     e2[0], e2[1], e2[2], 0.0f, cx * inv, cy * inv, cz * inv, 0.0f,
+                                     mt.diffuse[0], mt.diffuse[1], mt.diffuse[2], mt.diffuse[3]};
+                S.emit.insert(S.emit.end(), e, e + 20);
+                power.push_back(area * l);
+                lum.push_back(l);
+            }
+        }
+    }
+    const size_t n = power.size();
+    if (n == 0) return;
+    double total = 0.0;
+    for (size_t j = 0; j < n; ++j) total += (double)power[j];
+    for (size_t j = 0; j < n; ++j) S.emit[20 * j + 3] = (float)(total / (double)lum[j]);
+    std::vector<double> q(n);
+    std::vector<size_t> under, over;
+    for (size_t j = 0; j < n; ++j) {
+        q[j] = (double)power[j] * (double)n / total;
+        if (q[j] < 1.0) under.push_back(j);
+        else over.push_back(j);
+    }
+    S.emit_thr.assign(n, 1.0f);
+    S.emit_alias.resize(n);
+    for (size_t j = 0; j < n; ++j) S.emit_alias[j] = (uint32_t)j;
+    while (!under.empty() && !over.empty()) {
+        const size_t a = under.back(), b = over.back();
+        under.pop_back();
+        over.pop_back();
+        S.emit_thr[a] = (float)q[a];
+        S.emit_alias[a] = (uint32_t)b;
+        q[b] = (q[b] + q[a]) - 1.0;
+        if (q[b] < 1.0) under.push_back(b);
+        else over.push_back(b);
+    }
+}
+
+
+// ---- differentiable rendering (path replay): restatement of the GPU adjoint ----
+// The paths are built with the same FP32 operations as the forward estimator; the derivative
+// terms (products of the other factors, score terms) and their sums are FP64.
+struct AdjFactor {
+    f4 f;
+    uint32_t mat;
+};
+struct AdjPath {
+    std::vector<AdjFactor> fac;
+    std::vector<std::pair<uint32_t, double>> ggx;   // (material, d log p / d a)
+    f4 rest{1.0f, 1.0f, 1.0f, 1.0f};
+};
+
+float ggx_terms(float a, float c) {   // a^2 (1 + a^2) / (c^2 (a^2 - 1) + 1)^2
+    const float a2 = a * a;
+    const float q = fma_(c * c, a2 - 1.0f, 1.0f);
+    return (a2 * (1.0f + a2)) / (q * q);
+}
+double ggx_score_d(double a, double c) {
+    const double a2 = a * a, c2 = c * c;
+    return 2.0 / a + 2.0 * a / (1.0 + a2) - 4.0 * a * c2 / (c2 * (a2 - 1.0) + 1.0);
+}
+
+bool adj_ray_color(const OScene& S, const GkrtFrameConstants& fc, const float* sample_rough, Vtx& v, f3& dir,
+                   f4& color, uint32_t seed[4], bool first, bool& hitReflect, bool& hitMetal, AdjPath& R,
+                   uint64_t* rays) {
+    const GkrtMaterial& mat = get_mat(S, v.mat);
+    const bool diel = mat.material_model == GKRT_MAT_DIELECTRIC;
+    const float startPosOffset = diel ? 0.0f : 1.0f;
+    const float dotValue = dot3(dir, v.N);
+    const bool back = dotValue > 0.0f;
+    const f3 outward = back ? neg(v.N) : v.N;
+    const float niOverNt = back ? mat.refraction_index2 : (1.0f / mat.refraction_index2);
+    const float cosine = dotValue > 0.0f ? mat.refraction_index * dotValue : -dotValue;
+    const float reflectProb = schlick(cosine, mat.refraction_index);
+    const bool chanceReflect = rand1(seed) < reflectProb;
+    const bool chanceMetal = rand1(seed) < mat.metalness;
+    const bool chanceGGX = chanceReflect || chanceMetal;
+    f3 tdir;
+    float c = 0.0f, a_s = 0.0f;
+    if (chanceGGX) {
+        const f3 axis = reflect3(dir, outward);
+        const uint32_t nm = (uint32_t)S.mats.size();
+        const float fs = sample_rough ? sample_rough[v.mat < nm ? v.mat : nm - 1] : mat.fuzziness;
+        const float r = std::sqrt(fs);
+        a_s = r * r;
+        tdir = ggx_sampling(seed, r, axis);
+        c = dot3(axis, tdir);
+    } else {
+        tdir = align_with_normal(hemi1(seed), outward);
+    }
+    if (first) { hitReflect = chanceGGX; hitMetal = chanceMetal; }
+    const bool refracted = diel && !chanceReflect;
+    if (refracted) tdir = refract3(dir, outward, niOverNt);
+    if (chanceGGX && !refracted && a_s > 1e-6f) {
+        const float re = std::sqrt(mat.fuzziness);
+        const float a_e = re * re;
+        if (a_e != a_s) {
+            const float w = ggx_terms(a_e, c) / ggx_terms(a_s, c);
+            color = f4{color.x * w, color.y * w, color.z * w, color.w * w};
+            R.rest = f4{R.rest.x * w, R.rest.y * w, R.rest.z * w, R.rest.w * w};
+        }
+        R.ggx.push_back({v.mat, a_e > 1e-6f ? ggx_score_d((double)a_e, (double)c) : 0.0});
+    }
+    dir = tdir;
+    const f3 org = fma3(v.N, 0.001f * startPosOffset, v.P);
+    Vtx nv;
+    if (trace_ray(S, org, tdir, kPT_MAX, nv, nullptr, rays)) {
+        v = nv;
+        const GkrtMaterial& hm = get_mat(S, v.mat);
+        const f4 alb{hm.diffuse[0], hm.diffuse[1], hm.diffuse[2], hm.diffuse[3]};
+        if (hm.material_model == GKRT_MAT_DIFFUSE_LIGHT || !chanceReflect) {
+            color = mul4(color, alb);
+            R.fac.push_back({alb, v.mat});
+        }
+        if (back && !diel) {
+            color = f4{0.5f, 0.5f, 0.5f, 0.0f};
+            R.fac.clear();
+            R.ggx.clear();
+            R.rest = color;
+            return true;
+        }
+        return hm.material_model == GKRT_MAT_DIFFUSE_LIGHT;
+    }
+    const f4 sk = sky_color(fc);
+    color = mul4(color, sk);
+    R.rest = mul4(R.rest, sk);
+    return true;
+}
+
+// One pixel: image (composed radiance) and, when dimg is given, the gradient sums.
+void adjoint_pixel(const OScene& S, const GkrtFrameConstants& fc, int W, int H, int x, int y, uint32_t spp,
+                   const float* sample_rough, float* img, const float* dimg, double* ga, double* gr, uint64_t* rays) {
+    uint32_t seed[4] = {(uint32_t)x, (uint32_t)y, fc.total_frames, 0u};
+    float uvx = fma_((float)x / (float)W, 2.0f, -1.0f);
+    float uvy = fma_((float)y / (float)H, 2.0f, -1.0f);
+    if (fc.taa) {
+        const float* h = kHalton[fc.total_frames % 8];
+        uvx = uvx + (h[0] - 0.5f) / (float)W;
+        uvy = uvy + (h[1] - 0.5f) / (float)H;
+    }
+    f2 disk = unit_disk(seed);
+    float ha = fc.aperture / 2.0f;
+    f2 off{ha * disk.x, ha * disk.y};
+    f4 origin = mat4_mul(fc.model_view_inverse, f4{off.x, off.y, 0.0f, 1.0f});
+    f4 target = mat4_mul(fc.projection_inverse, f4{uvx, uvy, 1.0f, 1.0f});
+    f3 tv = f3{fma_(target.x, fc.focus_distance, -off.x), fma_(target.y, fc.focus_distance, -off.y),
+               target.z * fc.focus_distance};
+    f3 tn = normalize3(tv);
+    f4 direction = mat4_mul(fc.model_view_inverse, f4{tn.x, tn.y, tn.z, 0.0f});
+    f3 o3 = xyz(origin), d3 = xyz(direction);
+    Vtx pv;
+    const size_t pix = (size_t)y * W + x;
+    float* out = img ? img + 4 * pix : nullptr;
+    if (!trace_ray(S, o3, d3, kPT_MAX, pv, nullptr, rays)) {
+        const f4 sk = sky_color(fc);
+        if (out) { out[0] = sk.x; out[1] = sk.y; out[2] = sk.z; out[3] = 1.0f; }
+        return;
+    }
+    const GkrtMaterial& pm = get_mat(S, pv.mat);
+    if (pm.material_model != GKRT_MAT_DIELECTRIC) pv.P = fma3(normalize3(d3), -0.03f, pv.P);
+    if (pm.material_model == GKRT_MAT_DIFFUSE_LIGHT) {
+        if (out) { out[0] = pm.diffuse[0]; out[1] = pm.diffuse[1]; out[2] = pm.diffuse[2]; out[3] = 1.0f; }
+        return;
+    }
+    const bool pdiel = pm.material_model == GKRT_MAT_DIELECTRIC;
+    const uint32_t maxB = pdiel ? fc.max_number_of_bounces : fc.number_of_bounces;
+    const f4 eye = mat4_mul(fc.model_view_inverse, f4{0.0f, 0.0f, 0.0f, 1.0f});
+    const f4 ap{pm.diffuse[0], pm.diffuse[1], pm.diffuse[2], pm.diffuse[3]};
+    const double g[3] = {dimg ? dimg[4 * pix] : 0.0, dimg ? dimg[4 * pix + 1] : 0.0, dimg ? dimg[4 * pix + 2] : 0.0};
+    const uint32_t nm = (uint32_t)S.mats.size();
+    f4 fcol{0.0f, 0.0f, 0.0f, 0.0f}, frefl{0.0f, 0.0f, 0.0f, 0.0f};
+    for (uint32_t i = 0; i < spp; ++i) {
+        AdjPath R;
+        f4 rc{1.0f, 1.0f, 1.0f, 1.0f};
+        f3 dir = normalize3(sub(pv.P, xyz(eye)));
+        Vtx vs = pv;
+        bool hitReflect = false, hitMetal = false, dc = false;
+        const bool exitFirst = adj_ray_color(S, fc, sample_rough, vs, dir, rc, seed, true, hitReflect, hitMetal, R, rays);
+        if (!exitFirst) {
+            if (fc.fast_gather && !pdiel) {
+                const f4 pt = probe_term(S, vs.P, vs.N);
+                rc = mul4(rc, pt);
+                R.rest = mul4(R.rest, pt);
+            } else {
+                for (uint32_t b = 1; b < maxB; ++b) {
+                    if (adj_ray_color(S, fc, sample_rough, vs, dir, rc, seed, false, dc, dc, R, rays)) break;
+                    const bool early = !pdiel && rand1(seed) < 0.5f;
+                    if (b == maxB - 1 || early) {
+                        const f4 pt = probe_term(S, vs.P, vs.N);
+                        rc = mul4(rc, pt);
+                        R.rest = mul4(R.rest, pt);
+                        break;
+                    }
+                }
+            }
+        }
+        if (hitMetal) {
+            rc = mul4(rc, ap);
+            R.fac.push_back({ap, pv.mat});
+        }
+        if (hitReflect) frefl = add4(frefl, rc);
+        else fcol = add4(fcol, rc);
+        if (dimg) {
+            const double sp = (double)spp;
+            double u[3];
+            const double apd[3] = {ap.x, ap.y, ap.z};
+            const double rcd[3] = {rc.x, rc.y, rc.z};
+            for (int k = 0; k < 3; ++k) u[k] = hitReflect ? g[k] / sp : g[k] * apd[k] / sp;
+            const uint32_t mp = pv.mat < nm ? pv.mat : nm - 1;
+            if (!hitReflect)
+                for (int k = 0; k < 3; ++k) ga[3 * mp + k] += g[k] * rcd[k] / sp;
+            const size_t nf = R.fac.size();
+            for (size_t k = 0; k < nf; ++k) {
+                double d[3] = {R.rest.x, R.rest.y, R.rest.z};
+                for (size_t j = 0; j < nf; ++j) {
+                    if (j == k) continue;
+                    d[0] *= R.fac[j].f.x; d[1] *= R.fac[j].f.y; d[2] *= R.fac[j].f.z;
+                }
+                const uint32_t mk = R.fac[k].mat < nm ? R.fac[k].mat : nm - 1;
+                for (int q = 0; q < 3; ++q) ga[3 * mk + q] += d[q] * u[q];
+            }
+            const double uc = u[0] * rcd[0] + u[1] * rcd[1] + u[2] * rcd[2];
+            for (const auto& e : R.ggx) gr[e.first < nm ? e.first : nm - 1] += uc * e.second;
+        }
+    }
+    if (out) {
+        const float fs = (float)spp;
+        fcol = f4{fcol.x / fs, fcol.y / fs, fcol.z / fs, fcol.w / fs};
+        frefl = f4{frefl.x / fs, frefl.y / fs, frefl.z / fs, frefl.w / fs};
+        out[0] = fma_(fcol.x, ap.x, frefl.x);
+        out[1] = fma_(fcol.y, ap.y, frefl.y);
+        out[2] = fma_(fcol.z, ap.z, frefl.z);
+        out[3] = 1.0f;
+    }
+}
 }  // namespace
 
 // ===================================== C API ==========================================
@@ -956,6 +1293,7 @@ void* gko_scene_create(const GkrtSceneDesc* d) {
     S->meshes.assign(d->meshes, d->meshes + d->mesh_count);
     S->mats.assign(d->materials, d->materials + d->material_count);
     S->inst.assign(d->instances, d->instances + d->instance_count);
+    build_emitters(*S);
     if (d->lights && d->light_count) S->lights.assign(d->lights, d->lights + d->light_count);
     if (d->probe_cubes && d->probe_voxels) {
         size_t n = (size_t)kCubeXY * kCubeXY * kCubeZ;
@@ -1068,6 +1406,43 @@ uint64_t gko_trace_pass(void* s, const GkrtFrameConstants* fc, int W, int H, voi
         for (int64_t p = (int64_t)y0 * W; p < (int64_t)y1 * W; ++p)
             shade_pixel(S, *fc, W, H, (int)(p % W), (int)(p / W), images, &local);
         total += local;
+    }
+    return total.load();
+}
+
+// Adjoint restatement over the pixel window [x0, x1) x [y0, y1): image (dense W x H float4,
+// window written) and, when dimg is given, FP64 gradient sums (ga: 3 per material, gr: 1).
+uint64_t gko_adjoint(void* s, const GkrtFrameConstants* fc, int W, int H, int x0, int y0, int x1, int y1,
+                     uint32_t spp, const float* sample_rough, float* img, const float* dimg, double* ga, double* gr,
+                     int threads) {
+    const OScene& S = *(const OScene*)s;
+    const size_t nm = S.mats.size();
+    std::atomic<uint64_t> total{0};
+    std::vector<std::vector<double>> parts;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel
+#endif
+    {
+        std::vector<double> la(dimg ? 3 * nm : 0, 0.0), lr(dimg ? nm : 0, 0.0);
+        uint64_t local = 0;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16) nowait
+#endif
+        for (int64_t p = 0; p < (int64_t)(x1 - x0) * (y1 - y0); ++p) {
+            const int x = x0 + (int)(p % (x1 - x0)), y = y0 + (int)(p / (x1 - x0));
+            adjoint_pixel(S, *fc, W, H, x, y, spp, sample_rough, img, dimg, la.data(), lr.data(), &local);
+        }
+        total += local;
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        {
+            if (dimg) {
+                for (size_t k = 0; k < 3 * nm; ++k) ga[k] += la[k];
+                for (size_t k = 0; k < nm; ++k) gr[k] += lr[k];
+            }
+        }
     }
     return total.load();
 }

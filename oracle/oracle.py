@@ -49,6 +49,10 @@ def lib():
         L.gko_scene_create.argtypes = [C.POINTER(abi.GkrtSceneDesc)]
         L.gko_scene_destroy.argtypes = [C.c_void_p]
         L.gko_trace_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_int]
+        L.gko_adjoint.restype = C.c_uint64
+        L.gko_adjoint.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_int, C.c_int, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_int]
         L.gko_trace_pass.restype = C.c_uint64
         L.gko_trace_pass.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_int, C.c_int,
                                      C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
@@ -113,6 +117,22 @@ class OracleScene:
 
     def trace_pass(self, fc, width, height, images, y0=0, y1=0, threads=0) -> int:
         return int(lib().gko_trace_pass(self.h, C.byref(fc), width, height, _ptrs(images), y0, y1, threads))
+
+    def adjoint(self, fc, width, height, spp, sample_rough=None, dimage=None, window=None, threads=0):
+        """The differentiable estimator over a pixel window (x0, y0, x1, y1): the composed image
+        (dense H x W x 4, zero outside the window) and, when dimage (H x W x 4) is given, the
+        FP64 gradient sums (albedo (n, 3), roughness (n,))."""
+        x0, y0, x1, y1 = window or (0, 0, width, height)
+        nm = self.scene.materials.shape[0]
+        img = np.zeros((height, width, 4), np.float32)
+        ga = np.zeros((nm, 3), np.float64)
+        gr = np.zeros(nm, np.float64)
+        sr = None if sample_rough is None else np.ascontiguousarray(sample_rough, np.float32)
+        di = None if dimage is None else np.ascontiguousarray(dimage, np.float32)
+        lib().gko_adjoint(self.h, C.byref(fc), width, height, x0, y0, x1, y1, spp,
+                          sr.ctypes.data if sr is not None else None, img.ctypes.data,
+                          di.ctypes.data if di is not None else None, ga.ctypes.data, gr.ctypes.data, threads)
+        return img, ga, gr
 
 
 def reproject_pass(fc, width, height, images, threads=0):

@@ -240,3 +240,72 @@ def test_fp32_bounds_far_small_triangles():
             assert f[5] <= f[1]
         certain += kind != 2
     assert certain > 0.95 * n
+
+
+def _cornell_mean(mode, frames, W=24, H=24):
+    """Mean and per-sample variance of the 1-spp radiance (diffuse + specular) over frames."""
+    sc, cam, st = scenes.cornell()
+    osc = O.OracleScene(sc)
+    st.nee_mode = mode
+    fb = camera.FrameBuilder(W, H, st)
+    acc = np.zeros((H, W, 3))
+    acc2 = np.zeros((H, W, 3))
+    for f in range(frames):
+        im = O.new_images(W, H)
+        osc.trace_pass(fb.build(cam, f), W, H, im)
+        v = (im[abi.IMG_SINGLE_DIFFUSE] + im[abi.IMG_SINGLE_SPECULAR])[..., :3].astype(np.float64)
+        acc += v
+        acc2 += v * v
+    m = acc / frames
+    return m.mean(), (acc2 / frames - m * m).mean(), W * H * 3
+
+
+def test_emissive_nee_matches_bsdf_sampling_in_expectation():
+    """GKRT_NEE_EMISSIVE replaces the emission that diffuse bounces reach by light samples at
+    the vertices they leave: the same expectation, far lower variance."""
+    frames = 1500
+    m0, v0, n = _cornell_mean(abi.NEE_REFERENCE, frames)
+    m1, v1, _ = _cornell_mean(abi.NEE_EMISSIVE, frames)
+    se = math.sqrt((v0 + v1) / (frames * n))
+    assert abs(m0 - m1) < 4.0 * se, (m0, m1, se)
+    assert v1 < 0.1 * v0, (v0, v1)
+
+
+def test_adjoint_oracle_matches_finite_differences():
+    """The FP64 path-replay gradients of the oracle against central differences (h = 1e-3)
+    of its own estimator, sampled with fixed (detached) roughness: 24 albedo and 8
+    roughness parameters within 1%."""
+    sc, cam, st = scenes.cornell_materials(spp=4)
+    W = H = 40
+    fc = camera.FrameBuilder(W, H, st).build(cam, 0)
+    tgt = np.random.default_rng(0).uniform(0, 0.5, (H, W, 3))
+    a0 = sc.materials["diffuse"][:, :3].copy()
+    r0 = sc.materials["fuzziness"].copy()
+
+    def loss(a, r):
+        m = sc.materials.copy()
+        m["diffuse"][:, :3] = a
+        m["fuzziness"] = r
+        o = O.OracleScene(abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, m,
+                                          sc.instances))
+        img = o.adjoint(fc, W, H, 4, sample_rough=r0)[0][..., :3].astype(np.float64)
+        return ((img - tgt) ** 2).mean(), img
+
+    L0, img = loss(a0, r0)
+    dimg = np.zeros((H, W, 4), np.float32)
+    dimg[..., :3] = 2.0 * (img - tgt) / img.size
+    _, ga, gr = O.OracleScene(sc).adjoint(fc, W, H, 4, sample_rough=r0, dimage=dimg)
+    h = 1e-3
+    for m in np.argsort(-np.abs(ga[:256]).max(1))[:8]:
+        for c in range(3):
+            a1, a2 = a0.copy(), a0.copy()
+            a1[m, c] += h
+            a2[m, c] -= h
+            fd = (loss(a1, r0)[0] - loss(a2, r0)[0]) / (2 * h)
+            assert abs(ga[m, c] - fd) <= 0.01 * abs(fd), (m, c, ga[m, c], fd)
+    for m in np.argsort(-np.abs(gr[:256]))[:8]:
+        r1, r2 = r0.copy(), r0.copy()
+        r1[m] += h
+        r2[m] -= h
+        fd = (loss(a0, r1)[0] - loss(a0, r2)[0]) / (2 * h)
+        assert abs(gr[m] - fd) <= 0.01 * abs(fd), (m, gr[m], fd)
