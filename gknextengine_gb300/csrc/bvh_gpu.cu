@@ -100,7 +100,8 @@ __device__ __forceinline__ int bin_of(float c, float clo, float scale) {
     return min(max(b, 0), kBins - 1);
 }
 
-// Child `side` of node `parent` gets box and ref; a root's box goes to root_box instead.
+// Child `side` of node `parent` gets box (widened as node boxes are stored) and ref; a root's
+// box goes to root_box instead, unwidened.
 __device__ void write_child(BvhNode* nodes, float* root_box, int parent, int side, const float* box, int ref) {
     if (parent < 0) {
         float* rb = root_box + 6 * (-1 - parent);
@@ -108,7 +109,10 @@ __device__ void write_child(BvhNode* nodes, float* root_box, int parent, int sid
         return;
     }
     float* f = reinterpret_cast<float*>(nodes + parent);
-    for (int j = 0; j < 6; ++j) f[6 * side + j] = box[j];
+    for (int j = 0; j < 3; ++j) {
+        f[6 * side + j] = widen_lo(box[j]);
+        f[6 * side + 3 + j] = widen_hi(box[3 + j]);
+    }
     reinterpret_cast<int*>(nodes + parent)[12 + side] = ref;
 }
 
@@ -551,8 +555,8 @@ __global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, 
                 // a root that is a single leaf: interior root whose second child never intersects
                 write_child(nodes, root_box, it.parent, it.side, box, 0);
                 BvhNode nd;
-                nd.a = make_float4(box[0], box[1], box[2], box[3]);
-                nd.b = make_float4(box[4], box[5], kFar, kFar);
+                nd.a = make_float4(widen_lo(box[0]), widen_lo(box[1]), widen_lo(box[2]), widen_hi(box[3]));
+                nd.b = make_float4(widen_hi(box[4]), widen_hi(box[5]), kFar, kFar);
                 nd.c = make_float4(kFar, kFar, kFar, kFar);
                 nd.d = make_int4(ref, kRefPop, 0, 0);
                 nodes[S.root_node] = nd;

@@ -127,9 +127,9 @@ struct Builder {
         int lref = build(b, mid, lb, depth + 1);
         int rref = build(mid, e, rb, depth + 1);
         BvhNode& nd = out->nodes[me];
-        nd.a = make_float4(lb.lo[0], lb.lo[1], lb.lo[2], lb.hi[0]);
-        nd.b = make_float4(lb.hi[1], lb.hi[2], rb.lo[0], rb.lo[1]);
-        nd.c = make_float4(rb.lo[2], rb.hi[0], rb.hi[1], rb.hi[2]);
+        nd.a = make_float4(widen_lo(lb.lo[0]), widen_lo(lb.lo[1]), widen_lo(lb.lo[2]), widen_hi(lb.hi[0]));
+        nd.b = make_float4(widen_hi(lb.hi[1]), widen_hi(lb.hi[2]), widen_lo(rb.lo[0]), widen_lo(rb.lo[1]));
+        nd.c = make_float4(widen_lo(rb.lo[2]), widen_hi(rb.hi[0]), widen_hi(rb.hi[1]), widen_hi(rb.hi[2]));
         nd.d = make_int4(lref, rref, 0, 0);
         return (int)node_base + me;
     }
@@ -163,8 +163,8 @@ void build_bvh_host(const float* boxes, uint32_t n, uint32_t max_leaf, uint32_t 
         // a single leaf: wrap it in an interior root whose second child never intersects
         BvhNode nd;
         const float far = 1e30f;
-        nd.a = make_float4(box.lo[0], box.lo[1], box.lo[2], box.hi[0]);
-        nd.b = make_float4(box.hi[1], box.hi[2], far, far);
+        nd.a = make_float4(widen_lo(box.lo[0]), widen_lo(box.lo[1]), widen_lo(box.lo[2]), widen_hi(box.hi[0]));
+        nd.b = make_float4(widen_hi(box.hi[1]), widen_hi(box.hi[2]), far, far);
         nd.c = make_float4(far, far, far, far);
         nd.d = make_int4(ref, kRefPop, 0, 0);
         out.nodes.insert(out.nodes.begin(), nd);

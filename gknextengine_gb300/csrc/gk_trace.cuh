@@ -15,7 +15,10 @@
 //   * two hits whose t-intervals overlap -> both are decided in FP64 (the incumbent's
 //     triangle is fetched again) and the key is compared exactly.
 // Box tests widen the slab interval by 1e-6 relative (> 2.5 gamma_3), so no box holding
-// the FP64 winner is culled. The float t and barycentrics used for shading are those of
+// the FP64 winner is culled. A ray component of exactly zero lying on a box face is the one
+// case a t-interval widening cannot cover ((hi - o) * inv is 0 there), so the builders store
+// every node box widened in space as well (widen_lo / widen_hi): a triangle edge on the
+// face stays inside the box the ray is tested against. The float t and barycentrics used for shading are those of
 // the FP32 test when it is certain, else the rounded FP64 values.
 #pragma once
 #include "gk_device.cuh"
@@ -36,6 +39,10 @@ struct __align__(16) DevInst {
     uint32_t vertex_offset;
     uint32_t instance_id;
 };
+
+// Node boxes as stored: 1e-6 relative plus 1e-10 absolute beyond the primitives' bounds.
+GK_HD float widen_lo(float v) { return v - (fabsf(v) * 1e-6f + 1e-10f); }
+GK_HD float widen_hi(float v) { return v + (fabsf(v) * 1e-6f + 1e-10f); }
 
 constexpr int kStackSize = 64;
 constexpr int kRefPop = 0x7FFFFFFE;

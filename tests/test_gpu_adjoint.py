@@ -127,7 +127,11 @@ def test_adjoint_matches_finite_differences(env):
 
 def test_adam_fit_recovers_hidden_materials(env):
     """200 Adam steps (lr 1e-2) from a uniform start against a target rendered with the
-    hidden materials and independent noise: the albedo error of the visible materials falls."""
+    hidden materials and independent noise. The L2 loss of a noisy image contains the
+    estimator's variance, whose gradient would darken the materials; the fit therefore uses
+    the decorrelated gradient 2 (I_a - T) dI_b/dtheta of two independent renders (an unbiased
+    gradient of |E[I] - T|^2). Both the decorrelated loss (I_a - T)(I_b - T) and the albedo
+    error of the materials fall."""
     sc, cam, st, r, fc = env
     torch = _torch()
     from gknextengine_gb300.autograd import render_materials
@@ -146,21 +150,28 @@ def test_adam_fit_recovers_hidden_materials(env):
     t0 = time.perf_counter()
     for step in range(200):
         opt.zero_grad()
-        img = render_materials(r, fb.build(cam, step), SPP, albedo, rough)
-        loss = ((img - target) ** 2).mean()
-        loss.backward()
+        with torch.no_grad():
+            img_a = render_materials(r, fb.build(cam, 2 * step), SPP, albedo, rough)
+        img_b = render_materials(r, fb.build(cam, 2 * step + 1), SPP, albedo, rough)
+        resid = (img_a - target).detach()
+        (2.0 * resid * img_b).mean().backward()
         opt.step()
         with torch.no_grad():
             albedo.clamp_(0.01, 1.0)
             rough.clamp_(0.02, 1.0)
-        losses.append(float(loss))
+            losses.append(float((resid * (img_b - target)).mean()))
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    # materials the camera sees (non-zero gradient at the start)
-    seen = albedo.grad.abs().sum(1) > 0
-    err0 = (0.5 - hid_a[seen]).abs().mean().item()
-    err1 = (albedo.detach()[seen] - hid_a[seen]).abs().mean().item()
-    print(f"adam: {dt / 200 * 1e3:.1f} ms/step, loss {losses[0]:.4g} -> {np.mean(losses[-10:]):.4g}, "
-          f"albedo error {err0:.4f} -> {err1:.4f} over {int(seen.sum())} materials")
-    assert np.mean(losses[-10:]) < 0.5 * losses[0]
+    with torch.no_grad():   # the loss floor: the hidden materials against the noisy target
+        floor = []
+        for k in range(5):
+            ia = render_materials(r, fb.build(cam, 20000 + 2 * k), SPP, hid_a, hid_r)
+            ib = render_materials(r, fb.build(cam, 20001 + 2 * k), SPP, hid_a, hid_r)
+            floor.append(float(((ia - target) * (ib - target)).mean()))
+    err0 = (0.5 - hid_a).abs().mean().item()
+    err1 = (albedo.detach() - hid_a).abs().mean().item()
+    l0, l1, lf = np.mean(losses[:5]), np.mean(losses[-10:]), np.mean(floor)
+    print(f"adam: {dt / 200 * 1e3:.1f} ms/step (2 forward + 1 backward), decorrelated loss {l0:.4g} -> {l1:.4g} "
+          f"(floor of the hidden materials {lf:.4g}), albedo mean abs error {err0:.4f} -> {err1:.4f}")
     assert err1 < 0.5 * err0
+    assert (l1 - lf) < 0.5 * (l0 - lf)

@@ -138,3 +138,32 @@ def test_instance_rebuild_per_frame(soup_env):
             assert_hits_equal(gpu_trace_rays(r, rays), O.OracleScene(sc2).trace_rays(rays))
     finally:
         r.update_instances(sc.instances)
+
+
+@pytest.mark.parametrize("host", [False, True])
+def test_rays_along_box_faces(host):
+    """Rays with direction components of exactly zero that run along tile boundaries, i.e.
+    exactly on the faces of the boxes around the tiles: hits on the shared edges must match
+    the FP64 definition (the stored node boxes are widened so no such box is culled)."""
+    sc, cam, st = scenes.cornell_materials(spp=1)
+    with PathTracingRenderer(0) as r:
+        r.load_scene(sc)
+        if host:
+            r.build_bvh(abi.BUILD_ALL | abi.BUILD_ON_HOST)
+        osc = O.OracleScene(sc)
+        rng = np.random.default_rng(15)
+        n = 30000
+        edges = (np.arange(17) / 16.0 - 0.5).astype(np.float32)
+        rays = np.zeros(n, abi.RAY_DTYPE)
+        rays["origin"][:, 0] = rng.choice(edges, n)
+        rays["origin"][:, 1] = rng.choice((edges + 0.5).astype(np.float32), n)
+        rays["origin"][:, 2] = rng.uniform(-0.45, 0.45, n).astype(np.float32)
+        d = rng.normal(size=(n, 3))
+        axis = rng.integers(0, 3, n)
+        d[np.arange(n), axis] = 0.0          # one component exactly zero
+        d[: n // 3, 1] = 0.0                 # and a third of the rays with two
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        rays["dir"] = d
+        rays["tmin"] = 1e-3
+        rays["tmax"] = 1000.0
+        assert_hits_equal(gpu_trace_rays(r, rays), osc.trace_rays(rays))
