@@ -513,6 +513,41 @@ cudaError_t gkrt_encode_tmap_2d(CUtensorMap* map, const void* base, uint32_t ele
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// cuTensorMapEncodeTiled for bf16 tensors of rank 2..5 with 64-byte swizzle (the K-major
+// operand layout of the tensor-core kernels); zeros outside the tensor.
+cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                  const uint64_t* strides_bytes, const uint32_t* box) {
+    typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
+        fn = (EncodeFn)p;
+    }
+    if (rank < 2 || rank > 5 || ((uintptr_t)base & 15u) || box[0] * 2u > 64u || (box[0] * 2u) % 16u) return cudaErrorInvalidValue;
+    cuuint64_t d[5], s[4];
+    cuuint32_t b[5], es[5];
+    for (uint32_t i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        es[i] = 1;
+        if (box[i] == 0 || box[i] > 256) return cudaErrorInvalidValue;
+    }
+    for (uint32_t i = 0; i + 1 < rank; ++i) {
+        s[i] = strides_bytes[i];
+        if (s[i] % 16u) return cudaErrorInvalidValue;
+    }
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, const_cast<void*>(base), d, s, b, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 int gkrt_internal_ready_view(GkrtContext* ctx, SceneView* view, unsigned long long** counters, int* device) {
     if (!ctx->has_scene || !ctx->blas_ready || !ctx->tlas_ready)
         return fail(ctx, GKRT_ERR_STATE, "scene and BVH must be built before this call (it allocates nothing)");
@@ -944,6 +979,28 @@ int gkrt_adjoint_backward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32
     GK_CUDA(gkrt_launch_adjoint(shade_scene(ctx), *fc, (int)ctx->W, (int)ctx->H, spp, sample_roughness, nullptr,
                                 (const float4*)d_image, grad_albedo, grad_roughness, ctx->d_counters, st));
     return GKRT_OK;
+}
+
+int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin, const void* w,
+                      const float* bias, uint32_t cout, void* y, uint32_t y_channels, uint32_t y_offset,
+                      uint32_t y_store, uint32_t flags, void* stream) {
+    if (!x || !w || !y || batch == 0 || height == 0 || width == 0 || batch > 65535 || height > 65535 ||
+        width > 65535 || cin > 4096 || flags > 3u)
+        return GKRT_ERR_INVALID_ARG;
+    ConvArgs a;
+    a.B = (int)batch; a.H = (int)height; a.W = (int)width; a.cin = (int)cin; a.cout = (int)cout;
+    a.bias = bias;
+    a.out = y;
+    a.out_c = (int)y_channels;
+    a.out_off = (int)y_offset;
+    a.n_store = (int)y_store;
+    a.flags = (int)flags;
+    static uint32_t* d_err = nullptr;   // the standalone kernels' error word
+    if (!d_err && cudaMalloc((void**)&d_err, 4) != cudaSuccess) return GKRT_ERR_OOM;
+    a.err = d_err;
+    cudaError_t e = gkrt_launch_conv3x3(x, w, a, (cudaStream_t)stream);
+    if (e == cudaErrorInvalidValue) return GKRT_ERR_INVALID_ARG;
+    return e == cudaSuccess ? GKRT_OK : GKRT_ERR_CUDA;
 }
 
 int gkrt_affine_inverse(const float w[12], float winv[12]) {

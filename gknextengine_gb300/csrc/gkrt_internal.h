@@ -43,6 +43,19 @@ struct AtrousArgs {
     float4 *final_out, *final_linear;
 };
 
+// 3x3 convolution on the tensor cores (k_conv.cu). x: NHWC bf16 [B][H][W][cin];
+// w: [cout][9][cin] bf16; out: NHWC with out_c channels, written at channel out_off.
+constexpr int kConvRelu = 1, kConvF32Out = 2;
+struct ConvArgs {
+    int B, H, W, cin, cout;        // cin % 32 == 0; cout % 16 == 0, 16..256 (MMA N)
+    const float* bias;             // cout floats or null
+    void* out;
+    int out_c, out_off;            // multiples of 16 (bf16 output)
+    int n_store;                   // fp32 output: channels stored (<= cout)
+    int flags;                     // kConvRelu | kConvF32Out
+    uint32_t* err;                 // device error word
+};
+
 // Host-side BVH build (binned SAH over boxes). Returns nodes in device layout and the leaf
 // order of the primitives; refs follow the encoding of gk_trace.cuh.
 struct HostBvh {
@@ -116,6 +129,8 @@ cudaError_t gkrt_launch_adjoint(const gk::ShadeScene& sc, const GkrtFrameConstan
                                 double* g_rough, unsigned long long* counters, cudaStream_t st);
 cudaError_t gkrt_launch_set_params(GkrtMaterial* mats, const float* alb, const float* rough, uint32_t first,
                                    uint32_t count, cudaStream_t st);
+cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const gk::ConvArgs& args, cudaStream_t st);
+size_t gkrt_conv_smem_bytes(int cout);
 cudaError_t gkrt_launch_reproject(const gk::ReprojectArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_compose(const gk::ComposeArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_atrous(const gk::AtrousArgs& a, const float4* in, float4* tmp0, float4* tmp1, cudaStream_t st);

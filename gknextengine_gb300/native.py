@@ -52,6 +52,8 @@ def load(path: str | None = None):
     L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
     L.gkrt_synchronize.argtypes = [vp, vp]
     L.gkrt_affine_inverse.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.gkrt_conv3x3_bf16.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp,
+                                    C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]
     L.gkrt_set_material_params.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_adjoint_forward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp]
     L.gkrt_adjoint_backward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp, vp, vp]
@@ -69,5 +71,5 @@ EXPORTED = [
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
     "gkrt_get_stats",
     "gkrt_synchronize", "gkrt_affine_inverse",
-    "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward",
+    "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16",
 ]

@@ -330,6 +330,18 @@ int  gkrt_adjoint_backward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint3
                            const float* sample_roughness, const float* d_image,
                            double* grad_albedo, double* grad_roughness, void* stream);
 
+/* 3x3 "same" convolution on the tensor cores (building block of the learned denoiser; no
+ * counterpart in the reference). x: NHWC bf16 [batch][height][width][cin], cin a multiple
+ * of 32; w: bf16 [cout][3][3][cin], cout a multiple of 16 in 16..256; bias: cout floats or
+ * NULL; y: NHWC with y_channels channels, written at channel y_offset (bf16, multiples of
+ * 16), or fp32 with GKRT_CONV_F32 (then only y_store channels are written). Device
+ * pointers, 16-byte aligned. */
+#define GKRT_CONV_RELU 1u
+#define GKRT_CONV_F32  2u
+int  gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin,
+                       const void* w, const float* bias, uint32_t cout, void* y, uint32_t y_channels,
+                       uint32_t y_offset, uint32_t y_store, uint32_t flags, void* stream);
+
 int  gkrt_get_stats(GkrtContext* ctx, GkrtStats* out);
 int  gkrt_synchronize(GkrtContext* ctx, void* stream);
 

@@ -1,0 +1,76 @@
+"""The tensor-core 3x3 convolution (gkrt_conv3x3_bf16) against torch's fp32 convolution of the
+same bf16 values: odd image sizes (partial tiles, zero padding from out-of-range TMA boxes),
+channel counts of the denoiser's layers, ReLU, bias, channel offsets into a wider tensor,
+fp32 output."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gknextengine_gb300 import abi, native
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    assert torch.cuda.is_available()
+    return torch
+
+
+def conv(x, w, bias, cout, out, out_c, out_off, n_store=0, flags=0):
+    L = native.load()
+    B, H, W, cin = x.shape
+    rc = L.gkrt_conv3x3_bf16(C.c_void_p(x.data_ptr()), B, H, W, cin, C.c_void_p(w.data_ptr()),
+                             C.c_void_p(bias.data_ptr() if bias is not None else 0), cout,
+                             C.c_void_p(out.data_ptr()), out_c, out_off, n_store, flags, None)
+    assert rc == abi.GKRT_OK, rc
+
+
+@pytest.mark.parametrize("B,H,W,cin,cout,relu", [(2, 37, 45, 64, 96, True), (1, 64, 64, 32, 32, False),
+                                                  (1, 24, 40, 224, 96, True), (1, 17, 33, 160, 64, True),
+                                                  (3, 8, 16, 96, 128, False), (1, 20, 20, 128, 256, True)])
+def test_conv_matches_torch(B, H, W, cin, cout, relu):
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(B * 1000 + cin + cout)
+    x = torch.randn((B, H, W, cin), device="cuda", generator=g).bfloat16()
+    w = (torch.randn((cout, 3, 3, cin), device="cuda", generator=g) / (3 * cin ** 0.5)).bfloat16()
+    bias = torch.randn(cout, device="cuda", generator=g) * 0.1
+    out_c, off = cout + 32, 16
+    out = torch.full((B, H, W, out_c), 7.0, device="cuda").bfloat16()
+    conv(x, w, bias, cout, out, out_c, off, flags=1 if relu else 0)
+    torch.cuda.synchronize()
+    ref = torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), w.float().permute(0, 3, 1, 2), bias, padding=1)
+    if relu:
+        ref = torch.relu(ref)
+    ref = ref.permute(0, 2, 3, 1)
+    got = out[..., off:off + cout].float()
+    torch.testing.assert_close(got, ref.bfloat16().float(), rtol=2e-2, atol=2e-2)
+    # channels outside the written range are untouched
+    assert bool((out[..., :off].float() == 7.0).all()) and bool((out[..., off + cout:].float() == 7.0).all())
+
+
+def test_conv_f32_output_subset():
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    B, H, W, cin, cout = 2, 19, 29, 32, 16
+    x = torch.randn((B, H, W, cin), device="cuda", generator=g).bfloat16()
+    w = (torch.randn((cout, 3, 3, cin), device="cuda", generator=g) / 17.0).bfloat16()
+    out = torch.full((B, H, W, 4), -5.0, device="cuda")
+    conv(x, w, None, cout, out, 4, 0, n_store=3, flags=2)
+    torch.cuda.synchronize()
+    ref = torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), w.float().permute(0, 3, 1, 2), padding=1)
+    ref = ref.permute(0, 2, 3, 1)[..., :3]
+    torch.testing.assert_close(out[..., :3], ref, rtol=1e-4, atol=1e-4)
+    assert bool((out[..., 3] == -5.0).all())
+
+
+def test_conv_rejects_bad_shapes():
+    torch = _torch()
+    x = torch.zeros((1, 8, 16, 48), device="cuda").bfloat16()   # cin not a multiple of 32
+    w = torch.zeros((16, 3, 3, 48), device="cuda").bfloat16()
+    out = torch.zeros((1, 8, 16, 16), device="cuda").bfloat16()
+    L = native.load()
+    rc = L.gkrt_conv3x3_bf16(C.c_void_p(x.data_ptr()), 1, 8, 16, 48, C.c_void_p(w.data_ptr()), None, 16,
+                             C.c_void_p(out.data_ptr()), 16, 0, 0, 0, None)
+    assert rc == abi.GKRT_ERR_INVALID_ARG
