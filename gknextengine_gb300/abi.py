@@ -32,6 +32,7 @@ MAT_LAMBERTIAN, MAT_METALLIC, MAT_DIELECTRIC, MAT_ISOTROPIC, MAT_DIFFUSE_LIGHT, 
 
 DENOISE_JBF = 0
 DENOISE_ATROUS = 1
+DENOISE_UNET = 2
 NEE_REFERENCE = 0
 NEE_EMISSIVE = 1
 FRAME_PRIMARY_IDS = 1

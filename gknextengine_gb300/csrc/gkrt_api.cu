@@ -67,6 +67,7 @@ struct GkrtContext {
     bool blas_ready = false, tlas_ready = false;
     uint32_t inst_cap = 0;            // instance arrays allocated for this many instances
 
+    Unet* unet = nullptr;                       // learned denoiser (gkrt_unet_init)
     unsigned long long* d_counters = nullptr;   // see flush_counters: 5 per-pass slots + total rays
     uint32_t* d_error = nullptr;
     unsigned int* d_work = nullptr;             // pixel counter of the persistent trace kernel
@@ -598,6 +599,8 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     cudaDeviceSynchronize();
     free_images(ctx);
     free_scene(ctx);
+    gkrt_unet_delete(ctx->unet);
+    ctx->unet = nullptr;
     gpu_bvh_free(ctx->builder);
     ctx->builder = nullptr;
     dfree(ctx->d_counters);
@@ -773,8 +776,28 @@ int gkrt_reproject_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* st
 int gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
     int rc = check_frame(ctx, fc);
     if (rc != GKRT_OK) return rc;
-    if (fc->denoiser > GKRT_DENOISE_ATROUS) return fail(ctx, GKRT_ERR_UNSUPPORTED, "unknown denoiser");
+    if (fc->denoiser > GKRT_DENOISE_UNET) return fail(ctx, GKRT_ERR_UNSUPPORTED, "unknown denoiser");
     cudaSetDevice(ctx->device);
+    if (fc->denoiser == GKRT_DENOISE_UNET) {
+        if (!ctx->unet) return fail(ctx, GKRT_ERR_STATE, "gkrt_unet_init was not called");
+        if (ctx->W % 8 || ctx->H % 8) return fail(ctx, GKRT_ERR_UNSUPPORTED, "the learned denoiser needs sizes divisible by 8");
+        cudaStream_t st = (cudaStream_t)stream;
+        GK_CUDA(gkrt_unet_denoise_frame(ctx->unet, (const float4*)ctx->img[GKRT_IMG_SINGLE_DIFFUSE],
+                                        (const float4*)ctx->img[GKRT_IMG_SINGLE_SPECULAR],
+                                        (const float4*)ctx->img[GKRT_IMG_ALBEDO], (const float4*)ctx->img[GKRT_IMG_NORMAL],
+                                        (const float*)ctx->img[GKRT_IMG_PREV_DEPTH], (int)ctx->W, (int)ctx->H,
+                                        (int)ctx->P, nullptr, st));
+        ComposeArgs a;
+        a.W = (int)ctx->W; a.H = (int)ctx->H; a.P = (int)ctx->P;
+        a.bf_size = 0; a.hdr = fc->hdr;
+        a.bf_sigma = 0.0f; a.bf_sigma_lum = 0.0f; a.paper_white_nit = fc->paper_white_nit; a.pad = 0.0f;
+        a.err = ctx->d_error;
+        a.acc_d = a.acc_s = a.acc_a = nullptr;
+        a.out = (float4*)ctx->img[GKRT_IMG_DENOISED];
+        a.out_linear = (float4*)ctx->img[GKRT_IMG_DENOISED_LINEAR];
+        GK_CUDA(gkrt_launch_unet_compose(a, gkrt_unet_output(ctx->unet), st));
+        return GKRT_OK;
+    }
     if (fc->denoiser == GKRT_DENOISE_ATROUS && fc->bf_size > 0u) {
         AtrousArgs a;
         a.W = (int)ctx->W; a.H = (int)ctx->H; a.P = (int)ctx->P;
@@ -989,6 +1012,7 @@ int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t w
         return GKRT_ERR_INVALID_ARG;
     ConvArgs a;
     a.B = (int)batch; a.H = (int)height; a.W = (int)width; a.cin = (int)cin; a.cout = (int)cout;
+    a.x_c = (int)cin; a.x_off = 0;
     a.bias = bias;
     a.out = y;
     a.out_c = (int)y_channels;
@@ -999,6 +1023,105 @@ int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t w
     if (!d_err && cudaMalloc((void**)&d_err, 4) != cudaSuccess) return GKRT_ERR_OOM;
     a.err = d_err;
     cudaError_t e = gkrt_launch_conv3x3(x, w, a, (cudaStream_t)stream);
+    if (e == cudaErrorInvalidValue) return GKRT_ERR_INVALID_ARG;
+    return e == cudaSuccess ? GKRT_OK : GKRT_ERR_CUDA;
+}
+
+// ---- learned denoiser ----
+static int unet_ready(GkrtContext* ctx) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->unet) return fail(ctx, GKRT_ERR_STATE, "gkrt_unet_init was not called");
+    cudaSetDevice(ctx->device);
+    return GKRT_OK;
+}
+static int unet_size_ok(GkrtContext* ctx, uint32_t b, uint32_t h, uint32_t w) {
+    if (b == 0 || b > 64 || h < 16 || w < 16 || h % 8 || w % 8 || h > 8192 || w > 8192)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "batch 1..64, sizes multiples of 8 from 16 to 8192");
+    return GKRT_OK;
+}
+
+int gkrt_unet_init(GkrtContext* ctx, uint64_t seed) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->unet && !(ctx->unet = gkrt_unet_new())) return fail(ctx, GKRT_ERR_OOM, "denoiser");
+    GK_CUDA(gkrt_unet_init_params(ctx->unet, seed));
+    return GKRT_OK;
+}
+
+int gkrt_unet_param_count(GkrtContext* ctx, uint32_t* count) {
+    if (!ctx || !count) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->unet && !(ctx->unet = gkrt_unet_new())) return fail(ctx, GKRT_ERR_OOM, "denoiser");
+    *count = (uint32_t)gkrt_unet_nparams(ctx->unet);
+    return GKRT_OK;
+}
+
+int gkrt_unet_get_params(GkrtContext* ctx, float* params, float* grads) {
+    int rc = unet_ready(ctx);
+    if (rc != GKRT_OK) return rc;
+    GK_CUDA(gkrt_unet_get_params_host(ctx->unet, params, grads));
+    return GKRT_OK;
+}
+
+int gkrt_unet_set_params(GkrtContext* ctx, const float* params) {
+    if (!ctx || !params) return GKRT_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (!ctx->unet && !(ctx->unet = gkrt_unet_new())) return fail(ctx, GKRT_ERR_OOM, "denoiser");
+    GK_CUDA(gkrt_unet_set_params_host(ctx->unet, params));
+    return GKRT_OK;
+}
+
+int gkrt_unet_forward(GkrtContext* ctx, const float* input, uint32_t batch, uint32_t height, uint32_t width,
+                      float* out_linear, float* out_raw, void* stream) {
+    int rc = unet_ready(ctx);
+    if (rc != GKRT_OK) return rc;
+    if ((rc = unet_size_ok(ctx, batch, height, width)) != GKRT_OK) return rc;
+    if (!input) return fail(ctx, GKRT_ERR_INVALID_ARG, "null input");
+    GK_CUDA(gkrt_unet_forward_dev(ctx->unet, input, (int)batch, (int)height, (int)width, out_linear, out_raw,
+                                  (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
+int gkrt_unet_backward(GkrtContext* ctx, const float* d_raw, void* stream) {
+    int rc = unet_ready(ctx);
+    if (rc != GKRT_OK) return rc;
+    if (!d_raw) return fail(ctx, GKRT_ERR_INVALID_ARG, "null gradient");
+    GK_CUDA(gkrt_unet_backward_dev(ctx->unet, d_raw, (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
+int gkrt_unet_zero_grad(GkrtContext* ctx, void* stream) {
+    int rc = unet_ready(ctx);
+    if (rc != GKRT_OK) return rc;
+    GK_CUDA(gkrt_unet_zero_grad(ctx->unet, (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
+int gkrt_unet_train_step(GkrtContext* ctx, const float* input, const float* target, uint32_t batch, uint32_t height,
+                         uint32_t width, float lr, double* loss, void* stream) {
+    int rc = unet_ready(ctx);
+    if (rc != GKRT_OK) return rc;
+    if ((rc = unet_size_ok(ctx, batch, height, width)) != GKRT_OK) return rc;
+    if (!input || !target || !(lr > 0.0f)) return fail(ctx, GKRT_ERR_INVALID_ARG, "null buffer or lr <= 0");
+    GK_CUDA(gkrt_unet_train_step_dev(ctx->unet, input, target, (int)batch, (int)height, (int)width, lr, loss,
+                                     (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
+int gkrt_conv3x3_wgrad_bf16(const void* dy, const void* x, uint32_t batch, uint32_t height, uint32_t width,
+                            uint32_t cin, uint32_t cout, float* dw, void* stream) {
+    if (!dy || !x || !dw || batch == 0 || height == 0 || width == 0 || batch > 65535 || height > 65535 ||
+        width > 65535)
+        return GKRT_ERR_INVALID_ARG;
+    static uint32_t* d_err = nullptr;
+    if (!d_err && cudaMalloc((void**)&d_err, 4) != cudaSuccess) return GKRT_ERR_OOM;
+    WgradArgs a;
+    a.B = (int)batch; a.H = (int)height; a.W = (int)width;
+    a.dp = (const __nv_bfloat16*)dy; a.dp_c = (int)cout; a.dp_off = 0; a.cout = (int)cout;
+    a.x = (const __nv_bfloat16*)x; a.x_c = (int)cin; a.x_off = 0; a.cin = (int)cin;
+    a.dw = dw;
+    a.chunk = 2048;
+    a.err = d_err;
+    cudaError_t e = gkrt_launch_conv_wgrad(a, (cudaStream_t)stream);
     if (e == cudaErrorInvalidValue) return GKRT_ERR_INVALID_ARG;
     return e == cudaSuccess ? GKRT_OK : GKRT_ERR_CUDA;
 }

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <vector>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/gkrt.h"
@@ -48,6 +49,7 @@ struct AtrousArgs {
 constexpr int kConvRelu = 1, kConvF32Out = 2;
 struct ConvArgs {
     int B, H, W, cin, cout;        // cin % 32 == 0; cout % 16 == 0, 16..256 (MMA N)
+    int x_c, x_off;                // input: channel stride (>= cin) and first channel (multiple of 8)
     const float* bias;             // cout floats or null
     void* out;
     int out_c, out_off;            // multiples of 16 (bf16 output)
@@ -130,7 +132,58 @@ cudaError_t gkrt_launch_adjoint(const gk::ShadeScene& sc, const GkrtFrameConstan
 cudaError_t gkrt_launch_set_params(GkrtMaterial* mats, const float* alb, const float* rough, uint32_t first,
                                    uint32_t count, cudaStream_t st);
 cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const gk::ConvArgs& args, cudaStream_t st);
+// Weight gradient (k_unet.cu): dw[cout][9][cin] += sum_p dp[p][cout] * x[p + tap][cin].
+namespace gk {
+struct WgradArgs {
+    int B, H, W;
+    const __nv_bfloat16* dp;
+    int dp_c, dp_off, cout;
+    const __nv_bfloat16* x;
+    int x_c, x_off, cin;
+    float* dw;
+    int chunk;                     // pixels per CTA, a multiple of 32
+    uint32_t* err;
+};
+}
+cudaError_t gkrt_launch_conv_wgrad(const gk::WgradArgs& a, cudaStream_t st);
+cudaError_t gkrt_launch_avgpool2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
+                                 int h, int w, int C, cudaStream_t st);
+cudaError_t gkrt_launch_avgpool2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
+                                     int B, int H, int W, int C, int accumulate, cudaStream_t st);
+cudaError_t gkrt_launch_upsample2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
+                                  int H, int W, int C, cudaStream_t st);
+cudaError_t gkrt_launch_upsample2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
+                                      int B, int h, int w, int C, cudaStream_t st);
+cudaError_t gkrt_launch_relu_bwd(void* dy, int dy_c, int dy_off, const void* y, int y_c, int y_off, long long npix,
+                                 int C, cudaStream_t st);
+cudaError_t gkrt_launch_bias_grad(const void* dp, int dp_c, int dp_off, long long npix, int C, float* db,
+                                  cudaStream_t st);
 size_t gkrt_conv_smem_bytes(int cout);
+// The learned denoiser (unet.cu).
+namespace gk {
+constexpr int kUnetLayers = 15;
+constexpr float kUnetMaxLog = 12.0f;   // output log(1 + radiance) clamp before expm1
+struct Unet;
+}
+gk::Unet* gkrt_unet_new();
+void gkrt_unet_delete(gk::Unet* u);
+size_t gkrt_unet_nparams(const gk::Unet* u);
+cudaError_t gkrt_unet_init_params(gk::Unet* u, uint64_t seed);
+cudaError_t gkrt_unet_set_params_host(gk::Unet* u, const float* h);
+cudaError_t gkrt_unet_get_params_host(gk::Unet* u, float* params, float* grads);
+cudaError_t gkrt_unet_zero_grad(gk::Unet* u, cudaStream_t st);
+cudaError_t gkrt_unet_forward_dev(gk::Unet* u, const float* input, int b, int h, int w, float* out_linear,
+                                  float* out_raw, cudaStream_t st);
+cudaError_t gkrt_unet_backward_dev(gk::Unet* u, const float* d_raw, cudaStream_t st);
+cudaError_t gkrt_unet_train_step_dev(gk::Unet* u, const float* input, const float* target, int b, int h, int w,
+                                     float lr, double* loss_host, cudaStream_t st);
+cudaError_t gkrt_unet_denoise_frame(gk::Unet* u, const float4* sd, const float4* ss, const float4* alb,
+                                    const float4* nrm, const float* depth, int W, int H, int P, float* y_out_raw,
+                                    cudaStream_t st);
+const float* gkrt_unet_output(const gk::Unet* u);
+uint32_t* gkrt_unet_error_word(const gk::Unet* u);
+// compose writer over the denoiser's log-space output (k_post.cu)
+cudaError_t gkrt_launch_unet_compose(const gk::ComposeArgs& a, const float* y, cudaStream_t st);
 cudaError_t gkrt_launch_reproject(const gk::ReprojectArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_compose(const gk::ComposeArgs& a, cudaStream_t st);
 cudaError_t gkrt_launch_atrous(const gk::AtrousArgs& a, const float4* in, float4* tmp0, float4* tmp1, cudaStream_t st);

@@ -172,14 +172,16 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     if (args.cin % 32 || args.cin < 32 || args.cout % 16 || args.cout < 16 || args.cout > 256 || args.B < 1 ||
         args.H < 1 || args.W < 1 || (!f32 && (args.out_c % 16 || args.out_off % 16)) ||
         args.out_off + (f32 ? args.n_store : args.cout) > args.out_c || (f32 && args.n_store > args.cout) ||
-        ((uintptr_t)x & 15u) || ((uintptr_t)w & 15u) || ((uintptr_t)args.out & 15u))
+        ((uintptr_t)x & 15u) || ((uintptr_t)w & 15u) || ((uintptr_t)args.out & 15u) || args.x_off % 8 ||
+        (args.x_c > 0 && (args.x_c % 8 || args.x_off + args.cin > args.x_c)))
         return cudaErrorInvalidValue;
     CUtensorMap mx, mw;
+    const uint64_t xc = (uint64_t)(args.x_c > 0 ? args.x_c : args.cin);
     const uint64_t xd[4] = {(uint64_t)args.cin, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
-    const uint64_t xs[3] = {(uint64_t)args.cin * 2, (uint64_t)args.W * args.cin * 2,
-                            (uint64_t)args.H * args.W * args.cin * 2};
+    const uint64_t xs[3] = {xc * 2, (uint64_t)args.W * xc * 2, (uint64_t)args.H * args.W * xc * 2};
     const uint32_t xb[4] = {32, kTileX, kTileY, 1};
-    cudaError_t e = gkrt_encode_tmap_bf16(&mx, x, 4, xd, xs, xb);
+    const void* xbase = static_cast<const uint8_t*>(x) + (size_t)args.x_off * 2;
+    cudaError_t e = gkrt_encode_tmap_bf16(&mx, xbase, 4, xd, xs, xb);
     if (e != cudaSuccess) return e;
     const uint64_t wd[2] = {(uint64_t)9 * args.cin, (uint64_t)args.cout};
     const uint64_t ws[1] = {(uint64_t)9 * args.cin * 2};

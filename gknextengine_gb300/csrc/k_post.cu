@@ -358,6 +358,25 @@ cudaError_t map_f2(CUtensorMap* m, const void* base, int W, int H, int P, int bw
 }
 }  // namespace
 
+namespace gk {
+namespace {
+// the learned denoiser's output (dense W x H x 4, log(1 + radiance)) through the compose writer
+__global__ void k_unet_compose(ComposeArgs a, const float* y) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, yy = blockIdx.y;
+    if (x >= a.W || yy >= a.H) return;
+    const float* v = y + ((size_t)yy * a.W + x) * 4;
+    write_composed(a, (size_t)yy * a.P + x,
+                   F3(fmaxf(expm1f(fminf(v[0], kUnetMaxLog)), 0.0f), fmaxf(expm1f(fminf(v[1], kUnetMaxLog)), 0.0f),
+                      fmaxf(expm1f(fminf(v[2], kUnetMaxLog)), 0.0f)));
+}
+}  // namespace
+}  // namespace gk
+
+cudaError_t gkrt_launch_unet_compose(const ComposeArgs& a, const float* y, cudaStream_t st) {
+    k_unet_compose<<<dim3((a.W + 127) / 128, a.H), 128, 0, st>>>(a, y);
+    return cudaGetLastError();
+}
+
 cudaError_t gkrt_launch_reproject(const ReprojectArgs& a, cudaStream_t st) {
     CUtensorMap m_sd, m_ss, m_nrm, m_id, m_mv;
     cudaError_t e;

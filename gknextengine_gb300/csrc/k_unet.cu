@@ -1,0 +1,290 @@
+// k_unet.cu — the learned denoiser's training and inference kernels besides the forward
+// convolution (k_conv.cu): weight gradients on the tensor cores, and the element-wise,
+// pooling, loss and optimiser kernels.
+//
+// Weight gradient of a 3x3 convolution, dW[cout][tap][cin] = sum over pixels of
+// dP[p][cout] * X[p + tap offset][cin], is a GEMM with M = cout (padded to 128 rows of
+// zeros), N = cin and K = pixels. One CTA takes one tap and a run of pixels; both operands
+// are staged by the CTA's threads into the 64-byte-swizzled K-major layout (pixels along K)
+// straight from the NHWC tensors, made visible to the tensor core with a proxy fence, and
+// multiplied by one thread while the next pixels are staged (two buffers). The FP32
+// accumulator is added to dW with atomics. Every wait is bounded.
+#include "gk_umma.cuh"
+#include "gkrt_internal.h"
+
+namespace gk {
+
+namespace {
+
+constexpr int kWgThreads = 128;
+constexpr int kWgStep = 32;   // pixels per K step
+
+__device__ __forceinline__ uint32_t sw64_offset(int r, int k) {   // byte offset of element (row r, k) in a tile
+    return (uint32_t)((r >> 3) * 512 + (r & 7) * 64 + ((((k >> 3) ^ (r >> 1)) & 3) << 4) + (k & 7) * 2);
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int a_bytes = 128 * 64;
+    const int b_bytes = ((a.cin * 64) + 1023) & ~1023;
+    const int stage_bytes = a_bytes + b_bytes;
+    uint64_t* done = reinterpret_cast<uint64_t*>(smem + 2 * stage_bytes);
+    uint64_t* accb = done + 2;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const long long npix = (long long)a.B * a.H * a.W;
+    const long long p0 = (long long)blockIdx.x * a.chunk;
+    const int nk = (int)((min((long long)a.chunk, npix - p0) + kWgStep - 1) / kWgStep);
+    const uint32_t ncols = a.cin <= 32 ? 32u : a.cin <= 64 ? 64u : a.cin <= 128 ? 128u : 256u;
+
+    for (int i = tid; i < 2 * stage_bytes / 16; i += kWgThreads)   // zero rows stay zero (M padding)
+        reinterpret_cast<uint4*>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (tid == 0) {
+        mbar_init(&done[0], 1);
+        mbar_init(&done[1], 1);
+        mbar_init(accb, 1);
+        mbar_fence_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tslot, ncols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cin);
+    bool ok = true;
+    const int ga = a.cout / 8, gb = a.cin / 8;
+    for (int k = 0; k < nk && ok; ++k) {
+        const int s = k & 1;
+        if (k >= 2 && !mbar_wait_bounded(&done[s], (uint32_t)((k >> 1) - 1) & 1u, a.err)) ok = false;
+        if (__syncthreads_or(!ok)) { ok = false; break; }
+        uint8_t* sa = smem + s * stage_bytes;
+        uint8_t* sb = sa + a_bytes;
+        // A[cout][pixel] = dP[pixel][cout]
+        for (int it = tid; it < kWgStep * ga; it += kWgThreads) {
+            const int pl = it / ga, g = it % ga;
+            const long long q = p0 + (long long)k * kWgStep + pl;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (q < p0 + a.chunk && q < npix)
+                v = *reinterpret_cast<const uint4*>(a.dp + q * a.dp_c + a.dp_off + 8 * g);
+            const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) *reinterpret_cast<uint16_t*>(sa + sw64_offset(8 * g + i, pl)) = e[i];
+        }
+        // B[cin][pixel] = X[pixel shifted by the tap][cin], zero outside the image
+        for (int it = tid; it < kWgStep * gb; it += kWgThreads) {
+            const int pl = it / gb, g = it % gb;
+            const long long q = p0 + (long long)k * kWgStep + pl;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (q < p0 + a.chunk && q < npix) {
+                const int x = (int)(q % a.W), y = (int)((q / a.W) % a.H);
+                const long long b = q / ((long long)a.W * a.H);
+                const int xs = x + dx, ys = y + dy;
+                if (xs >= 0 && xs < a.W && ys >= 0 && ys < a.H)
+                    v = *reinterpret_cast<const uint4*>(a.x + ((b * a.H + ys) * a.W + xs) * a.x_c + a.x_off + 8 * g);
+            }
+            const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) *reinterpret_cast<uint16_t*>(sb + sw64_offset(8 * g + i, pl)) = e[i];
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t ua = smem_u32(sa), ub = smem_u32(sb);
+            umma_bf16(tmem, umma_desc_sw64(ua), umma_desc_sw64(ub), idesc, k != 0 ? 1u : 0u);
+            umma_bf16(tmem, umma_desc_sw64(ua + 32u), umma_desc_sw64(ub + 32u), idesc, 1u);
+            umma_commit(&done[s]);
+        }
+    }
+    if (tid == 0) umma_commit(accb);
+    const bool ready = mbar_wait_bounded(accb, 0u, a.err) && ok && nk > 0;
+    __syncwarp();
+    tc_fence_after();
+    const int r = warp * 32 + lane;   // TMEM lane = cout row
+    for (int c0 = 0; c0 < a.cin; c0 += 16) {
+        uint32_t v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+        tmem_ld_wait();
+        if (!ready || r >= a.cout) continue;
+        float* d = a.dw + ((size_t)r * 9 + tap) * a.cin + c0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float f = __uint_as_float(v[j]);
+            if (f != 0.0f) atomicAdd(d + j, f);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+// ---- element-wise kernels (NHWC bf16 with channel stride/offset) ----
+
+__global__ void k_avgpool2(const __nv_bfloat16* in, int in_c, int in_off, __nv_bfloat16* out, int out_c, int out_off,
+                           int B, int h, int w, int C) {   // h, w: output size
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)B * h * w * C;
+    if (i >= n) return;
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % w), y = (int)((p / w) % h);
+    const long long b = p / ((long long)w * h);
+    const int W = 2 * w, H = 2 * h;
+    float s = 0.0f;
+    for (int k = 0; k < 4; ++k) {
+        const long long q = (b * H + 2 * y + (k >> 1)) * W + 2 * x + (k & 1);
+        s += __bfloat162float(in[q * in_c + in_off + c]);
+    }
+    out[p * out_c + out_off + c] = __float2bfloat16_rn(0.25f * s);
+}
+
+// d_in (+)= d_out / 4 for each of the 2x2 inputs (accumulate: add to what is there)
+__global__ void k_avgpool2_bwd(const __nv_bfloat16* dout, int dout_c, int dout_off, __nv_bfloat16* din, int din_c,
+                               int din_off, int B, int H, int W, int C, int accumulate) {   // H, W: input size
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)B * H * W * C;
+    if (i >= n) return;
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % W), y = (int)((p / W) % H);
+    const long long b = p / ((long long)W * H);
+    const long long q = (b * (H / 2) + y / 2) * (W / 2) + x / 2;
+    float g = 0.25f * __bfloat162float(dout[q * dout_c + dout_off + c]);
+    __nv_bfloat16* d = din + p * din_c + din_off + c;
+    if (accumulate) g += __bfloat162float(*d);
+    *d = __float2bfloat16_rn(g);
+}
+
+__global__ void k_upsample2(const __nv_bfloat16* in, int in_c, int in_off, __nv_bfloat16* out, int out_c,
+                            int out_off, int B, int H, int W, int C) {   // H, W: output size
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)B * H * W * C;
+    if (i >= n) return;
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % W), y = (int)((p / W) % H);
+    const long long b = p / ((long long)W * H);
+    const long long q = (b * (H / 2) + y / 2) * (W / 2) + x / 2;
+    out[p * out_c + out_off + c] = in[q * in_c + in_off + c];
+}
+
+// d_in = sum of the 2x2 output gradients it was copied to
+__global__ void k_upsample2_bwd(const __nv_bfloat16* dout, int dout_c, int dout_off, __nv_bfloat16* din, int din_c,
+                                int din_off, int B, int h, int w, int C) {   // h, w: input size
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long n = (long long)B * h * w * C;
+    if (i >= n) return;
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % w), y = (int)((p / w) % h);
+    const long long b = p / ((long long)w * h);
+    const int W = 2 * w, H = 2 * h;
+    float s = 0.0f;
+    for (int k = 0; k < 4; ++k) {
+        const long long q = (b * H + 2 * y + (k >> 1)) * W + 2 * x + (k & 1);
+        s += __bfloat162float(dout[q * dout_c + dout_off + c]);
+    }
+    din[p * din_c + din_off + c] = __float2bfloat16_rn(s);
+}
+
+// dP = dY * (Y > 0) (ReLU), written in place of dY
+__global__ void k_relu_bwd(__nv_bfloat16* dy, int dy_c, int dy_off, const __nv_bfloat16* y, int y_c, int y_off,
+                           long long npix, int C) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= npix * C) return;
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    if (!(__bfloat162float(y[p * y_c + y_off + c]) > 0.0f)) dy[p * dy_c + dy_off + c] = __float2bfloat16_rn(0.0f);
+}
+
+// db[c] += sum over pixels of dP[p][c]; one block per run of pixels, shared partial sums
+__global__ void k_bias_grad(const __nv_bfloat16* dp, int dp_c, int dp_off, long long npix, int C, int run,
+                            float* db) {
+    __shared__ float part[256];
+    for (int c = threadIdx.x; c < C; c += blockDim.x) part[c] = 0.0f;
+    __syncthreads();
+    const long long p0 = (long long)blockIdx.x * run;
+    for (long long i = threadIdx.x; i < (long long)run * C; i += blockDim.x) {
+        const long long p = p0 + i / C;
+        if (p >= npix) break;
+        const int c = (int)(i % C);
+        atomicAdd(&part[c], __bfloat162float(dp[p * dp_c + dp_off + c]));
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < C; c += blockDim.x)
+        if (part[c] != 0.0f) atomicAdd(&db[c], part[c]);
+}
+
+}  // namespace
+
+}  // namespace gk
+
+using namespace gk;
+
+size_t gkrt_wgrad_smem_bytes(int cin) {
+    return 2 * (size_t)(128 * 64 + (((cin * 64) + 1023) & ~1023)) + 64 + 1024;
+}
+
+cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
+    if (a.cin % 16 || a.cin < 16 || a.cin > 256 || a.cout % 8 || a.cout > 128 || a.chunk % kWgStep || a.chunk <= 0 ||
+        a.dp_c % 8 || a.dp_off % 8 || a.x_c % 8 || a.x_off % 8 || ((uintptr_t)a.dp & 15u) || ((uintptr_t)a.x & 15u))
+        return cudaErrorInvalidValue;
+    const long long npix = (long long)a.B * a.H * a.W;
+    const size_t smem = gkrt_wgrad_smem_bytes(a.cin);
+    cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const dim3 grid((unsigned)((npix + a.chunk - 1) / a.chunk), 9);
+    k_conv_wgrad<<<grid, kWgThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+static inline unsigned nblk(long long n) { return (unsigned)((n + 255) / 256); }
+
+cudaError_t gkrt_launch_avgpool2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
+                                 int h, int w, int C, cudaStream_t st) {
+    k_avgpool2<<<nblk((long long)B * h * w * C), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
+                                                               (__nv_bfloat16*)out, out_c, out_off, B, h, w, C);
+    return cudaGetLastError();
+}
+cudaError_t gkrt_launch_avgpool2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
+                                     int B, int H, int W, int C, int accumulate, cudaStream_t st) {
+    k_avgpool2_bwd<<<nblk((long long)B * H * W * C), 256, 0, st>>>((const __nv_bfloat16*)dout, dout_c, dout_off,
+                                                                   (__nv_bfloat16*)din, din_c, din_off, B, H, W, C,
+                                                                   accumulate);
+    return cudaGetLastError();
+}
+cudaError_t gkrt_launch_upsample2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
+                                  int H, int W, int C, cudaStream_t st) {
+    k_upsample2<<<nblk((long long)B * H * W * C), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
+                                                                (__nv_bfloat16*)out, out_c, out_off, B, H, W, C);
+    return cudaGetLastError();
+}
+cudaError_t gkrt_launch_upsample2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
+                                      int B, int h, int w, int C, cudaStream_t st) {
+    k_upsample2_bwd<<<nblk((long long)B * h * w * C), 256, 0, st>>>((const __nv_bfloat16*)dout, dout_c, dout_off,
+                                                                    (__nv_bfloat16*)din, din_c, din_off, B, h, w, C);
+    return cudaGetLastError();
+}
+cudaError_t gkrt_launch_relu_bwd(void* dy, int dy_c, int dy_off, const void* y, int y_c, int y_off, long long npix,
+                                 int C, cudaStream_t st) {
+    k_relu_bwd<<<nblk(npix * C), 256, 0, st>>>((__nv_bfloat16*)dy, dy_c, dy_off, (const __nv_bfloat16*)y, y_c, y_off,
+                                               npix, C);
+    return cudaGetLastError();
+}
+cudaError_t gkrt_launch_bias_grad(const void* dp, int dp_c, int dp_off, long long npix, int C, float* db,
+                                  cudaStream_t st) {
+    if (C > 256) return cudaErrorInvalidValue;
+    const int run = 1024;
+    k_bias_grad<<<(unsigned)((npix + run - 1) / run), 256, 0, st>>>((const __nv_bfloat16*)dp, dp_c, dp_off, npix, C,
+                                                                   run, db);
+    return cudaGetLastError();
+}

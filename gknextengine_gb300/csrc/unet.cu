@@ -1,0 +1,448 @@
+// unet.cu — the learned denoiser: a 4-level convolutional U-Net in bf16 on the tensor cores,
+// trained and run by this library's own kernels (no counterpart in the reference: its learned
+// denoiser is the closed OIDN library, PathTracingRenderer.cpp:33-64, 234-269).
+//
+// Inputs, 10 channels per pixel: 1-spp linear radiance (as log(1 + x)), albedo, normal,
+// depth (NDC, clamped to [0, 1]: camera misses carry 100000); padded with zeros to 32 channels. Output: log(1 + radiance), 3 channels.
+//   level 0 (full)   enc0a 32->32, enc0b 32->32 ............ dec0a 96->32, dec0b 32->32, out 32->3
+//   level 1 (1/2)    enc1a 32->64, enc1b 64->64 ............ dec1a 160->64, dec1b 64->64
+//   level 2 (1/4)    enc2a 64->96, enc2b 96->96 ............ dec2a 224->96, dec2b 96->96
+//   level 3 (1/8)    enc3a 96->128, enc3b 128->128
+// 3x3 convolutions with ReLU (none on the output), 2x2 average pooling down, nearest 2x
+// upsampling up, skips concatenated in place: each decoder input tensor holds the upsampled
+// deeper features in its first channels and the encoder output (written there directly by
+// the encoder's convolution) in the rest. Training: loss = mean squared error in
+// log(1 + radiance) against the target, Adam on FP32 master weights, bf16 copies of the
+// weights in the forward layout [cout][tap][cin] and in the transposed, tap-mirrored layout
+// [cin][8 - tap][cout] that turns the input gradient into a forward convolution.
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "gk_device.cuh"
+#include "gkrt_internal.h"
+
+namespace gk {
+
+namespace {
+
+struct LayerDef {
+    int cin, cout, relu, n_store;
+};
+// enc0a enc0b enc1a enc1b enc2a enc2b enc3a enc3b dec2a dec2b dec1a dec1b dec0a dec0b out
+constexpr LayerDef kLayers[kUnetLayers] = {
+    {32, 32, 1, 32},   {32, 32, 1, 32},   {32, 64, 1, 64},  {64, 64, 1, 64},  {64, 96, 1, 96},
+    {96, 96, 1, 96},   {96, 128, 1, 128}, {128, 128, 1, 128}, {224, 96, 1, 96}, {96, 96, 1, 96},
+    {160, 64, 1, 64},  {64, 64, 1, 64},   {96, 32, 1, 32},  {32, 32, 1, 32},  {32, 32, 0, 3}};
+enum { E0A, E0B, E1A, E1B, E2A, E2B, E3A, E3B, D2A, D2B, D1A, D1B, D0A, D0B, OUT };
+
+__global__ void k_pack_input(const float* in, long long npix, __nv_bfloat16* x0) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= npix * 32) return;
+    const int c = (int)(i % 32);
+    const long long p = i / 32;
+    float v = 0.0f;
+    if (c < 10) {
+        v = in[p * 10 + c];
+        if (c < 3) v = log1pf(fmaxf(v, 0.0f));
+        if (c == 9) v = fminf(fmaxf(v, 0.0f), 1.0f);   // depth; misses carry 100000
+    }
+    x0[i] = __float2bfloat16_rn(v);
+}
+
+// From the pass's images (pitched float4 / float): composed 1-spp radiance
+// (diffuse x albedo + specular), albedo, normal, depth.
+__global__ void k_pack_frame(const float4* sd, const float4* ss, const float4* alb, const float4* nrm,
+                             const float* depth, int W, int H, int P, __nv_bfloat16* x0) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)W * H) return;
+    const int x = (int)(i % W), y = (int)(i / W);
+    const size_t q = (size_t)y * P + x;
+    const float4 d = sd[q], s = ss[q], a = alb[q], n = nrm[q];
+    float v[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) v[c] = 0.0f;
+    v[0] = log1pf(fmaxf(fmaf(d.x, a.x, s.x), 0.0f));
+    v[1] = log1pf(fmaxf(fmaf(d.y, a.y, s.y), 0.0f));
+    v[2] = log1pf(fmaxf(fmaf(d.z, a.z, s.z), 0.0f));
+    v[3] = a.x; v[4] = a.y; v[5] = a.z;
+    v[6] = n.x; v[7] = n.y; v[8] = n.z;
+    v[9] = fminf(fmaxf(depth[q], 0.0f), 1.0f);   // misses carry 100000
+    uint4* o = reinterpret_cast<uint4*>(x0 + i * 32);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        __nv_bfloat162 h[4];
+        for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(v[8 * k + 2 * j], v[8 * k + 2 * j + 1]);
+        o[k] = *reinterpret_cast<uint4*>(h);
+    }
+}
+
+// gradient of the loss in log space; loss sum in FP64
+__global__ void k_loss(const float* y, const float* target, long long npix, float gscale, __nv_bfloat16* gy,
+                       double* loss) {
+    __shared__ double part[8];
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (p < npix) {
+        __nv_bfloat16* g = gy + p * 32;
+        for (int c = 0; c < 3; ++c) {
+            const float e = y[p * 4 + c] - log1pf(fmaxf(target[p * 3 + c], 0.0f));
+            l += (double)e * e;
+            g[c] = __float2bfloat16_rn(2.0f * e * gscale);
+        }
+        for (int c = 3; c < 32; ++c) g[c] = __float2bfloat16_rn(0.0f);
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xFFFFFFFFu, l, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += part[k];
+        atomicAdd(loss, s);
+    }
+}
+
+// caller-supplied gradient of the raw output (f32, 4 channels) to the bf16 32-channel layout
+__global__ void k_grad_in(const float* d, long long npix, __nv_bfloat16* gy) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= npix * 32) return;
+    const int c = (int)(i % 32);
+    gy[i] = __float2bfloat16_rn(c < 3 ? d[(i / 32) * 4 + c] : 0.0f);
+}
+
+__global__ void k_out_linear(const float* y, long long npix, float* out) {
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    for (int c = 0; c < 3; ++c) out[p * 4 + c] = fmaxf(expm1f(fminf(y[p * 4 + c], kUnetMaxLog)), 0.0f);
+    out[p * 4 + 3] = 1.0f;
+}
+
+__global__ void k_adam(float* p, const float* g, float* m, float* v, long long n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+}
+
+// bf16 weights in both layouts: wb[co][tap][ci] and wf[ci][8 - tap][co]
+__global__ void k_weights_bf16(const float* w, int cin, int cout, __nv_bfloat16* wb, __nv_bfloat16* wf) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= 9LL * cin * cout) return;
+    const int ci = (int)(i % cin);
+    const int tap = (int)((i / cin) % 9);
+    const int co = (int)(i / (9LL * cin));
+    const __nv_bfloat16 h = __float2bfloat16_rn(w[i]);
+    wb[i] = h;
+    wf[((long long)ci * 9 + (8 - tap)) * cout + co] = h;
+}
+
+inline unsigned nb(long long n) { return (unsigned)((n + 255) / 256); }
+
+}  // namespace
+
+struct Unet {
+    size_t woff[kUnetLayers], boff[kUnetLayers], wb_off[kUnetLayers];
+    size_t nparams = 0, nweights_bf16 = 0;
+    float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *wb = nullptr, *wf = nullptr;
+    int step = 0;
+    int B = 0, H = 0, W = 0;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    // activations (bf16 NHWC) and their gradients
+    __nv_bfloat16 *x0, *e0a, *cat0, *p0, *e1a, *cat1, *p1, *e2a, *cat2, *p2, *e3a, *e3b, *d2a, *d2b, *d1a, *d1b, *d0a,
+        *d0b;
+    __nv_bfloat16 *gy, *g_d0b, *g_d0a, *g_cat0, *g_d1b, *g_d1a, *g_cat1, *g_d2b, *g_d2a, *g_cat2, *g_e3b, *g_e3a, *g_p2,
+        *g_e2a, *g_p1, *g_e1a, *g_p0, *g_e0a;
+    float* y = nullptr;
+    double* d_loss = nullptr;
+    uint32_t* err = nullptr;
+
+    Unet() {
+        size_t off = 0, wo = 0;
+        for (int l = 0; l < kUnetLayers; ++l) {
+            woff[l] = off;
+            off += 9ull * kLayers[l].cin * kLayers[l].cout;
+            boff[l] = off;
+            off += kLayers[l].cout;
+            wb_off[l] = wo;
+            wo += 9ull * kLayers[l].cin * kLayers[l].cout;
+        }
+        nparams = off;
+        nweights_bf16 = wo;
+    }
+    ~Unet() {
+        for (void* q : {(void*)p, (void*)g, (void*)m, (void*)v, (void*)wb, (void*)wf, arena, (void*)d_loss, (void*)err})
+            if (q) cudaFree(q);
+    }
+
+    cudaError_t alloc_params() {
+        cudaError_t e;
+        for (float** q : {&p, &g, &m, &v})
+            if ((e = cudaMalloc((void**)q, nparams * sizeof(float))) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&wb, nweights_bf16 * 2)) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&wf, nweights_bf16 * 2)) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&d_loss, sizeof(double))) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&err, 4)) != cudaSuccess) return e;
+        return cudaMemset(err, 0, 4);
+    }
+
+    // bf16 copies of the weights from the FP32 masters
+    cudaError_t refresh_bf16(cudaStream_t st) {
+        for (int l = 0; l < kUnetLayers; ++l) {
+            const long long n = 9LL * kLayers[l].cin * kLayers[l].cout;
+            k_weights_bf16<<<nb(n), 256, 0, st>>>(p + woff[l], kLayers[l].cin, kLayers[l].cout, wb + wb_off[l],
+                                                  wf + wb_off[l]);
+        }
+        return cudaGetLastError();
+    }
+
+    cudaError_t ensure_size(int b, int h, int w) {
+        if (b == B && h == H && w == W && arena) return cudaSuccess;
+        if (arena) cudaFree(arena);
+        arena = nullptr;
+        B = H = W = 0;
+        struct Req {
+            __nv_bfloat16** ptr;
+            int level, ch;
+        };
+        const Req reqs[] = {{&x0, 0, 32},    {&e0a, 0, 32},   {&cat0, 0, 96},   {&p0, 1, 32},    {&e1a, 1, 64},
+                            {&cat1, 1, 160}, {&p1, 2, 64},    {&e2a, 2, 96},    {&cat2, 2, 224}, {&p2, 3, 96},
+                            {&e3a, 3, 128},  {&e3b, 3, 128},  {&d2a, 2, 96},    {&d2b, 2, 96},   {&d1a, 1, 64},
+                            {&d1b, 1, 64},   {&d0a, 0, 32},   {&d0b, 0, 32},    {&gy, 0, 32},    {&g_d0b, 0, 32},
+                            {&g_d0a, 0, 32}, {&g_cat0, 0, 96}, {&g_d1b, 1, 64}, {&g_d1a, 1, 64}, {&g_cat1, 1, 160},
+                            {&g_d2b, 2, 96}, {&g_d2a, 2, 96}, {&g_cat2, 2, 224}, {&g_e3b, 3, 128}, {&g_e3a, 3, 128},
+                            {&g_p2, 3, 96},  {&g_e2a, 2, 96}, {&g_p1, 2, 64},   {&g_e1a, 1, 64}, {&g_p0, 1, 32},
+                            {&g_e0a, 0, 32}};
+        size_t total = 0;
+        std::vector<size_t> offs;
+        for (const Req& r : reqs) {
+            offs.push_back(total);
+            const size_t px = (size_t)b * (h >> r.level) * (w >> r.level);
+            total += (px * r.ch * 2 + 255) & ~(size_t)255;
+        }
+        const size_t ybytes = ((size_t)b * h * w * 16 + 255) & ~(size_t)255;
+        cudaError_t e = cudaMalloc(&arena, total + ybytes);
+        if (e != cudaSuccess) return e;
+        e = cudaMemset(arena, 0, total + ybytes);
+        if (e != cudaSuccess) return e;
+        for (size_t i = 0; i < offs.size(); ++i)
+            *reqs[i].ptr = reinterpret_cast<__nv_bfloat16*>(static_cast<uint8_t*>(arena) + offs[i]);
+        y = reinterpret_cast<float*>(static_cast<uint8_t*>(arena) + total);
+        B = b;
+        H = h;
+        W = w;
+        arena_bytes = total + ybytes;
+        return cudaSuccess;
+    }
+
+    cudaError_t conv(int l, const __nv_bfloat16* in, int in_c, int in_off, void* out, int out_c, int out_off, int level,
+                     cudaStream_t st) {
+        ConvArgs a;
+        a.B = B; a.H = H >> level; a.W = W >> level;
+        a.cin = kLayers[l].cin; a.cout = kLayers[l].cout;
+        a.x_c = in_c; a.x_off = in_off;
+        a.bias = p + boff[l];
+        a.out = out; a.out_c = out_c; a.out_off = out_off;
+        a.n_store = kLayers[l].n_store;
+        a.flags = (kLayers[l].relu ? kConvRelu : 0) | (l == OUT ? kConvF32Out : 0);
+        a.err = err;
+        return gkrt_launch_conv3x3(in, wb + wb_off[l], a, st);
+    }
+
+    cudaError_t forward(cudaStream_t st) {
+        cudaError_t e;
+#define GK_T(x) if ((e = (x)) != cudaSuccess) return e
+        GK_T(conv(E0A, x0, 32, 0, e0a, 32, 0, 0, st));
+        GK_T(conv(E0B, e0a, 32, 0, cat0, 96, 64, 0, st));
+        GK_T(gkrt_launch_avgpool2(cat0, 96, 64, p0, 32, 0, B, H >> 1, W >> 1, 32, st));
+        GK_T(conv(E1A, p0, 32, 0, e1a, 64, 0, 1, st));
+        GK_T(conv(E1B, e1a, 64, 0, cat1, 160, 96, 1, st));
+        GK_T(gkrt_launch_avgpool2(cat1, 160, 96, p1, 64, 0, B, H >> 2, W >> 2, 64, st));
+        GK_T(conv(E2A, p1, 64, 0, e2a, 96, 0, 2, st));
+        GK_T(conv(E2B, e2a, 96, 0, cat2, 224, 128, 2, st));
+        GK_T(gkrt_launch_avgpool2(cat2, 224, 128, p2, 96, 0, B, H >> 3, W >> 3, 96, st));
+        GK_T(conv(E3A, p2, 96, 0, e3a, 128, 0, 3, st));
+        GK_T(conv(E3B, e3a, 128, 0, e3b, 128, 0, 3, st));
+        GK_T(gkrt_launch_upsample2(e3b, 128, 0, cat2, 224, 0, B, H >> 2, W >> 2, 128, st));
+        GK_T(conv(D2A, cat2, 224, 0, d2a, 96, 0, 2, st));
+        GK_T(conv(D2B, d2a, 96, 0, d2b, 96, 0, 2, st));
+        GK_T(gkrt_launch_upsample2(d2b, 96, 0, cat1, 160, 0, B, H >> 1, W >> 1, 96, st));
+        GK_T(conv(D1A, cat1, 160, 0, d1a, 64, 0, 1, st));
+        GK_T(conv(D1B, d1a, 64, 0, d1b, 64, 0, 1, st));
+        GK_T(gkrt_launch_upsample2(d1b, 64, 0, cat0, 96, 0, B, H, W, 64, st));
+        GK_T(conv(D0A, cat0, 96, 0, d0a, 32, 0, 0, st));
+        GK_T(conv(D0B, d0a, 32, 0, d0b, 32, 0, 0, st));
+        GK_T(conv(OUT, d0b, 32, 0, y, 4, 0, 0, st));
+        return cudaSuccess;
+    }
+
+    // One layer's backward: dP (in place of dY) = dY * relu', weight and bias gradients, and
+    // (if din) the input gradient through the mirrored weights.
+    cudaError_t layer_bwd(int l, __nv_bfloat16* dy, int dy_c, int dy_off, const __nv_bfloat16* y_act, int y_c,
+                          int y_off, const __nv_bfloat16* x, int x_c, int x_off, __nv_bfloat16* din, int level,
+                          cudaStream_t st) {
+        cudaError_t e;
+        const int h = H >> level, w = W >> level;
+        const long long npix = (long long)B * h * w;
+        const LayerDef& L = kLayers[l];
+        if (L.relu) GK_T(gkrt_launch_relu_bwd(dy, dy_c, dy_off, y_act, y_c, y_off, npix, L.cout, st));
+        WgradArgs wa;
+        wa.B = B; wa.H = h; wa.W = w;
+        wa.dp = dy; wa.dp_c = dy_c; wa.dp_off = dy_off; wa.cout = L.cout;
+        wa.x = x; wa.x_c = x_c; wa.x_off = x_off; wa.cin = L.cin;
+        wa.dw = g + woff[l];
+        wa.chunk = 2048;
+        wa.err = err;
+        GK_T(gkrt_launch_conv_wgrad(wa, st));
+        GK_T(gkrt_launch_bias_grad(dy, dy_c, dy_off, npix, L.cout, g + boff[l], st));
+        if (din) {
+            ConvArgs a;
+            a.B = B; a.H = h; a.W = w;
+            a.cin = L.cout; a.cout = L.cin;
+            a.x_c = dy_c; a.x_off = dy_off;
+            a.bias = nullptr;
+            a.out = din; a.out_c = L.cin; a.out_off = 0;
+            a.n_store = L.cin;
+            a.flags = 0;
+            a.err = err;
+            GK_T(gkrt_launch_conv3x3(dy, wf + wb_off[l], a, st));
+        }
+        return cudaSuccess;
+    }
+
+    cudaError_t backward(cudaStream_t st) {   // gy holds d loss / d output (bf16, 32 channels)
+        cudaError_t e;
+        GK_T(layer_bwd(OUT, gy, 32, 0, nullptr, 0, 0, d0b, 32, 0, g_d0b, 0, st));
+        GK_T(layer_bwd(D0B, g_d0b, 32, 0, d0b, 32, 0, d0a, 32, 0, g_d0a, 0, st));
+        GK_T(layer_bwd(D0A, g_d0a, 32, 0, d0a, 32, 0, cat0, 96, 0, g_cat0, 0, st));
+        GK_T(gkrt_launch_upsample2_bwd(g_cat0, 96, 0, g_d1b, 64, 0, B, H >> 1, W >> 1, 64, st));
+        GK_T(layer_bwd(D1B, g_d1b, 64, 0, d1b, 64, 0, d1a, 64, 0, g_d1a, 1, st));
+        GK_T(layer_bwd(D1A, g_d1a, 64, 0, d1a, 64, 0, cat1, 160, 0, g_cat1, 1, st));
+        GK_T(gkrt_launch_upsample2_bwd(g_cat1, 160, 0, g_d2b, 96, 0, B, H >> 2, W >> 2, 96, st));
+        GK_T(layer_bwd(D2B, g_d2b, 96, 0, d2b, 96, 0, d2a, 96, 0, g_d2a, 2, st));
+        GK_T(layer_bwd(D2A, g_d2a, 96, 0, d2a, 96, 0, cat2, 224, 0, g_cat2, 2, st));
+        GK_T(gkrt_launch_upsample2_bwd(g_cat2, 224, 0, g_e3b, 128, 0, B, H >> 3, W >> 3, 128, st));
+        GK_T(layer_bwd(E3B, g_e3b, 128, 0, e3b, 128, 0, e3a, 128, 0, g_e3a, 3, st));
+        GK_T(layer_bwd(E3A, g_e3a, 128, 0, e3a, 128, 0, p2, 96, 0, g_p2, 3, st));
+        // the encoder output of level 2 feeds both the pool and the skip
+        GK_T(gkrt_launch_avgpool2_bwd(g_p2, 96, 0, g_cat2, 224, 128, B, H >> 2, W >> 2, 96, 1, st));
+        GK_T(layer_bwd(E2B, g_cat2, 224, 128, cat2, 224, 128, e2a, 96, 0, g_e2a, 2, st));
+        GK_T(layer_bwd(E2A, g_e2a, 96, 0, e2a, 96, 0, p1, 64, 0, g_p1, 2, st));
+        GK_T(gkrt_launch_avgpool2_bwd(g_p1, 64, 0, g_cat1, 160, 96, B, H >> 1, W >> 1, 64, 1, st));
+        GK_T(layer_bwd(E1B, g_cat1, 160, 96, cat1, 160, 96, e1a, 64, 0, g_e1a, 1, st));
+        GK_T(layer_bwd(E1A, g_e1a, 64, 0, e1a, 64, 0, p0, 32, 0, g_p0, 1, st));
+        GK_T(gkrt_launch_avgpool2_bwd(g_p0, 32, 0, g_cat0, 96, 64, B, H, W, 32, 1, st));
+        GK_T(layer_bwd(E0B, g_cat0, 96, 64, cat0, 96, 64, e0a, 32, 0, g_e0a, 0, st));
+        GK_T(layer_bwd(E0A, g_e0a, 32, 0, e0a, 32, 0, x0, 32, 0, nullptr, 0, st));
+        return cudaSuccess;
+    }
+#undef GK_T
+};
+
+}  // namespace gk
+
+using namespace gk;
+
+// ---- host entry points used by gkrt_api.cu ----
+Unet* gkrt_unet_new() { return new (std::nothrow) Unet(); }
+void gkrt_unet_delete(Unet* u) { delete u; }
+size_t gkrt_unet_nparams(const Unet* u) { return u->nparams; }
+
+cudaError_t gkrt_unet_init_params(Unet* u, uint64_t seed) {
+    cudaError_t e = u->p ? cudaSuccess : u->alloc_params();
+    if (e != cudaSuccess) return e;
+    std::vector<float> h(u->nparams, 0.0f);
+    std::mt19937_64 rng(seed);
+    for (int l = 0; l < kUnetLayers; ++l) {
+        const double sd = std::sqrt(2.0 / (9.0 * kLayers[l].cin)) * (l == OUT ? 0.1 : 1.0);
+        std::normal_distribution<double> nd(0.0, sd);
+        for (size_t i = 0; i < 9ull * kLayers[l].cin * kLayers[l].cout; ++i) h[u->woff[l] + i] = (float)nd(rng);
+    }
+    return gkrt_unet_set_params_host(u, h.data());
+}
+
+cudaError_t gkrt_unet_set_params_host(Unet* u, const float* h) {
+    cudaError_t e = u->p ? cudaSuccess : u->alloc_params();
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemcpy(u->p, h, u->nparams * 4, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    for (float* q : {u->g, u->m, u->v})
+        if ((e = cudaMemset(q, 0, u->nparams * 4)) != cudaSuccess) return e;
+    u->step = 0;
+    if ((e = u->refresh_bf16(0)) != cudaSuccess) return e;
+    return cudaDeviceSynchronize();
+}
+
+cudaError_t gkrt_unet_get_params_host(Unet* u, float* params, float* grads) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && params) e = cudaMemcpy(params, u->p, u->nparams * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && grads) e = cudaMemcpy(grads, u->g, u->nparams * 4, cudaMemcpyDeviceToHost);
+    return e;
+}
+
+cudaError_t gkrt_unet_zero_grad(Unet* u, cudaStream_t st) { return cudaMemsetAsync(u->g, 0, u->nparams * 4, st); }
+
+cudaError_t gkrt_unet_forward_dev(Unet* u, const float* input, int b, int h, int w, float* out_linear, float* out_raw,
+                                  cudaStream_t st) {
+    cudaError_t e = u->ensure_size(b, h, w);
+    if (e != cudaSuccess) return e;
+    const long long npix = (long long)b * h * w;
+    if (input) k_pack_input<<<nb(npix * 32), 256, 0, st>>>(input, npix, u->x0);
+    if ((e = u->forward(st)) != cudaSuccess) return e;
+    if (out_linear) k_out_linear<<<nb(npix), 256, 0, st>>>(u->y, npix, out_linear);
+    if (out_raw) e = cudaMemcpyAsync(out_raw, u->y, npix * 16, cudaMemcpyDeviceToDevice, st);
+    return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+cudaError_t gkrt_unet_backward_dev(Unet* u, const float* d_raw, cudaStream_t st) {
+    const long long npix = (long long)u->B * u->H * u->W;
+    k_grad_in<<<nb(npix * 32), 256, 0, st>>>(d_raw, npix, u->gy);
+    return u->backward(st);
+}
+
+cudaError_t gkrt_unet_train_step_dev(Unet* u, const float* input, const float* target, int b, int h, int w, float lr,
+                                     double* loss_host, cudaStream_t st) {
+    cudaError_t e = gkrt_unet_forward_dev(u, input, b, h, w, nullptr, nullptr, st);
+    if (e != cudaSuccess) return e;
+    const long long npix = (long long)b * h * w;
+    if ((e = cudaMemsetAsync(u->d_loss, 0, sizeof(double), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(u->g, 0, u->nparams * 4, st)) != cudaSuccess) return e;
+    // gradients of the per-image sum of squared log errors (Adam does not see the scale)
+    k_loss<<<nb(npix), 256, 0, st>>>(u->y, target, npix, 1.0f, u->gy, u->d_loss);
+    if ((e = u->backward(st)) != cudaSuccess) return e;
+    u->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, u->step)));
+    const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, u->step)));
+    k_adam<<<nb((long long)u->nparams), 256, 0, st>>>(u->p, u->g, u->m, u->v, (long long)u->nparams, lr, b1, b2, 1e-8f,
+                                                     c1, c2);
+    if ((e = u->refresh_bf16(st)) != cudaSuccess) return e;
+    if (loss_host) {
+        double l = 0.0;
+        if ((e = cudaMemcpyAsync(&l, u->d_loss, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        *loss_host = l / (double)(npix * 3);
+    }
+    return cudaGetLastError();
+}
+
+// Denoise the pass's current 1-spp images; writes linear radiance (float4, pitched) to
+// out_linear via the compose writer's arguments.
+cudaError_t gkrt_unet_denoise_frame(Unet* u, const float4* sd, const float4* ss, const float4* alb, const float4* nrm,
+                                    const float* depth, int W, int H, int P, float* y_out_raw, cudaStream_t st) {
+    cudaError_t e = u->ensure_size(1, H, W);
+    if (e != cudaSuccess) return e;
+    k_pack_frame<<<nb((long long)W * H), 256, 0, st>>>(sd, ss, alb, nrm, depth, W, H, P, u->x0);
+    if ((e = u->forward(st)) != cudaSuccess) return e;
+    (void)y_out_raw;
+    return cudaGetLastError();
+}
+
+const float* gkrt_unet_output(const Unet* u) { return u->y; }
+uint32_t* gkrt_unet_error_word(const Unet* u) { return u->err; }

@@ -54,6 +54,16 @@ def load(path: str | None = None):
     L.gkrt_affine_inverse.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.gkrt_conv3x3_bf16.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp,
                                     C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]
+    L.gkrt_conv3x3_wgrad_bf16.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp]
+    L.gkrt_unet_init.argtypes = [vp, C.c_uint64]
+    L.gkrt_unet_param_count.argtypes = [vp, C.POINTER(C.c_uint32)]
+    L.gkrt_unet_get_params.argtypes = [vp, vp, vp]
+    L.gkrt_unet_set_params.argtypes = [vp, vp]
+    L.gkrt_unet_forward.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, vp]
+    L.gkrt_unet_backward.argtypes = [vp, vp, vp]
+    L.gkrt_unet_zero_grad.argtypes = [vp, vp]
+    L.gkrt_unet_train_step.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float,
+                                       C.POINTER(C.c_double), vp]
     L.gkrt_set_material_params.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_adjoint_forward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp]
     L.gkrt_adjoint_backward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp, vp, vp]
@@ -71,5 +81,7 @@ EXPORTED = [
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
     "gkrt_get_stats",
     "gkrt_synchronize", "gkrt_affine_inverse",
-    "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16",
+    "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16", "gkrt_conv3x3_wgrad_bf16",
+    "gkrt_unet_init", "gkrt_unet_param_count", "gkrt_unet_get_params", "gkrt_unet_set_params", "gkrt_unet_forward",
+    "gkrt_unet_backward", "gkrt_unet_zero_grad", "gkrt_unet_train_step",
 ]

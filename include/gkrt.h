@@ -165,6 +165,7 @@ typedef struct GkrtFrameConstants {
 
 #define GKRT_DENOISE_JBF     0u    /* reference single-pass joint bilateral filter      */
 #define GKRT_DENOISE_ATROUS  1u    /* 5x5 edge-aware a-trous, 3 passes (no reference)   */
+#define GKRT_DENOISE_UNET    2u    /* learned bf16 U-Net on the current 1-spp images    */
 
 #define GKRT_NEE_REFERENCE   0u    /* sun-cone NEE only, as the built Slang path        */
 #define GKRT_NEE_EMISSIVE    1u    /* + emissive-triangle NEE via an alias table (new)  */
@@ -336,11 +337,38 @@ int  gkrt_adjoint_backward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint3
  * NULL; y: NHWC with y_channels channels, written at channel y_offset (bf16, multiples of
  * 16), or fp32 with GKRT_CONV_F32 (then only y_store channels are written). Device
  * pointers, 16-byte aligned. */
+/* Weight gradient of that convolution: dw[cout][3][3][cin] (fp32, ADDED to) = sum over pixels
+ * of dy[p][cout] * x[p + tap][cin]; dy NHWC bf16 with cout channels (a multiple of 8, at most
+ * 128), x with cin channels (a multiple of 16, at most 256). */
+int  gkrt_conv3x3_wgrad_bf16(const void* dy, const void* x, uint32_t batch, uint32_t height, uint32_t width,
+                             uint32_t cin, uint32_t cout, float* dw, void* stream);
 #define GKRT_CONV_RELU 1u
 #define GKRT_CONV_F32  2u
 int  gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin,
                        const void* w, const float* bias, uint32_t cout, void* y, uint32_t y_channels,
                        uint32_t y_offset, uint32_t y_store, uint32_t flags, void* stream);
+
+/* Learned denoiser (no counterpart in the reference, whose learned denoiser is the closed
+ * OIDN library): a 4-level 3x3-convolution U-Net (32/64/96/128 channels) in bf16 with FP32
+ * accumulation on the tensor cores, trained by this library's own forward and backward
+ * kernels with Adam. input: dense float [batch][height][width][10] device array, channels
+ * 1-spp linear radiance rgb, albedo rgb, normal xyz, NDC depth (clamped to [0, 1]); target:
+ * [..][3] linear radiance.
+ * out_linear: [..][4] denoised linear radiance (w = 1); out_raw: [..][4] the network's
+ * log(1 + radiance) output, the quantity gkrt_unet_backward's d_raw differentiates. Sizes
+ * are multiples of 8 from 16 to 8192, batch 1..64. Parameters: gkrt_unet_param_count floats,
+ * per layer the weights [cout][3][3][cin] then the biases; set_params resets Adam's state.
+ * The denoise pass uses it with GKRT_DENOISE_UNET. */
+int  gkrt_unet_init(GkrtContext* ctx, uint64_t seed);
+int  gkrt_unet_param_count(GkrtContext* ctx, uint32_t* count);
+int  gkrt_unet_get_params(GkrtContext* ctx, float* params, float* grads);
+int  gkrt_unet_set_params(GkrtContext* ctx, const float* params);
+int  gkrt_unet_forward(GkrtContext* ctx, const float* input, uint32_t batch, uint32_t height, uint32_t width,
+                       float* out_linear, float* out_raw, void* stream);
+int  gkrt_unet_backward(GkrtContext* ctx, const float* d_raw, void* stream);
+int  gkrt_unet_zero_grad(GkrtContext* ctx, void* stream);
+int  gkrt_unet_train_step(GkrtContext* ctx, const float* input, const float* target, uint32_t batch,
+                          uint32_t height, uint32_t width, float lr, double* loss, void* stream);
 
 int  gkrt_get_stats(GkrtContext* ctx, GkrtStats* out);
 int  gkrt_synchronize(GkrtContext* ctx, void* stream);

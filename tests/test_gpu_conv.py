@@ -74,3 +74,38 @@ def test_conv_rejects_bad_shapes():
     rc = L.gkrt_conv3x3_bf16(C.c_void_p(x.data_ptr()), 1, 8, 16, 48, C.c_void_p(w.data_ptr()), None, 16,
                              C.c_void_p(out.data_ptr()), 16, 0, 0, 0, None)
     assert rc == abi.GKRT_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("B,H,W,cin,cout", [(2, 37, 45, 64, 96), (1, 64, 64, 32, 32), (1, 24, 40, 224, 96),
+                                             (3, 16, 16, 160, 64), (1, 33, 17, 96, 128)])
+def test_wgrad_matches_torch(B, H, W, cin, cout):
+    """gkrt_conv3x3_wgrad_bf16 against torch's weight gradient of the same bf16 values."""
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(B * 7 + cin + cout)
+    x = torch.randn((B, H, W, cin), device="cuda", generator=g).bfloat16()
+    dy = torch.randn((B, H, W, cout), device="cuda", generator=g).bfloat16()
+    dw = torch.zeros((cout, 3, 3, cin), device="cuda")
+    L = native.load()
+    rc = L.gkrt_conv3x3_wgrad_bf16(C.c_void_p(dy.data_ptr()), C.c_void_p(x.data_ptr()), B, H, W, cin, cout,
+                                   C.c_void_p(dw.data_ptr()), None)
+    assert rc == abi.GKRT_OK
+    torch.cuda.synchronize()
+    ref = torch.nn.grad.conv2d_weight(x.float().permute(0, 3, 1, 2), (cout, cin, 3, 3),
+                                      dy.float().permute(0, 3, 1, 2), padding=1).permute(0, 2, 3, 1)
+    torch.testing.assert_close(dw, ref, rtol=1e-3, atol=1e-3 * float(ref.abs().max()))
+
+
+def test_input_gradient_is_a_mirrored_convolution():
+    """The denoiser's input gradient: the forward kernel with weights [cin][8 - tap][cout]."""
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(11)
+    B, H, W, cin, cout = 2, 24, 40, 96, 64
+    w = (torch.randn((cout, 3, 3, cin), device="cuda", generator=g) / 30).bfloat16()
+    dy = torch.randn((B, H, W, cout), device="cuda", generator=g).bfloat16()
+    wf = w.flip(1, 2).permute(3, 1, 2, 0).contiguous()   # [cin][3][3][cout], taps mirrored
+    dx = torch.zeros((B, H, W, cin), device="cuda").bfloat16()
+    conv(dy, wf, None, cin, dx, cin, 0)
+    torch.cuda.synchronize()
+    ref = torch.nn.grad.conv2d_input((B, cin, H, W), w.float().permute(0, 3, 1, 2), dy.float().permute(0, 3, 1, 2),
+                                     padding=1).permute(0, 2, 3, 1)
+    torch.testing.assert_close(dx.float(), ref.bfloat16().float(), rtol=2e-2, atol=2e-2)

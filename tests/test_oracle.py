@@ -309,3 +309,27 @@ def test_adjoint_oracle_matches_finite_differences():
         r2[m] -= h
         fd = (loss(a0, r1)[0] - loss(a0, r2)[0]) / (2 * h)
         assert abs(gr[m] - fd) <= 0.01 * abs(fd), (m, gr[m], fd)
+
+
+def test_unet_oracle_backward_matches_finite_differences(monkeypatch):
+    """The numpy restatement of the denoiser, with bf16 rounding switched off: its backward pass
+    against central differences of its forward pass, 3 parameters of every layer."""
+    from oracle import unet_ref as U
+    monkeypatch.setattr(U, "bf16", lambda x: np.asarray(x, np.float64))
+    rng = np.random.default_rng(0)
+    p = rng.normal(0, 0.05, U.param_count())
+    inp = rng.uniform(0, 1, (1, 16, 16, 10))
+    d = rng.normal(size=(1, 16, 16, 3))
+    _, cache = U.forward(p, inp)
+    g = U.backward(cache, d)
+    off = 0
+    for ci, co, _ in U.LAYERS:
+        n = 9 * ci * co + co
+        # weights on the first 10 input channels / first 3 outputs, where gradients are non-zero
+        for i in off + rng.integers(0, n, 3):
+            q1, q2 = p.copy(), p.copy()
+            q1[i] += 1e-5
+            q2[i] -= 1e-5
+            fd = ((U.forward(q1, inp)[0] * d).sum() - (U.forward(q2, inp)[0] * d).sum()) / 2e-5
+            assert abs(g[i] - fd) <= 1e-6 + 1e-5 * abs(fd), (i - off, g[i], fd)
+        off += n
