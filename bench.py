@@ -38,6 +38,9 @@ UNIT = "Mrays/s"
 W_, H_ = 1920, 1080
 HIT_FETCH_BYTES = 3 * 4 + 3 * 16 + 64 + 64 + 48   # indices, normals, material, instance, triangle
 NODE_BYTES, TRI_BYTES, RAY_BYTES = 64, 48, 32
+# DRAM bytes (read + write) of one 1080p trace launch of the default workload, from one ncu
+# capture; the node and triangle reads above are served by L1/L2
+TRACE_DRAM_BYTES_1080P = 7485696 + 117612544
 
 
 WORKLOAD = "bricks"
@@ -58,6 +61,87 @@ def workload_config():
             "l2": "per-frame image working set 0.5 GB > L2 (129 MB); the 0.6 MB BVH stays L2-resident as "
                   "in steady-state rendering",
             "data": "synthetic seeded scene (numpy default_rng seed 2)"}
+
+
+def measured_peak_bf16():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+UNET_LAYERS = [(32, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 96, 2), (96, 96, 2), (96, 128, 3),
+               (128, 128, 3), (224, 96, 2), (96, 96, 2), (160, 64, 1), (64, 64, 1), (96, 32, 0), (32, 32, 0),
+               (32, 32, 0)]   # (cin, cout as computed, level)
+
+
+def run_denoiser(args):
+    """The learned denoiser at 1920 x 1080: forward (inference) ms/frame through the C ABI with
+    device inputs, and one Adam training step at 2 x 512 x 512; tensor-core roofline of the
+    forward (algorithmic FLOPs of the 15 convolutions over the measured time)."""
+    import torch
+    from gknextengine_gb300.denoiser import Unet
+    from gknextengine_gb300.renderer import PathTracingRenderer
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    W, H = 1920, 1080
+    flops = sum(2 * 9 * ci * co * (W >> lv) * (H >> lv) for ci, co, lv in UNET_LAYERS)
+    with PathTracingRenderer(local) as r:
+        net = Unet(r, seed=7)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        inp = torch.rand((1, H, W, 10), device="cuda", generator=g)
+        out = torch.zeros((1, H, W, 4), device="cuda")
+        for _ in range(args.warmup):
+            net.forward(inp, out_linear=out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record()
+            for _ in range(args.steps):
+                net.forward(inp, out_linear=out)
+            e1.record()
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        # end to end: input from pinned host memory, denoised frame back to pinned host memory
+        hin = torch.rand((1, H, W, 10), generator=torch.Generator().manual_seed(1)).pin_memory()
+        hout = torch.empty((1, H, W, 4), pin_memory=True)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            inp.copy_(hin, non_blocking=True)
+            net.forward(inp, out_linear=out)
+            hout.copy_(out, non_blocking=True)
+            torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) / args.steps * 1e3
+        tin = torch.rand((2, 512, 512, 10), device="cuda", generator=g)
+        tgt = torch.rand((2, 512, 512, 3), device="cuda", generator=g)
+        for _ in range(3):
+            net.train_step(tin, tgt, 1e-4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            net.train_step(tin, tgt, 1e-4)
+        torch.cuda.synchronize()
+        train_ms = (time.perf_counter() - t0) / 10 * 1e3
+    peak, kind = measured_peak_bf16()
+    achieved = flops / (ms * 1e-3) / 1e12
+    line = {"metric": "learned denoiser ms/frame 1080p (bf16 U-Net forward)", "value": ms, "unit": "ms/frame",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "U-Net 32/64/96/128, 15 3x3 convs, 1920x1080, batch 1",
+                       "l2": "activations 0.4-0.8 GB per level-0 tensor > L2"},
+            "gpu_launches": 0, "e2e": {"value": e2e_ms, "unit": "ms/frame", "h2d_bytes_per_step": H * W * 40,
+                                       "d2h_bytes_per_step": H * W * 16},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "k_conv3x3 (15 launches)",
+                         "peak_kind": kind, "algorithmic_flops_per_frame": flops},
+            "train_step_ms_2x512x512": train_ms, "clocks": clk.summary()}
+    line["gpu_launches"] = 15 + 7 + 2   # convolutions, pools/upsamplings, input packing and output
+    print(json.dumps(line))
+    return 0
 
 
 def load_workload():
@@ -197,68 +281,20 @@ def run_reference(args):
     return 0
 
 
-def relmse(x, y):
-    """mean over pixels and RGB of (x - y)^2 / (y^2 + 1e-2), linear radiance."""
-    import numpy as np
-    d = x[..., :3].astype(np.float64) - y[..., :3]
-    return float(np.mean(d * d / (y[..., :3].astype(np.float64) ** 2 + 1e-2)))
-
-
-def relmse_measure(device: int, W: int = 960, H: int = 540, ref_spp: int = 4096, temporal: int = 16):
-    """Denoised RelMSE against a 4096-spp reference on the Cornell scene (static camera,
-    no TAA jitter). The reference is the mean of 4096 independent 1-spp trace passes,
-    remodulated like the compose pass (diffuse x albedo + specular). Compared: the raw
-    1-spp image, the reference's JBF and the a-trous filter on one frame, and the same after
-    `temporal` frames of reprojection."""
-    import numpy as np
-    import torch
-    from gknextengine_gb300 import abi, camera, scenes
+def relmse_measure(device: int):
+    """Denoised RelMSE against a 4096-spp reference at 1920 x 1080 on a held-out Cornell
+    variant: raw 1 spp, the reference's bilateral filter (JBF), the a-trous filter, the learned
+    denoiser (trained here first: 600 Adam steps on 16 variants at 512 x 512 with 256-spp
+    targets, by the library's own kernels) and the temporal steady state of the filters."""
+    from gknextengine_gb300.denoiser import evaluate, train_default
     from gknextengine_gb300.renderer import PathTracingRenderer
-    sc, cam, st = scenes.cornell()
-    st.taa = False
-    out = {"scene": f"cornell {W}x{H}", "reference_spp": ref_spp, "metric": "mean (x-y)^2/(y^2+1e-2) over px, RGB"}
     with PathTracingRenderer(device) as r:
-        r.load_scene(sc)
-        r.create_swap_chain(W, H)
-        fb = camera.FrameBuilder(W, H, st)
-        t0 = time.perf_counter()
-        acc_d = torch.zeros((H, r.image_view(abi.IMG_SINGLE_DIFFUSE).pitch_bytes // 16, 4), device="cuda")
-        acc_s = torch.zeros_like(acc_d)
-        vd = r.image_view(abi.IMG_SINGLE_DIFFUSE)
-        vs = r.image_view(abi.IMG_SINGLE_SPECULAR)
-        n = H * (vd.pitch_bytes // 16) * 4
-        for f in range(ref_spp):
-            fc = fb.build(cam, 100000 + f)
-            r.trace_pass(fc)
-            d = torch.as_tensor(_device_f32(vd.device_ptr, n)).view(H, -1, 4)
-            s_ = torch.as_tensor(_device_f32(vs.device_ptr, n)).view(H, -1, 4)
-            acc_d += d
-            acc_s += s_
-        torch.cuda.synchronize()
-        out["reference_seconds"] = time.perf_counter() - t0
-        alb = r.read_image(abi.IMG_ALBEDO)
-        ref = (acc_d[:, :W].cpu().numpy() / ref_spp) * alb + acc_s[:, :W].cpu().numpy() / ref_spp
-        for name, den, bf in (("raw", abi.DENOISE_JBF, 0), ("jbf", abi.DENOISE_JBF, 5),
-                              ("atrous", abi.DENOISE_ATROUS, 5)):
-            st.denoiser, st.bf_size = den, bf
-            # one frame on its own (history weight 0), then the steady state of the temporal
-            # blend (1/16 per frame) after 8 x 16 frames, when the zeroed start no longer counts
-            for tf, frames, key in ((1, 1, f"{name}_1spp"), (temporal, 8 * temporal, f"{name}_temporal")):
-                st.temporal_frames = tf
-                fbn = camera.FrameBuilder(W, H, st)
-                r.create_swap_chain(W, H)
-                for f in range(frames):
-                    r.render(fbn.build(cam, f))
-                out[key] = relmse(r.read_image(abi.IMG_DENOISED_LINEAR), ref)
+        net, losses, info = train_default(r)
+        out = evaluate(r, net)
+        info["loss_first"] = float(sum(losses[:20]) / 20)
+        info["loss_last"] = float(sum(losses[-20:]) / 20)
+        out["training"] = info
     return out
-
-
-def _device_f32(ptr, n):
-    """A float32 view of n floats of device memory (no copy)."""
-    import torch
-    class _A:
-        __cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (ptr, False), "version": 3}
-    return torch.as_tensor(_A(), device="cuda")
 
 
 def run_gkrt(args):
@@ -380,7 +416,12 @@ def run_gkrt(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ctypes.sizeof(abi.GkrtFrameConstants),
                         "d2h_bytes_per_step": W_ * H_ * 16, "ms_per_frame": e2e_s / K * 1e3},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None, "kernel": "k_trace_pass",
+                             "frac": achieved / peak,
+                             "traffic": TRACE_DRAM_BYTES_1080P if (WORKLOAD == "bricks" and (W_, H_) == (1920, 1080))
+                             else None,
+                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 1080p "
+                                               "k_trace_pass launch (profiles/k_trace_pass_bricks1080p_dram.md)",
+                             "kernel": "k_trace_pass",
                              "peak_kind": peak_kind,
                              "algorithmic_bytes_per_launch": alg_bytes,
                              "node_visits": st_last.node_visits, "triangle_tests": st_last.triangle_tests,
@@ -407,7 +448,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-relmse", action="store_true")
     ap.add_argument("--size", default=None, help="WxH override for profiling small cases (default 1920x1080)")
-    ap.add_argument("--workload", default="bricks", choices=["bricks", "city"],
+    ap.add_argument("--workload", default="bricks", choices=["bricks", "city", "denoiser"],
                     help="bricks: the 1080p headline workload; city: 10.5M tris at 4K with per-frame rebuild")
     args = ap.parse_args()
     global WORKLOAD, W_, H_
@@ -420,6 +461,8 @@ def main():
         W_, H_ = (int(v) for v in args.size.lower().split("x"))
     if args.impl == "reference":
         return run_reference(args)
+    if WORKLOAD == "denoiser":
+        return run_denoiser(args)
     return run_gkrt(args)
 
 

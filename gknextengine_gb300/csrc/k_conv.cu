@@ -5,18 +5,23 @@
 // are multiples of 32; weights are [Cout][3][3][Cin] bf16; accumulation is FP32 in tensor
 // memory.
 //
-// One CTA computes a tile of 8 x 16 pixels (M = 128) times all Cout (N <= 256) of one image:
+// Persistent, warp-specialised CTAs loop over tiles of 8 x 16 pixels (M = 128) times all Cout
+// (N <= 256) of one image:
 //   K loop   9 taps x Cin / 32 chunks. For tap (dy, dx) and chunk c the A operand is the
 //            4D TMA box {32 channels, 16 x, 8 y, 1 image} of the input shifted by the tap;
 //            coordinates outside the image read zeros, which is the zero padding. The B
 //            operand is the 2D box {32, Cout} of the weights at column tap * Cin + 32 c.
 //            Both land 64-byte swizzled, the K-major layout of gk_umma.cuh.
-//   stages   4 shared-memory stages; one thread issues the TMA loads (full barriers with
-//            transaction counts), one thread issues two K = 16 MMAs per stage and frees
-//            the stage with tcgen05.commit (empty barriers), then commits the accumulator.
-//   epilogue all four warps read their 32 TMEM lanes (pixels) 16 columns at a time, add the
-//            bias, apply ReLU, and store bf16 (or fp32) NHWC at a channel offset of a wider
-//            tensor, which is how skip connections are concatenated without copies.
+//   stages   warp 0 issues the TMA loads into a ring of shared-memory stages (full barriers
+//            with transaction counts) across tile boundaries; warp 1 issues two K = 16 MMAs per
+//            stage, frees the stage with tcgen05.commit (empty barriers) and commits each
+//            tile's accumulator; two accumulators in TMEM alternate between tiles, so the
+//            epilogue of one tile runs under the MMAs of the next.
+//   epilogue warps 2-5 (one per TMEM lane quarter) read their 32 lanes (pixels) 16 columns at
+//            a time, add the bias, apply ReLU, store bf16 (or fp32) NHWC at a channel offset of
+//            a wider tensor (skip connections are concatenated without copies), and release
+//            the accumulator.
+// The grid holds as many CTAs per SM as shared memory and the 512 TMEM columns allow.
 // Every barrier wait is bounded; a wait that runs out records the wait error bit in the
 // device error word and the CTA skips its stores.
 #include <algorithm>
@@ -30,8 +35,8 @@ namespace gk {
 
 namespace {
 
-constexpr int kConvThreads = 128;
-constexpr int kConvStages = 4;
+constexpr int kConvThreads = 192;   // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kEpiThreads = 128;
 constexpr int kTileX = 16, kTileY = 8;
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
@@ -39,34 +44,49 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
+__device__ __forceinline__ void tile_origin(int t, int tiles_x, int tiles_y, int& x0, int& y0, int& img) {
+    const int per_img = tiles_x * tiles_y;
+    img = t / per_img;
+    const int r = t - img * per_img;
+    y0 = (r / tiles_x) * kTileY;
+    x0 = (r % tiles_x) * kTileX;
+}
+
 __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant__ CUtensorMap mx,
-                                                             const __grid_constant__ CUtensorMap mw, ConvArgs a) {
+                                                          const __grid_constant__ CUtensorMap mw, ConvArgs a,
+                                                          int tiles_x, int tiles_y, int ntiles, int stages) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const int a_bytes = kTileX * kTileY * 64;
     const int b_bytes = a.cout * 64;
     const int stage_bytes = (a_bytes + b_bytes + 1023) & ~1023;
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kConvStages * stage_bytes);
-    uint64_t* empty = full + kConvStages;
-    uint64_t* accb = empty + kConvStages;
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + stages * stage_bytes);
+    uint64_t* empty = full + stages;
+    uint64_t* accf = empty + stages;   // accumulator ready (MMA commit)
+    uint64_t* acce = accf + 2;         // accumulator drained (128 epilogue arrivals)
+    uint64_t* fin = acce + 2;          // every MMA of this CTA completed
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(fin + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY, img = blockIdx.z;
     const int kc = a.cin / 32, nk = 9 * kc;
-    const uint32_t ncols = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : a.cout <= 128 ? 128u : 256u;
+    const uint32_t ncols1 = a.cout <= 32 ? 32u : a.cout <= 64 ? 64u : a.cout <= 128 ? 128u : 256u;
+    const uint32_t ncols = 2u * ncols1;
 
     if (tid == 0) {
-        for (int s = 0; s < kConvStages; ++s) {
+        for (int s = 0; s < stages; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accb, 1);
+        mbar_init(&accf[0], 1);
+        mbar_init(&accf[1], 1);
+        mbar_init(&acce[0], kEpiThreads);
+        mbar_init(&acce[1], kEpiThreads);
+        mbar_init(fin, 1);
         *abort_flag = 0;
         mbar_fence_init();
     }
-    if (warp == 0) {
+    if (warp == 1) {
         tmem_alloc(tslot, ncols);
         tmem_relinquish();
     }
@@ -75,82 +95,105 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    if (warp == 0 && lane == 0) {
-        // producer: TMA loads of the A (shifted input) and B (weights) chunks
-        int issued = 0;
-        for (int k = 0; k < nk; ++k) {
-            const int s = k % kConvStages;
-            const uint32_t it = (uint32_t)(k / kConvStages);
-            if (k >= kConvStages && !mbar_wait_bounded(&empty[s], (it - 1u) & 1u, a.err)) {
-                *abort_flag = 1;
-                break;
+    if (warp == 0) {
+        if (lane == 0) {   // producer
+            int kg = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                int x0, y0, img;
+                tile_origin(t, tiles_x, tiles_y, x0, y0, img);
+                for (int k = 0; k < nk; ++k, ++kg) {
+                    const int s = kg % stages;
+                    const uint32_t use = (uint32_t)(kg / stages);
+                    if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1u) & 1u, a.err)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    const int tap = k / kc, c = k - tap * kc;
+                    uint8_t* sa = smem + s * stage_bytes;
+                    mbar_expect_tx(&full[s], (uint32_t)(a_bytes + b_bytes));
+                    tma_load_4d(sa, &mx, c * 32, x0 + tap % 3 - 1, y0 + tap / 3 - 1, img, &full[s]);
+                    tma_load_2d(sa + a_bytes, &mw, tap * a.cin + c * 32, 0, &full[s]);
+                }
             }
-            if (*abort_flag) break;
-            const int tap = k / kc, c = k % kc;
-            uint8_t* sa = smem + s * stage_bytes;
-            mbar_expect_tx(&full[s], (uint32_t)(a_bytes + b_bytes));
-            tma_load_4d(sa, &mx, c * 32, x0 + tap % 3 - 1, y0 + tap / 3 - 1, img, &full[s]);
-            tma_load_2d(sa + a_bytes, &mw, tap * a.cin + c * 32, 0, &full[s]);
-            ++issued;
         }
-        // on an abort, let the loads already issued land before the CTA's memory goes away
-        for (int k = std::max(0, issued - kConvStages); k < issued && *abort_flag; ++k)
-            mbar_wait_bounded(&full[k % kConvStages], (uint32_t)(k / kConvStages) & 1u, a.err);
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cout);
-        bool ok = true;
-        for (int k = 0; k < nk; ++k) {
-            const int s = k % kConvStages;
-            if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kConvStages) & 1u, a.err)) {
-                *abort_flag = 1;
-                ok = false;
-                break;
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer
+            const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cout);
+            int kg = 0, i = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
+                const int acc = i & 1;
+                const uint32_t use = (uint32_t)(i >> 1);
+                if (use > 0 && !mbar_wait_bounded(&acce[acc], (use - 1u) & 1u, a.err)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)acc * ncols1;
+                for (int k = 0; k < nk; ++k, ++kg) {
+                    const int s = kg % stages;
+                    if (!mbar_wait_bounded(&full[s], (uint32_t)(kg / stages) & 1u, a.err)) {
+                        *abort_flag = 1;
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(smem + s * stage_bytes), sb = sa + (uint32_t)a_bytes;
+                    umma_bf16(d, umma_desc_sw64(sa), umma_desc_sw64(sb), idesc, k != 0 ? 1u : 0u);
+                    umma_bf16(d, umma_desc_sw64(sa + 32u), umma_desc_sw64(sb + 32u), idesc, 1u);
+                    umma_commit(&empty[s]);
+                }
+                if (ok) umma_commit(&accf[acc]);
             }
+            umma_commit(fin);
+            mbar_wait_bounded(fin, 0u, a.err);   // nothing may be in flight when TMEM is freed
+        }
+    } else {
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31, the tile's pixels of that quarter
+        const int q = warp & 3;
+        const int p = q * 32 + lane;
+        int i = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+            const int acc = i & 1;
+            const bool ready = mbar_wait_bounded(&accf[acc], (uint32_t)(i >> 1) & 1u, a.err);
+            __syncwarp();
             tc_fence_after();
-            const uint32_t sa = smem_u32(smem + s * stage_bytes), sb = sa + (uint32_t)a_bytes;
-            umma_bf16(tmem, umma_desc_sw64(sa), umma_desc_sw64(sb), idesc, k != 0 ? 1u : 0u);
-            umma_bf16(tmem, umma_desc_sw64(sa + 32u), umma_desc_sw64(sb + 32u), idesc, 1u);
-            umma_commit(&empty[s]);
-        }
-        (void)ok;
-        umma_commit(accb);   // arrives once every MMA issued above has completed
-    }
-    __syncwarp();
-
-    // epilogue: TMEM lanes 32 w .. 32 w + 31 are the tile's pixels 32 w .. 32 w + 31
-    const bool ready = mbar_wait_bounded(accb, 0u, a.err);
-    __syncwarp();
-    tc_fence_after();
-    const int p = warp * 32 + lane;
-    const int y = y0 + p / kTileX, x = x0 + p % kTileX;
-    const bool inside = ready && !*abort_flag && y < a.H && x < a.W;
-    const size_t pix = ((size_t)img * a.H + y) * a.W + x;
-    for (int c0 = 0; c0 < a.cout; c0 += 16) {
-        uint32_t r[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-        tmem_ld_wait();
-        if (!inside) continue;
-        float v[16];
+            if (!__all_sync(0xFFFFFFFFu, ready) || *abort_flag) break;
+            int x0, y0, img;
+            tile_origin(t, tiles_x, tiles_y, x0, y0, img);
+            const int y = y0 + p / kTileX, x = x0 + p % kTileX;
+            const bool inside = y < a.H && x < a.W;
+            const size_t pix = ((size_t)img * a.H + y) * a.W + x;
+            const uint32_t base = tmem + (uint32_t)acc * ncols1 + ((uint32_t)(q * 32) << 16);
+            for (int c0 = 0; c0 < a.cout; c0 += 16) {
+                uint32_t r[16];
+                tmem_ld16(base + (uint32_t)c0, r);
+                tmem_ld_wait();
+                if (!inside) continue;
+                float v[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
-            if (a.flags & kConvRelu) v[j] = fmaxf(v[j], 0.0f);
-        }
-        if (a.flags & kConvF32Out) {
-            float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
-            for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
-        } else {
-            uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + pix * a.out_c + a.out_off + c0);
-            o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
-                              pack_bf16x2(v[6], v[7]));
-            o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
-                              pack_bf16x2(v[14], v[15]));
+                for (int j = 0; j < 16; ++j) {
+                    v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                    if (a.flags & kConvRelu) v[j] = fmaxf(v[j], 0.0f);
+                }
+                if (a.flags & kConvF32Out) {
+                    float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
+                    for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
+                } else {
+                    uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + pix * a.out_c +
+                                                        a.out_off + c0);
+                    o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                                      pack_bf16x2(v[6], v[7]));
+                    o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
+                                      pack_bf16x2(v[14], v[15]));
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&acce[acc]);
         }
     }
-    tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (warp == 1) tmem_dealloc(tmem, ncols);
 }
 
 }  // namespace
@@ -162,9 +205,14 @@ using namespace gk;
 cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                   const uint64_t* strides_bytes, const uint32_t* box);
 
+// Four stages per CTA, so that several CTAs share an SM (as many as shared memory and the
+// 512 TMEM columns allow): independent load/MMA/epilogue streams hide L2 latency better than
+// deeper rings in fewer CTAs (measured on the level-0 layers).
+static int conv_stages(int) { return 4; }
+
 size_t gkrt_conv_smem_bytes(int cout) {
     const int stage = (kTileX * kTileY * 64 + cout * 64 + 1023) & ~1023;
-    return (size_t)kConvStages * stage + 2 * kConvStages * 8 + 8 + 8 + 1024;
+    return (size_t)conv_stages(cout) * stage + 2 * conv_stages(cout) * 8 + 5 * 8 + 8 + 1024;
 }
 
 cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& args, cudaStream_t st) {
@@ -189,9 +237,36 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     e = gkrt_encode_tmap_bf16(&mw, w, 2, wd, ws, wb);
     if (e != cudaSuccess) return e;
     const size_t smem = gkrt_conv_smem_bytes(args.cout);
-    e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    const dim3 grid((args.W + kTileX - 1) / kTileX, (args.H + kTileY - 1) / kTileY, args.B);
-    k_conv3x3<<<grid, kConvThreads, smem, st>>>(mx, mw, args);
+    // launch geometry per output width, computed once (host calls kept off the per-launch path)
+    static int sms = 0;
+    static int per_sm_cache[257] = {};
+    static size_t smem_set = 0;
+    if (!sms) {
+        int dev = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    }
+    if (smem > smem_set) {
+        if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)gkrt_conv_smem_bytes(256))) != cudaSuccess)
+            return e;
+        if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
+            return e;
+        smem_set = gkrt_conv_smem_bytes(256);
+    }
+    int per_sm = per_sm_cache[args.cout];
+    if (!per_sm) {
+        // resident CTAs per SM: shared memory (227 KB per SM, 1 KB reserved per CTA), the 512
+        // TMEM columns (two accumulators per CTA) and 2048 threads
+        const int ncols = 2 * (args.cout <= 32 ? 32 : args.cout <= 64 ? 64 : args.cout <= 128 ? 128 : 256);
+        per_sm = std::min({(int)((227 * 1024) / (smem + 1024)), 512 / ncols, 2048 / kConvThreads});
+        per_sm = std::max(1, per_sm);
+        per_sm_cache[args.cout] = per_sm;
+    }
+    const int tiles_x = (args.W + kTileX - 1) / kTileX, tiles_y = (args.H + kTileY - 1) / kTileY;
+    const int ntiles = tiles_x * tiles_y * args.B;
+    const int grid = std::min(ntiles, sms * per_sm);
+    k_conv3x3<<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles, conv_stages(args.cout));
     return cudaGetLastError();
 }

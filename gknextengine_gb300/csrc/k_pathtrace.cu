@@ -467,10 +467,14 @@ cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstant
                                    const PixelImages& im, unsigned long long* counters, unsigned int* work,
                                    int num_sms, cudaStream_t st) {
     const bool nee = fc.nee_mode == GKRT_NEE_EMISSIVE && sc.nemit > 0u;
-    int per_sm = 0;
-    cudaError_t e = nee ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pass<true>, kPtThreads, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pass<false>, kPtThreads, 0);
-    if (e != cudaSuccess) return e;
+    static int occ[2] = {0, 0};   // resident blocks per SM of each instantiation, queried once
+    cudaError_t e = cudaSuccess;
+    if (!occ[nee]) {
+        e = nee ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_trace_pass<true>, kPtThreads, 0)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_trace_pass<false>, kPtThreads, 0);
+        if (e != cudaSuccess) return e;
+    }
+    int per_sm = occ[nee];
     if (per_sm < 1) per_sm = 1;
     const int pixels = W * H;
     int blocks = num_sms * per_sm;

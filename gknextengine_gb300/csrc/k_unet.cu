@@ -128,82 +128,111 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
 }
 
 // ---- element-wise kernels (NHWC bf16 with channel stride/offset) ----
+// One thread per pixel and group of 8 channels (16-byte loads and stores); channel counts,
+// strides and offsets are multiples of 8. Pixel counts fit 32-bit indices.
+
+__device__ __forceinline__ void ld8(const __nv_bfloat16* p, float* v) {
+    const uint4 u = *reinterpret_cast<const uint4*>(p);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 f = __bfloat1622float2(h[k]);
+        v[2 * k] = f.x;
+        v[2 * k + 1] = f.y;
+    }
+}
+__device__ __forceinline__ void st8(__nv_bfloat16* p, const float* v) {
+    uint4 u;
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    *reinterpret_cast<uint4*>(p) = u;
+}
 
 __global__ void k_avgpool2(const __nv_bfloat16* in, int in_c, int in_off, __nv_bfloat16* out, int out_c, int out_off,
                            int B, int h, int w, int C) {   // h, w: output size
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long n = (long long)B * h * w * C;
-    if (i >= n) return;
-    const int c = (int)(i % C);
-    const long long p = i / C;
-    const int x = (int)(p % w), y = (int)((p / w) % h);
-    const long long b = p / ((long long)w * h);
+    const int g8 = C / 8;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B * h * w * g8) return;
+    const int g = i % g8, p = i / g8;
+    const int x = p % w, y = (p / w) % h, b = p / (w * h);
     const int W = 2 * w, H = 2 * h;
-    float s = 0.0f;
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
     for (int k = 0; k < 4; ++k) {
-        const long long q = (b * H + 2 * y + (k >> 1)) * W + 2 * x + (k & 1);
-        s += __bfloat162float(in[q * in_c + in_off + c]);
+        const size_t q = ((size_t)(b * H + 2 * y + (k >> 1)) * W + 2 * x + (k & 1));
+        ld8(in + q * in_c + in_off + 8 * g, v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s[j] += v[j];
     }
-    out[p * out_c + out_off + c] = __float2bfloat16_rn(0.25f * s);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s[j] *= 0.25f;
+    st8(out + (size_t)p * out_c + out_off + 8 * g, s);
 }
 
 // d_in (+)= d_out / 4 for each of the 2x2 inputs (accumulate: add to what is there)
 __global__ void k_avgpool2_bwd(const __nv_bfloat16* dout, int dout_c, int dout_off, __nv_bfloat16* din, int din_c,
                                int din_off, int B, int H, int W, int C, int accumulate) {   // H, W: input size
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long n = (long long)B * H * W * C;
-    if (i >= n) return;
-    const int c = (int)(i % C);
-    const long long p = i / C;
-    const int x = (int)(p % W), y = (int)((p / W) % H);
-    const long long b = p / ((long long)W * H);
-    const long long q = (b * (H / 2) + y / 2) * (W / 2) + x / 2;
-    float g = 0.25f * __bfloat162float(dout[q * dout_c + dout_off + c]);
-    __nv_bfloat16* d = din + p * din_c + din_off + c;
-    if (accumulate) g += __bfloat162float(*d);
-    *d = __float2bfloat16_rn(g);
+    const int g8 = C / 8;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B * H * W * g8) return;
+    const int g = i % g8, p = i / g8;
+    const int x = p % W, y = (p / W) % H, b = p / (W * H);
+    const size_t q = (size_t)(b * (H / 2) + y / 2) * (W / 2) + x / 2;
+    float v[8], d[8];
+    ld8(dout + q * dout_c + dout_off + 8 * g, v);
+    __nv_bfloat16* dst = din + (size_t)p * din_c + din_off + 8 * g;
+    if (accumulate) ld8(dst, d);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = 0.25f * v[j] + (accumulate ? d[j] : 0.0f);
+    st8(dst, v);
 }
 
 __global__ void k_upsample2(const __nv_bfloat16* in, int in_c, int in_off, __nv_bfloat16* out, int out_c,
                             int out_off, int B, int H, int W, int C) {   // H, W: output size
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long n = (long long)B * H * W * C;
-    if (i >= n) return;
-    const int c = (int)(i % C);
-    const long long p = i / C;
-    const int x = (int)(p % W), y = (int)((p / W) % H);
-    const long long b = p / ((long long)W * H);
-    const long long q = (b * (H / 2) + y / 2) * (W / 2) + x / 2;
-    out[p * out_c + out_off + c] = in[q * in_c + in_off + c];
+    const int g8 = C / 8;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B * H * W * g8) return;
+    const int g = i % g8, p = i / g8;
+    const int x = p % W, y = (p / W) % H, b = p / (W * H);
+    const size_t q = (size_t)(b * (H / 2) + y / 2) * (W / 2) + x / 2;
+    *reinterpret_cast<uint4*>(out + (size_t)p * out_c + out_off + 8 * g) =
+        *reinterpret_cast<const uint4*>(in + q * in_c + in_off + 8 * g);
 }
 
 // d_in = sum of the 2x2 output gradients it was copied to
 __global__ void k_upsample2_bwd(const __nv_bfloat16* dout, int dout_c, int dout_off, __nv_bfloat16* din, int din_c,
                                 int din_off, int B, int h, int w, int C) {   // h, w: input size
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long n = (long long)B * h * w * C;
-    if (i >= n) return;
-    const int c = (int)(i % C);
-    const long long p = i / C;
-    const int x = (int)(p % w), y = (int)((p / w) % h);
-    const long long b = p / ((long long)w * h);
+    const int g8 = C / 8;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B * h * w * g8) return;
+    const int g = i % g8, p = i / g8;
+    const int x = p % w, y = (p / w) % h, b = p / (w * h);
     const int W = 2 * w, H = 2 * h;
-    float s = 0.0f;
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
     for (int k = 0; k < 4; ++k) {
-        const long long q = (b * H + 2 * y + (k >> 1)) * W + 2 * x + (k & 1);
-        s += __bfloat162float(dout[q * dout_c + dout_off + c]);
+        const size_t q = (size_t)(b * H + 2 * y + (k >> 1)) * W + 2 * x + (k & 1);
+        ld8(dout + q * dout_c + dout_off + 8 * g, v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s[j] += v[j];
     }
-    din[p * din_c + din_off + c] = __float2bfloat16_rn(s);
+    st8(din + (size_t)p * din_c + din_off + 8 * g, s);
 }
 
 // dP = dY * (Y > 0) (ReLU), written in place of dY
 __global__ void k_relu_bwd(__nv_bfloat16* dy, int dy_c, int dy_off, const __nv_bfloat16* y, int y_c, int y_off,
-                           long long npix, int C) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= npix * C) return;
-    const int c = (int)(i % C);
-    const long long p = i / C;
-    if (!(__bfloat162float(y[p * y_c + y_off + c]) > 0.0f)) dy[p * dy_c + dy_off + c] = __float2bfloat16_rn(0.0f);
+                           int npix, int C) {
+    const int g8 = C / 8;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix * g8) return;
+    const int g = i % g8, p = i / g8;
+    float a[8], b[8];
+    __nv_bfloat16* d = dy + (size_t)p * dy_c + dy_off + 8 * g;
+    ld8(d, a);
+    ld8(y + (size_t)p * y_c + y_off + 8 * g, b);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (!(b[j] > 0.0f)) a[j] = 0.0f;
+    st8(d, a);
 }
 
 // db[c] += sum over pixels of dP[p][c]; one block per run of pixels, shared partial sums
@@ -240,8 +269,13 @@ cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
         return cudaErrorInvalidValue;
     const long long npix = (long long)a.B * a.H * a.W;
     const size_t smem = gkrt_wgrad_smem_bytes(a.cin);
-    cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    static bool attr_set = false;   // set once for the largest operand (cin = 256)
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)gkrt_wgrad_smem_bytes(256));
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
     const dim3 grid((unsigned)((npix + a.chunk - 1) / a.chunk), 9);
     k_conv_wgrad<<<grid, kWgThreads, smem, st>>>(a);
     return cudaGetLastError();
@@ -251,33 +285,33 @@ static inline unsigned nblk(long long n) { return (unsigned)((n + 255) / 256); }
 
 cudaError_t gkrt_launch_avgpool2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
                                  int h, int w, int C, cudaStream_t st) {
-    k_avgpool2<<<nblk((long long)B * h * w * C), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
+    k_avgpool2<<<nblk((long long)B * h * w * (C / 8)), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
                                                                (__nv_bfloat16*)out, out_c, out_off, B, h, w, C);
     return cudaGetLastError();
 }
 cudaError_t gkrt_launch_avgpool2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
                                      int B, int H, int W, int C, int accumulate, cudaStream_t st) {
-    k_avgpool2_bwd<<<nblk((long long)B * H * W * C), 256, 0, st>>>((const __nv_bfloat16*)dout, dout_c, dout_off,
+    k_avgpool2_bwd<<<nblk((long long)B * H * W * (C / 8)), 256, 0, st>>>((const __nv_bfloat16*)dout, dout_c, dout_off,
                                                                    (__nv_bfloat16*)din, din_c, din_off, B, H, W, C,
                                                                    accumulate);
     return cudaGetLastError();
 }
 cudaError_t gkrt_launch_upsample2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
                                   int H, int W, int C, cudaStream_t st) {
-    k_upsample2<<<nblk((long long)B * H * W * C), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
+    k_upsample2<<<nblk((long long)B * H * W * (C / 8)), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
                                                                 (__nv_bfloat16*)out, out_c, out_off, B, H, W, C);
     return cudaGetLastError();
 }
 cudaError_t gkrt_launch_upsample2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
                                       int B, int h, int w, int C, cudaStream_t st) {
-    k_upsample2_bwd<<<nblk((long long)B * h * w * C), 256, 0, st>>>((const __nv_bfloat16*)dout, dout_c, dout_off,
+    k_upsample2_bwd<<<nblk((long long)B * h * w * (C / 8)), 256, 0, st>>>((const __nv_bfloat16*)dout, dout_c, dout_off,
                                                                     (__nv_bfloat16*)din, din_c, din_off, B, h, w, C);
     return cudaGetLastError();
 }
 cudaError_t gkrt_launch_relu_bwd(void* dy, int dy_c, int dy_off, const void* y, int y_c, int y_off, long long npix,
                                  int C, cudaStream_t st) {
-    k_relu_bwd<<<nblk(npix * C), 256, 0, st>>>((__nv_bfloat16*)dy, dy_c, dy_off, (const __nv_bfloat16*)y, y_c, y_off,
-                                               npix, C);
+    k_relu_bwd<<<nblk(npix * (C / 8)), 256, 0, st>>>((__nv_bfloat16*)dy, dy_c, dy_off, (const __nv_bfloat16*)y, y_c,
+                                                     y_off, (int)npix, C);
     return cudaGetLastError();
 }
 cudaError_t gkrt_launch_bias_grad(const void* dp, int dp_c, int dp_off, long long npix, int C, float* db,

@@ -38,17 +38,23 @@ constexpr LayerDef kLayers[kUnetLayers] = {
 enum { E0A, E0B, E1A, E1B, E2A, E2B, E3A, E3B, D2A, D2B, D1A, D1B, D0A, D0B, OUT };
 
 __global__ void k_pack_input(const float* in, long long npix, __nv_bfloat16* x0) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= npix * 32) return;
-    const int c = (int)(i % 32);
-    const long long p = i / 32;
-    float v = 0.0f;
-    if (c < 10) {
-        v = in[p * 10 + c];
-        if (c < 3) v = log1pf(fmaxf(v, 0.0f));
-        if (c == 9) v = fminf(fmaxf(v, 0.0f), 1.0f);   // depth; misses carry 100000
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;   // one pixel
+    if (p >= npix) return;
+    float v[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) v[c] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 10; ++c) v[c] = in[p * 10 + c];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] = log1pf(fmaxf(v[c], 0.0f));
+    v[9] = fminf(fmaxf(v[9], 0.0f), 1.0f);   // depth; misses carry 100000
+    uint4* o = reinterpret_cast<uint4*>(x0 + p * 32);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        __nv_bfloat162 h[4];
+        for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(v[8 * k + 2 * j], v[8 * k + 2 * j + 1]);
+        o[k] = *reinterpret_cast<uint4*>(h);
     }
-    x0[i] = __float2bfloat16_rn(v);
 }
 
 // From the pass's images (pitched float4 / float): composed 1-spp radiance
@@ -393,7 +399,7 @@ cudaError_t gkrt_unet_forward_dev(Unet* u, const float* input, int b, int h, int
     cudaError_t e = u->ensure_size(b, h, w);
     if (e != cudaSuccess) return e;
     const long long npix = (long long)b * h * w;
-    if (input) k_pack_input<<<nb(npix * 32), 256, 0, st>>>(input, npix, u->x0);
+    if (input) k_pack_input<<<nb(npix), 256, 0, st>>>(input, npix, u->x0);
     if ((e = u->forward(st)) != cudaSuccess) return e;
     if (out_linear) k_out_linear<<<nb(npix), 256, 0, st>>>(u->y, npix, out_linear);
     if (out_raw) e = cudaMemcpyAsync(out_raw, u->y, npix * 16, cudaMemcpyDeviceToDevice, st);

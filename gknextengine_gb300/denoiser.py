@@ -11,6 +11,7 @@ are multiples of 8 and the image views are dense.
 from __future__ import annotations
 
 import ctypes as C
+import time
 
 import numpy as np
 
@@ -164,3 +165,75 @@ def train(net: Unet, data: CornellVariants, refs, steps: int, batch: int = 2, lr
         cur *= min(1.0, (step + 1) / warmup)
         losses.append(net.train_step(inp, tgt, cur))
     return losses
+
+
+def evaluate(r: PathTracingRenderer, net: Unet, width: int = 1920, height: int = 1080, variant: int = 16,
+             count: int = 17, seed: int = 5, ref_spp: int = 4096, reps: int = 10):
+    """RelMSE against a ref_spp reference of one held-out Cornell variant: the raw 1-spp frame,
+    the bilateral filter (the reference's JBF) and the a-trous filter on that frame (history
+    weight 0), the learned denoiser on it, and the temporal steady state of the two filters
+    (8 x 16 frames of reprojection at 1/16). Times are per 1080p frame, CUDA events."""
+    torch = _torch()
+    data = CornellVariants(r, width, height, count=count, seed=seed)
+    t0 = time.perf_counter()
+    ref = data.render_reference(variant, ref_spp)
+    out = {"scene": f"cornell variant {variant} {width}x{height}", "reference_spp": ref_spp,
+           "metric": "mean (x-y)^2/(y^2+1e-2) over px, RGB, linear radiance",
+           "reference_seconds": time.perf_counter() - t0}
+    st = data.settings
+    fseed = 424242
+    fc = data.frame(variant, fseed)
+    inp = torch.zeros((1, height, width, 10), device="cuda")
+    data.render_input(variant, fseed, inp[0])
+    out["raw_1spp"] = relmse(inp[0, ..., :3], ref)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    den = torch.zeros((1, height, width, 4), device="cuda")
+    out["learned_ms"] = timed(lambda: net.forward(inp, out_linear=den))
+    out["learned_1spp"] = relmse(den[0], ref)
+    out["trace_ms"] = timed(lambda: r.trace_pass(fc))
+    for name, mode in (("bilateral", abi.DENOISE_JBF), ("atrous", abi.DENOISE_ATROUS)):
+        st.denoiser, st.bf_size, st.temporal_frames = mode, 5, 1
+        fb = camera.FrameBuilder(width, height, st)
+        f1 = fb.build(data.cam.orbit(float(data.angles[variant])), fseed)
+        r.create_swap_chain(width, height)
+        r.trace_pass(f1)
+        r.reproject_pass(f1)
+        out[f"{name}_ms"] = timed(lambda: r.denoise_pass(f1))
+        out[f"{name}_1spp"] = relmse(device_view(r.image_view(abi.IMG_DENOISED_LINEAR), 4), ref)
+        st.temporal_frames = 16
+        fb = camera.FrameBuilder(width, height, st)
+        r.create_swap_chain(width, height)
+        for f in range(128):
+            r.render(fb.build(data.cam.orbit(float(data.angles[variant])), 500000 + f))
+        out[f"{name}_temporal"] = relmse(device_view(r.image_view(abi.IMG_DENOISED_LINEAR), 4), ref)
+        out["reproject_ms"] = timed(lambda: r.reproject_pass(f1))
+    out["learned_over_bilateral"] = out["learned_1spp"] / out["bilateral_1spp"]
+    out["frame_ms_bilateral"] = out["trace_ms"] + out["reproject_ms"] + out["bilateral_ms"]
+    out["frame_ms_learned"] = out["trace_ms"] + out["learned_ms"]
+    return out
+
+
+def train_default(r: PathTracingRenderer, steps: int = 600, variants: int = 16, ref_spp: int = 256,
+                  width: int = 512, height: int = 512, seed: int = 5):
+    """The training run the tests and the benchmark use; returns (net, losses, seconds)."""
+    data = CornellVariants(r, width, height, count=variants + 1, seed=seed)
+    t0 = time.perf_counter()
+    refs = [data.render_reference(v, ref_spp) for v in range(variants)]
+    t_data = time.perf_counter() - t0
+    net = Unet(r, seed=7)
+    t0 = time.perf_counter()
+    losses = train(net, data, refs, steps=steps, batch=2, lr=5e-4)
+    _torch().cuda.synchronize()
+    return net, losses, {"data_s": t_data, "train_s": time.perf_counter() - t0, "steps": steps,
+                         "ms_per_step": (time.perf_counter() - t0) / steps * 1e3}

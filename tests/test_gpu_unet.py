@@ -2,13 +2,11 @@
 numpy restatement (bf16 storage at the same points, FP64 arithmetic), training on the path
 tracer's own 1-spp / high-spp pairs, and its gain over the bilateral filter against a
 4096-spp reference at 1920 x 1080."""
-import time
-
 import numpy as np
 import pytest
 
 from gknextengine_gb300 import abi, camera, scenes
-from gknextengine_gb300.denoiser import CornellVariants, Unet, device_view, relmse, train
+from gknextengine_gb300.denoiser import Unet
 from gknextengine_gb300.renderer import PathTracingRenderer
 from oracle import unet_ref
 
@@ -87,50 +85,11 @@ def test_denoiser_beats_bilateral():
     """Train on 512 x 512 Cornell variants (256-spp targets), then on a held-out 1080p variant
     compare RelMSE against 4096 spp: the network must reach <= 0.8 x the bilateral filter's
     (the reference's joint bilateral filter on the same 1-spp frame)."""
-    torch = _torch()
+    from gknextengine_gb300.denoiser import evaluate, train_default
     with PathTracingRenderer(0) as r:
-        data = CornellVariants(r, 512, 512, count=17, seed=5)
-        t0 = time.perf_counter()
-        refs = [data.render_reference(v, 256) for v in range(16)]
-        t_data = time.perf_counter() - t0
-        net = Unet(r, seed=7)
-        t0 = time.perf_counter()
-        losses = train(net, data, refs, steps=600, batch=2, lr=5e-4)
-        torch.cuda.synchronize()
-        t_train = time.perf_counter() - t0
-        # held-out variant 16 at 1080p
-        Wt, Ht = 1920, 1080
-        test = CornellVariants(r, Wt, Ht, count=17, seed=5)
-        ref = test.render_reference(16, 4096)
-        inp = torch.zeros((1, Ht, Wt, 10), device="cuda")
-        test.render_input(16, 424242, inp[0])
-        out = torch.zeros((1, Ht, Wt, 4), device="cuda")
-        net.forward(inp, out_linear=out)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(5):
-            net.forward(inp, out_linear=out)
-        torch.cuda.synchronize()
-        t_net = (time.perf_counter() - t0) / 5
-        e_net = relmse(out[0], ref)
-        # the same 1-spp frame through the reference's bilateral filter (history weight 0)
-        st = test.settings
-        st.denoiser, st.bf_size, st.temporal_frames = abi.DENOISE_JBF, 5, 1
-        fb = camera.FrameBuilder(Wt, Ht, st)
-        fc = fb.build(test.cam.orbit(float(test.angles[16])), 424242)
-        r.create_swap_chain(Wt, Ht)
-        r.trace_pass(fc)
-        r.reproject_pass(fc)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(5):
-            r.denoise_pass(fc)
-        torch.cuda.synchronize()
-        t_jbf = (time.perf_counter() - t0) / 5
-        e_jbf = relmse(device_view(r.image_view(abi.IMG_DENOISED_LINEAR), 4), ref)
-        e_raw = relmse(inp[0, ..., :3], ref)
-        print(f"denoiser: data {t_data:.1f} s, train {t_train:.1f} s ({t_train / 600 * 1e3:.1f} ms/step), "
-              f"loss {np.mean(losses[:20]):.4f} -> {np.mean(losses[-20:]):.4f}; 1080p RelMSE raw {e_raw:.4f}, "
-              f"bilateral {e_jbf:.4f}, learned {e_net:.4f} (ratio {e_net / e_jbf:.3f}); "
-              f"ms: bilateral {t_jbf * 1e3:.3f}, learned {t_net * 1e3:.3f}")
-        assert e_net <= 0.8 * e_jbf
+        net, losses, info = train_default(r)
+        ev = evaluate(r, net)
+        print(f"denoiser: {info}, loss {np.mean(losses[:20]):.4f} -> {np.mean(losses[-20:]):.4f}; {ev}")
+        assert np.mean(losses[-20:]) < 0.2 * np.mean(losses[:20])
+        assert ev["learned_1spp"] <= 0.8 * ev["bilateral_1spp"]
+        assert ev["learned_1spp"] < ev["raw_1spp"]
