@@ -603,6 +603,146 @@ __global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, 
 }
 
 // ---------------------------------------------------------------------------------------------
+// collapse into compressed 8-wide nodes (WideNode, gk_trace.cuh)
+//
+// Top-down and breadth first over the two-child trees: a wide node starts from the children
+// of one binary interior node and repeatedly replaces its interior child of largest surface
+// area by that child's two children, up to 8 (Ylitie, Karras, Laine, HPG 2017, collapse by
+// greedy expansion). Its interior children become the next level's wide nodes; indices come
+// from an exclusive scan of the per-node interior counts, so the layout is deterministic.
+
+struct WEnt {
+    int ref;
+    float b[6];
+};
+
+// Children of binary node `node`: the first replaces e[at], the second is appended at e[n].
+// Returns false for a node without children (not produced by the builders).
+__device__ bool wide_children(const BvhNode* bin, int node, WEnt* e, int& n, int at) {
+    const float* f = reinterpret_cast<const float*>(bin + node);
+    const int* r = reinterpret_cast<const int*>(bin + node) + 12;
+    bool first = true;
+    for (int side = 0; side < 2; ++side) {
+        if (r[side] == kRefPop) continue;   // the empty half of a single-leaf root
+        WEnt& d = first ? e[at] : e[n++];
+        first = false;
+        d.ref = r[side];
+        for (int j = 0; j < 6; ++j) d.b[j] = f[6 * side + j];
+    }
+    return !first;
+}
+
+// Greedy expansion of binary node `root` into at most 8 children; -1 on a malformed tree.
+__device__ int wide_expand(const BvhNode* bin, int root, WEnt* e) {
+    int n = 1;
+    if (!wide_children(bin, root, e, n, 0)) return -1;
+    while (n < 8) {
+        int best = -1;
+        float ba = -1.0f;
+        for (int i = 0; i < n; ++i) {
+            if (e[i].ref < 0) continue;
+            const float a = area6(e[i].b);
+            if (a > ba) { ba = a; best = i; }
+        }
+        if (best < 0) break;
+        if (!wide_children(bin, e[best].ref, e, n, best)) return -1;
+    }
+    return n;
+}
+
+// Per-axis scale 2^ex and origin k for the children's boxes, one step of margin on each side
+// (exact double arithmetic: x / 2^ex of a float is exact here, so are floor and ceil). The
+// exponent is capped at 38 so that 2^23 s |inv| stays finite for |inv| <= 1e20. Fails on
+// non-finite or out-of-range boxes.
+__device__ bool wide_axis(const WEnt* e, int n, int ax, float& origin, uint32_t& ebyte, uint32_t* qlo,
+                          uint32_t* qhi) {
+    float lo = INFINITY, hi = -INFINITY;
+    for (int i = 0; i < n; ++i) {
+        lo = fminf(lo, e[i].b[ax]);
+        hi = fmaxf(hi, e[i].b[3 + ax]);
+    }
+    if (!(isfinite(lo) && isfinite(hi) && hi >= lo)) return false;
+    int ex = -100;
+    const double range = (double)hi - (double)lo;
+    if (range > 0.0) ex = max(ex, ilogb(range / 253.0));
+    if (lo != 0.0f) ex = max(ex, ilogb(fabs((double)lo)) - 21);
+    for (; ex <= 38; ++ex) {
+        const double s = ldexp(1.0, ex);
+        const double k = floor((double)lo / s) - 1.0;
+        if (fabs(k) >= 4194304.0) continue;   // |k| < 2^22
+        bool ok = true;
+        for (int i = 0; i < n; ++i) ok = ok && (ceil((double)e[i].b[3 + ax] / s) + 1.0 - k <= 255.0);
+        if (!ok) continue;
+        for (int i = 0; i < n; ++i) {
+            qlo[i] = (uint32_t)(floor((double)e[i].b[ax] / s) - 1.0 - k);
+            qhi[i] = (uint32_t)(ceil((double)e[i].b[3 + ax] / s) + 1.0 - k);
+        }
+        origin = (float)(k * s);
+        ebyte = (uint32_t)(ex + 127);
+        return true;
+    }
+    return false;
+}
+
+// items: x binary node, y wide index, z depth (1 at the roots)
+__global__ void k_wide_count(const BvhNode* bin, const int4* items, uint32_t n, uint32_t* cnt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    WEnt e[8];
+    const int m = wide_expand(bin, items[i].x, e);
+    uint32_t c = 0;
+    for (int j = 0; j < m; ++j) c += e[j].ref >= 0 ? 1u : 0u;
+    cnt[i] = c;   // 0 for a malformed node: k_wide_emit reports it
+}
+
+__global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, const uint32_t* off, uint32_t next_base,
+                            WideNode* out, int4* next, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 it = items[i];
+    WEnt e[8];
+    int m = wide_expand(bin, it.x, e);
+    if (m < 0) {
+        atomicOr(err, kBuildErrRange);
+        m = 0;
+    }
+    uint32_t qw[3][4] = {{0u, 0u, 0u, 0u}, {0u, 0u, 0u, 0u}, {0u, 0u, 0u, 0u}};
+    float origin[3] = {0.0f, 0.0f, 0.0f};
+    uint32_t meta = m > 0 ? ((1u << m) - 1u) << 24 : 0u;
+    for (int ax = 0; ax < 3; ++ax) {
+        uint32_t qlo[8], qhi[8], eb = 127u;
+        if (m > 0 && !wide_axis(e, m, ax, origin[ax], eb, qlo, qhi)) {
+            atomicOr(err, kBuildErrRange);   // the build fails; the node is written without slots
+            meta = 0u;
+            break;
+        }
+        meta |= eb << (8 * ax);
+        for (int j = 0; j < m; ++j) {
+            qw[ax][j >> 2] |= qlo[j] << (8 * (j & 3));
+            qw[ax][2 + (j >> 2)] |= qhi[j] << (8 * (j & 3));
+        }
+    }
+    int ref[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t rank = 0;
+    for (int j = 0; j < m; ++j) {   // interior children are still counted: the scan expects them
+        if (e[j].ref >= 0) {
+            const uint32_t wi = next_base + off[i] + rank;
+            next[off[i] + rank] = make_int4(e[j].ref, (int)wi, it.z + 1, 0);
+            ref[j] = (int)wi;
+            ++rank;
+        } else {
+            ref[j] = e[j].ref;
+        }
+    }
+    WideNode w;
+    w.h = make_float4(origin[0], origin[1], origin[2], __uint_as_float(meta));
+    for (int ax = 0; ax < 3; ++ax) w.q[ax] = make_uint4(qw[ax][0], qw[ax][1], qw[ax][2], qw[ax][3]);
+    w.ref[0] = make_int4(ref[0], ref[1], ref[2], ref[3]);
+    w.ref[1] = make_int4(ref[4], ref[5], ref[6], ref[7]);
+    out[it.y] = w;
+}
+
+// ---------------------------------------------------------------------------------------------
 // exclusive scans of uint32 / uint4: in-block inclusive scans, a scan of the block sums, a fix-up
 
 __device__ __forceinline__ uint32_t add_(uint32_t a, uint32_t b) { return a + b; }
@@ -716,6 +856,8 @@ struct GpuBvh {
     DBuf<BvhNode> nodes;
     DBuf<MeshRange> ranges;
     DBuf<GpuInstBox> inst;
+    DBuf<int4> witems[2];
+    DBuf<uint32_t> wcnt, woff, werr;
     uint32_t launches = 0;   // kernels launched by all builds so far
 
     ~GpuBvh() {
@@ -726,6 +868,7 @@ struct GpuBvh {
         wleft.release(); wleft_scan.release(); bsum32.release(); tot32.release(); info.release(); map.release();
         cc.release(); cc_scan.release(); bsum4.release(); tot4.release(); bins.release(); tb.release();
         split.release(); small.release(); nodes.release(); ranges.release(); inst.release();
+        witems[0].release(); witems[1].release(); wcnt.release(); woff.release(); werr.release();
     }
 
     template <class T>
@@ -875,6 +1018,59 @@ struct GpuBvh {
         out->root_box = root_box.p;
         return cudaSuccess;
     }
+
+    // Collapses the two-child trees rooted at roots[r] (refs into bin; -1: none) into wide
+    // nodes out[wide_base, wide_base + count), out holding out_cap nodes in all. The root of
+    // tree r becomes wide node wroots[r] = wide_base + (its position among the valid roots).
+    cudaError_t collapse(const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base, WideNode* out,
+                         size_t out_cap, std::vector<int>& wroots, uint32_t* count, int* depth, cudaStream_t st) {
+        wroots.assign(roots.size(), -1);
+        std::vector<int4> it0;
+        uint32_t next = wide_base;
+        for (size_t r = 0; r < roots.size(); ++r) {
+            if (roots[r] < 0) continue;
+            wroots[r] = (int)next;
+            it0.push_back(make_int4(roots[r], (int)next, 1, 0));
+            ++next;
+        }
+        *count = 0;
+        *depth = 0;
+        uint32_t n = (uint32_t)it0.size();
+        if (n == 0) return cudaSuccess;
+        if (next > out_cap) return cudaErrorInvalidValue;
+        GK_TRY(witems[0].need(n));
+        GK_TRY(werr.need(1));
+        GK_TRY(cudaMemsetAsync(werr.p, 0, 4, st));
+        GK_TRY(cudaMemcpyAsync(witems[0].p, it0.data(), n * sizeof(int4), cudaMemcpyHostToDevice, st));
+        int cur = 0, levels = 0;
+        while (n > 0) {
+            if (++levels > 64) return cudaErrorInvalidValue;
+            GK_TRY(wcnt.need(n));
+            GK_TRY(woff.need(n));
+            const uint32_t g = (n + 127) / 128;
+            k_wide_count<<<g, 128, 0, st>>>(bin, witems[cur].p, n, wcnt.p);
+            ++launches;
+            GK_TRY(scan<uint32_t>(wcnt.p, n, woff.p, bsum32, tot32, st));
+            uint32_t tot = 0;
+            GK_TRY(cudaMemcpyAsync(&tot, tot32.p, 4, cudaMemcpyDeviceToHost, st));
+            GK_TRY(cudaStreamSynchronize(st));
+            if ((size_t)next + tot > out_cap) return cudaErrorInvalidValue;
+            GK_TRY(witems[cur ^ 1].need(std::max<uint32_t>(tot, 1u)));
+            k_wide_emit<<<g, 128, 0, st>>>(bin, witems[cur].p, n, woff.p, next, out, witems[cur ^ 1].p, werr.p);
+            ++launches;
+            GK_TRY(cudaGetLastError());
+            next += tot;
+            n = tot;
+            cur ^= 1;
+        }
+        uint32_t herr = 0;
+        GK_TRY(cudaMemcpyAsync(&herr, werr.p, 4, cudaMemcpyDeviceToHost, st));
+        GK_TRY(cudaStreamSynchronize(st));
+        if (herr) return cudaErrorInvalidValue;
+        *count = next - wide_base;
+        *depth = levels;
+        return cudaSuccess;
+    }
 };
 
 GpuBvh* gpu_bvh_new() { return new (std::nothrow) GpuBvh(); }
@@ -932,6 +1128,12 @@ cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint
     const std::vector<uint32_t> rb(1, 0u), re(1, n);
     GK_TRY(B->build(n, rb, re, 1, true, B->map.p, node_base, out, st));
     return cudaStreamSynchronize(st);
+}
+
+cudaError_t gpu_bvh_collapse(GpuBvh* B, const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base,
+                             WideNode* out, size_t out_cap, std::vector<int>& wroots, uint32_t* count, int* depth,
+                             cudaStream_t st) {
+    return B->collapse(bin, roots, wide_base, out, out_cap, wroots, count, depth, st);
 }
 
 }  // namespace gk

@@ -1,10 +1,11 @@
 // gk_trace.cuh — two-level BVH traversal with an exact closest-hit contract (sm_103a).
 //
 // Replaces the RT-core RayQuery of FHardwareRayTracerV2 (assets/shaders/common/
-// Shading.slang:737-826). GB300 has no RT cores, so traversal is software: 64-byte
-// two-child nodes read as four 16-byte vector loads, 48-byte triangles in leaf order,
-// a per-thread stack in shared memory (strided by the block size, conflict-free) and a
-// marker entry for the hand-over from the instance level to the mesh level.
+// Shading.slang:737-826). GB300 has no RT cores, so traversal is software over compressed
+// 8-wide nodes (96 bytes: six 16-byte vector loads test eight child boxes), 48-byte
+// triangles in leaf order, a per-thread stack of node groups in shared memory (strided by
+// the block size, conflict-free) and a marker entry for the hand-over from the instance
+// level to the mesh level.
 //
 // Hit contract. The reported hit is the minimum of (t, instance index, primitive index)
 // under an FP64 evaluation of the watertight ray/triangle test (Woop, Benthin, Wald,
@@ -18,13 +19,16 @@
 // the FP64 winner is culled. A ray component of exactly zero lying on a box face is the one
 // case a t-interval widening cannot cover ((hi - o) * inv is 0 there), so the builders store
 // every node box widened in space as well (widen_lo / widen_hi): a triangle edge on the
-// face stays inside the box the ray is tested against. The float t and barycentrics used for shading are those of
-// the FP32 test when it is certain, else the rounded FP64 values.
+// face stays inside the box the ray is tested against. The 8-bit child boxes of the wide
+// nodes decode EXACTLY to planes at or outside those widened boxes (WideNode below), so the
+// compression adds boxes, never removes them. The float t and barycentrics used for shading
+// are those of the FP32 test when it is certain, else the rounded FP64 values.
 #pragma once
 #include "gk_device.cuh"
 
 namespace gk {
 
+// Two-child node: the output of the SAH builders, collapsed into WideNode for traversal.
 struct __align__(16) BvhNode {
     float4 a;   // c0.lo.x c0.lo.y c0.lo.z c0.hi.x
     float4 b;   // c0.hi.y c0.hi.z c1.lo.x c1.lo.y
@@ -32,9 +36,23 @@ struct __align__(16) BvhNode {
     int4 d;     // ref0 ref1 - -   (ref >= 0: interior node; ref < 0: ~(payload << 3 | count-1))
 };
 
+// Compressed 8-wide node. Per axis a scale s = 2^e (-100 <= e <= 38) and an integer origin k
+// (|k| < 2^22, origin p = k s exact in float); child slot j's planes are (k + q) s for 8-bit
+// q_lo = floor(lo / s) - 1 - k and q_hi = ceil(hi / s) + 1 - k of the child's stored (widened)
+// box: every encoded box lies at least one step s outside the box it encodes.
+// Traversal evaluates a plane's t as fma(2^23 + q, C, B') with C = s inv (exact) and
+// B' = (p - o) inv - 2^23 C (three roundings), whose error is below 5.02u|t| + 0.5001 s|inv|:
+// the step margin absorbs the absolute part and the 1e-6 slab widening the relative part, so
+// no box holding the exact winner is culled.
+struct __align__(16) WideNode {
+    float4 h;       // origin p x y z; w bits: 0-7 / 8-15 / 16-23 = e + 127 per axis, 24-31 valid-slot mask
+    uint4 q[3];     // per axis: q_lo slots 0-3, q_lo 4-7, q_hi 0-3, q_hi 4-7 (slot j in byte j & 3)
+    int4 ref[2];    // slot refs, BvhNode encoding (interior refs index the WideNode array)
+};
+
 struct __align__(16) DevInst {
     float winv[12];       // world -> object rows
-    int blas_root;        // interior node index of the mesh BVH
+    int blas_root;        // root WideNode index of the mesh BVH
     uint32_t index_offset;
     uint32_t vertex_offset;
     uint32_t instance_id;
@@ -44,7 +62,8 @@ struct __align__(16) DevInst {
 GK_HD float widen_lo(float v) { return v - (fabsf(v) * 1e-6f + 1e-10f); }
 GK_HD float widen_hi(float v) { return v + (fabsf(v) * 1e-6f + 1e-10f); }
 
-constexpr int kStackSize = 64;
+constexpr int kStackEntries = 24;                // node-group entries per thread
+constexpr int kStackSize = 3 * kStackEntries;    // 32-bit words per thread
 constexpr int kRefPop = 0x7FFFFFFE;
 constexpr int kRefMarker = 0x7FFFFFFF;
 constexpr int kIterCap = 1 << 22;
@@ -59,7 +78,7 @@ struct Counters {
 };
 
 struct SceneView {
-    const BvhNode* nodes;
+    const WideNode* nodes;
     const float4* tris;     // 3 float4 per triangle, v0.w = primitive index bits
     const DevInst* inst;
     int tlas_root;          // -1: empty scene
@@ -232,18 +251,6 @@ GK_D f3 safe_inv(f3 d) {
     return F3(rcp_(x), rcp_(y), rcp_(z));
 }
 
-// Slab test widened by 1e-6 relative; tcull already carries the same widening.
-GK_D bool slab(float lx, float ly, float lz, float hx, float hy, float hz, f3 o, f3 inv, float tmin, float tcull,
-               float& tnear) {
-    float t0x = (lx - o.x) * inv.x, t1x = (hx - o.x) * inv.x;
-    float t0y = (ly - o.y) * inv.y, t1y = (hy - o.y) * inv.y;
-    float t0z = (lz - o.z) * inv.z, t1z = (hz - o.z) * inv.z;
-    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z)) * 1.000001f;
-    tnear = tn;
-    return tn <= fminf(tf, tcull);
-}
-
 struct TraceOut {
     bool hit;
     bool ambiguous;
@@ -402,50 +409,124 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
     return false;
 }
 
-// Node phase of the traversal ("while-while" with speculative traversal, Aila and Laine,
-// HPG 2009): interior nodes, stack pops, returns to the instance level and instance entries.
-// The first triangle leaf found is postponed into T.leaf and the lane keeps traversing;
-// a second leaf, or leaving the instance the postponed leaf belongs to, makes the lane wait
-// for the leaf phase. Returns true while the lane can take another node step.
+// t of byte `b` of `word` (a WideNode plane): fma(2^23 + q, C, B').
+GK_D float wide_t(uint32_t word, int b, float C, float Bp) {
+    return fmaf_(__uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u + (uint32_t)b)), C, Bp);
+}
+
+GK_D void wide_sort_cx(uint32_t& a, uint32_t& b) {
+    const uint32_t lo = min(a, b);
+    b = max(a, b);
+    a = lo;
+}
+
+GK_D void trav_to_world(Trav& T) {
+    T.o = T.wo; T.d = T.wd; T.inv = safe_inv(T.wd);
+    T.inblas = false;
+}
+
+// Node phase of the traversal ("while-while", Aila and Laine, HPG 2009, over 8-wide nodes).
+// The group stack holds one entry per wide node with more than one child left to visit:
+// three words (node index or kRefMarker; pending slots; t lower bound). Pending word: bits
+// 0-2 the count c of slots left, bits 3 + 3i the i-th slot to visit next, nearest first.
+// A step pops (dropping groups whose nearest pending child lies beyond the current hit) and
+// tests the popped node's eight children in the same call, so the lanes of a warp stay on
+// the same instructions. A triangle leaf is postponed into T.leaf and the lane waits for the
+// leaf phase; so does a lane about to leave the instance of its postponed leaf. Returns true
+// while the lane can take another node step.
 GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn) {
     if (++T.iter > kIterCap) { atomicOr(S.error, kErrIter); T.done = true; return false; }
-    const int ref = T.ref;
-    if (ref == kRefPop) {
-        if (T.sp == 0) { T.done = true; return false; }
-        --T.sp;
-        T.ref = (int)stk[T.sp * stride];
-        return true;
+    int ref = T.ref;
+    if (ref == kRefMarker) {            // hand-back deferred until the postponed leaf was tested
+        if (T.has_leaf) return false;
+        trav_to_world(T);
+        ref = kRefPop;
     }
-    if (ref == kRefMarker) {
-        if (T.has_leaf) return false;   // the postponed leaf needs this instance's ray
-        T.o = T.wo; T.d = T.wd; T.inv = safe_inv(T.wd);
-        T.inblas = false;
-        T.ref = kRefPop;
-        return true;
+    if (ref == kRefPop) {
+        for (;;) {
+            if (T.sp == 0) { T.done = true; T.ref = kRefPop; return false; }
+            uint32_t* e = stk + 3 * (T.sp - 1) * stride;
+            const uint32_t node = e[0];
+            if (node == (uint32_t)kRefMarker) {
+                --T.sp;
+                if (T.has_leaf) { T.ref = kRefMarker; return false; }
+                trav_to_world(T);
+                continue;
+            }
+            const uint32_t w = e[stride];
+            if (__uint_as_float(e[2 * stride]) > T.tcull) { --T.sp; continue; }
+            const uint32_t c = w & 7u, slot = (w >> 3) & 7u;
+            if (c <= 1u) --T.sp;
+            else e[stride] = ((w >> 3) & ~7u) | (c - 1u);
+            ref = __ldg(reinterpret_cast<const int*>(S.nodes + node) + 16 + slot);
+            break;
+        }
     }
     if (ref >= 0) {
         ++cn.nodes;
         const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
-        const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
-        const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
-        float tn0, tn1;
-        const bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, T.o, T.inv, kTmin, T.tcull, tn0);
-        const bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, T.o, T.inv, kTmin, T.tcull, tn1);
-        if (h0 && h1) {
-            int nearr = nd.x, farr = nd.y;
-            if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
-            if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return false; }
-            stk[T.sp * stride] = (uint32_t)farr;
-            ++T.sp;
-            T.ref = nearr;
-        } else if (h0) {
-            T.ref = nd.x;
-        } else if (h1) {
-            T.ref = nd.y;
-        } else {
-            T.ref = kRefPop;
+        const float4 h = __ldg(np);
+        const uint4 qx = __ldg(reinterpret_cast<const uint4*>(np + 1));
+        const uint4 qy = __ldg(reinterpret_cast<const uint4*>(np + 2));
+        const uint4 qz = __ldg(reinterpret_cast<const uint4*>(np + 3));
+        const uint32_t meta = __float_as_uint(h.w);
+        const float Cx = __uint_as_float((meta & 0xFFu) << 23) * T.inv.x;
+        const float Cy = __uint_as_float(((meta >> 8) & 0xFFu) << 23) * T.inv.y;
+        const float Cz = __uint_as_float(((meta >> 16) & 0xFFu) << 23) * T.inv.z;
+        const float Bx = fmaf_(-8388608.0f, Cx, (h.x - T.o.x) * T.inv.x);
+        const float By = fmaf_(-8388608.0f, Cy, (h.y - T.o.y) * T.inv.y);
+        const float Bz = fmaf_(-8388608.0f, Cz, (h.z - T.o.z) * T.inv.z);
+        // near / far plane words by the sign of the direction (the slab min / max)
+        const bool nx = T.inv.x < 0.0f, ny = T.inv.y < 0.0f, nz = T.inv.z < 0.0f;
+        const uint32_t nx0 = nx ? qx.z : qx.x, nx1 = nx ? qx.w : qx.y, fx0 = nx ? qx.x : qx.z, fx1 = nx ? qx.y : qx.w;
+        const uint32_t ny0 = ny ? qy.z : qy.x, ny1 = ny ? qy.w : qy.y, fy0 = ny ? qy.x : qy.z, fy1 = ny ? qy.y : qy.w;
+        const uint32_t nz0 = nz ? qz.z : qz.x, nz1 = nz ? qz.w : qz.y, fz0 = nz ? qz.x : qz.z, fz1 = nz ? qz.y : qz.w;
+        uint32_t key[8];
+        uint32_t nhit = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int b = i & 3;
+            const float tnx = wide_t(i < 4 ? nx0 : nx1, b, Cx, Bx), tfx = wide_t(i < 4 ? fx0 : fx1, b, Cx, Bx);
+            const float tny = wide_t(i < 4 ? ny0 : ny1, b, Cy, By), tfy = wide_t(i < 4 ? fy0 : fy1, b, Cy, By);
+            const float tnz = wide_t(i < 4 ? nz0 : nz1, b, Cz, Bz), tfz = wide_t(i < 4 ? fz0 : fz1, b, Cz, Bz);
+            // slab interval widened by 1e-6 relative; T.tcull carries the same widening
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, kTmin));
+            const float tf = fminf(fminf(tfx, tfy), tfz) * 1.000001f;
+            const bool hit = ((meta >> (24 + i)) & 1u) && tn <= fminf(tf, T.tcull);
+            key[i] = hit ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xFFFFFFFFu;
+            nhit += hit ? 1u : 0u;
         }
-        return true;
+        if (nhit == 0u) {
+            T.ref = kRefPop;
+            return true;
+        }
+        // Batcher's odd-even merge sort of the 8 keys (tnear bits, slot in the low bits)
+        wide_sort_cx(key[0], key[1]); wide_sort_cx(key[2], key[3]); wide_sort_cx(key[4], key[5]);
+        wide_sort_cx(key[6], key[7]); wide_sort_cx(key[0], key[2]); wide_sort_cx(key[1], key[3]);
+        wide_sort_cx(key[4], key[6]); wide_sort_cx(key[5], key[7]); wide_sort_cx(key[1], key[2]);
+        wide_sort_cx(key[5], key[6]); wide_sort_cx(key[0], key[4]); wide_sort_cx(key[1], key[5]);
+        wide_sort_cx(key[2], key[6]); wide_sort_cx(key[3], key[7]); wide_sort_cx(key[2], key[4]);
+        wide_sort_cx(key[3], key[5]); wide_sort_cx(key[1], key[2]); wide_sort_cx(key[3], key[4]);
+        wide_sort_cx(key[5], key[6]);
+        if (nhit > 1u) {
+            if (T.sp >= kStackEntries) { atomicOr(S.error, kErrStack); T.done = true; return false; }
+            uint32_t w = nhit - 1u;
+#pragma unroll
+            for (int j = 1; j < 8; ++j) w |= (key[j] & 7u) << (3 * j);
+            uint32_t* e = stk + 3 * T.sp * stride;
+            e[0] = (uint32_t)ref;
+            e[stride] = w;
+            e[2 * stride] = key[1] & ~7u;   // <= the nearest pending child's tnear
+            ++T.sp;
+        }
+        const uint32_t s0 = key[0] & 7u;
+        const int4 rr = __ldg(reinterpret_cast<const int4*>(np + 4 + (s0 >> 2)));
+        ref = (s0 & 2u) ? ((s0 & 1u) ? rr.w : rr.z) : ((s0 & 1u) ? rr.y : rr.x);
+        if (ref >= 0) {
+            T.ref = ref;
+            return true;
+        }
+        // nearest child is an instance or a triangle leaf: enter or postpone it here
     }
     const uint32_t payload = ~(uint32_t)ref;
     if (!T.inblas) {
@@ -458,14 +539,20 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         T.d = xvector(w, T.wd);
         T.inv = safe_inv(T.d);
         T.sh = make_shear(T.d);
-        if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return false; }
-        stk[T.sp * stride] = (uint32_t)kRefMarker;
+        if (T.sp >= kStackEntries) { atomicOr(S.error, kErrStack); T.done = true; return false; }
+        uint32_t* e = stk + 3 * T.sp * stride;
+        e[0] = (uint32_t)kRefMarker;
+        e[stride] = 0u;
+        e[2 * stride] = 0u;
         ++T.sp;
         T.inblas = true;
         T.ref = __ldg(&ip->blas_root);
         return true;
     }
-    if (T.has_leaf) return false;       // one postponed leaf at a time
+    if (T.has_leaf) {                   // one postponed leaf at a time
+        T.ref = ref;
+        return false;
+    }
     T.leaf = payload;
     T.has_leaf = true;
     T.ref = kRefPop;

@@ -51,8 +51,10 @@ struct GkrtContext {
     uint32_t* d_cubes = nullptr;
     uint32_t* d_voxels = nullptr;
 
-    // acceleration structures: d_nodes holds the mesh-level nodes [0, blas_node_count) and
-    // the instance-level nodes after them
+    // acceleration structures: d_nodes holds the builders' two-child mesh-level nodes
+    // [0, blas_node_count) and the instance-level nodes after them; d_wide holds their
+    // collapse into the 8-wide nodes the kernels traverse (mesh level [0, blas_wide_count),
+    // then the instance level)
     bool host_build = false;          // GKRT_BUILD_ON_HOST
     GpuBvh* builder = nullptr;
     uint32_t blas_node_count = 0, blas_nodes_used = 0;
@@ -64,6 +66,11 @@ struct GkrtContext {
     float4* d_tris = nullptr;
     int tlas_root = -1;
     uint32_t tlas_nodes = 0;
+    WideNode* d_wide = nullptr;
+    size_t d_wide_cap = 0;
+    std::vector<int> blas_wide_root;
+    uint32_t blas_wide_count = 0, tlas_wide_count = 0;
+    int blas_wide_depth = 0, tlas_wide_depth = 0, tlas_wide_root = -1;
     bool blas_ready = false, tlas_ready = false;
     uint32_t inst_cap = 0;            // instance arrays allocated for this many instances
 
@@ -133,10 +140,15 @@ void free_images(GkrtContext* c) {
 void free_scene(GkrtContext* c) {
     dfree(c->d_pos); dfree(c->d_nrm); dfree(c->d_slot); dfree(c->d_idx); dfree(c->d_mat);
     dfree(c->d_inst_mat); dfree(c->d_inst_prev); dfree(c->d_inst); dfree(c->d_cubes); dfree(c->d_voxels);
-    dfree(c->d_nodes); dfree(c->d_tris); dfree(c->d_blas_box); dfree(c->d_emit); dfree(c->d_emit_alias);
+    dfree(c->d_nodes); dfree(c->d_wide); dfree(c->d_tris); dfree(c->d_blas_box); dfree(c->d_emit); dfree(c->d_emit_alias);
     c->nemit = c->emit_cap = 0;
     c->mat_host.clear(); c->slot_tris.clear();
     c->d_nodes_cap = 0;
+    c->d_wide_cap = 0;
+    c->blas_wide_root.clear();
+    c->blas_wide_count = c->tlas_wide_count = 0;
+    c->blas_wide_depth = c->tlas_wide_depth = 0;
+    c->tlas_wide_root = -1;
     c->inst_cap = 0;
     c->has_scene = false;
     c->blas_ready = c->tlas_ready = false;
@@ -199,7 +211,7 @@ int upload_instances(GkrtContext* ctx) {
         std::memcpy(&prev[12 * (size_t)i], s.combined_prev, 48);
         std::memcpy(di[i].winv, s.world_inv, 48);
         const GkrtMesh& m = ctx->meshes[s.mesh_id];
-        di[i].blas_root = ctx->blas_ready ? ctx->blas_root[s.mesh_id] : -1;
+        di[i].blas_root = ctx->blas_ready ? ctx->blas_wide_root[s.mesh_id] : -1;
         di[i].index_offset = m.index_offset;
         di[i].vertex_offset = m.vertex_offset;
         di[i].instance_id = s.instance_id;
@@ -241,12 +253,69 @@ int get_builder(GkrtContext* ctx) {
     return ctx->builder ? GKRT_OK : fail(ctx, GKRT_ERR_OOM, "BVH builder");
 }
 
-int finish_blas(GkrtContext* ctx) {
+// d_wide capacity for `total` wide nodes, keeping the first `keep`.
+int ensure_wide_cap(GkrtContext* ctx, size_t total, size_t keep) {
+    if (total <= ctx->d_wide_cap && ctx->d_wide) return GKRT_OK;
+    const size_t cap = std::max<size_t>(total + total / 4, 16);
+    WideNode* q = nullptr;
+    GK_CUDA(cudaMalloc((void**)&q, cap * sizeof(WideNode)));
+    cudaError_t e = cudaSuccess;
+    if (ctx->d_wide && keep) e = cudaMemcpy(q, ctx->d_wide, keep * sizeof(WideNode), cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(q);
+        return cuda_fail(ctx, e, "cudaMemcpy(wide nodes)");
+    }
+    dfree(ctx->d_wide);
+    ctx->d_wide = q;
+    ctx->d_wide_cap = cap;
+    return GKRT_OK;
+}
+
+// Group-stack entries a ray can need: one per wide level of each tree plus the marker.
+int check_stack_bound(GkrtContext* ctx) {
+    if (ctx->blas_wide_depth + ctx->tlas_wide_depth + 1 > kStackEntries)
+        return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "BVH deeper than the traversal stack allows (" +
+                                                    std::to_string(ctx->blas_wide_depth) + " mesh + " +
+                                                    std::to_string(ctx->tlas_wide_depth) + " instance levels)");
+    return GKRT_OK;
+}
+
+// The mesh-level two-child trees in d_nodes collapsed into wide nodes [0, blas_wide_count).
+int finish_blas(GkrtContext* ctx, cudaStream_t st) {
     int rc = upload(ctx, ctx->d_blas_box, ctx->blas_box.data(), ctx->blas_box.size() * 4);
     if (rc != GKRT_OK) return rc;
+    if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
+    const size_t cap = (size_t)ctx->blas_node_count + 2 * ctx->inst.size() + 2;
+    dfree(ctx->d_wide);
+    ctx->d_wide_cap = 0;
+    if ((rc = ensure_wide_cap(ctx, cap, 0)) != GKRT_OK) return rc;
+    const cudaError_t e = gpu_bvh_collapse(ctx->builder, ctx->d_nodes, ctx->blas_root, 0, ctx->d_wide, ctx->d_wide_cap,
+                                           ctx->blas_wide_root, &ctx->blas_wide_count, &ctx->blas_wide_depth, st);
+    if (e == cudaErrorInvalidValue)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "mesh BVH collapse failed (non-finite geometry or depth > 64)");
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "gpu_bvh_collapse(mesh level)");
+    ctx->tlas_wide_depth = 0;
+    if ((rc = check_stack_bound(ctx)) != GKRT_OK) return rc;
     ctx->blas_ready = true;
     ctx->tlas_ready = false;
     return GKRT_OK;
+}
+
+// The instance-level two-child tree (root ctx->tlas_root) collapsed after the mesh level.
+int finish_tlas(GkrtContext* ctx, uint32_t bin_count, cudaStream_t st) {
+    int rc;
+    if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
+    if ((rc = ensure_wide_cap(ctx, (size_t)ctx->blas_wide_count + bin_count + 1, ctx->blas_wide_count)) != GKRT_OK)
+        return rc;
+    std::vector<int> wr;
+    const cudaError_t e = gpu_bvh_collapse(ctx->builder, ctx->d_nodes, std::vector<int>(1, ctx->tlas_root),
+                                           ctx->blas_wide_count, ctx->d_wide, ctx->d_wide_cap, wr,
+                                           &ctx->tlas_wide_count, &ctx->tlas_wide_depth, st);
+    if (e == cudaErrorInvalidValue)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "instance BVH collapse failed (non-finite transforms or depth > 64)");
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "gpu_bvh_collapse(instance level)");
+    ctx->tlas_wide_root = wr[0];
+    return check_stack_bound(ctx);
 }
 
 // Mesh-level trees on the GPU: one build over every mesh's triangles.
@@ -262,7 +331,6 @@ int build_blas_gpu(GkrtContext* ctx, cudaStream_t st) {
     if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
     GpuBvhResult r;
     GK_CUDA(gpu_bvh_build_meshes(ctx->builder, ctx->d_pos, ctx->d_idx, ctx->meshes.data(), nm, 0, ctx->d_tris, &r, st));
-    if (r.depth > kStackSize - 24) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "mesh BVH deeper than the traversal stack allows");
     ctx->blas_root = r.root_node;
     if (nm) GK_CUDA(cudaMemcpy(ctx->blas_box.data(), r.root_box, 6 * (size_t)nm * 4, cudaMemcpyDeviceToHost));
     ctx->blas_node_count = r.node_count;
@@ -272,11 +340,11 @@ int build_blas_gpu(GkrtContext* ctx, cudaStream_t st) {
     if ((rc = ensure_node_cap(ctx, (size_t)r.node_count + 2 * ctx->inst.size() + 2)) != GKRT_OK) return rc;
     if (r.node_count)
         GK_CUDA(cudaMemcpy(ctx->d_nodes, r.nodes, (size_t)r.node_count * sizeof(BvhNode), cudaMemcpyDeviceToDevice));
-    return finish_blas(ctx);
+    return finish_blas(ctx, st);
 }
 
 // Mesh-level trees on the host (GKRT_BUILD_ON_HOST).
-int build_blas_host(GkrtContext* ctx) {
+int build_blas_host(GkrtContext* ctx, cudaStream_t st) {
     const uint32_t nm = (uint32_t)ctx->meshes.size();
     std::vector<BvhNode> nodes;
     ctx->blas_root.assign(nm, -1);
@@ -305,8 +373,6 @@ int build_blas_host(GkrtContext* ctx) {
         if (nt == 0) continue;
         HostBvh hb;
         build_bvh_host(boxes.data(), nt, 4, (uint32_t)nodes.size(), (uint32_t)(tris.size() / 3), false, hb);
-        if (hb.depth > kStackSize - 24)
-            return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "mesh BVH deeper than the traversal stack allows");
         ctx->blas_root[mi] = hb.root;
         nodes.insert(nodes.end(), hb.nodes.begin(), hb.nodes.end());
         for (uint32_t k = 0; k < nt; ++k) {
@@ -326,11 +392,11 @@ int build_blas_host(GkrtContext* ctx) {
     ctx->d_nodes_cap = 0;
     if ((rc = ensure_node_cap(ctx, nodes.size() + 2 * ctx->inst.size() + 2)) != GKRT_OK) return rc;
     if ((rc = copy_in(ctx, ctx->d_nodes, nodes.data(), nodes.size() * sizeof(BvhNode))) != GKRT_OK) return rc;
-    return finish_blas(ctx);
+    return finish_blas(ctx, st);
 }
 
 int build_blas(GkrtContext* ctx, cudaStream_t st) {
-    return ctx->host_build ? build_blas_host(ctx) : build_blas_gpu(ctx, st);
+    return ctx->host_build ? build_blas_host(ctx, st) : build_blas_gpu(ctx, st);
 }
 
 int build_tlas(GkrtContext* ctx, cudaStream_t st) {
@@ -353,7 +419,6 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
         if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
         GpuBvhResult r;
         GK_CUDA(gpu_bvh_build_instances(ctx->builder, ib.data(), (uint32_t)ib.size(), ctx->d_blas_box, base, &r, st));
-        if (r.depth > 24 + 8) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "instance BVH too deep");
         if ((rc = ensure_node_cap(ctx, (size_t)base + r.node_count)) != GKRT_OK) return rc;
         if (r.node_count)
             GK_CUDA(cudaMemcpyAsync(ctx->d_nodes + base, r.nodes, (size_t)r.node_count * sizeof(BvhNode),
@@ -361,6 +426,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
         GK_CUDA(cudaStreamSynchronize(st));
         ctx->tlas_root = ib.empty() ? -1 : r.root_node[0];
         ctx->tlas_nodes = r.nodes_used;
+        if ((rc = finish_tlas(ctx, r.node_count, st)) != GKRT_OK) return rc;
         ctx->tlas_ready = true;
         return upload_instances(ctx);
     }
@@ -404,12 +470,12 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
                 *r[k] = (int)(~(map[pos] << 3));
             }
     }
-    if (hb.depth > 24 + 8) return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "instance BVH too deep");
     if ((rc = ensure_node_cap(ctx, (size_t)base + hb.nodes.size())) != GKRT_OK) return rc;
     if ((rc = copy_in(ctx, ctx->d_nodes + base, hb.nodes.data(), hb.nodes.size() * sizeof(BvhNode))) != GKRT_OK)
         return rc;
     ctx->tlas_root = map.empty() ? -1 : hb.root;
     ctx->tlas_nodes = (uint32_t)hb.nodes.size();
+    if ((rc = finish_tlas(ctx, (uint32_t)hb.nodes.size(), st)) != GKRT_OK) return rc;
     ctx->tlas_ready = true;
     return upload_instances(ctx);
 }
@@ -449,10 +515,10 @@ int ensure_bvh(GkrtContext* ctx, uint32_t flags, cudaStream_t st) {
 
 SceneView scene_view(GkrtContext* c) {
     SceneView S;
-    S.nodes = c->d_nodes;
+    S.nodes = c->d_wide;
     S.tris = c->d_tris;
     S.inst = c->d_inst;
-    S.tlas_root = c->tlas_root;
+    S.tlas_root = c->tlas_wide_root;
     S.error = c->d_error;
     return S;
 }
@@ -950,6 +1016,8 @@ int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     out->bvh_leaf_tris = ctx->nidx / 3;
     out->emitters = ctx->nemit;
     out->build_launches = gpu_bvh_launches(ctx->builder);
+    out->wide_nodes = ctx->blas_wide_count + ctx->tlas_wide_count;
+    out->wide_depth = (uint32_t)(ctx->blas_wide_depth + ctx->tlas_wide_depth);
     return GKRT_OK;
 }
 

@@ -12,6 +12,7 @@ struct ShadeScene;
 struct PixelImages;
 struct SceneView;
 struct BvhNode;
+struct WideNode;
 
 struct ReprojectArgs {
     int W, H, P;                   // P: row pitch in pixels (a multiple of 4)
@@ -112,6 +113,12 @@ cudaError_t gpu_bvh_build_meshes(GpuBvh* b, const float4* pos, const uint32_t* i
 // Instance-level tree; mesh_box: device, 6 floats per mesh.
 cudaError_t gpu_bvh_build_instances(GpuBvh* b, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
                                     uint32_t node_base, GpuBvhResult* out, cudaStream_t st);
+// Collapse of two-child trees (device array bin, roots: node refs, -1 for none) into the
+// compressed 8-wide nodes the kernels traverse, at out[wide_base ...) of an array of out_cap
+// nodes. wroots: wide root per tree (-1 for none); count: wide nodes written; depth: levels.
+cudaError_t gpu_bvh_collapse(GpuBvh* b, const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base,
+                             WideNode* out, size_t out_cap, std::vector<int>& wroots, uint32_t* count, int* depth,
+                             cudaStream_t st);
 }  // namespace gk
 
 cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,

@@ -246,6 +246,8 @@ typedef struct GkrtStats {
     uint32_t tlas_nodes;
     uint32_t emitters;          /* emissive triangles in the GKRT_NEE_EMISSIVE table      */
     uint32_t build_launches;    /* kernels launched by GPU BVH builds since creation      */
+    uint32_t wide_nodes;        /* compressed 8-wide nodes traversed (mesh + instance)    */
+    uint32_t wide_depth;        /* wide levels, deepest mesh tree + instance tree         */
 } GkrtStats;
 
 typedef struct GkrtContext GkrtContext;
