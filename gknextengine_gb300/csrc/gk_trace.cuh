@@ -1,10 +1,16 @@
 // gk_trace.cuh — two-level BVH traversal with an exact closest-hit contract (sm_103a).
 //
 // Replaces the RT-core RayQuery of FHardwareRayTracerV2 (assets/shaders/common/
-// Shading.slang:737-826). GB300 has no RT cores, so traversal is software over compressed
-// 8-wide nodes (96 bytes: six 16-byte vector loads test eight child boxes), 48-byte
-// triangles in leaf order, a per-thread stack of node groups in shared memory (strided by
-// the block size, conflict-free) and a marker entry for the hand-over from the instance
+// Shading.slang:737-826). GB300 has no RT cores, so traversal is software, over either of
+// the two node formats the builders produce from the same SAH trees:
+//   * two-child nodes (64 bytes, four 16-byte loads per node, a stack of node refs): used by
+//     the rt pass, whose per-pixel megakernel interleaves shading with traversal and runs
+//     fastest with the short node step;
+//   * compressed 8-wide nodes (96 bytes, six loads test eight 8-bit child boxes, a stack of
+//     sorted node groups): used by the ray-query kernels, where traversal runs alone and the
+//     wide nodes halve the node steps of incoherent rays.
+// Both keep 48-byte triangles in leaf order, a per-thread stack in shared memory (strided
+// by the block size, conflict-free) and a marker entry for the hand-over from the instance
 // level to the mesh level.
 //
 // Hit contract. The reported hit is the minimum of (t, instance index, primitive index)
@@ -52,18 +58,20 @@ struct __align__(16) WideNode {
 
 struct __align__(16) DevInst {
     float winv[12];       // world -> object rows
-    int blas_root;        // root WideNode index of the mesh BVH
+    int blas_root;        // root BvhNode index of the mesh BVH
     uint32_t index_offset;
     uint32_t vertex_offset;
     uint32_t instance_id;
+    int blas_wide_root;   // root WideNode index of the mesh BVH
+    uint32_t pad[3];
 };
 
 // Node boxes as stored: 1e-6 relative plus 1e-10 absolute beyond the primitives' bounds.
 GK_HD float widen_lo(float v) { return v - (fabsf(v) * 1e-6f + 1e-10f); }
 GK_HD float widen_hi(float v) { return v + (fabsf(v) * 1e-6f + 1e-10f); }
 
-constexpr int kStackEntries = 24;                // node-group entries per thread
-constexpr int kStackSize = 3 * kStackEntries;    // 32-bit words per thread
+constexpr int kStackEntries = 24;                // wide node-group entries per thread (3 words each)
+constexpr int kStackSize = 3 * kStackEntries;    // 32-bit words per thread; two-child refs: one word each
 constexpr int kRefPop = 0x7FFFFFFE;
 constexpr int kRefMarker = 0x7FFFFFFF;
 constexpr int kIterCap = 1 << 22;
@@ -78,10 +86,12 @@ struct Counters {
 };
 
 struct SceneView {
-    const WideNode* nodes;
+    const BvhNode* nodes;   // two-child nodes
+    const WideNode* wide;   // the same trees collapsed into 8-wide nodes
     const float4* tris;     // 3 float4 per triangle, v0.w = primitive index bits
     const DevInst* inst;
-    int tlas_root;          // -1: empty scene
+    int tlas_root;          // two-child root of the instance level, -1: empty scene
+    int tlas_wide_root;     // wide root of the instance level
     uint32_t* error;
 };
 
@@ -251,6 +261,18 @@ GK_D f3 safe_inv(f3 d) {
     return F3(rcp_(x), rcp_(y), rcp_(z));
 }
 
+// Slab test widened by 1e-6 relative; tcull already carries the same widening.
+GK_D bool slab(float lx, float ly, float lz, float hx, float hy, float hz, f3 o, f3 inv, float tmin, float tcull,
+               float& tnear) {
+    float t0x = (lx - o.x) * inv.x, t1x = (hx - o.x) * inv.x;
+    float t0y = (ly - o.y) * inv.y, t1y = (hy - o.y) * inv.y;
+    float t0z = (lz - o.z) * inv.z, t1z = (hz - o.z) * inv.z;
+    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z)) * 1.000001f;
+    tnear = tn;
+    return tn <= fminf(tf, tcull);
+}
+
 struct TraceOut {
     bool hit;
     bool ambiguous;
@@ -284,6 +306,7 @@ struct Trav {
 
 constexpr float kTmin = 1e-3f;   // EPS, assets/shaders/common/PreProcessor.slang:13
 
+template <bool kWide = false>
 GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int mode) {
     T.wo = wo; T.wd = wd; T.o = wo; T.d = wd;
     T.inv = safe_inv(wd);
@@ -296,8 +319,8 @@ GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int m
     T.mode = mode;
     T.hit = false; T.best_exact = false; T.inblas = false; T.ambiguous = false;
     T.has_leaf = false; T.leaf = 0u;
-    T.ref = S.tlas_root;
-    T.done = S.tlas_root < 0;
+    T.ref = kWide ? S.tlas_wide_root : S.tlas_root;
+    T.done = T.ref < 0;
 }
 
 // FP64 t of the current best candidate: its triangle against its instance's
@@ -409,6 +432,76 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
     return false;
 }
 
+// Node phase over two-child nodes ("while-while", Aila and Laine, HPG 2009): interior
+// nodes, stack pops, returns to the instance level and instance entries.
+// The first triangle leaf found is postponed into T.leaf and the lane keeps traversing;
+// a second leaf, or leaving the instance the postponed leaf belongs to, makes the lane wait
+// for the leaf phase. Returns true while the lane can take another node step.
+GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn) {
+    if (++T.iter > kIterCap) { atomicOr(S.error, kErrIter); T.done = true; return false; }
+    const int ref = T.ref;
+    if (ref == kRefPop) {
+        if (T.sp == 0) { T.done = true; return false; }
+        --T.sp;
+        T.ref = (int)stk[T.sp * stride];
+        return true;
+    }
+    if (ref == kRefMarker) {
+        if (T.has_leaf) return false;   // the postponed leaf needs this instance's ray
+        T.o = T.wo; T.d = T.wd; T.inv = safe_inv(T.wd);
+        T.inblas = false;
+        T.ref = kRefPop;
+        return true;
+    }
+    if (ref >= 0) {
+        ++cn.nodes;
+        const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
+        const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+        const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
+        float tn0, tn1;
+        const bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, T.o, T.inv, kTmin, T.tcull, tn0);
+        const bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, T.o, T.inv, kTmin, T.tcull, tn1);
+        if (h0 && h1) {
+            int nearr = nd.x, farr = nd.y;
+            if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
+            if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return false; }
+            stk[T.sp * stride] = (uint32_t)farr;
+            ++T.sp;
+            T.ref = nearr;
+        } else if (h0) {
+            T.ref = nd.x;
+        } else if (h1) {
+            T.ref = nd.y;
+        } else {
+            T.ref = kRefPop;
+        }
+        return true;
+    }
+    const uint32_t payload = ~(uint32_t)ref;
+    if (!T.inblas) {
+        T.cur = payload >> 3;
+        const DevInst* ip = S.inst + T.cur;
+        float w[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) w[k] = __ldg(&ip->winv[k]);
+        T.o = xpoint(w, T.wo);
+        T.d = xvector(w, T.wd);
+        T.inv = safe_inv(T.d);
+        T.sh = make_shear(T.d);
+        if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return false; }
+        stk[T.sp * stride] = (uint32_t)kRefMarker;
+        ++T.sp;
+        T.inblas = true;
+        T.ref = __ldg(&ip->blas_root);
+        return true;
+    }
+    if (T.has_leaf) return false;       // one postponed leaf at a time
+    T.leaf = payload;
+    T.has_leaf = true;
+    T.ref = kRefPop;
+    return kSpeculative;
+}
+
 // t of byte `b` of `word` (a WideNode plane): fma(2^23 + q, C, B').
 GK_D float wide_t(uint32_t word, int b, float C, float Bp) {
     return fmaf_(__uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u + (uint32_t)b)), C, Bp);
@@ -434,7 +527,7 @@ GK_D void trav_to_world(Trav& T) {
 // the same instructions. A triangle leaf is postponed into T.leaf and the lane waits for the
 // leaf phase; so does a lane about to leave the instance of its postponed leaf. Returns true
 // while the lane can take another node step.
-GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn) {
+GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn) {
     if (++T.iter > kIterCap) { atomicOr(S.error, kErrIter); T.done = true; return false; }
     int ref = T.ref;
     if (ref == kRefMarker) {            // hand-back deferred until the postponed leaf was tested
@@ -458,13 +551,13 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
             const uint32_t c = w & 7u, slot = (w >> 3) & 7u;
             if (c <= 1u) --T.sp;
             else e[stride] = ((w >> 3) & ~7u) | (c - 1u);
-            ref = __ldg(reinterpret_cast<const int*>(S.nodes + node) + 16 + slot);
+            ref = __ldg(reinterpret_cast<const int*>(S.wide + node) + 16 + slot);
             break;
         }
     }
     if (ref >= 0) {
         ++cn.nodes;
-        const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
+        const float4* np = reinterpret_cast<const float4*>(S.wide + ref);
         const float4 h = __ldg(np);
         const uint4 qx = __ldg(reinterpret_cast<const uint4*>(np + 1));
         const uint4 qy = __ldg(reinterpret_cast<const uint4*>(np + 2));
@@ -546,7 +639,7 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         e[2 * stride] = 0u;
         ++T.sp;
         T.inblas = true;
-        T.ref = __ldg(&ip->blas_root);
+        T.ref = __ldg(&ip->blas_wide_root);
         return true;
     }
     if (T.has_leaf) {                   // one postponed leaf at a time
@@ -569,14 +662,19 @@ GK_D void trav_leaf_step(Trav& T, const SceneView& S, Counters& cn) {
 GK_D bool trav_finished(const Trav& T) { return T.done && !T.has_leaf; }
 
 // Whole-ray traversal on top of the two phases.
-template <int MODE>
+template <int MODE, bool kWide = false>
 GK_D TraceOut traverse(const SceneView& S, f3 wo, f3 wd, float tmin, float tmax, uint32_t* stk, int stride,
                        Counters& cn) {
     (void)tmin;
     Trav T;
-    trav_init(T, S, wo, wd, tmax, MODE);
+    trav_init<kWide>(T, S, wo, wd, tmax, MODE);
     while (!trav_finished(T)) {
-        while (!T.done && trav_node_step(T, S, stk, stride, cn)) {
+        if (kWide) {
+            while (!T.done && trav_node_step_wide(T, S, stk, stride, cn)) {
+            }
+        } else {
+            while (!T.done && trav_node_step(T, S, stk, stride, cn)) {
+            }
         }
         trav_leaf_step(T, S, cn);
     }

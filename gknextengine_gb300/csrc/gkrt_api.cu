@@ -71,6 +71,7 @@ struct GkrtContext {
     std::vector<int> blas_wide_root;
     uint32_t blas_wide_count = 0, tlas_wide_count = 0;
     int blas_wide_depth = 0, tlas_wide_depth = 0, tlas_wide_root = -1;
+    int blas_bin_depth = 0, tlas_bin_depth = 0;   // two-child levels (root = 0)
     bool blas_ready = false, tlas_ready = false;
     uint32_t inst_cap = 0;            // instance arrays allocated for this many instances
 
@@ -148,6 +149,7 @@ void free_scene(GkrtContext* c) {
     c->blas_wide_root.clear();
     c->blas_wide_count = c->tlas_wide_count = 0;
     c->blas_wide_depth = c->tlas_wide_depth = 0;
+    c->blas_bin_depth = c->tlas_bin_depth = 0;
     c->tlas_wide_root = -1;
     c->inst_cap = 0;
     c->has_scene = false;
@@ -211,7 +213,9 @@ int upload_instances(GkrtContext* ctx) {
         std::memcpy(&prev[12 * (size_t)i], s.combined_prev, 48);
         std::memcpy(di[i].winv, s.world_inv, 48);
         const GkrtMesh& m = ctx->meshes[s.mesh_id];
-        di[i].blas_root = ctx->blas_ready ? ctx->blas_wide_root[s.mesh_id] : -1;
+        di[i].blas_root = ctx->blas_ready ? ctx->blas_root[s.mesh_id] : -1;
+        di[i].blas_wide_root = ctx->blas_ready ? ctx->blas_wide_root[s.mesh_id] : -1;
+        di[i].pad[0] = di[i].pad[1] = di[i].pad[2] = 0u;
         di[i].index_offset = m.index_offset;
         di[i].vertex_offset = m.vertex_offset;
         di[i].instance_id = s.instance_id;
@@ -271,8 +275,13 @@ int ensure_wide_cap(GkrtContext* ctx, size_t total, size_t keep) {
     return GKRT_OK;
 }
 
-// Group-stack entries a ray can need: one per wide level of each tree plus the marker.
+// Stack a ray can need: two-child traversal pushes at most one ref per level of each tree
+// plus the marker; wide traversal one group per wide level plus the marker.
 int check_stack_bound(GkrtContext* ctx) {
+    if (ctx->blas_bin_depth + ctx->tlas_bin_depth + 3 > kStackSize)
+        return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "BVH deeper than the traversal stack allows (" +
+                                                    std::to_string(ctx->blas_bin_depth) + " mesh + " +
+                                                    std::to_string(ctx->tlas_bin_depth) + " instance levels)");
     if (ctx->blas_wide_depth + ctx->tlas_wide_depth + 1 > kStackEntries)
         return fail(ctx, GKRT_ERR_DEVICE_LIMIT, "BVH deeper than the traversal stack allows (" +
                                                     std::to_string(ctx->blas_wide_depth) + " mesh + " +
@@ -295,6 +304,7 @@ int finish_blas(GkrtContext* ctx, cudaStream_t st) {
         return fail(ctx, GKRT_ERR_INVALID_ARG, "mesh BVH collapse failed (non-finite geometry or depth > 64)");
     if (e != cudaSuccess) return cuda_fail(ctx, e, "gpu_bvh_collapse(mesh level)");
     ctx->tlas_wide_depth = 0;
+    ctx->tlas_bin_depth = 0;
     if ((rc = check_stack_bound(ctx)) != GKRT_OK) return rc;
     ctx->blas_ready = true;
     ctx->tlas_ready = false;
@@ -332,6 +342,7 @@ int build_blas_gpu(GkrtContext* ctx, cudaStream_t st) {
     GpuBvhResult r;
     GK_CUDA(gpu_bvh_build_meshes(ctx->builder, ctx->d_pos, ctx->d_idx, ctx->meshes.data(), nm, 0, ctx->d_tris, &r, st));
     ctx->blas_root = r.root_node;
+    ctx->blas_bin_depth = r.depth;
     if (nm) GK_CUDA(cudaMemcpy(ctx->blas_box.data(), r.root_box, 6 * (size_t)nm * 4, cudaMemcpyDeviceToHost));
     ctx->blas_node_count = r.node_count;
     ctx->blas_nodes_used = r.nodes_used;
@@ -346,6 +357,7 @@ int build_blas_gpu(GkrtContext* ctx, cudaStream_t st) {
 // Mesh-level trees on the host (GKRT_BUILD_ON_HOST).
 int build_blas_host(GkrtContext* ctx, cudaStream_t st) {
     const uint32_t nm = (uint32_t)ctx->meshes.size();
+    ctx->blas_bin_depth = 0;
     std::vector<BvhNode> nodes;
     ctx->blas_root.assign(nm, -1);
     ctx->blas_box.assign(6 * (size_t)nm, 0.0f);
@@ -374,6 +386,7 @@ int build_blas_host(GkrtContext* ctx, cudaStream_t st) {
         HostBvh hb;
         build_bvh_host(boxes.data(), nt, 4, (uint32_t)nodes.size(), (uint32_t)(tris.size() / 3), false, hb);
         ctx->blas_root[mi] = hb.root;
+        ctx->blas_bin_depth = std::max(ctx->blas_bin_depth, hb.depth);
         nodes.insert(nodes.end(), hb.nodes.begin(), hb.nodes.end());
         for (uint32_t k = 0; k < nt; ++k) {
             const uint32_t prim = hb.order[k];
@@ -426,6 +439,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
         GK_CUDA(cudaStreamSynchronize(st));
         ctx->tlas_root = ib.empty() ? -1 : r.root_node[0];
         ctx->tlas_nodes = r.nodes_used;
+        ctx->tlas_bin_depth = r.depth;
         if ((rc = finish_tlas(ctx, r.node_count, st)) != GKRT_OK) return rc;
         ctx->tlas_ready = true;
         return upload_instances(ctx);
@@ -475,6 +489,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
         return rc;
     ctx->tlas_root = map.empty() ? -1 : hb.root;
     ctx->tlas_nodes = (uint32_t)hb.nodes.size();
+    ctx->tlas_bin_depth = hb.depth;
     if ((rc = finish_tlas(ctx, (uint32_t)hb.nodes.size(), st)) != GKRT_OK) return rc;
     ctx->tlas_ready = true;
     return upload_instances(ctx);
@@ -515,10 +530,12 @@ int ensure_bvh(GkrtContext* ctx, uint32_t flags, cudaStream_t st) {
 
 SceneView scene_view(GkrtContext* c) {
     SceneView S;
-    S.nodes = c->d_wide;
+    S.nodes = c->d_nodes;
+    S.wide = c->d_wide;
     S.tris = c->d_tris;
     S.inst = c->d_inst;
-    S.tlas_root = c->tlas_wide_root;
+    S.tlas_root = c->tlas_root;
+    S.tlas_wide_root = c->tlas_wide_root;
     S.error = c->d_error;
     return S;
 }

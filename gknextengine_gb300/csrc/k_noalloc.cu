@@ -52,8 +52,8 @@ __global__ void __launch_bounds__(kNaThreads) k_trace_rays_noalloc(SceneView S, 
         h.pad[0] = h.pad[1] = h.pad[2] = 0u;
         cn.rays = 1;
         const TraceOut t = mode == GKRT_TRACE_ANY
-                               ? traverse<kAny>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kNaThreads, cn)
-                               : traverse<kClosest>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kNaThreads, cn);
+                               ? traverse<kAny, true>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kNaThreads, cn)
+                               : traverse<kClosest, true>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kNaThreads, cn);
         if (t.hit) {
             const HitShade s = hit_shade(S, o, d, t.inst, t.tri);
             h.t = s.t; h.inst = t.inst; h.prim = t.prim;

@@ -447,8 +447,8 @@ __global__ void __launch_bounds__(kRqThreads) k_trace_rays(SceneView S, const Gk
         cn.rays = 1;
         // tmin of the query is fixed at EPS like the reference's TraceRay/TraceOcclusion
         const TraceOut t = mode == GKRT_TRACE_ANY
-                               ? traverse<kAny>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn)
-                               : traverse<kClosest>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn);
+                               ? traverse<kAny, true>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn)
+                               : traverse<kClosest, true>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn);
         if (t.hit) {
             const HitShade s = hit_shade(S, o, d, t.inst, t.tri);
             h.t = s.t; h.inst = t.inst; h.prim = t.prim;
