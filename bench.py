@@ -404,12 +404,33 @@ def run_gkrt(args):
     barrier()
     e2e_value = e2e_rays / e2e_s / 1e6
 
+    # ---- probe grid (after the timed frames: a baked grid changes path termination) ----
+    probe_ms = None
+    if WORKLOAD == "bricks" and rank == 0:
+        e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+        r.probe_voxelize(stream)
+        r.probe_bake(fcs[0], 0, None, stream)
+        r.synchronize(stream)
+        per = (r.PROBE_COUNT // 64) // 120
+        with torch.cuda.stream(stream):
+            e0.record()
+            r.probe_voxelize(stream)
+            e1.record()
+            r.probe_bake_slice(fcs[0], 7, 120, stream)
+            e2.record()
+            r.probe_bake(fcs[0], 0, None, stream)
+            e3.record()
+        r.synchronize(stream)
+        probe_ms = {"voxelize_grid": e0.elapsed_time(e1), "bake_slice_f120": e1.elapsed_time(e2),
+                    "bake_grid": e2.elapsed_time(e3), "slice_probes": per * 64, "grid_probes": r.PROBE_COUNT}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
                 "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic", "config": workload_config(),
                 "ms_per_frame": ms_total / K, "trace_ms": trace_avg_ms, "rays_per_frame": rays / max(K, 1) / world,
                 "gpu_launches": 3 * K + 2 * K * (fcs[0].denoiser == abi.DENOISE_ATROUS) + build_launches,
+                "probe_ms": probe_ms,
                 "bvh_build_ms": {"all_levels": build_all_ms, "instance_level": build_inst_ms,
                                  "scene_load_s": load_s, "triangles": int(sc.triangle_count),
                                  "instances": int(sc.instances.shape[0])},

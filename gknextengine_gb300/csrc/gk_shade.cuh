@@ -83,6 +83,19 @@ GK_D f4 sky(const GkrtFrameConstants& fc) {
 }
 
 // ---- probes (AmbientCube.slang:71-78, 178-223, 290-382) ----
+// Grid: CUBE_SIZE_XY x CUBE_SIZE_Z x CUBE_SIZE_XY probes, CUBE_UNIT apart from CUBE_OFFSET
+// (AmbientCube.slang:12-15); index y * 192 * 192 + z * 192 + x.
+constexpr int kProbeXY = 192, kProbeZ = 48;
+constexpr float kProbeOffX = -24.0f, kProbeOffY = -0.34375f, kProbeOffZ = -24.0f;
+
+// Light 0 of the scene as the probe bake uses it (FaceTask, AmbientCube.slang:528-537):
+// the centre lerp(p1, p3, 0.5) of the quad, the power (its material's diffuse) and the area.
+struct ProbeLight {
+    f3 pos;
+    f4 power;
+    float area;
+    int valid;
+};
 GK_D f4 unpack10(uint32_t p) {
     float r = div_((float)(p & 0x3FFu), 1023.0f), g = div_((float)((p >> 10) & 0x3FFu), 1023.0f),
           b = div_((float)((p >> 20) & 0x3FFu), 1023.0f);

@@ -48,8 +48,10 @@ struct GkrtContext {
     uint32_t* d_inst_mat = nullptr;
     float* d_inst_prev = nullptr;
     DevInst* d_inst = nullptr;
-    uint32_t* d_cubes = nullptr;
+    uint32_t* d_cubes = nullptr;                // probe grid (uploaded, or made by gkrt_probe_voxelize)
     uint32_t* d_voxels = nullptr;
+    uint32_t* d_cubes_prev = nullptr;           // snapshot the bake interpolates from
+    std::vector<GkrtLight> lights_host;
 
     // acceleration structures: d_nodes holds the builders' two-child mesh-level nodes
     // [0, blas_node_count) and the instance-level nodes after them; d_wide holds their
@@ -141,6 +143,8 @@ void free_images(GkrtContext* c) {
 void free_scene(GkrtContext* c) {
     dfree(c->d_pos); dfree(c->d_nrm); dfree(c->d_slot); dfree(c->d_idx); dfree(c->d_mat);
     dfree(c->d_inst_mat); dfree(c->d_inst_prev); dfree(c->d_inst); dfree(c->d_cubes); dfree(c->d_voxels);
+    dfree(c->d_cubes_prev);
+    c->lights_host.clear();
     dfree(c->d_nodes); dfree(c->d_wide); dfree(c->d_tris); dfree(c->d_blas_box); dfree(c->d_emit); dfree(c->d_emit_alias);
     c->nemit = c->emit_cap = 0;
     c->mat_host.clear(); c->slot_tris.clear();
@@ -760,6 +764,7 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
     ctx->nidx = d->index_count;
     ctx->nmat = d->material_count;
     ctx->mat_host.assign(d->materials, d->materials + d->material_count);
+    if (d->light_count) ctx->lights_host.assign(d->lights, d->lights + d->light_count);
     mesh_slot_triangles(d->meshes, d->mesh_count, d->indices, d->material_slots, ctx->slot_tris);
     if ((rc = upload(ctx, ctx->d_pos, d->positions, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
     if ((rc = upload(ctx, ctx->d_nrm, d->normals, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
@@ -1009,6 +1014,71 @@ int gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32
     if (rc != GKRT_OK) return rc;
     GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
     GK_CUDA(gkrt_launch_trace_rays(scene_view(ctx), rays, hits, count, mode, ctx->d_counters, st));
+    return GKRT_OK;
+}
+
+// ---- ambient-cube probe grid ----
+
+namespace {
+constexpr size_t kProbeCount = (size_t)kProbeXY * kProbeXY * kProbeZ;
+}
+
+int gkrt_probe_voxelize(GkrtContext* ctx, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = ensure_bvh(ctx, 0, st);
+    if (rc != GKRT_OK) return rc;
+    if (!ctx->d_cubes) GK_CUDA(cudaMalloc((void**)&ctx->d_cubes, kProbeCount * 14 * sizeof(uint32_t)));
+    if (!ctx->d_voxels) GK_CUDA(cudaMalloc((void**)&ctx->d_voxels, kProbeCount * 4 * sizeof(uint32_t)));
+    GK_CUDA(cudaMemsetAsync(ctx->d_cubes, 0, kProbeCount * 14 * sizeof(uint32_t), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(gkrt_launch_probe_voxelize(shade_scene(ctx), 0, (uint32_t)kProbeCount, (uint4*)ctx->d_voxels,
+                                       ctx->d_counters, st));
+    return GKRT_OK;
+}
+
+int gkrt_probe_bake(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t first, uint32_t count, void* stream) {
+    if (!ctx || !fc) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    if (!ctx->d_cubes || !ctx->d_voxels)
+        return fail(ctx, GKRT_ERR_STATE, "no probe grid: upload one or call gkrt_probe_voxelize");
+    if ((size_t)first + count > kProbeCount) return fail(ctx, GKRT_ERR_INVALID_ARG, "probe range outside the grid");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = ensure_bvh(ctx, 0, st);
+    if (rc != GKRT_OK) return rc;
+    if (!ctx->d_cubes_prev) GK_CUDA(cudaMalloc((void**)&ctx->d_cubes_prev, kProbeCount * 14 * sizeof(uint32_t)));
+    GK_CUDA(cudaMemcpyAsync(ctx->d_cubes_prev, ctx->d_cubes, kProbeCount * 14 * sizeof(uint32_t),
+                            cudaMemcpyDeviceToDevice, st));
+    ProbeLight lt;
+    std::memset(&lt, 0, sizeof(lt));
+    if (!ctx->lights_host.empty()) {
+        const GkrtLight& L = ctx->lights_host[0];
+        if (L.light_mat_idx >= ctx->nmat) return fail(ctx, GKRT_ERR_INVALID_ARG, "light 0 has no material");
+        // lerp(p1, p3, 0.5) as p1 + (p3 - p1) 0.5, one rounding per step
+        lt.pos.x = std::fmaf(0.5f, L.p3[0] - L.p1[0], L.p1[0]);
+        lt.pos.y = std::fmaf(0.5f, L.p3[1] - L.p1[1], L.p1[1]);
+        lt.pos.z = std::fmaf(0.5f, L.p3[2] - L.p1[2], L.p1[2]);
+        const float* dif = ctx->mat_host[L.light_mat_idx].diffuse;
+        lt.power.x = dif[0]; lt.power.y = dif[1]; lt.power.z = dif[2]; lt.power.w = dif[3];
+        lt.area = L.normal_area[3];
+        lt.valid = 1;
+    }
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(gkrt_launch_probe_bake(shade_scene(ctx), *fc, lt, first, count, ctx->d_cubes_prev, ctx->d_cubes,
+                                   (uint4*)ctx->d_voxels, ctx->d_counters, st));
+    return GKRT_OK;
+}
+
+int gkrt_probe_download(GkrtContext* ctx, uint32_t* cubes, uint32_t* voxels) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->d_cubes || !ctx->d_voxels) return fail(ctx, GKRT_ERR_STATE, "no probe grid");
+    cudaSetDevice(ctx->device);
+    GK_CUDA(cudaDeviceSynchronize());
+    if (cubes) GK_CUDA(cudaMemcpy(cubes, ctx->d_cubes, kProbeCount * 14 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (voxels) GK_CUDA(cudaMemcpy(voxels, ctx->d_voxels, kProbeCount * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return GKRT_OK;
 }
 

@@ -13,6 +13,7 @@ struct PixelImages;
 struct SceneView;
 struct BvhNode;
 struct WideNode;
+struct ProbeLight;
 
 struct ReprojectArgs {
     int W, H, P;                   // P: row pitch in pixels (a multiple of 4)
@@ -124,6 +125,13 @@ cudaError_t gpu_bvh_collapse(GpuBvh* b, const BvhNode* bin, const std::vector<in
 cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,
                                    const gk::PixelImages& im, unsigned long long* counters, unsigned int* work,
                                    int num_sms, cudaStream_t st);
+// Probe grid (k_probes.cu): voxel distance data of probes [first, first + count), and one bake
+// step of those probes reading neighbours from cubes_prev (a snapshot of cubes).
+cudaError_t gkrt_launch_probe_voxelize(const gk::ShadeScene& sc, uint32_t first, uint32_t count, uint4* voxels,
+                                       unsigned long long* counters, cudaStream_t st);
+cudaError_t gkrt_launch_probe_bake(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, const gk::ProbeLight& lt,
+                                   uint32_t first, uint32_t count, const uint32_t* cubes_prev, uint32_t* cubes,
+                                   uint4* voxels, unsigned long long* counters, cudaStream_t st);
 cudaError_t gkrt_launch_trace_rays(const gk::SceneView& S, const GkrtRay* rays, GkrtHit* hits, uint32_t n,
                                    uint32_t mode, unsigned long long* counters, cudaStream_t st);
 // Internal helpers for entry points defined outside gkrt_api.cu.

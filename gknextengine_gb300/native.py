@@ -50,6 +50,9 @@ def load(path: str | None = None):
     L.gkrt_trace_rays.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_trace_rays_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
+    L.gkrt_probe_voxelize.argtypes = [vp, vp]
+    L.gkrt_probe_bake.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, C.c_uint32, vp]
+    L.gkrt_probe_download.argtypes = [vp, vp, vp]
     L.gkrt_synchronize.argtypes = [vp, vp]
     L.gkrt_affine_inverse.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.gkrt_conv3x3_bf16.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp,
@@ -79,7 +82,7 @@ EXPORTED = [
     "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_build_bvh",
     "gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_end_frame", "gkrt_render_frame",
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
-    "gkrt_get_stats",
+    "gkrt_get_stats", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",
     "gkrt_synchronize", "gkrt_affine_inverse",
     "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16", "gkrt_conv3x3_wgrad_bf16",
     "gkrt_unet_init", "gkrt_unet_param_count", "gkrt_unet_get_params", "gkrt_unet_set_params", "gkrt_unet_forward",

@@ -137,6 +137,32 @@ class PathTracingRenderer:
         self._check(self._lib.gkrt_trace_rays(self._h, C.c_void_p(rays_ptr), C.c_void_p(hits_ptr), count, mode,
                                               self._stream(stream)))
 
+    # ---- ambient-cube probe grid (AmbientCube.slang; see gkrt.h) ----
+    PROBE_COUNT = 192 * 192 * 48
+
+    def probe_voxelize(self, stream=None):
+        """Distance data of every probe (the reference's CPU voxelizer, on the GPU)."""
+        self._check(self._lib.gkrt_probe_voxelize(self._h, self._stream(stream)))
+
+    def probe_bake(self, fc, first: int = 0, count: int | None = None, stream=None):
+        """One bake step of probes [first, first + count)."""
+        if count is None:
+            count = self.PROBE_COUNT - first
+        self._check(self._lib.gkrt_probe_bake(self._h, C.byref(fc), first, count, self._stream(stream)))
+
+    def probe_bake_slice(self, fc, frame: int, temporal_frames: int = 120, stream=None):
+        """The reference's per-frame schedule (RayTraceBaseRenderer::PostRender): slice
+        frame % F of (27648 // F) groups of 64 probes."""
+        per = (self.PROBE_COUNT // 64) // temporal_frames
+        self.probe_bake(fc, (frame % temporal_frames) * per * 64, per * 64, stream)
+
+    def probe_download(self):
+        """(cubes (N, 14) uint32, voxels (N, 4) uint32) of the whole grid."""
+        cubes = np.zeros((self.PROBE_COUNT, 14), np.uint32)
+        vox = np.zeros((self.PROBE_COUNT, 4), np.uint32)
+        self._check(self._lib.gkrt_probe_download(self._h, cubes.ctypes.data, vox.ctypes.data))
+        return cubes, vox
+
     def trace_rays_noalloc_device(self, rays_ptr: int, hits_ptr: int, count: int, mode=abi.TRACE_CLOSEST,
                                   stream=None):
         """Ray queries that allocate no device memory (static scratch; see gkrt.h)."""

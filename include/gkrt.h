@@ -312,6 +312,28 @@ int  gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint3
 int  gkrt_trace_rays_noalloc(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32_t count,
                              uint32_t mode, void* stream);
 
+/* Ambient-cube probe grid (AmbientCube.slang:12-15: 192 x 48 x 192 probes, 0.25 m apart from
+ * (-24, -0.34375, -24); index y*192*192 + z*192 + x; 14 u32 per AmbientCube, 4 u32 per
+ * VoxelData), read by the rt pass's path termination.
+ *
+ * gkrt_probe_voxelize: the distance data of every probe, computed on the GPU the way the
+ * reference's CPU voxelizer computes it (VoxelizeCube, src/Assets/CPUAccelerationStructure.cpp:
+ * 112-160: six axis rays of 16 m, diagonal rays in open space; a hit within 0.25 m on a back
+ * face or an emitter marks the probe solid). Creates the grid when the scene had none, clears
+ * the colours and resets the ages.
+ *
+ * gkrt_probe_bake: one bake step of probes [first, first + count) (the hw-lightbake dispatch
+ * of RayTraceBaseRenderer::PostRender, RayTraceBaseRenderer.cpp:225-274, running
+ * RenderAmbientCubeOnly, AmbientCube.slang:656-690): probes within 2 m of a surface trace 16
+ * jittered rays per face, add sky, light 0 and sun, and blend into their colours with weight
+ * 1/8. The reference's schedule bakes slice (frame % F) of size (27648 / F) * 64 with F = 30,
+ * 120 or 300. Neighbour probes are read as they were before the call.
+ *
+ * gkrt_probe_download: the grid to host memory (either pointer may be NULL); synchronous. */
+int  gkrt_probe_voxelize(GkrtContext* ctx, void* stream);
+int  gkrt_probe_bake(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t first, uint32_t count, void* stream);
+int  gkrt_probe_download(GkrtContext* ctx, uint32_t* cubes, uint32_t* voxels);
+
 /* Differentiable rendering (no counterpart in the reference): the pass's estimator with
  * `spp` samples per pixel from the primary hit, composed as the compose pass composes it
  * (diffuse x primary albedo + specular, no filter), and its path-replay adjoint.

@@ -1277,6 +1277,243 @@ void adjoint_pixel(const OScene& S, const GkrtFrameConstants& fc, int W, int H, 
 }
 }  // namespace
 
+// ---- ambient-cube probe grid: voxelization and bake (test restatement of k_probes.cu) ----
+// VoxelizeCube (src/Assets/CPUAccelerationStructure.cpp:70-160) and FGpuProbeGenerator::
+// RenderAmbientCubeOnly / FaceTask (assets/shaders/common/AmbientCube.slang:477-553, 656-690).
+
+struct ProbeHitO {
+    bool hit = false, back = false;
+    float t = 0.0f;
+    uint32_t mat = 0;
+    Vtx v;
+};
+
+f3 probe_origin(uint32_t g) {
+    uint32_t y = g / (uint32_t)(kCubeXY * kCubeXY);
+    uint32_t z = (g - y * (uint32_t)(kCubeXY * kCubeXY)) / (uint32_t)kCubeXY;
+    uint32_t x = g - y * (uint32_t)(kCubeXY * kCubeXY) - z * (uint32_t)kCubeXY;
+    return f3{(float)x * kCubeUnit + kCubeOff[0], (float)y * kCubeUnit + kCubeOff[1], (float)z * kCubeUnit + kCubeOff[2]};
+}
+
+f3 face_basis(int f) {   // +Y, -Y, +X, -X, +Z, -Z
+    float s = (f & 1) ? -1.0f : 1.0f;
+    return f < 2 ? f3{0.0f, s, 0.0f} : (f < 4 ? f3{s, 0.0f, 0.0f} : f3{0.0f, 0.0f, s});
+}
+
+// Closest hit over [EPS, tmax] with its float t, material, back-face flag (object-space face
+// normal cross(v1 - v0, v2 - v1) against the object-space direction) and shading vertex.
+ProbeHitO probe_hit(const OScene& S, f3 o, f3 d, float tmax) {
+    ProbeHitO r;
+    HitRec h = trace(S, o, d, kEPS, tmax, false, false, nullptr);
+    if (!h.hit) return r;
+    r.hit = true;
+    const GkrtInstance& in = S.inst[h.inst];
+    const GkrtMesh& m = S.meshes[in.mesh_id];
+    LocalRay lr = to_object(in, o, d);
+    f3 v0, v1, v2;
+    uint32_t vi[3];
+    tri_verts(S, m, h.prim, v0, v1, v2, vi);
+    HybridHit hh = hybrid_eval(lr.o, lr.s, v0, v1, v2);
+    r.t = hh.t;
+    r.mat = in.mat_id[S.slot[vi[0]] & 15u];
+    f3 a = sub(v1, v0), b = sub(v2, v1);
+    f3 n{fma_(a.y, b.z, -(a.z * b.y)), fma_(a.z, b.x, -(a.x * b.z)), fma_(a.x, b.y, -(a.y * b.x))};
+    r.back = fma_(n.z, lr.d.z, fma_(n.y, lr.d.y, n.x * lr.d.x)) > 0.0f;
+    f3 n0 = S.nrm[vi[0]], n1 = S.nrm[vi[1]], n2 = S.nrm[vi[2]];
+    f3 e1 = sub(n1, n0), e2 = sub(n2, n0);
+    f3 nobj = f3{fma_(e2.x, hh.b2, fma_(e1.x, hh.b1, n0.x)), fma_(e2.y, hh.b2, fma_(e1.y, hh.b1, n0.y)),
+                 fma_(e2.z, hh.b2, fma_(e1.z, hh.b1, n0.z))};
+    r.v.N = normalize3(xform_normal(in.world_inv, nobj));
+    r.v.P = fma3(d, hh.t, o);
+    r.v.mat = r.mat;
+    r.v.inst = h.inst;
+    return r;
+}
+
+void voxelize_probe(const OScene& S, uint32_t g, uint32_t out[4]) {
+    const f3 o = probe_origin(g);
+    uint32_t mat = 0;
+    float dist[6];
+    for (int f = 0; f < 6; ++f) {   // InsideGeometry along +Y, -Y, +X, -X, +Z, -Z
+        dist[f] = 255.0f;
+        ProbeHitO h = probe_hit(S, o, face_basis(f), kCubeUnit * 64.0f);
+        if (!h.hit) continue;
+        dist[f] = h.t;
+        if (h.t <= kCubeUnit) {
+            mat = h.mat;
+            if (h.back || get_mat(S, h.mat).material_model == GKRT_MAT_DIFFUSE_LIGHT) dist[f] = 0.0f;
+        }
+    }
+    float md = fmin_(fmin_(fmin_(fmin_(fmin_(dist[0], dist[1]), dist[2]), dist[3]), dist[4]), dist[5]);
+    if (md > 254.0f) {   // DetectDistance along the six distinct diagonals of the reference's list
+        const float k = 0.577350269f;
+        const int sgn[6][3] = {{1, 1, 1}, {-1, 1, 1}, {-1, -1, 1}, {1, 1, -1}, {-1, 1, -1}, {-1, -1, -1}};
+        for (int q = 0; q < 6; ++q) {
+            f3 d{(float)sgn[q][0] * k, (float)sgn[q][1] * k, (float)sgn[q][2] * k};
+            ProbeHitO h = probe_hit(S, o, d, kCubeUnit * 64.0f);
+            md = fmin_(md, h.hit ? h.t : 255.0f);
+        }
+    }
+    float c[6];
+    for (int f = 0; f < 6; ++f) c[f] = fmin_(fmax_(dist[f] / kCubeUnit, 0.0f), 1.0f);
+    float inside = ((((c[0] * c[1]) * c[2]) * c[3]) * c[4]) * c[5];
+    out[0] = mat;
+    out[1] = 0;
+    out[2] = ((uint32_t)(md / kCubeUnit) & 0xFFu) | (((uint32_t)(inside * 255.0f) & 0xFFu) << 8) |
+             (((uint32_t)(c[4] * 255.0f) & 0xFFu) << 16) | (((uint32_t)(c[5] * 255.0f) & 0xFFu) << 24);
+    out[3] = ((uint32_t)(c[2] * 255.0f) & 0xFFu) | (((uint32_t)(c[3] * 255.0f) & 0xFFu) << 8) |
+             (((uint32_t)(c[0] * 255.0f) & 0xFFu) << 16) | (((uint32_t)(c[1] * 255.0f) & 0xFFu) << 24);
+}
+
+uint32_t pack_rgb10a2(f4 c) {   // AmbientCube.slang:59-69
+    float r = fmin_(fmax_(c.x * 0.001953125f, 0.0f), 1.0f), g = fmin_(fmax_(c.y * 0.001953125f, 0.0f), 1.0f);
+    float b = fmin_(fmax_(c.z * 0.001953125f, 0.0f), 1.0f), a = fmin_(fmax_(c.w * 0.001953125f, 0.0f), 1.0f);
+    return (uint32_t)(r * 1023.0f) | ((uint32_t)(g * 1023.0f) << 10) | ((uint32_t)(b * 1023.0f) << 20) |
+           ((uint32_t)(a * 3.0f) << 30);
+}
+
+f4 sample_cube_di(const uint32_t* cube, f3 n) {   // sampleAmbientCubeHL2_DI, AmbientCube.slang:127-150
+    float wx = fmax_(n.x, 0.0f), wnx = fmax_(-n.x, 0.0f), wy = fmax_(n.y, 0.0f), wny = fmax_(-n.y, 0.0f);
+    float wz = fmax_(n.z, 0.0f), wnz = fmax_(-n.z, 0.0f);
+    float sum = ((((wx + wnx) + wy) + wny) + wz) + wnz;
+    f4 col{0.0f, 0.0f, 0.0f, 0.0f};
+    col = add4(col, scale4(unpack_rgb10a2(cube[10]), wx));
+    col = add4(col, scale4(unpack_rgb10a2(cube[11]), wnx));
+    col = add4(col, scale4(unpack_rgb10a2(cube[8]), wy));
+    col = add4(col, scale4(unpack_rgb10a2(cube[9]), wny));
+    col = add4(col, scale4(unpack_rgb10a2(cube[6]), wz));
+    col = add4(col, scale4(unpack_rgb10a2(cube[7]), wnz));
+    return scale4(col, sum > 0.0f ? 1.0f / sum : 1.0f);
+}
+
+// interpolateAmbientCubesV2<DIAmbientCubeSampler> (AmbientCube.slang:290-382) over given arrays.
+f4 probe_di(const uint32_t* cubes, const uint32_t* voxels, f3 p, f3 n) {
+    float npx = (p.x - kCubeOff[0]) / kCubeUnit, npy = (p.y - kCubeOff[1]) / kCubeUnit,
+          npz = (p.z - kCubeOff[2]) / kCubeUnit;
+    if (!(npx >= 0.0f) || !(npy >= 0.0f) || !(npz >= 0.0f) || npx > (float)(kCubeXY - 2) || npy > (float)(kCubeZ - 2) ||
+        npz > (float)(kCubeXY - 2))
+        return f4{0.0f, 0.0f, 0.0f, 1.0f};
+    float fx = std::floor(npx), fy = std::floor(npy), fz = std::floor(npz);
+    int bx = (int)fx, by = (int)fy, bz = (int)fz;
+    float frx = npx - fx, fry = npy - fy, frz = npz - fz;
+    float tw = 0.0f;
+    f4 res{0.0f, 0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < 8; ++i) {
+        int ox = i & 1, oy = (i >> 1) & 1, oz = (i >> 2) & 1;
+        size_t id = (size_t)(by + oy) * kCubeXY * kCubeXY + (size_t)(bz + oz) * kCubeXY + (size_t)(bx + ox);
+        uint32_t u0 = voxels[id * 4 + 2], u1 = voxels[id * 4 + 3];
+        float d0y = (float)((u0 >> 8) & 0xFFu) / 255.0f;
+        if (d0y < 0.01f) continue;
+        float d0z = (float)((u0 >> 16) & 0xFFu) / 255.0f, d0w = (float)((u0 >> 24) & 0xFFu) / 255.0f;
+        float d1x = (float)(u1 & 0xFFu) / 255.0f, d1y = (float)((u1 >> 8) & 0xFFu) / 255.0f;
+        float d1z = (float)((u1 >> 16) & 0xFFu) / 255.0f, d1w = (float)((u1 >> 24) & 0xFFu) / 255.0f;
+        f3 pl{frx - (float)ox, fry - (float)oy, frz - (float)oz};
+        float dist = length3(pl);
+        f3 dir = normalize3(pl);
+        float hl = std::sqrt(fmax_(dir.x, 0.0f)) * d1x;
+        hl = hl + std::sqrt(fmax_(-dir.x, 0.0f)) * d1y;
+        hl = hl + std::sqrt(fmax_(dir.y, 0.0f)) * d1z;
+        hl = hl + std::sqrt(fmax_(-dir.y, 0.0f)) * d1w;
+        hl = hl + std::sqrt(fmax_(dir.z, 0.0f)) * d0z;
+        hl = hl + std::sqrt(fmax_(-dir.z, 0.0f)) * d0w;
+        if (dist > hl + 0.05f) continue;
+        float wx = ox == 0 ? 1.0f - frx : frx, wy = oy == 0 ? 1.0f - fry : fry, wz = oz == 0 ? 1.0f - frz : frz;
+        float wgt = (wx * wy) * wz;
+        res = add4(res, scale4(sample_cube_di(cubes + id * 14, n), wgt));
+        tw = tw + wgt;
+    }
+    if (tw > 0.0f) return f4{res.x / tw, res.y / tw, res.z / tw, res.w / tw};
+    return f4{0.0f, 0.0f, 0.0f, 0.0f};
+}
+
+inline float lerpf_(float a, float b, float t) { return fma_(t, b - a, a); }
+
+// One bake step of probe g: new cube words (14) and age; cubes_prev / voxels are whole grids.
+void bake_probe(const OScene& S, const GkrtFrameConstants& fc, uint32_t g, const uint32_t* cubes_prev,
+                const uint32_t* voxels, uint32_t out[14], uint32_t* age) {
+    static const float g44[32] = {-0.75f, -0.75f, -0.25f, -0.75f, 0.25f, -0.75f, 0.75f, -0.75f,
+                                  -0.75f, -0.25f, -0.25f, -0.25f, 0.25f, -0.25f, 0.75f, -0.25f,
+                                  -0.75f, 0.25f,  -0.25f, 0.25f,  0.25f, 0.25f,  0.75f, 0.25f,
+                                  -0.75f, 0.75f,  -0.25f, 0.75f,  0.25f, 0.75f,  0.75f, 0.75f};
+    static const float g33[18] = {-0.667f, -0.667f, 0.0f, -0.667f, 0.667f, -0.667f, -0.667f, 0.0f, 0.0f,
+                                  0.0f,    0.667f,  0.0f, -0.667f, 0.667f, 0.0f,    0.667f, 0.667f, 0.667f};
+    const uint32_t* prev = cubes_prev + (size_t)g * 14;
+    const uint32_t* vox = voxels + (size_t)g * 4;
+    for (int w = 0; w < 14; ++w) out[w] = prev[w];
+    *age = vox[1];
+    if ((vox[2] & 0xFFu) >= 8u) return;   // surface probes only
+    *age = vox[1] + 1u;
+    uint32_t sky[6];
+    uint32_t sun = (prev[13] >> 16) & 0xFFu;
+    const int dws[6] = {8, 9, 10, 11, 6, 7};
+    const int sws[6] = {12, 12, 13, 13, 12, 12}, sbs[6] = {2, 3, 0, 1, 0, 1};
+    // light 0: centre lerp(p1, p3, 0.5), power = its material's diffuse, area
+    bool lvalid = !S.lights.empty();
+    f3 lpos{0.0f, 0.0f, 0.0f};
+    f4 lpow{0.0f, 0.0f, 0.0f, 0.0f};
+    float larea = 0.0f;
+    if (lvalid) {
+        const GkrtLight& L = S.lights[0];
+        lpos = f3{fma_(0.5f, L.p3[0] - L.p1[0], L.p1[0]), fma_(0.5f, L.p3[1] - L.p1[1], L.p1[1]),
+                  fma_(0.5f, L.p3[2] - L.p1[2], L.p1[2])};
+        const GkrtMaterial& lm = S.mats[L.light_mat_idx];
+        lpow = f4{lm.diffuse[0], lm.diffuse[1], lm.diffuse[2], lm.diffuse[3]};
+        larea = L.normal_area[3];
+    }
+    for (int f = 0; f < 6; ++f) {
+        const f3 basis = face_basis(f);
+        const f3 o = fma3(basis, kCubeUnit * 0.25f, probe_origin(g));
+        f4 direct{0.0f, 0.0f, 0.0f, 0.0f}, bounce{0.0f, 0.0f, 0.0f, 0.0f};
+        float skyv = 0.0f;
+        const uint32_t j = vox[1] % 9u;
+        const float jx = g33[2 * j] * 0.25f, jy = g33[2 * j + 1] * 0.25f;
+        for (int i = 0; i < 16; ++i) {
+            f3 hv = normalize3(f3{g44[2 * i] + jx, g44[2 * i + 1] + jy, 1.0f});
+            f3 dir = align_with_normal(hv, basis);
+            ProbeHitO h = probe_hit(S, o, dir, 20.0f);
+            if (h.hit) {
+                const GkrtMaterial& hm = get_mat(S, h.v.mat);
+                f4 alb{hm.diffuse[0], hm.diffuse[1], hm.diffuse[2], hm.diffuse[3]};
+                bounce = add4(bounce, scale4(mul4(alb, probe_di(cubes_prev, voxels, h.v.P, h.v.N)), 1.25f));
+            } else {
+                direct = add4(direct, sky_color(fc));
+                skyv = skyv + 1.0f;
+            }
+        }
+        direct = scale4(direct, 0.0625f);
+        bounce = scale4(bounce, 0.0625f);
+        if (lvalid) {
+            f3 dv = sub(lpos, o);
+            float len = length3(dv);
+            f3 dn{dv.x / len, dv.y / len, dv.z / len};
+            bool hit = trace(S, fma3(dn, kCubeUnit * 0.5f, o), dn, kEPS, len - kCubeUnit, true, false, nullptr).hit;
+            float atten = hit ? 0.0f : 1.0f;
+            f3 ldir = normalize3(dv);
+            float ndotl = fmin_(fmax_(dot3(basis, ldir), 0.0f), 1.0f);
+            float att = (ndotl * larea) / ((len * len) * 3.14159f);
+            direct = add4(direct, scale4(scale4(lpow, att), atten));
+        }
+        if (fc.has_sun) {
+            f3 sd{fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]};
+            bool hit = trace(S, o, sd, kEPS, kPT_MAX, true, false, nullptr).hit;
+            float atten = hit ? 0.0f : 1.0f;
+            float ndotl = fmin_(fmax_(dot3(basis, sd), 0.0f), 1.0f);
+            if (f == 0) sun = atten > 0.0f ? 1u : 0u;
+            f4 sc4{fc.sun_color[0], fc.sun_color[1], fc.sun_color[2], fc.sun_color[3]};
+            direct = add4(direct, scale4(scale4(scale4(scale4(sc4, atten), ndotl), 1.0f), 0.25f));
+        }
+        float ov = (float)((prev[sws[f]] >> (8 * sbs[f])) & 0xFFu);
+        sky[f] = (uint32_t)lerpf_(ov, (255.0f * skyv) / 16.0f, 0.125f) & 0xFFu;
+        f4 od = unpack_rgb10a2(prev[dws[f]]), oi = unpack_rgb10a2(prev[dws[f] - 6]);
+        out[dws[f]] = pack_rgb10a2(f4{lerpf_(od.x, direct.x, 0.125f), lerpf_(od.y, direct.y, 0.125f),
+                                      lerpf_(od.z, direct.z, 0.125f), lerpf_(od.w, direct.w, 0.125f)});
+        out[dws[f] - 6] = pack_rgb10a2(f4{lerpf_(oi.x, bounce.x, 0.125f), lerpf_(oi.y, bounce.y, 0.125f),
+                                          lerpf_(oi.z, bounce.z, 0.125f), lerpf_(oi.w, bounce.w, 0.125f)});
+    }
+    out[12] = sky[4] | (sky[5] << 8) | (sky[0] << 16) | (sky[1] << 24);
+    out[13] = sky[2] | (sky[3] << 8) | (sun << 16) | (prev[13] & 0xFF000000u);
+}
+
 // ===================================== C API ==========================================
 extern "C" {
 
@@ -1481,6 +1718,23 @@ void gko_denoise_pass(const GkrtFrameConstants* fc, int W, int H, void** images,
 }
 
 void gko_set_fast(int on) { g_fast = on; }
+
+// Probe voxelization of probes [first, first + count): 4 words each into out.
+void gko_probe_voxelize(void* s, uint32_t first, uint32_t count, uint32_t* out, int threads) {
+    const OScene& S = *(const OScene*)s;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : omp_get_max_threads())
+    for (int64_t k = 0; k < (int64_t)count; ++k) voxelize_probe(S, first + (uint32_t)k, out + 4 * k);
+}
+
+// One bake step of probes [first, first + count) from whole-grid cubes_prev / voxels: 14 cube
+// words and the new age of each probe.
+void gko_probe_bake(void* s, const GkrtFrameConstants* fc, uint32_t first, uint32_t count, const uint32_t* cubes_prev,
+                    const uint32_t* voxels, uint32_t* cubes_out, uint32_t* ages_out, int threads) {
+    const OScene& S = *(const OScene*)s;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads > 0 ? threads : omp_get_max_threads())
+    for (int64_t k = 0; k < (int64_t)count; ++k)
+        bake_probe(S, *fc, first + (uint32_t)k, cubes_prev, voxels, cubes_out + 14 * k, ages_out + k);
+}
 
 // Small known-answer hooks for the unit tests.
 void gko_pcg4d(uint32_t v[4]) { pcg4d(v); }

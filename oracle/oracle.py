@@ -68,6 +68,9 @@ def lib():
         L.gko_gt_tonemap.restype = C.c_float
         L.gko_gt_tonemap.argtypes = [C.c_float]
         L.gko_set_fast.argtypes = [C.c_int]
+        L.gko_probe_voxelize.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int]
+        L.gko_probe_bake.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, C.c_uint32,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.gko_exact_tri.restype = C.c_int
         L.gko_fp32_tri.restype = C.c_int
         _lib = L
@@ -114,6 +117,23 @@ class OracleScene:
         hits = np.zeros(rays.shape[0], abi.HIT_DTYPE)
         lib().gko_trace_rays(self.h, rays.ctypes.data, hits.ctypes.data, rays.shape[0], mode, int(brute), threads)
         return hits
+
+    def probe_voxelize(self, first: int, count: int, threads: int = 0) -> np.ndarray:
+        """VoxelData words (count, 4) of probes [first, first + count)."""
+        out = np.zeros((count, 4), np.uint32)
+        lib().gko_probe_voxelize(self.h, first, count, out.ctypes.data, threads)
+        return out
+
+    def probe_bake(self, fc, first: int, count: int, cubes_prev: np.ndarray, voxels: np.ndarray, threads: int = 0):
+        """One bake step of probes [first, first + count) from whole-grid arrays; returns
+        (cube words (count, 14), ages (count,))."""
+        cubes_prev = np.ascontiguousarray(cubes_prev, np.uint32)
+        voxels = np.ascontiguousarray(voxels, np.uint32)
+        out = np.zeros((count, 14), np.uint32)
+        ages = np.zeros(count, np.uint32)
+        lib().gko_probe_bake(self.h, C.byref(fc), first, count, cubes_prev.ctypes.data, voxels.ctypes.data,
+                             out.ctypes.data, ages.ctypes.data, threads)
+        return out, ages
 
     def trace_pass(self, fc, width, height, images, y0=0, y1=0, threads=0) -> int:
         return int(lib().gko_trace_pass(self.h, C.byref(fc), width, height, _ptrs(images), y0, y1, threads))
