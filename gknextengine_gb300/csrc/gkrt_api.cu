@@ -992,6 +992,18 @@ int gkrt_copy_image_to_host(GkrtContext* ctx, int id, void* dst, size_t dst_byte
     return gkrt_synchronize(ctx, stream);
 }
 
+int gkrt_copy_image_to_host_async(GkrtContext* ctx, int id, void* dst, size_t dst_bytes, void* stream) {
+    GkrtImageView v;
+    int rc = gkrt_get_image(ctx, id, &v);
+    if (rc != GKRT_OK) return rc;
+    const size_t row = (size_t)v.width * image_bytes_per_px(id);
+    if (!dst || dst_bytes < row * v.height) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
+    cudaSetDevice(ctx->device);
+    GK_CUDA(cudaMemcpy2DAsync(dst, row, v.device_ptr, v.pitch_bytes, row, v.height, cudaMemcpyDeviceToHost,
+                              (cudaStream_t)stream));
+    return GKRT_OK;
+}
+
 int gkrt_upload_image(GkrtContext* ctx, int id, const void* src, size_t src_bytes, void* stream) {
     GkrtImageView v;
     int rc = gkrt_get_image(ctx, id, &v);

@@ -46,6 +46,7 @@ def load(path: str | None = None):
     L.gkrt_end_frame.argtypes = [vp, vp]
     L.gkrt_get_image.argtypes = [vp, C.c_int, C.POINTER(abi.GkrtImageView)]
     L.gkrt_copy_image_to_host.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
+    L.gkrt_copy_image_to_host_async.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
     L.gkrt_upload_image.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
     L.gkrt_trace_rays.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_trace_rays_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
@@ -81,7 +82,7 @@ EXPORTED = [
     "gkrt_context_create", "gkrt_context_destroy", "gkrt_last_error_message", "gkrt_abi_version",
     "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_build_bvh",
     "gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_end_frame", "gkrt_render_frame",
-    "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
+    "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_copy_image_to_host_async", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
     "gkrt_get_stats", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",
     "gkrt_synchronize", "gkrt_affine_inverse",
     "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16", "gkrt_conv3x3_wgrad_bf16",

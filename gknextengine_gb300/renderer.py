@@ -123,6 +123,17 @@ class PathTracingRenderer:
                                                       self._stream(stream)))
         return out
 
+    def read_image_async(self, image_id: int, out: np.ndarray, stream=None) -> np.ndarray:
+        """The copy of read_image ordered on stream without waiting (out: page-locked memory for
+        the copy to overlap other work; synchronize before reading it)."""
+        dt, ch = abi.IMAGE_FORMATS[image_id]
+        shape = (self.height, self.width) if ch == 1 else (self.height, self.width, ch)
+        if out.dtype != np.dtype(dt) or out.shape != shape or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be a contiguous {dt} array of shape {shape}")
+        self._check(self._lib.gkrt_copy_image_to_host_async(self._h, image_id, out.ctypes.data, out.nbytes,
+                                                            self._stream(stream)))
+        return out
+
     def write_image(self, image_id: int, data: np.ndarray, stream=None):
         dt, ch = abi.IMAGE_FORMATS[image_id]
         a = np.ascontiguousarray(data, dtype=dt)

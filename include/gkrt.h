@@ -292,6 +292,12 @@ int  gkrt_render_frame(GkrtContext* ctx, const GkrtFrameConstants* fc, void* str
 /* Outputs (bindless storage images, BindlessTexture.slang:8-40). */
 int  gkrt_get_image(GkrtContext* ctx, int image_id, GkrtImageView* out);
 int  gkrt_copy_image_to_host(GkrtContext* ctx, int image_id, void* dst, size_t dst_bytes, void* stream);
+/* The copy of gkrt_copy_image_to_host ordered on `stream` without waiting for it: the caller
+ * synchronizes (the stream or an event recorded after the call) before reading dst, and keeps
+ * the image unwritten until then. dst in page-locked memory makes the copy overlap later work
+ * on other streams, as the reference's frames in flight overlap their readbacks
+ * (VulkanBaseRenderer.cpp:727-869). */
+int  gkrt_copy_image_to_host_async(GkrtContext* ctx, int image_id, void* dst, size_t dst_bytes, void* stream);
 int  gkrt_upload_image(GkrtContext* ctx, int image_id, const void* src, size_t src_bytes, void* stream);
 
 /* Ray queries on the scene's BVH (FHardwareRayTracerV2::TraceRay / TraceOcclusion,
