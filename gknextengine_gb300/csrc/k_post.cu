@@ -142,12 +142,19 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid
     const f3 cn = xyz(tf4(t_nrm, kRpT, cx, cy));
     f4 sd = F4(0.0f, 0.0f, 0.0f, 0.0f), ss = F4(0.0f, 0.0f, 0.0f, 0.0f);
     float tw = 0.0f, mir = 0.0f;
+    // the tap distance sqrt(ox^2 + oy^2) takes six values (r^2 = 0, 1, 2, 4, 5, 8)
+    float dtab[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) dtab[q] = sqrt_((float)(q < 3 ? q : (q == 3 ? 4 : (q == 4 ? 5 : 8))));
+#pragma unroll
     for (int oy = -2; oy <= 2; ++oy) {
+#pragma unroll
         for (int ox = -2; ox <= 2; ++ox) {
             const uint32_t pid = t_id[(cy + oy) * kRpIdX + (ix + ox)];
             const f3 wn = xyz(tf4(t_nrm, kRpT, cx + ox, cy + oy));
-            const float fox = (float)ox, foy = (float)oy;
-            const float w = reproj_weight(sqrt_(fmaf_(foy, foy, fox * fox)), pid == cur, ox == 0 && oy == 0, wn, cn);
+            const int r2 = ox * ox + oy * oy;
+            const float dist = dtab[r2 < 3 ? r2 : (r2 == 4 ? 3 : (r2 == 5 ? 4 : 5))];
+            const float w = reproj_weight(dist, pid == cur, ox == 0 && oy == 0, wn, cn);
             sd = sd + tf4(t_sd, kRpT, cx + ox, cy + oy) * w;
             ss = ss + tf4(t_ss, kRpT, cx + ox, cy + oy) * w;
             tw = tw + w;
@@ -173,21 +180,22 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid
 // ---------------------------------------------------------------------------------------
 // compose: remodulation and tone map (Process.DenoiseJBF.comp.slang:145-181)
 
-// GranTurismoTonemapper (Const_Func.slang:100-121)
+// GranTurismoTonemapper (Const_Func.slang:100-121). The toe (T) and shoulder (S) curves are
+// evaluated only where their weight is not zero; powf is the fast form (__powf, a few ulps).
 GK_D float gt_tonemap(float x) {
     const float P = 1.0f, a = 0.7f, m = 0.22f, l = 0.4f, c = 1.33f, b = 0.0f, e = 2.71828f;
     const float l0 = div_((P - m) * l, a);
     const float L_x = m + a * (x - m);
-    const float T_x = m * powf(div_(x, m), c) + b;
     const float S0 = m + l0, S1 = m + a * l0;
     const float C2 = div_(a * P, P - S1);
-    const float S_x = P - (P - S1) * powf(e, -div_(C2 * (x - S0), P));
     float w0;
     if (x <= 0.0f) w0 = 1.0f;
     else if (x >= m) w0 = 0.0f;
     else { float q = div_(x, m); w0 = 1.0f - (q * q) * (3.0f - 2.0f * q); }
     const float w2 = x <= m + l0 ? 0.0f : 1.0f;
     const float w1 = (1.0f - w0) - w2;
+    const float T_x = w0 != 0.0f ? m * __powf(div_(x, m), c) + b : 0.0f;
+    const float S_x = w2 != 0.0f ? P - (P - S1) * __powf(e, -div_(C2 * (x - S0), P)) : 0.0f;
     return (T_x * w0 + L_x * w1) + S_x * w2;
 }
 GK_D float pq_encode(float v) {
@@ -210,7 +218,9 @@ GK_D void write_composed(const ComposeArgs& a, size_t pix, f3 total) {
 }
 
 // joint bilateral filter (Process.DenoiseJBF.comp.slang:49-148): 36 taps at stride 2 over
-// 11 x 11; the 26 x 26 diffuse neighbourhood of the block is staged by TMA.
+// 11 x 11; the 26 x 26 diffuse neighbourhood of the block is staged by TMA. The spatial weight
+// takes four values (computed once per pixel); the range weight uses the fast exponential
+// (__expf, relative error below 1e-6 where the weight matters).
 constexpr int kJbfHalo = 5;
 constexpr int kJbfT = kTile + 2 * kJbfHalo;   // 26
 
@@ -242,18 +252,30 @@ __global__ void __launch_bounds__(256) k_compose_jbf(ComposeArgs a, const __grid
         const float clum = dot3(cc, lw);
         const float sigmaL = a.bf_sigma_lum * 100.0f;
         const float den_s = (2.0f * a.bf_sigma) * a.bf_sigma, den_l = (2.0f * sigmaL) * sigmaL;
+        // spatial weights: i^2 + j^2 over the taps takes the values 2, 10, 18, 26, 34, 50, and
+        // dist = sat((i^2 + j^2) / 25) is 1 from 26 on
+        float fs[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float dist = sat(div_((float)(q < 3 ? 2 + 8 * q : 26), 25.0f));
+            fs[q] = expf(div_(-(dist * dist), den_s));
+        }
+        const float ninv_l = -div_(1.0f, den_l);
         total = F3(0.0f, 0.0f, 0.0f);
         float wsum = 0.0f;
+#pragma unroll
         for (int i = -5; i <= 5; i += 2) {
+#pragma unroll
             for (int j = -5; j <= 5; j += 2) {
+                const int r2 = i * i + j * j;
+                const float Fi = r2 == 2 ? fs[0] : (r2 == 10 ? fs[1] : (r2 == 18 ? fs[2] : fs[3]));
                 const f3 ci = xyz(tf4(t_d, kJbfT, cx + j, cy + i)) + eps;
                 const float lumi = dot3(ci, lw);
-                const float dist = sat(div_((float)(i * i + j * j), 25.0f));
                 const float dl = (clum - lumi) * (clum - lumi);
-                const float Fi = expf(div_(-(dist * dist), den_s));
-                const float Li = expf(div_(-(dl * dl), den_l));
-                total = total + (ci * Fi) * Li;
-                wsum = wsum + Fi * Li;
+                const float Li = __expf((dl * dl) * ninv_l);
+                const float w = Fi * Li;
+                total = total + ci * w;
+                wsum = wsum + w;
             }
         }
         total = F3(div_(total.x, wsum), div_(total.y, wsum), div_(total.z, wsum));
