@@ -56,7 +56,7 @@ def workload_config():
                 "per_frame": "gkrt_scene_update_instances (instance-level BVH rebuild on the GPU + emitter "
                              "alias table) inside the timed frame",
                 "data": "synthetic seeded scene (numpy default_rng seed 3)"}
-    return {"workload": f"bricks-1.03M-tris {W_}x{H_} 1spp depth8 orbit0.5deg/frame reproject+JBF",
+    return {"workload": f"bricks-1.03M-tris {W_}x{H_} 1spp depth8 orbit0.5deg/frame reproject+atrous5x5x3",
             "triangles": 1032194, "instances": 4097, "width": W_, "height": H_, "spp": 1, "max_depth": 8,
             "l2": "per-frame image working set 0.5 GB > L2 (129 MB); the 0.6 MB BVH stays L2-resident as "
                   "in steady-state rendering",
@@ -450,6 +450,7 @@ def run_gkrt(args):
                 "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic", "config": workload_config(),
                 "ms_per_frame": ms_total / K, "trace_ms": trace_avg_ms, "rays_per_frame": rays / max(K, 1) / world,
+                "trace_pass_mrays_s": rays / max(K, 1) / world / (trace_avg_ms * 1e-3) / 1e6,
                 "gpu_launches": 3 * K + 2 * K * (fcs[0].denoiser == abi.DENOISE_ATROUS) + build_launches,
                 "probe_ms": probe_ms,
                 "bvh_build_ms": {"all_levels": build_all_ms, "instance_level": build_inst_ms,

@@ -54,14 +54,16 @@ struct TileLoad {
 // ---------------------------------------------------------------------------------------
 // reprojection (Process.ReProject.comp.slang:71-223)
 
-// calculateWeight (Process.ReProject.comp.slang:32-47)
-GK_D float reproj_weight(float cd, bool same, bool center, f3 n, f3 cn) {
+// calculateWeight (Process.ReProject.comp.slang:32-47) with the tap's distance term given as
+// the reciprocal rd = 1 / (1.5 cd + 4) (a per-tap constant): the two divisions become
+// multiplications, within a few ulps of the quotients.
+GK_D float reproj_weight(float rd, bool same, bool center, f3 n, f3 cn) {
     if (center) return 0.4f;
     if (!same) return 0.0f;
     float nd = sat(dot3(n, cn));
     if (nd < 0.98f) return 0.0f;
-    float nw = div_(nd - 0.98f, 1.0f - 0.98f);
-    return div_(nw * 2.0f, fmaf_(cd, 1.5f, 4.0f));
+    float nw = (nd - 0.98f) * 50.0f;   // 1 / (1 - 0.98)
+    return (nw * 2.0f) * rd;
 }
 
 // FilterHistoryColor (Process.ReProject.comp.slang:49-68)
@@ -142,10 +144,11 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid
     const f3 cn = xyz(tf4(t_nrm, kRpT, cx, cy));
     f4 sd = F4(0.0f, 0.0f, 0.0f, 0.0f), ss = F4(0.0f, 0.0f, 0.0f, 0.0f);
     float tw = 0.0f, mir = 0.0f;
-    // the tap distance sqrt(ox^2 + oy^2) takes six values (r^2 = 0, 1, 2, 4, 5, 8)
+    // 1 / (1.5 d + 4) of the tap distance d = sqrt(ox^2 + oy^2), six values (r^2 = 0, 1, 2, 4, 5, 8)
     float dtab[6];
 #pragma unroll
-    for (int q = 0; q < 6; ++q) dtab[q] = sqrt_((float)(q < 3 ? q : (q == 3 ? 4 : (q == 4 ? 5 : 8))));
+    for (int q = 0; q < 6; ++q)
+        dtab[q] = div_(1.0f, fmaf_(sqrt_((float)(q < 3 ? q : (q == 3 ? 4 : (q == 4 ? 5 : 8)))), 1.5f, 4.0f));
 #pragma unroll
     for (int oy = -2; oy <= 2; ++oy) {
 #pragma unroll
@@ -153,8 +156,8 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid
             const uint32_t pid = t_id[(cy + oy) * kRpIdX + (ix + ox)];
             const f3 wn = xyz(tf4(t_nrm, kRpT, cx + ox, cy + oy));
             const int r2 = ox * ox + oy * oy;
-            const float dist = dtab[r2 < 3 ? r2 : (r2 == 4 ? 3 : (r2 == 5 ? 4 : 5))];
-            const float w = reproj_weight(dist, pid == cur, ox == 0 && oy == 0, wn, cn);
+            const float rd = dtab[r2 < 3 ? r2 : (r2 == 4 ? 3 : (r2 == 5 ? 4 : 5))];
+            const float w = reproj_weight(rd, pid == cur, ox == 0 && oy == 0, wn, cn);
             sd = sd + tf4(t_sd, kRpT, cx + ox, cy + oy) * w;
             ss = ss + tf4(t_ss, kRpT, cx + ox, cy + oy) * w;
             tw = tw + w;
@@ -297,21 +300,25 @@ __global__ void __launch_bounds__(256) k_compose_jbf(ComposeArgs a, const __grid
 //   luminance weight  exp(-|L_p - L_q| / sigma_L)  (sigma_L = bf_sigma_lum),
 //   0 when the object ids differ or q lies outside the image.
 // Three passes with s = 1, 2, 4; the last one remodulates (x albedo + specular) and tone maps.
-constexpr int kAtMaxHalo = 8;
-constexpr int kAtT = kTile + 2 * kAtMaxHalo;   // 32
 
 GK_D float b3(int k) { return k == 0 ? 0.375f : (k == 1 ? 0.25f : 0.0625f); }
 GK_D float pow16(float v) { float a = v * v; a = a * a; a = a * a; return a * a; }
 
+// One pass, templated on its step S so that every tap's shared-memory offset is an immediate.
+// The taps read the luminance from the colour's fourth channel: the first pass (S = 1) writes
+// it into its staged tile after the load (each thread its share), and every pass but the last
+// stores its output with the output's luminance there, which only the next pass reads. The
+// image bounds are tested once per tap row and column.
+template <int S>
 __global__ void __launch_bounds__(256) k_atrous(AtrousArgs a, const __grid_constant__ CUtensorMap m_in,
                                                 const __grid_constant__ CUtensorMap m_nrm,
                                                 const __grid_constant__ CUtensorMap m_id) {
-    __shared__ __align__(128) float4 t_c[kAtT * kAtT];
-    __shared__ __align__(128) float4 t_n[kAtT * kAtT];
-    __shared__ __align__(128) uint32_t t_id[kAtT * kAtT];
+    constexpr int halo = 2 * S, T = kTile + 2 * halo;
+    constexpr int hid = (halo + 3) & ~3, Tid = kTile + 2 * hid;   // id tile starts on a 16-byte boundary
+    __shared__ __align__(128) float4 t_c[T * T];
+    __shared__ __align__(128) float4 t_n[T * T];
+    __shared__ __align__(128) uint32_t t_id[T * Tid];
     __shared__ __align__(8) uint64_t bar;
-    const int s = a.step, halo = 2 * s, T = kTile + 2 * halo;
-    const int hid = (halo + 3) & ~3, Tid = kTile + 2 * hid;   // id tile starts on a 16-byte boundary
     const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int x = x0 + tx, y = y0 + ty;
@@ -323,36 +330,57 @@ __global__ void __launch_bounds__(256) k_atrous(AtrousArgs a, const __grid_const
         tma_load_2d(t_n, &m_nrm, 4 * (x0 - halo), y0 - halo, &bar);
         tma_load_2d(t_id, &m_id, x0 - hid, y0 - halo, &bar);
     }
-    if (!tl.wait(a.err)) return;
-    if (x >= a.W || y >= a.H) return;
-    const size_t pix = (size_t)y * a.P + x;
+    // the block agrees on the load's outcome before the barriers below
+    if (!__syncthreads_and(tl.wait(a.err) ? 1 : 0)) return;
     const int cx = tx + halo, cy = ty + halo;
     const f3 lw = F3(0.212671f, 0.715160f, 0.072169f);
-    const f4 cp = tf4(t_c, T, cx, cy);
+    if (S == 1) {
+        for (int i = threadIdx.x; i < T * T; i += 256) {
+            float4 v = t_c[i];
+            v.w = dot3(F3(v.x, v.y, v.z), lw);
+            t_c[i] = v;
+        }
+        __syncthreads();
+    }
+    if (x >= a.W || y >= a.H) return;
+    const size_t pix = (size_t)y * a.P + x;
+    const float4* cbase = t_c + cy * T + cx;
+    const float4* nbase = t_n + cy * T + cx;
+    const uint32_t* ibase = t_id + cy * Tid + tx + hid;
+    const float4 c4 = *cbase;
     const f3 np = xyz(tf4(t_n, T, cx, cy));
-    const uint32_t idp = t_id[cy * Tid + tx + hid];
-    const float lp = dot3(xyz(cp), lw);
+    const uint32_t idp = *ibase;
+    const float lp = c4.w;
     const float inv_sl = div_(1.0f, fmaxf(a.sigma_lum, 1e-4f));
+    bool vx[5], vy[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const int qx = x + (k - 2) * S, qy = y + (k - 2) * S;
+        vx[k] = qx >= 0 && qx < a.W;
+        vy[k] = qy >= 0 && qy < a.H;
+    }
     f3 sum = F3(0.0f, 0.0f, 0.0f);
     float wsum = 0.0f;
+#pragma unroll
     for (int dy = -2; dy <= 2; ++dy) {
+#pragma unroll
         for (int dx = -2; dx <= 2; ++dx) {
-            const int qx = x + dx * s, qy = y + dy * s;
-            if (qx < 0 || qy < 0 || qx >= a.W || qy >= a.H) continue;
-            const int lx = cx + dx * s, ly = cy + dy * s;
-            if (t_id[ly * Tid + tx + hid + dx * s] != idp) continue;
-            const f4 cq = tf4(t_c, T, lx, ly);
-            const float wn = pow16(fmaxf(dot3(np, xyz(tf4(t_n, T, lx, ly))), 0.0f));
-            const float wl = expf(-(fabsf(lp - dot3(xyz(cq), lw)) * inv_sl));
+            if (!(vx[dx + 2] && vy[dy + 2])) continue;
+            if (ibase[dy * S * Tid + dx * S] != idp) continue;
+            const float4 cq = cbase[dy * S * T + dx * S];
+            const float4 nq = nbase[dy * S * T + dx * S];
+            const float wn = pow16(fmaxf(fmaf_(np.z, nq.z, fmaf_(np.y, nq.y, np.x * nq.x)), 0.0f));
+            // fast exponential (__expf): relative error below 1e-6 where the weight matters
+            const float wl = __expf(-(fabsf(lp - cq.w) * inv_sl));
             const float w = ((b3(dx < 0 ? -dx : dx) * b3(dy < 0 ? -dy : dy)) * wn) * wl;
-            sum = sum + xyz(cq) * w;
+            sum = sum + F3(cq.x, cq.y, cq.z) * w;
             wsum = wsum + w;
         }
     }
     // the centre tap always passes (weight 0.140625 > 0)
     const f3 f = F3(div_(sum.x, wsum), div_(sum.y, wsum), div_(sum.z, wsum));
     if (!a.last) {
-        a.out[pix] = make_float4(f.x, f.y, f.z, cp.w);
+        a.out[pix] = make_float4(f.x, f.y, f.z, dot3(f, lw));
         return;
     }
     const ImgDims g{a.W, a.H, a.P};
@@ -437,7 +465,9 @@ cudaError_t gkrt_launch_atrous(const AtrousArgs& base, const float4* in, float4*
         if ((e = map_f4(&m_in, src, a.W, a.H, a.P, T, T)) != cudaSuccess) return e;
         if ((e = map_f4(&m_n, a.normal, a.W, a.H, a.P, T, T)) != cudaSuccess) return e;
         if ((e = map_u32(&m_id, a.id0, a.W, a.H, a.P, Tid, T)) != cudaSuccess) return e;
-        k_atrous<<<grid, 256, 0, st>>>(a, m_in, m_n, m_id);
+        if (p == 0) k_atrous<1><<<grid, 256, 0, st>>>(a, m_in, m_n, m_id);
+        else if (p == 1) k_atrous<2><<<grid, 256, 0, st>>>(a, m_in, m_n, m_id);
+        else k_atrous<4><<<grid, 256, 0, st>>>(a, m_in, m_n, m_id);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         src = a.out;
     }

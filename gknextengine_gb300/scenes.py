@@ -268,7 +268,9 @@ def bricks(seed: int = 2, width: int = 1920, height: int = 1080, grid: int = 64,
     scene = abi.SceneArrays(pos, nrm, slot, idx, meshes, materials, insts, lights=lights, name="bricks")
     center = np.array([ext_x * 0.5, 0.0, ext_z * 0.5])
     cam = Camera(eye=center + np.array([0.0, 40.0, 90.0]), center=center + np.array([0.0, 2.0, 0.0]), fov_deg=40.0)
-    settings = Settings(samples=1, bounces=8, max_bounces=8, temporal_frames=16, taa=True)
+    # the configuration's denoiser: bilateral 5 x 5, three a-trous passes
+    settings = Settings(samples=1, bounces=8, max_bounces=8, temporal_frames=16, taa=True,
+                        denoiser=abi.DENOISE_ATROUS)
     return scene, cam, settings
 
 
