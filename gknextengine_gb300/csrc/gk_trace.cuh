@@ -437,7 +437,8 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
 // The first triangle leaf found is postponed into T.leaf and the lane keeps traversing;
 // a second leaf, or leaving the instance the postponed leaf belongs to, makes the lane wait
 // for the leaf phase. Returns true while the lane can take another node step.
-GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn) {
+// cap: the stack's capacity in words (entries); the caller's stack holds at least cap * stride.
+GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn, int cap = kStackSize) {
     if (++T.iter > kIterCap) { atomicOr(S.error, kErrIter); T.done = true; return false; }
     const int ref = T.ref;
     if (ref == kRefPop) {
@@ -464,7 +465,7 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         if (h0 && h1) {
             int nearr = nd.x, farr = nd.y;
             if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
-            if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return false; }
+            if (T.sp >= cap) { atomicOr(S.error, kErrStack); T.done = true; return false; }
             stk[T.sp * stride] = (uint32_t)farr;
             ++T.sp;
             T.ref = nearr;
@@ -488,7 +489,7 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         T.d = xvector(w, T.wd);
         T.inv = safe_inv(T.d);
         T.sh = make_shear(T.d);
-        if (T.sp >= kStackSize) { atomicOr(S.error, kErrStack); T.done = true; return false; }
+        if (T.sp >= cap) { atomicOr(S.error, kErrStack); T.done = true; return false; }
         stk[T.sp * stride] = (uint32_t)kRefMarker;
         ++T.sp;
         T.inblas = true;

@@ -830,7 +830,10 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     im.hit_inst = (uint32_t*)ctx->img[GKRT_IMG_HIT_INST];
     im.hit_prim = (uint32_t*)ctx->img[GKRT_IMG_HIT_PRIM];
     GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
-    GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, (int)ctx->P, im, ctx->d_counters, ctx->d_work, ctx->num_sms, st));
+    // the stack bound check_stack_bound enforced at build time, at least 8 entries
+    const int stack_words = std::max(8, std::min(kStackSize, ctx->blas_bin_depth + ctx->tlas_bin_depth + 3));
+    GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, (int)ctx->P, im, ctx->d_counters, ctx->d_work,
+                                   ctx->num_sms, stack_words, st));
     return GKRT_OK;
 }
 
