@@ -51,6 +51,11 @@ struct GkrtContext {
     uint32_t* d_cubes = nullptr;                // probe grid (uploaded, or made by gkrt_probe_voxelize)
     uint32_t* d_voxels = nullptr;
     uint32_t* d_cubes_prev = nullptr;           // snapshot the bake interpolates from
+    // page-locked staging of the per-update tables (instance tables, emitter table), so that
+    // their uploads are asynchronous on the caller's stream; staged is recorded after them
+    void* h_stage[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    size_t h_stage_cap[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t staged = nullptr;
     std::vector<GkrtLight> lights_host;
 
     // acceleration structures: d_nodes holds the builders' two-child mesh-level nodes
@@ -205,12 +210,43 @@ int copy_in(GkrtContext* ctx, T* dst, const void* src, size_t bytes) {
     return GKRT_OK;
 }
 
-// Instance tables of the kernels; allocated once per scene (updates keep the count).
-int upload_instances(GkrtContext* ctx) {
+// Page-locked staging buffer `slot` of at least `bytes`; the uploads staged from it before
+// (recorded by ctx->staged) have completed when it returns.
+void* stage_buf(GkrtContext* ctx, int slot, size_t bytes) {
+    if (ctx->staged) cudaEventSynchronize(ctx->staged);
+    if (bytes > ctx->h_stage_cap[slot]) {
+        if (ctx->h_stage[slot]) cudaFreeHost(ctx->h_stage[slot]);
+        ctx->h_stage[slot] = nullptr;
+        ctx->h_stage_cap[slot] = 0;
+        const size_t cap = bytes + bytes / 4 + 256;
+        if (cudaMallocHost(&ctx->h_stage[slot], cap) != cudaSuccess) {
+            ctx->h_stage[slot] = nullptr;
+            return nullptr;
+        }
+        ctx->h_stage_cap[slot] = cap;
+    }
+    return ctx->h_stage[slot];
+}
+
+int copy_staged(GkrtContext* ctx, void* dst, const void* staged, size_t bytes, cudaStream_t st) {
+    if (bytes) GK_CUDA(cudaMemcpyAsync(dst, staged, bytes, cudaMemcpyHostToDevice, st));
+    return GKRT_OK;
+}
+
+int record_staged(GkrtContext* ctx, cudaStream_t st) {
+    if (!ctx->staged) GK_CUDA(cudaEventCreateWithFlags(&ctx->staged, cudaEventDisableTiming));
+    GK_CUDA(cudaEventRecord(ctx->staged, st));
+    return GKRT_OK;
+}
+
+// Instance tables of the kernels; allocated once per scene (updates keep the count). Updates
+// are built in page-locked memory and uploaded asynchronously on `st`.
+int upload_instances(GkrtContext* ctx, cudaStream_t st) {
     const uint32_t n = (uint32_t)ctx->inst.size();
-    std::vector<uint32_t> mats(16 * (size_t)n);
-    std::vector<float> prev(12 * (size_t)n);
-    std::vector<DevInst> di(n);
+    uint32_t* mats = static_cast<uint32_t*>(stage_buf(ctx, 0, 64 * (size_t)n + 4));
+    float* prev = static_cast<float*>(stage_buf(ctx, 1, 48 * (size_t)n + 4));
+    DevInst* di = static_cast<DevInst*>(stage_buf(ctx, 2, sizeof(DevInst) * (size_t)n + 16));
+    if (!mats || !prev || !di) return fail(ctx, GKRT_ERR_OOM, "page-locked staging of the instance tables");
     for (uint32_t i = 0; i < n; ++i) {
         const GkrtInstance& s = ctx->inst[i];
         std::memcpy(&mats[16 * (size_t)i], s.mat_id, 64);
@@ -226,15 +262,16 @@ int upload_instances(GkrtContext* ctx) {
     }
     int rc;
     if (ctx->inst_cap < n || !ctx->d_inst) {
-        if ((rc = upload(ctx, ctx->d_inst_mat, mats.data(), mats.size() * 4)) != GKRT_OK) return rc;
-        if ((rc = upload(ctx, ctx->d_inst_prev, prev.data(), prev.size() * 4)) != GKRT_OK) return rc;
-        if ((rc = upload(ctx, ctx->d_inst, di.data(), di.size() * sizeof(DevInst))) != GKRT_OK) return rc;
+        if ((rc = upload(ctx, ctx->d_inst_mat, mats, 64 * (size_t)n)) != GKRT_OK) return rc;
+        if ((rc = upload(ctx, ctx->d_inst_prev, prev, 48 * (size_t)n)) != GKRT_OK) return rc;
+        if ((rc = upload(ctx, ctx->d_inst, di, sizeof(DevInst) * (size_t)n)) != GKRT_OK) return rc;
         ctx->inst_cap = n;
         return GKRT_OK;
     }
-    if ((rc = copy_in(ctx, ctx->d_inst_mat, mats.data(), mats.size() * 4)) != GKRT_OK) return rc;
-    if ((rc = copy_in(ctx, ctx->d_inst_prev, prev.data(), prev.size() * 4)) != GKRT_OK) return rc;
-    return copy_in(ctx, ctx->d_inst, di.data(), di.size() * sizeof(DevInst));
+    if ((rc = copy_staged(ctx, ctx->d_inst_mat, mats, 64 * (size_t)n, st)) != GKRT_OK) return rc;
+    if ((rc = copy_staged(ctx, ctx->d_inst_prev, prev, 48 * (size_t)n, st)) != GKRT_OK) return rc;
+    if ((rc = copy_staged(ctx, ctx->d_inst, di, sizeof(DevInst) * (size_t)n, st)) != GKRT_OK) return rc;
+    return record_staged(ctx, st);
 }
 
 // d_nodes capacity for `total` nodes, keeping the mesh-level part.
@@ -434,6 +471,8 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
             ib.push_back(b);
         }
         if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
+        // the instance tables first: their host work and uploads overlap the stream's earlier work
+        if ((rc = upload_instances(ctx, st)) != GKRT_OK) return rc;
         GpuBvhResult r;
         GK_CUDA(gpu_bvh_build_instances(ctx->builder, ib.data(), (uint32_t)ib.size(), ctx->d_blas_box, base, &r, st));
         if ((rc = ensure_node_cap(ctx, (size_t)base + r.node_count)) != GKRT_OK) return rc;
@@ -446,7 +485,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
         ctx->tlas_bin_depth = r.depth;
         if ((rc = finish_tlas(ctx, r.node_count, st)) != GKRT_OK) return rc;
         ctx->tlas_ready = true;
-        return upload_instances(ctx);
+        return GKRT_OK;
     }
     std::vector<float> boxes;
     std::vector<uint32_t> map;
@@ -496,11 +535,11 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
     ctx->tlas_bin_depth = hb.depth;
     if ((rc = finish_tlas(ctx, (uint32_t)hb.nodes.size(), st)) != GKRT_OK) return rc;
     ctx->tlas_ready = true;
-    return upload_instances(ctx);
+    return upload_instances(ctx, st);
 }
 
 // The emissive-triangle table of the current instances (rebuilt with every instance update).
-int build_emitters(GkrtContext* ctx) {
+int build_emitters(GkrtContext* ctx, cudaStream_t st) {
     EmitterTable t;
     build_emitter_table(ctx->inst.data(), (uint32_t)ctx->inst.size(), ctx->meshes.data(), ctx->pos_host.data(),
                         ctx->idx_host.data(), ctx->slot_tris, ctx->mat_host.data(), ctx->nmat, t);
@@ -514,8 +553,15 @@ int build_emitters(GkrtContext* ctx) {
         ctx->emit_cap = n;
     }
     int rc;
-    if ((rc = copy_in(ctx, ctx->d_emit, t.geo.data(), t.geo.size() * sizeof(float4))) != GKRT_OK) return rc;
-    if ((rc = copy_in(ctx, ctx->d_emit_alias, t.alias.data(), t.alias.size() * sizeof(float2))) != GKRT_OK) return rc;
+    const size_t gb = t.geo.size() * sizeof(float4), ab = t.alias.size() * sizeof(float2);
+    void* hg = stage_buf(ctx, 3, gb + 16);
+    void* ha = stage_buf(ctx, 4, ab + 16);
+    if (!hg || !ha) return fail(ctx, GKRT_ERR_OOM, "page-locked staging of the emitter table");
+    if (gb) std::memcpy(hg, t.geo.data(), gb);
+    if (ab) std::memcpy(ha, t.alias.data(), ab);
+    if ((rc = copy_staged(ctx, ctx->d_emit, hg, gb, st)) != GKRT_OK) return rc;
+    if ((rc = copy_staged(ctx, ctx->d_emit_alias, ha, ab, st)) != GKRT_OK) return rc;
+    if ((rc = record_staged(ctx, st)) != GKRT_OK) return rc;
     ctx->nemit = n;
     return GKRT_OK;
 }
@@ -690,6 +736,12 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     ctx->unet = nullptr;
     gpu_bvh_free(ctx->builder);
     ctx->builder = nullptr;
+    for (void*& h : ctx->h_stage) {
+        if (h) cudaFreeHost(h);
+        h = nullptr;
+    }
+    if (ctx->staged) cudaEventDestroy(ctx->staged);
+    ctx->staged = nullptr;
     dfree(ctx->d_counters);
     dfree(ctx->d_error);
     dfree(ctx->d_work);
@@ -779,7 +831,9 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
     }
     ctx->has_scene = true;
     if ((rc = ensure_bvh(ctx, GKRT_BUILD_ALL, (cudaStream_t)0)) != GKRT_OK) return rc;
-    return build_emitters(ctx);
+    if ((rc = build_emitters(ctx, (cudaStream_t)0)) != GKRT_OK) return rc;
+    GK_CUDA(cudaStreamSynchronize((cudaStream_t)0));
+    return GKRT_OK;
 }
 
 int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count, void* stream) {
@@ -791,10 +845,11 @@ int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
     if (rc != GKRT_OK) return rc;
     cudaSetDevice(ctx->device);
     ctx->inst.assign(instances, instances + count);
-    if (!ctx->blas_ready) rc = ensure_bvh(ctx, 0, (cudaStream_t)stream);
-    else rc = build_tlas(ctx, (cudaStream_t)stream);
-    if (rc != GKRT_OK) return rc;
-    return build_emitters(ctx);
+    // host work first (emitter table, then the instance tables inside build_tlas), uploaded
+    // asynchronously, so that it overlaps the stream's earlier frames; the GPU build follows
+    if ((rc = build_emitters(ctx, (cudaStream_t)stream)) != GKRT_OK) return rc;
+    if (!ctx->blas_ready) return ensure_bvh(ctx, 0, (cudaStream_t)stream);
+    return build_tlas(ctx, (cudaStream_t)stream);
 }
 
 int gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream) {
