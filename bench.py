@@ -346,10 +346,12 @@ def run_gkrt(args):
     rays0, bl0 = s0.rays_total, s0.build_launches
     barrier()
     torch.cuda.synchronize()
+    ev_u = [torch.cuda.Event(enable_timing=True) for _ in range(K)]   # before each instance update
     with ClockSampler(local) as clk, torch.cuda.stream(stream):
         start.record(stream)
         for k in range(K):
             fc = fcs[Wm + k]
+            ev_u[k].record(stream)
             if insts is not None:
                 r.update_instances(insts[Wm + k], stream)
             ev[k][0].record(stream)
@@ -366,6 +368,7 @@ def run_gkrt(args):
     build_launches = st_last.build_launches - bl0
     ms_total = start.elapsed_time(end)
     trace_ms = [a.elapsed_time(b) for a, b in ev]
+    update_span_ms = sum(u.elapsed_time(a) for u, (a, _) in zip(ev_u, ev)) / K
     if world > 1:
         t = torch.tensor([ms_total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -425,6 +428,58 @@ def run_gkrt(args):
     barrier()
     e2e_value = e2e_rays / e2e_s / 1e6
 
+    # ---- the same frames with the instance level refit instead of rebuilt (animated scenes) ----
+    # Frame rays differ between runs of the same frames (moving pixels get 4x samples while
+    # their motion moment lasts), so the comparison is Mrays/s and the update's own time.
+    refit = None
+    if insts is not None:
+        def call_host_ms(fn, frames):   # host time of an update call with the GPU idle
+            t = []
+            for i in frames:
+                r.synchronize(stream)
+                t0 = time.perf_counter()
+                fn(insts[i], stream)
+                t.append(time.perf_counter() - t0)
+            r.synchronize(stream)
+            return sum(t) / len(t) * 1e3
+        rebuild_host = call_host_ms(r.update_instances, range(Wm, Wm + 3))
+        r.update_instances(insts[0], stream)        # the tree of frame 0's layout; refits from here on
+        refit_host = call_host_ms(r.refit_instances, range(1, Wm))
+        for i in range(1, Wm):
+            r.refit_instances(insts[i], stream)
+            r.render(fcs[i], stream)
+        r.synchronize(stream)
+        s0r = r.stats()
+        fe = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+        rs, re_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            rs.record(stream)
+            for k in range(K):
+                fc = fcs[Wm + k]
+                fe[k][0].record(stream)
+                r.refit_instances(insts[Wm + k], stream)
+                fe[k][1].record(stream)
+                r.trace_pass(fc, stream)
+                fe[k][2].record(stream)
+                r.reproject_pass(fc, stream)
+                r.denoise_pass(fc, stream)
+                r.end_frame(stream)
+            re_.record(stream)
+            torch.cuda.synchronize()
+        s1r = r.stats()
+        ms_r = rs.elapsed_time(re_)
+        refit = {"mrays_s": (s1r.rays_total - s0r.rays_total) / (ms_r * 1e-3) / 1e6,
+                 "ms_per_frame": ms_r / K,
+                 "trace_ms": sum(a.elapsed_time(b) for _, a, b in fe) / K,
+                 "update_span_ms": sum(a.elapsed_time(b) for a, b, _ in fe) / K,
+                 "rebuild_update_span_ms": update_span_ms,
+                 "call_host_ms": refit_host, "rebuild_call_host_ms": rebuild_host,
+                 "refits": s1r.tlas_refits - s0r.tlas_refits,
+                 "node_visits_last_frame": s1r.node_visits,
+                 "node_visits_last_frame_rebuilt": st_last.node_visits}
+
     # ---- probe grid (after the timed frames: a baked grid changes path termination) ----
     probe_ms = None
     if WORKLOAD == "bricks" and rank == 0:
@@ -453,6 +508,7 @@ def run_gkrt(args):
                 "trace_pass_mrays_s": rays / max(K, 1) / world / (trace_avg_ms * 1e-3) / 1e6,
                 "gpu_launches": 3 * K + 2 * K * (fcs[0].denoiser == abi.DENOISE_ATROUS) + build_launches,
                 "probe_ms": probe_ms,
+                "tlas_refit": refit,
                 "bvh_build_ms": {"all_levels": build_all_ms, "instance_level": build_inst_ms,
                                  "scene_load_s": load_s, "triangles": int(sc.triangle_count),
                                  "instances": int(sc.instances.shape[0])},

@@ -159,7 +159,8 @@ class GkrtStats(C.Structure):
                 ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64), ("rays_total", C.c_uint64),
                 ("device_error", C.c_uint32), ("bvh_nodes", C.c_uint32), ("bvh_leaf_tris", C.c_uint32),
                 ("tlas_nodes", C.c_uint32), ("emitters", C.c_uint32), ("build_launches", C.c_uint32),
-                ("wide_nodes", C.c_uint32), ("wide_depth", C.c_uint32)]
+                ("wide_nodes", C.c_uint32), ("wide_depth", C.c_uint32), ("tlas_refits", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 def fptr(a: np.ndarray, ctype=C.c_float):

@@ -164,10 +164,10 @@ __global__ void k_gather_tris(const float4* pos, const uint32_t* ind, const Mesh
 
 // World boxes of instances: the mesh box's 8 corners through the 3x4 world matrix in FP64,
 // widened because the mesh level traverses the FP32 object-space ray.
-__global__ void k_inst_boxes(const GpuInstBox* in, uint32_t n, const float* mesh_box, float* box, float* cent) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const GpuInstBox I = in[i];
+// World box of an instance: the mesh root box's corners through its transform in FP64, padded
+// as the mesh level traverses the FP32-transformed ray, whose points sit within rounding of the
+// world ray's. Shared by the instance-level build and its refit.
+__device__ void inst_box(const GpuInstBox& I, const float* mesh_box, float* out) {
     const float* rb = mesh_box + 6 * (size_t)I.mesh;
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int c = 0; c < 8; ++c) {
@@ -181,10 +181,20 @@ __global__ void k_inst_boxes(const GpuInstBox* in, uint32_t n, const float* mesh
     }
     for (int r = 0; r < 3; ++r) {
         const double pad = 1e-5 * (fabs(lo[r]) + fabs(hi[r]) + (hi[r] - lo[r])) + 1e-7;
-        const float l = (float)(lo[r] - pad), h = (float)(hi[r] + pad);
-        box[6 * (size_t)i + r] = l;
-        box[6 * (size_t)i + 3 + r] = h;
-        cent[3 * (size_t)i + r] = 0.5f * (l + h);
+        out[r] = (float)(lo[r] - pad);
+        out[3 + r] = (float)(hi[r] + pad);
+    }
+}
+
+__global__ void k_inst_boxes(const GpuInstBox* in, uint32_t n, const float* mesh_box, float* box, float* cent) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float b[6];
+    inst_box(in[i], mesh_box, b);
+    for (int r = 0; r < 3; ++r) {
+        box[6 * (size_t)i + r] = b[r];
+        box[6 * (size_t)i + 3 + r] = b[3 + r];
+        cent[3 * (size_t)i + r] = 0.5f * (b[r] + b[3 + r]);
     }
 }
 
@@ -613,12 +623,14 @@ __global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, 
 
 struct WEnt {
     int ref;
+    int slot;   // 2 * binary node + side: where the box and ref come from
     float b[6];
 };
 
 // Children of binary node `node`: the first replaces e[at], the second is appended at e[n].
-// Returns false for a node without children (not produced by the builders).
-__device__ bool wide_children(const BvhNode* bin, int node, WEnt* e, int& n, int at) {
+// Returns false for a node without children (not produced by the builders). With links, each
+// child's slot is recorded as its parent (interior child) or its instance's leaf (leaf child).
+__device__ bool wide_children(const BvhNode* bin, int node, WEnt* e, int& n, int at, const RefitLinks* lk) {
     const float* f = reinterpret_cast<const float*>(bin + node);
     const int* r = reinterpret_cast<const int*>(bin + node) + 12;
     bool first = true;
@@ -627,15 +639,25 @@ __device__ bool wide_children(const BvhNode* bin, int node, WEnt* e, int& n, int
         WEnt& d = first ? e[at] : e[n++];
         first = false;
         d.ref = r[side];
+        d.slot = 2 * node + side;
         for (int j = 0; j < 6; ++j) d.b[j] = f[6 * side + j];
+        if (lk) {
+            if (d.ref >= 0) {
+                const uint32_t k = (uint32_t)(d.ref - (int)lk->nbase);
+                if (k < lk->ncap) lk->parent[k] = d.slot;
+            } else {
+                const uint32_t k = ~(uint32_t)d.ref >> 3;   // instance leaves hold one instance
+                if (k < lk->ninst) lk->leaf[k] = d.slot;
+            }
+        }
     }
     return !first;
 }
 
 // Greedy expansion of binary node `root` into at most 8 children; -1 on a malformed tree.
-__device__ int wide_expand(const BvhNode* bin, int root, WEnt* e) {
+__device__ int wide_expand(const BvhNode* bin, int root, WEnt* e, const RefitLinks* lk = nullptr) {
     int n = 1;
-    if (!wide_children(bin, root, e, n, 0)) return -1;
+    if (!wide_children(bin, root, e, n, 0, lk)) return -1;
     while (n < 8) {
         int best = -1;
         float ba = -1.0f;
@@ -645,7 +667,7 @@ __device__ int wide_expand(const BvhNode* bin, int root, WEnt* e) {
             if (a > ba) { ba = a; best = i; }
         }
         if (best < 0) break;
-        if (!wide_children(bin, e[best].ref, e, n, best)) return -1;
+        if (!wide_children(bin, e[best].ref, e, n, best, lk)) return -1;
     }
     return n;
 }
@@ -695,16 +717,25 @@ __global__ void k_wide_count(const BvhNode* bin, const int4* items, uint32_t n, 
     cnt[i] = c;   // 0 for a malformed node: k_wide_emit reports it
 }
 
+// links (optional, links.parent null for none): refit links of the trees being collapsed
 __global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, const uint32_t* off, uint32_t next_base,
-                            WideNode* out, int4* next, uint32_t* err) {
+                            WideNode* out, int4* next, uint32_t* err, RefitLinks links) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int4 it = items[i];
+    const RefitLinks* lk = links.parent ? &links : nullptr;
     WEnt e[8];
-    int m = wide_expand(bin, it.x, e);
+    int m = wide_expand(bin, it.x, e, lk);
     if (m < 0) {
         atomicOr(err, kBuildErrRange);
         m = 0;
+    }
+    if (lk) {
+        const uint32_t w = (uint32_t)it.y - lk->wbase;
+        if (w < lk->wcap)
+            for (int j = 0; j < 8; ++j) lk->wsrc[8 * (size_t)w + j] = j < m ? e[j].slot : -1;
+        else
+            atomicOr(err, kBuildErrRange);
     }
     uint32_t qw[3][4] = {{0u, 0u, 0u, 0u}, {0u, 0u, 0u, 0u}, {0u, 0u, 0u, 0u}};
     float origin[3] = {0.0f, 0.0f, 0.0f};
@@ -740,6 +771,89 @@ __global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, c
     w.ref[0] = make_int4(ref[0], ref[1], ref[2], ref[3]);
     w.ref[1] = make_int4(ref[4], ref[5], ref[6], ref[7]);
     out[it.y] = w;
+}
+
+// ---------------------------------------------------------------------------------------------
+// refit of the instance level, topology kept
+//
+// One thread per instance climbs from its leaf: it writes its box into its slot (widened, as
+// node boxes are stored; unwidened into ubox, 12 floats per node), and at a node with two
+// children only the second arrival goes on, with the union of both children's boxes (Karras,
+// HPG 2012, bottom-up boxes). The second arrival resets the node's counter for the next refit.
+// Nothing waits: the first arrival stops. The union of exact boxes is exact, so every node
+// gets the box a build of the same topology would give it.
+
+__global__ void __launch_bounds__(128) k_refit_boxes(RefitLinks lk, const GpuInstBox* inst, const float* mesh_box,
+                                                     BvhNode* nodes, float* ubox, uint32_t* arrive) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= lk.ninst) return;
+    int s = lk.leaf[i];
+    if (s < 0) return;   // not in the tree (invisible, or an empty mesh)
+    float b[6];
+    inst_box(inst[i], mesh_box, b);
+    for (int hop = 0; hop < 128; ++hop) {   // the builders stop at 64 levels
+        const int node = s >> 1, side = s & 1;
+        const uint32_t k = (uint32_t)(node - (int)lk.nbase);
+        if (k >= lk.ncap) return;
+        float* f = reinterpret_cast<float*>(nodes + node);
+        float* u = ubox + 12 * (size_t)k;
+        for (int j = 0; j < 3; ++j) {
+            f[6 * side + j] = widen_lo(b[j]);
+            f[6 * side + 3 + j] = widen_hi(b[3 + j]);
+            u[6 * side + j] = b[j];
+            u[6 * side + 3 + j] = b[3 + j];
+        }
+        const int* r = reinterpret_cast<const int*>(nodes + node) + 12;
+        if (r[1] != kRefPop) {
+            __threadfence();
+            if (atomicAdd(&arrive[k], 1u) == 0u) return;   // the sibling's thread finishes the node
+            __threadfence();
+            arrive[k] = 0u;
+            const float* o = u + 6 * (1 - side);
+            for (int j = 0; j < 3; ++j) {
+                b[j] = fminf(b[j], __ldcg(o + j));
+                b[3 + j] = fmaxf(b[3 + j], __ldcg(o + 3 + j));
+            }
+        }
+        s = lk.parent[k];
+        if (s < 0) return;   // the root: its box sits in no slot
+    }
+}
+
+// The wide nodes re-quantized from the refit slot boxes; their children, refs and slot masks
+// stay as the collapse wrote them.
+__global__ void __launch_bounds__(128) k_refit_wide(RefitLinks lk, const BvhNode* nodes, WideNode* wide, uint32_t nw,
+                                                    uint32_t* err, uint32_t err_bit) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nw || j >= lk.wcap) return;
+    WEnt e[8];
+    int m = 0;
+    for (int c = 0; c < 8; ++c) {
+        const int s = lk.wsrc[8 * (size_t)j + c];
+        if (s < 0) break;
+        const float* f = reinterpret_cast<const float*>(nodes + (s >> 1)) + 6 * (s & 1);
+        for (int q = 0; q < 6; ++q) e[m].b[q] = f[q];
+        ++m;
+    }
+    uint32_t qw[3][4] = {{0u, 0u, 0u, 0u}, {0u, 0u, 0u, 0u}, {0u, 0u, 0u, 0u}};
+    float origin[3] = {0.0f, 0.0f, 0.0f};
+    uint32_t meta = m > 0 ? ((1u << m) - 1u) << 24 : 0u;
+    for (int ax = 0; ax < 3; ++ax) {
+        uint32_t qlo[8], qhi[8], eb = 127u;
+        if (m > 0 && !wide_axis(e, m, ax, origin[ax], eb, qlo, qhi)) {
+            atomicOr(err, err_bit);   // the node loses its slots; the error word reports it
+            meta = 0u;
+            break;
+        }
+        meta |= eb << (8 * ax);
+        for (int c = 0; c < m; ++c) {
+            qw[ax][c >> 2] |= qlo[c] << (8 * (c & 3));
+            qw[ax][2 + (c >> 2)] |= qhi[c] << (8 * (c & 3));
+        }
+    }
+    WideNode& w = wide[lk.wbase + j];
+    w.h = make_float4(origin[0], origin[1], origin[2], __uint_as_float(meta));
+    for (int ax = 0; ax < 3; ++ax) w.q[ax] = make_uint4(qw[ax][0], qw[ax][1], qw[ax][2], qw[ax][3]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1023,7 +1137,9 @@ struct GpuBvh {
     // nodes out[wide_base, wide_base + count), out holding out_cap nodes in all. The root of
     // tree r becomes wide node wroots[r] = wide_base + (its position among the valid roots).
     cudaError_t collapse(const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base, WideNode* out,
-                         size_t out_cap, std::vector<int>& wroots, uint32_t* count, int* depth, cudaStream_t st) {
+                         size_t out_cap, std::vector<int>& wroots, uint32_t* count, int* depth, cudaStream_t st,
+                         const RefitLinks* links) {
+        const RefitLinks lk = links ? *links : RefitLinks();
         wroots.assign(roots.size(), -1);
         std::vector<int4> it0;
         uint32_t next = wide_base;
@@ -1056,7 +1172,7 @@ struct GpuBvh {
             GK_TRY(cudaStreamSynchronize(st));
             if ((size_t)next + tot > out_cap) return cudaErrorInvalidValue;
             GK_TRY(witems[cur ^ 1].need(std::max<uint32_t>(tot, 1u)));
-            k_wide_emit<<<g, 128, 0, st>>>(bin, witems[cur].p, n, woff.p, next, out, witems[cur ^ 1].p, werr.p);
+            k_wide_emit<<<g, 128, 0, st>>>(bin, witems[cur].p, n, woff.p, next, out, witems[cur ^ 1].p, werr.p, lk);
             ++launches;
             GK_TRY(cudaGetLastError());
             next += tot;
@@ -1132,8 +1248,16 @@ cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint
 
 cudaError_t gpu_bvh_collapse(GpuBvh* B, const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base,
                              WideNode* out, size_t out_cap, std::vector<int>& wroots, uint32_t* count, int* depth,
-                             cudaStream_t st) {
-    return B->collapse(bin, roots, wide_base, out, out_cap, wroots, count, depth, st);
+                             cudaStream_t st, const RefitLinks* links) {
+    return B->collapse(bin, roots, wide_base, out, out_cap, wroots, count, depth, st, links);
+}
+
+cudaError_t gpu_bvh_refit_instances(const RefitLinks& lk, const GpuInstBox* inst, const float* mesh_box,
+                                    BvhNode* nodes, float* ubox, uint32_t* arrive, WideNode* wide, uint32_t nw,
+                                    uint32_t* err, uint32_t err_bit, cudaStream_t st) {
+    if (lk.ninst) k_refit_boxes<<<(lk.ninst + 127) / 128, 128, 0, st>>>(lk, inst, mesh_box, nodes, ubox, arrive);
+    if (nw) k_refit_wide<<<(nw + 127) / 128, 128, 0, st>>>(lk, nodes, wide, nw, err, err_bit);
+    return cudaGetLastError();
 }
 
 }  // namespace gk

@@ -79,6 +79,8 @@ constexpr int kIterCap = 1 << 22;
 // is measured slower here: a lane stops at its first leaf.
 constexpr bool kSpeculative = false;   // measured: 4.01 ms without, 4.16 ms with (1080p bricks)
 constexpr uint32_t kErrStack = 1u, kErrIter = 2u;
+// (4u is the TMA wait timeout of the post passes, gk_tma.cuh)
+constexpr uint32_t kErrRefit = 8u;   // a refit box that the 8-wide nodes cannot quantize
 
 // Per-thread event counts, flushed once per warp at the end of a kernel.
 struct Counters {

@@ -21,6 +21,16 @@
 
 using namespace gk;
 
+// Staging tables: 0 instance materials, 1 previous transforms, 2 DevInst, 3 emitter geometry,
+// 4 emitter alias table, 5 refit transforms.
+constexpr int kStageSlots = 6;
+struct StageSlot {
+    void* p[2] = {nullptr, nullptr};
+    size_t cap[2] = {0, 0};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int cur = 0;
+};
+
 struct GkrtContext {
     int device = 0;
     uint32_t watchdog_ms = 60000;
@@ -51,11 +61,10 @@ struct GkrtContext {
     uint32_t* d_cubes = nullptr;                // probe grid (uploaded, or made by gkrt_probe_voxelize)
     uint32_t* d_voxels = nullptr;
     uint32_t* d_cubes_prev = nullptr;           // snapshot the bake interpolates from
-    // page-locked staging of the per-update tables (instance tables, emitter table), so that
-    // their uploads are asynchronous on the caller's stream; staged is recorded after them
-    void* h_stage[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    size_t h_stage_cap[5] = {0, 0, 0, 0, 0};
-    cudaEvent_t staged = nullptr;
+    // page-locked staging of the per-update tables (instance tables, emitter table, refit
+    // transforms), so that their uploads are asynchronous on the caller's stream: two buffers
+    // per table, each with the event recorded after its last upload
+    StageSlot stage[kStageSlots];
     std::vector<GkrtLight> lights_host;
 
     // acceleration structures: d_nodes holds the builders' two-child mesh-level nodes
@@ -81,6 +90,15 @@ struct GkrtContext {
     int blas_bin_depth = 0, tlas_bin_depth = 0;   // two-child levels (root = 0)
     bool blas_ready = false, tlas_ready = false;
     uint32_t inst_cap = 0;            // instance arrays allocated for this many instances
+    // instance-level refit: links recorded by the last instance-level collapse, scratch, and
+    // which instances that build put in the tree
+    RefitLinks refit;
+    float* d_refit_ubox = nullptr;
+    uint32_t* d_refit_arrive = nullptr;
+    GpuInstBox* d_refit_inst = nullptr;
+    size_t refit_ncap = 0, refit_wcap = 0, refit_icap = 0;
+    std::vector<uint8_t> tlas_members;
+    uint32_t tlas_refits = 0;
 
     Unet* unet = nullptr;                       // learned denoiser (gkrt_unet_init)
     unsigned long long* d_counters = nullptr;   // see flush_counters: 5 per-pass slots + total rays
@@ -167,6 +185,11 @@ void free_scene(GkrtContext* c) {
     c->blas_node_count = c->blas_nodes_used = 0;
     c->meshes.clear(); c->inst.clear(); c->pos_host.clear(); c->idx_host.clear();
     c->blas_root.clear(); c->blas_box.clear();
+    dfree(c->refit.parent); dfree(c->refit.leaf); dfree(c->refit.wsrc);
+    dfree(c->d_refit_ubox); dfree(c->d_refit_arrive); dfree(c->d_refit_inst);
+    c->refit = RefitLinks();
+    c->refit_ncap = c->refit_wcap = c->refit_icap = 0;
+    c->tlas_members.clear();
 }
 
 template <class T>
@@ -210,32 +233,34 @@ int copy_in(GkrtContext* ctx, T* dst, const void* src, size_t bytes) {
     return GKRT_OK;
 }
 
-// Page-locked staging buffer `slot` of at least `bytes`; the uploads staged from it before
-// (recorded by ctx->staged) have completed when it returns.
+// Page-locked staging buffer of table `slot`, at least `bytes`: the other of its two buffers
+// than the last call's, so the host waits only for the upload staged two updates ago.
 void* stage_buf(GkrtContext* ctx, int slot, size_t bytes) {
-    if (ctx->staged) cudaEventSynchronize(ctx->staged);
-    if (bytes > ctx->h_stage_cap[slot]) {
-        if (ctx->h_stage[slot]) cudaFreeHost(ctx->h_stage[slot]);
-        ctx->h_stage[slot] = nullptr;
-        ctx->h_stage_cap[slot] = 0;
+    StageSlot& S = ctx->stage[slot];
+    S.cur ^= 1;
+    const int c = S.cur;
+    if (S.ev[c]) cudaEventSynchronize(S.ev[c]);
+    if (bytes > S.cap[c]) {
+        if (S.p[c]) cudaFreeHost(S.p[c]);
+        S.p[c] = nullptr;
+        S.cap[c] = 0;
         const size_t cap = bytes + bytes / 4 + 256;
-        if (cudaMallocHost(&ctx->h_stage[slot], cap) != cudaSuccess) {
-            ctx->h_stage[slot] = nullptr;
+        if (cudaMallocHost(&S.p[c], cap) != cudaSuccess) {
+            S.p[c] = nullptr;
             return nullptr;
         }
-        ctx->h_stage_cap[slot] = cap;
+        S.cap[c] = cap;
     }
-    return ctx->h_stage[slot];
+    return S.p[c];
 }
 
-int copy_staged(GkrtContext* ctx, void* dst, const void* staged, size_t bytes, cudaStream_t st) {
-    if (bytes) GK_CUDA(cudaMemcpyAsync(dst, staged, bytes, cudaMemcpyHostToDevice, st));
-    return GKRT_OK;
-}
-
-int record_staged(GkrtContext* ctx, cudaStream_t st) {
-    if (!ctx->staged) GK_CUDA(cudaEventCreateWithFlags(&ctx->staged, cudaEventDisableTiming));
-    GK_CUDA(cudaEventRecord(ctx->staged, st));
+// Upload of the buffer stage_buf(slot) returned last to dst, asynchronous on st; the slot's
+// event is recorded after it.
+int copy_staged(GkrtContext* ctx, int slot, void* dst, size_t bytes, cudaStream_t st) {
+    StageSlot& S = ctx->stage[slot];
+    if (bytes) GK_CUDA(cudaMemcpyAsync(dst, S.p[S.cur], bytes, cudaMemcpyHostToDevice, st));
+    if (!S.ev[S.cur]) GK_CUDA(cudaEventCreateWithFlags(&S.ev[S.cur], cudaEventDisableTiming));
+    GK_CUDA(cudaEventRecord(S.ev[S.cur], st));
     return GKRT_OK;
 }
 
@@ -268,10 +293,9 @@ int upload_instances(GkrtContext* ctx, cudaStream_t st) {
         ctx->inst_cap = n;
         return GKRT_OK;
     }
-    if ((rc = copy_staged(ctx, ctx->d_inst_mat, mats, 64 * (size_t)n, st)) != GKRT_OK) return rc;
-    if ((rc = copy_staged(ctx, ctx->d_inst_prev, prev, 48 * (size_t)n, st)) != GKRT_OK) return rc;
-    if ((rc = copy_staged(ctx, ctx->d_inst, di, sizeof(DevInst) * (size_t)n, st)) != GKRT_OK) return rc;
-    return record_staged(ctx, st);
+    if ((rc = copy_staged(ctx, 0, ctx->d_inst_mat, 64 * (size_t)n, st)) != GKRT_OK) return rc;
+    if ((rc = copy_staged(ctx, 1, ctx->d_inst_prev, 48 * (size_t)n, st)) != GKRT_OK) return rc;
+    return copy_staged(ctx, 2, ctx->d_inst, sizeof(DevInst) * (size_t)n, st);
 }
 
 // d_nodes capacity for `total` nodes, keeping the mesh-level part.
@@ -352,16 +376,61 @@ int finish_blas(GkrtContext* ctx, cudaStream_t st) {
     return GKRT_OK;
 }
 
+// Refit links and scratch for an instance level of `bin_count` two-child node slots, reset
+// (parents and leaves -1, counters 0) on st before the collapse records the links.
+int prepare_refit(GkrtContext* ctx, uint32_t bin_count, cudaStream_t st) {
+    const size_t nc = std::max<size_t>(bin_count, 1), wc = nc + 1, ic = std::max<size_t>(ctx->inst.size(), 1);
+    if (nc > ctx->refit_ncap) {
+        dfree(ctx->refit.parent); dfree(ctx->d_refit_ubox); dfree(ctx->d_refit_arrive);
+        ctx->refit_ncap = 0;
+        GK_CUDA(cudaMalloc((void**)&ctx->refit.parent, nc * sizeof(int)));
+        GK_CUDA(cudaMalloc((void**)&ctx->d_refit_ubox, nc * 12 * sizeof(float)));
+        GK_CUDA(cudaMalloc((void**)&ctx->d_refit_arrive, nc * sizeof(uint32_t)));
+        ctx->refit_ncap = nc;
+    }
+    if (wc > ctx->refit_wcap) {
+        dfree(ctx->refit.wsrc);
+        ctx->refit_wcap = 0;
+        GK_CUDA(cudaMalloc((void**)&ctx->refit.wsrc, wc * 8 * sizeof(int)));
+        ctx->refit_wcap = wc;
+    }
+    if (ic > ctx->refit_icap) {
+        dfree(ctx->refit.leaf); dfree(ctx->d_refit_inst);
+        ctx->refit_icap = 0;
+        GK_CUDA(cudaMalloc((void**)&ctx->refit.leaf, ic * sizeof(int)));
+        GK_CUDA(cudaMalloc((void**)&ctx->d_refit_inst, ic * sizeof(GpuInstBox)));
+        ctx->refit_icap = ic;
+    }
+    GK_CUDA(cudaMemsetAsync(ctx->refit.parent, 0xFF, nc * sizeof(int), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_refit_arrive, 0, nc * sizeof(uint32_t), st));
+    GK_CUDA(cudaMemsetAsync(ctx->refit.leaf, 0xFF, ic * sizeof(int), st));
+    ctx->refit.nbase = ctx->blas_node_count;
+    ctx->refit.ncap = (uint32_t)nc;
+    ctx->refit.ninst = (uint32_t)ctx->inst.size();
+    ctx->refit.wbase = ctx->blas_wide_count;
+    ctx->refit.wcap = (uint32_t)wc;
+    return GKRT_OK;
+}
+
+// Per instance: whether the instance-level build puts it in the tree.
+void tlas_members(const GkrtContext* ctx, std::vector<uint8_t>& m) {
+    m.resize(ctx->inst.size());
+    for (size_t i = 0; i < ctx->inst.size(); ++i)
+        m[i] = (ctx->inst[i].visible && ctx->blas_root[ctx->inst[i].mesh_id] >= 0) ? 1 : 0;
+}
+
 // The instance-level two-child tree (root ctx->tlas_root) collapsed after the mesh level.
 int finish_tlas(GkrtContext* ctx, uint32_t bin_count, cudaStream_t st) {
     int rc;
     if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
     if ((rc = ensure_wide_cap(ctx, (size_t)ctx->blas_wide_count + bin_count + 1, ctx->blas_wide_count)) != GKRT_OK)
         return rc;
+    if ((rc = prepare_refit(ctx, bin_count, st)) != GKRT_OK) return rc;
+    tlas_members(ctx, ctx->tlas_members);
     std::vector<int> wr;
     const cudaError_t e = gpu_bvh_collapse(ctx->builder, ctx->d_nodes, std::vector<int>(1, ctx->tlas_root),
                                            ctx->blas_wide_count, ctx->d_wide, ctx->d_wide_cap, wr,
-                                           &ctx->tlas_wide_count, &ctx->tlas_wide_depth, st);
+                                           &ctx->tlas_wide_count, &ctx->tlas_wide_depth, st, &ctx->refit);
     if (e == cudaErrorInvalidValue)
         return fail(ctx, GKRT_ERR_INVALID_ARG, "instance BVH collapse failed (non-finite transforms or depth > 64)");
     if (e != cudaSuccess) return cuda_fail(ctx, e, "gpu_bvh_collapse(instance level)");
@@ -538,6 +607,29 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
     return upload_instances(ctx, st);
 }
 
+// Instance-level refit in place, for instances that keep the members of the last build: the
+// instance tables and the transforms staged and uploaded, then the two refit launches, all
+// asynchronous on st (no host synchronisation).
+int refit_tlas(GkrtContext* ctx, cudaStream_t st) {
+    const uint32_t n = (uint32_t)ctx->inst.size();
+    int rc;
+    if ((rc = upload_instances(ctx, st)) != GKRT_OK) return rc;
+    GpuInstBox* hb = static_cast<GpuInstBox*>(stage_buf(ctx, 5, sizeof(GpuInstBox) * (size_t)n + 16));
+    if (!hb) return fail(ctx, GKRT_ERR_OOM, "page-locked staging of the refit transforms");
+    for (uint32_t i = 0; i < n; ++i) {
+        std::memcpy(hb[i].world, ctx->inst[i].world, 48);
+        hb[i].mesh = ctx->inst[i].mesh_id;
+        hb[i].inst = i;
+        hb[i].pad0 = hb[i].pad1 = 0u;
+    }
+    if ((rc = copy_staged(ctx, 5, ctx->d_refit_inst, sizeof(GpuInstBox) * (size_t)n, st)) != GKRT_OK) return rc;
+    GK_CUDA(gpu_bvh_refit_instances(ctx->refit, ctx->d_refit_inst, ctx->d_blas_box, ctx->d_nodes, ctx->d_refit_ubox,
+                                    ctx->d_refit_arrive, ctx->d_wide, ctx->tlas_wide_count, ctx->d_error, kErrRefit,
+                                    st));
+    ++ctx->tlas_refits;
+    return GKRT_OK;
+}
+
 // The emissive-triangle table of the current instances (rebuilt with every instance update).
 int build_emitters(GkrtContext* ctx, cudaStream_t st) {
     EmitterTable t;
@@ -559,9 +651,8 @@ int build_emitters(GkrtContext* ctx, cudaStream_t st) {
     if (!hg || !ha) return fail(ctx, GKRT_ERR_OOM, "page-locked staging of the emitter table");
     if (gb) std::memcpy(hg, t.geo.data(), gb);
     if (ab) std::memcpy(ha, t.alias.data(), ab);
-    if ((rc = copy_staged(ctx, ctx->d_emit, hg, gb, st)) != GKRT_OK) return rc;
-    if ((rc = copy_staged(ctx, ctx->d_emit_alias, ha, ab, st)) != GKRT_OK) return rc;
-    if ((rc = record_staged(ctx, st)) != GKRT_OK) return rc;
+    if ((rc = copy_staged(ctx, 3, ctx->d_emit, gb, st)) != GKRT_OK) return rc;
+    if ((rc = copy_staged(ctx, 4, ctx->d_emit_alias, ab, st)) != GKRT_OK) return rc;
     ctx->nemit = n;
     return GKRT_OK;
 }
@@ -736,12 +827,13 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     ctx->unet = nullptr;
     gpu_bvh_free(ctx->builder);
     ctx->builder = nullptr;
-    for (void*& h : ctx->h_stage) {
-        if (h) cudaFreeHost(h);
-        h = nullptr;
-    }
-    if (ctx->staged) cudaEventDestroy(ctx->staged);
-    ctx->staged = nullptr;
+    for (StageSlot& S : ctx->stage)
+        for (int k = 0; k < 2; ++k) {
+            if (S.p[k]) cudaFreeHost(S.p[k]);
+            if (S.ev[k]) cudaEventDestroy(S.ev[k]);
+            S.p[k] = nullptr;
+            S.ev[k] = nullptr;
+        }
     dfree(ctx->d_counters);
     dfree(ctx->d_error);
     dfree(ctx->d_work);
@@ -850,6 +942,23 @@ int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
     if ((rc = build_emitters(ctx, (cudaStream_t)stream)) != GKRT_OK) return rc;
     if (!ctx->blas_ready) return ensure_bvh(ctx, 0, (cudaStream_t)stream);
     return build_tlas(ctx, (cudaStream_t)stream);
+}
+
+int gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    if (!instances || count != ctx->inst.size())
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "instance update must keep the instance count");
+    int rc = validate_instances(ctx, instances, count, (uint32_t)ctx->meshes.size(), ctx->nmat);
+    if (rc != GKRT_OK) return rc;
+    cudaSetDevice(ctx->device);
+    ctx->inst.assign(instances, instances + count);
+    if ((rc = build_emitters(ctx, (cudaStream_t)stream)) != GKRT_OK) return rc;
+    if (!ctx->blas_ready || !ctx->tlas_ready) return ensure_bvh(ctx, 0, (cudaStream_t)stream);
+    std::vector<uint8_t> m;
+    tlas_members(ctx, m);
+    if (m != ctx->tlas_members) return build_tlas(ctx, (cudaStream_t)stream);   // the tree's members changed
+    return refit_tlas(ctx, (cudaStream_t)stream);
 }
 
 int gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream) {
@@ -1175,6 +1284,8 @@ int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     out->build_launches = gpu_bvh_launches(ctx->builder);
     out->wide_nodes = ctx->blas_wide_count + ctx->tlas_wide_count;
     out->wide_depth = (uint32_t)(ctx->blas_wide_depth + ctx->tlas_wide_depth);
+    out->tlas_refits = ctx->tlas_refits;
+    out->reserved = 0;
     return GKRT_OK;
 }
 

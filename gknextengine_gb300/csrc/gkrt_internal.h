@@ -90,7 +90,7 @@ void build_emitter_table(const GkrtInstance* inst, uint32_t ninst, const GkrtMes
 // GPU builder (bvh_gpu.cu): same split rule and node layout, device scratch reused across
 // builds. Results stay in the builder's memory until its next build.
 struct GpuBvh;
-struct GpuInstBox {                 // one visible instance for the instance-level build
+struct GpuInstBox {                 // one instance for the instance-level build or refit
     float world[12];
     uint32_t mesh, inst, pad0, pad1;
 };
@@ -117,9 +117,28 @@ cudaError_t gpu_bvh_build_instances(GpuBvh* b, const GpuInstBox* inst_host, uint
 // Collapse of two-child trees (device array bin, roots: node refs, -1 for none) into the
 // compressed 8-wide nodes the kernels traverse, at out[wide_base ...) of an array of out_cap
 // nodes. wroots: wide root per tree (-1 for none); count: wide nodes written; depth: levels.
+// links: when non-null, the collapse also records what a refit of these trees needs.
+struct RefitLinks;
 cudaError_t gpu_bvh_collapse(GpuBvh* b, const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base,
                              WideNode* out, size_t out_cap, std::vector<int>& wroots, uint32_t* count, int* depth,
-                             cudaStream_t st);
+                             cudaStream_t st, const RefitLinks* links = nullptr);
+
+// Links of the instance level for refits, recorded by its collapse. A slot is 2 * node + side:
+// the half of two-child node `node` that holds one child's box and ref. Device arrays.
+struct RefitLinks {
+    int* parent = nullptr;     // per two-child node nbase + i: the slot holding its box; -1 at the root
+    int* leaf = nullptr;       // per instance: the slot of its leaf; -1 when not in the tree
+    int* wsrc = nullptr;       // 8 per wide node wbase + j: the slots of its children's boxes; -1 unused
+    uint32_t nbase = 0, ncap = 0, ninst = 0, wbase = 0, wcap = 0;
+};
+// Refit of the instance level in place: the two-child boxes of the leaves from the instances'
+// current transforms (inst: device, one record per instance index), unions up to the root, then
+// the wide nodes [wbase, wbase + nw) re-quantized. arrive: ncap counters, zero between refits.
+// Two launches, no host synchronisation; a wide node whose boxes cannot be quantized sets
+// err_bit in *err (the traversal error word).
+cudaError_t gpu_bvh_refit_instances(const RefitLinks& links, const GpuInstBox* inst, const float* mesh_box,
+                                    BvhNode* nodes, float* ubox, uint32_t* arrive, WideNode* wide, uint32_t nw,
+                                    uint32_t* err, uint32_t err_bit, cudaStream_t st);
 }  // namespace gk
 
 // stack_words: traversal stack entries per thread, at least the scene's two-child depth bound

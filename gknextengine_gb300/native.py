@@ -40,6 +40,7 @@ def load(path: str | None = None):
     L.gkrt_resize.argtypes = [vp, C.c_uint32, C.c_uint32]
     L.gkrt_scene_upload.argtypes = [vp, C.POINTER(abi.GkrtSceneDesc)]
     L.gkrt_scene_update_instances.argtypes = [vp, vp, C.c_uint32, vp]
+    L.gkrt_scene_refit_instances.argtypes = [vp, vp, C.c_uint32, vp]
     L.gkrt_build_bvh.argtypes = [vp, C.c_uint32, vp]
     for n in ("gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_render_frame"):
         getattr(L, n).argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), vp]
@@ -80,7 +81,8 @@ def load(path: str | None = None):
 # every function include/gkrt.h declares (checked by the CPU test suite)
 EXPORTED = [
     "gkrt_context_create", "gkrt_context_destroy", "gkrt_last_error_message", "gkrt_abi_version",
-    "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_build_bvh",
+    "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_scene_refit_instances",
+    "gkrt_build_bvh",
     "gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_end_frame", "gkrt_render_frame",
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_copy_image_to_host_async", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
     "gkrt_get_stats", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",

@@ -86,6 +86,13 @@ class PathTracingRenderer:
         self._check(self._lib.gkrt_scene_update_instances(self._h, inst.ctypes.data, inst.shape[0],
                                                           self._stream(stream)))
 
+    def refit_instances(self, instances: np.ndarray, stream=None):
+        """The same update with the instance level refit in place (topology kept, no host
+        synchronisation); rebuilds instead when the set of instances in the tree changes."""
+        inst = np.ascontiguousarray(instances, dtype=abi.INSTANCE_DTYPE)
+        self._check(self._lib.gkrt_scene_refit_instances(self._h, inst.ctypes.data, inst.shape[0],
+                                                         self._stream(stream)))
+
     def build_bvh(self, flags: int = abi.BUILD_ALL, stream=None):
         self._check(self._lib.gkrt_build_bvh(self._h, flags, self._stream(stream)))
 

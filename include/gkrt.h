@@ -240,7 +240,8 @@ typedef struct GkrtStats {
     uint64_t node_visits;       /* BVH nodes visited, last pass                           */
     uint64_t triangle_tests;    /* ray/triangle tests, last pass                          */
     uint64_t rays_total;        /* rays traced since the context was created              */
-    uint32_t device_error;      /* device error word (iteration caps hit)                 */
+    uint32_t device_error;      /* device error word: 1 stack, 2 iteration cap, 4 TMA wait,
+                                   8 a refit box the 8-wide nodes cannot quantize          */
     uint32_t bvh_nodes;
     uint32_t bvh_leaf_tris;
     uint32_t tlas_nodes;
@@ -248,6 +249,8 @@ typedef struct GkrtStats {
     uint32_t build_launches;    /* kernels launched by GPU BVH builds since creation      */
     uint32_t wide_nodes;        /* compressed 8-wide nodes traversed (mesh + instance)    */
     uint32_t wide_depth;        /* wide levels, deepest mesh tree + instance tree         */
+    uint32_t tlas_refits;       /* instance-level refits since creation                   */
+    uint32_t reserved;
 } GkrtStats;
 
 typedef struct GkrtContext GkrtContext;
@@ -268,6 +271,16 @@ int  gkrt_resize(GkrtContext* ctx, uint32_t width, uint32_t height);
 int  gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* scene);
 int  gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
                                  uint32_t count, void* stream);
+/* The same update with the instance level refit in place instead of rebuilt (the update mode
+ * the reference's TLAS allows, VK_BUILD_ACCELERATION_STRUCTURE_ALLOW_UPDATE_BIT_KHR,
+ * TopLevelAccelerationStructure.cpp:30): the tree keeps its topology, its boxes follow the new
+ * transforms bottom-up and its 8-wide nodes are re-quantized, in two launches ordered on
+ * `stream` with no host synchronisation. Trace results are identical to a rebuild's (the hit
+ * rule does not depend on the tree); traversal cost grows as instances drift from the build's
+ * layout, so callers rebuild now and then. When the set of instances in the tree changes
+ * (visibility, or a mesh without triangles) it rebuilds instead. */
+int  gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances,
+                                uint32_t count, void* stream);
 
 /* Acceleration structures (RayTraceBaseRenderer::CreateBottomLevelStructures /
  * CreateTopLevelStructures, RayTraceBaseRenderer.cpp:276-386; TLAS update :205-218).
