@@ -442,7 +442,7 @@ def run_gkrt(args):
                 t.append(time.perf_counter() - t0)
             r.synchronize(stream)
             return sum(t) / len(t) * 1e3
-        rebuild_host = call_host_ms(r.update_instances, range(Wm, Wm + 3))
+        rebuild_host = call_host_ms(r.update_instances, [Wm + i % K for i in range(3)])
         r.update_instances(insts[0], stream)        # the tree of frame 0's layout; refits from here on
         refit_host = call_host_ms(r.refit_instances, range(1, Wm))
         for i in range(1, Wm):
@@ -500,6 +500,27 @@ def run_gkrt(args):
         probe_ms = {"voxelize_grid": e0.elapsed_time(e1), "bake_slice_f120": e1.elapsed_time(e2),
                     "bake_grid": e2.elapsed_time(e3), "slice_probes": per * 64, "grid_probes": r.PROBE_COUNT}
 
+    # ---- output stage: the denoised frame onto a 4K presentation image (mean of 20 launches) ----
+    output_ms = None
+    if WORKLOAD == "bricks" and rank == 0:
+        r.output_resize(3840, 2160)
+        res = {}
+        for name, mode, size in (("resolve_to_3840x2160", abi.OUTPUT_RESOLVE, (3840, 2160)),
+                                 ("fsr_to_3840x2160", abi.OUTPUT_FSR, (3840, 2160))):
+            r.output_pass(mode, (0, 0), size, stream=stream)
+            r.synchronize(stream)
+            o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                o0.record()
+                for _ in range(20):
+                    r.output_pass(mode, (0, 0), size, stream=stream)
+                o1.record()
+            r.synchronize(stream)
+            res[name] = o0.elapsed_time(o1) / 20
+        res["store_gbs_resolve"] = 3840 * 2160 * 4 / (res["resolve_to_3840x2160"] * 1e-3) / 1e9
+        output_ms = res
+        r.output_resize(0, 0)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": Wm,
                 "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -508,6 +529,7 @@ def run_gkrt(args):
                 "trace_pass_mrays_s": rays / max(K, 1) / world / (trace_avg_ms * 1e-3) / 1e6,
                 "gpu_launches": 3 * K + 2 * K * (fcs[0].denoiser == abi.DENOISE_ATROUS) + build_launches,
                 "probe_ms": probe_ms,
+                "output_ms": output_ms,
                 "tlas_refit": refit,
                 "bvh_build_ms": {"all_levels": build_all_ms, "instance_level": build_inst_ms,
                                  "scene_load_s": load_s, "triangles": int(sc.triangle_count),

@@ -58,7 +58,8 @@ IMG_HIT_INST = 17
 IMG_HIT_PRIM = 18
 IMG_COUNT = 19
 
-FMT_F32X4, FMT_F32X2, FMT_F32, FMT_U32 = range(4)
+FMT_F32X4, FMT_F32X2, FMT_F32, FMT_U32, FMT_BGRA8 = range(5)
+OUTPUT_RESOLVE, OUTPUT_FSR = 0, 1
 
 # (numpy dtype, channels) of each image, as the library allocates them
 IMAGE_FORMATS = {
@@ -147,6 +148,11 @@ class GkrtFrameConstants(C.Structure):
 class GkrtImageView(C.Structure):
     _fields_ = [("device_ptr", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("pitch_bytes", C.c_uint32), ("format", C.c_uint32)]
+
+
+class GkrtOutputDesc(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("offset_x", C.c_int32), ("offset_y", C.c_int32), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("source_image", C.c_uint32)]
 
 
 class GkrtDeviceDesc(C.Structure):

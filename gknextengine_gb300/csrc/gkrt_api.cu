@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -38,6 +39,8 @@ struct GkrtContext {
     uint32_t W = 0, H = 0, P = 0;     // P: row pitch in pixels (W rounded up to 4: 16-byte rows)
     void* img[GKRT_IMG_COUNT] = {};
     float4* atrous_tmp[2] = {nullptr, nullptr};   // ping-pong of the a-trous passes
+    uint32_t* d_output = nullptr;     // presentation image, OW x OH BGRA8 words (gkrt_output_resize)
+    uint32_t OW = 0, OH = 0;
 
     bool has_scene = false;
     std::vector<GkrtMesh> meshes;
@@ -827,6 +830,7 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     ctx->unet = nullptr;
     gpu_bvh_free(ctx->builder);
     ctx->builder = nullptr;
+    dfree(ctx->d_output);
     for (StageSlot& S : ctx->stage)
         for (int k = 0; k < 2; ++k) {
             if (S.p[k]) cudaFreeHost(S.p[k]);
@@ -1169,6 +1173,89 @@ int gkrt_copy_image_to_host_async(GkrtContext* ctx, int id, void* dst, size_t ds
     GK_CUDA(cudaMemcpy2DAsync(dst, row, v.device_ptr, v.pitch_bytes, row, v.height, cudaMemcpyDeviceToHost,
                               (cudaStream_t)stream));
     return GKRT_OK;
+}
+
+int gkrt_output_resize(GkrtContext* ctx, uint32_t width, uint32_t height) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if ((width == 0) != (height == 0) || width > 16384 || height > 16384)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "output size must be 1..16384 (or 0 x 0 to free)");
+    cudaSetDevice(ctx->device);
+    GK_CUDA(cudaDeviceSynchronize());
+    dfree(ctx->d_output);
+    ctx->OW = ctx->OH = 0;
+    if (width == 0) return GKRT_OK;
+    const size_t bytes = (size_t)width * height * 4;
+    GK_CUDA(cudaMalloc((void**)&ctx->d_output, bytes));
+    GK_CUDA(cudaMemset(ctx->d_output, 0, bytes));
+    ctx->OW = width;
+    ctx->OH = height;
+    return GKRT_OK;
+}
+
+int gkrt_output_pass(GkrtContext* ctx, const GkrtOutputDesc* d, void* stream) {
+    if (!ctx || !d) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->d_output) return fail(ctx, GKRT_ERR_STATE, "gkrt_output_resize was not called");
+    if (ctx->W == 0) return fail(ctx, GKRT_ERR_STATE, "gkrt_resize was not called");
+    if (d->mode != GKRT_OUTPUT_RESOLVE && d->mode != GKRT_OUTPUT_FSR)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown output mode");
+    if (d->source_image >= GKRT_IMG_COUNT || image_format((int)d->source_image) != GKRT_FMT_F32X4)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "output source must be an RGBA32F image");
+    if (d->width == 0 || d->height == 0 || d->width > 65536 || d->height > 65536)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "output rectangle must be 1..65536 a side");
+    if (std::abs((long long)d->offset_x) > 65536 || std::abs((long long)d->offset_y) > 65536)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "output offset beyond +-65536");
+    cudaSetDevice(ctx->device);
+    const float4* src = static_cast<const float4*>(ctx->img[d->source_image]);
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (d->mode == GKRT_OUTPUT_RESOLVE)
+        GK_CUDA(gkrt_launch_output_resolve(src, (int)ctx->W, (int)ctx->H, (int)ctx->P, ctx->d_output, (int)ctx->OW,
+                                           (int)ctx->OH, d->offset_x, d->offset_y, (int)d->width, (int)d->height, st));
+    else
+        GK_CUDA(gkrt_launch_output_fsr(src, (int)ctx->W, (int)ctx->H, (int)ctx->P, ctx->d_output, (int)ctx->OW,
+                                       (int)ctx->OH, d->offset_x, d->offset_y, (int)d->width, (int)d->height, st));
+    return GKRT_OK;
+}
+
+int gkrt_get_output(GkrtContext* ctx, GkrtImageView* out) {
+    if (!ctx || !out) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->d_output) return fail(ctx, GKRT_ERR_STATE, "gkrt_output_resize was not called");
+    out->device_ptr = ctx->d_output;
+    out->width = ctx->OW;
+    out->height = ctx->OH;
+    out->pitch_bytes = ctx->OW * 4;
+    out->format = GKRT_FMT_BGRA8;
+    return GKRT_OK;
+}
+
+int gkrt_copy_output_to_host(GkrtContext* ctx, void* dst, size_t dst_bytes, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->d_output) return fail(ctx, GKRT_ERR_STATE, "gkrt_output_resize was not called");
+    const size_t bytes = (size_t)ctx->OW * ctx->OH * 4;
+    if (!dst || dst_bytes < bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
+    cudaSetDevice(ctx->device);
+    GK_CUDA(cudaMemcpyAsync(dst, ctx->d_output, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    return gkrt_synchronize(ctx, stream);
+}
+
+int gkrt_screenshot(GkrtContext* ctx, uint32_t x, uint32_t y, uint32_t width, uint32_t height, void* dst,
+                    size_t dst_bytes, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->d_output) return fail(ctx, GKRT_ERR_STATE, "gkrt_output_resize was not called");
+    if (width == 0 || height == 0 || (uint64_t)x + width > ctx->OW || (uint64_t)y + height > ctx->OH)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "screenshot crop must lie inside the presentation image");
+    const size_t bytes = (size_t)width * height * 3;
+    if (!dst || dst_bytes < bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the crop");
+    cudaSetDevice(ctx->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    uint8_t* d_rgb = nullptr;
+    GK_CUDA(cudaMallocAsync((void**)&d_rgb, bytes, st));
+    cudaError_t e = gkrt_launch_screenshot(ctx->d_output, (int)ctx->OW, (int)x, (int)y, (int)width, (int)height, d_rgb,
+                                           st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, d_rgb, bytes, cudaMemcpyDeviceToHost, st);
+    const cudaError_t ef = cudaFreeAsync(d_rgb, st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "screenshot");
+    if (ef != cudaSuccess) return cuda_fail(ctx, ef, "cudaFreeAsync(screenshot)");
+    return gkrt_synchronize(ctx, stream);
 }
 
 int gkrt_upload_image(GkrtContext* ctx, int id, const void* src, size_t src_bytes, void* stream) {

@@ -141,6 +141,17 @@ cudaError_t gpu_bvh_refit_instances(const RefitLinks& links, const GpuInstBox* i
                                     uint32_t* err, uint32_t err_bit, cudaStream_t st);
 }  // namespace gk
 
+// Output stage (k_output.cu): src the tone-mapped image (W x H, pitch P pixels) into the
+// presentation image out (OW x OH BGRA8 words). Resolve: linear blit onto the rectangle at
+// (ox, oy) of ow x oh. FSR: the EASU compose with push constants offset and output size.
+cudaError_t gkrt_launch_output_resolve(const float4* src, int W, int H, int P, uint32_t* out, int OW, int OH, int ox,
+                                       int oy, int ow, int oh, cudaStream_t st);
+cudaError_t gkrt_launch_output_fsr(const float4* src, int W, int H, int P, uint32_t* out, int OW, int OH, int offx,
+                                   int offy, int outw, int outh, cudaStream_t st);
+// rgb: w x h x 3 bytes of the crop at (x0, y0), which lies inside the OW-wide image
+cudaError_t gkrt_launch_screenshot(const uint32_t* img, int OW, int x0, int y0, int w, int h, uint8_t* rgb,
+                                   cudaStream_t st);
+
 // stack_words: traversal stack entries per thread, at least the scene's two-child depth bound
 // (mesh depth + instance depth + 3) and at most kStackSize.
 cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,

@@ -52,6 +52,11 @@ def load(path: str | None = None):
     L.gkrt_trace_rays.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_trace_rays_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
+    L.gkrt_output_resize.argtypes = [vp, C.c_uint32, C.c_uint32]
+    L.gkrt_output_pass.argtypes = [vp, C.POINTER(abi.GkrtOutputDesc), vp]
+    L.gkrt_get_output.argtypes = [vp, C.POINTER(abi.GkrtImageView)]
+    L.gkrt_copy_output_to_host.argtypes = [vp, vp, C.c_size_t, vp]
+    L.gkrt_screenshot.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, C.c_size_t, vp]
     L.gkrt_probe_voxelize.argtypes = [vp, vp]
     L.gkrt_probe_bake.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, C.c_uint32, vp]
     L.gkrt_probe_download.argtypes = [vp, vp, vp]
@@ -84,6 +89,8 @@ EXPORTED = [
     "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_scene_refit_instances",
     "gkrt_build_bvh",
     "gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_end_frame", "gkrt_render_frame",
+    "gkrt_output_resize", "gkrt_output_pass", "gkrt_get_output", "gkrt_copy_output_to_host",
+    "gkrt_screenshot",
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_copy_image_to_host_async", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
     "gkrt_get_stats", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",
     "gkrt_synchronize", "gkrt_affine_inverse",

@@ -130,6 +130,47 @@ class PathTracingRenderer:
                                                       self._stream(stream)))
         return out
 
+    # ---- output stage: the presentation image (headless swapchain image, 8-bit BGRA) ----
+    def output_resize(self, width: int, height: int):
+        """SwapChain extent: (re)allocates the presentation image, black."""
+        self._check(self._lib.gkrt_output_resize(self._h, width, height))
+        self.output_width, self.output_height = int(width), int(height)
+
+    def output_pass(self, mode=abi.OUTPUT_RESOLVE, offset=(0, 0), size=None, source=abi.IMG_DENOISED, stream=None):
+        """Resolve (linear blit onto the rectangle offset + size, default the whole presentation
+        image) or FSR compose (Process.UpScaleFSR: offset and size are its push constants)."""
+        w, h = size if size is not None else (self.output_width, self.output_height)
+        d = abi.GkrtOutputDesc(mode, int(offset[0]), int(offset[1]), int(w), int(h), int(source))
+        self._check(self._lib.gkrt_output_pass(self._h, C.byref(d), self._stream(stream)))
+
+    def read_output(self, stream=None) -> np.ndarray:
+        """The presentation image as (height, width, 4) bytes B, G, R, A."""
+        out = np.empty((self.output_height, self.output_width, 4), np.uint8)
+        self._check(self._lib.gkrt_copy_output_to_host(self._h, out.ctypes.data, out.nbytes, self._stream(stream)))
+        return out
+
+    def save_screenshot(self, path: str, x=0, y=0, width=None, height=None, stream=None) -> np.ndarray:
+        """ScreenShot::SaveSwapChainToFileFast: the crop written as an 8-bit RGB PNG."""
+        from . import imageio
+        rgb = self.screenshot(x, y, width, height, stream)
+        imageio.write_png(path, rgb)
+        return rgb
+
+    def save_hdr(self, path: str, image_id=abi.IMG_DENOISED_LINEAR, stream=None) -> np.ndarray:
+        """A linear float image written as PFM (the HDR dump in place of ScreenShot.cpp's AVIF)."""
+        from . import imageio
+        img = self.read_image(image_id, stream)
+        imageio.write_pfm(path, img)
+        return img
+
+    def screenshot(self, x=0, y=0, width=None, height=None, stream=None) -> np.ndarray:
+        """ScreenShot::SaveSwapChainToFileFast's crop: (height, width, 3) bytes R, G, B."""
+        w = self.output_width - x if width is None else width
+        h = self.output_height - y if height is None else height
+        out = np.empty((h, w, 3), np.uint8)
+        self._check(self._lib.gkrt_screenshot(self._h, x, y, w, h, out.ctypes.data, out.nbytes, self._stream(stream)))
+        return out
+
     def read_image_async(self, image_id: int, out: np.ndarray, stream=None) -> np.ndarray:
         """The copy of read_image ordered on stream without waiting (out: page-locked memory for
         the copy to overlap other work; synchronize before reading it)."""

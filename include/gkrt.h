@@ -302,6 +302,38 @@ int  gkrt_end_frame(GkrtContext* ctx, void* stream);                            
 /* All four in order: the whole Render() of the path-tracing logic renderer. */
 int  gkrt_render_frame(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream);
 
+/* Output stage: the presentation image, a headless device buffer of width x height 8-bit BGRA
+ * words (byte order B, G, R, A) in place of the reference's B8G8R8A8_UNORM swapchain image
+ * (SwapChain.cpp). Values convert as a UNORM store does: clamp to [0, 1] (NaN to 0), x 255,
+ * round to nearest even. */
+#define GKRT_FMT_BGRA8  4
+#define GKRT_OUTPUT_RESOLVE 0   /* linear blit of the image onto the rectangle (offset, width x height):
+                                   the resolve pass, VulkanBaseRenderer.cpp:1036-1068                 */
+#define GKRT_OUTPUT_FSR     1   /* Process.UpScaleFSR.comp.slang: EASU from the render size to the
+                                   presentation size when they differ, else a nearest copy; pixels
+                                   [0, width/8*8) x [0, height/8*8) written at + offset; offset, width,
+                                   height are its push constants (VulkanBaseRenderer.cpp:958-986)      */
+typedef struct GkrtOutputDesc {
+    uint32_t mode;              /* GKRT_OUTPUT_*                                              */
+    int32_t  offset_x, offset_y;
+    uint32_t width, height;
+    uint32_t source_image;      /* image id read, normally GKRT_IMG_DENOISED                  */
+} GkrtOutputDesc;
+/* (Re)allocate the presentation image (SwapChain extent); contents start black (all zero).
+ * width = height = 0 frees it. */
+int  gkrt_output_resize(GkrtContext* ctx, uint32_t width, uint32_t height);
+/* One output pass on `stream`; pixels outside the presentation image are not written. */
+int  gkrt_output_pass(GkrtContext* ctx, const GkrtOutputDesc* desc, void* stream);
+int  gkrt_get_output(GkrtContext* ctx, GkrtImageView* out);
+/* The whole presentation image to host memory (width x height x 4 bytes); waits for `stream`. */
+int  gkrt_copy_output_to_host(GkrtContext* ctx, void* dst, size_t dst_bytes, void* stream);
+/* ScreenShot::SaveSwapChainToFileFast (ScreenShot.cpp:18-79): the crop (x, y, width, height) of
+ * the presentation image as width x height x 3 bytes R, G, B, rows top to bottom, into dst (host
+ * memory); waits for `stream`. The crop must lie inside the image. Encoding to a file is the
+ * caller's (the Python layer writes PNG). */
+int  gkrt_screenshot(GkrtContext* ctx, uint32_t x, uint32_t y, uint32_t width, uint32_t height,
+                     void* dst, size_t dst_bytes, void* stream);
+
 /* Outputs (bindless storage images, BindlessTexture.slang:8-40). */
 int  gkrt_get_image(GkrtContext* ctx, int image_id, GkrtImageView* out);
 int  gkrt_copy_image_to_host(GkrtContext* ctx, int image_id, void* dst, size_t dst_bytes, void* stream);

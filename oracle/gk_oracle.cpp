@@ -1514,6 +1514,185 @@ void bake_probe(const OScene& S, const GkrtFrameConstants& fc, uint32_t g, const
     out[13] = sky[2] | (sky[3] << 8) | (sun << 16) | (prev[13] & 0xFF000000u);
 }
 
+// ================================ output stage ========================================
+// The presentation image as 8-bit BGRA words (the reference's B8G8R8A8_UNORM swapchain image).
+// A UNORM store clamps to [0, 1] (NaN to 0), scales by 255 and rounds to nearest even.
+
+static uint32_t unorm8_o(float v) {
+    v = std::fmin(std::fmax(v, 0.0f), 1.0f);
+    return (uint32_t)std::nearbyint(v * 255.0f);
+}
+static uint32_t bgra_o(const float* c) {
+    return unorm8_o(c[2]) | (unorm8_o(c[1]) << 8) | (unorm8_o(c[0]) << 16) | (unorm8_o(c[3]) << 24);
+}
+
+// Resolve pass: vkCmdBlitImage with VK_FILTER_LINEAR from the render extent onto the rectangle
+// (ox, oy, ow, oh) (VulkanBaseRenderer.cpp:1036-1068). The Vulkan specification's scaled-blit
+// rule: destination centre x + 0.5 -> u = (x - ox + 0.5) * W / ow, then a linear filter with
+// clamp-to-edge: texels floor(u - 0.5) and the next, weights 1 - a and a, a = frac(u - 0.5).
+static void output_resolve_o(const float* src, int W, int H, int P, uint32_t* out, int OW, int OH, int ox, int oy,
+                             int ow, int oh) {
+    const float su = (float)W / (float)ow, sv = (float)H / (float)oh;
+    const long long xa = std::max<long long>(ox, 0), xb = std::min<long long>((long long)ox + ow, OW);
+    const long long ya = std::max<long long>(oy, 0), yb = std::min<long long>((long long)oy + oh, OH);
+    for (long long y = ya; y < yb; ++y)
+        for (long long x = xa; x < xb; ++x) {
+            const float u = ((float)(x - ox) + 0.5f) * su - 0.5f;
+            const float v = ((float)(y - oy) + 0.5f) * sv - 0.5f;
+            const float fu = std::floor(u), fv = std::floor(v);
+            const float a = u - fu, b = v - fv;
+            const int i0 = (int)fu, j0 = (int)fv;
+            const int i[2] = {std::min(std::max(i0, 0), W - 1), std::min(std::max(i0 + 1, 0), W - 1)};
+            const int j[2] = {std::min(std::max(j0, 0), H - 1), std::min(std::max(j0 + 1, 0), H - 1)};
+            const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+            float c[4];
+            for (int k = 0; k < 4; ++k) {
+                const float t00 = src[4 * ((size_t)j[0] * P + i[0]) + k], t10 = src[4 * ((size_t)j[0] * P + i[1]) + k];
+                const float t01 = src[4 * ((size_t)j[1] * P + i[0]) + k], t11 = src[4 * ((size_t)j[1] * P + i[1]) + k];
+                c[k] = ((t00 * w00 + t10 * w10) + t01 * w01) + t11 * w11;
+            }
+            out[(size_t)y * OW + x] = bgra_o(c);
+        }
+}
+
+// Process.UpScaleFSR.comp.slang: FsrEasuCF (:23-29), FsrEasuTapF (:74-101), FsrEasuSetF (:105-132),
+// FsrEasuCon (:32-72), FsrEasuF (:135-248), main (:264-299). rsqrt as 1 / sqrt.
+namespace easu_o {
+struct V4 { float v[4]; };
+struct Img { const float* p; int W, H, P; };
+static V4 tex(const Img& s, int x, int y) {
+    V4 r;
+    for (int k = 0; k < 4; ++k) r.v[k] = s.p[4 * ((size_t)y * s.P + x) + k];
+    return r;
+}
+static V4 cf(const Img& s, float px, float py) {   // FsrEasuCF: int(p * size), clamped
+    int cx = (int)(px * (float)s.W), cy = (int)(py * (float)s.H);
+    cx = std::min(std::max(cx, 0), s.W - 1);
+    cy = std::min(std::max(cy, 0), s.H - 1);
+    return tex(s, cx, cy);
+}
+static float luma(const V4& c) { return c.v[1] + 0.5f * (c.v[0] + c.v[2]); }
+static float sat(float x) { return std::fmin(std::fmax(x, 0.0f), 1.0f); }
+static void setf(float& dx, float& dy, float& len, float w, float lA, float lB, float lC, float lD, float lE) {
+    float lenX = std::fmax(std::fabs(lD - lC), std::fabs(lC - lB));
+    float dirX = lD - lB;
+    dx += dirX * w;
+    lenX = sat(std::fabs(dirX) / lenX);
+    lenX *= lenX;
+    len += lenX * w;
+    float lenY = std::fmax(std::fabs(lE - lC), std::fabs(lC - lA));
+    float dirY = lE - lA;
+    dy += dirY * w;
+    lenY = sat(std::fabs(dirY) / lenY);
+    lenY *= lenY;
+    len += lenY * w;
+}
+static void tapf(V4& aC, float& aW, float offx, float offy, float dx, float dy, float lx, float ly, float lob,
+                 float clp, const V4& c) {
+    float vx = offx * dx + offy * dy;
+    float vy = offx * (-dy) + offy * dx;
+    vx *= lx;
+    vy *= ly;
+    float d2 = std::fmin(vx * vx + vy * vy, clp);
+    float wB = 0.4f * d2 - 1.0f;
+    float wA = lob * d2 - 1.0f;
+    wB *= wB;
+    wA *= wA;
+    wB = 1.5625f * wB - 0.5625f;
+    float w = wB * wA;
+    for (int k = 0; k < 4; ++k) aC.v[k] += c.v[k] * w;
+    aW += w;
+}
+static V4 easu(const Img& s, float OWf, float OHf, float ipx, float ipy) {
+    const float Wf = (float)s.W, Hf = (float)s.H;
+    // FsrEasuCon(con0..3, viewport = input = W x H, output = OW x OH)
+    const float con0[4] = {Wf / OWf, Hf / OHf, 0.5f * Wf / OWf - 0.5f, 0.5f * Hf / OHf - 0.5f};
+    const float con1[4] = {1.0f / Wf, 1.0f / Hf, 1.0f / Wf, -1.0f / Hf};
+    const float con2[4] = {-1.0f / Wf, 2.0f / Hf, 1.0f / Wf, 2.0f / Hf};
+    const float con3[2] = {0.0f / Wf, 4.0f / Hf};
+    float ppx = ipx * con0[0] + con0[2], ppy = ipy * con0[1] + con0[3];
+    const float fpx = std::floor(ppx), fpy = std::floor(ppy);
+    ppx -= fpx;
+    ppy -= fpy;
+    const float p0x = fpx * con1[0] + con1[2], p0y = fpy * con1[1] + con1[3];
+    const float p1x = p0x + con2[0], p1y = p0y + con2[1];
+    const float p2x = p0x + con2[2], p2y = p0y + con2[3];
+    const float p3x = p0x + con3[0], p3y = p0y + con3[1];
+    const float off[4] = {-0.5f * con1[0], 0.5f * con1[0], -0.5f * con1[1], 0.5f * con1[1]};   // x y z w
+    const V4 bC = cf(s, p0x + off[0], p0y + off[3]), cC = cf(s, p0x + off[1], p0y + off[3]);
+    const V4 iC = cf(s, p1x + off[0], p1y + off[3]), jC = cf(s, p1x + off[1], p1y + off[3]);
+    const V4 fC = cf(s, p1x + off[1], p1y + off[2]), eC = cf(s, p1x + off[0], p1y + off[2]);
+    const V4 kC = cf(s, p2x + off[0], p2y + off[3]), lC = cf(s, p2x + off[1], p2y + off[3]);
+    const V4 hC = cf(s, p2x + off[1], p2y + off[2]), gC = cf(s, p2x + off[0], p2y + off[2]);
+    const V4 oC = cf(s, p3x + off[1], p3y + off[2]), nC = cf(s, p3x + off[0], p3y + off[2]);
+    const float bL = luma(bC), cL = luma(cC), iL = luma(iC), jL = luma(jC), fL = luma(fC), eL = luma(eC);
+    const float kL = luma(kC), lL = luma(lC), hL = luma(hC), gL = luma(gC), oL = luma(oC), nL = luma(nC);
+    float dx = 0.0f, dy = 0.0f, len = 0.0f;
+    setf(dx, dy, len, (1.0f - ppx) * (1.0f - ppy), bL, eL, fL, gL, jL);
+    setf(dx, dy, len, ppx * (1.0f - ppy), cL, fL, gL, hL, kL);
+    setf(dx, dy, len, (1.0f - ppx) * ppy, fL, iL, jL, kL, nL);
+    setf(dx, dy, len, ppx * ppy, gL, jL, kL, lL, oL);
+    const float d2x = dx * dx, d2y = dy * dy;
+    float dirR = d2x + d2y;
+    const bool zro = dirR < (1.0f / 32768.0f);
+    dirR = 1.0f / std::sqrt(dirR);
+    dirR = zro ? 1.0f : dirR;
+    dx = zro ? 1.0f : dx;
+    dx *= dirR;
+    dy *= dirR;
+    len = len * 0.5f;
+    len *= len;
+    const float stretch = (dx * dx + dy * dy) / std::fmax(std::fabs(dx), std::fabs(dy));
+    const float l2x = 1.0f + (stretch - 1.0f) * len, l2y = 1.0f - 0.5f * len;
+    const float lob = 0.5f - 0.29f * len;
+    const float clp = 1.0f / lob;
+    V4 mn, mx;
+    for (int k = 0; k < 4; ++k) {
+        mn.v[k] = std::fmin(std::fmin(fC.v[k], gC.v[k]), std::fmin(jC.v[k], kC.v[k]));
+        mx.v[k] = std::fmax(std::fmax(fC.v[k], gC.v[k]), std::fmax(jC.v[k], kC.v[k]));
+    }
+    V4 aC = {{0.0f, 0.0f, 0.0f, 0.0f}};
+    float aW = 0.0f;
+    tapf(aC, aW, 0.0f - ppx, -1.0f - ppy, dx, dy, l2x, l2y, lob, clp, bC);
+    tapf(aC, aW, 1.0f - ppx, -1.0f - ppy, dx, dy, l2x, l2y, lob, clp, cC);
+    tapf(aC, aW, -1.0f - ppx, 1.0f - ppy, dx, dy, l2x, l2y, lob, clp, iC);
+    tapf(aC, aW, 0.0f - ppx, 1.0f - ppy, dx, dy, l2x, l2y, lob, clp, jC);
+    tapf(aC, aW, 0.0f - ppx, 0.0f - ppy, dx, dy, l2x, l2y, lob, clp, fC);
+    tapf(aC, aW, -1.0f - ppx, 0.0f - ppy, dx, dy, l2x, l2y, lob, clp, eC);
+    tapf(aC, aW, 1.0f - ppx, 1.0f - ppy, dx, dy, l2x, l2y, lob, clp, kC);
+    tapf(aC, aW, 2.0f - ppx, 1.0f - ppy, dx, dy, l2x, l2y, lob, clp, lC);
+    tapf(aC, aW, 2.0f - ppx, 0.0f - ppy, dx, dy, l2x, l2y, lob, clp, hC);
+    tapf(aC, aW, 1.0f - ppx, 0.0f - ppy, dx, dy, l2x, l2y, lob, clp, gC);
+    tapf(aC, aW, 1.0f - ppx, 2.0f - ppy, dx, dy, l2x, l2y, lob, clp, oC);
+    tapf(aC, aW, 0.0f - ppx, 2.0f - ppy, dx, dy, l2x, l2y, lob, clp, nC);
+    V4 r;
+    for (int k = 0; k < 4; ++k) r.v[k] = std::fmin(mx.v[k], std::fmax(mn.v[k], aC.v[k] / aW));
+    return r;
+}
+}  // namespace easu_o
+
+static void output_fsr_o(const float* src, int W, int H, int P, uint32_t* out, int OW, int OH, int offx, int offy,
+                         int outw, int outh) {
+    const easu_o::Img s{src, W, H, P};
+    const int gw = (outw / 8) * 8, gh = (outh / 8) * 8;   // vkCmdDispatch(outw / 8, outh / 8) of 8 x 8 groups
+    for (int y = 0; y < gh; ++y)
+        for (int x = 0; x < gw; ++x) {
+            easu_o::V4 c;
+            if (OW != W || OH != H) {
+                const float uvx = (float)x / (float)outw, uvy = (float)y / (float)outh;
+                c = easu_o::easu(s, (float)OW, (float)OH, uvx * (float)OW, uvy * (float)OH);
+            } else {
+                int sx = (int)((float)x * (float)OW / (float)outw), sy = (int)((float)y * (float)OH / (float)outh);
+                sx = std::min(std::max(sx, 0), W - 1);
+                sy = std::min(std::max(sy, 0), H - 1);
+                c = easu_o::tex(s, sx, sy);
+            }
+            const long long dx = (long long)x + offx, dy = (long long)y + offy;
+            if (dx < 0 || dy < 0 || dx >= OW || dy >= OH) continue;
+            out[(size_t)dy * OW + (size_t)dx] = bgra_o(c.v);
+        }
+}
+
 // ===================================== C API ==========================================
 extern "C" {
 
@@ -1718,6 +1897,27 @@ void gko_denoise_pass(const GkrtFrameConstants* fc, int W, int H, void** images,
 }
 
 void gko_set_fast(int on) { g_fast = on; }
+
+// Output stage on a W x H RGBA32F image (pitch P pixels) into OW x OH BGRA8 words.
+void gko_output_resolve(const float* src, int W, int H, int P, uint32_t* out, int OW, int OH, int ox, int oy, int ow,
+                        int oh) {
+    output_resolve_o(src, W, H, P, out, OW, OH, ox, oy, ow, oh);
+}
+void gko_output_fsr(const float* src, int W, int H, int P, uint32_t* out, int OW, int OH, int offx, int offy,
+                    int outw, int outh) {
+    output_fsr_o(src, W, H, P, out, OW, OH, offx, offy, outw, outh);
+}
+// ScreenShot::SaveSwapChainToFileFast (ScreenShot.cpp:18-79): bytes (bits 16, 8, 0) of each word.
+void gko_screenshot(const uint32_t* img, int OW, int x0, int y0, int w, int h, uint8_t* rgb) {
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const uint32_t p = img[(size_t)(y0 + y) * OW + (x0 + x)];
+            uint8_t* d = rgb + 3 * ((size_t)y * w + x);
+            d[0] = (uint8_t)((p >> 16) & 0xFFu);
+            d[1] = (uint8_t)((p >> 8) & 0xFFu);
+            d[2] = (uint8_t)(p & 0xFFu);
+        }
+}
 
 // Probe voxelization of probes [first, first + count): 4 words each into out.
 void gko_probe_voxelize(void* s, uint32_t first, uint32_t count, uint32_t* out, int threads) {

@@ -68,6 +68,9 @@ def lib():
         L.gko_gt_tonemap.restype = C.c_float
         L.gko_gt_tonemap.argtypes = [C.c_float]
         L.gko_set_fast.argtypes = [C.c_int]
+        for n in ("gko_output_resolve", "gko_output_fsr"):
+            getattr(L, n).argtypes = [C.c_void_p] + [C.c_int] * 3 + [C.c_void_p] + [C.c_int] * 6
+        L.gko_screenshot.argtypes = [C.c_void_p] + [C.c_int] * 5 + [C.c_void_p]
         L.gko_probe_voxelize.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int]
         L.gko_probe_bake.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, C.c_uint32,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
@@ -161,6 +164,37 @@ def reproject_pass(fc, width, height, images, threads=0):
 
 def denoise_pass(fc, width, height, images, threads=0):
     lib().gko_denoise_pass(C.byref(fc), width, height, _ptrs(images), threads)
+
+
+def _output(fn, src, out_w, out_h, a, b, c, d, out=None):
+    src = np.ascontiguousarray(src, np.float32)
+    H, W = src.shape[:2]
+    if out is None:
+        out = np.zeros((out_h, out_w), np.uint32)
+    assert out.dtype == np.uint32 and out.shape == (out_h, out_w) and out.flags["C_CONTIGUOUS"]
+    fn(src.ctypes.data, W, H, W, out.ctypes.data, out_w, out_h, a, b, c, d)
+    return out
+
+
+def output_resolve(src, out_w, out_h, offset=(0, 0), size=None, out=None):
+    """The resolve pass (linear blit) of an (H, W, 4) float image onto the rectangle offset +
+    size of an out_w x out_h presentation image of BGRA8 words (uint32 (out_h, out_w))."""
+    w, h = size if size is not None else (out_w, out_h)
+    return _output(lib().gko_output_resolve, src, out_w, out_h, offset[0], offset[1], w, h, out)
+
+
+def output_fsr(src, out_w, out_h, offset=(0, 0), size=None, out=None):
+    """Process.UpScaleFSR.comp.slang with push constants offset and size (output_w, output_h)."""
+    w, h = size if size is not None else (out_w, out_h)
+    return _output(lib().gko_output_fsr, src, out_w, out_h, offset[0], offset[1], w, h, out)
+
+
+def screenshot(img, x, y, w, h):
+    """ScreenShot.cpp's crop of a BGRA8 presentation image as (h, w, 3) bytes R, G, B."""
+    img = np.ascontiguousarray(img, np.uint32)
+    out = np.empty((h, w, 3), np.uint8)
+    lib().gko_screenshot(img.ctypes.data, img.shape[1], x, y, w, h, out.ctypes.data)
+    return out
 
 
 def end_frame(images):
