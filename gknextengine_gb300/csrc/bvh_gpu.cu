@@ -689,15 +689,16 @@ __device__ bool wide_axis(const WEnt* e, int n, int ax, float& origin, uint32_t&
     if (range > 0.0) ex = max(ex, ilogb(range / 253.0));
     if (lo != 0.0f) ex = max(ex, ilogb(fabs((double)lo)) - 21);
     for (; ex <= 38; ++ex) {
-        const double s = ldexp(1.0, ex);
-        const double k = floor((double)lo / s) - 1.0;
+        // x / 2^ex as x * 2^-ex: exact for a float x and -100 <= ex <= 38 (no double underflow)
+        const double s = ldexp(1.0, ex), rs = ldexp(1.0, -ex);
+        const double k = floor((double)lo * rs) - 1.0;
         if (fabs(k) >= 4194304.0) continue;   // |k| < 2^22
         bool ok = true;
-        for (int i = 0; i < n; ++i) ok = ok && (ceil((double)e[i].b[3 + ax] / s) + 1.0 - k <= 255.0);
+        for (int i = 0; i < n; ++i) ok = ok && (ceil((double)e[i].b[3 + ax] * rs) + 1.0 - k <= 255.0);
         if (!ok) continue;
         for (int i = 0; i < n; ++i) {
-            qlo[i] = (uint32_t)(floor((double)e[i].b[ax] / s) - 1.0 - k);
-            qhi[i] = (uint32_t)(ceil((double)e[i].b[3 + ax] / s) + 1.0 - k);
+            qlo[i] = (uint32_t)(floor((double)e[i].b[ax] * rs) - 1.0 - k);
+            qhi[i] = (uint32_t)(ceil((double)e[i].b[3 + ax] * rs) + 1.0 - k);
         }
         origin = (float)(k * s);
         ebyte = (uint32_t)(ex + 127);
@@ -1256,7 +1257,8 @@ cudaError_t gpu_bvh_refit_instances(const RefitLinks& lk, const GpuInstBox* inst
                                     BvhNode* nodes, float* ubox, uint32_t* arrive, WideNode* wide, uint32_t nw,
                                     uint32_t* err, uint32_t err_bit, cudaStream_t st) {
     if (lk.ninst) k_refit_boxes<<<(lk.ninst + 127) / 128, 128, 0, st>>>(lk, inst, mesh_box, nodes, ubox, arrive);
-    if (nw) k_refit_wide<<<(nw + 127) / 128, 128, 0, st>>>(lk, nodes, wide, nw, err, err_bit);
+    // a few thousand nodes: 32-thread blocks spread them over the SMs (FP64 latency-bound)
+    if (nw) k_refit_wide<<<(nw + 31) / 32, 32, 0, st>>>(lk, nodes, wide, nw, err, err_bit);
     return cudaGetLastError();
 }
 
