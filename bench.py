@@ -40,7 +40,7 @@ HIT_FETCH_BYTES = 3 * 4 + 3 * 16 + 64 + 64 + 48   # indices, normals, material, 
 NODE_BYTES, TRI_BYTES, RAY_BYTES = 64, 48, 32
 # DRAM bytes (read + write) of one 1080p trace launch of the default workload, from one ncu
 # capture; the node and triangle reads above are served by L1/L2
-TRACE_DRAM_BYTES_1080P = 7485696 + 117612544
+TRACE_DRAM_BYTES_1080P = 9999872 + 133538304
 
 
 WORKLOAD = "bricks"
