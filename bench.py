@@ -154,6 +154,21 @@ def load_workload():
     return sc, cam, st, None
 
 
+def job_totals(ms, units, world, device):
+    """Whole-job figures over `world` ranks: the slowest rank's time (max over ranks) and the
+    units all ranks processed (sum), by one all-reduce each when world > 1. The job's rate is
+    units / ms."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        n = torch.tensor([float(units)], dtype=torch.float64, device=device)
+        dist.all_reduce(n)
+        ms, units = float(t.item()), float(n.item())
+    return ms, units
+
+
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -369,13 +384,7 @@ def run_gkrt(args):
     ms_total = start.elapsed_time(end)
     trace_ms = [a.elapsed_time(b) for a, b in ev]
     update_span_ms = sum(u.elapsed_time(a) for u, (a, _) in zip(ev_u, ev)) / K
-    if world > 1:
-        t = torch.tensor([ms_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
-        n = torch.tensor([float(rays)], device="cuda")
-        torch.distributed.all_reduce(n)
-        rays = int(n.item())
+    ms_total, rays = job_totals(ms_total, rays, world, "cuda")
     value = rays / (ms_total * 1e-3) / 1e6
 
     # ---- algorithmic bytes of the trace kernel (counters of the last timed frame) ----
@@ -426,6 +435,8 @@ def run_gkrt(args):
     e2e_s = time.perf_counter() - t0
     e2e_rays = r.stats().rays_total - e2e_rays0
     barrier()
+    e2e_ms, e2e_rays = job_totals(e2e_s * 1e3, e2e_rays, world, "cuda")
+    e2e_s = e2e_ms * 1e-3
     e2e_value = e2e_rays / e2e_s / 1e6
 
     # ---- the same frames with the instance level refit instead of rebuilt (animated scenes) ----
