@@ -26,6 +26,17 @@ __device__ __forceinline__ uint64_t umma_desc_sw64(uint32_t saddr) {
     return d;
 }
 
+// Descriptor of a K-major operand without swizzle: core matrices of 8 rows x 16 bytes, each
+// stored as 128 contiguous bytes; lbo: bytes between core matrices adjacent along K, sbo: bytes
+// between core matrices adjacent along M (or N). Start, lbo and sbo are multiples of 16.
+__device__ __forceinline__ uint64_t umma_desc_dense(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;                 // version; layout type 0 (no swizzle) at bits 61-63
+    return d;
+}
+
 // Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1),
 // both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 __host__ __device__ constexpr uint32_t umma_idesc_bf16(uint32_t M, uint32_t N) {

@@ -741,10 +741,11 @@ cudaError_t gkrt_encode_tmap_2d(CUtensorMap* map, const void* base, uint32_t ele
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// cuTensorMapEncodeTiled for bf16 tensors of rank 2..5 with 64-byte swizzle (the K-major
-// operand layout of the tensor-core kernels); zeros outside the tensor.
-cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
-                                  const uint64_t* strides_bytes, const uint32_t* box) {
+// cuTensorMapEncodeTiled for bf16 tensors of rank 2..5; zeros outside the tensor. swizzle64:
+// the 64-byte swizzle of the tensor-core kernels' K-major operands (inner box <= 64 bytes),
+// else no swizzle (dense boxes).
+static cudaError_t encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                    const uint64_t* strides_bytes, const uint32_t* box, bool swizzle64) {
     typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -757,7 +758,8 @@ cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t r
         if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
         fn = (EncodeFn)p;
     }
-    if (rank < 2 || rank > 5 || ((uintptr_t)base & 15u) || box[0] * 2u > 64u || (box[0] * 2u) % 16u) return cudaErrorInvalidValue;
+    if (rank < 2 || rank > 5 || ((uintptr_t)base & 15u) || (box[0] * 2u) % 16u || (swizzle64 && box[0] * 2u > 64u))
+        return cudaErrorInvalidValue;
     cuuint64_t d[5], s[4];
     cuuint32_t b[5], es[5];
     for (uint32_t i = 0; i < rank; ++i) {
@@ -771,9 +773,18 @@ cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t r
         if (s[i] % 16u) return cudaErrorInvalidValue;
     }
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, const_cast<void*>(base), d, s, b, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                  const uint64_t* strides_bytes, const uint32_t* box) {
+    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, true);
+}
+cudaError_t gkrt_encode_tmap_bf16_dense(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                        const uint64_t* strides_bytes, const uint32_t* box) {
+    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, false);
 }
 
 int gkrt_internal_ready_view(GkrtContext* ctx, SceneView* view, unsigned long long** counters, int* device) {

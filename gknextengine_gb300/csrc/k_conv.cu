@@ -214,6 +214,189 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
     if (warp == 1) tmem_dealloc(tmem, ncols);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Halo tiles: outputs of up to 32 channels whose weights fit in shared memory (the
+// full-resolution layers). Tiles of 8 x 16 pixels (x by y, M = 128). The CTA loads all weights
+// once ({32 Cin, Cout} boxes per tap and input chunk, 64-byte swizzled) and keeps them; per
+// 32-channel input chunk a stage holds the chunk's 10 x 18-pixel halo box as four 8-channel
+// planes without swizzle (180 pixel rows of 16 bytes each, planes 2944 bytes apart: a TMA
+// destination must be 128-byte aligned), so that the A operand of tap (dy, dx) is that box at
+// start offset (10 dy + dx) x 16 bytes: core matrices of 8 pixels (one tile row) are 160 bytes
+// apart, K halves one plane pair apart. Each input chunk is read
+// once per tile (with its halo, 1.4x) instead of three times, and no weights per tile.
+
+constexpr int kHaloX = 8, kHaloY = 16;
+constexpr int kHaloBoxX = kHaloX + 2, kHaloBoxY = kHaloY + 2;
+constexpr int kHaloPlane = kHaloBoxX * kHaloBoxY * 16;             // 8 channels: 2880 bytes
+constexpr int kHaloPlaneStride = (kHaloPlane + 127) & ~127;        // 2944
+constexpr int kHaloStage = (4 * kHaloPlaneStride + 1023) & ~1023;  // 32 channels
+constexpr int kHaloStages = 4;
+constexpr int kHaloWeightMax = 96 * 1024;
+
+__global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_constant__ CUtensorMap mx,
+                                                               const __grid_constant__ CUtensorMap mw, ConvArgs a,
+                                                               int tiles_x, int tiles_y, int ntiles) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int kc = a.cin / 32;
+    const int b_bytes = a.cout * 64;   // one weight box: a multiple of 1024 bytes
+    const int w_bytes = 9 * kc * b_bytes;
+    uint8_t* wsm = smem;               // box (chunk c, tap) at (9 c + tap) * b_bytes
+    uint8_t* stage0 = smem + w_bytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(stage0 + kHaloStages * kHaloStage);
+    uint64_t* empty = full + kHaloStages;
+    uint64_t* wbar = empty + kHaloStages;
+    uint64_t* accf = wbar + 1;
+    uint64_t* acce = accf + 2;
+    uint64_t* fin = acce + 2;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(fin + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t ncols1 = a.cout <= 32 ? 32u : 64u;
+    const uint32_t ncols = 2u * ncols1;
+
+    if (tid == 0) {
+        for (int s = 0; s < kHaloStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(wbar, 1);
+        mbar_init(&accf[0], 1);
+        mbar_init(&accf[1], 1);
+        mbar_init(&acce[0], kEpiThreads);
+        mbar_init(&acce[1], kEpiThreads);
+        mbar_init(fin, 1);
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(tslot, ncols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0) {
+        if (lane == 0) {   // producer: the weights once, then one halo box per tile and chunk
+            mbar_expect_tx(wbar, (uint32_t)w_bytes);
+            for (int c = 0; c < kc; ++c)
+                for (int tap = 0; tap < 9; ++tap)
+                    tma_load_2d(wsm + (9 * c + tap) * b_bytes, &mw, tap * a.cin + c * 32, 0, wbar);
+            int kg = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                const int per_img = tiles_x * tiles_y, img = t / per_img, r = t - img * per_img;
+                const int y0 = (r / tiles_x) * kHaloY, x0 = (r % tiles_x) * kHaloX;
+                for (int c = 0; c < kc; ++c, ++kg) {
+                    const int s = kg % kHaloStages;
+                    const uint32_t use = (uint32_t)(kg / kHaloStages);
+                    if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1u) & 1u, a.err)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    uint8_t* sa = stage0 + s * kHaloStage;
+                    if (smem_u32(sa) & 127u) {   // every plane starts 128-byte aligned (stride 2944)
+                        atomicOr(a.err, kErrTmaWait);
+                        *abort_flag = 1;
+                        break;
+                    }
+                    mbar_expect_tx(&full[s], (uint32_t)(4 * kHaloPlane));
+                    for (int j = 0; j < 4; ++j)
+                        tma_load_4d(sa + j * kHaloPlaneStride, &mx, c * 32 + j * 8, x0 - 1, y0 - 1, img, &full[s]);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer
+            const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cout);
+            bool ok = mbar_wait_bounded(wbar, 0u, a.err);
+            if (!ok) *abort_flag = 1;
+            tc_fence_after();
+            const uint32_t wb0 = smem_u32(wsm);
+            int kg = 0, i = 0;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
+                const int acc = i & 1;
+                const uint32_t use = (uint32_t)(i >> 1);
+                if (use > 0 && !mbar_wait_bounded(&acce[acc], (use - 1u) & 1u, a.err)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)acc * ncols1;
+                for (int c = 0; c < kc; ++c, ++kg) {
+                    const int s = kg % kHaloStages;
+                    if (!mbar_wait_bounded(&full[s], (uint32_t)(kg / kHaloStages) & 1u, a.err)) {
+                        *abort_flag = 1;
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(stage0 + s * kHaloStage);
+                    const uint32_t wb = wb0 + (uint32_t)(9 * c * b_bytes);
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const uint32_t off = (uint32_t)(((tap / 3) * kHaloBoxX + tap % 3) * 16);
+                        for (int kk = 0; kk < 2; ++kk) {
+                            const uint64_t ad = umma_desc_dense(sa + (uint32_t)(2 * kk * kHaloPlaneStride) + off,
+                                                                (uint32_t)kHaloPlaneStride, (uint32_t)(kHaloBoxX * 16));
+                            const uint64_t bd = umma_desc_sw64(wb + (uint32_t)(tap * b_bytes + kk * 32));
+                            umma_bf16(d, ad, bd, idesc, (c | tap | kk) != 0 ? 1u : 0u);
+                        }
+                    }
+                    umma_commit(&empty[s]);
+                }
+                if (ok) umma_commit(&accf[acc]);
+            }
+            umma_commit(fin);
+            mbar_wait_bounded(fin, 0u, a.err);   // nothing may be in flight when TMEM is freed
+        }
+    } else {
+        const int q = warp & 3;
+        const int p = q * 32 + lane;
+        int i = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+            const int acc = i & 1;
+            const bool ready = mbar_wait_bounded(&accf[acc], (uint32_t)(i >> 1) & 1u, a.err);
+            __syncwarp();
+            tc_fence_after();
+            if (!__all_sync(0xFFFFFFFFu, ready) || *abort_flag) break;
+            const int per_img = tiles_x * tiles_y, img = t / per_img, r = t - img * per_img;
+            const int y = (r / tiles_x) * kHaloY + p / kHaloX, x = (r % tiles_x) * kHaloX + p % kHaloX;
+            const bool inside = y < a.H && x < a.W;
+            const size_t pix = ((size_t)img * a.H + y) * a.W + x;
+            const uint32_t base = tmem + (uint32_t)acc * ncols1 + ((uint32_t)(q * 32) << 16);
+            for (int c0 = 0; c0 < a.cout; c0 += 16) {
+                uint32_t rr[16];
+                tmem_ld16(base + (uint32_t)c0, rr);
+                tmem_ld_wait();
+                if (!inside) continue;
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    v[j] = __uint_as_float(rr[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                    if (a.flags & kConvRelu) v[j] = fmaxf(v[j], 0.0f);
+                }
+                if (a.flags & kConvF32Out) {
+                    float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
+                    for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
+                } else {
+                    uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + pix * a.out_c +
+                                                        a.out_off + c0);
+                    o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                                      pack_bf16x2(v[6], v[7]));
+                    o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
+                                      pack_bf16x2(v[14], v[15]));
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&acce[acc]);
+        }
+    }
+    __syncthreads();
+    if (warp == 1) tmem_dealloc(tmem, ncols);
+}
+
 }  // namespace
 
 }  // namespace gk
@@ -222,6 +405,17 @@ using namespace gk;
 
 cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                   const uint64_t* strides_bytes, const uint32_t* box);
+cudaError_t gkrt_encode_tmap_bf16_dense(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                        const uint64_t* strides_bytes, const uint32_t* box);
+
+// Halo tiles for outputs of up to 32 channels whose weights (9 Cin Cout bf16) fit in 96 KB.
+// The 1080p forward (event-timed, one box): row-box stages everywhere 1.560 ms; halo tiles for
+// Cout <= 32 1.503 ms; also for Cout <= 64 with weights <= 40 KB 1.504 ms, <= 96 KB 1.556 ms
+// (the 64 -> 64 layers then run one CTA per SM behind 72 KB of weights).
+static bool conv_halo(int cin, int cout) { return cout <= 32 && 9 * cin * cout * 2 <= kHaloWeightMax; }
+static size_t conv_halo_smem(int cin, int cout) {
+    return (size_t)9 * cin * cout * 2 + kHaloStages * kHaloStage + (2 * kHaloStages + 6) * 8 + 8 + 1024;
+}
 
 // Outputs of up to 128 channels use the row-box stages (three vertical taps per box); the
 // 1080p forward: none 1.94 ms, up to 64 channels 1.67 ms, up to 128 channels 1.58 ms.
@@ -255,6 +449,45 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         return cudaErrorInvalidValue;
     CUtensorMap mx, mw;
     const uint64_t xc = (uint64_t)(args.x_c > 0 ? args.x_c : args.cin);
+    static int sms_h = 0;
+    if (!sms_h) {
+        int dev = 0;
+        cudaError_t e0 = cudaGetDevice(&dev);
+        if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&sms_h, cudaDevAttrMultiProcessorCount, dev);
+        if (e0 != cudaSuccess) return e0;
+    }
+    if (conv_halo(args.cin, args.cout)) {
+        const uint64_t xd[4] = {(uint64_t)args.cin, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
+        const uint64_t xs[3] = {xc * 2, (uint64_t)args.W * xc * 2, (uint64_t)args.H * args.W * xc * 2};
+        const uint32_t xb[4] = {8, kHaloBoxX, kHaloBoxY, 1};
+        const void* xbase = static_cast<const uint8_t*>(x) + (size_t)args.x_off * 2;
+        cudaError_t e = gkrt_encode_tmap_bf16_dense(&mx, xbase, 4, xd, xs, xb);
+        if (e != cudaSuccess) return e;
+        const uint64_t wd[2] = {(uint64_t)9 * args.cin, (uint64_t)args.cout};
+        const uint64_t ws[1] = {(uint64_t)9 * args.cin * 2};
+        const uint32_t wb[2] = {32, (uint32_t)args.cout};
+        if ((e = gkrt_encode_tmap_bf16(&mw, w, 2, wd, ws, wb)) != cudaSuccess) return e;
+        const size_t smem = conv_halo_smem(args.cin, args.cout);
+        static bool attr = false;
+        if (!attr) {
+            const int mx_smem = (int)(kHaloWeightMax + kHaloStages * kHaloStage + 4096);
+            if ((e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, mx_smem)) !=
+                cudaSuccess)
+                return e;
+            if ((e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
+                return e;
+            attr = true;
+        }
+        const int ncols = 2 * (args.cout <= 32 ? 32 : 64);
+        const int per_sm = std::max(1, std::min({(int)((227 * 1024) / (smem + 1024)), 512 / ncols,
+                                                 2048 / kConvThreads}));
+        const int tiles_x = (args.W + kHaloX - 1) / kHaloX, tiles_y = (args.H + kHaloY - 1) / kHaloY;
+        const int ntiles = tiles_x * tiles_y * args.B;
+        const int grid = std::min(ntiles, sms_h * per_sm);
+        k_conv3x3_halo<<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles);
+        return cudaGetLastError();
+    }
     const uint64_t xd[4] = {(uint64_t)args.cin, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
     const uint64_t xs[3] = {xc * 2, (uint64_t)args.W * xc * 2, (uint64_t)args.H * args.W * xc * 2};
     const bool rows = conv_rows(args.cout);

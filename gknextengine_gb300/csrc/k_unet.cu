@@ -235,22 +235,35 @@ __global__ void k_relu_bwd(__nv_bfloat16* dy, int dy_c, int dy_off, const __nv_b
     st8(d, a);
 }
 
-// db[c] += sum over pixels of dP[p][c]; one block per run of pixels, shared partial sums
-__global__ void k_bias_grad(const __nv_bfloat16* dp, int dp_c, int dp_off, long long npix, int C, int run,
-                            float* db) {
-    __shared__ float part[256];
-    for (int c = threadIdx.x; c < C; c += blockDim.x) part[c] = 0.0f;
-    __syncthreads();
-    const long long p0 = (long long)blockIdx.x * run;
-    for (long long i = threadIdx.x; i < (long long)run * C; i += blockDim.x) {
-        const long long p = p0 + i / C;
-        if (p >= npix) break;
-        const int c = (int)(i % C);
-        atomicAdd(&part[c], __bfloat162float(dp[p * dp_c + dp_off + c]));
+// db[c] += sum over pixels of dP[p][c]; one block per run of pixels. Thread t owns the 8
+// channels 8 (t % G) .. +7 (G = C / 8, one 16-byte load per pixel) of every (256 / G)-th pixel
+// of the run and sums them in registers; the threads of each channel group are then reduced
+// in shared memory and each channel gets one atomic per block.
+__global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16* dp, int dp_c, int dp_off, long long npix,
+                                                   int C, int run, float* db) {
+    __shared__ float part[256 * 8];
+    const int G = C / 8, per = 256 / G;
+    const int g = threadIdx.x % G, k = threadIdx.x / G;
+    float acc[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (k < per) {
+        const long long p0 = (long long)blockIdx.x * run;
+        const long long p1 = p0 + run < npix ? p0 + run : npix;
+        for (long long p = p0 + k; p < p1; p += per) {
+            float v[8];
+            ld8(dp + p * dp_c + dp_off + 8 * g, v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] += v[j];
+        }
     }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) part[threadIdx.x * 8 + j] = acc[j];
     __syncthreads();
-    for (int c = threadIdx.x; c < C; c += blockDim.x)
-        if (part[c] != 0.0f) atomicAdd(&db[c], part[c]);
+    if (threadIdx.x < C) {
+        const int c = threadIdx.x, cg = c / 8, cj = c % 8;
+        float sum = 0.0f;
+        for (int i = 0; i < per; ++i) sum += part[(i * G + cg) * 8 + cj];
+        if (sum != 0.0f) atomicAdd(&db[c], sum);
+    }
 }
 
 }  // namespace
@@ -316,7 +329,7 @@ cudaError_t gkrt_launch_relu_bwd(void* dy, int dy_c, int dy_off, const void* y, 
 }
 cudaError_t gkrt_launch_bias_grad(const void* dp, int dp_c, int dp_off, long long npix, int C, float* db,
                                   cudaStream_t st) {
-    if (C > 256) return cudaErrorInvalidValue;
+    if (C > 256 || C % 8 || dp_c % 8 || dp_off % 8 || ((uintptr_t)dp & 15u)) return cudaErrorInvalidValue;
     const int run = 1024;
     k_bias_grad<<<(unsigned)((npix + run - 1) / run), 256, 0, st>>>((const __nv_bfloat16*)dp, dp_c, dp_off, npix, C,
                                                                    run, db);

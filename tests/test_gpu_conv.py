@@ -29,7 +29,11 @@ def conv(x, w, bias, cout, out, out_c, out_off, n_store=0, flags=0):
 
 @pytest.mark.parametrize("B,H,W,cin,cout,relu", [(2, 37, 45, 64, 96, True), (1, 64, 64, 32, 32, False),
                                                   (1, 24, 40, 224, 96, True), (1, 17, 33, 160, 64, True),
-                                                  (3, 8, 16, 96, 128, False), (1, 20, 20, 128, 256, True)])
+                                                  (3, 8, 16, 96, 128, False), (1, 20, 20, 128, 256, True),
+                                                  # halo tiles (Cout <= 64, weights <= 96 KB): partial
+                                                  # 8 x 16 tiles, several chunks, images
+                                                  (2, 37, 45, 96, 32, True), (1, 19, 23, 32, 64, False),
+                                                  (1, 40, 24, 64, 64, True), (2, 9, 7, 32, 48, False)])
 def test_conv_matches_torch(B, H, W, cin, cout, relu):
     torch = _torch()
     g = torch.Generator(device="cuda").manual_seed(B * 1000 + cin + cout)
