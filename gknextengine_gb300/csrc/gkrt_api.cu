@@ -1397,6 +1397,16 @@ int gkrt_set_material_params(GkrtContext* ctx, const float* albedo_rgb, const fl
     return GKRT_OK;
 }
 
+// Error word of the context-free kernel entry points, one per device (allocated on first use,
+// kept for the process).
+static uint32_t* standalone_err_word() {
+    static uint32_t* words[kMaxDevices] = {};
+    const int dev = current_device_slot();
+    if (dev < 0) return nullptr;
+    if (!words[dev] && cudaMalloc((void**)&words[dev], 4) != cudaSuccess) return nullptr;
+    return words[dev];
+}
+
 static int adjoint_checks(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t spp) {
     int rc = check_frame(ctx, fc);
     if (rc != GKRT_OK) return rc;
@@ -1453,8 +1463,8 @@ int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t w
     a.out_off = (int)y_offset;
     a.n_store = (int)y_store;
     a.flags = (int)flags;
-    static uint32_t* d_err = nullptr;   // the standalone kernels' error word
-    if (!d_err && cudaMalloc((void**)&d_err, 4) != cudaSuccess) return GKRT_ERR_OOM;
+    uint32_t* d_err = standalone_err_word();   // the standalone kernels' error word (this device's)
+    if (!d_err) return GKRT_ERR_OOM;
     a.err = d_err;
     cudaError_t e = gkrt_launch_conv3x3(x, w, a, (cudaStream_t)stream);
     if (e == cudaErrorInvalidValue) return GKRT_ERR_INVALID_ARG;
@@ -1546,8 +1556,8 @@ int gkrt_conv3x3_wgrad_bf16(const void* dy, const void* x, uint32_t batch, uint3
     if (!dy || !x || !dw || batch == 0 || height == 0 || width == 0 || batch > 65535 || height > 65535 ||
         width > 65535)
         return GKRT_ERR_INVALID_ARG;
-    static uint32_t* d_err = nullptr;
-    if (!d_err && cudaMalloc((void**)&d_err, 4) != cudaSuccess) return GKRT_ERR_OOM;
+    uint32_t* d_err = standalone_err_word();
+    if (!d_err) return GKRT_ERR_OOM;
     WgradArgs a;
     a.B = (int)batch; a.H = (int)height; a.W = (int)width;
     a.dp = (const __nv_bfloat16*)dy; a.dp_c = (int)cout; a.dp_off = 0; a.cout = (int)cout;

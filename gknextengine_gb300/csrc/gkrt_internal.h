@@ -15,6 +15,15 @@ struct BvhNode;
 struct WideNode;
 struct ProbeLight;
 
+// Launch-geometry and attribute caches of the launchers are kept per device (a process may
+// drive several GPUs): the current device's slot, or -1 past kMaxDevices.
+constexpr int kMaxDevices = 64;
+inline int current_device_slot() {
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) return -1;
+    return d;
+}
+
 struct ReprojectArgs {
     int W, H, P;                   // P: row pitch in pixels (a multiple of 4)
     uint32_t progressive, temporal_frames;

@@ -449,13 +449,18 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         return cudaErrorInvalidValue;
     CUtensorMap mx, mw;
     const uint64_t xc = (uint64_t)(args.x_c > 0 ? args.x_c : args.cin);
-    static int sms_h = 0;
-    if (!sms_h) {
-        int dev = 0;
-        cudaError_t e0 = cudaGetDevice(&dev);
-        if (e0 == cudaSuccess) e0 = cudaDeviceGetAttribute(&sms_h, cudaDevAttrMultiProcessorCount, dev);
+    // per device: SM count, the attributes set, resident CTAs per output width
+    static int sms_dev[kMaxDevices] = {};
+    static bool halo_attr[kMaxDevices] = {};
+    static size_t smem_set[kMaxDevices] = {};
+    static int per_sm_cache[kMaxDevices][257] = {};
+    const int dev = current_device_slot();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    if (!sms_dev[dev]) {
+        const cudaError_t e0 = cudaDeviceGetAttribute(&sms_dev[dev], cudaDevAttrMultiProcessorCount, dev);
         if (e0 != cudaSuccess) return e0;
     }
+    const int sms = sms_dev[dev];
     if (conv_halo(args.cin, args.cout)) {
         const uint64_t xd[4] = {(uint64_t)args.cin, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
         const uint64_t xs[3] = {xc * 2, (uint64_t)args.W * xc * 2, (uint64_t)args.H * args.W * xc * 2};
@@ -468,8 +473,7 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         const uint32_t wb[2] = {32, (uint32_t)args.cout};
         if ((e = gkrt_encode_tmap_bf16(&mw, w, 2, wd, ws, wb)) != cudaSuccess) return e;
         const size_t smem = conv_halo_smem(args.cin, args.cout);
-        static bool attr = false;
-        if (!attr) {
+        if (!halo_attr[dev]) {
             const int mx_smem = (int)(kHaloWeightMax + kHaloStages * kHaloStage + 4096);
             if ((e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, mx_smem)) !=
                 cudaSuccess)
@@ -477,14 +481,14 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
             if ((e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributePreferredSharedMemoryCarveout,
                                           (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
                 return e;
-            attr = true;
+            halo_attr[dev] = true;
         }
         const int ncols = 2 * (args.cout <= 32 ? 32 : 64);
         const int per_sm = std::max(1, std::min({(int)((227 * 1024) / (smem + 1024)), 512 / ncols,
                                                  2048 / kConvThreads}));
         const int tiles_x = (args.W + kHaloX - 1) / kHaloX, tiles_y = (args.H + kHaloY - 1) / kHaloY;
         const int ntiles = tiles_x * tiles_y * args.B;
-        const int grid = std::min(ntiles, sms_h * per_sm);
+        const int grid = std::min(ntiles, sms * per_sm);
         k_conv3x3_halo<<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles);
         return cudaGetLastError();
     }
@@ -501,32 +505,25 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     e = gkrt_encode_tmap_bf16(&mw, w, 2, wd, ws, wb);
     if (e != cudaSuccess) return e;
     const size_t smem = gkrt_conv_smem_bytes(args.cout);
-    // launch geometry per output width, computed once (host calls kept off the per-launch path)
-    static int sms = 0;
-    static int per_sm_cache[257] = {};
-    static size_t smem_set = 0;
-    if (!sms) {
-        int dev = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    }
-    if (smem > smem_set) {
+    // launch geometry per output width, computed once per device (host calls kept off the
+    // per-launch path)
+    if (smem > smem_set[dev]) {
         if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)conv_smem_max())) !=
             cudaSuccess)
             return e;
         if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributePreferredSharedMemoryCarveout,
                                       (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
             return e;
-        smem_set = conv_smem_max();
+        smem_set[dev] = conv_smem_max();
     }
-    int per_sm = per_sm_cache[args.cout];
+    int per_sm = per_sm_cache[dev][args.cout];
     if (!per_sm) {
         // resident CTAs per SM: shared memory (227 KB per SM, 1 KB reserved per CTA), the 512
         // TMEM columns (two accumulators per CTA) and 2048 threads
         const int ncols = 2 * (args.cout <= 32 ? 32 : args.cout <= 64 ? 64 : args.cout <= 128 ? 128 : 256);
         per_sm = std::min({(int)((227 * 1024) / (smem + 1024)), 512 / ncols, 2048 / kConvThreads});
         per_sm = std::max(1, per_sm);
-        per_sm_cache[args.cout] = per_sm;
+        per_sm_cache[dev][args.cout] = per_sm;
     }
     const int tiles_x = (args.W + kTileX - 1) / kTileX, tiles_y = (args.H + kTileY - 1) / kTileY;
     const int ntiles = tiles_x * tiles_y * args.B;

@@ -479,15 +479,18 @@ cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstant
     if (stack_words < 1 || stack_words > kStackSize) return cudaErrorInvalidValue;
     const bool nee = fc.nee_mode == GKRT_NEE_EMISSIVE && sc.nemit > 0u;
     const size_t smem = (size_t)(stack_words + SL_COUNT) * kPtThreads * 4u;
-    // resident blocks per SM of each instantiation and stack size, queried once each
-    static int occ[2][kStackSize + 1] = {};
+    // resident blocks per SM of each instantiation and stack size, queried once per device
+    static int occ[kMaxDevices][2][kStackSize + 1] = {};
+    const int dev = current_device_slot();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    int* o = &occ[dev][nee][stack_words];
     cudaError_t e = cudaSuccess;
-    if (!occ[nee][stack_words]) {
-        e = nee ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1][stack_words], k_trace_pass<true>, kPtThreads, smem)
-                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0][stack_words], k_trace_pass<false>, kPtThreads, smem);
+    if (!*o) {
+        e = nee ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<true>, kPtThreads, smem)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<false>, kPtThreads, smem);
         if (e != cudaSuccess) return e;
     }
-    int per_sm = occ[nee][stack_words];
+    int per_sm = *o;
     if (per_sm < 1) per_sm = 1;
     const int pixels = W * H;
     int blocks = num_sms * per_sm;

@@ -282,12 +282,14 @@ cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
         return cudaErrorInvalidValue;
     const long long npix = (long long)a.B * a.H * a.W;
     const size_t smem = gkrt_wgrad_smem_bytes(a.cin);
-    static bool attr_set = false;   // set once for the largest operand (cin = 256)
-    if (!attr_set) {
+    static bool attr_set[kMaxDevices] = {};   // set once per device for the largest operand (cin = 256)
+    const int dev = current_device_slot();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    if (!attr_set[dev]) {
         cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)gkrt_wgrad_smem_bytes(256));
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        attr_set[dev] = true;
     }
     const dim3 grid((unsigned)((npix + a.chunk - 1) / a.chunk), 9);
     k_conv_wgrad<<<grid, kWgThreads, smem, st>>>(a);
