@@ -155,3 +155,35 @@ def test_refit_rebuilds_when_members_change(env):
     for i in ga:
         assert np.array_equal(ga[i].view(np.uint32), gb[i].view(np.uint32)), i
     assert a.stats().device_error == 0
+
+
+def test_refit_of_a_host_built_tree_and_mesh_changes(env):
+    """The instance level built by the host builder (links recorded by the same GPU collapse),
+    then refit on the GPU; and instances that change mesh between frames (the refit computes
+    their boxes from the new mesh). Both equal a rebuild image for image."""
+    sc, cam, st, motion, a, b = env
+    for r in (a, b):
+        r.create_swap_chain(W, H)
+    st.flags = abi.FRAME_PRIMARY_IDS
+    fb = camera.FrameBuilder(W, H, st)
+    try:
+        inst10 = frame_instances(motion, sc.instances, 10)   # all visible again (the last test hid 40)
+        for r in (a, b):
+            r.update_instances(inst10)
+        a.build_bvh(abi.BUILD_ALL | abi.BUILD_ON_HOST)
+        b.build_bvh(abi.BUILD_ALL)
+        n0 = a.stats().tlas_refits
+        for k, swap in ((11, False), (12, True)):
+            inst = frame_instances(motion, sc.instances, k)
+            if swap:   # every fifth building becomes a sphere of the same transform, and back
+                inst["mesh_id"][0:motion.first:5] = 1
+            a.refit_instances(inst)
+            b.update_instances(inst)
+            fc = fb.build(cam, k)
+            ga, gb = render(a, fc), render(b, fc)
+            for i in ga:
+                assert np.array_equal(ga[i].view(np.uint32), gb[i].view(np.uint32)), (k, i)
+        assert a.stats().tlas_refits == n0 + 2
+        assert a.stats().device_error == 0
+    finally:
+        a.build_bvh(abi.BUILD_ALL)
