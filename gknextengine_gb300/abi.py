@@ -150,6 +150,14 @@ class GkrtImageView(C.Structure):
                 ("pitch_bytes", C.c_uint32), ("format", C.c_uint32)]
 
 
+DEVICE_PASS_TIMERS = 1
+
+
+class GkrtPassTimes(C.Structure):
+    _fields_ = [("rt_pass_ms", C.c_float), ("reproject_pass_ms", C.c_float), ("compose_pass_ms", C.c_float),
+                ("copy_pass_ms", C.c_float), ("tlas_update_ms", C.c_float), ("reserved", C.c_float * 3)]
+
+
 class GkrtOutputDesc(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("offset_x", C.c_int32), ("offset_y", C.c_int32), ("width", C.c_uint32),
                 ("height", C.c_uint32), ("source_image", C.c_uint32)]

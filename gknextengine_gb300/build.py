@@ -61,7 +61,7 @@ def build(force: bool = False, jobs: int | None = None) -> str:
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, BUILD_DIR), srcs))
     tmp = LIB_PATH + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs
+    cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs + ["-ldl"]   # NVTX loads tools
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")

@@ -16,6 +16,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "gk_shade.cuh"
 #include "gk_tma.cuh"
 #include "gkrt_internal.h"
@@ -32,8 +34,17 @@ struct StageSlot {
     int cur = 0;
 };
 
+// Pass scopes, named as the reference's GPU timer scopes (PathTracingRenderer.cpp:111, 126, 138,
+// 160; RayTraceBaseRenderer.cpp:209).
+enum PassId { kPassRt, kPassReproject, kPassCompose, kPassCopy, kPassTlas, kPassCount };
+static const char* const kPassNames[kPassCount] = {"rt pass", "reproject pass", "compose pass", "copy pass",
+                                                   "TLAS Update"};
+
 struct GkrtContext {
     int device = 0;
+    bool timers = false;                        // GKRT_DEVICE_PASS_TIMERS
+    cudaEvent_t pass_ev[kPassCount][2] = {};    // begin / end of each pass's last run
+    bool pass_recorded[kPassCount] = {};
     uint32_t watchdog_ms = 60000;
     std::string err;
     uint32_t W = 0, H = 0, P = 0;     // P: row pitch in pixels (W rounded up to 4: 16-byte rows)
@@ -108,6 +119,24 @@ struct GkrtContext {
     uint32_t* d_error = nullptr;
     unsigned int* d_work = nullptr;             // pixel counter of the persistent trace kernel
     int num_sms = 1;
+};
+
+// Scope of one pass on its stream: an NVTX range, and with pass timers the begin and end events.
+struct PassScope {
+    GkrtContext* ctx;
+    int id;
+    cudaStream_t st;
+    PassScope(GkrtContext* c, int i, cudaStream_t s) : ctx(c), id(i), st(s) {
+        nvtxRangePushA(kPassNames[i]);
+        if (ctx->timers) cudaEventRecord(ctx->pass_ev[i][0], st);
+    }
+    ~PassScope() {
+        if (ctx->timers) {
+            cudaEventRecord(ctx->pass_ev[id][1], st);
+            ctx->pass_recorded[id] = true;
+        }
+        nvtxRangePop();
+    }
 };
 
 namespace {
@@ -812,8 +841,14 @@ int gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out) {
     if (!ctx) return GKRT_ERR_OOM;
     ctx->device = desc ? desc->device : 0;
     if (desc && desc->watchdog_ms) ctx->watchdog_ms = desc->watchdog_ms;
-    if (ctx->device < 0 || ctx->device >= ndev) { delete ctx; return GKRT_ERR_INVALID_ARG; }
+    if (ctx->device < 0 || ctx->device >= ndev || (desc && (desc->flags & ~GKRT_DEVICE_PASS_TIMERS))) {
+        delete ctx;
+        return GKRT_ERR_INVALID_ARG;
+    }
+    ctx->timers = desc && (desc->flags & GKRT_DEVICE_PASS_TIMERS);
     cudaError_t e = cudaSetDevice(ctx->device);
+    for (int i = 0; i < kPassCount && ctx->timers && e == cudaSuccess; ++i)
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreate(&ctx->pass_ev[i][k]);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_counters, 8 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_error, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_work, sizeof(unsigned int));
@@ -824,6 +859,9 @@ int gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out) {
         dfree(ctx->d_counters);
         dfree(ctx->d_error);
         dfree(ctx->d_work);
+        for (auto& pe : ctx->pass_ev)
+            for (cudaEvent_t& ev : pe)
+                if (ev) cudaEventDestroy(ev);
         delete ctx;
         return e == cudaErrorMemoryAllocation ? GKRT_ERR_OOM : GKRT_ERR_CUDA;
     }
@@ -852,6 +890,9 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     dfree(ctx->d_counters);
     dfree(ctx->d_error);
     dfree(ctx->d_work);
+    for (auto& pe : ctx->pass_ev)
+        for (cudaEvent_t& ev : pe)
+            if (ev) cudaEventDestroy(ev);
     delete ctx;
     return GKRT_OK;
 }
@@ -951,6 +992,7 @@ int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
     int rc = validate_instances(ctx, instances, count, (uint32_t)ctx->meshes.size(), ctx->nmat);
     if (rc != GKRT_OK) return rc;
     cudaSetDevice(ctx->device);
+    const PassScope scope(ctx, kPassTlas, (cudaStream_t)stream);
     ctx->inst.assign(instances, instances + count);
     // host work first (emitter table, then the instance tables inside build_tlas), uploaded
     // asynchronously, so that it overlaps the stream's earlier frames; the GPU build follows
@@ -967,6 +1009,7 @@ int gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances, 
     int rc = validate_instances(ctx, instances, count, (uint32_t)ctx->meshes.size(), ctx->nmat);
     if (rc != GKRT_OK) return rc;
     cudaSetDevice(ctx->device);
+    const PassScope scope(ctx, kPassTlas, (cudaStream_t)stream);
     ctx->inst.assign(instances, instances + count);
     if ((rc = build_emitters(ctx, (cudaStream_t)stream)) != GKRT_OK) return rc;
     if (!ctx->blas_ready || !ctx->tlas_ready) return ensure_bvh(ctx, 0, (cudaStream_t)stream);
@@ -996,6 +1039,7 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     cudaSetDevice(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
+    const PassScope scope(ctx, kPassRt, st);
     const ShadeScene sc = shade_scene(ctx);
     PixelImages im;
     im.single_diffuse = (float4*)ctx->img[GKRT_IMG_SINGLE_DIFFUSE];
@@ -1020,6 +1064,7 @@ int gkrt_reproject_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* st
     int rc = check_frame(ctx, fc);
     if (rc != GKRT_OK) return rc;
     cudaSetDevice(ctx->device);
+    const PassScope scope(ctx, kPassReproject, (cudaStream_t)stream);
     ReprojectArgs a;
     a.W = (int)ctx->W; a.H = (int)ctx->H; a.P = (int)ctx->P;
     a.err = ctx->d_error;
@@ -1048,6 +1093,7 @@ int gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stre
     if (rc != GKRT_OK) return rc;
     if (fc->denoiser > GKRT_DENOISE_UNET) return fail(ctx, GKRT_ERR_UNSUPPORTED, "unknown denoiser");
     cudaSetDevice(ctx->device);
+    const PassScope scope(ctx, kPassCompose, (cudaStream_t)stream);
     if (fc->denoiser == GKRT_DENOISE_UNET) {
         if (!ctx->unet) return fail(ctx, GKRT_ERR_STATE, "gkrt_unet_init was not called");
         if (ctx->W % 8 || ctx->H % 8) return fail(ctx, GKRT_ERR_UNSUPPORTED, "the learned denoiser needs sizes divisible by 8");
@@ -1105,9 +1151,10 @@ int gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stre
 }
 
 int gkrt_end_frame(GkrtContext* ctx, void* stream) {
-    (void)stream;
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (ctx->W == 0) return fail(ctx, GKRT_ERR_STATE, "gkrt_resize was not called");
+    cudaSetDevice(ctx->device);
+    const PassScope scope(ctx, kPassCopy, (cudaStream_t)stream);   // a buffer swap: no GPU work
     const int pairs[4][2] = {{GKRT_IMG_ACCUM_DIFFUSE, GKRT_IMG_PREV_DIFFUSE},
                              {GKRT_IMG_ACCUM_SPECULAR, GKRT_IMG_PREV_SPECULAR},
                              {GKRT_IMG_ACCUM_ALBEDO, GKRT_IMG_PREV_ALBEDO},
@@ -1122,6 +1169,26 @@ int gkrt_render_frame(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stre
     if ((rc = gkrt_reproject_pass(ctx, fc, stream)) != GKRT_OK) return rc;
     if ((rc = gkrt_denoise_pass(ctx, fc, stream)) != GKRT_OK) return rc;
     return gkrt_end_frame(ctx, stream);
+}
+
+int gkrt_get_pass_times(GkrtContext* ctx, GkrtPassTimes* out) {
+    if (!ctx || !out) return GKRT_ERR_INVALID_ARG;
+    if (!ctx->timers) return fail(ctx, GKRT_ERR_STATE, "the context was created without GKRT_DEVICE_PASS_TIMERS");
+    cudaSetDevice(ctx->device);
+    float ms[kPassCount];
+    for (int i = 0; i < kPassCount; ++i) {
+        ms[i] = -1.0f;
+        if (!ctx->pass_recorded[i]) continue;
+        GK_CUDA(cudaEventSynchronize(ctx->pass_ev[i][1]));
+        GK_CUDA(cudaEventElapsedTime(&ms[i], ctx->pass_ev[i][0], ctx->pass_ev[i][1]));
+    }
+    out->rt_pass_ms = ms[kPassRt];
+    out->reproject_pass_ms = ms[kPassReproject];
+    out->compose_pass_ms = ms[kPassCompose];
+    out->copy_pass_ms = ms[kPassCopy];
+    out->tlas_update_ms = ms[kPassTlas];
+    out->reserved[0] = out->reserved[1] = out->reserved[2] = 0.0f;
+    return GKRT_OK;
 }
 
 int gkrt_get_image(GkrtContext* ctx, int id, GkrtImageView* out) {

@@ -52,6 +52,7 @@ def load(path: str | None = None):
     L.gkrt_trace_rays.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_trace_rays_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
+    L.gkrt_get_pass_times.argtypes = [vp, C.POINTER(abi.GkrtPassTimes)]
     L.gkrt_output_resize.argtypes = [vp, C.c_uint32, C.c_uint32]
     L.gkrt_output_pass.argtypes = [vp, C.POINTER(abi.GkrtOutputDesc), vp]
     L.gkrt_get_output.argtypes = [vp, C.POINTER(abi.GkrtImageView)]
@@ -92,7 +93,7 @@ EXPORTED = [
     "gkrt_output_resize", "gkrt_output_pass", "gkrt_get_output", "gkrt_copy_output_to_host",
     "gkrt_screenshot",
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_copy_image_to_host_async", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
-    "gkrt_get_stats", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",
+    "gkrt_get_stats", "gkrt_get_pass_times", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",
     "gkrt_synchronize", "gkrt_affine_inverse",
     "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16", "gkrt_conv3x3_wgrad_bf16",
     "gkrt_unet_init", "gkrt_unet_param_count", "gkrt_unet_get_params", "gkrt_unet_set_params", "gkrt_unet_forward",

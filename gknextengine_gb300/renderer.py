@@ -18,11 +18,12 @@ from . import abi, native
 
 
 class PathTracingRenderer:
-    def __init__(self, device: int = 0, watchdog_ms: int = 0):
+    def __init__(self, device: int = 0, watchdog_ms: int = 0, pass_timers: bool = False):
         self._lib = native.load()
         d = abi.GkrtDeviceDesc()
         d.device = device
         d.watchdog_ms = watchdog_ms
+        d.flags = abi.DEVICE_PASS_TIMERS if pass_timers else 0
         h = C.c_void_p()
         rc = self._lib.gkrt_context_create(C.byref(d), C.byref(h))
         if rc != abi.GKRT_OK:
@@ -247,6 +248,14 @@ class PathTracingRenderer:
         self._check(self._lib.gkrt_adjoint_backward(self._h, C.byref(fc), spp, C.c_void_p(sample_rough_ptr or 0),
                                                     C.c_void_p(dimage_ptr), C.c_void_p(grad_albedo_ptr),
                                                     C.c_void_p(grad_rough_ptr), self._stream(stream)))
+
+    def pass_times(self) -> dict:
+        """GPU ms of each pass's last run (contexts made with pass_timers=True): the reference's
+        "rt pass", "reproject pass", "compose pass", "copy pass" and "TLAS Update" timers."""
+        t = abi.GkrtPassTimes()
+        self._check(self._lib.gkrt_get_pass_times(self._h, C.byref(t)))
+        return {"rt pass": t.rt_pass_ms, "reproject pass": t.reproject_pass_ms, "compose pass": t.compose_pass_ms,
+                "copy pass": t.copy_pass_ms, "TLAS Update": t.tlas_update_ms}
 
     def stats(self) -> abi.GkrtStats:
         s = abi.GkrtStats()

@@ -228,10 +228,24 @@ typedef struct GkrtHit {
 
 typedef struct GkrtDeviceDesc {
     int32_t  device;            /* CUDA ordinal                                          */
-    uint32_t flags;
+    uint32_t flags;             /* GKRT_DEVICE_*                                         */
     uint32_t watchdog_ms;       /* 0: default bounded wait for gkrt_synchronize          */
     uint32_t reserved;
 } GkrtDeviceDesc;
+
+/* Per-pass GPU timers, as the reference's SCOPED_GPU_TIMER scopes read back at frame end
+ * (VulkanGpuTimer.hpp:12-120; scopes PathTracingRenderer.cpp:111,126,138,160 and "TLAS Update"
+ * RayTraceBaseRenderer.cpp:209): with this flag each pass records an event pair on its stream.
+ * Every pass also opens an NVTX range of the same name, with or without the flag. */
+#define GKRT_DEVICE_PASS_TIMERS 1u
+typedef struct GkrtPassTimes {  /* ms of each pass's last run, -1 if it has not run      */
+    float rt_pass_ms;
+    float reproject_pass_ms;
+    float compose_pass_ms;       /* the denoise pass                                     */
+    float copy_pass_ms;          /* gkrt_end_frame: a buffer swap, no GPU work           */
+    float tlas_update_ms;        /* gkrt_scene_update_instances / _refit_instances        */
+    float reserved[3];
+} GkrtPassTimes;
 
 typedef struct GkrtStats {
     uint64_t rays_traced;       /* camera + bounce + shadow rays of the last trace pass   */
@@ -333,6 +347,10 @@ int  gkrt_copy_output_to_host(GkrtContext* ctx, void* dst, size_t dst_bytes, voi
  * caller's (the Python layer writes PNG). */
 int  gkrt_screenshot(GkrtContext* ctx, uint32_t x, uint32_t y, uint32_t width, uint32_t height,
                      void* dst, size_t dst_bytes, void* stream);
+
+/* Waits for each pass's last recorded run and returns its GPU time (GKRT_ERR_STATE without
+ * GKRT_DEVICE_PASS_TIMERS). */
+int  gkrt_get_pass_times(GkrtContext* ctx, GkrtPassTimes* out);
 
 /* Outputs (bindless storage images, BindlessTexture.slang:8-40). */
 int  gkrt_get_image(GkrtContext* ctx, int image_id, GkrtImageView* out);
