@@ -1573,6 +1573,21 @@ int gkrt_unet_get_params(GkrtContext* ctx, float* params, float* grads) {
     return GKRT_OK;
 }
 
+int gkrt_unet_get_state(GkrtContext* ctx, float* m, float* v, uint64_t* step) {
+    int rc = unet_ready(ctx);
+    if (rc != GKRT_OK) return rc;
+    GK_CUDA(gkrt_unet_get_state_host(ctx->unet, m, v, step));
+    return GKRT_OK;
+}
+
+int gkrt_unet_set_state(GkrtContext* ctx, const float* m, const float* v, uint64_t step) {
+    int rc = unet_ready(ctx);
+    if (rc != GKRT_OK) return rc;
+    if (!m || !v || step > 0x7FFFFFFFull) return fail(ctx, GKRT_ERR_INVALID_ARG, "null moments or step out of range");
+    GK_CUDA(gkrt_unet_set_state_host(ctx->unet, m, v, step));
+    return GKRT_OK;
+}
+
 int gkrt_unet_set_params(GkrtContext* ctx, const float* params) {
     if (!ctx || !params) return GKRT_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);

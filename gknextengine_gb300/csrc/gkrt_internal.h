@@ -227,6 +227,8 @@ size_t gkrt_unet_nparams(const gk::Unet* u);
 cudaError_t gkrt_unet_init_params(gk::Unet* u, uint64_t seed);
 cudaError_t gkrt_unet_set_params_host(gk::Unet* u, const float* h);
 cudaError_t gkrt_unet_get_params_host(gk::Unet* u, float* params, float* grads);
+cudaError_t gkrt_unet_get_state_host(gk::Unet* u, float* m, float* v, uint64_t* step);
+cudaError_t gkrt_unet_set_state_host(gk::Unet* u, const float* m, const float* v, uint64_t step);
 cudaError_t gkrt_unet_zero_grad(gk::Unet* u, cudaStream_t st);
 cudaError_t gkrt_unet_forward_dev(gk::Unet* u, const float* input, int b, int h, int w, float* out_linear,
                                   float* out_raw, cudaStream_t st);

@@ -392,6 +392,24 @@ cudaError_t gkrt_unet_get_params_host(Unet* u, float* params, float* grads) {
     return e;
 }
 
+// Adam's moments and step count, for checkpoints (set_params resets them).
+cudaError_t gkrt_unet_get_state_host(Unet* u, float* m, float* v, uint64_t* step) {
+    if (!u->p) return cudaErrorInvalidValue;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess && m) e = cudaMemcpy(m, u->m, u->nparams * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && v) e = cudaMemcpy(v, u->v, u->nparams * 4, cudaMemcpyDeviceToHost);
+    if (step) *step = (uint64_t)u->step;
+    return e;
+}
+cudaError_t gkrt_unet_set_state_host(Unet* u, const float* m, const float* v, uint64_t step) {
+    if (!u->p || step > 0x7FFFFFFFull) return cudaErrorInvalidValue;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(u->m, m, u->nparams * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(u->v, v, u->nparams * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) u->step = (int)step;
+    return e;
+}
+
 cudaError_t gkrt_unet_zero_grad(Unet* u, cudaStream_t st) { return cudaMemsetAsync(u->g, 0, u->nparams * 4, st); }
 
 cudaError_t gkrt_unet_forward_dev(Unet* u, const float* input, int b, int h, int w, float* out_linear, float* out_raw,

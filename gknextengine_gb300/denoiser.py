@@ -143,6 +143,32 @@ class Unet:
         p = np.ascontiguousarray(p, np.float32)
         self._check(self.L.gkrt_unet_set_params(self.h, p.ctypes.data))
 
+    def optimizer_state(self):
+        """(first moments, second moments, step) of Adam."""
+        m = np.zeros(self.nparams, np.float32)
+        v = np.zeros(self.nparams, np.float32)
+        step = C.c_uint64()
+        self._check(self.L.gkrt_unet_get_state(self.h, m.ctypes.data, v.ctypes.data, C.byref(step)))
+        return m, v, step.value
+
+    def set_optimizer_state(self, m, v, step: int):
+        m = np.ascontiguousarray(m, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        self._check(self.L.gkrt_unet_set_state(self.h, m.ctypes.data, v.ctypes.data, int(step)))
+
+    def save(self, path: str):
+        """Parameters and Adam's state to a checkpoint file (checkpoint.py)."""
+        from . import checkpoint
+        m, v, step = self.optimizer_state()
+        checkpoint.save(path, self.params(), m, v, step)
+
+    def load(self, path: str):
+        """Restore a checkpoint written by save(); training continues from its step."""
+        from . import checkpoint
+        p, m, v, step = checkpoint.load(path, self.nparams)
+        self.set_params(p)
+        self.set_optimizer_state(m, v, step)
+
 
 def train(net: Unet, data: CornellVariants, refs, steps: int, batch: int = 2, lr: float = 5e-4, seed: int = 9,
           lr_decay_from: float = 0.6, warmup: int = 40):

@@ -456,6 +456,10 @@ int  gkrt_unet_init(GkrtContext* ctx, uint64_t seed);
 int  gkrt_unet_param_count(GkrtContext* ctx, uint32_t* count);
 int  gkrt_unet_get_params(GkrtContext* ctx, float* params, float* grads);
 int  gkrt_unet_set_params(GkrtContext* ctx, const float* params);
+/* Adam's first and second moments (gkrt_unet_param_count floats each, host memory) and its step
+ * count, for checkpoints: restored after gkrt_unet_set_params, training resumes where it was. */
+int  gkrt_unet_get_state(GkrtContext* ctx, float* m, float* v, uint64_t* step);
+int  gkrt_unet_set_state(GkrtContext* ctx, const float* m, const float* v, uint64_t step);
 int  gkrt_unet_forward(GkrtContext* ctx, const float* input, uint32_t batch, uint32_t height, uint32_t width,
                        float* out_linear, float* out_raw, void* stream);
 int  gkrt_unet_backward(GkrtContext* ctx, const float* d_raw, void* stream);

@@ -81,6 +81,37 @@ def test_unet_overfits_a_batch():
         assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
 
 
+def test_checkpoint_resume(tmp_path):
+    """Save after a few steps, load into a freshly initialised network on another context:
+    parameters and Adam's state come back bit for bit, and both networks then take the same
+    steps (equal up to the float-atomic order of the gradient sums)."""
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(2)
+    inp = torch.rand((2, 32, 32, 10), device="cuda", generator=g)
+    tgt = 0.8 * inp[..., 3:6] * inp[..., 4:5] + 0.1
+    path = str(tmp_path / "unet.ckpt")
+    with PathTracingRenderer(0) as r1, PathTracingRenderer(0) as r2:
+        a = Unet(r1, seed=5)
+        for _ in range(5):
+            a.train_step(inp, tgt, 1e-3)
+        a.save(path)
+        pa, (ma, va, sa) = a.params(), a.optimizer_state()
+        assert sa == 5
+        b = Unet(r2, seed=11)
+        assert not np.array_equal(b.params(), pa)
+        b.load(path)
+        mb, vb, sb = b.optimizer_state()
+        assert np.array_equal(b.params().view(np.uint32), pa.view(np.uint32))
+        assert np.array_equal(mb.view(np.uint32), ma.view(np.uint32)) and np.array_equal(vb.view(np.uint32),
+                                                                                          va.view(np.uint32))
+        assert sb == sa
+        la = [a.train_step(inp, tgt, 1e-3) for _ in range(3)]
+        lb = [b.train_step(inp, tgt, 1e-3) for _ in range(3)]
+        np.testing.assert_allclose(la, lb, rtol=1e-3)
+        np.testing.assert_allclose(b.params(), a.params(), rtol=1e-3, atol=1e-5)
+        assert b.optimizer_state()[2] == 8
+
+
 def test_denoiser_beats_bilateral():
     """Train on 512 x 512 Cornell variants (256-spp targets), then on a held-out 1080p variant
     compare RelMSE against 4096 spp: the network must reach <= 0.8 x the bilateral filter's
