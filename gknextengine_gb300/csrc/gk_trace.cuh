@@ -81,6 +81,26 @@ constexpr bool kSpeculative = false;   // measured: 4.01 ms without, 4.16 ms wit
 constexpr uint32_t kErrStack = 1u, kErrIter = 2u;
 // (4u is the TMA wait timeout of the post passes, gk_tma.cuh)
 constexpr uint32_t kErrRefit = 8u;   // a refit box that the 8-wide nodes cannot quantize
+constexpr uint32_t kErrBounds = 16u;  // checked builds: an index outside its array (access skipped)
+
+// Checked builds (GKRT_CHECKED) test every node, triangle and instance index against its array
+// before the access; a bad index records kErrBounds, ends the ray and skips the access. The
+// default build compiles the checks away.
+#ifdef GKRT_CHECKED
+#define GK_CHECK_OR_END(ok, S, T, ret)              \
+    do {                                            \
+        if (!(ok)) {                                \
+            atomicOr((S).error, kErrBounds);        \
+            (T).done = true;                        \
+            (T).has_leaf = false;                   \
+            return ret;                             \
+        }                                           \
+    } while (0)
+#else
+#define GK_CHECK_OR_END(ok, S, T, ret) \
+    do {                               \
+    } while (0)
+#endif
 
 // Per-thread event counts, flushed once per warp at the end of a kernel.
 struct Counters {
@@ -95,6 +115,7 @@ struct SceneView {
     int tlas_root;          // two-child root of the instance level, -1: empty scene
     int tlas_wide_root;     // wide root of the instance level
     uint32_t* error;
+    uint32_t node_count, wide_count, tri_count, inst_count;   // array sizes (checked builds)
 };
 
 struct Shear {
@@ -457,6 +478,7 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         return true;
     }
     if (ref >= 0) {
+        GK_CHECK_OR_END((uint32_t)ref < S.node_count, S, T, false);
         ++cn.nodes;
         const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
         const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
@@ -483,6 +505,7 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
     const uint32_t payload = ~(uint32_t)ref;
     if (!T.inblas) {
         T.cur = payload >> 3;
+        GK_CHECK_OR_END(T.cur < S.inst_count, S, T, false);
         const DevInst* ip = S.inst + T.cur;
         float w[12];
 #pragma unroll
@@ -551,6 +574,7 @@ GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int st
             }
             const uint32_t w = e[stride];
             if (__uint_as_float(e[2 * stride]) > T.tcull) { --T.sp; continue; }
+            GK_CHECK_OR_END(node < S.wide_count, S, T, false);
             const uint32_t c = w & 7u, slot = (w >> 3) & 7u;
             if (c <= 1u) --T.sp;
             else e[stride] = ((w >> 3) & ~7u) | (c - 1u);
@@ -559,6 +583,7 @@ GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int st
         }
     }
     if (ref >= 0) {
+        GK_CHECK_OR_END((uint32_t)ref < S.wide_count, S, T, false);
         ++cn.nodes;
         const float4* np = reinterpret_cast<const float4*>(S.wide + ref);
         const float4 h = __ldg(np);
@@ -627,6 +652,7 @@ GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int st
     const uint32_t payload = ~(uint32_t)ref;
     if (!T.inblas) {
         T.cur = payload >> 3;
+        GK_CHECK_OR_END(T.cur < S.inst_count, S, T, false);
         const DevInst* ip = S.inst + T.cur;
         float w[12];
 #pragma unroll
@@ -658,6 +684,7 @@ GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int st
 // Leaf phase: test the postponed leaf's triangles.
 GK_D void trav_leaf_step(Trav& T, const SceneView& S, Counters& cn) {
     if (!T.has_leaf) return;
+    GK_CHECK_OR_END((T.leaf >> 3) + (T.leaf & 7u) + 1u <= S.tri_count, S, T, );
     T.has_leaf = false;
     if (trav_leaf(T, S, T.leaf >> 3, (T.leaf & 7u) + 1u, cn)) T.done = true;
 }

@@ -88,6 +88,7 @@ struct GkrtContext {
     bool host_build = false;          // GKRT_BUILD_ON_HOST
     GpuBvh* builder = nullptr;
     uint32_t blas_node_count = 0, blas_nodes_used = 0;
+    uint32_t tri_count = 0;           // triangles in d_tris
     std::vector<int> blas_root;
     std::vector<float> blas_box;      // 6 per mesh
     float* d_blas_box = nullptr;
@@ -215,6 +216,7 @@ void free_scene(GkrtContext* c) {
     c->blas_ready = c->tlas_ready = false;
     c->tlas_root = -1;
     c->blas_node_count = c->blas_nodes_used = 0;
+    c->tri_count = 0;
     c->meshes.clear(); c->inst.clear(); c->pos_host.clear(); c->idx_host.clear();
     c->blas_root.clear(); c->blas_box.clear();
     dfree(c->refit.parent); dfree(c->refit.leaf); dfree(c->refit.wsrc);
@@ -479,6 +481,7 @@ int build_blas_gpu(GkrtContext* ctx, cudaStream_t st) {
     for (const GkrtMesh& m : ctx->meshes) ntri += m.index_count / 3;
     dfree(ctx->d_tris);
     if (ntri) GK_CUDA(cudaMalloc((void**)&ctx->d_tris, 3 * ntri * sizeof(float4)));
+    ctx->tri_count = (uint32_t)ntri;
     int rc;
     if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
     GpuBvhResult r;
@@ -542,6 +545,7 @@ int build_blas_host(GkrtContext* ctx, cudaStream_t st) {
     }
     int rc = upload(ctx, ctx->d_tris, tris.data(), tris.size() * sizeof(float4));
     if (rc != GKRT_OK) return rc;
+    ctx->tri_count = (uint32_t)(tris.size() / 3);
     ctx->blas_node_count = ctx->blas_nodes_used = (uint32_t)nodes.size();
     dfree(ctx->d_nodes);
     ctx->d_nodes_cap = 0;
@@ -710,6 +714,10 @@ SceneView scene_view(GkrtContext* c) {
     S.tlas_root = c->tlas_root;
     S.tlas_wide_root = c->tlas_wide_root;
     S.error = c->d_error;
+    S.node_count = (uint32_t)c->d_nodes_cap;
+    S.wide_count = (uint32_t)c->d_wide_cap;
+    S.tri_count = c->tri_count;
+    S.inst_count = (uint32_t)c->inst.size();
     return S;
 }
 

@@ -23,11 +23,13 @@ class GkrtError(RuntimeError):
 
 
 def load(path: str | None = None):
-    """Load libgkrt.so; raises if it is absent (build it with gknextengine_gb300.build)."""
+    """Load libgkrt.so (or the library the environment variable GKRT_LIBRARY names, e.g. the
+    bounds-checked libgkrt_checked.so); raises if it is absent (build it with
+    gknextengine_gb300.build)."""
     global _lib
     if _lib is not None:
         return _lib
-    p = path or LIB_PATH
+    p = path or os.environ.get("GKRT_LIBRARY") or LIB_PATH
     if not os.path.exists(p):
         raise RuntimeError(f"libgkrt.so not found at {p}: run __graft_entry__.build() first")
     L = C.CDLL(p)
