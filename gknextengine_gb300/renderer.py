@@ -30,6 +30,7 @@ class PathTracingRenderer:
             raise native.GkrtError(rc, "gkrt_context_create failed")
         self._h = h
         self.width = self.height = 0
+        self.output_width = self.output_height = 0   # presentation image (output_resize)
         self._scene = None
 
     # -- helpers ---------------------------------------------------------------------------
