@@ -1,6 +1,7 @@
 """Output stage on the CPU: the oracle's resolve blit, FSR compose and screenshot crop on
 properties that pin them (identity scale, constant images, clipping, UNORM rounding), the
-resolve blit against an independent numpy restatement, and the PNG / PFM writers."""
+resolve blit and the FSR EASU against independent numpy restatements (vectorised float32 in
+the same operation order), and the PNG / PFM writers."""
 import numpy as np
 import pytest
 
@@ -139,3 +140,112 @@ def test_pfm_round_trip(tmp_path):
     p = tmp_path / "x.pfm"
     imageio.write_pfm(str(p), a)
     assert np.array_equal(imageio.read_pfm(str(p)), a[..., :3])
+
+
+def easu_numpy(src, out_w, out_h, outw, outh, offx=0, offy=0):
+    """Process.UpScaleFSR.comp.slang (EASU, different sizes) restated with numpy float32 in the
+    shader's operation order; fmin/fmax ignore NaN as the GPU's min/max do."""
+    f = np.float32
+    H, W = src.shape[:2]
+    Wf, Hf, OWf, OHf = f(W), f(H), f(out_w), f(out_h)
+    gw, gh = (outw // 8) * 8, (outh // 8) * 8
+    ys, xs = np.meshgrid(np.arange(gh), np.arange(gw), indexing="ij")
+    ipx = (xs.astype(f) / f(outw)) * OWf
+    ipy = (ys.astype(f) / f(outh)) * OHf
+    c0 = (Wf / OWf, Hf / OHf, f(0.5) * Wf / OWf - f(0.5), f(0.5) * Hf / OHf - f(0.5))
+    c1 = (f(1) / Wf, f(1) / Hf, f(1) / Wf, f(-1) / Hf)
+    c2 = (f(-1) / Wf, f(2) / Hf, f(1) / Wf, f(2) / Hf)
+    c3 = (f(0) / Wf, f(4) / Hf)
+    ppx, ppy = ipx * c0[0] + c0[2], ipy * c0[1] + c0[3]
+    fpx, fpy = np.floor(ppx), np.floor(ppy)
+    ppx, ppy = ppx - fpx, ppy - fpy
+    p0x, p0y = fpx * c1[0] + c1[2], fpy * c1[1] + c1[3]
+    p1x, p1y = p0x + c2[0], p0y + c2[1]
+    p2x, p2y = p0x + c2[2], p0y + c2[3]
+    p3x, p3y = p0x + c3[0], p0y + c3[1]
+    ox, oy, oz, ow = f(-0.5) * c1[0], f(0.5) * c1[0], f(-0.5) * c1[1], f(0.5) * c1[1]
+
+    def cf(px, py):
+        cx = np.clip((px * Wf).astype(np.int64), 0, W - 1)
+        cy = np.clip((py * Hf).astype(np.int64), 0, H - 1)
+        return src[cy, cx]                       # (gh, gw, 4)
+
+    bC, cC = cf(p0x + ox, p0y + ow), cf(p0x + oy, p0y + ow)
+    iC, jC = cf(p1x + ox, p1y + ow), cf(p1x + oy, p1y + ow)
+    fC, eC = cf(p1x + oy, p1y + oz), cf(p1x + ox, p1y + oz)
+    kC, lC = cf(p2x + ox, p2y + ow), cf(p2x + oy, p2y + ow)
+    hC, gC = cf(p2x + oy, p2y + oz), cf(p2x + ox, p2y + oz)
+    oC, nC = cf(p3x + oy, p3y + oz), cf(p3x + ox, p3y + oz)
+    L = lambda c: c[..., 1] + f(0.5) * (c[..., 0] + c[..., 2])
+    bL, cL, iL, jL, fL, eL, kL, lL, hL, gL, oL, nL = (L(c) for c in (bC, cC, iC, jC, fC, eC, kC, lC, hC, gC, oC, nC))
+    sat = lambda v: np.fmin(np.fmax(v, f(0)), f(1))
+    dx = np.zeros_like(ppx); dy = np.zeros_like(ppx); ln = np.zeros_like(ppx)
+
+    def setf(w, lA, lB, lC_, lD, lE):
+        nonlocal dx, dy, ln
+        with np.errstate(divide="ignore", invalid="ignore"):
+            lenX = np.fmax(np.abs(lD - lC_), np.abs(lC_ - lB))
+            dirX = lD - lB
+            dx = dx + dirX * w
+            lenX = sat(np.abs(dirX) / lenX)
+            lenX = lenX * lenX
+            ln = ln + lenX * w
+            lenY = np.fmax(np.abs(lE - lC_), np.abs(lC_ - lA))
+            dirY = lE - lA
+            dy = dy + dirY * w
+            lenY = sat(np.abs(dirY) / lenY)
+            lenY = lenY * lenY
+            ln = ln + lenY * w
+
+    one = f(1)
+    setf((one - ppx) * (one - ppy), bL, eL, fL, gL, jL)
+    setf(ppx * (one - ppy), cL, fL, gL, hL, kL)
+    setf((one - ppx) * ppy, fL, iL, jL, kL, nL)
+    setf(ppx * ppy, gL, jL, kL, lL, oL)
+    dirR = dx * dx + dy * dy
+    zro = dirR < f(1.0 / 32768.0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        dirR = f(1) / np.sqrt(dirR)
+    dirR = np.where(zro, f(1), dirR).astype(f)
+    dx = np.where(zro, f(1), dx).astype(f)
+    dx, dy = dx * dirR, dy * dirR
+    ln = ln * f(0.5)
+    ln = ln * ln
+    stretch = (dx * dx + dy * dy) / np.fmax(np.abs(dx), np.abs(dy))
+    l2x, l2y = one + (stretch - one) * ln, one - f(0.5) * ln
+    lob = f(0.5) - f(0.29) * ln
+    clp = one / lob
+    mn = np.fmin(np.fmin(fC, gC), np.fmin(jC, kC))
+    mx = np.fmax(np.fmax(fC, gC), np.fmax(jC, kC))
+    aC = np.zeros(ppx.shape + (4,), f)
+    aW = np.zeros_like(ppx)
+    for (tx, ty), c in (((0, -1), bC), ((1, -1), cC), ((-1, 1), iC), ((0, 1), jC), ((0, 0), fC), ((-1, 0), eC),
+                        ((1, 1), kC), ((2, 1), lC), ((2, 0), hC), ((1, 0), gC), ((1, 2), oC), ((0, 2), nC)):
+        offx_, offy_ = f(tx) - ppx, f(ty) - ppy
+        vx = offx_ * dx + offy_ * dy
+        vy = offx_ * (-dy) + offy_ * dx
+        vx, vy = vx * l2x, vy * l2y
+        d2 = np.fmin(vx * vx + vy * vy, clp)
+        wB = f(0.4) * d2 - one
+        wA = lob * d2 - one
+        wB, wA = wB * wB, wA * wA
+        wB = f(1.5625) * wB - f(0.5625)
+        w = wB * wA
+        aC = aC + c * w[..., None]
+        aW = aW + w
+    with np.errstate(divide="ignore", invalid="ignore"):
+        q = aC / aW[..., None]
+    pix = np.fmin(mx, np.fmax(mn, q)).astype(f)
+    out = np.zeros((out_h, out_w), np.uint32)
+    X, Y = xs + offx, ys + offy
+    ok = (X >= 0) & (Y >= 0) & (X < out_w) & (Y < out_h)
+    out[Y[ok], X[ok]] = quantize(pix)[ok]
+    return out
+
+
+@pytest.mark.filterwarnings("ignore::RuntimeWarning")   # the fixture's NaN and inf texels
+@pytest.mark.parametrize("out_w,out_h,outw,outh,off", [(80, 60, 80, 60, (0, 0)), (123, 77, 123, 77, (0, 0)),
+                                                        (200, 150, 64, 45, (30, 20)), (50, 40, 50, 40, (-9, 5))])
+def test_fsr_matches_numpy(img, out_w, out_h, outw, outh, off):
+    o = O.output_fsr(img, out_w, out_h, off, (outw, outh))
+    assert np.array_equal(o, easu_numpy(img, out_w, out_h, outw, outh, *off))
