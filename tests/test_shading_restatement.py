@@ -15,7 +15,8 @@ pure Python (FP64) written from the shader text, on a small Cornell render:
 Choices where the shader leaves room, as this build reads it: ?: evaluates one side; the sky is
 the constant colour (capped at 10) times the intensity; the camera ray is traced (the
 visibility-buffer raster needs a graphics API). FP32 (oracle) against FP64 (here): per-pixel
-radiance within 1e-3 relative on nearly every pixel (paths through triangle edges may part)."""
+radiance within 1e-3 relative on nearly every pixel (paths through triangle edges may part;
+through the glass box on about 94 %), image means within 0.5 %."""
 import math
 
 import numpy as np
@@ -307,11 +308,18 @@ def render_pixel(S, fc, W, H, x, y):
     return tuple(final_c[:3]), tuple(final_r[:3])
 
 
-@pytest.mark.parametrize("sky_sun", [False, True])
-def test_rt_pass_matches_the_python_restatement(sky_sun):
+@pytest.mark.parametrize("sky_sun,materials", [(False, False), (True, False), (True, True)])
+def test_rt_pass_matches_the_python_restatement(sky_sun, materials):
     sc, cam, st = scenes.cornell()
     st.taa = False
     st.samples = 16           # most pixels then carry light from some path (zero probes end the rest)
+    if materials:             # the boxes as a rough metal and a glass: GGX VNDF, metal tint, refraction
+        sc.materials[5]["metalness"] = 1.0
+        sc.materials[5]["fuzziness"] = 0.2
+        sc.materials[6]["material_model"] = abi.MAT_DIELECTRIC
+        sc.materials[6]["refraction_index"] = 1.5
+        sc.materials[6]["refraction_index2"] = 1.5
+        sc.materials[6]["fuzziness"] = 0.0
     if sky_sun:
         st.has_sky, st.sky_color, st.sky_intensity = True, (0.6, 0.7, 0.9, 1.0), 1.5
         st.has_sun, st.sun_direction, st.sun_intensity = True, (0.3, 0.6, 1.0), 3.0
@@ -329,9 +337,15 @@ def test_rt_pass_matches_the_python_restatement(sky_sun):
             ref_d[y, x], ref_s[y, x] = render_pixel(S, fc, W, H, x, y)
     close = (np.isclose(got_d, ref_d, rtol=1e-3, atol=1e-4).all(axis=-1) &
              np.isclose(got_s, ref_s, rtol=1e-3, atol=1e-4).all(axis=-1))
-    assert close.mean() >= 0.98, (close.mean(), np.argwhere(~close)[:5])
+    # Refraction and internal reflection in the glass box carry FP32-vs-FP64 differences to the
+    # box's edges, where a path's next hit can change (neighbouring pixels then trade values):
+    # per pixel a lower bar there, and the image means, which such trades leave unchanged.
+    assert close.mean() >= (0.90 if materials else 0.98), (close.mean(), np.argwhere(~close)[:5])
+    if sky_sun:   # dense images (every pixel sees sky or sun); the C1 image is sparse
+        np.testing.assert_allclose(got_d.mean(), ref_d.mean(), rtol=5e-3)
+        np.testing.assert_allclose(got_s.mean(), ref_s.mean(), rtol=5e-3, atol=1e-6)
     lit = ref_d.sum(axis=-1) > 0
     assert lit.mean() > 0.15                                           # a fifth of the pixels carry light
-    assert close[lit].mean() >= 0.97                                   # and those agree too
+    assert close[lit].mean() >= (0.90 if materials else 0.97)          # and those agree too
     if sky_sun:
         assert (ref_d.max(axis=-1) > 0.0).mean() > 0.5
