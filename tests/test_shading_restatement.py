@@ -10,7 +10,9 @@ pure Python (FP64) written from the shader text, on a small Cornell render:
 * Render (:1084-1184) with GetRayColor (:1003-1082): Schlick reflect / metal choices, GGX VNDF
   or cosine hemisphere (Const_Func.slang:290-340), back faces, emitters, sky, the sun-cone NEE
   per bounce, the 0.5 early exit, zero ambient probes at termination, the primary's direct sun
-  light (:886-908); PCG4D seeds per pixel (Const_Func.slang:227-258).
+  light (:886-908); PCG4D seeds per pixel (Const_Func.slang:227-258);
+* the primary G-buffer of PrimaryHit (:1187-1223): albedo, normal and roughness, object id,
+  motion vector and moment of a moving instance under a moving camera, NDC depth.
 
 Choices where the shader leaves room, as this build reads it: ?: evaluates one side; the sky is
 the constant colour (capped at 10) times the intensity; the camera ray is traced (the
@@ -349,3 +351,76 @@ def test_rt_pass_matches_the_python_restatement(sky_sun, materials):
     assert close[lit].mean() >= (0.90 if materials else 0.97)          # and those agree too
     if sky_sun:
         assert (ref_d.max(axis=-1) > 0.0).mean() > 0.5
+
+
+def primary_gbuffer(S, fc, W, H, x, y):
+    """PrimaryHit (Shading.slang:1187-1223): albedo, normal and roughness (FetchGBufferV2,
+    Shading.slang:82-112, untextured), object id, motion vector in pixels and its moment
+    (CalculateMotionVectorV2, Shading.slang:50-72, on zeroed moments), NDC depth; the miss
+    defaults otherwise."""
+    sc = S.sc
+    rng = Rng(x, y, fc.total_frames)
+    uvx, uvy = x / W * 2.0 - 1.0, y / H * 2.0 - 1.0
+    disk = unit_disk(rng)
+    ha = fc.aperture / 2.0
+    mvi, pinv = list(fc.model_view_inverse), list(fc.projection_inverse)
+    origin = mat4(mvi, (ha * disk[0], ha * disk[1], 0.0, 1.0))[:3]
+    target = mat4(pinv, (uvx, uvy, 1.0, 1.0))
+    tn = norm((target[0] * fc.focus_distance - ha * disk[0], target[1] * fc.focus_distance - ha * disk[1],
+               target[2] * fc.focus_distance))
+    direction = mat4(mvi, (tn[0], tn[1], tn[2], 0.0))[:3]
+    h = S.hit(origin, direction)
+    if h is None:
+        return {"albedo": (1.0, 1.0, 1.0, 1.0), "normal": (0.0, 1.0, 0.0, 1.0), "id": 65535,
+                "motion": (0.0, 0.0), "depth": 100000.0, "moment": 0, "prim": 0xFFFFFFFF}
+    pv = S.vertex(origin, direction, h)
+    P = pv["P"]
+    m = sc.materials[pv["mat"]]
+    inst = sc.instances[h[0][1]]
+    clip = mat4(list(fc.view_projection), (*P, 1.0))
+    cur = mat4(list(fc.view_projection_unjit), (*P, 1.0))
+    cp = [float(c) for c in inst["combined_prev"]]
+    prevP = tuple(cp[4 * r] * P[0] + cp[4 * r + 1] * P[1] + cp[4 * r + 2] * P[2] + cp[4 * r + 3]
+                  for r in range(3))
+    prv = mat4(list(fc.prev_view_projection_unjit), (*prevP, 1.0))
+    motion = ((prv[0] / prv[3] - cur[0] / cur[3]) * 0.5 * W, (prv[1] / prv[3] - cur[1] / cur[3]) * 0.5 * H)
+    moment = fc.temporal_frames if math.dist(P, prevP) > 0.02 else 0
+    return {"albedo": tuple(float(c) for c in m["diffuse"][:4]), "normal": (*pv["N"], float(m["fuzziness"])),
+            "id": int(inst["instance_id"]), "motion": motion, "depth": clip[2] / clip[3], "moment": moment,
+            "prim": h[0][2]}
+
+
+def test_primary_gbuffer_matches_the_python_restatement():
+    sc, cam, st = scenes.cornell()
+    st.taa = False
+    # the tall box moved 0.1 along x since last frame (its motion vectors and moments), the
+    # camera orbited a little (everyone's motion vectors)
+    cp = sc.instances["combined_prev"][2].reshape(3, 4).astype(np.float64)
+    cp[0, 3] += 0.1
+    sc.instances["combined_prev"][2] = cp.reshape(-1).astype(np.float32)
+    W = H = 32
+    fb = camera.FrameBuilder(W, H, st)
+    fb.build(cam.orbit(0.02), 4)
+    fc = fb.build(cam, 5)
+    im = O.new_images(W, H)
+    O.OracleScene(sc).trace_pass(fc, W, H, im)
+    S = Scene(sc)
+    ref = [[primary_gbuffer(S, fc, W, H, x, y) for x in range(W)] for y in range(H)]
+    rid = np.array([[p["id"] for p in row] for row in ref], np.uint32)
+    rprim = np.array([[p["prim"] for p in row] for row in ref], np.uint32)
+    same = (im[abi.IMG_OBJECT_ID] == rid) & (im[abi.IMG_HIT_PRIM] == rprim)
+    # which triangle a pixel sees may part only on an edge (the exact FP64 watertight test
+    # against FP64 Moller-Trumbore); everything else is compared where both see the same one
+    assert same.mean() >= 0.99, np.argwhere(~same)[:5]
+    assert {0, 1, 2, 65535} <= set(np.unique(rid).tolist())
+    def field(k):
+        return np.array([[p[k] for p in row] for row in ref], np.float64)
+    np.testing.assert_array_equal(im[abi.IMG_ALBEDO][same], field("albedo")[same].astype(np.float32))
+    np.testing.assert_allclose(im[abi.IMG_NORMAL][same], field("normal")[same], atol=2e-6)
+    np.testing.assert_allclose(im[abi.IMG_PREV_DEPTH][same], field("depth")[same], rtol=1e-6, atol=1e-6)
+    mv = field("motion")
+    np.testing.assert_allclose(im[abi.IMG_MOTION][same], mv[same], atol=1e-4)   # pixels
+    moved = same & (rid == 2)
+    assert moved.any() and np.all(np.abs(mv[moved][:, 0]) > 0.5)      # the box moved on screen
+    np.testing.assert_array_equal(im[abi.IMG_MOTION_MOMENT][same], field("moment")[same].astype(np.uint32))
+    assert np.all(im[abi.IMG_MOTION_MOMENT][moved] == fc.temporal_frames)
