@@ -12,7 +12,8 @@ pure Python (FP64) written from the shader text, on a small Cornell render:
   per bounce, the 0.5 early exit, zero ambient probes at termination, the primary's direct sun
   light (:886-908); PCG4D seeds per pixel (Const_Func.slang:227-258);
 * the primary G-buffer of PrimaryHit (:1187-1223): albedo, normal and roughness, object id,
-  motion vector and moment of a moving instance under a moving camera, NDC depth.
+  motion vector and moment of a moving instance under a moving camera, NDC depth; with and
+  without the TAA jitter (the Halton (2, 3) table of Shading.slang:4-13, computed here).
 
 Choices where the shader leaves room, as this build reads it: ?: evaluates one side; the sky is
 the constant colour (capped at 10) times the intensity; the camera ray is traced (the
@@ -353,6 +354,19 @@ def test_rt_pass_matches_the_python_restatement(sky_sun, materials):
         assert (ref_d.max(axis=-1) > 0.0).mean() > 0.5
 
 
+def radical_inverse(i, base):
+    f, r = 1.0, 0.0
+    while i:
+        f /= base
+        r += f * (i % base)
+        i //= base
+    return r
+
+
+# The TAA jitter table (Shading.slang:4-13): Halton (2, 3) points 1..8, base 3 to four decimals.
+HALTON = [(radical_inverse(i, 2), round(radical_inverse(i, 3), 4)) for i in range(1, 9)]
+
+
 def primary_gbuffer(S, fc, W, H, x, y):
     """PrimaryHit (Shading.slang:1187-1223): albedo, normal and roughness (FetchGBufferV2,
     Shading.slang:82-112, untextured), object id, motion vector in pixels and its moment
@@ -361,6 +375,9 @@ def primary_gbuffer(S, fc, W, H, x, y):
     sc = S.sc
     rng = Rng(x, y, fc.total_frames)
     uvx, uvy = x / W * 2.0 - 1.0, y / H * 2.0 - 1.0
+    if fc.taa:
+        hx, hy = HALTON[fc.total_frames % 8]
+        uvx, uvy = uvx + (hx - 0.5) / W, uvy + (hy - 0.5) / H
     disk = unit_disk(rng)
     ha = fc.aperture / 2.0
     mvi, pinv = list(fc.model_view_inverse), list(fc.projection_inverse)
@@ -390,9 +407,10 @@ def primary_gbuffer(S, fc, W, H, x, y):
             "prim": h[0][2]}
 
 
-def test_primary_gbuffer_matches_the_python_restatement():
+@pytest.mark.parametrize("taa", [False, True])
+def test_primary_gbuffer_matches_the_python_restatement(taa):
     sc, cam, st = scenes.cornell()
-    st.taa = False
+    st.taa = taa              # Halton jitter of the primary ray, frame 5 (and frame 4 before it)
     # the tall box moved 0.1 along x since last frame (its motion vectors and moments), the
     # camera orbited a little (everyone's motion vectors)
     cp = sc.instances["combined_prev"][2].reshape(3, 4).astype(np.float64)
