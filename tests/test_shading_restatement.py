@@ -9,8 +9,10 @@ pure Python (FP64) written from the shader text, on a small Cornell render:
   the instance's slot table of vertex 0;
 * Render (:1084-1184) with GetRayColor (:1003-1082): Schlick reflect / metal choices, GGX VNDF
   or cosine hemisphere (Const_Func.slang:290-340), back faces, emitters, sky, the sun-cone NEE
-  per bounce, the 0.5 early exit, zero ambient probes at termination, the primary's direct sun
-  light (:886-908); PCG4D seeds per pixel (Const_Func.slang:227-258);
+  per bounce, the 0.5 early exit, the primary's direct sun light (:886-908); PCG4D seeds per
+  pixel (Const_Func.slang:227-258);
+* path ends on zero probes, or on a random ambient-cube grid through interpolateAmbientCubesV2
+  with the full sampler (AmbientCube.slang:178-222, 290-382; layouts BasicTypes.slang:116-151);
 * the primary G-buffer of PrimaryHit (:1187-1223): albedo, normal and roughness, object id,
   motion vector and moment of a moving instance under a moving camera, NDC depth; with and
   without the TAA jitter (the Halton (2, 3) table of Shading.slang:4-13, computed here).
@@ -149,6 +151,8 @@ def mat4(m, v):
 class Scene:
     def __init__(self, sc):
         self.sc = sc
+        self.probes = None if sc.probe_cubes is None else (sc.probe_cubes.reshape(-1, 14),
+                                                           sc.probe_voxels.reshape(-1, 4))
         self.tris = []                                  # (inst, prim, v0, v1, v2, i0, i1, i2)
         for ii, inst in enumerate(sc.instances):
             if not inst["visible"]:
@@ -208,6 +212,94 @@ class Scene:
         slot = int(sc.material_slots[idx[0]]) & 15
         mat = int(sc.instances[ii]["mat_id"][slot])
         return {"P": add(o, mul(d, t)), "N": nw, "mat": mat}
+
+
+# Ambient-cube probe grid (AmbientCube.slang:12-15): 192 x 48 x 192 probes, 0.25 m apart.
+CUBE_XY, CUBE_Z, CUBE_UNIT = 192, 48, 0.25
+CUBE_OFFSET = (-CUBE_XY / 2 * CUBE_UNIT, -1.375 * CUBE_UNIT, -CUBE_XY / 2 * CUBE_UNIT)
+
+
+def unpack_color(w):
+    """unpackRGB10A2 (AmbientCube.slang:74-81): 10-bit channels scaled to MAX_ILLUMINANCE 512."""
+    return ((w & 0x3FF) / 1023.0 * 512.0, ((w >> 10) & 0x3FF) / 1023.0 * 512.0,
+            ((w >> 20) & 0x3FF) / 1023.0 * 512.0, 0.0)
+
+
+def unpack_bytes(w):
+    return (w & 0xFF, (w >> 8) & 0xFF, (w >> 16) & 0xFF, (w >> 24) & 0xFF)
+
+
+def sample_cube_full(cube, n):
+    """sampleAmbientCubeHL2_Full (AmbientCube.slang:178-222). cube: the 14 words of AmbientCube
+    (BasicTypes.slang:116-137): PosZ NegZ PosY NegY PosX NegX, the same six _D, two sky words."""
+    wx, wnx, wy, wny, wz, wnz = (max(n[0], 0.0), max(-n[0], 0.0), max(n[1], 0.0), max(-n[1], 0.0),
+                                 max(n[2], 0.0), max(-n[2], 0.0))
+    total = wx + wnx + wy + wny + wz + wnz
+    s0, s1 = unpack_bytes(cube[12]), unpack_bytes(cube[13])
+    sky = s0[0] * wz + s0[1] * wnz + s0[2] * wy + s0[3] * wny + s1[0] * wx + s1[1] * wnx
+    face = {"PZ": 0, "NZ": 1, "PY": 2, "NY": 3, "PX": 4, "NX": 5}
+    weights = {"PX": wx, "NX": wnx, "PY": wy, "NY": wny, "PZ": wz, "NZ": wnz}
+    col = [0.0, 0.0, 0.0]
+    for shift in (6, 0):                                  # the _D faces, then the plain ones
+        for f, wgt in weights.items():
+            c = unpack_color(cube[face[f] + shift])
+            for k in range(3):
+                col[k] += wgt * c[k]
+    k = 1.0 / total if total > 0.0 else 1.0
+    return (col[0] * k, col[1] * k, col[2] * k, sky * k / 255.0)
+
+
+def probe_term(cubes, voxels, p, n):
+    """interpolateAmbientCubesV2<FullAmbientCubeSampler> (AmbientCube.slang:290-382): the eight
+    surrounding probes, trilinear weights, probes with no space around them (distance byte
+    below 0.01) or hidden behind the voxel distances skipped."""
+    near = [(p[k] - CUBE_OFFSET[k]) / CUBE_UNIT for k in range(3)]
+    if (min(near) < 0 or near[0] > CUBE_XY - 2 or near[1] > CUBE_Z - 2 or near[2] > CUBE_XY - 2):
+        return (0.0, 0.0, 0.0, 1.0)
+    base = [math.floor(c) for c in near]
+    frac = [c - b for c, b in zip(near, base)]
+    total, res = 0.0, [0.0] * 4
+    for i in range(8):
+        off = (i & 1, (i >> 1) & 1, (i >> 2) & 1)
+        q = [b + o for b, o in zip(base, off)]
+        idx = q[1] * CUBE_XY * CUBE_XY + q[2] * CUBE_XY + q[0]
+        d0 = [b / 255.0 for b in unpack_bytes(int(voxels[idx, 2]))]     # distanceToSolid_gg_z01
+        d1 = [b / 255.0 for b in unpack_bytes(int(voxels[idx, 3]))]     # distanceToSolid_x01_y01
+        if d0[1] < 0.01:
+            continue
+        pl = [f - o for f, o in zip(frac, off)]
+        dist = math.sqrt(dot(pl, pl))
+        if dist > 0.0:
+            dr = [c / dist for c in pl]
+            hit_len = (math.sqrt(max(dr[0], 0.0)) * d1[0] + math.sqrt(max(-dr[0], 0.0)) * d1[1] +
+                       math.sqrt(max(dr[1], 0.0)) * d1[2] + math.sqrt(max(-dr[1], 0.0)) * d1[3] +
+                       math.sqrt(max(dr[2], 0.0)) * d0[2] + math.sqrt(max(-dr[2], 0.0)) * d0[3])
+            if dist > hit_len + 0.05:
+                continue
+        wgt = 1.0
+        for k in range(3):
+            wgt *= (1.0 - frac[k]) if off[k] == 0 else frac[k]
+        c = sample_cube_full([int(w) for w in cubes[idx]], n)
+        for k in range(4):
+            res[k] += c[k] * wgt
+        total += wgt
+    return tuple(r / total for r in res) if total > 0.0 else (0.0, 0.0, 0.0, 0.0)
+
+
+def random_probe_grid(seed):
+    """Random cubes and voxel distances over the probes around the unit Cornell room; a fifth
+    of them with no space around them; zero (skipped) probes elsewhere."""
+    rng = np.random.default_rng(seed)
+    cubes = np.zeros((CUBE_Z, CUBE_XY, CUBE_XY, 14), np.uint32)
+    voxels = np.zeros((CUBE_Z, CUBE_XY, CUBE_XY, 4), np.uint32)
+    ys, xs = slice(0, 9), slice(90, 102)               # y rows, then z and x columns
+    cubes[ys, xs, xs] = rng.integers(0, 2 ** 32, cubes[ys, xs, xs].shape, dtype=np.uint32)
+    cubes[ys, xs, xs, :12] &= np.uint32(0x07F1FC7F)    # colours up to 64 per channel
+    vox = rng.integers(0, 2 ** 32, voxels[ys, xs, xs].shape, dtype=np.uint32)
+    empty = rng.random(vox.shape[:-1]) < 0.2
+    vox[..., 2] = np.where(empty, vox[..., 2] & np.uint32(0xFFFF00FF), vox[..., 2] | np.uint32(0x00000800))
+    voxels[ys, xs, xs] = vox
+    return cubes.reshape(-1, 14), voxels.reshape(-1, 4)
 
 
 def render_pixel(S, fc, W, H, x, y):
@@ -292,7 +384,10 @@ def render_pixel(S, fc, W, H, x, y):
                         break
                 early = b > 0 and not diel0 and rng.f1() < 0.5
                 if b == max_b - 1 or early:
-                    color = (0.0, 0.0, 0.0, 0.0)          # zero ambient probes
+                    if S.probes is None:
+                        color = (0.0, 0.0, 0.0, 0.0)      # zero ambient probes
+                    else:
+                        color = had(color, probe_term(*S.probes, v["P"], v["N"]))
                     break
         if hit_metal:
             color = had(color, primary_albedo)
@@ -311,8 +406,9 @@ def render_pixel(S, fc, W, H, x, y):
     return tuple(final_c[:3]), tuple(final_r[:3])
 
 
-@pytest.mark.parametrize("sky_sun,materials", [(False, False), (True, False), (True, True)])
-def test_rt_pass_matches_the_python_restatement(sky_sun, materials):
+@pytest.mark.parametrize("sky_sun,materials,probes", [(False, False, False), (True, False, False),
+                                                      (True, True, False), (False, False, True)])
+def test_rt_pass_matches_the_python_restatement(sky_sun, materials, probes):
     sc, cam, st = scenes.cornell()
     st.taa = False
     st.samples = 16           # most pixels then carry light from some path (zero probes end the rest)
@@ -326,6 +422,8 @@ def test_rt_pass_matches_the_python_restatement(sky_sun, materials):
     if sky_sun:
         st.has_sky, st.sky_color, st.sky_intensity = True, (0.6, 0.7, 0.9, 1.0), 1.5
         st.has_sun, st.sun_direction, st.sun_intensity = True, (0.3, 0.6, 1.0), 3.0
+    if probes:                # path ends read a random ambient-cube grid instead of zero probes
+        sc.probe_cubes, sc.probe_voxels = (a.reshape(-1) for a in random_probe_grid(7))
     W = H = 24
     fc = camera.FrameBuilder(W, H, st).build(cam, 5)
     im = O.new_images(W, H)
@@ -344,11 +442,12 @@ def test_rt_pass_matches_the_python_restatement(sky_sun, materials):
     # box's edges, where a path's next hit can change (neighbouring pixels then trade values):
     # per pixel a lower bar there, and the image means, which such trades leave unchanged.
     assert close.mean() >= (0.90 if materials else 0.98), (close.mean(), np.argwhere(~close)[:5])
-    if sky_sun:   # dense images (every pixel sees sky or sun); the C1 image is sparse
+    if sky_sun:   # dense, smooth images (every pixel sees sky or sun); the C1 image is sparse and
+        # random probe colours make single pixels weigh too much in the mean
         np.testing.assert_allclose(got_d.mean(), ref_d.mean(), rtol=5e-3)
         np.testing.assert_allclose(got_s.mean(), ref_s.mean(), rtol=5e-3, atol=1e-6)
     lit = ref_d.sum(axis=-1) > 0
-    assert lit.mean() > 0.15                                           # a fifth of the pixels carry light
+    assert lit.mean() > (0.8 if probes else 0.15)                      # pixels that carry light
     assert close[lit].mean() >= (0.90 if materials else 0.97)          # and those agree too
     if sky_sun:
         assert (ref_d.max(axis=-1) > 0.0).mean() > 0.5
