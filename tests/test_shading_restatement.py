@@ -166,7 +166,7 @@ class Scene:
     def winv(self, ii):
         return [float(x) for x in self.sc.instances[ii]["world_inv"]]
 
-    def hit(self, o, d, any_hit=False):
+    def hit(self, o, d, any_hit=False, tmax=TMAX):
         best = None
         cache = {}
         for ii, p, v0, v1, v2, idx in self.tris:
@@ -190,7 +190,7 @@ class Scene:
             if b2 < 0.0 or b1 + b2 > 1.0:
                 continue
             t = dot(e2, qv) / det
-            if t < EPS or t > TMAX:
+            if t < EPS or t > tmax:
                 continue
             if any_hit:
                 return True
