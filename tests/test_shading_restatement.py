@@ -166,7 +166,7 @@ class Scene:
     def winv(self, ii):
         return [float(x) for x in self.sc.instances[ii]["world_inv"]]
 
-    def hit(self, o, d, any_hit=False, tmax=TMAX):
+    def hit(self, o, d, any_hit=False, tmax=TMAX, tmin=EPS):
         best = None
         cache = {}
         for ii, p, v0, v1, v2, idx in self.tris:
@@ -190,7 +190,7 @@ class Scene:
             if b2 < 0.0 or b1 + b2 > 1.0:
                 continue
             t = dot(e2, qv) / det
-            if t < EPS or t > tmax:
+            if t < tmin or t > tmax:
                 continue
             if any_hit:
                 return True
@@ -249,10 +249,10 @@ def sample_cube_full(cube, n):
     return (col[0] * k, col[1] * k, col[2] * k, sky * k / 255.0)
 
 
-def probe_term(cubes, voxels, p, n):
-    """interpolateAmbientCubesV2<FullAmbientCubeSampler> (AmbientCube.slang:290-382): the eight
-    surrounding probes, trilinear weights, probes with no space around them (distance byte
-    below 0.01) or hidden behind the voxel distances skipped."""
+def probe_term(cubes, voxels, p, n, sampler=sample_cube_full):
+    """interpolateAmbientCubesV2<FullAmbientCubeSampler> (AmbientCube.slang:290-382), or with
+    another sampler: the eight surrounding probes, trilinear weights, probes with no space
+    around them (distance byte below 0.01) or hidden behind the voxel distances skipped."""
     near = [(p[k] - CUBE_OFFSET[k]) / CUBE_UNIT for k in range(3)]
     if (min(near) < 0 or near[0] > CUBE_XY - 2 or near[1] > CUBE_Z - 2 or near[2] > CUBE_XY - 2):
         return (0.0, 0.0, 0.0, 1.0)
@@ -279,7 +279,7 @@ def probe_term(cubes, voxels, p, n):
         wgt = 1.0
         for k in range(3):
             wgt *= (1.0 - frac[k]) if off[k] == 0 else frac[k]
-        c = sample_cube_full([int(w) for w in cubes[idx]], n)
+        c = sampler([int(w) for w in cubes[idx]], n)
         for k in range(4):
             res[k] += c[k] * wgt
         total += wgt
