@@ -13,6 +13,8 @@ pure Python (FP64) written from the shader text, on a small Cornell render:
   pixel (Const_Func.slang:227-258);
 * path ends on zero probes, or on a random ambient-cube grid through interpolateAmbientCubesV2
   with the full sampler (AmbientCube.slang:178-222, 290-382; layouts BasicTypes.slang:116-151);
+  FastGather's exit after the first bounce (ExitAfterFirst, :1118-1121); four times the samples
+  where a moving instance set the motion moment (Core.PathTracing.comp.slang:28);
 * the primary G-buffer of PrimaryHit (:1187-1223): albedo, normal and roughness, object id,
   motion vector and moment of a moving instance under a moving camera, NDC depth; with and
   without the TAA jitter (the Halton (2, 3) table of Shading.slang:4-13, computed here).
@@ -323,6 +325,10 @@ def render_pixel(S, fc, W, H, x, y):
     if h is None:
         return sky[:3], (0.0, 0.0, 0.0)
     pv = S.vertex(origin, direction, h)
+    cp = [float(c) for c in sc.instances[h[0][1]]["combined_prev"]]
+    prev_p = tuple(cp[4 * r] * pv["P"][0] + cp[4 * r + 1] * pv["P"][1] + cp[4 * r + 2] * pv["P"][2] + cp[4 * r + 3]
+                   for r in range(3))
+    moment = fc.temporal_frames if math.dist(pv["P"], prev_p) > 0.02 else 0      # zeroed moments before
     mat = sc.materials[pv["mat"]]
     if mat["material_model"] != abi.MAT_DIELECTRIC:
         pv["P"] = sub(pv["P"], mul(prim_dir, 0.03))
@@ -367,12 +373,14 @@ def render_pixel(S, fc, W, H, x, y):
     eye = mat4(mvi, (0.0, 0.0, 0.0, 1.0))[:3]
     diel0 = mat["material_model"] == abi.MAT_DIELECTRIC
     max_b = fc.max_number_of_bounces if diel0 else fc.number_of_bounces
-    samples = max(1, fc.number_of_samples)
+    samples = max(1, fc.number_of_samples) * (4 if moment > 0 else 1)   # Core.PathTracing.comp.slang:28
     for _ in range(samples):
         color = (1.0, 1.0, 1.0, 1.0)
         d = norm(sub(pv["P"], eye))
         done, v, d, color, hit_reflect, hit_metal = get_ray_color(pv, d, color)
-        if not done:
+        if not done and fc.fast_gather and not diel0:   # ExitAfterFirst: the probes end the path
+            color = had(color, probe_term(*S.probes, v["P"], v["N"]) if S.probes else (0.0,) * 4)
+        elif not done:
             for b in range(1, max_b):
                 stop, v, d, color, _, _ = get_ray_color(v, d, color)
                 if stop:
@@ -406,12 +414,18 @@ def render_pixel(S, fc, W, H, x, y):
     return tuple(final_c[:3]), tuple(final_r[:3])
 
 
-@pytest.mark.parametrize("sky_sun,materials,probes", [(False, False, False), (True, False, False),
-                                                      (True, True, False), (False, False, True)])
-def test_rt_pass_matches_the_python_restatement(sky_sun, materials, probes):
+@pytest.mark.parametrize("sky_sun,materials,probes,variant", [
+    (False, False, False, ""), (True, False, False, ""), (True, True, False, ""), (False, False, True, ""),
+    (False, False, True, "fast_gather"), (True, False, False, "moving")])
+def test_rt_pass_matches_the_python_restatement(sky_sun, materials, probes, variant):
     sc, cam, st = scenes.cornell()
     st.taa = False
     st.samples = 16           # most pixels then carry light from some path (zero probes end the rest)
+    st.fast_gather = variant == "fast_gather"
+    if variant == "moving":   # the tall box moved: its pixels' motion moments call for 4x the samples
+        cp = sc.instances["combined_prev"][2].reshape(3, 4).astype(np.float64)
+        cp[0, 3] += 0.1
+        sc.instances["combined_prev"][2] = cp.reshape(-1).astype(np.float32)
     if materials:             # the boxes as a rough metal and a glass: GGX VNDF, metal tint, refraction
         sc.materials[5]["metalness"] = 1.0
         sc.materials[5]["fuzziness"] = 0.2
