@@ -43,7 +43,7 @@ def face_rays(rng, sc, n, offset, scale):
     d = rng.normal(size=(n, 3))
     axis = rng.integers(0, 3, n)
     d[np.arange(n), axis] = 0.0
-    d[: n // 4, (axis[: n // 4] + 1) % 3] = 0.0
+    d[np.arange(n // 4), (axis[: n // 4] + 1) % 3] = 0.0     # a quarter run along an axis
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     # start behind the vertex along the ray, beyond the fixed tmin (EPS = 1e-3) of ray queries
     back = rng.uniform(2.0, 8.0, n)[:, None] * max(scale, 1e-3)
