@@ -108,6 +108,7 @@ class FrameBuilder:
         self.s = settings
         self.prev_vp = None
         self.prev_vp_unjit = None
+        self.prev_total_frames = 0      # TotalFrames of the previous UBO (zero before the first)
         self.total_frames = 0
 
     def build(self, cam: Camera, total_frames: int | None = None) -> abi.GkrtFrameConstants:
@@ -134,8 +135,11 @@ class FrameBuilder:
         fc.projection_inverse[:] = _cm(np.linalg.inv(proj))
         fc.view_projection[:] = _cm(vp)
         fc.view_projection_unjit[:] = _cm(vp_unjit)
-        prev = self.prev_vp if (self.prev_vp is not None and total_frames != 0) else vp
-        prevu = self.prev_vp_unjit if (self.prev_vp_unjit is not None and total_frames != 0) else vp_unjit
+        # last frame's matrices only when last frame's TotalFrames was not zero (Engine.cpp:786-787):
+        # the first frame, and the one after it, see no camera motion
+        keep = self.prev_vp is not None and self.prev_total_frames != 0
+        prev = self.prev_vp if keep else vp
+        prevu = self.prev_vp_unjit if keep else vp_unjit
         fc.prev_view_projection[:] = _cm(prev)
         fc.prev_view_projection_unjit[:] = _cm(prevu)
         sd = _normalize(s.sun_direction)
@@ -165,5 +169,6 @@ class FrameBuilder:
         fc.nee_mode = s.nee_mode
         fc.flags = s.flags
         self.prev_vp, self.prev_vp_unjit = vp, vp_unjit
+        self.prev_total_frames = total_frames
         self.total_frames = total_frames + 1
         return fc
