@@ -88,7 +88,10 @@ class Camera:
 
 
 class Settings:
-    """User settings that reach the UBO (UserSettings defaults: src/Runtime/Engine.cpp:111-163)."""
+    """User settings that reach the UBO (the UserSettings fields of src/Runtime/Engine.cpp:111-163).
+    The defaults here are a light test setting (1 sample, 4 bounces, no TAA); the scene
+    constructors set their configuration's values, and reference_defaults() gives the
+    reference's own."""
 
     def __init__(self, samples=1, bounces=4, max_bounces=10, temporal_frames=16, taa=False,
                  bf_size=5, bf_sigma=2.0, bf_sigma_lum=3.0, bf_sigma_normal=0.005, paper_white_nit=600.0,
@@ -97,6 +100,13 @@ class Settings:
                  hdr=False, denoiser=abi.DENOISE_JBF, nee_mode=abi.NEE_REFERENCE, flags=0):
         self.__dict__.update(locals())
         del self.__dict__["self"]
+
+    @classmethod
+    def reference_defaults(cls) -> "Settings":
+        """The reference's startup values: the command-line defaults (8 samples, 5 bounces, 10 at
+        most, 16 temporal frames; src/Options.cpp:11-14) and TAA on, the bilateral filter's
+        2.0 / 3.0 / 0.005 with size 5, 600-nit paper white (src/Runtime/Engine.cpp:111-163)."""
+        return cls(samples=8, bounces=5, max_bounces=10, temporal_frames=16, taa=True)
 
 
 class FrameBuilder:

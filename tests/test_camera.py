@@ -109,3 +109,10 @@ def test_settings_rules():
                                                    sun_direction=(1.0, 1.0, 0.0))).build(cam0(), 0)
     assert fc.has_sun == 1 and list(fc.sun_color) == [3.5, 3.5, 3.5, 0.0]
     np.testing.assert_allclose(list(fc.sun_direction), [math.sqrt(0.5), math.sqrt(0.5), 0.0, 0.0], atol=1e-7)
+
+
+def test_reference_defaults():
+    s = camera.Settings.reference_defaults()
+    assert (s.samples, s.bounces, s.max_bounces, s.temporal_frames, s.taa) == (8, 5, 10, 16, True)
+    assert (s.bf_size, s.bf_sigma, s.bf_sigma_lum, s.bf_sigma_normal, s.paper_white_nit) == (5, 2.0, 3.0, 0.005, 600.0)
+    assert not s.fast_gather
