@@ -10,9 +10,13 @@ reprojection and the joint bilateral filter. The scene is synthetic (seeded nump
             timed frames, inputs resident on the GPU, CUDA events on the launch stream.
 * e2e     : the same frames through the C ABI with host buffers: frame constants from
             host memory and the denoised image read back to pinned host memory each frame.
-* roofline: the trace kernel's algorithmic bytes per launch (node visits x 64 B + triangle
-            tests x 48 B + rays x 32 B in + per-hit fetches) over its event-timed duration,
+* roofline: the trace kernel against its binding resource, instruction issue: warp
+            instructions per ray (ncu) x the frame's rays over the event-timed duration,
+            against SMs x 4 issue slots x the sampled SM clock. Beside it (roofline.hbm) the
+            algorithmic bytes (node visits x 64 B + triangle tests x 48 B + rays x 32 B +
+            hit fetches x 236 B + outputs, all device-counted) and the DRAM traffic (ncu)
             against the measured HBM copy bandwidth.
+* city    : 3 timed 4K frames of the 10.5 M-triangle city with the per-frame instance rebuild.
 * cpu_baseline: the CPU oracle (C++ restatement of the reference's shading logic) on the
             host cores over a bounded sample of the same frames.
 
@@ -38,9 +42,44 @@ UNIT = "Mrays/s"
 W_, H_ = 1920, 1080
 HIT_FETCH_BYTES = 3 * 4 + 3 * 16 + 64 + 64 + 48   # indices, normals, material, instance, triangle
 NODE_BYTES, TRI_BYTES, RAY_BYTES = 64, 48, 32
-# DRAM bytes (read + write) of one 1080p trace launch of the default workload, from one ncu
-# capture; the node and triangle reads above are served by L1/L2
-TRACE_DRAM_BYTES_1080P = 9999872 + 133538304
+# ncu counters of one 1080p k_trace_pass launch of the default workload (one capture of
+# `python bench.py --steps 3 --warmup 3 --no-cpu-baseline --no-relmse --no-city`, fifth launch):
+# warp instructions issued (sm__inst_executed.sum), thread instructions
+# (smsp__thread_inst_executed.sum), DRAM bytes read + written, and the rays of that launch.
+# The node and triangle reads of the algorithmic bytes are served by L1/L2.
+TRACE_NCU_1080P = {"inst": None, "thread_inst": None, "dram_bytes": 9999872 + 133538304, "rays": None}
+ISSUE_PER_SM_PER_CLOCK = 4   # four schedulers per SM, one warp instruction each per cycle
+
+
+def trace_roofline(st, trace_ms, alg_bytes, alg_gbs, hbm_peak, peak_kind, num_sms, clocks):
+    """Roofline of the rt-pass kernel against the bound that holds: issue slots. The BVH is
+    cache-resident, so DRAM carries little more than the output images (dram_frac), and the
+    kernel is bound by instruction issue and SIMT efficiency (divergent traversal and shading).
+    achieved: warp instructions per ray (ncu, one 1080p launch) x the rays of the timed frame over
+    its event-timed duration; peak: SMs x 4 issue slots x the SM clock sampled during the run."""
+    n = TRACE_NCU_1080P
+    full = WORKLOAD == "bricks" and (W_, H_) == (1920, 1080)
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    issue_peak = num_sms * ISSUE_PER_SM_PER_CLOCK * sm_mhz * 1e6 / 1e9
+    out = {"bound": "issue", "unit": "G warp-instructions/s", "kernel": "k_trace_pass",
+           "peak": issue_peak, "peak_kind": f"{num_sms} SMs x {ISSUE_PER_SM_PER_CLOCK} issue slots x {sm_mhz:.0f} MHz",
+           "achieved": None, "frac": None,
+           "traffic": n["dram_bytes"] if full else None,
+           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 1080p k_trace_pass launch"}
+    if full and n["inst"] and n["rays"]:
+        achieved = n["inst"] / n["rays"] * st.rays_traced / (trace_ms * 1e-3) / 1e9
+        out.update({"achieved": achieved, "frac": achieved / issue_peak,
+                    "warp_instructions_per_ray": n["inst"] / n["rays"],
+                    "threads_per_instruction": n["thread_inst"] / n["inst"]})
+    dram_gbs = n["dram_bytes"] / (trace_ms * 1e-3) / 1e9 if full else None
+    out["hbm"] = {"peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
+                  "algorithmic_bytes_per_launch": alg_bytes, "algorithmic_gbs": alg_gbs,
+                  "algorithmic_frac": alg_gbs / hbm_peak,
+                  "dram_gbs": dram_gbs, "dram_frac": dram_gbs / hbm_peak if dram_gbs else None}
+    out.update({"rays": st.rays_traced, "hit_fetches": st.hit_fetches, "node_visits": st.node_visits,
+                "triangle_tests": st.triangle_tests, "exact_fallbacks": st.exact_fallbacks,
+                "exact_retraces": st.exact_retraces})
+    return out
 
 
 WORKLOAD = "bricks"
@@ -260,6 +299,9 @@ def cpu_baseline_measure(budget_s: float = 12.0):
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the C++ restatement of the reference's shading logic; the
+    reference's Slang has no CPU build here) on all host cores, one whole frame of the workload
+    per step (rt pass, reproject pass, compose pass: the work the GPU arm times)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
@@ -271,11 +313,11 @@ def run_reference(args):
     fb = camera.FrameBuilder(W_, H_, st)
     im = O.new_images(W_, H_)
     cores = os.cpu_count() or 1
-    band = 64   # rows per step: a bounded sample of each frame
+
     def step(i):
         fc = fb.build(cam.orbit(0.5 * i), i)
-        y0 = (i * band) % (H_ - band)
-        return osc.trace_pass(fc, W_, H_, im, y0=y0, y1=y0 + band, threads=cores)
+        return O.render_frame(osc, fc, W_, H_, im, threads=cores)
+
     for i in range(args.warmup):
         step(i)
     rays = 0
@@ -284,13 +326,13 @@ def run_reference(args):
         rays += step(args.warmup + i)
     dt = time.perf_counter() - t0
     v = rays / dt / 1e6
-    ms_frame = dt / args.steps * (H_ / band) * 1e3
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
-            "ms_per_frame_extrapolated": ms_frame, "higher_is_better": True, "scaling": "weak",
+            "ms_per_frame": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{band} rows of a 1080p frame per step (trace pass), {args.steps} steps"},
+                             "sample": f"{args.steps} whole {W_}x{H_} frames of the workload "
+                                       f"(trace+reproject+compose), {rays} rays in {dt:.1f} s"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -310,6 +352,59 @@ def relmse_measure(device: int):
         info["loss_last"] = float(sum(losses[-20:]) / 20)
         out["training"] = info
     return out
+
+
+def city_measure(device: int, frames: int = 3, warmup: int = 3):
+    """The 10.5 M-triangle city at 3840 x 2160 (alias-table NEE over 10,240 emissive
+    triangles, 5 k moving spheres): `frames` timed frames after `warmup`, each with the
+    per-frame instance update (GPU instance-level rebuild and emitter table) inside the frame,
+    then the rt, reproject and compose passes. Device-resident inputs, CUDA events."""
+    import torch
+    from gknextengine_gb300 import camera, scenes
+    from gknextengine_gb300.renderer import PathTracingRenderer
+    W, H = 3840, 2160
+    sc, cam, st, motion = scenes.city(width=W, height=H)
+    with PathTracingRenderer(device) as r:
+        t0 = time.perf_counter()
+        r.load_scene(sc)
+        load_s = time.perf_counter() - t0
+        r.create_swap_chain(W, H)
+        stream = torch.cuda.Stream()
+        fb = camera.FrameBuilder(W, H, st)
+        n = warmup + frames
+        fcs = [fb.build(cam.orbit(0.25 * i), i) for i in range(n)]
+        insts = [motion.instances(i) for i in range(n)]
+        for i in range(warmup):
+            r.update_instances(insts[i], stream)
+            r.render(fcs[i], stream)
+        r.synchronize(stream)
+        rays0 = r.stats().rays_total
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(frames)]
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for k in range(frames):
+                fc = fcs[warmup + k]
+                ev[k][0].record(stream)
+                r.update_instances(insts[warmup + k], stream)
+                ev[k][1].record(stream)
+                r.trace_pass(fc, stream)
+                ev[k][2].record(stream)
+                r.reproject_pass(fc, stream)
+                r.denoise_pass(fc, stream)
+                r.end_frame(stream)
+            end.record(stream)
+            torch.cuda.synchronize()
+        rays = r.stats().rays_total - rays0
+        ms = start.elapsed_time(end)
+    return {"workload": "city-10.48M-tris 3840x2160 1spp depth8 alias-table-NEE moving-spheres "
+                        "per-frame-instance-rebuild reproject+JBF",
+            "mrays_s": rays / (ms * 1e-3) / 1e6, "ms_per_frame": ms / frames, "frames": frames,
+            "rays_per_frame": rays / frames,
+            "trace_ms": sum(a.elapsed_time(b) for _, a, b in ev) / frames,
+            "update_span_ms": sum(a.elapsed_time(b) for a, b, _ in ev) / frames,
+            "scene_load_s": load_s, "triangles": int(sc.triangle_count)}
 
 
 def run_gkrt(args):
@@ -387,13 +482,13 @@ def run_gkrt(args):
     ms_total, rays = job_totals(ms_total, rays, world, "cuda")
     value = rays / (ms_total * 1e-3) / 1e6
 
-    # ---- algorithmic bytes of the trace kernel (counters of the last timed frame) ----
-    hits_est = st_last.rays_traced   # upper bound on hits: every ray fetches hit data at most once
+    # ---- algorithmic bytes of the trace kernel (device counters of the last timed frame) ----
     alg_bytes = (st_last.node_visits * NODE_BYTES + st_last.triangle_tests * TRI_BYTES +
-                 st_last.rays_traced * RAY_BYTES + hits_est * HIT_FETCH_BYTES + W_ * H_ * 7 * 16)
+                 st_last.rays_traced * RAY_BYTES + st_last.hit_fetches * HIT_FETCH_BYTES + W_ * H_ * 7 * 16)
     trace_avg_ms = sum(trace_ms) / len(trace_ms)
     achieved = alg_bytes / (trace_avg_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
 
     # ---- e2e through the C ABI with host buffers ----
     # Two frames in flight, as the reference keeps frames in flight behind fences
@@ -573,18 +668,11 @@ def run_gkrt(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "frames_in_flight": 2,
                         "h2d_bytes_per_step": ctypes.sizeof(abi.GkrtFrameConstants),
                         "d2h_bytes_per_step": W_ * H_ * 16, "ms_per_frame": e2e_s / K * 1e3},
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak,
-                             "traffic": TRACE_DRAM_BYTES_1080P if (WORKLOAD == "bricks" and (W_, H_) == (1920, 1080))
-                             else None,
-                             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 1080p "
-                                               "k_trace_pass launch (profiles/k_trace_pass_bricks1080p_dram.md)",
-                             "kernel": "k_trace_pass",
-                             "peak_kind": peak_kind,
-                             "algorithmic_bytes_per_launch": alg_bytes,
-                             "node_visits": st_last.node_visits, "triangle_tests": st_last.triangle_tests,
-                             "exact_fallbacks": st_last.exact_fallbacks, "exact_retraces": st_last.exact_retraces},
+                "roofline": trace_roofline(st_last, trace_avg_ms, alg_bytes, achieved, peak, peak_kind, num_sms,
+                                           clk.summary()),
                 "clocks": clk.summary()}
+        if world == 1 and WORKLOAD == "bricks" and not args.no_city:
+            line["city"] = city_measure(local)
         if world == 1 and WORKLOAD == "bricks" and not args.no_relmse:
             line["relmse"] = relmse_measure(local)
         if world == 1 and not args.no_cpu_baseline and WORKLOAD == "bricks":
@@ -605,6 +693,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-relmse", action="store_true")
+    ap.add_argument("--no-city", action="store_true", help="skip the 4K city frames of the default line")
     ap.add_argument("--size", default=None, help="WxH override for profiling small cases (default 1920x1080)")
     ap.add_argument("--workload", default="bricks", choices=["bricks", "city", "denoiser"],
                     help="bricks: the 1080p headline workload; city: 10.5M tris at 4K with per-frame rebuild")

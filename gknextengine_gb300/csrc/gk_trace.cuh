@@ -102,9 +102,12 @@ constexpr uint32_t kErrBounds = 16u;  // checked builds: an index outside its ar
     } while (0)
 #endif
 
-// Per-thread event counts, flushed once per warp at the end of a kernel.
+// Per-thread event counts, flushed once per warp at the end of a kernel. Context counter
+// slots: 0 rays, 1 FP64 fallbacks, 2 exact re-traces, 3 node visits, 4 triangle tests,
+// 5 hit fetches (closest hits whose vertex, normal, material and instance data were read),
+// all per pass; 6 rays since the context was created.
 struct Counters {
-    uint32_t rays, fallbacks, retraces, nodes, tris;
+    uint32_t rays, fallbacks, retraces, nodes, tris, hits;
 };
 
 struct SceneView {
@@ -317,6 +320,7 @@ struct Trav {
     f3 wo, wd;            // world ray
     f3 o, d, inv;         // ray in the current space (world or instance)
     Shear sh;
+    float tmin;           // read by the ray-query kernels (kRayTmin); the rt pass uses kTmin
     float tmax, tcull, best_lo, best_hi;
     double best_td;
     uint32_t inst, prim, tri;   // current best
@@ -329,11 +333,14 @@ struct Trav {
 
 constexpr float kTmin = 1e-3f;   // EPS, assets/shaders/common/PreProcessor.slang:13
 
+// tmin: the ray's lower bound, honoured by the functions instantiated with kRayTmin (the ray
+// queries); the rt pass and the bake kernels trace every ray from EPS and keep it a constant.
 template <bool kWide = false>
-GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int mode) {
+GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int mode, float tmin = kTmin) {
     T.wo = wo; T.wd = wd; T.o = wo; T.d = wd;
     T.inv = safe_inv(wd);
     T.sh = make_shear(wd);
+    T.tmin = tmin;
     T.tmax = tmax;
     T.tcull = tmax * 1.000001f;
     T.best_lo = 0.0f; T.best_hi = 0.0f; T.best_td = 0.0;
@@ -365,9 +372,11 @@ GK_D double exact_t_of(const Trav& T, const SceneView& S) {
 }
 
 // Test the triangles of one leaf against the current best. Returns true when the ray is
-// finished early (any-hit found).
+// finished early (any-hit found). kRayTmin: the ray's own tmin, else the constant EPS.
+template <bool kRayTmin = false>
 GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, Counters& cn) {
-    const double tmind = (double)kTmin, tmaxd = (double)T.tmax;
+    const float tmin = kRayTmin ? T.tmin : kTmin;
+    const double tmind = (double)tmin, tmaxd = (double)T.tmax;
     for (uint32_t k = 0; k < cnt; ++k) {
         const uint32_t ti = first + k;
         uint32_t prim;
@@ -401,8 +410,8 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
             t = (float)x.t;
             e = 2.384185791e-07f * fabsf(t);   // 4u |t|
         }
-        if (t + e < kTmin || t - e > T.tmax) continue;
-        if (t - e < kTmin || t + e > T.tmax) {
+        if (t + e < tmin || t - e > T.tmax) continue;
+        if (t - e < tmin || t + e > T.tmax) {
             if (!have_td) {
                 const ExactHit x = exact_test(T.o, T.d, T.sh, v0, v1, v2);
                 ++cn.fallbacks;
@@ -461,7 +470,9 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
 // a second leaf, or leaving the instance the postponed leaf belongs to, makes the lane wait
 // for the leaf phase. Returns true while the lane can take another node step.
 // cap: the stack's capacity in words (entries); the caller's stack holds at least cap * stride.
+template <bool kRayTmin = false>
 GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn, int cap = kStackSize) {
+    const float tmin = kRayTmin ? T.tmin : kTmin;
     if (++T.iter > kIterCap) { atomicOr(S.error, kErrIter); T.done = true; return false; }
     const int ref = T.ref;
     if (ref == kRefPop) {
@@ -484,8 +495,8 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
         const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
         float tn0, tn1;
-        const bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, T.o, T.inv, kTmin, T.tcull, tn0);
-        const bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, T.o, T.inv, kTmin, T.tcull, tn1);
+        const bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, T.o, T.inv, tmin, T.tcull, tn0);
+        const bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, T.o, T.inv, tmin, T.tcull, tn1);
         if (h0 && h1) {
             int nearr = nd.x, farr = nd.y;
             if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
@@ -611,7 +622,7 @@ GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int st
             const float tny = wide_t(i < 4 ? ny0 : ny1, b, Cy, By), tfy = wide_t(i < 4 ? fy0 : fy1, b, Cy, By);
             const float tnz = wide_t(i < 4 ? nz0 : nz1, b, Cz, Bz), tfz = wide_t(i < 4 ? fz0 : fz1, b, Cz, Bz);
             // slab interval widened by 1e-6 relative; T.tcull carries the same widening
-            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, kTmin));
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, T.tmin));
             const float tf = fminf(fminf(tfx, tfy), tfz) * 1.000001f;
             const bool hit = ((meta >> (24 + i)) & 1u) && tn <= fminf(tf, T.tcull);
             key[i] = hit ? ((__float_as_uint(tn) & ~7u) | (uint32_t)i) : 0xFFFFFFFFu;
@@ -682,31 +693,31 @@ GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int st
 }
 
 // Leaf phase: test the postponed leaf's triangles.
+template <bool kRayTmin = false>
 GK_D void trav_leaf_step(Trav& T, const SceneView& S, Counters& cn) {
     if (!T.has_leaf) return;
     GK_CHECK_OR_END((T.leaf >> 3) + (T.leaf & 7u) + 1u <= S.tri_count, S, T, );
     T.has_leaf = false;
-    if (trav_leaf(T, S, T.leaf >> 3, (T.leaf & 7u) + 1u, cn)) T.done = true;
+    if (trav_leaf<kRayTmin>(T, S, T.leaf >> 3, (T.leaf & 7u) + 1u, cn)) T.done = true;
 }
 
 GK_D bool trav_finished(const Trav& T) { return T.done && !T.has_leaf; }
 
-// Whole-ray traversal on top of the two phases.
+// Whole-ray traversal on top of the two phases: hits with tmin <= t <= tmax.
 template <int MODE, bool kWide = false>
 GK_D TraceOut traverse(const SceneView& S, f3 wo, f3 wd, float tmin, float tmax, uint32_t* stk, int stride,
                        Counters& cn) {
-    (void)tmin;
     Trav T;
-    trav_init<kWide>(T, S, wo, wd, tmax, MODE);
+    trav_init<kWide>(T, S, wo, wd, tmax, MODE, tmin);
     while (!trav_finished(T)) {
         if (kWide) {
             while (!T.done && trav_node_step_wide(T, S, stk, stride, cn)) {
             }
         } else {
-            while (!T.done && trav_node_step(T, S, stk, stride, cn)) {
+            while (!T.done && trav_node_step<true>(T, S, stk, stride, cn)) {
             }
         }
-        trav_leaf_step(T, S, cn);
+        trav_leaf_step<true>(T, S, cn);
     }
     TraceOut R;
     R.hit = T.hit; R.ambiguous = false; R.inst = T.inst; R.prim = T.prim; R.tri = T.tri;

@@ -116,7 +116,7 @@ struct GkrtContext {
     uint32_t tlas_refits = 0;
 
     Unet* unet = nullptr;                       // learned denoiser (gkrt_unet_init)
-    unsigned long long* d_counters = nullptr;   // see flush_counters: 5 per-pass slots + total rays
+    unsigned long long* d_counters = nullptr;   // see Counters (gk_trace.cuh): 6 per-pass slots + total rays
     uint32_t* d_error = nullptr;
     unsigned int* d_work = nullptr;             // pixel counter of the persistent trace kernel
     int num_sms = 1;
@@ -854,7 +854,8 @@ int gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out) {
         return GKRT_ERR_INVALID_ARG;
     }
     ctx->timers = desc && (desc->flags & GKRT_DEVICE_PASS_TIMERS);
-    cudaError_t e = cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
+    cudaError_t e = device_guard.status;
     for (int i = 0; i < kPassCount && ctx->timers && e == cudaSuccess; ++i)
         for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreate(&ctx->pass_ev[i][k]);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_counters, 8 * sizeof(unsigned long long));
@@ -879,7 +880,7 @@ int gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out) {
 
 int gkrt_context_destroy(GkrtContext* ctx) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaDeviceSynchronize();
     free_images(ctx);
     free_scene(ctx);
@@ -911,7 +912,7 @@ int gkrt_resize(GkrtContext* ctx, uint32_t width, uint32_t height) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (width == 0 || height == 0 || width > 16384 || height > 16384)
         return fail(ctx, GKRT_ERR_INVALID_ARG, "image size must be 1..16384");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     free_images(ctx);
     const uint32_t pitch = (width + 3u) & ~3u;
     const size_t px = (size_t)pitch * height;
@@ -962,7 +963,7 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
     }
     int rc = validate_instances(ctx, d->instances, d->instance_count, d->mesh_count, d->material_count);
     if (rc != GKRT_OK) return rc;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     free_scene(ctx);
     ctx->meshes.assign(d->meshes, d->meshes + d->mesh_count);
     ctx->inst.assign(d->instances, d->instances + d->instance_count);
@@ -999,7 +1000,7 @@ int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
         return fail(ctx, GKRT_ERR_INVALID_ARG, "instance update must keep the instance count");
     int rc = validate_instances(ctx, instances, count, (uint32_t)ctx->meshes.size(), ctx->nmat);
     if (rc != GKRT_OK) return rc;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const PassScope scope(ctx, kPassTlas, (cudaStream_t)stream);
     ctx->inst.assign(instances, instances + count);
     // host work first (emitter table, then the instance tables inside build_tlas), uploaded
@@ -1016,7 +1017,7 @@ int gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances, 
         return fail(ctx, GKRT_ERR_INVALID_ARG, "instance update must keep the instance count");
     int rc = validate_instances(ctx, instances, count, (uint32_t)ctx->meshes.size(), ctx->nmat);
     if (rc != GKRT_OK) return rc;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const PassScope scope(ctx, kPassTlas, (cudaStream_t)stream);
     ctx->inst.assign(instances, instances + count);
     if ((rc = build_emitters(ctx, (cudaStream_t)stream)) != GKRT_OK) return rc;
@@ -1030,7 +1031,7 @@ int gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances, 
 int gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (flags & ~(GKRT_BUILD_ALL | GKRT_BUILD_ON_HOST)) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown build flags");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const bool host = (flags & GKRT_BUILD_ON_HOST) != 0;
     if (host != ctx->host_build) {
         ctx->host_build = host;
@@ -1044,7 +1045,7 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     if (rc != GKRT_OK) return rc;
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
     if (fc->nee_mode > GKRT_NEE_EMISSIVE) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown nee_mode");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
     const PassScope scope(ctx, kPassRt, st);
@@ -1060,7 +1061,7 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     im.motion_moment = (uint32_t*)ctx->img[GKRT_IMG_MOTION_MOMENT];
     im.hit_inst = (uint32_t*)ctx->img[GKRT_IMG_HIT_INST];
     im.hit_prim = (uint32_t*)ctx->img[GKRT_IMG_HIT_PRIM];
-    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 6 * sizeof(unsigned long long), st));
     // the stack bound check_stack_bound enforced at build time, at least 8 entries
     const int stack_words = std::max(8, std::min(kStackSize, ctx->blas_bin_depth + ctx->tlas_bin_depth + 3));
     GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, (int)ctx->P, im, ctx->d_counters, ctx->d_work,
@@ -1071,7 +1072,7 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
 int gkrt_reproject_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
     int rc = check_frame(ctx, fc);
     if (rc != GKRT_OK) return rc;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const PassScope scope(ctx, kPassReproject, (cudaStream_t)stream);
     ReprojectArgs a;
     a.W = (int)ctx->W; a.H = (int)ctx->H; a.P = (int)ctx->P;
@@ -1100,7 +1101,7 @@ int gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stre
     int rc = check_frame(ctx, fc);
     if (rc != GKRT_OK) return rc;
     if (fc->denoiser > GKRT_DENOISE_UNET) return fail(ctx, GKRT_ERR_UNSUPPORTED, "unknown denoiser");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const PassScope scope(ctx, kPassCompose, (cudaStream_t)stream);
     if (fc->denoiser == GKRT_DENOISE_UNET) {
         if (!ctx->unet) return fail(ctx, GKRT_ERR_STATE, "gkrt_unet_init was not called");
@@ -1161,7 +1162,7 @@ int gkrt_denoise_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stre
 int gkrt_end_frame(GkrtContext* ctx, void* stream) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (ctx->W == 0) return fail(ctx, GKRT_ERR_STATE, "gkrt_resize was not called");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const PassScope scope(ctx, kPassCopy, (cudaStream_t)stream);   // a buffer swap: no GPU work
     const int pairs[4][2] = {{GKRT_IMG_ACCUM_DIFFUSE, GKRT_IMG_PREV_DIFFUSE},
                              {GKRT_IMG_ACCUM_SPECULAR, GKRT_IMG_PREV_SPECULAR},
@@ -1172,6 +1173,8 @@ int gkrt_end_frame(GkrtContext* ctx, void* stream) {
 }
 
 int gkrt_render_frame(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc;
     if ((rc = gkrt_trace_pass(ctx, fc, stream)) != GKRT_OK) return rc;
     if ((rc = gkrt_reproject_pass(ctx, fc, stream)) != GKRT_OK) return rc;
@@ -1182,7 +1185,7 @@ int gkrt_render_frame(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stre
 int gkrt_get_pass_times(GkrtContext* ctx, GkrtPassTimes* out) {
     if (!ctx || !out) return GKRT_ERR_INVALID_ARG;
     if (!ctx->timers) return fail(ctx, GKRT_ERR_STATE, "the context was created without GKRT_DEVICE_PASS_TIMERS");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     float ms[kPassCount];
     for (int i = 0; i < kPassCount; ++i) {
         ms[i] = -1.0f;
@@ -1213,7 +1216,7 @@ int gkrt_get_image(GkrtContext* ctx, int id, GkrtImageView* out) {
 
 int gkrt_synchronize(GkrtContext* ctx, void* stream) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     auto t0 = std::chrono::steady_clock::now();
     for (;;) {
@@ -1242,7 +1245,7 @@ int gkrt_copy_image_to_host(GkrtContext* ctx, int id, void* dst, size_t dst_byte
     if (rc != GKRT_OK) return rc;
     const size_t row = (size_t)v.width * image_bytes_per_px(id);
     if (!dst || dst_bytes < row * v.height) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     // the host copy is dense (width x height); the device rows are padded
     GK_CUDA(cudaMemcpy2DAsync(dst, row, v.device_ptr, v.pitch_bytes, row, v.height, cudaMemcpyDeviceToHost,
                               (cudaStream_t)stream));
@@ -1255,7 +1258,7 @@ int gkrt_copy_image_to_host_async(GkrtContext* ctx, int id, void* dst, size_t ds
     if (rc != GKRT_OK) return rc;
     const size_t row = (size_t)v.width * image_bytes_per_px(id);
     if (!dst || dst_bytes < row * v.height) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     GK_CUDA(cudaMemcpy2DAsync(dst, row, v.device_ptr, v.pitch_bytes, row, v.height, cudaMemcpyDeviceToHost,
                               (cudaStream_t)stream));
     return GKRT_OK;
@@ -1265,7 +1268,7 @@ int gkrt_output_resize(GkrtContext* ctx, uint32_t width, uint32_t height) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if ((width == 0) != (height == 0) || width > 16384 || height > 16384)
         return fail(ctx, GKRT_ERR_INVALID_ARG, "output size must be 1..16384 (or 0 x 0 to free)");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     GK_CUDA(cudaDeviceSynchronize());
     dfree(ctx->d_output);
     ctx->OW = ctx->OH = 0;
@@ -1290,7 +1293,7 @@ int gkrt_output_pass(GkrtContext* ctx, const GkrtOutputDesc* d, void* stream) {
         return fail(ctx, GKRT_ERR_INVALID_ARG, "output rectangle must be 1..65536 a side");
     if (std::abs((long long)d->offset_x) > 65536 || std::abs((long long)d->offset_y) > 65536)
         return fail(ctx, GKRT_ERR_INVALID_ARG, "output offset beyond +-65536");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const float4* src = static_cast<const float4*>(ctx->img[d->source_image]);
     const cudaStream_t st = (cudaStream_t)stream;
     if (d->mode == GKRT_OUTPUT_RESOLVE)
@@ -1318,7 +1321,7 @@ int gkrt_copy_output_to_host(GkrtContext* ctx, void* dst, size_t dst_bytes, void
     if (!ctx->d_output) return fail(ctx, GKRT_ERR_STATE, "gkrt_output_resize was not called");
     const size_t bytes = (size_t)ctx->OW * ctx->OH * 4;
     if (!dst || dst_bytes < bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the image");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     GK_CUDA(cudaMemcpyAsync(dst, ctx->d_output, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     return gkrt_synchronize(ctx, stream);
 }
@@ -1331,7 +1334,7 @@ int gkrt_screenshot(GkrtContext* ctx, uint32_t x, uint32_t y, uint32_t width, ui
         return fail(ctx, GKRT_ERR_INVALID_ARG, "screenshot crop must lie inside the presentation image");
     const size_t bytes = (size_t)width * height * 3;
     if (!dst || dst_bytes < bytes) return fail(ctx, GKRT_ERR_INVALID_ARG, "destination smaller than the crop");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     const cudaStream_t st = (cudaStream_t)stream;
     uint8_t* d_rgb = nullptr;
     GK_CUDA(cudaMallocAsync((void**)&d_rgb, bytes, st));
@@ -1350,7 +1353,7 @@ int gkrt_upload_image(GkrtContext* ctx, int id, const void* src, size_t src_byte
     if (rc != GKRT_OK) return rc;
     const size_t row = (size_t)v.width * image_bytes_per_px(id);
     if (!src || src_bytes != row * v.height) return fail(ctx, GKRT_ERR_INVALID_ARG, "source size differs from the image");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     GK_CUDA(cudaMemcpy2DAsync(v.device_ptr, v.pitch_bytes, src, row, row, v.height, cudaMemcpyHostToDevice,
                               (cudaStream_t)stream));
     return gkrt_synchronize(ctx, stream);
@@ -1360,11 +1363,11 @@ int gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (count && (!rays || !hits)) return fail(ctx, GKRT_ERR_INVALID_ARG, "null ray or hit buffer");
     if (mode > GKRT_TRACE_ANY) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown trace mode");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = ensure_bvh(ctx, 0, st);
     if (rc != GKRT_OK) return rc;
-    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 6 * sizeof(unsigned long long), st));
     GK_CUDA(gkrt_launch_trace_rays(scene_view(ctx), rays, hits, count, mode, ctx->d_counters, st));
     return GKRT_OK;
 }
@@ -1378,14 +1381,14 @@ constexpr size_t kProbeCount = (size_t)kProbeXY * kProbeXY * kProbeZ;
 int gkrt_probe_voxelize(GkrtContext* ctx, void* stream) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = ensure_bvh(ctx, 0, st);
     if (rc != GKRT_OK) return rc;
     if (!ctx->d_cubes) GK_CUDA(cudaMalloc((void**)&ctx->d_cubes, kProbeCount * 14 * sizeof(uint32_t)));
     if (!ctx->d_voxels) GK_CUDA(cudaMalloc((void**)&ctx->d_voxels, kProbeCount * 4 * sizeof(uint32_t)));
     GK_CUDA(cudaMemsetAsync(ctx->d_cubes, 0, kProbeCount * 14 * sizeof(uint32_t), st));
-    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 6 * sizeof(unsigned long long), st));
     GK_CUDA(gkrt_launch_probe_voxelize(shade_scene(ctx), 0, (uint32_t)kProbeCount, (uint4*)ctx->d_voxels,
                                        ctx->d_counters, st));
     return GKRT_OK;
@@ -1397,7 +1400,7 @@ int gkrt_probe_bake(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t fir
     if (!ctx->d_cubes || !ctx->d_voxels)
         return fail(ctx, GKRT_ERR_STATE, "no probe grid: upload one or call gkrt_probe_voxelize");
     if ((size_t)first + count > kProbeCount) return fail(ctx, GKRT_ERR_INVALID_ARG, "probe range outside the grid");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = ensure_bvh(ctx, 0, st);
     if (rc != GKRT_OK) return rc;
@@ -1418,7 +1421,7 @@ int gkrt_probe_bake(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t fir
         lt.area = L.normal_area[3];
         lt.valid = 1;
     }
-    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 6 * sizeof(unsigned long long), st));
     GK_CUDA(gkrt_launch_probe_bake(shade_scene(ctx), *fc, lt, first, count, ctx->d_cubes_prev, ctx->d_cubes,
                                    (uint4*)ctx->d_voxels, ctx->d_counters, st));
     return GKRT_OK;
@@ -1427,7 +1430,7 @@ int gkrt_probe_bake(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t fir
 int gkrt_probe_download(GkrtContext* ctx, uint32_t* cubes, uint32_t* voxels) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (!ctx->d_cubes || !ctx->d_voxels) return fail(ctx, GKRT_ERR_STATE, "no probe grid");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     GK_CUDA(cudaDeviceSynchronize());
     if (cubes) GK_CUDA(cudaMemcpy(cubes, ctx->d_cubes, kProbeCount * 14 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     if (voxels) GK_CUDA(cudaMemcpy(voxels, ctx->d_voxels, kProbeCount * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -1436,9 +1439,9 @@ int gkrt_probe_download(GkrtContext* ctx, uint32_t* cubes, uint32_t* voxels) {
 
 int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     if (!ctx || !out) return GKRT_ERR_INVALID_ARG;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     std::memset(out, 0, sizeof(*out));
-    unsigned long long c[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0};
     GK_CUDA(cudaDeviceSynchronize());
     GK_CUDA(cudaMemcpy(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost));
     uint32_t errw = 0;
@@ -1448,7 +1451,8 @@ int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     out->exact_retraces = c[2];
     out->node_visits = c[3];
     out->triangle_tests = c[4];
-    out->rays_total = c[5];
+    out->rays_total = c[6];
+    out->hit_fetches = c[5] > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)c[5];
     out->device_error = errw;
     out->bvh_nodes = ctx->blas_nodes_used;
     out->tlas_nodes = ctx->tlas_nodes;
@@ -1458,7 +1462,6 @@ int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     out->wide_nodes = ctx->blas_wide_count + ctx->tlas_wide_count;
     out->wide_depth = (uint32_t)(ctx->blas_wide_depth + ctx->tlas_wide_depth);
     out->tlas_refits = ctx->tlas_refits;
-    out->reserved = 0;
     return GKRT_OK;
 }
 
@@ -1467,7 +1470,7 @@ int gkrt_set_material_params(GkrtContext* ctx, const float* albedo_rgb, const fl
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
     if ((uint64_t)first + count > ctx->nmat) return fail(ctx, GKRT_ERR_INVALID_ARG, "material range outside the scene");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     GK_CUDA(gkrt_launch_set_params(ctx->d_mat, albedo_rgb, roughness, first, count, (cudaStream_t)stream));
     return GKRT_OK;
 }
@@ -1500,10 +1503,10 @@ int gkrt_adjoint_forward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_
     int rc = adjoint_checks(ctx, fc, spp);
     if (rc != GKRT_OK) return rc;
     if (!image) return fail(ctx, GKRT_ERR_INVALID_ARG, "null image");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
-    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 6 * sizeof(unsigned long long), st));
     GK_CUDA(gkrt_launch_adjoint(shade_scene(ctx), *fc, (int)ctx->W, (int)ctx->H, spp, sample_roughness,
                                 (float4*)image, nullptr, nullptr, nullptr, ctx->d_counters, st));
     return GKRT_OK;
@@ -1514,10 +1517,10 @@ int gkrt_adjoint_backward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32
     int rc = adjoint_checks(ctx, fc, spp);
     if (rc != GKRT_OK) return rc;
     if (!d_image || !grad_albedo || !grad_roughness) return fail(ctx, GKRT_ERR_INVALID_ARG, "null buffer");
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
-    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 5 * sizeof(unsigned long long), st));
+    GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 6 * sizeof(unsigned long long), st));
     GK_CUDA(gkrt_launch_adjoint(shade_scene(ctx), *fc, (int)ctx->W, (int)ctx->H, spp, sample_roughness, nullptr,
                                 (const float4*)d_image, grad_albedo, grad_roughness, ctx->d_counters, st));
     return GKRT_OK;
@@ -1547,10 +1550,9 @@ int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t w
 }
 
 // ---- learned denoiser ----
+// The caller holds a DeviceGuard for ctx->device.
 static int unet_ready(GkrtContext* ctx) {
-    if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (!ctx->unet) return fail(ctx, GKRT_ERR_STATE, "gkrt_unet_init was not called");
-    cudaSetDevice(ctx->device);
     return GKRT_OK;
 }
 static int unet_size_ok(GkrtContext* ctx, uint32_t b, uint32_t h, uint32_t w) {
@@ -1561,7 +1563,7 @@ static int unet_size_ok(GkrtContext* ctx, uint32_t b, uint32_t h, uint32_t w) {
 
 int gkrt_unet_init(GkrtContext* ctx, uint64_t seed) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     if (!ctx->unet && !(ctx->unet = gkrt_unet_new())) return fail(ctx, GKRT_ERR_OOM, "denoiser");
     GK_CUDA(gkrt_unet_init_params(ctx->unet, seed));
     return GKRT_OK;
@@ -1569,12 +1571,15 @@ int gkrt_unet_init(GkrtContext* ctx, uint64_t seed) {
 
 int gkrt_unet_param_count(GkrtContext* ctx, uint32_t* count) {
     if (!ctx || !count) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     if (!ctx->unet && !(ctx->unet = gkrt_unet_new())) return fail(ctx, GKRT_ERR_OOM, "denoiser");
     *count = (uint32_t)gkrt_unet_nparams(ctx->unet);
     return GKRT_OK;
 }
 
 int gkrt_unet_get_params(GkrtContext* ctx, float* params, float* grads) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     GK_CUDA(gkrt_unet_get_params_host(ctx->unet, params, grads));
@@ -1582,6 +1587,8 @@ int gkrt_unet_get_params(GkrtContext* ctx, float* params, float* grads) {
 }
 
 int gkrt_unet_get_state(GkrtContext* ctx, float* m, float* v, uint64_t* step) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     GK_CUDA(gkrt_unet_get_state_host(ctx->unet, m, v, step));
@@ -1589,6 +1596,8 @@ int gkrt_unet_get_state(GkrtContext* ctx, float* m, float* v, uint64_t* step) {
 }
 
 int gkrt_unet_set_state(GkrtContext* ctx, const float* m, const float* v, uint64_t step) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     if (!m || !v || step > 0x7FFFFFFFull) return fail(ctx, GKRT_ERR_INVALID_ARG, "null moments or step out of range");
@@ -1598,7 +1607,7 @@ int gkrt_unet_set_state(GkrtContext* ctx, const float* m, const float* v, uint64
 
 int gkrt_unet_set_params(GkrtContext* ctx, const float* params) {
     if (!ctx || !params) return GKRT_ERR_INVALID_ARG;
-    cudaSetDevice(ctx->device);
+    DeviceGuard device_guard(ctx->device);
     if (!ctx->unet && !(ctx->unet = gkrt_unet_new())) return fail(ctx, GKRT_ERR_OOM, "denoiser");
     GK_CUDA(gkrt_unet_set_params_host(ctx->unet, params));
     return GKRT_OK;
@@ -1606,6 +1615,8 @@ int gkrt_unet_set_params(GkrtContext* ctx, const float* params) {
 
 int gkrt_unet_forward(GkrtContext* ctx, const float* input, uint32_t batch, uint32_t height, uint32_t width,
                       float* out_linear, float* out_raw, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     if ((rc = unet_size_ok(ctx, batch, height, width)) != GKRT_OK) return rc;
@@ -1616,6 +1627,8 @@ int gkrt_unet_forward(GkrtContext* ctx, const float* input, uint32_t batch, uint
 }
 
 int gkrt_unet_backward(GkrtContext* ctx, const float* d_raw, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     if (!d_raw) return fail(ctx, GKRT_ERR_INVALID_ARG, "null gradient");
@@ -1624,6 +1637,8 @@ int gkrt_unet_backward(GkrtContext* ctx, const float* d_raw, void* stream) {
 }
 
 int gkrt_unet_zero_grad(GkrtContext* ctx, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     GK_CUDA(gkrt_unet_zero_grad(ctx->unet, (cudaStream_t)stream));
@@ -1632,6 +1647,8 @@ int gkrt_unet_zero_grad(GkrtContext* ctx, void* stream) {
 
 int gkrt_unet_train_step(GkrtContext* ctx, const float* input, const float* target, uint32_t batch, uint32_t height,
                          uint32_t width, float lr, double* loss, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    DeviceGuard device_guard(ctx->device);
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     if ((rc = unet_size_ok(ctx, batch, height, width)) != GKRT_OK) return rc;

@@ -24,6 +24,27 @@ inline int current_device_slot() {
     return d;
 }
 
+// Makes `device` current for the life of the object and gives the caller's current device
+// back at the end, so that an entry point leaves the calling thread's device as it found it.
+// status: the cudaSetDevice result (entry points that report it check it).
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t status = cudaSuccess;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            prev = -1;
+        }
+        if (prev != device) status = cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 struct ReprojectArgs {
     int W, H, P;                   // P: row pitch in pixels (a multiple of 4)
     uint32_t progressive, temporal_frames;

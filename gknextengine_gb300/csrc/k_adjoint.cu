@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(ShadeScene sc, GkrtFram
         __syncthreads();
     }
     Counters cn;
-    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0;
+    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0; cn.hits = 0;
     const AdjCtx a{sc, fc, sample_rough, stack + tid, cn};
     const int pix = blockIdx.x * kAdjThreads + tid;
     if (pix < W * H) {

@@ -25,20 +25,20 @@ constexpr int kPtMinBlocks = 5;
 constexpr int kRefillBelow = 1;    // shade and refill once every lane of the warp has finished its ray
 constexpr float kCosCone = 0.999990482f;   // cos(0.25 deg), Shading.slang:897
 
-// Warp-aggregated flush: one atomic per counter per warp. Slots 0-4 are per pass
-// (rays, FP64 fallbacks, exact re-traces, node visits, triangle tests); slot 5 counts rays
-// since the context was created.
+// Warp-aggregated flush: one atomic per counter per warp. Slots 0-5 are per pass
+// (rays, FP64 fallbacks, exact re-traces, node visits, triangle tests, hit fetches); slot 6
+// counts rays since the context was created.
 __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long long* out) {
-    unsigned long long v[5] = {c.rays, c.fallbacks, c.retraces, c.nodes, c.tris};
+    unsigned long long v[6] = {c.rays, c.fallbacks, c.retraces, c.nodes, c.tris, c.hits};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-        for (int k = 0; k < 5; ++k) v[k] += __shfl_down_sync(0xFFFFFFFFu, v[k], o);
+        for (int k = 0; k < 6; ++k) v[k] += __shfl_down_sync(0xFFFFFFFFu, v[k], o);
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-        for (int k = 0; k < 5; ++k)
+        for (int k = 0; k < 6; ++k)
             if (v[k]) atomicAdd(&out[k], v[k]);
-        if (v[0]) atomicAdd(&out[5], v[0]);
+        if (v[0]) atomicAdd(&out[6], v[0]);
     }
 }
 
@@ -120,6 +120,7 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
             if (want_ids) { c.im.hit_inst[pix] = 0xFFFFFFFFu; c.im.hit_prim[pix] = 0xFFFFFFFFu; }
             L.pix = -1;
         } else {
+            ++c.cn.hits;
             Vtx pv = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
             if (want_ids) { c.im.hit_inst[pix] = T.inst; c.im.hit_prim[pix] = T.prim; }
             const f4 P4 = F4(pv.P.x, pv.P.y, pv.P.z, 1.0f);
@@ -169,6 +170,7 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
     if (stage == ST_FIRST || stage == ST_BOUNCE) {
         bool term;
         if (T.hit) {
+            ++c.cn.hits;
             L.vs = hit_vertex(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
             const MatV hm = load_mat(c.sc, L.vs.mat);
             if (kNee && L.neeLobe && hm.model == GKRT_MAT_DIFFUSE_LIGHT) {
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeSc
     const int tid = threadIdx.x;
     const unsigned lane = tid & 31u;
     Counters cn;
-    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0;
+    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0; cn.hits = 0;
     const Ctx c{sc, fc, im, W, H, P, pslots + tid, kPtThreads, cn};
     const int tiles_x = (W + 7) / 8, tiles_y = (H + 3) / 4;
     const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(kRqThreads) k_trace_rays(SceneView S, const Gk
     __shared__ uint32_t stack[kStackSize * kRqThreads];
     const uint32_t i = blockIdx.x * kRqThreads + threadIdx.x;
     Counters cn;
-    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0;
+    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0; cn.hits = 0;
     if (i < n) {
         GkrtRay r = rays[i];
         f3 o = F3(r.origin[0], r.origin[1], r.origin[2]), d = F3(r.dir[0], r.dir[1], r.dir[2]);
@@ -455,11 +457,12 @@ __global__ void __launch_bounds__(kRqThreads) k_trace_rays(SceneView S, const Gk
         h.t = -1.0f; h.b1 = 0.0f; h.b2 = 0.0f; h.inst = 0xFFFFFFFFu; h.prim = 0xFFFFFFFFu;
         h.pad[0] = h.pad[1] = h.pad[2] = 0u;
         cn.rays = 1;
-        // tmin of the query is fixed at EPS like the reference's TraceRay/TraceOcclusion
+        // hits with r.tmin <= t <= r.tmax (the reference's shaders pass EPS as TMin)
         const TraceOut t = mode == GKRT_TRACE_ANY
                                ? traverse<kAny, true>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn)
                                : traverse<kClosest, true>(S, o, d, r.tmin, r.tmax, stack + threadIdx.x, kRqThreads, cn);
         if (t.hit) {
+            ++cn.hits;
             const HitShade s = hit_shade(S, o, d, t.inst, t.tri);
             h.t = s.t; h.inst = t.inst; h.prim = t.prim;
             if (mode != GKRT_TRACE_ANY) { h.b1 = s.b1; h.b2 = s.b2; }

@@ -36,18 +36,18 @@ __constant__ float c_grid4x4[32] = {-0.75f, -0.75f, -0.25f, -0.75f, 0.25f, -0.75
 __constant__ float c_grid3x3[18] = {-0.667f, -0.667f, 0.0f, -0.667f, 0.667f, -0.667f, -0.667f, 0.0f, 0.0f,
                                     0.0f,    0.667f,  0.0f, -0.667f, 0.667f, 0.0f,    0.667f, 0.667f, 0.667f};
 
-// Warp-aggregated flush of the ray counters (per-pass slots 0-4, total rays in slot 5).
+// Warp-aggregated flush of the ray counters (per-pass slots 0-5, total rays in slot 6).
 __device__ __forceinline__ void flush_ray_counters(const Counters& c, unsigned long long* out) {
-    unsigned long long v[5] = {c.rays, c.fallbacks, c.retraces, c.nodes, c.tris};
+    unsigned long long v[6] = {c.rays, c.fallbacks, c.retraces, c.nodes, c.tris, c.hits};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-        for (int k = 0; k < 5; ++k) v[k] += __shfl_down_sync(0xFFFFFFFFu, v[k], o);
+        for (int k = 0; k < 6; ++k) v[k] += __shfl_down_sync(0xFFFFFFFFu, v[k], o);
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-        for (int k = 0; k < 5; ++k)
+        for (int k = 0; k < 6; ++k)
             if (v[k]) atomicAdd(&out[k], v[k]);
-        if (v[0]) atomicAdd(&out[5], v[0]);
+        if (v[0]) atomicAdd(&out[6], v[0]);
     }
 }
 
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kVoxThreads) k_probe_voxelize(ShadeScene sc, u
                                                                 uint4* voxels, unsigned long long* counters) {
     __shared__ uint32_t stack[kStackSize * kVoxThreads];
     Counters cn;
-    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0;
+    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0; cn.hits = 0;
     const uint32_t k = blockIdx.x * kVoxThreads + threadIdx.x;
     if (k < count) {
         const uint32_t g = first + k;
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kBakeThreads) k_probe_bake(ShadeScene sc, Gkrt
                                                              uint4* voxels, unsigned long long* counters) {
     __shared__ uint32_t stack[kStackSize * kBakeThreads];
     Counters cn;
-    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0;
+    cn.rays = 0; cn.fallbacks = 0; cn.retraces = 0; cn.nodes = 0; cn.tris = 0; cn.hits = 0;
     const uint32_t lane = threadIdx.x & 31u, sub = lane & 7u;
     const uint32_t k = (blockIdx.x * kBakeThreads + threadIdx.x) >> 3;
     const uint32_t g = first + k;

@@ -264,7 +264,8 @@ typedef struct GkrtStats {
     uint32_t wide_nodes;        /* compressed 8-wide nodes traversed (mesh + instance)    */
     uint32_t wide_depth;        /* wide levels, deepest mesh tree + instance tree         */
     uint32_t tlas_refits;       /* instance-level refits since creation                   */
-    uint32_t reserved;
+    uint32_t hit_fetches;       /* closest hits whose vertex, normal, material and instance
+                                   data were read (hit reconstruction), last pass          */
 } GkrtStats;
 
 typedef struct GkrtContext GkrtContext;
@@ -364,14 +365,15 @@ int  gkrt_copy_image_to_host_async(GkrtContext* ctx, int image_id, void* dst, si
 int  gkrt_upload_image(GkrtContext* ctx, int image_id, const void* src, size_t src_bytes, void* stream);
 
 /* Ray queries on the scene's BVH (FHardwareRayTracerV2::TraceRay / TraceOcclusion,
- * assets/shaders/common/Shading.slang:737-826). rays/hits are device pointers. */
+ * assets/shaders/common/Shading.slang:737-826). rays/hits are device pointers. A ray reports
+ * hits with tmin <= t <= tmax (the reference's shaders pass TMin = EPS = 1e-3). Every entry
+ * point of this header leaves the calling thread's current CUDA device as it found it. */
 int  gkrt_trace_rays(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hits, uint32_t count,
                      uint32_t mode, void* stream);
 
 /* The same ray queries for callers that cannot allocate device memory while they issue work
- * (a host engine whose device memory belongs to its own pool allocator, a process at its
- * memory budget, or code running inside CUDA stream capture, where allocation is not
- * allowed). No counterpart in the reference. The call allocates nothing: it needs a context
+ * (a host engine whose device memory belongs to its own pool allocator, or a process at its
+ * memory budget). No counterpart in the reference. The call allocates nothing: it needs a context
  * whose scene and BVH are already built (else GKRT_ERR_STATE), and its scratch memory is a
  * fixed 2 MiB static device array that every GPU loading the library keeps until process
  * exit. At most 4,194,304 rays per call (GKRT_ERR_INVALID_ARG above that). The first call on

@@ -228,7 +228,11 @@ def sincos_2pi(u: float):
 # ---- the reference's own CPU BVH (tinybvh, vendored in gkNextEngine), test use only ----
 REF_DIR = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_DIR, "libtinybvh_ref.so")
-REFERENCE_TINYBVH = "/root/reference/src/ThirdParty/tinybvh"
+# The reference tree, read where it lies (present where this library is developed, absent on
+# GPU hosts); the environment variable GKNE_REFERENCE_TREE points elsewhere. Pins that need
+# it are skipped when it is absent.
+REFERENCE_TREE = os.environ.get("GKNE_REFERENCE_TREE", "/root/reference")
+REFERENCE_TINYBVH = os.path.join(REFERENCE_TREE, "src", "ThirdParty", "tinybvh")
 
 
 def build_ref(force: bool = False):

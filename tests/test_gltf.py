@@ -11,7 +11,9 @@ import pytest
 
 from gknextengine_gb300 import abi, gltf
 
-REF_MODELS = "/root/reference/assets/models"
+from oracle.oracle import REFERENCE_TREE
+
+REF_MODELS = os.path.join(REFERENCE_TREE, "assets", "models")
 
 
 def write_glb(doc: dict, binchunk: bytes) -> bytes:

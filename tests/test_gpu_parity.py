@@ -122,14 +122,20 @@ def _moving_cornell():
     return sc, cam, st
 
 
-@pytest.mark.parametrize("W,H,denoiser", [(160, 120, abi.DENOISE_JBF), (150, 90, abi.DENOISE_ATROUS),
-                                           (97, 61, abi.DENOISE_JBF), (61, 47, abi.DENOISE_ATROUS)])
-def test_frames_reproject_and_compose(W, H, denoiser):
+@pytest.mark.parametrize("W,H,denoiser,progressive", [(160, 120, abi.DENOISE_JBF, False),
+                                                       (150, 90, abi.DENOISE_ATROUS, False),
+                                                       (97, 61, abi.DENOISE_JBF, False),
+                                                       (61, 47, abi.DENOISE_ATROUS, False),
+                                                       (97, 61, abi.DENOISE_JBF, True)])
+def test_frames_reproject_and_compose(W, H, denoiser, progressive):
     """Three frames with a moving box and an orbiting camera: every image after each
     pass matches the oracle (history, motion moment, accumulation, denoised). Odd sizes
-    exercise the padded rows and the zero fill of tile loads outside the image."""
+    exercise the padded rows and the zero fill of tile loads outside the image. The
+    progressive case runs the ProgressiveRender branch of the reprojection
+    (Process.ReProject.comp.slang:95-101; TemporalFrames 256, Engine.cpp:826)."""
     sc, cam, st = _moving_cornell()
     st.denoiser = denoiser
+    st.progressive = progressive
     st.taa = True
     st.flags = abi.FRAME_PRIMARY_IDS
     r = PathTracingRenderer(0)
@@ -177,6 +183,35 @@ def test_trace_rays_bricks_exact(bricks_env):
     g = gpu_trace_rays(r, rays)
     o = osc.trace_rays(rays)
     assert_hits_equal(g, o)
+
+
+@pytest.mark.parametrize("mode", [abi.TRACE_CLOSEST, abi.TRACE_ANY])
+def test_trace_rays_honour_tmin(bricks_env, mode):
+    """Per-ray tmin: hits with tmin <= t <= tmax, equal to the oracle's, with lower bounds that
+    skip the first surfaces (tmin up to 40, rays from above the bricks)."""
+    sc, cam, st, r, osc = bricks_env
+    rng = np.random.default_rng(41)
+    n = 60000
+    rays = np.zeros(n, abi.RAY_DTYPE)
+    rays["origin"] = np.stack([rng.uniform(-5, 145, n), rng.uniform(0.5, 30, n), rng.uniform(-5, 80, n)], 1)
+    d = rng.normal(size=(n, 3))
+    d[:, 1] = -np.abs(d[:, 1])
+    rays["dir"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmin"] = rng.uniform(0.0, 40.0, n).astype(np.float32)
+    rays["tmax"] = rays["tmin"] + rng.uniform(0.0, 200.0, n).astype(np.float32)
+    g = gpu_trace_rays(r, rays, mode)
+    o = osc.trace_rays(rays, mode)
+    if mode == abi.TRACE_CLOSEST:
+        assert_hits_equal(g, o)
+        hit = o["inst"] != 0xFFFFFFFF
+        assert (g["t"][hit] >= rays["tmin"][hit] * (1 - 1e-6)).all()
+        # the bound matters: with tmin = EPS the same rays hit nearer surfaces
+        base = rays.copy()
+        base["tmin"] = 1e-3
+        g0 = gpu_trace_rays(r, base, mode)
+        assert ((g0["t"] < g["t"]) & hit).sum() > n // 20
+    else:
+        assert np.array_equal(g["inst"] != 0xFFFFFFFF, o["inst"] != 0xFFFFFFFF)
 
 
 def test_bricks_trace_pass_reduced(bricks_env):

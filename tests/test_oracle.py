@@ -98,6 +98,28 @@ def test_bvh_equals_brute_force_cornell():
     assert (a["inst"] != 0xFFFFFFFF).mean() > 0.5
 
 
+def test_bvh_equals_brute_force_with_ray_tmin():
+    """The oracle's ray queries honour each ray's tmin, through its BVH as by brute force."""
+    sc, cam, st = scenes.cornell()
+    osc = O.OracleScene(sc)
+    rng = np.random.default_rng(31)
+    n = 20000
+    rays = np.zeros(n, abi.RAY_DTYPE)
+    rays["origin"] = rng.uniform(-0.45, 0.45, (n, 3)) + np.array([0, 0.5, 0])
+    d = rng.normal(size=(n, 3))
+    rays["dir"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["tmin"] = rng.uniform(0.0, 0.8, n)
+    rays["tmax"] = 1000.0
+    a = osc.trace_rays(rays)
+    b = osc.trace_rays(rays, brute=True)
+    assert np.array_equal(a["inst"], b["inst"]) and np.array_equal(a["prim"], b["prim"])
+    hit = a["inst"] != 0xFFFFFFFF
+    assert (a["t"][hit] >= rays["tmin"][hit]).all()
+    base = rays.copy()
+    base["tmin"] = 1e-3
+    assert (osc.trace_rays(base)["t"][hit] < a["t"][hit]).sum() > n // 10
+
+
 def test_bvh_equals_brute_force_bricks_subset():
     sc, cam, st = scenes.bricks()
     # keep a 6 x 6 patch of the grid so brute force stays cheap

@@ -6,7 +6,9 @@ weighted 0.4 at the centre and by normal agreement (>= 0.98) on the same object 
 (FilterHistoryColor :49-68), with the gates opened when the motion in range is below 0.1
 (:154-163); the blend 1 / TemporalFrames (:211-215). Reads outside the image are zero. Compared
 on rgb (the product keeps the previous alpha) within 1e-5 relative: the product and the oracle
-evaluate lerp as one fma and the distance weight with reciprocals."""
+evaluate lerp as one fma and the distance weight with reciprocals. With ProgressiveRender set
+(:95-101, the engine's progressive mode, TemporalFrames 256, Engine.cpp:826) every pixel blends
+the whole float4 of the history image towards the current sample by 1/512, with no rejection."""
 import numpy as np
 
 from gknextengine_gb300 import abi, camera
@@ -26,10 +28,13 @@ def lerp(a, b, t):
     return a + t * (b - a)
 
 
-def reproject_numpy(im, temporal_frames):
+def reproject_numpy(im, temporal_frames, progressive=False):
     f = np.float32
     SD, SS, SA = im[abi.IMG_SINGLE_DIFFUSE], im[abi.IMG_SINGLE_SPECULAR], im[abi.IMG_ALBEDO]
     PD, PS, PA = im[abi.IMG_PREV_DIFFUSE], im[abi.IMG_PREV_SPECULAR], im[abi.IMG_PREV_ALBEDO]
+    if progressive:   # the whole float4, history towards the sample by 1/512 (:95-101)
+        k = f(min(max(1.0 / 512.0, 0.0), 1.0))
+        return [lerp(P, S, k).astype(f) for P, S in ((PD, SD), (PS, SS), (PA, SA))], None
     O0, O1 = im[abi.IMG_OBJECT_ID], im[abi.IMG_OBJECT_ID_PREV]
     MV, N, MM = im[abi.IMG_MOTION], im[abi.IMG_NORMAL], im[abi.IMG_MOTION_MOMENT]
     H, W = O0.shape
@@ -82,9 +87,7 @@ def reproject_numpy(im, temporal_frames):
     return out, use
 
 
-def test_reproject_matches_the_numpy_restatement():
-    rng = np.random.default_rng(33)
-    W, H = 47, 39
+def _random_inputs(rng, W, H):
     im = O.new_images(W, H)
     for k in (abi.IMG_SINGLE_DIFFUSE, abi.IMG_SINGLE_SPECULAR, abi.IMG_ALBEDO, abi.IMG_PREV_DIFFUSE,
               abi.IMG_PREV_SPECULAR, abi.IMG_PREV_ALBEDO):
@@ -107,6 +110,13 @@ def test_reproject_matches_the_numpy_restatement():
     mm = np.zeros((H, W), np.uint32)
     mm[rng.random((H, W)) < 0.1] = 7                        # moving pixels: no history
     im[abi.IMG_MOTION_MOMENT][...] = mm
+    return im
+
+
+def test_reproject_matches_the_numpy_restatement():
+    rng = np.random.default_rng(33)
+    W, H = 47, 39
+    im = _random_inputs(rng, W, H)
     st = camera.Settings(temporal_frames=16)
     fc = camera.FrameBuilder(W, H, st).build(camera.Camera(eye=(0, 0, 3), center=(0, 0, 0), fov_deg=40.0), 0)
     assert fc.progressive_render == 0 and fc.temporal_frames == 16
@@ -115,3 +125,20 @@ def test_reproject_matches_the_numpy_restatement():
     for k, ref in ((abi.IMG_ACCUM_DIFFUSE, d), (abi.IMG_ACCUM_SPECULAR, s), (abi.IMG_ACCUM_ALBEDO, a)):
         np.testing.assert_allclose(im[k][..., :3], ref, rtol=1e-5, atol=1e-5, err_msg=str(k))
     assert 0.2 < use.mean() < 0.9                            # both branches exercised
+
+
+def test_progressive_reproject_matches_the_numpy_restatement():
+    """ProgressiveRender: a 1/512 blend of the whole float4 at every pixel, moving, missed and
+    disoccluded pixels included (the oracle keeps no alpha of its own here)."""
+    rng = np.random.default_rng(34)
+    W, H = 45, 37
+    im = _random_inputs(rng, W, H)
+    st = camera.Settings(progressive=True)
+    fc = camera.FrameBuilder(W, H, st).build(camera.Camera(eye=(0, 0, 3), center=(0, 0, 0), fov_deg=40.0), 0)
+    assert fc.progressive_render == 1 and fc.temporal_frames == 256
+    (d, s, a), _ = reproject_numpy(im, fc.temporal_frames, progressive=True)
+    O.reproject_pass(fc, W, H, im)
+    for k, ref in ((abi.IMG_ACCUM_DIFFUSE, d), (abi.IMG_ACCUM_SPECULAR, s), (abi.IMG_ACCUM_ALBEDO, a)):
+        np.testing.assert_allclose(im[k], ref, rtol=1e-6, atol=1e-6, err_msg=str(k))
+    # the history dominates: 511/512 of it survives
+    np.testing.assert_allclose(im[abi.IMG_ACCUM_DIFFUSE], im[abi.IMG_PREV_DIFFUSE], rtol=0.02, atol=0.02)

@@ -1,8 +1,8 @@
 """The ray-query entry point for callers that cannot allocate device memory.
 
 Some hosts cannot call cudaMalloc when they issue work: an engine whose device memory is
-owned by its own pool allocator, a process at its memory budget, or code running inside
-CUDA stream capture. gkrt_trace_rays_noalloc answers the same queries as gkrt_trace_rays
+owned by its own pool allocator, or a process at its memory budget that must not grow.
+gkrt_trace_rays_noalloc answers the same queries as gkrt_trace_rays
 with its scratch in a fixed static device array. This test calls both through the C ABI on
 the same rays, twice in a row, and requires bit-identical hits (the tolerance the ray
 query parity tests use), and checks that an over-limit batch is refused with a clear
@@ -27,6 +27,7 @@ def _rays(rng, n):
     rays["dir"] = d / np.linalg.norm(d, axis=1, keepdims=True)
     rays["tmin"] = 1e-3
     rays["tmax"] = 1000.0
+    rays["tmin"][::3] = rng.uniform(0.0, 20.0, rays["tmin"][::3].shape[0])   # per-ray lower bounds
     return rays
 
 
@@ -47,9 +48,12 @@ def test_noalloc_ray_queries_match_allocating_entry_point():
                 r.trace_rays_device(rb.data_ptr(), h_ref.data_ptr(), n, mode)
                 r.synchronize()
                 s_ref = r.stats()
+                free0 = torch.cuda.mem_get_info()[0]
                 r.trace_rays_noalloc_device(rb.data_ptr(), h_na.data_ptr(), n, mode)
                 r.synchronize()
                 s_na = r.stats()
+                if call > 0:   # the device's free memory does not move across the call
+                    assert torch.cuda.mem_get_info()[0] == free0
                 a = h_ref.cpu().numpy().view(abi.HIT_DTYPE)
                 b = h_na.cpu().numpy().view(abi.HIT_DTYPE)
                 assert np.array_equal(a["inst"], b["inst"]) and np.array_equal(a["prim"], b["prim"])
@@ -61,6 +65,11 @@ def test_noalloc_ray_queries_match_allocating_entry_point():
                 assert s_na.rays_traced == s_ref.rays_traced == n
                 assert s_na.node_visits == s_ref.node_visits
                 assert s_na.triangle_tests == s_ref.triangle_tests
+        # an empty batch resets the per-call statistics as gkrt_trace_rays does
+        r.trace_rays_noalloc_device(rb.data_ptr(), h_na.data_ptr(), 0, abi.TRACE_CLOSEST)
+        r.synchronize()
+        s0 = r.stats()
+        assert s0.rays_traced == 0 and s0.node_visits == 0 and s0.triangle_tests == 0
 
 
 def test_noalloc_rejects_batches_above_the_scratch_limit():
