@@ -464,58 +464,35 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
     return false;
 }
 
-// Node phase over two-child nodes ("while-while", Aila and Laine, HPG 2009): interior
-// nodes, stack pops, returns to the instance level and instance entries.
-// The first triangle leaf found is postponed into T.leaf and the lane keeps traversing;
-// a second leaf, or leaving the instance the postponed leaf belongs to, makes the lane wait
-// for the leaf phase. Returns true while the lane can take another node step.
+// Node phase over two-child nodes ("while-while", Aila and Laine, HPG 2009). One step
+// resolves the lane's next reference to a node and tests that node: a pop, the hand-back
+// from an instance to the instance level (which pops again: the entries below a marker all
+// belong to the instance level) and an instance entry (whose mesh root is then tested) take
+// no step of their own, so every step of the warp's node loop is one box test per lane.
+// The first triangle leaf found is postponed into T.leaf and the lane waits for the leaf
+// phase; so does a lane about to leave the instance of its postponed leaf. Returns true
+// while the lane can take another node step.
 // cap: the stack's capacity in words (entries); the caller's stack holds at least cap * stride.
 template <bool kRayTmin = false>
 GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride, Counters& cn, int cap = kStackSize) {
     const float tmin = kRayTmin ? T.tmin : kTmin;
     if (++T.iter > kIterCap) { atomicOr(S.error, kErrIter); T.done = true; return false; }
-    const int ref = T.ref;
+    int ref = T.ref;
     if (ref == kRefPop) {
         if (T.sp == 0) { T.done = true; return false; }
         --T.sp;
-        T.ref = (int)stk[T.sp * stride];
-        return true;
+        ref = (int)stk[T.sp * stride];
     }
     if (ref == kRefMarker) {
-        if (T.has_leaf) return false;   // the postponed leaf needs this instance's ray
+        if (T.has_leaf) { T.ref = kRefMarker; return false; }   // the postponed leaf needs this instance's ray
         T.o = T.wo; T.d = T.wd; T.inv = safe_inv(T.wd);
         T.inblas = false;
-        T.ref = kRefPop;
-        return true;
+        if (T.sp == 0) { T.done = true; T.ref = kRefPop; return false; }
+        --T.sp;
+        ref = (int)stk[T.sp * stride];
     }
-    if (ref >= 0) {
-        GK_CHECK_OR_END((uint32_t)ref < S.node_count, S, T, false);
-        ++cn.nodes;
-        const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
-        const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
-        const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
-        float tn0, tn1;
-        const bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, T.o, T.inv, tmin, T.tcull, tn0);
-        const bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, T.o, T.inv, tmin, T.tcull, tn1);
-        if (h0 && h1) {
-            int nearr = nd.x, farr = nd.y;
-            if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
-            if (T.sp >= cap) { atomicOr(S.error, kErrStack); T.done = true; return false; }
-            stk[T.sp * stride] = (uint32_t)farr;
-            ++T.sp;
-            T.ref = nearr;
-        } else if (h0) {
-            T.ref = nd.x;
-        } else if (h1) {
-            T.ref = nd.y;
-        } else {
-            T.ref = kRefPop;
-        }
-        return true;
-    }
-    const uint32_t payload = ~(uint32_t)ref;
-    if (!T.inblas) {
-        T.cur = payload >> 3;
+    if (ref < 0 && !T.inblas) {         // an instance: enter it
+        T.cur = ~(uint32_t)ref >> 3;
         GK_CHECK_OR_END(T.cur < S.inst_count, S, T, false);
         const DevInst* ip = S.inst + T.cur;
         float w[12];
@@ -529,14 +506,38 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         stk[T.sp * stride] = (uint32_t)kRefMarker;
         ++T.sp;
         T.inblas = true;
-        T.ref = __ldg(&ip->blas_root);
-        return true;
+        ref = __ldg(&ip->blas_root);
     }
-    if (T.has_leaf) return false;       // one postponed leaf at a time
-    T.leaf = payload;
-    T.has_leaf = true;
-    T.ref = kRefPop;
-    return kSpeculative;
+    if (ref < 0) {                      // a triangle leaf: postpone it
+        if (T.has_leaf) { T.ref = ref; return false; }   // one postponed leaf at a time
+        T.leaf = ~(uint32_t)ref;
+        T.has_leaf = true;
+        T.ref = kRefPop;
+        return kSpeculative;
+    }
+    GK_CHECK_OR_END((uint32_t)ref < S.node_count, S, T, false);
+    ++cn.nodes;
+    const float4* np = reinterpret_cast<const float4*>(S.nodes + ref);
+    const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+    const int4 nd = __ldg(reinterpret_cast<const int4*>(np + 3));
+    float tn0, tn1;
+    const bool h0 = slab(na.x, na.y, na.z, na.w, nb.x, nb.y, T.o, T.inv, tmin, T.tcull, tn0);
+    const bool h1 = slab(nb.z, nb.w, nc.x, nc.y, nc.z, nc.w, T.o, T.inv, tmin, T.tcull, tn1);
+    if (h0 && h1) {
+        int nearr = nd.x, farr = nd.y;
+        if (tn1 < tn0) { nearr = nd.y; farr = nd.x; }
+        if (T.sp >= cap) { atomicOr(S.error, kErrStack); T.done = true; return false; }
+        stk[T.sp * stride] = (uint32_t)farr;
+        ++T.sp;
+        T.ref = nearr;
+    } else if (h0) {
+        T.ref = nd.x;
+    } else if (h1) {
+        T.ref = nd.y;
+    } else {
+        T.ref = kRefPop;
+    }
+    return true;
 }
 
 // t of byte `b` of `word` (a WideNode plane): fma(2^23 + q, C, B').

@@ -11,6 +11,9 @@ are multiples of 8 and the image views are dense.
 from __future__ import annotations
 
 import ctypes as C
+import json
+import os
+import sys
 import time
 
 import numpy as np
@@ -91,6 +94,149 @@ class CornellVariants:
             self.r.trace_pass(self.frame(v, seed0 + k))
             acc += (d[..., :3] * a[..., :3] + s[..., :3]).double()
         return (acc / spp).float()
+
+
+def compose_input(r: PathTracingRenderer, out):
+    """The pass's images after a trace pass as the network's input, out (H, W, 10): radiance
+    composed as the compose pass does (diffuse x albedo + specular), albedo, normal, depth."""
+    d = device_view(r.image_view(abi.IMG_SINGLE_DIFFUSE), 4)
+    s = device_view(r.image_view(abi.IMG_SINGLE_SPECULAR), 4)
+    a = device_view(r.image_view(abi.IMG_ALBEDO), 4)
+    n = device_view(r.image_view(abi.IMG_NORMAL), 4)
+    z = device_view(r.image_view(abi.IMG_PREV_DEPTH), 1)
+    out[..., 0:3] = d[..., :3] * a[..., :3] + s[..., :3]
+    out[..., 3:6] = a[..., :3]
+    out[..., 6:9] = n[..., :3]
+    out[..., 9:10] = z
+    return out
+
+
+def render_reference_frames(r: PathTracingRenderer, fb: camera.FrameBuilder, cam: camera.Camera, spp: int,
+                            spp_per_pass: int = 64, seed0: int = 1 << 20):
+    """Composed radiance (H, W, 3) averaged over spp samples per pixel: spp / spp_per_pass
+    trace passes of the static view, each with spp_per_pass samples per pixel (the pass's own
+    multi-sample loop) and its own RNG stream (TotalFrames seed0 + pass index)."""
+    torch = _torch()
+    passes = max(1, spp // spp_per_pass)
+    keep = fb.s.samples
+    fb.s.samples = spp_per_pass
+    try:
+        acc = torch.zeros((r.height, r.width, 3), dtype=torch.float64, device="cuda")
+        d = device_view(r.image_view(abi.IMG_SINGLE_DIFFUSE), 4)
+        s = device_view(r.image_view(abi.IMG_SINGLE_SPECULAR), 4)
+        a = device_view(r.image_view(abi.IMG_ALBEDO), 4)
+        for k in range(passes):
+            r.trace_pass(fb.build(cam, seed0 + k))
+            acc += (d[..., :3] * a[..., :3] + s[..., :3]).double()
+    finally:
+        fb.s.samples = keep
+    return (acc / passes).float()
+
+
+# ---- the C5 training set: renderer-generated 1-spp / 4096-spp crop pairs ----
+
+def cornell_family_view(seed: int, index: int):
+    """View `index` of the training family: the C1 Cornell box (scenes.cornell) with seeded
+    variations, so that the network sees the materials and lighting of other scenes while
+    staying on config-1 frames. Per view: albedos U(0.15, 0.9)^3; each wall Lambertian (75 %),
+    a GGX mixture (15 %) or a rough metal (10 %); each box Lambertian (35 %), mixture (25 %),
+    metal with roughness U(0.02, 1) (20 %), glass (10 %) or an emitter of radiance U(3, 20)
+    (10 %); the ceiling light's radiance U(5, 25); the camera orbited U(-40, 40) degrees,
+    raised or lowered, moved in or out and given a field of view U(32, 55) degrees.
+    Returns (SceneArrays, Camera, Settings) with C1's 4 bounces and no TAA."""
+    rng = np.random.default_rng([seed, index])
+    sc, cam, st = scenes.cornell(seed=int(rng.integers(1 << 30)))
+    mats = []
+    for i in range(7):
+        alb = rng.uniform(0.15, 0.9, 3)
+        u = rng.random()
+        if i < 5:
+            m = (scenes.lambertian(alb) if u < 0.75 else
+                 scenes.mixture(alb, rng.uniform(0.05, 1.0)) if u < 0.9 else scenes.metallic(alb, rng.uniform(0.2, 1.0)))
+        else:
+            m = (scenes.lambertian(alb) if u < 0.35 else
+                 scenes.mixture(alb, rng.uniform(0.05, 1.0)) if u < 0.6 else
+                 scenes.metallic(alb, rng.uniform(0.02, 1.0)) if u < 0.8 else
+                 scenes.dielectric(1.5) if u < 0.9 else scenes.diffuse_light(np.full(3, rng.uniform(3.0, 20.0))))
+        mats.append(m)
+    mats.append(scenes.diffuse_light(np.full(3, rng.uniform(5.0, 25.0))))
+    materials = np.array(mats, dtype=abi.MATERIAL_DTYPE)
+    sc = abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, materials,
+                         sc.instances, lights=sc.lights, name=f"cornell-family-{seed}-{index}")
+    c = cam.orbit(float(rng.uniform(-40.0, 40.0)))
+    eye = c.center + (c.eye - c.center) * rng.uniform(0.7, 1.25)
+    eye[1] = c.center[1] + rng.uniform(-0.3, 0.35)
+    cam = camera.Camera(eye=eye, center=c.center, fov_deg=float(rng.uniform(32.0, 55.0)))
+    st.taa = False
+    st.flags = 0
+    return sc, cam, st
+
+
+def build_crop_set(r: PathTracingRenderer, views: int = 128, view_size: int = 1024, crop: int = 256,
+                   ref_spp: int = 4096, inputs_per_crop: int = 4, seed: int = 11, spp_per_pass: int = 64,
+                   log=None):
+    """The C5 training set on the GPU: `views` family views rendered at view_size^2, each cut
+    into (view_size / crop)^2 crops (128 views x 16 = 2048 crops of 256 x 256). Per crop: the
+    ref_spp-sample composed radiance (the target) and inputs_per_crop independent 1-spp inputs
+    (10 channels each). Returns (inputs (N, R, crop, crop, 10), targets (N, crop, crop, 3),
+    info), device float32."""
+    torch = _torch()
+    g = view_size // crop
+    n = views * g * g
+    inputs = torch.zeros((n, inputs_per_crop, crop, crop, 10), device="cuda")
+    targets = torch.zeros((n, crop, crop, 3), device="cuda")
+    full = torch.zeros((view_size, view_size, 10), device="cuda")
+    t0 = time.perf_counter()
+    for v in range(views):
+        sc, cam, st = cornell_family_view(seed, v)
+        r.load_scene(sc)
+        if (r.width, r.height) != (view_size, view_size):
+            r.create_swap_chain(view_size, view_size)
+        fb = camera.FrameBuilder(view_size, view_size, st)
+        ref = render_reference_frames(r, fb, cam, ref_spp, spp_per_pass)
+        base = v * g * g
+        targets[base:base + g * g] = ref.view(g, crop, g, crop, 3).permute(0, 2, 1, 3, 4).reshape(g * g, crop, crop, 3)
+        for k in range(inputs_per_crop):
+            r.trace_pass(fb.build(cam, 1000 + k))
+            compose_input(r, full)
+            inputs[base:base + g * g, k] = full.view(g, crop, g, crop, 10).permute(0, 2, 1, 3, 4).reshape(
+                g * g, crop, crop, 10)
+        if log and (v + 1) % 16 == 0:
+            torch.cuda.synchronize()
+            log(f"crop set: {v + 1}/{views} views, {time.perf_counter() - t0:.1f} s")
+    torch.cuda.synchronize()
+    return inputs, targets, {"views": views, "view_size": view_size, "crop": crop, "crops": n,
+                             "reference_spp": ref_spp, "inputs_per_crop": inputs_per_crop, "seed": seed,
+                             "seconds": time.perf_counter() - t0}
+
+
+def lr_at(step: int, steps: int, lr: float, lr_decay_from: float = 0.6, warmup: int = 40) -> float:
+    """Linear warm-up over `warmup` steps, constant, then a decay to lr / 10 over the steps
+    after lr_decay_from."""
+    frac = step / max(steps - 1, 1)
+    cur = lr if frac < lr_decay_from else lr * (0.1 ** ((frac - lr_decay_from) / (1.0 - lr_decay_from)))
+    return cur * min(1.0, (step + 1) / warmup)
+
+
+def train_crops(net: "Unet", inputs, targets, steps: int, batch: int = 8, lr: float = 5e-4, seed: int = 9,
+                log=None):
+    """Adam steps on random crops of the set, each with one of its 1-spp inputs picked at
+    random. Returns the per-step losses (mean squared log error)."""
+    torch = _torch()
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    n, R = inputs.shape[0], inputs.shape[1]
+    losses = []
+    t0 = time.perf_counter()
+    for step in range(steps):
+        idx = torch.randint(0, n, (batch,), device="cuda", generator=gen)
+        rep = torch.randint(0, R, (batch,), device="cuda", generator=gen)
+        inp = inputs[idx, rep].contiguous()
+        tgt = targets[idx].contiguous()
+        losses.append(net.train_step(inp, tgt, lr_at(step, steps, lr)))
+        if log and (step + 1) % 1000 == 0:
+            log(f"train: step {step + 1}/{steps}, loss {np.mean(losses[-200:]):.5f}, "
+                f"{time.perf_counter() - t0:.1f} s")
+    return losses
 
 
 def relmse(x, y) -> float:
@@ -250,6 +396,124 @@ def evaluate(r: PathTracingRenderer, net: Unet, width: int = 1920, height: int =
     return out
 
 
+def evaluate_view(r: PathTracingRenderer, net: "Unet", scene, cam: camera.Camera, settings: camera.Settings,
+                  name: str, width: int = 1920, height: int = 1080, ref_spp: int = 4096, reps: int = 10,
+                  load: bool = True):
+    """RelMSE against a ref_spp reference of one static view, for the raw 1-spp frame, the
+    reference's joint bilateral filter (JBF, 5 x 5) and the a-trous filter on that frame
+    (history weight 1), the learned denoiser through the library's own denoise pass
+    (GKRT_DENOISE_UNET) on the same frame, and the temporal steady state of the two filters
+    (128 frames of reprojection at 1/16). Frame times in ms, CUDA events: a bilateral frame is
+    trace + reproject + JBF, a learned frame is trace + the learned denoise pass. TAA is off, so
+    every frame sees the camera the reference was rendered with."""
+    torch = _torch()
+    st = settings
+    st.taa = False
+    st.flags = 0
+    if load:
+        r.load_scene(scene)
+    r.create_swap_chain(width, height)
+    fb = camera.FrameBuilder(width, height, st)
+    t0 = time.perf_counter()
+    ref = render_reference_frames(r, fb, cam, ref_spp)
+    torch.cuda.synchronize()
+    out = {"scene": f"{name} {width}x{height}", "reference_spp": ref_spp,
+           "metric": "mean (x-y)^2/(y^2+1e-2) over px, RGB, linear radiance",
+           "reference_seconds": time.perf_counter() - t0}
+    fseed = 424242
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    linear = device_view(r.image_view(abi.IMG_DENOISED_LINEAR), 4)
+    keep = (st.denoiser, st.bf_size, st.temporal_frames)
+    try:
+        st.denoiser, st.temporal_frames = abi.DENOISE_UNET, 1
+        fb = camera.FrameBuilder(width, height, st)
+        f1 = fb.build(cam, fseed)
+        r.trace_pass(f1)
+        inp = torch.zeros((height, width, 10), device="cuda")
+        out["raw_1spp"] = relmse(compose_input(r, inp)[..., :3], ref)
+        out["trace_ms"] = timed(lambda: r.trace_pass(f1))
+        out["learned_ms"] = timed(lambda: r.denoise_pass(f1))
+        out["learned_1spp"] = relmse(linear, ref)
+        for fname, mode in (("bilateral", abi.DENOISE_JBF), ("atrous", abi.DENOISE_ATROUS)):
+            st.denoiser, st.bf_size, st.temporal_frames = mode, 5, 1
+            fb = camera.FrameBuilder(width, height, st)
+            f1 = fb.build(cam, fseed)
+            r.create_swap_chain(width, height)
+            r.trace_pass(f1)
+            r.reproject_pass(f1)
+            out[f"{fname}_ms"] = timed(lambda: r.denoise_pass(f1))
+            linear = device_view(r.image_view(abi.IMG_DENOISED_LINEAR), 4)
+            out[f"{fname}_1spp"] = relmse(linear, ref)
+            out["reproject_ms"] = timed(lambda: r.reproject_pass(f1))
+            st.temporal_frames = 16
+            fb = camera.FrameBuilder(width, height, st)
+            r.create_swap_chain(width, height)
+            for f in range(128):
+                r.render(fb.build(cam, 500000 + f))
+            linear = device_view(r.image_view(abi.IMG_DENOISED_LINEAR), 4)
+            out[f"{fname}_temporal"] = relmse(linear, ref)
+    finally:
+        st.denoiser, st.bf_size, st.temporal_frames = keep
+    out["learned_over_bilateral"] = out["learned_1spp"] / out["bilateral_1spp"]
+    out["learned_over_bilateral_temporal"] = out["learned_1spp"] / out["bilateral_temporal"]
+    out["frame_ms_bilateral"] = out["trace_ms"] + out["reproject_ms"] + out["bilateral_ms"]
+    out["frame_ms_learned"] = out["trace_ms"] + out["learned_ms"]
+    out["frame_time_ratio"] = out["frame_ms_learned"] / out["frame_ms_bilateral"]
+    return out
+
+
+# The network trained on the C5 crop set (train_c5 below), shipped with the library.
+C5_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "unet_c5.ckpt")
+
+
+def load_c5(r: PathTracingRenderer, path: str = C5_WEIGHTS) -> "Unet":
+    """The shipped C5 network on a renderer's context (the context's denoise pass uses it)."""
+    net = Unet(r, seed=7)
+    net.load(path)
+    return net
+
+
+def evaluate_c5(r: PathTracingRenderer, net: "Unet", width: int = 1920, height: int = 1080,
+                ref_spp: int = 4096) -> dict:
+    """The learned denoiser against the filters on two views, neither in the training set: the
+    config-1 Cornell box itself (scenes.cornell, its own albedos) and a frame of the C2 brick
+    scene (1.03 M triangles, GGX metals and mixtures, 64 emissive bricks, 8 bounces), a scene
+    family the network has never seen."""
+    sc, cam, st = scenes.cornell()
+    cornell = evaluate_view(r, net, sc, cam, st, "config-1 cornell (held out)", width, height, ref_spp)
+    sc, cam, st = scenes.bricks()
+    bricks = evaluate_view(r, net, sc, cam, st, "c2 bricks (unseen scene family)", width, height, ref_spp)
+    return {"cornell": cornell, "bricks": bricks}
+
+
+def train_c5(r: PathTracingRenderer, steps: int = 8000, batch: int = 8, lr: float = 5e-4, views: int = 128,
+             ref_spp: int = 4096, inputs_per_crop: int = 4, seed: int = 11, log=None):
+    """The C5 training run: the crop set (build_crop_set: 2048 crops of 256 x 256 with 4096-spp
+    targets) rendered by the path tracer, then `steps` Adam steps of the library's own training
+    kernels on batches of crops. Returns (net, losses, info)."""
+    inputs, targets, info = build_crop_set(r, views=views, ref_spp=ref_spp, inputs_per_crop=inputs_per_crop,
+                                           seed=seed, log=log)
+    net = Unet(r, seed=7)
+    t0 = time.perf_counter()
+    losses = train_crops(net, inputs, targets, steps, batch=batch, lr=lr, log=log)
+    _torch().cuda.synchronize()
+    info.update({"steps": steps, "batch": batch, "lr": lr, "train_s": time.perf_counter() - t0,
+                 "loss_first": float(np.mean(losses[:50])), "loss_last": float(np.mean(losses[-200:]))})
+    del inputs, targets
+    return net, losses, info
+
+
 def train_default(r: PathTracingRenderer, steps: int = 600, variants: int = 16, ref_spp: int = 256,
                   width: int = 512, height: int = 512, seed: int = 5):
     """The training run the tests and the benchmark use; returns (net, losses, seconds)."""
@@ -263,3 +527,37 @@ def train_default(r: PathTracingRenderer, steps: int = 600, variants: int = 16, 
     _torch().cuda.synchronize()
     return net, losses, {"data_s": t_data, "train_s": time.perf_counter() - t0, "steps": steps,
                          "ms_per_step": (time.perf_counter() - t0) / steps * 1e3}
+
+
+def main(argv=None):
+    """python -m gknextengine_gb300.denoiser --train-c5 OUT.ckpt [--steps N] [--views V]:
+    renders the C5 crop set, trains, writes the checkpoint and prints the evaluation."""
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train-c5", required=True, help="checkpoint file to write")
+    ap.add_argument("--steps", type=int, default=8000)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--views", type=int, default=128)
+    ap.add_argument("--ref-spp", type=int, default=4096)
+    ap.add_argument("--eval-spp", type=int, default=4096)
+    ap.add_argument("--info", default=None, help="JSON file for the training and evaluation record")
+    a = ap.parse_args(argv)
+
+    def log(msg):
+        print(msg, flush=True)
+
+    with PathTracingRenderer(0) as r:
+        net, losses, info = train_c5(r, steps=a.steps, batch=a.batch, views=a.views, ref_spp=a.ref_spp, log=log)
+        net.save(a.train_c5)
+        info["losses_every_100"] = [float(np.mean(losses[i:i + 100])) for i in range(0, len(losses), 100)]
+        log(json.dumps({k: v for k, v in info.items() if k != "losses_every_100"}))
+        ev = evaluate_c5(r, net, ref_spp=a.eval_spp)
+        log(json.dumps(ev))
+        if a.info:
+            with open(a.info, "w") as f:
+                json.dump({"training": info, "evaluation": ev}, f, indent=1)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -98,6 +98,10 @@ def diffuse_light(rgb):
     return material(rgb, abi.MAT_DIFFUSE_LIGHT, fuzziness=0.0, ri=0.0, metalness=0.0)
 
 
+def dielectric(ri, fuzz=0.0):
+    return material((1.0, 1.0, 1.0), abi.MAT_DIELECTRIC, fuzziness=fuzz, ri=ri, metalness=0.0, ri2=ri)
+
+
 class MeshBuilder:
     def __init__(self):
         self.pos, self.nrm, self.slot, self.idx = [], [], [], []

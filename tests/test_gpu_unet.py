@@ -112,15 +112,36 @@ def test_checkpoint_resume(tmp_path):
         assert b.optimizer_state()[2] == 8
 
 
-def test_denoiser_beats_bilateral():
-    """Train on 512 x 512 Cornell variants (256-spp targets), then on a held-out 1080p variant
-    compare RelMSE against 4096 spp: the network must reach <= 0.8 x the bilateral filter's
-    (the reference's joint bilateral filter on the same 1-spp frame)."""
-    from gknextengine_gb300.denoiser import evaluate, train_default
+def test_training_on_crops_lowers_the_loss():
+    """The C5 training path at a small size: a crop set rendered by the path tracer (4 family
+    views at 512^2 cut into 16 crops of 128^2, 256-spp targets, two 1-spp inputs each), then
+    300 Adam steps of the library's training kernels on random crops."""
+    torch = _torch()
+    from gknextengine_gb300.denoiser import Unet, build_crop_set, train_crops
     with PathTracingRenderer(0) as r:
-        net, losses, info = train_default(r)
-        ev = evaluate(r, net)
-        print(f"denoiser: {info}, loss {np.mean(losses[:20]):.4f} -> {np.mean(losses[-20:]):.4f}; {ev}")
-        assert np.mean(losses[-20:]) < 0.2 * np.mean(losses[:20])
-        assert ev["learned_1spp"] <= 0.8 * ev["bilateral_1spp"]
+        inputs, targets, info = build_crop_set(r, views=4, view_size=512, crop=128, ref_spp=256, inputs_per_crop=2)
+        assert inputs.shape == (64, 2, 128, 128, 10) and targets.shape == (64, 128, 128, 3)
+        assert torch.isfinite(targets).all() and float(targets.mean()) > 0.0
+        # two 1-spp inputs of a crop are independent samples of its target
+        assert not torch.equal(inputs[:, 0, ..., :3], inputs[:, 1, ..., :3])
+        net = Unet(r, seed=7)
+        losses = train_crops(net, inputs, targets, 300, batch=4)
+        assert np.mean(losses[-30:]) < 0.5 * np.mean(losses[:10]), (np.mean(losses[:10]), np.mean(losses[-30:]))
+
+
+def test_denoiser_beats_bilateral():
+    """The shipped network (trained by train_c5 on 2048 crops of 256^2 with 4096-spp targets,
+    Cornell-family views only) on a 1920 x 1080 frame of the C2 brick scene, a scene family it
+    has never seen (1.03 M triangles, GGX metals and mixtures, 64 emissive bricks, 8 bounces):
+    RelMSE against 4096 spp at most 0.8 x the reference's joint bilateral filter on the same
+    1-spp frame, in at most 1.5 x its frame time (trace + reproject + JBF against trace + the
+    learned denoise pass, CUDA events)."""
+    from gknextengine_gb300.denoiser import evaluate_view, load_c5
+    with PathTracingRenderer(0) as r:
+        net = load_c5(r)
+        sc, cam, st = scenes.bricks()
+        ev = evaluate_view(r, net, sc, cam, st, "c2 bricks", 1920, 1080, ref_spp=4096)
+        print(ev)
+        assert ev["learned_1spp"] <= 0.8 * ev["bilateral_1spp"], ev
         assert ev["learned_1spp"] < ev["raw_1spp"]
+        assert ev["frame_time_ratio"] <= 1.5, ev
