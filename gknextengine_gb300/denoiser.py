@@ -137,36 +137,63 @@ def render_reference_frames(r: PathTracingRenderer, fb: camera.FrameBuilder, cam
 
 def cornell_family_view(seed: int, index: int):
     """View `index` of the training family: the C1 Cornell box (scenes.cornell) with seeded
-    variations, so that the network sees the materials and lighting of other scenes while
-    staying on config-1 frames. Per view: albedos U(0.15, 0.9)^3; each wall Lambertian (75 %),
-    a GGX mixture (15 %) or a rough metal (10 %); each box Lambertian (35 %), mixture (25 %),
-    metal with roughness U(0.02, 1) (20 %), glass (10 %) or an emitter of radiance U(3, 20)
-    (10 %); the ceiling light's radiance U(5, 25); the camera orbited U(-40, 40) degrees,
-    raised or lowered, moved in or out and given a field of view U(32, 55) degrees.
+    variations, so that the network meets other materials, lighting regimes and framings while
+    staying on config-1 frames. Per view:
+      * albedos U(0.15, 0.9)^3; each wall Lambertian (70 %), a GGX mixture (20 %) or a rough
+        metal (10 %); each box Lambertian (30 %), mixture (30 %), metal with roughness
+        U(0.02, 1) (25 %) or glass (15 %);
+      * lighting: the ceiling light at radiance U(5, 25) (55 %), dimmed to U(0.5, 5) (15 %), or
+        off with a box as the only emitter, radiance U(5, 20) (30 %); otherwise a box emits
+        with probability 0.1;
+      * the boxes moved, turned and scaled inside the room;
+      * the camera orbited U(-50, 50) degrees, moved 0.6 to 3 times as far, raised or lowered,
+        with a field of view U(25, 60) degrees;
+      * in half of the views the whole scene and the camera scaled by a factor log-uniform in
+        [1, 80]: the image stays the same while the depth channel (NDC depth, near 0.2, far
+        2000) moves towards 1 as in large scenes.
     Returns (SceneArrays, Camera, Settings) with C1's 4 bounces and no TAA."""
     rng = np.random.default_rng([seed, index])
     sc, cam, st = scenes.cornell(seed=int(rng.integers(1 << 30)))
     mats = []
-    for i in range(7):
+    for i in range(5):
         alb = rng.uniform(0.15, 0.9, 3)
         u = rng.random()
-        if i < 5:
-            m = (scenes.lambertian(alb) if u < 0.75 else
-                 scenes.mixture(alb, rng.uniform(0.05, 1.0)) if u < 0.9 else scenes.metallic(alb, rng.uniform(0.2, 1.0)))
+        mats.append(scenes.lambertian(alb) if u < 0.7 else
+                    scenes.mixture(alb, rng.uniform(0.05, 1.0)) if u < 0.9 else
+                    scenes.metallic(alb, rng.uniform(0.2, 1.0)))
+    u = rng.random()
+    mode = "ceiling" if u < 0.55 else "dim" if u < 0.7 else "box"
+    emitting_box = int(rng.integers(0, 2)) if mode == "box" else (int(rng.integers(0, 2)) if rng.random() < 0.1 else -1)
+    for b in range(2):
+        alb = rng.uniform(0.15, 0.9, 3)
+        u = rng.random()
+        if b == emitting_box:
+            mats.append(scenes.diffuse_light(np.full(3, rng.uniform(5.0, 20.0))))
         else:
-            m = (scenes.lambertian(alb) if u < 0.35 else
-                 scenes.mixture(alb, rng.uniform(0.05, 1.0)) if u < 0.6 else
-                 scenes.metallic(alb, rng.uniform(0.02, 1.0)) if u < 0.8 else
-                 scenes.dielectric(1.5) if u < 0.9 else scenes.diffuse_light(np.full(3, rng.uniform(3.0, 20.0))))
-        mats.append(m)
-    mats.append(scenes.diffuse_light(np.full(3, rng.uniform(5.0, 25.0))))
+            mats.append(scenes.lambertian(alb) if u < 0.3 else
+                        scenes.mixture(alb, rng.uniform(0.05, 1.0)) if u < 0.6 else
+                        scenes.metallic(alb, rng.uniform(0.02, 1.0)) if u < 0.85 else scenes.dielectric(1.5))
+    light = {"ceiling": rng.uniform(5.0, 25.0), "dim": rng.uniform(0.5, 5.0), "box": 0.0}[mode]
+    mats.append(scenes.diffuse_light(np.full(3, light)))
     materials = np.array(mats, dtype=abi.MATERIAL_DTYPE)
-    sc = abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, materials,
-                         sc.instances, lights=sc.lights, name=f"cornell-family-{seed}-{index}")
-    c = cam.orbit(float(rng.uniform(-40.0, 40.0)))
-    eye = c.center + (c.eye - c.center) * rng.uniform(0.7, 1.25)
-    eye[1] = c.center[1] + rng.uniform(-0.3, 0.35)
-    cam = camera.Camera(eye=eye, center=c.center, fov_deg=float(rng.uniform(32.0, 55.0)))
+    inst = sc.instances.copy()
+    scale = float(np.exp(rng.uniform(0.0, np.log(80.0)))) if rng.random() < 0.5 else 1.0
+    inst[0] = scenes.make_instance(0, scenes.trs(scale=(scale, scale, scale)), [0, 1, 2, 3, 4, 7], 0)
+    for k, (mat, iid) in enumerate(((5, 1), (6, 2))):
+        sxz = rng.uniform(0.15, 0.35)
+        world = scenes.trs((rng.uniform(-0.3, 0.3), 0.0, rng.uniform(-0.3, 0.3)), rot_y_deg=rng.uniform(-45, 45),
+                           scale=(sxz, rng.uniform(0.15, 0.7), sxz * rng.uniform(0.7, 1.4)))
+        inst[1 + k] = scenes.make_instance(1, world * scale, [mat], iid)
+    lights = sc.lights.copy()
+    for f in ("p0", "p1", "p3"):
+        lights[f][:, :3] *= scale
+    lights["normal_area"][:, 3] *= scale * scale
+    sc = abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, materials, inst,
+                         lights=lights, name=f"cornell-family-{seed}-{index}")
+    c = cam.orbit(float(rng.uniform(-50.0, 50.0)))
+    eye = c.center + (c.eye - c.center) * rng.uniform(0.6, 3.0)
+    eye[1] = c.center[1] + rng.uniform(-0.35, 0.45)
+    cam = camera.Camera(eye=eye * scale, center=c.center * scale, fov_deg=float(rng.uniform(25.0, 60.0)))
     st.taa = False
     st.flags = 0
     return sc, cam, st
