@@ -319,7 +319,6 @@ GK_D f3 tri_v(const float4* tris, uint32_t ti, int k, uint32_t* prim = nullptr) 
 struct Trav {
     f3 wo, wd;            // world ray
     f3 o, d, inv;         // ray in the current space (world or instance)
-    Shear sh;
     float tmin;           // read by the ray-query kernels (kRayTmin); the rt pass uses kTmin
     float tmax, tcull, best_lo, best_hi;
     double best_td;
@@ -339,7 +338,6 @@ template <bool kWide = false>
 GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int mode, float tmin = kTmin) {
     T.wo = wo; T.wd = wd; T.o = wo; T.d = wd;
     T.inv = safe_inv(wd);
-    T.sh = make_shear(wd);
     T.tmin = tmin;
     T.tmax = tmax;
     T.tcull = tmax * 1.000001f;
@@ -464,12 +462,13 @@ static __device__ __noinline__ LeafSlow leaf_slow(f3 o, f3 d, Shear sh, f3 v0, f
 template <bool kRayTmin = false>
 GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, Counters& cn) {
     const float tmin = kRayTmin ? T.tmin : kTmin;
+    const Shear sh = make_shear(T.d);
     for (uint32_t k = 0; k < cnt; ++k) {
         const uint32_t ti = first + k;
         uint32_t prim;
         const f3 v0 = tri_v(S.tris, ti, 0, &prim), v1 = tri_v(S.tris, ti, 1), v2 = tri_v(S.tris, ti, 2);
         ++cn.tris;
-        const Fp32Hit f = fp32_test(T.o, T.sh, v0, v1, v2);
+        const Fp32Hit f = fp32_test(T.o, sh, v0, v1, v2);
         if (f.kind == 0) continue;
         float t, e;
         if (f.kind == 1 && plane_interval(T.o, T.d, v0, v1, v2, f.e, t, e) && t - e >= tmin && t + e <= T.tmax) {
@@ -491,7 +490,7 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
         LeafBest b;
         b.td = T.best_td; b.lo = T.best_lo; b.hi = T.best_hi; b.inst = T.inst; b.prim = T.prim; b.tri = T.tri;
         b.hit = T.hit; b.exact = T.best_exact;
-        const LeafSlow r = leaf_slow(T.o, T.d, T.sh, v0, v1, v2, f, tmin, T.tmax, T.mode, T.cur, prim, b, T.inblas,
+        const LeafSlow r = leaf_slow(T.o, T.d, sh, v0, v1, v2, f, tmin, T.tmax, T.mode, T.cur, prim, b, T.inblas,
                                      T.wo, T.wd, S.inst, S.tris);
         cn.fallbacks += r.fallbacks;
         cn.retraces += r.retraces;
@@ -545,7 +544,6 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
         T.o = xpoint(w, T.wo);
         T.d = xvector(w, T.wd);
         T.inv = safe_inv(T.d);
-        T.sh = make_shear(T.d);
         if (T.sp >= cap) { atomicOr(S.error, kErrStack); T.done = true; return false; }
         stk[T.sp * stride] = (uint32_t)kRefMarker;
         ++T.sp;
@@ -716,7 +714,6 @@ GK_D bool trav_node_step_wide(Trav& T, const SceneView& S, uint32_t* stk, int st
         T.o = xpoint(w, T.wo);
         T.d = xvector(w, T.wd);
         T.inv = safe_inv(T.d);
-        T.sh = make_shear(T.d);
         if (T.sp >= kStackEntries) { atomicOr(S.error, kErrStack); T.done = true; return false; }
         uint32_t* e = stk + 3 * T.sp * stride;
         e[0] = (uint32_t)kRefMarker;
