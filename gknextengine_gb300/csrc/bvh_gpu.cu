@@ -875,8 +875,9 @@ __global__ void __launch_bounds__(128) k_refit_wide(RefitLinks lk, const BvhNode
 // the round-by-round build above waits for a host readback after every round. For up to kOneMax
 // instances one block of kOneT threads builds the whole tree instead, with the same split rule,
 // level by level:
-//   * tasks of more than kWarpTask instances: the whole block (bounds, bins in shared memory,
-//     the SAH per axis on three threads, a stable partition by block-wide ballots);
+//   * tasks of more than kWarpTask instances: the whole block (bounds, per-warp bins in shared
+//     memory merged after, the SAH per axis on three threads, a stable partition by block-wide
+//     ballots);
 //   * tasks of kSmall + 1 .. kWarpTask instances: one warp each (warp reductions, bins in the
 //     warp's shared memory, a stable partition by ballots);
 //   * tasks of up to kSmall instances: one thread each, the sequential builder of k_small.
@@ -888,7 +889,7 @@ __global__ void __launch_bounds__(128) k_refit_wide(RefitLinks lk, const BvhNode
 // A second one-block kernel collapses the tree into 8-wide nodes level by level, numbering the
 // wide nodes as gpu_bvh_collapse does.
 
-constexpr int kOneT = 1024;
+constexpr int kOneT = 512;   // 128 registers a thread: the sequential subtree builds keep their state
 constexpr int kOneWarps = kOneT / 32;
 constexpr uint32_t kWarpTask = 2048;
 constexpr uint32_t kOneMax = 1u << 16;
@@ -1014,7 +1015,7 @@ __device__ void one_block_task(const LTask& T, const Geo& g, uint32_t* idx, uint
     warp_bounds(v);
     if (lane == 0)
         for (int k = 0; k < 12; ++k) S.red[warp][k] = v[k];
-    bins_clear(S.bins, t, kOneT);
+    bins_clear(S.wbins[warp], lane, 32);   // each warp bins into its own copy (less contention)
     __syncthreads();
     for (int k = 0; k < 12; ++k) {   // every thread combines the warps in the same order
         float a = S.red[0][k];
@@ -1027,7 +1028,17 @@ __device__ void one_block_task(const LTask& T, const Geo& g, uint32_t* idx, uint
         write_child(nodes, root_box, T.parent, T.side, v, (int)node_base + T.node);
         atomicAdd(&info[0], 1u);
     }
-    for (uint32_t i = T.begin + (uint32_t)t; i < T.end; i += kOneT) bins_add(S.bins, g, idx[i], clo, scale);
+    for (uint32_t i = T.begin + (uint32_t)t; i < T.end; i += kOneT) bins_add(S.wbins[warp], g, idx[i], clo, scale);
+    __syncthreads();
+    for (int i = t; i < kBinWords; i += kOneT) {   // merge the warps' copies
+        const int q = i % 7;
+        int a = S.wbins[0][i];
+        for (int w = 1; w < kOneWarps; ++w) {
+            const int b = S.wbins[w][i];
+            a = q == 6 ? a + b : (q < 3 ? min(a, b) : max(a, b));
+        }
+        S.bins[i] = a;
+    }
     __syncthreads();
     if (t < 3) S.ab[t] = axis_best(S.bins, t, scale[t]);
     __syncthreads();

@@ -305,7 +305,7 @@ struct TraceOut {
     uint32_t inst, prim, tri;
 };
 
-enum { kClosest = 0, kAny = 1 };
+enum { kClosest = 0, kAny = 1, kExact = 2 };
 
 GK_D f3 tri_v(const float4* tris, uint32_t ti, int k, uint32_t* prim = nullptr) {
     float4 v = __ldg(&tris[3 * ti + k]);
@@ -325,7 +325,7 @@ struct Trav {
     uint32_t inst, prim, tri;   // current best
     uint32_t cur;               // instance being traversed
     int ref, sp, iter;
-    int mode;                   // kClosest / kAny
+    int mode;                   // kClosest / kAny / kExact
     uint32_t leaf;              // postponed triangle leaf (payload), valid when has_leaf
     bool hit, best_exact, inblas, done, ambiguous, has_leaf;
 };
@@ -351,117 +351,29 @@ GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int m
     T.done = T.ref < 0;
 }
 
-// FP64 t of a candidate: its triangle against its instance's object-space ray (recomputed
-// with the same FP32 operations as during traversal when it is not the instance in hand).
-GK_D double exact_t_of(f3 o, f3 d, Shear sh, bool same_space, uint32_t inst, uint32_t tri, f3 wo, f3 wd,
-                       const DevInst* insts, const float4* tris) {
-    if (!same_space) {
-        const DevInst* ip = insts + inst;
+// FP64 t of the current best candidate: its triangle against its instance's
+// object-space ray (recomputed with the same FP32 operations as during traversal).
+GK_D double exact_t_of(const Trav& T, const SceneView& S, Shear sh) {
+    f3 o = T.o, d = T.d;
+    if (!T.inblas || T.inst != T.cur) {
+        const DevInst* ip = S.inst + T.inst;
         float w[12];
 #pragma unroll
         for (int k = 0; k < 12; ++k) w[k] = __ldg(&ip->winv[k]);
-        o = xpoint(w, wo);
-        d = xvector(w, wd);
+        o = xpoint(w, T.wo);
+        d = xvector(w, T.wd);
         sh = make_shear(d);
     }
-    const f3 v0 = tri_v(tris, tri, 0), v1 = tri_v(tris, tri, 1), v2 = tri_v(tris, tri, 2);
+    const f3 v0 = tri_v(S.tris, T.tri, 0), v1 = tri_v(S.tris, T.tri, 1), v2 = tri_v(S.tris, T.tri, 2);
     return exact_test(o, d, sh, v0, v1, v2).t;
-}
-
-// The incumbent closest hit of a ray, as the leaf test sees it.
-struct LeafBest {
-    double td;            // FP64 t, valid when exact
-    float lo, hi;         // certified interval of t
-    uint32_t inst, prim, tri;
-    bool hit, exact;
-};
-
-// Verdict on a candidate that the FP32 fast path of trav_leaf did not decide.
-struct LeafSlow {
-    double td, best_td;   // the candidate's FP64 t (when exact); the incumbent's after the call
-    float lo, hi;         // the candidate's interval
-    uint32_t fallbacks, retraces;
-    int verdict;          // 0 reject, 1 the new closest hit, 2 an any-hit found
-    bool exact, best_exact;
-};
-
-// The rare cases of the leaf test, out of line so that the traversal kernels' hot loop holds
-// only the FP32 path: an undecided edge test or grazing plane (FP64 test), t within its
-// bound of tmin or tmax (FP64 t), and overlapping intervals of the candidate and the
-// incumbent (both decided in FP64, the key (t, instance, primitive) compared exactly).
-static __device__ __noinline__ LeafSlow leaf_slow(f3 o, f3 d, Shear sh, f3 v0, f3 v1, f3 v2, Fp32Hit f, float tmin,
-                                                  float tmax, int mode, uint32_t cur, uint32_t prim, LeafBest b,
-                                                  bool inblas, f3 wo, f3 wd, const DevInst* insts,
-                                                  const float4* tris) {
-    LeafSlow r;
-    r.td = 0.0; r.best_td = b.td; r.lo = 0.0f; r.hi = 0.0f; r.fallbacks = 0u; r.retraces = 0u;
-    r.verdict = 0; r.exact = false; r.best_exact = b.exact;
-    const double tmind = (double)tmin, tmaxd = (double)tmax;
-    float t, e;
-    double td = 0.0;
-    bool have_td = false;
-    if (!(f.kind == 1 && plane_interval(o, d, v0, v1, v2, f.e, t, e))) {
-        const ExactHit x = exact_test(o, d, sh, v0, v1, v2);
-        ++r.fallbacks;
-        if (!x.hit) return r;
-        td = x.t; have_td = true;
-        t = (float)x.t;
-        e = 2.384185791e-07f * fabsf(t);   // 4u |t|
-    }
-    if (t + e < tmin || t - e > tmax) return r;
-    if (t - e < tmin || t + e > tmax) {
-        if (!have_td) {
-            const ExactHit x = exact_test(o, d, sh, v0, v1, v2);
-            ++r.fallbacks;
-            td = x.t; have_td = true;
-            t = (float)x.t;
-            e = 2.384185791e-07f * fabsf(t);
-        }
-        if (!(td >= tmind && td <= tmaxd)) return r;
-    }
-    if (mode == kAny) { r.verdict = 2; return r; }
-    const float lo = t - e, hi = t + e;
-    if (b.hit) {
-        if (have_td && b.exact) {
-            // both FP64: compare the key (t, instance, primitive) exactly
-            const bool closer = td < b.td || (td == b.td && (cur < b.inst || (cur == b.inst && prim < b.prim)));
-            if (!closer) return r;
-        } else {
-            if (lo > b.hi) return r;
-            if (!(hi < b.lo)) {
-                // intervals overlap: decide both in FP64 and compare the key exactly
-                ++r.retraces;
-                if (!have_td) {
-                    const ExactHit x = exact_test(o, d, sh, v0, v1, v2);
-                    ++r.fallbacks;
-                    td = x.t; have_td = true;
-                    t = (float)x.t;
-                    e = 2.384185791e-07f * fabsf(t);
-                }
-                if (!b.exact) {
-                    r.best_td = exact_t_of(o, d, sh, inblas && b.inst == cur, b.inst, b.tri, wo, wd, insts, tris);
-                    r.best_exact = true;
-                    ++r.fallbacks;
-                }
-                const bool closer = td < r.best_td ||
-                                    (td == r.best_td && (cur < b.inst || (cur == b.inst && prim < b.prim)));
-                if (!closer) return r;
-            }
-        }
-    }
-    r.verdict = 1;
-    r.lo = t - e; r.hi = t + e;
-    r.td = td; r.exact = have_td;
-    return r;
 }
 
 // Test the triangles of one leaf against the current best. Returns true when the ray is
 // finished early (any-hit found). kRayTmin: the ray's own tmin, else the constant EPS.
-// Inline: the FP32 test and, when its interval is certain, the decision against the
-// incumbent; everything else goes to leaf_slow with the same outcome.
 template <bool kRayTmin = false>
 GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, Counters& cn) {
     const float tmin = kRayTmin ? T.tmin : kTmin;
+    const double tmind = (double)tmin, tmaxd = (double)T.tmax;
     const Shear sh = make_shear(T.d);
     for (uint32_t k = 0; k < cnt; ++k) {
         const uint32_t ti = first + k;
@@ -470,39 +382,82 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
         ++cn.tris;
         const Fp32Hit f = fp32_test(T.o, sh, v0, v1, v2);
         if (f.kind == 0) continue;
-        float t, e;
-        if (f.kind == 1 && plane_interval(T.o, T.d, v0, v1, v2, f.e, t, e) && t - e >= tmin && t + e <= T.tmax) {
-            if (T.mode == kAny) {
+        if (T.mode == kExact) {
+            const ExactHit x = exact_test(T.o, T.d, sh, v0, v1, v2);
+            ++cn.fallbacks;
+            if (!x.hit || !(x.t >= tmind && x.t <= tmaxd)) continue;
+            const bool better = !T.hit || x.t < T.best_td ||
+                                (x.t == T.best_td && (T.cur < T.inst || (T.cur == T.inst && prim < T.prim)));
+            if (better) {
                 T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
-                return true;
+                T.best_td = x.t;
+                T.tcull = (float)x.t * 1.000001f;
             }
-            const float lo = t - e, hi = t + e;
-            if (T.hit && lo > T.best_hi) continue;   // certainly farther than the incumbent
-            if (!T.hit || hi < T.best_lo) {            // certainly closer
-                T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
-                T.best_lo = lo; T.best_hi = hi;
-                T.best_exact = false;
-                T.best_td = 0.0;
-                T.tcull = hi * 1.000001f;
-                continue;
+            continue;
+        }
+        float t, e;
+        double td = 0.0;
+        bool have_td = false;
+        if (f.kind == 1 && plane_interval(T.o, T.d, v0, v1, v2, f.e, t, e)) {
+            // certified interval from the plane equation
+        } else {
+            const ExactHit x = exact_test(T.o, T.d, sh, v0, v1, v2);
+            ++cn.fallbacks;
+            if (!x.hit) continue;
+            td = x.t; have_td = true;
+            t = (float)x.t;
+            e = 2.384185791e-07f * fabsf(t);   // 4u |t|
+        }
+        if (t + e < tmin || t - e > T.tmax) continue;
+        if (t - e < tmin || t + e > T.tmax) {
+            if (!have_td) {
+                const ExactHit x = exact_test(T.o, T.d, sh, v0, v1, v2);
+                ++cn.fallbacks;
+                td = x.t; have_td = true;
+                t = (float)x.t;
+                e = 2.384185791e-07f * fabsf(t);
+            }
+            if (!(td >= tmind && td <= tmaxd)) continue;
+        }
+        if (T.mode == kAny) {
+            T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
+            return true;
+        }
+        const float lo = t - e, hi = t + e;
+        if (T.hit) {
+            if (have_td && T.best_exact) {
+                // both FP64: compare the key (t, instance, primitive) exactly
+                const bool closer = td < T.best_td ||
+                                    (td == T.best_td && (T.cur < T.inst || (T.cur == T.inst && prim < T.prim)));
+                if (!closer) continue;
+            } else {
+                if (lo > T.best_hi) continue;
+                if (!(hi < T.best_lo)) {
+                    // intervals overlap: decide both in FP64 and compare the key exactly
+                    ++cn.retraces;
+                    if (!have_td) {
+                        const ExactHit x = exact_test(T.o, T.d, sh, v0, v1, v2);
+                        ++cn.fallbacks;
+                        td = x.t; have_td = true;
+                        t = (float)x.t;
+                        e = 2.384185791e-07f * fabsf(t);
+                    }
+                    if (!T.best_exact) {
+                        T.best_td = exact_t_of(T, S, sh);
+                        T.best_exact = true;
+                        ++cn.fallbacks;
+                    }
+                    const bool closer = td < T.best_td ||
+                                        (td == T.best_td && (T.cur < T.inst || (T.cur == T.inst && prim < T.prim)));
+                    if (!closer) continue;
+                }
             }
         }
-        LeafBest b;
-        b.td = T.best_td; b.lo = T.best_lo; b.hi = T.best_hi; b.inst = T.inst; b.prim = T.prim; b.tri = T.tri;
-        b.hit = T.hit; b.exact = T.best_exact;
-        const LeafSlow r = leaf_slow(T.o, T.d, sh, v0, v1, v2, f, tmin, T.tmax, T.mode, T.cur, prim, b, T.inblas,
-                                     T.wo, T.wd, S.inst, S.tris);
-        cn.fallbacks += r.fallbacks;
-        cn.retraces += r.retraces;
-        T.best_td = r.best_td;
-        T.best_exact = r.best_exact;
-        if (r.verdict == 0) continue;
         T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
-        if (r.verdict == 2) return true;
-        T.best_lo = r.lo; T.best_hi = r.hi;
-        T.best_exact = r.exact;
-        T.best_td = r.td;
-        T.tcull = r.hi * 1.000001f;
+        T.best_lo = lo; T.best_hi = hi;
+        T.best_exact = have_td;
+        T.best_td = td;
+        T.tcull = hi * 1.000001f;
     }
     return false;
 }
