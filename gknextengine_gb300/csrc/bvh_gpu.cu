@@ -493,9 +493,12 @@ __global__ void k_emit(const BigTask* tasks, uint32_t ntask, const Split* split,
 // rules (triangle ranges of up to 2 are leaves, up to max_leaf when the SAH prefers a leaf;
 // instance leaves hold one instance). info[0] += nodes used, info[1] = max depth, info[2]
 // error bits.
-__device__ void small_subtree(const Geo& g, uint32_t* idx, const SmallTask& S, BvhNode* nodes, float* root_box,
-                              uint32_t max_leaf, int inst_leaf, const uint32_t* prim_map, uint32_t node_base,
-                              uint32_t* info) {
+__global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, BvhNode* nodes, float* root_box,
+                        uint32_t max_leaf, int inst_leaf, const uint32_t* prim_map, uint32_t node_base,
+                        uint32_t* info) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns) return;
+    const SmallTask S = st[i];
     struct Item {
         uint32_t b, e;
         int parent, side, depth;
@@ -609,14 +612,6 @@ __device__ void small_subtree(const Geo& g, uint32_t* idx, const SmallTask& S, B
     atomicMax(&info[1], (uint32_t)maxd);
 }
 
-__global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, BvhNode* nodes, float* root_box,
-                        uint32_t max_leaf, int inst_leaf, const uint32_t* prim_map, uint32_t node_base,
-                        uint32_t* info) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ns) return;
-    small_subtree(g, idx, st[i], nodes, root_box, max_leaf, inst_leaf, prim_map, node_base, info);
-}
-
 // ---------------------------------------------------------------------------------------------
 // collapse into compressed 8-wide nodes (WideNode, gk_trace.cuh)
 //
@@ -723,11 +718,13 @@ __global__ void k_wide_count(const BvhNode* bin, const int4* items, uint32_t n, 
     cnt[i] = c;   // 0 for a malformed node: k_wide_emit reports it
 }
 
-// One wide node: item it (binary node, wide index, depth) expanded and written; its interior
-// children become items next[off + r] with wide indices next_base + off + r.
-// lk (optional): refit links of the trees being collapsed.
-__device__ void wide_emit_one(const BvhNode* bin, int4 it, uint32_t off, uint32_t next_base, WideNode* out,
-                              int4* next, uint32_t* err, const RefitLinks* lk) {
+// links (optional, links.parent null for none): refit links of the trees being collapsed
+__global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, const uint32_t* off, uint32_t next_base,
+                            WideNode* out, int4* next, uint32_t* err, RefitLinks links) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 it = items[i];
+    const RefitLinks* lk = links.parent ? &links : nullptr;
     WEnt e[8];
     int m = wide_expand(bin, it.x, e, lk);
     if (m < 0) {
@@ -761,8 +758,8 @@ __device__ void wide_emit_one(const BvhNode* bin, int4 it, uint32_t off, uint32_
     uint32_t rank = 0;
     for (int j = 0; j < m; ++j) {   // interior children are still counted: the scan expects them
         if (e[j].ref >= 0) {
-            const uint32_t wi = next_base + off + rank;
-            next[off + rank] = make_int4(e[j].ref, (int)wi, it.z + 1, 0);
+            const uint32_t wi = next_base + off[i] + rank;
+            next[off[i] + rank] = make_int4(e[j].ref, (int)wi, it.z + 1, 0);
             ref[j] = (int)wi;
             ++rank;
         } else {
@@ -775,14 +772,6 @@ __device__ void wide_emit_one(const BvhNode* bin, int4 it, uint32_t off, uint32_
     w.ref[0] = make_int4(ref[0], ref[1], ref[2], ref[3]);
     w.ref[1] = make_int4(ref[4], ref[5], ref[6], ref[7]);
     out[it.y] = w;
-}
-
-// links (optional, links.parent null for none): refit links of the trees being collapsed
-__global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, const uint32_t* off, uint32_t next_base,
-                            WideNode* out, int4* next, uint32_t* err, RefitLinks links) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    wide_emit_one(bin, items[i], off[i], next_base, out, next, err, links.parent ? &links : nullptr);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -866,422 +855,6 @@ __global__ void __launch_bounds__(128) k_refit_wide(RefitLinks lk, const BvhNode
     WideNode& w = wide[lk.wbase + j];
     w.h = make_float4(origin[0], origin[1], origin[2], __uint_as_float(meta));
     for (int ax = 0; ax < 3; ++ax) w.q[ax] = make_uint4(qw[ax][0], qw[ax][1], qw[ax][2], qw[ax][3]);
-}
-
-// ---------------------------------------------------------------------------------------------
-// the instance level in one thread block
-//
-// The instance level is rebuilt whenever instances move (every frame of an animated scene), and
-// the round-by-round build above waits for a host readback after every round. For up to kOneMax
-// instances one block of kOneT threads builds the whole tree instead, with the same split rule,
-// level by level:
-//   * tasks of more than kWarpTask instances: the whole block (bounds, per-warp bins in shared
-//     memory merged after, the SAH per axis on three threads, a stable partition by block-wide
-//     ballots);
-//   * tasks of kSmall + 1 .. kWarpTask instances: one warp each (warp reductions, bins in the
-//     warp's shared memory, a stable partition by ballots);
-//   * tasks of up to kSmall instances: one thread each, the sequential builder of k_small.
-// Node slots follow from the task alone: a subtree of m instances (one per leaf) has exactly
-// m - 1 interior nodes, numbered in preorder, so a task's node sits at its slot, its left
-// child's at slot + 1 and its right child's at slot + (left count). The layout is therefore
-// the same whichever warp takes which task, and the node array is sized before the build.
-// The splits are those of the round-by-round build, so the tree is the same.
-// A second one-block kernel collapses the tree into 8-wide nodes level by level, numbering the
-// wide nodes as gpu_bvh_collapse does.
-
-constexpr int kOneT = 512;   // 128 registers a thread: the sequential subtree builds keep their state
-constexpr int kOneWarps = kOneT / 32;
-constexpr uint32_t kWarpTask = 2048;
-constexpr uint32_t kOneMax = 1u << 16;
-constexpr int kOneLevels = 64;
-
-struct LTask {
-    uint32_t begin, end;
-    int parent, side, depth;   // parent: relative node index, -1 for the root
-    int node;                  // this task's node slot (relative)
-};
-
-struct AxisBest {
-    float cost;
-    int bin;
-    uint32_t left;
-};
-
-struct OneShared {
-    int bins[kBinWords];                 // the block task's bins
-    int wbins[kOneWarps][kBinWords];     // one set per warp
-    float red[kOneWarps][12];
-    uint32_t cnt[kOneWarps];
-    AxisBest ab[3];
-    uint32_t ntask, nnext, cursor;
-};
-
-__device__ __forceinline__ void bins_clear(int* sb, int t, int nt) {
-    const int pinf = f2o(INFINITY), ninf = f2o(-INFINITY);
-    for (int i = t; i < kBinWords; i += nt) {
-        const int q = i % 7;
-        sb[i] = q == 6 ? 0 : (q < 3 ? pinf : ninf);
-    }
-}
-
-__device__ __forceinline__ void bins_add(int* sb, const Geo& g, uint32_t p, const float* clo, const float* scale) {
-    int b6[6];
-    for (int j = 0; j < 6; ++j) b6[j] = f2o(g.box[6 * (size_t)p + j]);
-    for (int k = 0; k < 3; ++k) {
-        int* q = &sb[(k * kBins + bin_of(g.cent[3 * (size_t)p + k], clo[k], scale[k])) * 7];
-        for (int j = 0; j < 3; ++j) {
-            atomicMin(&q[j], b6[j]);
-            atomicMax(&q[3 + j], b6[3 + j]);
-        }
-        atomicAdd(&q[6], 1);
-    }
-}
-
-// Box and centroid bounds (lo xyz, hi xyz, centroid lo xyz, centroid hi xyz) over
-// idx[b + first], idx[b + first + stride], ... below e.
-__device__ __forceinline__ void range_bounds(const Geo& g, const uint32_t* idx, uint32_t b, uint32_t e,
-                                             uint32_t first, uint32_t stride, float* v) {
-    for (int k = 0; k < 3; ++k) {
-        v[k] = INFINITY; v[3 + k] = -INFINITY; v[6 + k] = INFINITY; v[9 + k] = -INFINITY;
-    }
-    for (uint32_t i = b + first; i < e; i += stride) {
-        const uint32_t p = idx[i];
-        for (int k = 0; k < 3; ++k) {
-            v[k] = fminf(v[k], g.box[6 * (size_t)p + k]);
-            v[3 + k] = fmaxf(v[3 + k], g.box[6 * (size_t)p + 3 + k]);
-            const float c = g.cent[3 * (size_t)p + k];
-            v[6 + k] = fminf(v[6 + k], c);
-            v[9 + k] = fmaxf(v[9 + k], c);
-        }
-    }
-}
-
-__device__ __forceinline__ void warp_bounds(float* v) {
-    for (int k = 0; k < 12; ++k)
-        for (int o = 16; o > 0; o >>= 1) {
-            const float u = __shfl_xor_sync(0xFFFFFFFFu, v[k], o);
-            v[k] = (k % 6) < 3 ? fminf(v[k], u) : fmaxf(v[k], u);
-        }
-}
-
-// Per-axis bin origin and scale from the centroid bounds (axis_scale's rule).
-__device__ __forceinline__ void bin_scales(const float* v, float* clo, float* scale) {
-    for (int k = 0; k < 3; ++k) {
-        clo[k] = v[6 + k];
-        const float ext = v[9 + k] - clo[k];
-        scale[k] = ext > 0.0f ? (float)kBins / ext : 0.0f;
-    }
-}
-
-// Best SAH candidate of one axis from its bins (cost INFINITY: none).
-__device__ AxisBest axis_best(const int* sb, int k, float scale) {
-    AxisBest r;
-    r.cost = INFINITY; r.bin = 0; r.left = 0;
-    if (!(scale > 0.0f)) return r;
-    float bb[kBins][6];
-    uint32_t bc[kBins];
-    for (int i = 0; i < kBins; ++i) {
-        const int* q = &sb[(k * kBins + i) * 7];
-        for (int j = 0; j < 6; ++j) bb[i][j] = o2f(q[j]);
-        bc[i] = (uint32_t)q[6];
-    }
-    int ax = -1;
-    sah_axis(bb, bc, k, &r.cost, &ax, &r.bin, &r.left);
-    if (ax < 0) r.cost = INFINITY;
-    return r;
-}
-
-// The split of a task of m primitives: the axes in order, each replacing the best only when
-// strictly cheaper (k_split's sweep); the median of the range when no axis has a candidate.
-__device__ Split combine_axes(const AxisBest* a, const float* clo, const float* scale, uint32_t m) {
-    Split sp;
-    sp.axis = -1; sp.bin = 0; sp.nleft = m / 2u; sp.clo = 0.0f; sp.scale = 0.0f;
-    float best = INFINITY;
-    for (int k = 0; k < 3; ++k)
-        if (a[k].cost < best) {
-            best = a[k].cost; sp.axis = k; sp.bin = a[k].bin; sp.nleft = a[k].left;
-        }
-    if (sp.axis >= 0) { sp.clo = clo[sp.axis]; sp.scale = scale[sp.axis]; }
-    return sp;
-}
-
-// A task split by the whole block (every thread calls it with the same task).
-__device__ void one_block_task(const LTask& T, const Geo& g, uint32_t* idx, uint32_t* tmp, BvhNode* nodes,
-                               float* root_box, uint32_t node_base, LTask* next, OneShared& S, uint32_t* info) {
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t m = T.end - T.begin;
-    float v[12];
-    range_bounds(g, idx, T.begin, T.end, (uint32_t)t, kOneT, v);
-    warp_bounds(v);
-    if (lane == 0)
-        for (int k = 0; k < 12; ++k) S.red[warp][k] = v[k];
-    bins_clear(S.wbins[warp], lane, 32);   // each warp bins into its own copy (less contention)
-    __syncthreads();
-    for (int k = 0; k < 12; ++k) {   // every thread combines the warps in the same order
-        float a = S.red[0][k];
-        for (int w = 1; w < kOneWarps; ++w) a = (k % 6) < 3 ? fminf(a, S.red[w][k]) : fmaxf(a, S.red[w][k]);
-        v[k] = a;
-    }
-    float clo[3], scale[3];
-    bin_scales(v, clo, scale);
-    if (t == 0) {
-        write_child(nodes, root_box, T.parent, T.side, v, (int)node_base + T.node);
-        atomicAdd(&info[0], 1u);
-    }
-    for (uint32_t i = T.begin + (uint32_t)t; i < T.end; i += kOneT) bins_add(S.wbins[warp], g, idx[i], clo, scale);
-    __syncthreads();
-    for (int i = t; i < kBinWords; i += kOneT) {   // merge the warps' copies
-        const int q = i % 7;
-        int a = S.wbins[0][i];
-        for (int w = 1; w < kOneWarps; ++w) {
-            const int b = S.wbins[w][i];
-            a = q == 6 ? a + b : (q < 3 ? min(a, b) : max(a, b));
-        }
-        S.bins[i] = a;
-    }
-    __syncthreads();
-    if (t < 3) S.ab[t] = axis_best(S.bins, t, scale[t]);
-    __syncthreads();
-    const Split sp = combine_axes(S.ab, clo, scale, m);
-    if (sp.axis >= 0) {   // stable partition: left in order, then right in order
-        uint32_t lbase = 0, rbase = 0;
-        for (uint32_t c = T.begin; c < T.end; c += kOneT) {
-            const uint32_t i = c + (uint32_t)t;
-            const bool in = i < T.end;
-            const uint32_t p = in ? idx[i] : 0u;
-            const bool left = in && bin_of(g.cent[3 * (size_t)p + sp.axis], sp.clo, sp.scale) < sp.bin;
-            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, left);
-            if (lane == 0) S.cnt[warp] = __popc(bal);
-            __syncthreads();
-            uint32_t before = 0, total = 0;
-            for (int w = 0; w < kOneWarps; ++w) {
-                const uint32_t cw = S.cnt[w];
-                before += w < warp ? cw : 0u;
-                total += cw;
-            }
-            const uint32_t lpos = before + __popc(bal & ((1u << lane) - 1u));
-            if (in) {
-                if (left) tmp[T.begin + lbase + lpos] = p;
-                else if (sp.nleft + rbase + (i - c - lpos) < m) tmp[T.begin + sp.nleft + rbase + (i - c - lpos)] = p;
-            }
-            lbase += total;
-            rbase += min((uint32_t)kOneT, T.end - c) - total;
-            __syncthreads();
-        }
-        if (lbase != sp.nleft) {
-            if (t == 0) atomicOr(&info[2], kBuildErrRange);
-        } else {
-            for (uint32_t i = T.begin + (uint32_t)t; i < T.end; i += kOneT) idx[i] = tmp[i];
-        }
-    }
-    if (t == 0) {
-        const uint32_t at = atomicAdd(&S.nnext, 2u);
-        next[at] = LTask{T.begin, T.begin + sp.nleft, T.node, 0, T.depth + 1, T.node + 1};
-        next[at + 1] = LTask{T.begin + sp.nleft, T.end, T.node, 1, T.depth + 1, T.node + (int)sp.nleft};
-    }
-    __syncthreads();
-}
-
-// A task split by one warp (every lane calls it with the same task).
-__device__ void one_warp_task(const LTask& T, const Geo& g, uint32_t* idx, uint32_t* tmp, BvhNode* nodes,
-                              float* root_box, uint32_t node_base, LTask* next, int* wb, OneShared& S,
-                              uint32_t* info) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t m = T.end - T.begin;
-    float v[12];
-    range_bounds(g, idx, T.begin, T.end, (uint32_t)lane, 32u, v);
-    warp_bounds(v);
-    float clo[3], scale[3];
-    bin_scales(v, clo, scale);
-    if (lane == 0) {
-        write_child(nodes, root_box, T.parent, T.side, v, (int)node_base + T.node);
-        atomicAdd(&info[0], 1u);
-    }
-    bins_clear(wb, lane, 32);
-    __syncwarp();
-    for (uint32_t i = T.begin + (uint32_t)lane; i < T.end; i += 32u) bins_add(wb, g, idx[i], clo, scale);
-    __syncwarp();
-    AxisBest mine;
-    mine.cost = INFINITY; mine.bin = 0; mine.left = 0;
-    if (lane < 3) mine = axis_best(wb, lane, scale[lane]);
-    AxisBest ab[3];
-    for (int k = 0; k < 3; ++k) {
-        ab[k].cost = __shfl_sync(0xFFFFFFFFu, mine.cost, k);
-        ab[k].bin = __shfl_sync(0xFFFFFFFFu, mine.bin, k);
-        ab[k].left = __shfl_sync(0xFFFFFFFFu, mine.left, k);
-    }
-    const Split sp = combine_axes(ab, clo, scale, m);
-    if (sp.axis >= 0) {   // stable partition: left in order, then right in order
-        uint32_t lbase = 0, rbase = 0;
-        for (uint32_t c = T.begin; c < T.end; c += 32u) {
-            const uint32_t i = c + (uint32_t)lane;
-            const bool in = i < T.end;
-            const uint32_t p = in ? idx[i] : 0u;
-            const bool left = in && bin_of(g.cent[3 * (size_t)p + sp.axis], sp.clo, sp.scale) < sp.bin;
-            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, left);
-            const uint32_t lpos = __popc(bal & ((1u << lane) - 1u));
-            if (in) {
-                if (left) tmp[T.begin + lbase + lpos] = p;
-                else if (sp.nleft + rbase + ((uint32_t)lane - lpos) < m)
-                    tmp[T.begin + sp.nleft + rbase + ((uint32_t)lane - lpos)] = p;
-            }
-            const uint32_t tot = __popc(bal);
-            lbase += tot;
-            rbase += min(32u, T.end - c) - tot;
-        }
-        __syncwarp();
-        if (lbase != sp.nleft) {
-            if (lane == 0) atomicOr(&info[2], kBuildErrRange);
-        } else {
-            for (uint32_t i = T.begin + (uint32_t)lane; i < T.end; i += 32u) idx[i] = tmp[i];
-        }
-        __syncwarp();
-    }
-    if (lane == 0) {
-        const uint32_t at = atomicAdd(&S.nnext, 2u);
-        next[at] = LTask{T.begin, T.begin + sp.nleft, T.node, 0, T.depth + 1, T.node + 1};
-        next[at + 1] = LTask{T.begin + sp.nleft, T.end, T.node, 1, T.depth + 1, T.node + (int)sp.nleft};
-    }
-    __syncwarp();
-}
-
-// The whole instance-level tree over the n primitives of g (one instance per leaf, payload
-// prim_map[primitive]) into nodes[0, max(n - 1, 1)), refs node_base + slot; the root's box into
-// root_box. q0, q1: n tasks each. info: [0] interior nodes, [1] depth, [2] error bits.
-__global__ void __launch_bounds__(kOneT, 1) k_build_one_block(Geo g, uint32_t* idx, uint32_t* tmp, uint32_t n,
-                                                             LTask* q0, LTask* q1, BvhNode* nodes, float* root_box,
-                                                             const uint32_t* prim_map, uint32_t node_base,
-                                                             uint32_t* info) {
-    __shared__ OneShared S;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    for (uint32_t i = (uint32_t)t; i < n; i += kOneT) idx[i] = i;
-    if (t == 0) {
-        S.ntask = n ? 1u : 0u;
-        S.nnext = 0u;
-        S.cursor = 0u;
-        if (n) q0[0] = LTask{0u, n, -1, 0, 0, 0};
-    }
-    __syncthreads();
-    LTask* cur = q0;
-    LTask* nxt = q1;
-    int level = 0;
-    for (; level < kOneLevels; ++level) {
-        const uint32_t nt = S.ntask;
-        if (nt == 0u) break;
-        for (uint32_t k = 0; k < nt; ++k) {   // tasks above kWarpTask: the whole block, one at a time
-            const LTask T = cur[k];
-            if (T.end - T.begin > kWarpTask) one_block_task(T, g, idx, tmp, nodes, root_box, node_base, nxt, S, info);
-        }
-        for (;;) {                            // medium tasks: one warp each, taken in turn
-            uint32_t k = 0u;
-            if (lane == 0) k = atomicAdd(&S.cursor, 1u);
-            k = __shfl_sync(0xFFFFFFFFu, k, 0);
-            if (k >= nt) break;
-            const LTask T = cur[k];
-            const uint32_t m = T.end - T.begin;
-            if (m > kSmall && m <= kWarpTask)
-                one_warp_task(T, g, idx, tmp, nodes, root_box, node_base, nxt, S.wbins[warp], S, info);
-        }
-        for (uint32_t k = (uint32_t)t; k < nt; k += kOneT) {   // small tasks: one thread each
-            const LTask T = cur[k];
-            if (T.end - T.begin > kSmall) continue;
-            SmallTask st;
-            st.parent = T.parent;
-            st.side = T.side;
-            st.depth = T.depth;
-            st.root_node = T.parent < 0 ? T.node : -1;
-            st.begin = T.begin;
-            st.end = T.end;
-            st.res0 = (uint32_t)(T.parent < 0 ? T.node + 1 : T.node);
-            st.pad = 0u;
-            small_subtree(g, idx, st, nodes, root_box, 1u, 1, prim_map, node_base, info);
-        }
-        __syncthreads();
-        if (t == 0) {
-            S.ntask = S.nnext;
-            S.nnext = 0u;
-            S.cursor = 0u;
-        }
-        LTask* sw = cur;
-        cur = nxt;
-        nxt = sw;
-        __syncthreads();
-    }
-    if (t == 0 && S.ntask != 0u) atomicOr(&info[2], kBuildErrStack);   // deeper than kOneLevels levels
-}
-
-// The tree of k_build_one_block (root: absolute node index, -1 for none) collapsed into wide
-// nodes from wide_base (wide nodes below wide_cap exist), as gpu_bvh_collapse numbers them.
-// q0, q1: one item per wide node. res: [0] wide nodes written, [1] levels, [2] error bits.
-__global__ void __launch_bounds__(kOneT, 1) k_collapse_one_block(const BvhNode* bin, int root, uint32_t wide_base,
-                                                                uint32_t wide_cap, WideNode* out, int4* q0, int4* q1,
-                                                                RefitLinks links, uint32_t* res) {
-    __shared__ uint32_t cnt[kOneWarps];
-    __shared__ uint32_t s_n, s_next;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const RefitLinks* lk = links.parent ? &links : nullptr;
-    if (t == 0) {
-        s_n = (root >= 0 && wide_base < wide_cap) ? 1u : 0u;
-        s_next = wide_base + s_n;
-        if (s_n) q0[0] = make_int4(root, (int)wide_base, 1, 0);
-        if (root >= 0 && !s_n) atomicOr(&res[2], kBuildErrRange);
-    }
-    __syncthreads();
-    int4* cur = q0;
-    int4* nxt = q1;
-    uint32_t levels = 0;
-    while (s_n > 0u) {
-        const uint32_t n = s_n, base_next = s_next;
-        if (++levels > (uint32_t)kOneLevels) {
-            if (t == 0) atomicOr(&res[2], kBuildErrRange);
-            break;
-        }
-        uint32_t run = 0;   // wide nodes given to earlier chunks of this level (the same in every thread)
-        for (uint32_t c = 0; c < n; c += kOneT) {
-            const uint32_t i = c + (uint32_t)t;
-            uint32_t ci = 0;
-            int4 it = make_int4(0, 0, 0, 0);
-            if (i < n) {
-                it = cur[i];
-                WEnt e[8];
-                const int m = wide_expand(bin, it.x, e);
-                for (int j = 0; j < m; ++j) ci += e[j].ref >= 0 ? 1u : 0u;
-            }
-            // exclusive prefix of ci over the block: lanes by shuffles, warps by shared counts
-            uint32_t incl = ci;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= o) incl += u;
-            }
-            if (lane == 31) cnt[warp] = incl;
-            __syncthreads();
-            uint32_t before = 0, total = 0;
-            for (int w = 0; w < kOneWarps; ++w) {
-                const uint32_t cw = cnt[w];
-                before += w < warp ? cw : 0u;
-                total += cw;
-            }
-            if (i < n) wide_emit_one(bin, it, run + before + incl - ci, base_next, out, nxt, &res[2], lk);
-            run += total;
-            __syncthreads();
-        }
-        if (t == 0) {
-            s_n = run;
-            s_next = base_next + run;
-            if ((size_t)base_next + run > wide_cap) {   // the next level would write past the array
-                atomicOr(&res[2], kBuildErrRange);
-                s_n = 0u;
-            }
-        }
-        int4* sw = cur;
-        cur = nxt;
-        nxt = sw;
-        __syncthreads();
-    }
-    if (t == 0) {
-        res[0] = s_next - wide_base;
-        res[1] = levels;
-    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1400,8 +973,6 @@ struct GpuBvh {
     DBuf<GpuInstBox> inst;
     DBuf<int4> witems[2];
     DBuf<uint32_t> wcnt, woff, werr;
-    DBuf<LTask> lq[2];
-    uint32_t* result_host = nullptr;   // page-locked result words of the one-block instance level
     uint32_t launches = 0;   // kernels launched by all builds so far
 
     ~GpuBvh() {
@@ -1413,8 +984,6 @@ struct GpuBvh {
         cc.release(); cc_scan.release(); bsum4.release(); tot4.release(); bins.release(); tb.release();
         split.release(); small.release(); nodes.release(); ranges.release(); inst.release();
         witems[0].release(); witems[1].release(); wcnt.release(); woff.release(); werr.release();
-        lq[0].release(); lq[1].release();
-        if (result_host) cudaFreeHost(result_host);
     }
 
     template <class T>
@@ -1676,57 +1245,6 @@ cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint
     const std::vector<uint32_t> rb(1, 0u), re(1, n);
     GK_TRY(B->build(n, rb, re, 1, true, B->map.p, node_base, out, st));
     return cudaStreamSynchronize(st);
-}
-
-bool gpu_bvh_instance_level_fits(uint32_t n) { return n <= kOneMax; }
-
-cudaError_t gpu_bvh_instance_level(GpuBvh* B, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
-                                   BvhNode* nodes, uint32_t node_base, WideNode* wide, size_t wide_cap,
-                                   uint32_t wide_base, const RefitLinks* links, GpuInstLevel* out, cudaStream_t st) {
-    *out = GpuInstLevel();
-    if (n > kOneMax || wide_cap > 0xFFFFFFFFull) return cudaErrorInvalidValue;
-    const uint32_t nc = n ? std::max<uint32_t>(n - 1u, 1u) : 0u;
-    out->node_count = nc;
-    if (n == 0) return cudaSuccess;
-    std::vector<uint32_t> map(n);
-    for (uint32_t i = 0; i < n; ++i) map[i] = inst_host[i].inst;
-    GK_TRY(B->inst.need(n));
-    GK_TRY(B->map.need(n));
-    GK_TRY(B->box.need(6 * (size_t)n));
-    GK_TRY(B->cent.need(3 * (size_t)n));
-    GK_TRY(B->idx.need(n));
-    GK_TRY(B->tmp.need(n));
-    GK_TRY(B->lq[0].need(n));
-    GK_TRY(B->lq[1].need(n));
-    GK_TRY(B->witems[0].need(nc));
-    GK_TRY(B->witems[1].need(nc));
-    GK_TRY(B->root_box.need(6));
-    GK_TRY(B->info.need(8));
-    if (!B->result_host) GK_TRY(cudaMallocHost((void**)&B->result_host, 8 * sizeof(uint32_t)));
-    GK_TRY(cudaMemcpyAsync(B->inst.p, inst_host, n * sizeof(GpuInstBox), cudaMemcpyHostToDevice, st));
-    GK_TRY(cudaMemcpyAsync(B->map.p, map.data(), n * 4ull, cudaMemcpyHostToDevice, st));
-    GK_TRY(cudaMemsetAsync(B->info.p, 0, 8 * sizeof(uint32_t), st));
-    GK_TRY(cudaMemsetAsync(nodes, 0, nc * sizeof(BvhNode), st));
-    k_inst_boxes<<<(n + 255) / 256, 256, 0, st>>>(B->inst.p, n, mesh_box, B->box.p, B->cent.p);
-    const Geo g{B->box.p, B->cent.p};
-    k_build_one_block<<<1, kOneT, 0, st>>>(g, B->idx.p, B->tmp.p, n, B->lq[0].p, B->lq[1].p, nodes, B->root_box.p,
-                                           B->map.p, node_base, B->info.p);
-    const RefitLinks lk = links ? *links : RefitLinks();
-    k_collapse_one_block<<<1, kOneT, 0, st>>>(nodes - node_base, (int)node_base, wide_base, (uint32_t)wide_cap, wide,
-                                              B->witems[0].p, B->witems[1].p, lk, B->info.p + 4);
-    B->launches += 3;
-    GK_TRY(cudaGetLastError());
-    GK_TRY(cudaMemcpyAsync(B->result_host, B->info.p, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    GK_TRY(cudaStreamSynchronize(st));   // the one host wait: depth and counts for the caller
-    const uint32_t* r = B->result_host;
-    if (r[2] || r[6]) return cudaErrorInvalidValue;
-    out->nodes_used = r[0];
-    out->depth = (int)r[1];
-    out->wide_count = r[4];
-    out->wide_depth = (int)r[5];
-    out->root = (int)node_base;
-    out->wide_root = (int)wide_base;
-    return cudaSuccess;
 }
 
 cudaError_t gpu_bvh_collapse(GpuBvh* B, const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base,

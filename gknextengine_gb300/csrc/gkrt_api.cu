@@ -578,33 +578,6 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
         if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
         // the instance tables first: their host work and uploads overlap the stream's earlier work
         if ((rc = upload_instances(ctx, st)) != GKRT_OK) return rc;
-        const uint32_t nv = (uint32_t)ib.size();
-        if (gpu_bvh_instance_level_fits(nv)) {
-            // one-block build and collapse, sized before the build: one host wait in all
-            const uint32_t nc = nv ? std::max<uint32_t>(nv - 1u, 1u) : 0u;
-            if ((rc = ensure_node_cap(ctx, (size_t)base + nc)) != GKRT_OK) return rc;
-            if ((rc = ensure_wide_cap(ctx, (size_t)ctx->blas_wide_count + nc + 1, ctx->blas_wide_count)) != GKRT_OK)
-                return rc;
-            if ((rc = prepare_refit(ctx, nc, st)) != GKRT_OK) return rc;
-            tlas_members(ctx, ctx->tlas_members);
-            GpuInstLevel L;
-            const cudaError_t e = gpu_bvh_instance_level(ctx->builder, ib.data(), nv, ctx->d_blas_box,
-                                                         ctx->d_nodes + base, base, ctx->d_wide, ctx->d_wide_cap,
-                                                         ctx->blas_wide_count, &ctx->refit, &L, st);
-            if (e == cudaErrorInvalidValue)
-                return fail(ctx, GKRT_ERR_INVALID_ARG,
-                            "instance BVH build failed (non-finite transforms or more than 64 levels)");
-            if (e != cudaSuccess) return cuda_fail(ctx, e, "gpu_bvh_instance_level");
-            ctx->tlas_root = nv ? L.root : -1;
-            ctx->tlas_nodes = L.nodes_used;
-            ctx->tlas_bin_depth = L.depth;
-            ctx->tlas_wide_root = nv ? L.wide_root : -1;
-            ctx->tlas_wide_count = L.wide_count;
-            ctx->tlas_wide_depth = L.wide_depth;
-            if ((rc = check_stack_bound(ctx)) != GKRT_OK) return rc;
-            ctx->tlas_ready = true;
-            return GKRT_OK;
-        }
         GpuBvhResult r;
         GK_CUDA(gpu_bvh_build_instances(ctx->builder, ib.data(), (uint32_t)ib.size(), ctx->d_blas_box, base, &r, st));
         if ((rc = ensure_node_cap(ctx, (size_t)base + r.node_count)) != GKRT_OK) return rc;

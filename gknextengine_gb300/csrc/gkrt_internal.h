@@ -161,21 +161,6 @@ struct RefitLinks {
     int* wsrc = nullptr;       // 8 per wide node wbase + j: the slots of its children's boxes; -1 unused
     uint32_t nbase = 0, ncap = 0, ninst = 0, wbase = 0, wcap = 0;
 };
-// The instance level of n instances (gpu_bvh_instance_level_fits(n)) built and collapsed by two
-// one-block kernels with no host round trip between levels, straight into the caller's arrays:
-// two-child nodes at nodes[0, max(n - 1, 1)) (refs node_base + slot; the root at node_base), wide
-// nodes from wide_base in wide[0, wide_cap); links (optional) as gpu_bvh_collapse records them.
-// One host synchronisation at the end, for the depth and counts.
-struct GpuInstLevel {
-    int root = -1, wide_root = -1;
-    uint32_t node_count = 0, nodes_used = 0, wide_count = 0;
-    int depth = 0, wide_depth = 0;
-};
-bool gpu_bvh_instance_level_fits(uint32_t n);
-cudaError_t gpu_bvh_instance_level(GpuBvh* b, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
-                                   BvhNode* nodes, uint32_t node_base, WideNode* wide, size_t wide_cap,
-                                   uint32_t wide_base, const RefitLinks* links, GpuInstLevel* out, cudaStream_t st);
-
 // Refit of the instance level in place: the two-child boxes of the leaves from the instances'
 // current transforms (inst: device, one record per instance index), unions up to the root, then
 // the wide nodes [wbase, wbase + nw) re-quantized. arrive: ncap counters, zero between refits.
