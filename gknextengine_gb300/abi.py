@@ -122,7 +122,7 @@ class GkrtSceneDesc(C.Structure):
         ("meshes", C.c_void_p), ("mesh_count", C.c_uint32), ("materials", C.c_void_p),
         ("material_count", C.c_uint32), ("instances", C.c_void_p), ("instance_count", C.c_uint32),
         ("lights", C.c_void_p), ("light_count", C.c_uint32), ("probe_cubes", _p(C.c_uint32)),
-        ("probe_voxels", _p(C.c_uint32)),
+        ("probe_voxels", _p(C.c_uint32)), ("texcoords", _p(C.c_float)), ("tangents", _p(C.c_float)),
     ]
 
 
@@ -141,7 +141,7 @@ class GkrtFrameConstants(C.Structure):
         ("progressive_render", C.c_uint32), ("bf_size", C.c_uint32), ("hdr", C.c_uint32),
         ("bf_sigma", C.c_float), ("bf_sigma_lum", C.c_float), ("bf_sigma_normal", C.c_float),
         ("denoiser", C.c_uint32), ("nee_mode", C.c_uint32), ("flags", C.c_uint32),
-        ("reserved", C.c_uint32 * 2),
+        ("sky_index", C.c_uint32), ("sky_rotation", C.c_float),
     ]
 
 
@@ -182,10 +182,12 @@ def fptr(a: np.ndarray, ctype=C.c_float):
 
 
 class SceneArrays:
-    """Host-side scene arrays in the exact layouts GkrtSceneDesc points at."""
+    """Host-side scene arrays in the exact layouts GkrtSceneDesc points at, plus the scene's
+    textures: {texture id: (format TEX_*, texels (h, w, 4) uint8 or float32)}."""
 
     def __init__(self, positions, normals, material_slots, indices, meshes, materials, instances,
-                 lights=None, probe_cubes=None, probe_voxels=None, name="scene"):
+                 lights=None, probe_cubes=None, probe_voxels=None, name="scene", texcoords=None, tangents=None,
+                 textures=None):
         self.positions = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 4)
         self.normals = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 4)
         self.material_slots = np.ascontiguousarray(material_slots, dtype=np.uint32).reshape(-1)
@@ -197,6 +199,9 @@ class SceneArrays:
                                            dtype=LIGHT_DTYPE)
         self.probe_cubes = None if probe_cubes is None else np.ascontiguousarray(probe_cubes, dtype=np.uint32)
         self.probe_voxels = None if probe_voxels is None else np.ascontiguousarray(probe_voxels, dtype=np.uint32)
+        self.texcoords = None if texcoords is None else np.ascontiguousarray(texcoords, dtype=np.float32).reshape(-1, 2)
+        self.tangents = None if tangents is None else np.ascontiguousarray(tangents, dtype=np.float32).reshape(-1, 4)
+        self.textures = dict(textures or {})
         self.name = name
 
     @property
@@ -223,4 +228,20 @@ class SceneArrays:
         d.light_count = self.lights.shape[0]
         d.probe_cubes = fptr(self.probe_cubes, C.c_uint32) if self.probe_cubes is not None else None
         d.probe_voxels = fptr(self.probe_voxels, C.c_uint32) if self.probe_voxels is not None else None
+        d.texcoords = fptr(self.texcoords) if self.texcoords is not None else None
+        d.tangents = fptr(self.tangents) if self.tangents is not None else None
         return d
+
+
+TEX_RGBA8_UNORM, TEX_RGBA8_SRGB, TEX_RGBA32F = 0, 1, 2
+MAX_TEXTURES = 4096
+FRAME_SKY_TEXTURE = 2
+
+
+def texel_buffer(fmt: int, texels: np.ndarray) -> np.ndarray:
+    """Texels (h, w, 4) as the contiguous buffer gkrt_texture_upload takes for `fmt`."""
+    dt = np.float32 if fmt == TEX_RGBA32F else np.uint8
+    t = np.ascontiguousarray(texels, dtype=dt)
+    if t.ndim != 3 or t.shape[2] != 4:
+        raise ValueError("texels must be (height, width, 4)")
+    return t

@@ -97,7 +97,8 @@ class Settings:
                  bf_size=5, bf_sigma=2.0, bf_sigma_lum=3.0, bf_sigma_normal=0.005, paper_white_nit=600.0,
                  has_sky=False, sky_color=(0.0, 0.0, 0.0, 1.0), sky_intensity=1.0, has_sun=False,
                  sun_direction=(0.0, 1.0, 0.0), sun_intensity=0.0, progressive=False, fast_gather=False,
-                 hdr=False, denoiser=abi.DENOISE_JBF, nee_mode=abi.NEE_REFERENCE, flags=0):
+                 hdr=False, denoiser=abi.DENOISE_JBF, nee_mode=abi.NEE_REFERENCE, flags=0, sky_texture=None,
+                 sky_rotation=0.0):
         self.__dict__.update(locals())
         del self.__dict__["self"]
 
@@ -178,6 +179,10 @@ class FrameBuilder:
         fc.denoiser = s.denoiser
         fc.nee_mode = s.nee_mode
         fc.flags = s.flags
+        if getattr(s, "sky_texture", None) is not None:   # the HDR sky (SkyIdx, SkyRotation)
+            fc.flags |= abi.FRAME_SKY_TEXTURE
+            fc.sky_index = int(s.sky_texture)
+            fc.sky_rotation = float(getattr(s, "sky_rotation", 0.0))
         self.prev_vp, self.prev_vp_unjit = vp, vp_unjit
         self.prev_total_frames = total_frames
         self.total_frames = total_frames + 1

@@ -40,6 +40,10 @@ GK_D float dot3(f3 a, f3 b) { return fmaf_(a.z, b.z, fmaf_(a.y, b.y, a.x * b.x))
 GK_D float len3(f3 a) { return sqrt_(dot3(a, a)); }
 GK_D f3 normalize3(f3 a) { float k = div_(1.0f, sqrt_(dot3(a, a))); return a * k; }
 GK_D f3 fma3(f3 v, float s, f3 o) { return F3(fmaf_(v.x, s, o.x), fmaf_(v.y, s, o.y), fmaf_(v.z, s, o.z)); }
+// cross: each component a*b - c*d with the product fused into the difference
+GK_D f3 cross3(f3 a, f3 b) {
+    return F3(fmaf_(a.y, b.z, -(a.z * b.y)), fmaf_(a.z, b.x, -(a.x * b.z)), fmaf_(a.x, b.y, -(a.y * b.x)));
+}
 GK_D f3 reflect3(f3 d, f3 n) {
     float k = 2.0f * dot3(n, d);
     return F3(fmaf_(-k, n.x, d.x), fmaf_(-k, n.y, d.y), fmaf_(-k, n.z, d.z));
@@ -120,6 +124,38 @@ GK_D void sincos2pi(float u, float& s, float& c) {
     else if (qi == 1) { s = cp; c = -sp; }
     else if (qi == 2) { s = -sp; c = -cp; }
     else { s = -cp; c = sp; }
+}
+
+// ---- atan2 and acos for the sky's equirectangular lookup (SampleIBLV2). atan on [0, 1]:
+// above tan(pi/12) the argument is reduced by atan(a) = pi/6 + atan((a sqrt3 - 1) / (a + sqrt3)),
+// then the Taylor series x - x^3/3 + ... - x^15/15 on |x| <= tan(pi/12) (truncation below
+// 2^-36), Horner with fused steps; octant fix-ups give atan2; acos(x) = atan2(sqrt((1 - x)
+// (1 + x)), x). Our own routines, so that CPU checks round the same way. ----
+GK_D float atan01(float a) {
+    const bool red = a > 0.267949194f;
+    const float x = red ? div_(fmaf_(a, 1.73205081f, -1.0f), a + 1.73205081f) : a;
+    const float x2 = x * x;
+    float p = fmaf_(x2, -6.66666701e-02f, 7.69230798e-02f);   // -1/15, 1/13
+    p = fmaf_(x2, p, -9.09090936e-02f);                        // -1/11
+    p = fmaf_(x2, p, 1.11111112e-01f);                         //  1/9
+    p = fmaf_(x2, p, -1.42857149e-01f);                        // -1/7
+    p = fmaf_(x2, p, 2.00000003e-01f);                         //  1/5
+    p = fmaf_(x2, p, -3.33333343e-01f);                        // -1/3
+    const float r = fmaf_(x * x2, p, x);
+    return red ? r + 0.523598790f : r;                         // + pi/6
+}
+GK_D float atan2_(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    if (!(ax > 0.0f) && !(ay > 0.0f)) return 0.0f;
+    const bool swap = ay > ax;
+    float r = atan01(swap ? div_(ax, ay) : div_(ay, ax));
+    if (swap) r = 1.57079637f - r;                             // pi/2 - r
+    if (x < 0.0f) r = 3.14159274f - r;                         // pi - r
+    return y < 0.0f ? -r : r;
+}
+GK_D float acos_(float x) {
+    const float s = sqrt_(mx((1.0f - x) * (1.0f + x), 0.0f));
+    return atan2_(s, x);
 }
 
 // ---- samplers (Const_Func.slang:8-49, 260-340) ----

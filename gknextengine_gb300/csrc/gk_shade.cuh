@@ -11,13 +11,19 @@
 
 namespace gk {
 
+// A texture of the pool: RGBA float texels, rows first to last; null texels: no texture.
+struct DevTex {
+    const float4* texels;
+    uint32_t w, h;
+};
+
 struct ShadeScene {
     SceneView S;
     const float4* normals;       // per vertex
     const uint32_t* slots;       // per vertex material slot
     const uint32_t* indices;
     const uint32_t* inst_mat;    // 16 per instance
-    const float* inst_prev;      // 12 per instance: combined_prev
+    const float* inst_prev;      // 24 per instance: combined_prev, then the world transform (3x4)
     const GkrtMaterial* mats;
     uint32_t nmat;
     const uint32_t* cubes;       // optional probe grid
@@ -25,6 +31,9 @@ struct ShadeScene {
     const float4* emit;          // emissive triangles, 5 float4 each (see nee_sample)
     const float2* emit_alias;    // alias table: (threshold, alias index bits) per entry
     uint32_t nemit;              // 0: no emissive-triangle NEE
+    const DevTex* tex;           // GKRT_MAX_TEXTURES entries (the texture pool)
+    const float2* uv;            // per vertex texture coordinates, or null
+    const float4* tangents;      // per vertex object-space tangent (w: handedness), or null
 };
 
 struct Vtx {
@@ -37,6 +46,7 @@ struct MatV {
     f4 diffuse;
     float fuzz, ri, metal, ri2;
     uint32_t model;
+    int dtex, mtex, ntex;   // diffuse, MRA and normal-map texture ids (-1: none)
 };
 
 GK_D MatV load_mat(const ShadeScene& sc, uint32_t i) {
@@ -45,6 +55,9 @@ GK_D MatV load_mat(const ShadeScene& sc, uint32_t i) {
     float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
     MatV m;
     m.diffuse = F4(a.x, a.y, a.z, a.w);
+    m.dtex = __float_as_int(b.x);
+    m.mtex = __float_as_int(b.y);
+    m.ntex = __float_as_int(b.z);
     m.fuzz = b.w;
     m.ri = c.x;
     m.model = __float_as_uint(c.y);
@@ -80,6 +93,130 @@ GK_D f4 sky(const GkrtFrameConstants& fc) {
     if (!fc.has_sky) return F4(0.0f, 0.0f, 0.0f, 0.0f);
     return F4(mn(10.0f, fc.sky_color[0]), mn(10.0f, fc.sky_color[1]), mn(10.0f, fc.sky_color[2]),
               mn(1.0f, fc.sky_color[3])) * fc.sky_intensity;
+}
+
+// ---- textures (the pool's sampler at level 0: Vulkan's linear filter, repeat addressing) ----
+// Texel index of the integral float f modulo n (exact: fmodf is exact).
+GK_D uint32_t wrap_repeat(float f, uint32_t n) {
+    float m = fmodf(f, (float)n);
+    if (m < 0.0f) m = m + (float)n;
+    const uint32_t i = (uint32_t)m;
+    return i < n ? i : 0u;
+}
+GK_D f4 texel(const DevTex& t, uint32_t x, uint32_t y) {
+    const float4 v = __ldg(&t.texels[(size_t)y * t.w + x]);
+    return F4(v.x, v.y, v.z, v.w);
+}
+// SampleLevel(uv, 0): x = u w - 1/2 and y = v h - 1/2 split into texel and fraction, the four
+// texels weighted in one fixed order. An id without a texture samples as opaque white.
+GK_D f4 tex_sample(const DevTex* pool, int id, float u, float v) {
+    const f4 white = F4(1.0f, 1.0f, 1.0f, 1.0f);
+    if (id < 0 || id >= (int)GKRT_MAX_TEXTURES) return white;
+    DevTex t;
+    t.texels = reinterpret_cast<const float4*>(__ldg(reinterpret_cast<const unsigned long long*>(&pool[id].texels)));
+    t.w = __ldg(&pool[id].w);
+    t.h = __ldg(&pool[id].h);
+    if (!t.texels || !t.w || !t.h) return white;
+    float x = fmaf_(u, (float)t.w, -0.5f), y = fmaf_(v, (float)t.h, -0.5f);
+    if (!(fabsf(x) < 1e30f)) x = -0.5f;   // non-finite coordinates read texel 0's neighbourhood
+    if (!(fabsf(y) < 1e30f)) y = -0.5f;
+    const float fx = floorf(x), fy = floorf(y);
+    const float a = x - fx, b = y - fy;
+    const uint32_t x0 = wrap_repeat(fx, t.w), x1 = wrap_repeat(fx + 1.0f, t.w);
+    const uint32_t y0 = wrap_repeat(fy, t.h), y1 = wrap_repeat(fy + 1.0f, t.h);
+    const float ia = 1.0f - a, ib = 1.0f - b;
+    const float w00 = ia * ib, w10 = a * ib, w01 = ia * b, w11 = a * b;
+    const f4 t00 = texel(t, x0, y0), t10 = texel(t, x1, y0), t01 = texel(t, x0, y1), t11 = texel(t, x1, y1);
+    return F4(fmaf_(t11.x, w11, fmaf_(t01.x, w01, fmaf_(t10.x, w10, t00.x * w00))),
+              fmaf_(t11.y, w11, fmaf_(t01.y, w01, fmaf_(t10.y, w10, t00.y * w00))),
+              fmaf_(t11.z, w11, fmaf_(t01.z, w01, fmaf_(t10.z, w10, t00.z * w00))),
+              fmaf_(t11.w, w11, fmaf_(t01.w, w01, fmaf_(t10.w, w10, t00.w * w00))));
+}
+
+// Radiance of a sky miss in direction dir: SampleIBLV2 (Shading.slang:194-199) with the
+// texture sky_index when the frame asks for it, else the constant colour.
+GK_D f4 sky_dir(const ShadeScene& sc, const GkrtFrameConstants& fc, f3 dir) {
+    if (!fc.has_sky || !(fc.flags & GKRT_FRAME_SKY_TEXTURE)) return sky(fc);
+    const f3 d = normalize3(dir);
+    const float u = (atan2_(d.x, d.z) + 3.14159274f * fc.sky_rotation) * 0.159154937f;   // M_1_OVER_TWO_PI
+    const float v = acos_(d.y) * 0.318309873f;                                        // M_1_PI
+    const f4 c = tex_sample(sc.tex, (int)fc.sky_index, u, v);
+    return F4(mn(10.0f, c.x), mn(10.0f, c.y), mn(10.0f, c.z), mn(1.0f, c.w)) * fc.sky_intensity;
+}
+
+// Texture coordinates and the object-space normal and tangent at a hit: the barycentric mix
+// a + (b - a) b1 + (c - a) b2 of TraceRay (Shading.slang:820) for each. The tangent's w is the
+// reference's vertex packing of the handedness, 2 when positive and 0 otherwise
+// (MakeVertex, Vertex.hpp:97; UnpackVertexV2, Const_Func.slang:356-364).
+struct HitAttr {
+    float u, v;
+    f3 ln;
+    f4 lt;
+};
+static __device__ __noinline__ HitAttr hit_attr(const ShadeScene& sc, f3 o, f3 d, uint32_t inst, uint32_t prim,
+                                                uint32_t tri) {
+    const HitShade h = hit_shade(sc.S, o, d, inst, tri);
+    const DevInst* ip = sc.S.inst + inst;
+    const uint32_t ioff = __ldg(&ip->index_offset) + 3u * prim, voff = __ldg(&ip->vertex_offset);
+    const uint32_t i0 = __ldg(&sc.indices[ioff]) + voff, i1 = __ldg(&sc.indices[ioff + 1]) + voff,
+                   i2 = __ldg(&sc.indices[ioff + 2]) + voff;
+    HitAttr r;
+    r.u = 0.0f; r.v = 0.0f;
+    r.lt = F4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (sc.uv) {
+        const float2 a = __ldg(&sc.uv[i0]), b = __ldg(&sc.uv[i1]), c = __ldg(&sc.uv[i2]);
+        r.u = fmaf_(c.x - a.x, h.b2, fmaf_(b.x - a.x, h.b1, a.x));
+        r.v = fmaf_(c.y - a.y, h.b2, fmaf_(b.y - a.y, h.b1, a.y));
+    }
+    {
+        const float4 a = __ldg(&sc.normals[i0]), b = __ldg(&sc.normals[i1]), c = __ldg(&sc.normals[i2]);
+        r.ln = F3(fmaf_(c.x - a.x, h.b2, fmaf_(b.x - a.x, h.b1, a.x)), fmaf_(c.y - a.y, h.b2, fmaf_(b.y - a.y, h.b1, a.y)),
+                  fmaf_(c.z - a.z, h.b2, fmaf_(b.z - a.z, h.b1, a.z)));
+    }
+    if (sc.tangents) {
+        float4 a = __ldg(&sc.tangents[i0]), b = __ldg(&sc.tangents[i1]), c = __ldg(&sc.tangents[i2]);
+        a.w = a.w > 0.0f ? 2.0f : 0.0f;
+        b.w = b.w > 0.0f ? 2.0f : 0.0f;
+        c.w = c.w > 0.0f ? 2.0f : 0.0f;
+        r.lt = F4(fmaf_(c.x - a.x, h.b2, fmaf_(b.x - a.x, h.b1, a.x)), fmaf_(c.y - a.y, h.b2, fmaf_(b.y - a.y, h.b1, a.y)),
+                  fmaf_(c.z - a.z, h.b2, fmaf_(b.z - a.z, h.b1, a.z)), fmaf_(c.w - a.w, h.b2, fmaf_(b.w - a.w, h.b1, a.w)));
+    }
+    return r;
+}
+
+// The primary vertex's albedo, roughness and normal after FetchGBufferV2 (Shading.slang:82-112):
+// diffuse x diffuse texture, fuzziness x the MRA texture's green channel, and the normal map in
+// the mesh's tangent frame (mikkTSpace, :74-80) carried to world space by the instance's
+// transform. The traced camera ray of the reference leaves the vertex's local normal and
+// tangent unset; here they are the barycentric mixes of the vertex attributes, as the
+// visibility-buffer caster computes them (GeneralFunc.slang:51-52).
+struct GBufTex {
+    f4 albedo;
+    float rough;
+    f3 n;
+};
+static __device__ __noinline__ GBufTex fetch_gbuffer(const ShadeScene& sc, const MatV& m, const HitAttr& a, f3 n,
+                                                     uint32_t inst) {
+    GBufTex g;
+    g.albedo = m.diffuse;
+    if (m.dtex >= 0) g.albedo = g.albedo * tex_sample(sc.tex, m.dtex, a.u, a.v);
+    g.rough = m.fuzz;
+    if (m.mtex >= 0) g.rough = g.rough * tex_sample(sc.tex, m.mtex, a.u, a.v).y;
+    g.n = n;
+    if (m.ntex >= 0) {
+        const f4 t = tex_sample(sc.tex, m.ntex, a.u, a.v);
+        const f3 vn = F3(fmaf_(t.x, 2.0f, -1.0f), fmaf_(t.y, 2.0f, -1.0f), fmaf_(t.z, 2.0f, -1.0f));
+        const f3 T = F3(a.lt.x, a.lt.y, a.lt.z);
+        const f3 B = cross3(a.ln, T) * a.lt.w;
+        const f3 nl = normalize3(F3(fmaf_(vn.z, a.ln.x, fmaf_(vn.y, B.x, vn.x * T.x)),
+                                    fmaf_(vn.z, a.ln.y, fmaf_(vn.y, B.y, vn.x * T.y)),
+                                    fmaf_(vn.z, a.ln.z, fmaf_(vn.y, B.z, vn.x * T.z))));
+        float w[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) w[k] = __ldg(&sc.inst_prev[24u * inst + 12u + k]);
+        g.n = normalize3(xvector(w, nl));
+    }
+    return g;
 }
 
 // ---- probes (AmbientCube.slang:71-78, 178-223, 290-382) ----

@@ -66,6 +66,9 @@ struct GkrtContext {
     uint32_t nvert = 0, nidx = 0, nmat = 0;
     float4* d_pos = nullptr;
     float4* d_nrm = nullptr;
+    float2* d_uv = nullptr;           // texture coordinates (optional)
+    float4* d_tan = nullptr;          // object-space tangents (optional)
+    bool textured = false;            // some material names a texture
     uint32_t* d_slot = nullptr;
     uint32_t* d_idx = nullptr;
     GkrtMaterial* d_mat = nullptr;
@@ -114,6 +117,11 @@ struct GkrtContext {
     size_t refit_ncap = 0, refit_wcap = 0, refit_icap = 0;
     std::vector<uint8_t> tlas_members;
     uint32_t tlas_refits = 0;
+
+    // the texture pool: one RGBA-float buffer per uploaded id and the device table the kernels
+    // read (GKRT_MAX_TEXTURES entries, null texels for an id without a texture)
+    std::vector<float4*> tex_buf;
+    DevTex* d_tex = nullptr;
 
     Unet* unet = nullptr;                       // learned denoiser (gkrt_unet_init)
     unsigned long long* d_counters = nullptr;   // see Counters (gk_trace.cuh): 6 per-pass slots + total rays
@@ -198,6 +206,8 @@ void free_images(GkrtContext* c) {
 
 void free_scene(GkrtContext* c) {
     dfree(c->d_pos); dfree(c->d_nrm); dfree(c->d_slot); dfree(c->d_idx); dfree(c->d_mat);
+    dfree(c->d_uv); dfree(c->d_tan);
+    c->textured = false;
     dfree(c->d_inst_mat); dfree(c->d_inst_prev); dfree(c->d_inst); dfree(c->d_cubes); dfree(c->d_voxels);
     dfree(c->d_cubes_prev);
     c->lights_host.clear();
@@ -303,13 +313,14 @@ int copy_staged(GkrtContext* ctx, int slot, void* dst, size_t bytes, cudaStream_
 int upload_instances(GkrtContext* ctx, cudaStream_t st) {
     const uint32_t n = (uint32_t)ctx->inst.size();
     uint32_t* mats = static_cast<uint32_t*>(stage_buf(ctx, 0, 64 * (size_t)n + 4));
-    float* prev = static_cast<float*>(stage_buf(ctx, 1, 48 * (size_t)n + 4));
+    float* prev = static_cast<float*>(stage_buf(ctx, 1, 96 * (size_t)n + 4));
     DevInst* di = static_cast<DevInst*>(stage_buf(ctx, 2, sizeof(DevInst) * (size_t)n + 16));
     if (!mats || !prev || !di) return fail(ctx, GKRT_ERR_OOM, "page-locked staging of the instance tables");
     for (uint32_t i = 0; i < n; ++i) {
         const GkrtInstance& s = ctx->inst[i];
         std::memcpy(&mats[16 * (size_t)i], s.mat_id, 64);
-        std::memcpy(&prev[12 * (size_t)i], s.combined_prev, 48);
+        std::memcpy(&prev[24 * (size_t)i], s.combined_prev, 48);
+        std::memcpy(&prev[24 * (size_t)i + 12], s.world, 48);
         std::memcpy(di[i].winv, s.world_inv, 48);
         const GkrtMesh& m = ctx->meshes[s.mesh_id];
         di[i].blas_root = ctx->blas_ready ? ctx->blas_root[s.mesh_id] : -1;
@@ -322,13 +333,13 @@ int upload_instances(GkrtContext* ctx, cudaStream_t st) {
     int rc;
     if (ctx->inst_cap < n || !ctx->d_inst) {
         if ((rc = upload(ctx, ctx->d_inst_mat, mats, 64 * (size_t)n)) != GKRT_OK) return rc;
-        if ((rc = upload(ctx, ctx->d_inst_prev, prev, 48 * (size_t)n)) != GKRT_OK) return rc;
+        if ((rc = upload(ctx, ctx->d_inst_prev, prev, 96 * (size_t)n)) != GKRT_OK) return rc;
         if ((rc = upload(ctx, ctx->d_inst, di, sizeof(DevInst) * (size_t)n)) != GKRT_OK) return rc;
         ctx->inst_cap = n;
         return GKRT_OK;
     }
     if ((rc = copy_staged(ctx, 0, ctx->d_inst_mat, 64 * (size_t)n, st)) != GKRT_OK) return rc;
-    if ((rc = copy_staged(ctx, 1, ctx->d_inst_prev, 48 * (size_t)n, st)) != GKRT_OK) return rc;
+    if ((rc = copy_staged(ctx, 1, ctx->d_inst_prev, 96 * (size_t)n, st)) != GKRT_OK) return rc;
     return copy_staged(ctx, 2, ctx->d_inst, sizeof(DevInst) * (size_t)n, st);
 }
 
@@ -736,7 +747,18 @@ ShadeScene shade_scene(GkrtContext* ctx) {
     sc.emit = ctx->d_emit;
     sc.emit_alias = ctx->d_emit_alias;
     sc.nemit = ctx->nemit;
+    sc.tex = ctx->d_tex;
+    sc.uv = ctx->d_uv;
+    sc.tangents = ctx->d_tan;
     return sc;
+}
+
+// Texels of one channel byte as the sampler returns them: UNORM c / 255; sRGB through the
+// sRGB transfer function (Vulkan's sRGB-to-linear conversion) evaluated in double.
+float unorm8(uint8_t c) { return (float)c / 255.0f; }
+float srgb8(uint8_t c) {
+    const double v = (double)c / 255.0;
+    return (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
 }
 
 int check_frame(GkrtContext* ctx, const GkrtFrameConstants* fc) {
@@ -861,13 +883,16 @@ int gkrt_context_create(const GkrtDeviceDesc* desc, GkrtContext** out) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_counters, 8 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_error, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_work, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&ctx->d_tex, GKRT_MAX_TEXTURES * sizeof(DevTex));
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device);
     if (e == cudaSuccess) e = cudaMemset(ctx->d_counters, 0, 8 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_error, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_tex, 0, GKRT_MAX_TEXTURES * sizeof(DevTex));
     if (e != cudaSuccess) {
         dfree(ctx->d_counters);
         dfree(ctx->d_error);
         dfree(ctx->d_work);
+        dfree(ctx->d_tex);
         for (auto& pe : ctx->pass_ev)
             for (cudaEvent_t& ev : pe)
                 if (ev) cudaEventDestroy(ev);
@@ -899,6 +924,8 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     dfree(ctx->d_counters);
     dfree(ctx->d_error);
     dfree(ctx->d_work);
+    dfree(ctx->d_tex);
+    for (float4*& t : ctx->tex_buf) dfree(t);
     for (auto& pe : ctx->pass_ev)
         for (cudaEvent_t& ev : pe)
             if (ev) cudaEventDestroy(ev);
@@ -955,12 +982,22 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
             if (d->indices[ms.index_offset + k] >= ms.vertex_count)
                 return fail(ctx, GKRT_ERR_INVALID_ARG, "index outside its mesh's vertex range");
     }
+    bool textured = false;
     for (uint32_t i = 0; i < d->material_count; ++i) {
         const GkrtMaterial& mt = d->materials[i];
-        if (mt.diffuse_texture_id >= 0 || mt.mra_texture_id >= 0 || mt.normal_texture_id >= 0)
-            return fail(ctx, GKRT_ERR_UNSUPPORTED, "textured materials are outside this pass (texture ids must be -1)");
+        for (int32_t id : {mt.diffuse_texture_id, mt.mra_texture_id, mt.normal_texture_id}) {
+            if (id < -1 || id >= (int32_t)GKRT_MAX_TEXTURES)
+                return fail(ctx, GKRT_ERR_INVALID_ARG, "texture id outside -1 .. GKRT_MAX_TEXTURES - 1");
+            textured = textured || id >= 0;
+        }
         if (mt.material_model > GKRT_MAT_MIXTURE) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown material model");
     }
+    for (uint32_t i = 0; d->texcoords && i < d->vertex_count; ++i)
+        if (!std::isfinite(d->texcoords[2 * (size_t)i]) || !std::isfinite(d->texcoords[2 * (size_t)i + 1]))
+            return fail(ctx, GKRT_ERR_INVALID_ARG, "non-finite texture coordinate");
+    for (uint32_t i = 0; d->tangents && i < d->vertex_count; ++i)
+        if (!finite3(d->tangents + 4 * (size_t)i) || !std::isfinite(d->tangents[4 * (size_t)i + 3]))
+            return fail(ctx, GKRT_ERR_INVALID_ARG, "non-finite tangent");
     int rc = validate_instances(ctx, d->instances, d->instance_count, d->mesh_count, d->material_count);
     if (rc != GKRT_OK) return rc;
     DeviceGuard device_guard(ctx->device);
@@ -977,6 +1014,9 @@ int gkrt_scene_upload(GkrtContext* ctx, const GkrtSceneDesc* d) {
     mesh_slot_triangles(d->meshes, d->mesh_count, d->indices, d->material_slots, ctx->slot_tris);
     if ((rc = upload(ctx, ctx->d_pos, d->positions, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
     if ((rc = upload(ctx, ctx->d_nrm, d->normals, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
+    if (d->texcoords && (rc = upload(ctx, ctx->d_uv, d->texcoords, 8 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
+    if (d->tangents && (rc = upload(ctx, ctx->d_tan, d->tangents, 16 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
+    ctx->textured = textured;
     if ((rc = upload(ctx, ctx->d_slot, d->material_slots, 4 * (size_t)d->vertex_count)) != GKRT_OK) return rc;
     if ((rc = upload(ctx, ctx->d_idx, d->indices, 4 * (size_t)d->index_count)) != GKRT_OK) return rc;
     if ((rc = upload(ctx, ctx->d_mat, d->materials, sizeof(GkrtMaterial) * (size_t)d->material_count)) != GKRT_OK)
@@ -1045,6 +1085,8 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     if (rc != GKRT_OK) return rc;
     if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
     if (fc->nee_mode > GKRT_NEE_EMISSIVE) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown nee_mode");
+    if ((fc->flags & GKRT_FRAME_SKY_TEXTURE) && fc->sky_index >= GKRT_MAX_TEXTURES)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "sky_index outside the texture pool");
     DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = ensure_bvh(ctx, 0, st)) != GKRT_OK) return rc;
@@ -1065,7 +1107,48 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     // the stack bound check_stack_bound enforced at build time, at least 8 entries
     const int stack_words = std::max(8, std::min(kStackSize, ctx->blas_bin_depth + ctx->tlas_bin_depth + 3));
     GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, (int)ctx->P, im, ctx->d_counters, ctx->d_work,
-                                   ctx->num_sms, stack_words, st));
+                                   ctx->num_sms, stack_words, ctx->textured, st));
+    return GKRT_OK;
+}
+
+int gkrt_texture_upload(GkrtContext* ctx, uint32_t texture_id, uint32_t width, uint32_t height, uint32_t format,
+                        const void* texels, size_t bytes) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (texture_id >= GKRT_MAX_TEXTURES) return fail(ctx, GKRT_ERR_INVALID_ARG, "texture id >= GKRT_MAX_TEXTURES");
+    if (format > GKRT_TEX_RGBA32F) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown texture format");
+    if (width == 0 || height == 0 || width > 16384 || height > 16384)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "texture size must be 1..16384");
+    const size_t n = (size_t)width * height;
+    if (!texels || bytes != n * (format == GKRT_TEX_RGBA32F ? 16u : 4u))
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "texel buffer missing or of the wrong size");
+    std::vector<float4> t(n);
+    if (format == GKRT_TEX_RGBA32F) {
+        std::memcpy(t.data(), texels, n * 16);
+    } else {
+        const uint8_t* b = static_cast<const uint8_t*>(texels);
+        for (size_t i = 0; i < n; ++i) {
+            const uint8_t* c = b + 4 * i;
+            if (format == GKRT_TEX_RGBA8_SRGB) t[i] = make_float4(srgb8(c[0]), srgb8(c[1]), srgb8(c[2]), unorm8(c[3]));
+            else t[i] = make_float4(unorm8(c[0]), unorm8(c[1]), unorm8(c[2]), unorm8(c[3]));
+        }
+    }
+    DeviceGuard device_guard(ctx->device);
+    if (ctx->tex_buf.size() < GKRT_MAX_TEXTURES) ctx->tex_buf.resize(GKRT_MAX_TEXTURES, nullptr);
+    float4* d = nullptr;
+    GK_CUDA(cudaMalloc((void**)&d, n * sizeof(float4)));
+    cudaError_t e = cudaMemcpy(d, t.data(), n * sizeof(float4), cudaMemcpyHostToDevice);
+    DevTex entry;
+    entry.texels = d;
+    entry.w = width;
+    entry.h = height;
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();   // no kernel still reads the texture replaced here
+    if (e == cudaSuccess) e = cudaMemcpy(ctx->d_tex + texture_id, &entry, sizeof(DevTex), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(ctx, e, "gkrt_texture_upload");
+    }
+    dfree(ctx->tex_buf[texture_id]);
+    ctx->tex_buf[texture_id] = d;
     return GKRT_OK;
 }
 

@@ -183,10 +183,11 @@ cudaError_t gkrt_launch_screenshot(const uint32_t* img, int OW, int x0, int y0, 
                                    cudaStream_t st);
 
 // stack_words: traversal stack entries per thread, at least the scene's two-child depth bound
-// (mesh depth + instance depth + 3) and at most kStackSize.
+// (mesh depth + instance depth + 3) and at most kStackSize. textured: the scene's materials
+// name textures (the textured instantiation also runs when the frame samples a sky texture).
 cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,
                                    const gk::PixelImages& im, unsigned long long* counters, unsigned int* work,
-                                   int num_sms, int stack_words, cudaStream_t st);
+                                   int num_sms, int stack_words, bool textured, cudaStream_t st);
 // Probe grid (k_probes.cu): voxel distance data of probes [first, first + count), and one bake
 // step of those probes reading neighbours from cubes_prev (a snapshot of cubes).
 cudaError_t gkrt_launch_probe_voxelize(const gk::ShadeScene& sc, uint32_t first, uint32_t count, uint4* voxels,

@@ -48,10 +48,11 @@ enum Stage : uint32_t {
 };
 
 // Per-thread slots in shared memory (strided by the block size): the primary vertex,
-// the per-pixel loop bounds, the two accumulators and the pending emissive-NEE sample.
+// the per-pixel loop bounds, the two accumulators, the pending emissive-NEE sample and, in the
+// textured instantiation, the primary albedo (material diffuse x diffuse texture).
 enum Slot {
     SL_PX = 0, SL_PY, SL_PZ, SL_NX, SL_NY, SL_NZ, SL_MAT, SL_LOOP, SL_FC, SL_FR = SL_FC + 4, SL_NEE = SL_FR + 4,
-    SL_COUNT = SL_NEE + 4
+    SL_COUNT = SL_NEE + 4, SL_ALB = SL_COUNT, SL_COUNT_TEX = SL_ALB + 4
 };
 
 struct Lane {
@@ -84,6 +85,12 @@ __device__ __forceinline__ void emit(Trav& T, const Ctx& c, f3 o, f3 d, int mode
 
 __device__ __forceinline__ f3 pv_pos(const Ctx& c) { return F3(c.slot(SL_PX), c.slot(SL_PY), c.slot(SL_PZ)); }
 __device__ __forceinline__ f3 pv_nrm(const Ctx& c) { return F3(c.slot(SL_NX), c.slot(SL_NY), c.slot(SL_NZ)); }
+// primaryAlbedo_ of the reference: the material's diffuse, times its diffuse texture (kTex)
+template <bool kTex>
+__device__ __forceinline__ f4 pv_albedo(const Ctx& c) {
+    if (kTex) return F4(c.slot(SL_ALB), c.slot(SL_ALB + 1), c.slot(SL_ALB + 2), c.slot(SL_ALB + 3));
+    return load_mat(c.sc, __float_as_uint(c.slot(SL_MAT))).diffuse;
+}
 
 // Run the lane's state machine on the ray that just finished, up to the next ray
 // (returns true) or the end of the pixel (returns false). Follows FPathTracingRendererV2:
@@ -95,7 +102,9 @@ __device__ __forceinline__ f3 pv_nrm(const Ctx& c) { return F3(c.slot(SL_NX), c.
 // section at most once per call, so lanes in different states re-converge after each
 // section and the expensive ones (the sampling before a trace, the hit reconstruction
 // after it) run once per warp for all the lanes that need them.
-template <bool kNee>
+// kTex: textured materials and the textured sky compiled in (the scene has texture ids or the
+// frame samples a sky texture).
+template <bool kNee, bool kTex>
 __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
     const GkrtFrameConstants& fc = c.fc;
     const f3 sunDir = F3(fc.sun_direction[0], fc.sun_direction[1], fc.sun_direction[2]);
@@ -110,7 +119,7 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
         const bool want_ids = (fc.flags & GKRT_FRAME_PRIMARY_IDS) != 0u;
         c.im.single_specular[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (!T.hit) {
-            const f4 s = sky(fc);
+            const f4 s = kTex ? sky_dir(c.sc, fc, normalize3(T.wd)) : sky(fc);
             c.im.single_diffuse[pix] = make_float4(s.x, s.y, s.z, s.w);
             c.im.motion[pix] = make_float2(0.0f, 0.0f);
             c.im.albedo[pix] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
@@ -129,7 +138,7 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
             const float cfx = div_(ch.x, ch.w) * 0.5f, cfy = div_(ch.y, ch.w) * 0.5f;
             float cp[12];
 #pragma unroll
-            for (int q = 0; q < 12; ++q) cp[q] = __ldg(&c.sc.inst_prev[12u * pv.inst + q]);
+            for (int q = 0; q < 12; ++q) cp[q] = __ldg(&c.sc.inst_prev[24u * pv.inst + q]);
             const f3 prevP = xpoint(cp, pv.P);
             const f4 ph = mat4v(fc.prev_view_projection_unjit, F4(prevP.x, prevP.y, prevP.z, 1.0f));
             const float pfx = div_(ph.x, ph.w) * 0.5f, pfy = div_(ph.y, ph.w) * 0.5f;
@@ -138,8 +147,17 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
             else mom = mom > 0u ? mom - 1u : 0u;
             c.im.motion_moment[pix] = mom;
             const MatV pm = load_mat(c.sc, pv.mat);
-            c.im.albedo[pix] = make_float4(pm.diffuse.x, pm.diffuse.y, pm.diffuse.z, pm.diffuse.w);
-            c.im.normal[pix] = make_float4(pv.N.x, pv.N.y, pv.N.z, pm.fuzz);
+            f4 palb = pm.diffuse;
+            float prough = pm.fuzz;
+            if (kTex) {   // FetchGBufferV2 (Shading.slang:82-112)
+                const HitAttr ha = hit_attr(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
+                const GBufTex g = fetch_gbuffer(c.sc, pm, ha, pv.N, pv.inst);
+                palb = g.albedo;
+                prough = g.rough;
+                pv.N = g.n;
+            }
+            c.im.albedo[pix] = make_float4(palb.x, palb.y, palb.z, palb.w);
+            c.im.normal[pix] = make_float4(pv.N.x, pv.N.y, pv.N.z, prough);
             c.im.object_id[pix] = __ldg(&c.sc.S.inst[pv.inst].instance_id);
             c.im.motion[pix] = make_float2((pfx - cfx) * (float)c.W, (pfy - cfy) * (float)c.H);
             c.im.prev_depth[pix] = div_(clip.z, clip.w);
@@ -160,6 +178,10 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
                 c.slot(SL_LOOP) = __uint_as_float((uint32_t)samples | (maxB << 16) | (pdiel ? 0x80000000u : 0u));
 #pragma unroll
                 for (int q = 0; q < 4; ++q) { c.slot(SL_FC + q) = 0.0f; c.slot(SL_FR + q) = 0.0f; }
+                if (kTex) {
+                    c.slot(SL_ALB) = palb.x; c.slot(SL_ALB + 1) = palb.y;
+                    c.slot(SL_ALB + 2) = palb.z; c.slot(SL_ALB + 3) = palb.w;
+                }
                 L.i = 0;
                 need_begin = true;
             }
@@ -178,12 +200,17 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
                 L.rc = F4(0.0f, 0.0f, 0.0f, 0.0f);
                 term = true;
             } else {
-                if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !L.chanceReflect) L.rc = L.rc * hm.diffuse;
+                f4 halb = hm.diffuse;
+                if (kTex && hm.dtex >= 0) {   // the hit's diffuse texture (Shading.slang:1046-1050)
+                    const HitAttr ha = hit_attr(c.sc, T.wo, T.wd, T.inst, T.prim, T.tri);
+                    halb = halb * tex_sample(c.sc.tex, hm.dtex, ha.u, ha.v);
+                }
+                if (hm.model == GKRT_MAT_DIFFUSE_LIGHT || !L.chanceReflect) L.rc = L.rc * halb;
                 if (L.back && !L.diel) { L.rc = F4(0.5f, 0.5f, 0.5f, 0.0f); term = true; }
                 else term = hm.model == GKRT_MAT_DIFFUSE_LIGHT;
             }
         } else {
-            L.rc = L.rc * sky(fc);
+            L.rc = L.rc * (kTex ? sky_dir(c.sc, fc, T.wd) : sky(fc));
             term = true;
         }
         const uint32_t loop = __float_as_uint(c.slot(SL_LOOP));
@@ -237,7 +264,7 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
 
     // 5. end of a sample (Shading.slang:1159-1176), then the next sample or DirectIlluminate
     if (need_end) {
-        if (L.hitMetal) L.rc = L.rc * load_mat(c.sc, __float_as_uint(c.slot(SL_MAT))).diffuse;
+        if (L.hitMetal) L.rc = L.rc * pv_albedo<kTex>(c);
         const int acc = L.hitReflect ? SL_FR : SL_FC;
         c.slot(acc) = c.slot(acc) + L.rc.x;
         c.slot(acc + 1) = c.slot(acc + 1) + L.rc.y;
@@ -336,7 +363,7 @@ __device__ bool advance(Lane& L, Trav& T, const Ctx& c) {
         NeeSample ns;
         if (kNee && L.neeLobe && nee_sample(c.sc, L.seed, L.vs.P, L.vs.N, L.rc, ns)) {
             f4 contrib = ns.contrib;
-            if (L.hitMetal) contrib = contrib * load_mat(c.sc, __float_as_uint(c.slot(SL_MAT))).diffuse;
+            if (L.hitMetal) contrib = contrib * pv_albedo<kTex>(c);
             c.slot(SL_NEE) = contrib.x; c.slot(SL_NEE + 1) = contrib.y;
             c.slot(SL_NEE + 2) = contrib.z; c.slot(SL_NEE + 3) = contrib.w;
             L.stage = pre_first ? ST_NEE_FIRST : ST_NEE_BOUNCE;
@@ -381,7 +408,7 @@ __device__ void start_pixel(Lane& L, Trav& T, const Ctx& c, int x, int y) {
 // two-child depth bound), then the per-pixel slots. A stack no larger than the scene needs
 // leaves the rest of the SM's 256 KB to L1, which serves the node fetches (measured on 1080p
 // bricks: 72-word stacks 4.15 ms, 36-word 4.01 ms).
-template <bool kNee>
+template <bool kNee, bool kTex>
 __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeScene sc, GkrtFrameConstants fc, int W, int H,
                                                            int P, PixelImages im, unsigned long long* counters,
                                                            unsigned int* work, int stack_words) {
@@ -404,7 +431,7 @@ __global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeSc
     bool tracing = false, exhausted = false;
     for (;;) {
         if (!tracing) {
-            if (L.pix >= 0) tracing = advance<kNee>(L, T, c);
+            if (L.pix >= 0) tracing = advance<kNee, kTex>(L, T, c);
             while (!tracing && !exhausted) {
                 // next pixel: warp-aggregated fetch over 8 x 4 tiles
                 const unsigned m = __activemask();
@@ -478,19 +505,23 @@ using namespace gk;
 
 cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstants& fc, int W, int H, int P,
                                    const PixelImages& im, unsigned long long* counters, unsigned int* work,
-                                   int num_sms, int stack_words, cudaStream_t st) {
+                                   int num_sms, int stack_words, bool textured, cudaStream_t st) {
     if (stack_words < 1 || stack_words > kStackSize) return cudaErrorInvalidValue;
     const bool nee = fc.nee_mode == GKRT_NEE_EMISSIVE && sc.nemit > 0u;
-    const size_t smem = (size_t)(stack_words + SL_COUNT) * kPtThreads * 4u;
+    const bool tex = textured || (fc.has_sky && (fc.flags & GKRT_FRAME_SKY_TEXTURE));
+    if (tex && !sc.tex) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)(stack_words + (tex ? SL_COUNT_TEX : SL_COUNT)) * kPtThreads * 4u;
     // resident blocks per SM of each instantiation and stack size, queried once per device
-    static int occ[kMaxDevices][2][kStackSize + 1] = {};
+    static int occ[kMaxDevices][2][2][kStackSize + 1] = {};
     const int dev = current_device_slot();
     if (dev < 0) return cudaErrorInvalidDevice;
-    int* o = &occ[dev][nee][stack_words];
+    int* o = &occ[dev][nee][tex][stack_words];
     cudaError_t e = cudaSuccess;
     if (!*o) {
-        e = nee ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<true>, kPtThreads, smem)
-                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<false>, kPtThreads, smem);
+        e = nee ? (tex ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<true, true>, kPtThreads, smem)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<true, false>, kPtThreads, smem))
+                : (tex ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<false, true>, kPtThreads, smem)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, k_trace_pass<false, false>, kPtThreads, smem));
         if (e != cudaSuccess) return e;
     }
     int per_sm = *o;
@@ -501,8 +532,14 @@ cudaError_t gkrt_launch_trace_pass(const ShadeScene& sc, const GkrtFrameConstant
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(work, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    if (nee) k_trace_pass<true><<<blocks, kPtThreads, smem, st>>>(sc, fc, W, H, P, im, counters, work, stack_words);
-    else k_trace_pass<false><<<blocks, kPtThreads, smem, st>>>(sc, fc, W, H, P, im, counters, work, stack_words);
+    if (nee && tex)
+        k_trace_pass<true, true><<<blocks, kPtThreads, smem, st>>>(sc, fc, W, H, P, im, counters, work, stack_words);
+    else if (nee)
+        k_trace_pass<true, false><<<blocks, kPtThreads, smem, st>>>(sc, fc, W, H, P, im, counters, work, stack_words);
+    else if (tex)
+        k_trace_pass<false, true><<<blocks, kPtThreads, smem, st>>>(sc, fc, W, H, P, im, counters, work, stack_words);
+    else
+        k_trace_pass<false, false><<<blocks, kPtThreads, smem, st>>>(sc, fc, W, H, P, im, counters, work, stack_words);
     return cudaGetLastError();
 }
 

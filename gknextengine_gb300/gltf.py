@@ -25,11 +25,18 @@ Follows the reference's loader, FSceneLoader::LoadGLTFScene and ParseGltfNode
 * without a camera, AutoFocusCamera (:755-783): from the union of the meshes' local boxes,
   looking at its centre from +z at the box diagonal's length.
 
-Not taken over: textures (the pass takes material factors only; texture references are
-dropped), animations, KHR_draco_mesh_compression (a third-party decoder; such files raise
-GlbError), node matrices (the reference reads TRS only), sparse accessors. A primitive
-without normals gets area-weighted vertex normals (the reference would read an invalid
-accessor).
+* textures (:259-309, 328-331): base colour (sRGB), metallic-roughness and normal textures;
+  image i of the file becomes texture id TEXTURE_BASE + i (the pool's ids below that hold the
+  skies, Engine.cpp:853-870); PNG images embedded in the binary chunk are decoded (8-bit, any
+  colour type); TEXCOORD_0 and TANGENT become the scene's vertex attributes. The sky samples
+  texture SkyIdx (default 0), rotated by SkyRotation, as the reference's pool does; the caller
+  uploads the reference's sky there (imageio.load_hdr, imageio.REFERENCE_SKIES).
+
+Not taken over: images in other formats (JPEG and KTX2/BasisU need third-party decoders; their
+ids stay on the materials and sample as white, and info["textures_not_decoded"] lists them),
+animations, KHR_draco_mesh_compression (a third-party decoder; such files raise GlbError), node
+matrices (the reference reads TRS only), sparse accessors. A primitive without normals gets
+area-weighted vertex normals (the reference would read an invalid accessor).
 """
 from __future__ import annotations
 
@@ -39,7 +46,9 @@ import struct
 
 import numpy as np
 
-from . import abi, camera, scenes
+from . import abi, camera, imageio, scenes
+
+TEXTURE_BASE = 100   # texture id of the file's image 0
 
 
 class GlbError(ValueError):
@@ -115,7 +124,16 @@ def local_transform(node: dict) -> np.ndarray:
     return m
 
 
-def _material(mat: dict) -> np.ndarray:
+def _texture_id(gl: dict, ref) -> int:
+    """Texture id of a glTF texture reference ({"index": t}): TEXTURE_BASE + its image index."""
+    if not ref or "index" not in ref:
+        return -1
+    t = gl.get("textures", [])[ref["index"]]
+    src = t.get("source", ref["index"])
+    return TEXTURE_BASE + int(src)
+
+
+def _material(mat: dict, gl: dict) -> np.ndarray:
     pbr = mat.get("pbrMetallicRoughness", {})
     base = pbr.get("baseColorFactor", [1.0, 1.0, 1.0, 1.0])
     rough = float(pbr.get("roughnessFactor", 1.0))
@@ -144,7 +162,47 @@ def _material(mat: dict) -> np.ndarray:
     m = scenes.material([math.sqrt(base[0]), math.sqrt(base[1]), math.sqrt(base[2]), 1.0], model,
                         fuzziness=rough, ri=ri, metalness=metal, ri2=ri2)
     m["normal_texture_scale"] = float(mat.get("normalTexture", {}).get("scale", 1.0))
+    m["diffuse_texture_id"] = _texture_id(gl, pbr.get("baseColorTexture"))
+    m["mra_texture_id"] = _texture_id(gl, pbr.get("metallicRoughnessTexture"))
+    m["normal_texture_id"] = _texture_id(gl, mat.get("normalTexture"))
     return m
+
+
+def _textures(gl: dict, binchunk: bytes):
+    """{texture id: (format, texels)} of the images the materials use, and the images that
+    are not decoded here. Base colour images are sRGB, the others linear."""
+    srgb, used = set(), set()
+    for mat in gl.get("materials", []):
+        pbr = mat.get("pbrMetallicRoughness", {})
+        for key, is_srgb in ((pbr.get("baseColorTexture"), True), (pbr.get("metallicRoughnessTexture"), False),
+                             (mat.get("normalTexture"), False)):
+            tid = _texture_id(gl, key)
+            if tid >= 0:
+                used.add(tid)
+                if is_srgb:
+                    srgb.add(tid)
+    out, skipped = {}, []
+    for tid in sorted(used):
+        img = gl.get("images", [])[tid - TEXTURE_BASE]
+        mime = img.get("mimeType", "")
+        if "bufferView" not in img or mime != "image/png":
+            skipped.append({"image": tid - TEXTURE_BASE, "mime": mime or img.get("uri", "")})
+            continue
+        v = gl["bufferViews"][img["bufferView"]]
+        data = binchunk[v.get("byteOffset", 0):v.get("byteOffset", 0) + v["byteLength"]]
+        out[tid] = (abi.TEX_RGBA8_SRGB if tid in srgb else abi.TEX_RGBA8_UNORM, imageio.decode_png(data, rgba=True))
+    return out, skipped
+
+
+def _float_attr(gl: dict, binchunk: bytes, idx: int) -> np.ndarray:
+    """An accessor as float32, normalized integer types mapped to [0, 1] / [-1, 1]."""
+    a = gl["accessors"][idx]
+    v = accessor(gl, binchunk, idx)
+    ct = a["componentType"]
+    if ct == 5126 or not a.get("normalized", False):
+        return v.astype(np.float32)
+    scale = {5121: 255.0, 5123: 65535.0, 5120: 127.0, 5122: 32767.0}[ct]
+    return np.maximum(v.astype(np.float32) / np.float32(scale), np.float32(-1.0))
 
 
 def _vertex_normals(pos: np.ndarray, idx: np.ndarray) -> np.ndarray:
@@ -162,15 +220,17 @@ def load_glb(source, width: int = 1920, height: int = 1080):
     """(SceneArrays, Camera, camera.Settings, info) of a .glb file path or bytes; info holds
     the node names of the instances, all cameras and the light count."""
     gl, binchunk = read_glb(source)
-    # materials
-    mats = [_material(m) for m in gl.get("materials", [])]
+    # materials and their textures
+    mats = [_material(m, gl) for m in gl.get("materials", [])]
+    textures, tex_skipped = _textures(gl, binchunk)
     if not mats:
         mats = [scenes.mixture((1.0, 1.0, 1.0), 1.0)]
     # meshes
-    pos_l, nrm_l, slot_l, idx_l, mesh_rows, local_boxes = [], [], [], [], [], []
+    pos_l, nrm_l, slot_l, idx_l, mesh_rows, local_boxes, uv_l, tan_l = [], [], [], [], [], [], [], []
+    any_uv = any_tan = False
     voff = ioff = 0
     for mesh in gl.get("meshes", []):
-        mp, mn_, ms, mi = [], [], [], []
+        mp, mn_, ms, mi, mu, mt = [], [], [], [], [], []
         section = 0
         vbase = 0
         for prim in mesh.get("primitives", []):
@@ -192,13 +252,21 @@ def load_glb(source, width: int = 1920, height: int = 1080):
                 raise GlbError("index outside the primitive's vertices")
             n = (accessor(gl, binchunk, attrs["NORMAL"]).astype(np.float32)[:, :3] if "NORMAL" in attrs
                  else _vertex_normals(p, ind))
-            mp.append(p); mn_.append(n)
+            uv = (_float_attr(gl, binchunk, attrs["TEXCOORD_0"])[:, :2] if "TEXCOORD_0" in attrs
+                  else np.zeros((p.shape[0], 2), np.float32))
+            tg = (_float_attr(gl, binchunk, attrs["TANGENT"])[:, :4] if "TANGENT" in attrs
+                  else np.zeros((p.shape[0], 4), np.float32))
+            any_uv = any_uv or "TEXCOORD_0" in attrs
+            any_tan = any_tan or "TANGENT" in attrs
+            mp.append(p); mn_.append(n); mu.append(uv); mt.append(tg)
             ms.append(np.full(p.shape[0], section, np.uint32))
             mi.append((ind + vbase).astype(np.uint32))
             vbase += p.shape[0]
             section += 1
         p = np.concatenate(mp) if mp else np.zeros((0, 3), np.float32)
         n = np.concatenate(mn_) if mn_ else np.zeros((0, 3), np.float32)
+        uv_l.append(np.concatenate(mu) if mu else np.zeros((0, 2), np.float32))
+        tan_l.append(np.concatenate(mt) if mt else np.zeros((0, 4), np.float32))
         i = np.concatenate(mi) if mi else np.zeros(0, np.uint32)
         pos_l.append(np.concatenate([p, np.ones((p.shape[0], 1), np.float32)], axis=1))
         nrm_l.append(np.concatenate([n, np.zeros((n.shape[0], 1), np.float32)], axis=1))
@@ -212,7 +280,7 @@ def load_glb(source, width: int = 1920, height: int = 1080):
         raise GlbError("no triangle meshes")
     # environment (EnvironmentSetting::Reset and the scene's extras)
     st = camera.Settings(has_sky=True, sky_intensity=100.0, has_sun=False, sun_intensity=500.0)
-    sky_rotation, sun_rotation = 0.0, 0.5
+    sky_rotation, sun_rotation, sky_idx = 0.0, 0.5, 0
     scene_idx = gl.get("scene", 0)
     root = gl["scenes"][scene_idx] if gl.get("scenes") else {"nodes": list(range(len(gl.get("nodes", []))))}
     ex = root.get("extras", {})
@@ -222,6 +290,8 @@ def load_glb(source, width: int = 1920, height: int = 1080):
         st.sky_intensity = float(ex["SkyIntensity"])
     if "SkyRotation" in ex:
         sky_rotation = float(ex["SkyRotation"])
+    if "SkyIdx" in ex:
+        sky_idx = int(ex["SkyIdx"])
     if "SunIntensity" in ex:
         st.has_sun = True
         st.sun_intensity = float(ex["SunIntensity"])
@@ -289,10 +359,15 @@ def load_glb(source, width: int = 1920, height: int = 1080):
         c = (hi - lo) * 0.5 + lo
         cams.append(camera.Camera(eye=(c[0], c[1], c[2] + np.linalg.norm(hi - lo)), center=c, fov_deg=40.0))
     st.sky_color = (1.0, 1.0, 1.0, 1.0)
+    st.sky_texture = sky_idx
+    st.sky_rotation = sky_rotation
     sc = abi.SceneArrays(np.concatenate(pos_l), np.concatenate(nrm_l), np.concatenate(slot_l),
                          np.concatenate(idx_l), np.array(mesh_rows, dtype=abi.MESH_DTYPE),
                          np.array(mats, dtype=abi.MATERIAL_DTYPE), np.array(insts, dtype=abi.INSTANCE_DTYPE),
-                         lights=np.array(lights, dtype=abi.LIGHT_DTYPE) if lights else None, name="glb")
+                         lights=np.array(lights, dtype=abi.LIGHT_DTYPE) if lights else None, name="glb",
+                         texcoords=np.concatenate(uv_l) if any_uv else None,
+                         tangents=np.concatenate(tan_l) if any_tan else None, textures=textures)
     info = {"instance_names": names, "cameras": cams, "lights": len(lights), "sky_rotation": sky_rotation,
-            "nodes": counter[0]}
+            "sky_index": sky_idx, "nodes": counter[0], "textures": sorted(textures),
+            "textures_not_decoded": tex_skipped}
     return sc, cams[0], st, info

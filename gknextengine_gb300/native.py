@@ -52,6 +52,7 @@ def load(path: str | None = None):
     L.gkrt_copy_image_to_host_async.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
     L.gkrt_upload_image.argtypes = [vp, C.c_int, vp, C.c_size_t, vp]
     L.gkrt_trace_rays.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
+    L.gkrt_texture_upload.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, C.c_size_t]
     L.gkrt_trace_rays_noalloc.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_get_stats.argtypes = [vp, C.POINTER(abi.GkrtStats)]
     L.gkrt_get_pass_times.argtypes = [vp, C.POINTER(abi.GkrtPassTimes)]
@@ -82,7 +83,7 @@ def load(path: str | None = None):
     L.gkrt_set_material_params.argtypes = [vp, vp, vp, C.c_uint32, C.c_uint32, vp]
     L.gkrt_adjoint_forward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp]
     L.gkrt_adjoint_backward.argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, vp, vp, vp, vp, vp]
-    if L.gkrt_abi_version() != 1:
+    if L.gkrt_abi_version() != 2:
         raise RuntimeError("libgkrt ABI version mismatch")
     _lib = L
     return L
@@ -97,6 +98,7 @@ EXPORTED = [
     "gkrt_output_resize", "gkrt_output_pass", "gkrt_get_output", "gkrt_copy_output_to_host",
     "gkrt_screenshot",
     "gkrt_get_image", "gkrt_copy_image_to_host", "gkrt_copy_image_to_host_async", "gkrt_upload_image", "gkrt_trace_rays", "gkrt_trace_rays_noalloc",
+    "gkrt_texture_upload",
     "gkrt_get_stats", "gkrt_get_pass_times", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",
     "gkrt_synchronize", "gkrt_affine_inverse",
     "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16", "gkrt_conv3x3_wgrad_bf16",

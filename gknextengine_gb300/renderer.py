@@ -77,6 +77,15 @@ class PathTracingRenderer:
         self._scene = scene
         desc = scene.desc()
         self._check(self._lib.gkrt_scene_upload(self._h, C.byref(desc)))
+        for tid, (fmt, texels) in sorted(getattr(scene, "textures", {}).items()):
+            self.upload_texture(tid, fmt, texels)
+
+    def upload_texture(self, texture_id: int, fmt: int, texels: np.ndarray):
+        """Texture `texture_id` of the pool (GlobalTexturePool): texels (h, w, 4) uint8 for the
+        RGBA8 formats, float32 for TEX_RGBA32F."""
+        t = abi.texel_buffer(fmt, texels)
+        self._check(self._lib.gkrt_texture_upload(self._h, texture_id, t.shape[1], t.shape[0], fmt,
+                                                  t.ctypes.data, t.nbytes))
 
     @property
     def material_count(self) -> int:

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GKRT_ABI_VERSION 1
+#define GKRT_ABI_VERSION 2
 
 /* ---- status codes (the reference throws instead: src/Utilities/Exception.hpp:10) ---- */
 #define GKRT_OK                0
@@ -36,7 +36,7 @@ extern "C" {
 #define GKRT_ERR_CUDA          3  /* a CUDA runtime call failed                         */
 #define GKRT_ERR_TIMEOUT       4  /* a bounded wait ran out (host watchdog)             */
 #define GKRT_ERR_DEVICE_LIMIT  5  /* a device loop hit its iteration cap                */
-#define GKRT_ERR_UNSUPPORTED   6  /* feature outside this pass (textures, ...)          */
+#define GKRT_ERR_UNSUPPORTED   6  /* feature outside this pass                           */
 #define GKRT_ERR_STATE         7  /* call order: render before scene/resize, ...        */
 #define GKRT_ERR_NO_DEVICE     8  /* no CUDA device / the kernels are not loadable      */
 
@@ -49,7 +49,7 @@ extern "C" {
 #define GKRT_MAT_MIXTURE       5u
 
 /* Material: byte-for-byte the reference's 64-byte Material (BasicTypes.slang:218-236).
- * Texture ids must be -1: bindless textures are outside this pass. */
+ * Texture ids are -1 or ids of textures given to gkrt_texture_upload (below GKRT_MAX_TEXTURES). */
 typedef struct GkrtMaterial {
     float    diffuse[4];
     int32_t  diffuse_texture_id;
@@ -121,6 +121,11 @@ typedef struct GkrtSceneDesc {
      * 14 u32 per AmbientCube and 4 u32 per VoxelData, or NULL for all-zero probes. */
     const uint32_t*     probe_cubes;
     const uint32_t*     probe_voxels;
+    /* Optional vertex attributes of textured materials (GPUVertex, Vertex.hpp:80-99): the
+     * texture coordinates (Position_Tx.w, Normal_Ty.w) and the object-space tangent with its
+     * handedness in w. NULL: all zero. */
+    const float*        texcoords;      /* float2 per vertex                               */
+    const float*        tangents;       /* float4 per vertex                               */
 } GkrtSceneDesc;
 
 /* Frame constants: the fields of UniformBufferObject (BasicTypes.slang:22-84) the pass
@@ -137,7 +142,7 @@ typedef struct GkrtFrameConstants {
     float    prev_view_projection_unjit[16];
     float    sun_direction[4];
     float    sun_color[4];
-    float    sky_color[4];          /* constant sky radiance (stands in for the HDR map) */
+    float    sky_color[4];          /* constant sky radiance (without GKRT_FRAME_SKY_TEXTURE) */
     float    aperture;
     float    focus_distance;
     float    paper_white_nit;
@@ -160,7 +165,8 @@ typedef struct GkrtFrameConstants {
     uint32_t denoiser;             /* GKRT_DENOISE_*                                    */
     uint32_t nee_mode;             /* GKRT_NEE_*                                        */
     uint32_t flags;                /* GKRT_FRAME_*                                      */
-    uint32_t reserved[2];
+    uint32_t sky_index;            /* SkyIdx: texture of the HDR sky, with GKRT_FRAME_SKY_TEXTURE */
+    float    sky_rotation;         /* SkyRotation (half turns)                          */
 } GkrtFrameConstants;
 
 #define GKRT_DENOISE_JBF     0u    /* reference single-pass joint bilateral filter      */
@@ -171,6 +177,18 @@ typedef struct GkrtFrameConstants {
 #define GKRT_NEE_EMISSIVE    1u    /* + emissive-triangle NEE via an alias table (new)  */
 
 #define GKRT_FRAME_PRIMARY_IDS  1u /* also write HIT_INST / HIT_PRIM of the camera ray  */
+#define GKRT_FRAME_SKY_TEXTURE  2u /* sky misses sample texture sky_index as an equirect-
+                                      angular map (SampleIBLV2, Shading.slang:194-199);
+                                      without the flag the sky is sky_color              */
+
+/* Textures (the reference's bindless GlobalTexturePool). Texels are stored as RGBA float:
+ * RGBA8 UNORM decoded as c / 255, RGBA8 sRGB through the sRGB transfer function (alpha c / 255),
+ * RGBA32F as given. Sampling follows the pool's sampler (Sampler.hpp:9-27, TextureImage.cpp:
+ * 24-31) at level 0 (SampleLevel(uv, 0)): Vulkan's linear filter with repeat addressing. */
+#define GKRT_TEX_RGBA8_UNORM 0u
+#define GKRT_TEX_RGBA8_SRGB  1u
+#define GKRT_TEX_RGBA32F     2u
+#define GKRT_MAX_TEXTURES    4096u
 
 /* Images owned by the context (formats: FP32x4 unless stated). */
 #define GKRT_IMG_SINGLE_DIFFUSE    0
@@ -363,6 +381,14 @@ int  gkrt_copy_image_to_host(GkrtContext* ctx, int image_id, void* dst, size_t d
  * (VulkanBaseRenderer.cpp:727-869). */
 int  gkrt_copy_image_to_host_async(GkrtContext* ctx, int image_id, void* dst, size_t dst_bytes, void* stream);
 int  gkrt_upload_image(GkrtContext* ctx, int image_id, const void* src, size_t src_bytes, void* stream);
+
+/* Texture `texture_id` (< GKRT_MAX_TEXTURES) of width x height texels (rows first to last, 4
+ * channels in `format`, bytes = width * height * texel size), replacing an earlier texture of
+ * that id. Materials name textures by id (diffuse, MRA, normal map); the sky by
+ * GkrtFrameConstants.sky_index. An id without a texture samples as opaque white. Synchronous.
+ * (GlobalTexturePool::CreateTextureImage / TextureImage, src/Assets/Texture.cpp:380-620.) */
+int  gkrt_texture_upload(GkrtContext* ctx, uint32_t texture_id, uint32_t width, uint32_t height, uint32_t format,
+                         const void* texels, size_t bytes);
 
 /* Ray queries on the scene's BVH (FHardwareRayTracerV2::TraceRay / TraceOcclusion,
  * assets/shaders/common/Shading.slang:737-826). rays/hits are device pointers. A ray reports

@@ -159,6 +159,15 @@ struct OScene {
     std::vector<float> emit;
     std::vector<float> emit_thr;
     std::vector<uint32_t> emit_alias;
+    // textured materials: per-vertex texture coordinates and tangents (empty: all zero), and the
+    // texture pool by id (RGBA float texels as the sampler returns them)
+    std::vector<f2> uv;
+    std::vector<f4> tan;
+    struct Tex {
+        uint32_t w = 0, h = 0;
+        std::vector<f4> t;
+    };
+    std::vector<Tex> tex;
 };
 
 // 0: every candidate triangle is decided by the FP64 test (the definition itself).
@@ -278,6 +287,9 @@ struct Vtx {
     f3 P, N;
     uint32_t mat;
     uint32_t inst;   // instance index
+    f2 uv;           // texture coordinates at the hit
+    f3 ln;           // object-space normal mix (the LocalNormal of the texture path)
+    f4 lt;           // object-space tangent mix, w the packed handedness (LocalTangent)
 };
 
 const GkrtMaterial& get_mat(const OScene& S, uint32_t i) {
@@ -306,8 +318,54 @@ bool trace_ray(const OScene& S, f3 o, f3 d, float tmax, Vtx& out, uint32_t* out_
     out.P = fma3(d, hh.t, o);
     out.mat = in.mat_id[S.slot[vi[0]] & 15u];
     out.inst = h.inst;
+    // the texture path's vertex attributes, each the same barycentric mix
+    out.ln = nobj;
+    out.uv = f2{0.0f, 0.0f};
+    out.lt = f4{0.0f, 0.0f, 0.0f, 0.0f};
+    if (!S.uv.empty()) {
+        const f2 a = S.uv[vi[0]], b = S.uv[vi[1]], c = S.uv[vi[2]];
+        out.uv = f2{fma_(c.x - a.x, hh.b2, fma_(b.x - a.x, hh.b1, a.x)), fma_(c.y - a.y, hh.b2, fma_(b.y - a.y, hh.b1, a.y))};
+    }
+    if (!S.tan.empty()) {
+        f4 a = S.tan[vi[0]], b = S.tan[vi[1]], c = S.tan[vi[2]];
+        // the vertex packing of the handedness (MakeVertex, Vertex.hpp:97): 2 when positive, else 0
+        a.w = a.w > 0.0f ? 2.0f : 0.0f;
+        b.w = b.w > 0.0f ? 2.0f : 0.0f;
+        c.w = c.w > 0.0f ? 2.0f : 0.0f;
+        out.lt = f4{fma_(c.x - a.x, hh.b2, fma_(b.x - a.x, hh.b1, a.x)), fma_(c.y - a.y, hh.b2, fma_(b.y - a.y, hh.b1, a.y)),
+                    fma_(c.z - a.z, hh.b2, fma_(b.z - a.z, hh.b1, a.z)), fma_(c.w - a.w, hh.b2, fma_(b.w - a.w, hh.b1, a.w))};
+    }
     if (out_prim) *out_prim = h.prim;
     return true;
+}
+
+// ---- textures: the pool's sampler at level 0 (Sampler.hpp:9-27, TextureImage.cpp:24-31):
+// Vulkan's linear filter with repeat addressing; weights in FP32 in one fixed order ----
+uint32_t wrap_repeat(float f, uint32_t n) {
+    float m = std::fmod(f, (float)n);
+    if (m < 0.0f) m = m + (float)n;
+    const uint32_t i = (uint32_t)m;
+    return i < n ? i : 0u;
+}
+f4 tex_sample(const OScene& S, int id, float u, float v) {
+    const f4 white{1.0f, 1.0f, 1.0f, 1.0f};
+    if (id < 0 || (size_t)id >= S.tex.size() || S.tex[id].t.empty()) return white;
+    const OScene::Tex& t = S.tex[id];
+    float x = fma_(u, (float)t.w, -0.5f), y = fma_(v, (float)t.h, -0.5f);
+    if (!(std::fabs(x) < 1e30f)) x = -0.5f;
+    if (!(std::fabs(y) < 1e30f)) y = -0.5f;
+    const float fx = std::floor(x), fy = std::floor(y);
+    const float a = x - fx, b = y - fy;
+    const uint32_t x0 = wrap_repeat(fx, t.w), x1 = wrap_repeat(fx + 1.0f, t.w);
+    const uint32_t y0 = wrap_repeat(fy, t.h), y1 = wrap_repeat(fy + 1.0f, t.h);
+    const float ia = 1.0f - a, ib = 1.0f - b;
+    const float w00 = ia * ib, w10 = a * ib, w01 = ia * b, w11 = a * b;
+    const f4 t00 = t.t[(size_t)y0 * t.w + x0], t10 = t.t[(size_t)y0 * t.w + x1];
+    const f4 t01 = t.t[(size_t)y1 * t.w + x0], t11 = t.t[(size_t)y1 * t.w + x1];
+    return f4{fma_(t11.x, w11, fma_(t01.x, w01, fma_(t10.x, w10, t00.x * w00))),
+              fma_(t11.y, w11, fma_(t01.y, w01, fma_(t10.y, w10, t00.y * w00))),
+              fma_(t11.z, w11, fma_(t01.z, w01, fma_(t10.z, w10, t00.z * w00))),
+              fma_(t11.w, w11, fma_(t01.w, w01, fma_(t10.w, w10, t00.w * w00)))};
 }
 
 bool trace_occlusion(const OScene& S, f3 o, f3 d, uint64_t* rays) {
@@ -494,6 +552,40 @@ f4 sky_color(const GkrtFrameConstants& fc) {
     return scale4(c, fc.sky_intensity);
 }
 
+// A sky miss in direction dir: SampleIBLV2 (Shading.slang:194-199) on texture sky_index when
+// the frame asks for it (d = normalize(dir), t = ((atan2(d.x, d.z) + pi rotate) / 2pi,
+// acos(d.y) / pi), min((10, 10, 10, 1), sample) x SkyIntensity), else the constant colour.
+f4 sky_dir(const OScene& S, const GkrtFrameConstants& fc, f3 dir) {
+    if (!fc.has_sky || !(fc.flags & GKRT_FRAME_SKY_TEXTURE)) return sky_color(fc);
+    const f3 d = normalize3(dir);
+    const float u = (atan2_(d.x, d.z) + 3.14159274f * fc.sky_rotation) * 0.159154937f;
+    const float v = acos_(d.y) * 0.318309873f;
+    const f4 c = tex_sample(S, (int)fc.sky_index, u, v);
+    return scale4(f4{fmin_(10.0f, c.x), fmin_(10.0f, c.y), fmin_(10.0f, c.z), fmin_(1.0f, c.w)}, fc.sky_intensity);
+}
+
+// FetchGBufferV2 (Shading.slang:82-112) for the primary vertex: albedo = diffuse x diffuse
+// texture, roughness = fuzziness x the MRA texture's green channel, and the normal map through
+// mikkTSpace (:74-80) on the vertex's local normal and tangent (the barycentric mixes the
+// visibility-buffer caster computes, GeneralFunc.slang:51-52), carried to world space by the
+// instance transform and normalized.
+void fetch_gbuffer(const OScene& S, const GkrtMaterial& m, Vtx& v, f4& albedo, float& rough) {
+    albedo = f4{m.diffuse[0], m.diffuse[1], m.diffuse[2], m.diffuse[3]};
+    if (m.diffuse_texture_id >= 0) albedo = mul4(albedo, tex_sample(S, m.diffuse_texture_id, v.uv.x, v.uv.y));
+    rough = m.fuzziness;
+    if (m.mra_texture_id >= 0) rough = rough * tex_sample(S, m.mra_texture_id, v.uv.x, v.uv.y).y;
+    if (m.normal_texture_id >= 0) {
+        const f4 t = tex_sample(S, m.normal_texture_id, v.uv.x, v.uv.y);
+        const f3 vn{fma_(t.x, 2.0f, -1.0f), fma_(t.y, 2.0f, -1.0f), fma_(t.z, 2.0f, -1.0f)};
+        const f3 T{v.lt.x, v.lt.y, v.lt.z};
+        const f3 B = mul(cross3(v.ln, T), v.lt.w);
+        const f3 nl = normalize3(f3{fma_(vn.z, v.ln.x, fma_(vn.y, B.x, vn.x * T.x)),
+                                    fma_(vn.z, v.ln.y, fma_(vn.y, B.y, vn.x * T.y)),
+                                    fma_(vn.z, v.ln.z, fma_(vn.y, B.z, vn.x * T.z))});
+        v.N = normalize3(xform_vector(S.inst[v.inst].world, nl));
+    }
+}
+
 // Emissive-triangle NEE (GKRT_NEE_EMISSIVE, no counterpart in the built reference path; the
 // estimator of the legacy area-light branch, Scatter.glsl:55-76, with the alias-table pick
 // of the light). Samples one point for vertex (P, N) with throughput rc; false when the
@@ -580,6 +672,7 @@ bool get_ray_color(const OScene& S, const GkrtFrameConstants& fc, Vtx& v, f3& di
             return true;
         }
         f4 alb{hm.diffuse[0], hm.diffuse[1], hm.diffuse[2], hm.diffuse[3]};
+        if (hm.diffuse_texture_id >= 0) alb = mul4(alb, tex_sample(S, hm.diffuse_texture_id, v.uv.x, v.uv.y));
         if (hm.material_model == GKRT_MAT_DIFFUSE_LIGHT || !chanceReflect) color = mul4(color, alb);
         if (back && !diel) {
             color = f4{0.5f, 0.5f, 0.5f, 0.0f};
@@ -588,7 +681,7 @@ bool get_ray_color(const OScene& S, const GkrtFrameConstants& fc, Vtx& v, f3& di
         if (hm.material_model == GKRT_MAT_DIFFUSE_LIGHT) return true;
         return false;
     }
-    color = mul4(color, sky_color(fc));
+    color = mul4(color, sky_dir(S, fc, tdir));
     return true;
 }
 
@@ -640,7 +733,7 @@ void shade_pixel(const OScene& S, const GkrtFrameConstants& fc, int W, int H, in
     uint32_t* oid = (uint32_t*)im[GKRT_IMG_OBJECT_ID];
     uint32_t* mom = (uint32_t*)im[GKRT_IMG_MOTION_MOMENT];
     if (!hit) {
-        f4 sky = sky_color(fc);
+        f4 sky = sky_dir(S, fc, primDir);
         sd[0] = sky.x; sd[1] = sky.y; sd[2] = sky.z; sd[3] = sky.w;
         mot[0] = 0.0f; mot[1] = 0.0f;
         alb[0] = alb[1] = alb[2] = alb[3] = 1.0f;
@@ -665,9 +758,11 @@ void shade_pixel(const OScene& S, const GkrtFrameConstants& fc, int W, int H, in
     else mom[pix] = mom[pix] > 0u ? mom[pix] - 1u : 0u;
     float mx = pfx - cfx, my = pfy - cfy;
     const GkrtMaterial& pmat = get_mat(S, pv.mat);
-    f4 primaryAlbedo{pmat.diffuse[0], pmat.diffuse[1], pmat.diffuse[2], pmat.diffuse[3]};
+    f4 primaryAlbedo;
+    float proughness;
+    fetch_gbuffer(S, pmat, pv, primaryAlbedo, proughness);
     alb[0] = primaryAlbedo.x; alb[1] = primaryAlbedo.y; alb[2] = primaryAlbedo.z; alb[3] = primaryAlbedo.w;
-    nrm[0] = pv.N.x; nrm[1] = pv.N.y; nrm[2] = pv.N.z; nrm[3] = pmat.fuzziness;
+    nrm[0] = pv.N.x; nrm[1] = pv.N.y; nrm[2] = pv.N.z; nrm[3] = proughness;
     oid[pix] = pin.instance_id;
     mot[0] = mx * (float)W; mot[1] = my * (float)H;
     ((float*)im[GKRT_IMG_PREV_DEPTH])[pix] = ndcDepth;
@@ -1696,6 +1791,35 @@ static void output_fsr_o(const float* src, int W, int H, int P, uint32_t* out, i
 // ===================================== C API ==========================================
 extern "C" {
 
+// Texture `id` of the oracle scene: texels as the sampler returns them (RGBA8 UNORM c / 255;
+// sRGB through the sRGB transfer function in double; RGBA32F as given). 0 on success.
+int gko_texture_upload(void* h, uint32_t id, uint32_t w, uint32_t ht, uint32_t format, const void* texels) {
+    OScene* S = static_cast<OScene*>(h);
+    if (id >= GKRT_MAX_TEXTURES || !w || !ht || format > GKRT_TEX_RGBA32F || !texels) return -1;
+    if (S->tex.size() <= id) S->tex.resize(id + 1);
+    OScene::Tex& t = S->tex[id];
+    t.w = w;
+    t.h = ht;
+    const size_t n = (size_t)w * ht;
+    t.t.resize(n);
+    if (format == GKRT_TEX_RGBA32F) {
+        std::memcpy(t.t.data(), texels, n * 16);
+        return 0;
+    }
+    const uint8_t* b = static_cast<const uint8_t*>(texels);
+    auto unorm = [](uint8_t c) { return (float)c / 255.0f; };
+    auto srgb = [](uint8_t c) {
+        const double v = (double)c / 255.0;
+        return (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+    };
+    for (size_t i = 0; i < n; ++i) {
+        const uint8_t* c = b + 4 * i;
+        t.t[i] = format == GKRT_TEX_RGBA8_SRGB ? f4{srgb(c[0]), srgb(c[1]), srgb(c[2]), unorm(c[3])}
+                                               : f4{unorm(c[0]), unorm(c[1]), unorm(c[2]), unorm(c[3])};
+    }
+    return 0;
+}
+
 void* gko_scene_create(const GkrtSceneDesc* d) {
     OScene* S = new OScene();
     S->pos.resize(d->vertex_count);
@@ -1704,6 +1828,15 @@ void* gko_scene_create(const GkrtSceneDesc* d) {
     for (uint32_t i = 0; i < d->vertex_count; ++i) {
         S->pos[i] = f3{d->positions[4 * i], d->positions[4 * i + 1], d->positions[4 * i + 2]};
         S->nrm[i] = f3{d->normals[4 * i], d->normals[4 * i + 1], d->normals[4 * i + 2]};
+    }
+    if (d->texcoords) {
+        S->uv.resize(d->vertex_count);
+        for (uint32_t i = 0; i < d->vertex_count; ++i) S->uv[i] = f2{d->texcoords[2 * i], d->texcoords[2 * i + 1]};
+    }
+    if (d->tangents) {
+        S->tan.resize(d->vertex_count);
+        for (uint32_t i = 0; i < d->vertex_count; ++i)
+            S->tan[i] = f4{d->tangents[4 * i], d->tangents[4 * i + 1], d->tangents[4 * i + 2], d->tangents[4 * i + 3]};
     }
     S->idx.assign(d->indices, d->indices + d->index_count);
     S->meshes.assign(d->meshes, d->meshes + d->mesh_count);

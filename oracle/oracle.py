@@ -74,6 +74,7 @@ def lib():
         L.gko_probe_voxelize.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int]
         L.gko_probe_bake.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, C.c_uint32,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.gko_texture_upload.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
         L.gko_exact_tri.restype = C.c_int
         L.gko_fp32_tri.restype = C.c_int
         _lib = L
@@ -102,6 +103,10 @@ class OracleScene:
         self.scene = scene
         self._desc = scene.desc()
         self.h = lib().gko_scene_create(C.byref(self._desc))
+        for tid, (fmt, texels) in sorted(getattr(scene, "textures", {}).items()):
+            t = abi.texel_buffer(fmt, texels)
+            if lib().gko_texture_upload(self.h, tid, t.shape[1], t.shape[0], fmt, t.ctypes.data) != 0:
+                raise ValueError(f"texture {tid} rejected by the oracle")
 
     def close(self):
         if self.h:

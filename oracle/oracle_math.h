@@ -42,6 +42,10 @@ static inline f3 normalize3(f3 a) {
 }
 // v * s + o, one fma per component
 static inline f3 fma3(f3 v, float s, f3 o) { return f3{fma_(v.x, s, o.x), fma_(v.y, s, o.y), fma_(v.z, s, o.z)}; }
+// cross(a, b): each component fma(p, q, -(r * s))
+static inline f3 cross3(f3 a, f3 b) {
+    return f3{fma_(a.y, b.z, -(a.z * b.y)), fma_(a.z, b.x, -(a.x * b.z)), fma_(a.x, b.y, -(a.y * b.x))};
+}
 
 // reflect(d, n) = d - 2 dot(n, d) n  ->  fma(-k, n, d), k = 2 dot(n, d)
 static inline f3 reflect3(f3 d, f3 n) {
@@ -141,6 +145,37 @@ static inline void sincos_2pi(float u, float* s, float* c) {
     else if (qi == 1) { *s = cp; *c = -sp; }
     else if (qi == 2) { *s = -sp; *c = -cp; }
     else { *s = -cp; *c = sp; }
+}
+
+// atan on [0, 1]: above tan(pi/12) reduced by atan(a) = pi/6 + atan((a sqrt3 - 1) / (a + sqrt3)),
+// then the Taylor series x - x^3/3 + ... - x^15/15 (Horner with fma); atan2 by octant fix-ups;
+// acos(x) = atan2(sqrt((1 - x)(1 + x)), x). The sky lookup of the shading (SampleIBLV2)
+// uses these on both sides of the parity check.
+static inline float atan01(float a) {
+    const bool red = a > 0.267949194f;                                  // tan(pi/12)
+    const float x = red ? fma_(a, 1.73205081f, -1.0f) / (a + 1.73205081f) : a;
+    const float x2 = x * x;
+    float p = fma_(x2, -6.66666701e-02f, 7.69230798e-02f);
+    p = fma_(x2, p, -9.09090936e-02f);
+    p = fma_(x2, p, 1.11111112e-01f);
+    p = fma_(x2, p, -1.42857149e-01f);
+    p = fma_(x2, p, 2.00000003e-01f);
+    p = fma_(x2, p, -3.33333343e-01f);
+    const float r = fma_(x * x2, p, x);
+    return red ? r + 0.523598790f : r;
+}
+static inline float atan2_(float y, float x) {
+    const float ax = std::fabs(x), ay = std::fabs(y);
+    if (!(ax > 0.0f) && !(ay > 0.0f)) return 0.0f;
+    const bool swap = ay > ax;
+    float r = atan01(swap ? ax / ay : ay / ax);
+    if (swap) r = 1.57079637f - r;
+    if (x < 0.0f) r = 3.14159274f - r;
+    return y < 0.0f ? -r : r;
+}
+static inline float acos_(float x) {
+    const float s = std::sqrt(fmax_((1.0f - x) * (1.0f + x), 0.0f));
+    return atan2_(s, x);
 }
 
 }  // namespace gko

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol(gkrt_lib):
 
 
 def test_abi_version(gkrt_lib):
-    assert native.load().gkrt_abi_version() == 1
+    assert native.load().gkrt_abi_version() == 2
 
 
 def test_struct_layouts_match_c(tmp_path):

@@ -271,12 +271,12 @@ def test_errors_are_status_codes(cornell_env):
         r.update_instances(bad)
     assert e.value.code == abi.GKRT_ERR_INVALID_ARG
     tex = sc.materials.copy()
-    tex["diffuse_texture_id"][0] = 3
+    tex["diffuse_texture_id"][0] = abi.MAX_TEXTURES   # outside the texture pool
     sc2 = abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, tex, sc.instances)
     r2 = PathTracingRenderer(0)
     with pytest.raises(GkrtError) as e:
         r2.load_scene(sc2)
-    assert e.value.code == abi.GKRT_ERR_UNSUPPORTED
+    assert e.value.code == abi.GKRT_ERR_INVALID_ARG
     nanpos = sc.positions.copy()
     nanpos[0, 0] = np.nan
     sc3 = abi.SceneArrays(nanpos, sc.normals, sc.material_slots, sc.indices, sc.meshes, sc.materials, sc.instances)
