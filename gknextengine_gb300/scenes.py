@@ -479,3 +479,95 @@ def cornell_materials(seed: int = 4, tiles: int = 16, width: int = 512, height: 
     cam = Camera(eye=(0.0, 0.5, 1.94), center=(0.0, 0.5, 0.0), fov_deg=40.0)
     settings = Settings(samples=spp, bounces=4, max_bounces=4, taa=False)
     return scene, cam, settings
+
+
+def planar_attributes(pos: np.ndarray, nrm: np.ndarray, tiles: float = 2.0):
+    """Texture coordinates and tangents for axis-aligned geometry: each vertex projects onto the
+    two axes across its normal's dominant axis (u along the first, scaled by `tiles`); the
+    tangent runs along u, its w the sign of the normal's dominant component (so both
+    handedness cases occur)."""
+    p = np.asarray(pos, np.float64)[:, :3]
+    n = np.asarray(nrm, np.float64)[:, :3]
+    k = np.argmax(np.abs(n), axis=1)
+    a = (k + 1) % 3
+    b = (k + 2) % 3
+    r = np.arange(p.shape[0])
+    uv = np.stack([p[r, a] * tiles, p[r, b] * tiles], axis=1).astype(np.float32)
+    tan = np.zeros((p.shape[0], 4), np.float32)
+    tan[r, a] = 1.0
+    tan[:, 3] = np.where(n[r, k] > 0, 1.0, -1.0)
+    return uv, tan
+
+
+def procedural_textures(seed: int = 3, size: int = 32):
+    """Test textures: an sRGB checker with coloured noise (RGBA8), a linear RGBA32F gradient, an
+    MRA map (RGBA8 UNORM, green = roughness), a tangent-space normal map of round bumps (RGBA8
+    UNORM) and an equirectangular HDR sky (RGBA32F, 64 x 32) with a sun above the clamp of 10."""
+    rng = np.random.default_rng(seed)
+    s = size
+    y, x = np.mgrid[0:s, 0:s]
+    chk = ((x // 4 + y // 4) % 2).astype(np.float64)
+    col = np.zeros((s, s, 4), np.uint8)
+    col[..., :3] = np.clip(40 + 180 * chk[..., None] + rng.integers(0, 35, (s, s, 3)), 0, 255)
+    col[..., 3] = 255
+    grad = np.zeros((s, s, 4), np.float32)
+    grad[..., 0] = x / (s - 1)
+    grad[..., 1] = y / (s - 1)
+    grad[..., 2] = 0.3 + 0.4 * np.sin(x * 0.7) ** 2
+    grad[..., 3] = 1.0
+    mra = np.zeros((s, s, 4), np.uint8)
+    mra[..., 1] = np.clip(30 + 220 * ((x * 7 + y * 3) % s) / s, 0, 255)
+    mra[..., 2] = 128
+    mra[..., 3] = 255
+    cx, cy = (x % 8) - 3.5, (y % 8) - 3.5
+    h = np.exp(-(cx * cx + cy * cy) / 6.0)
+    nx, ny = -cx * h * 0.4, -cy * h * 0.4
+    nz = np.sqrt(np.maximum(1.0 - nx * nx - ny * ny, 0.0))
+    nmap = np.zeros((s, s, 4), np.uint8)
+    nmap[..., 0] = np.round((nx * 0.5 + 0.5) * 255)
+    nmap[..., 1] = np.round((ny * 0.5 + 0.5) * 255)
+    nmap[..., 2] = np.round((nz * 0.5 + 0.5) * 255)
+    nmap[..., 3] = 255
+    sy, sx = np.mgrid[0:32, 0:64]
+    sky = np.zeros((32, 64, 4), np.float32)
+    sky[..., 0] = 0.3 + 0.5 * (1 - sy / 31)
+    sky[..., 1] = 0.4 + 0.4 * (1 - sy / 31)
+    sky[..., 2] = 0.6 + 0.3 * np.cos(sx / 63 * 2 * np.pi) ** 2
+    sun = np.exp(-(((sx - 20) ** 2) + ((sy - 9) ** 2)) / 3.0)
+    sky[..., :3] += 40.0 * sun[..., None]
+    sky[..., 3] = 1.0
+    return {"checker": (abi.TEX_RGBA8_SRGB, col), "gradient": (abi.TEX_RGBA32F, grad),
+            "mra": (abi.TEX_RGBA8_UNORM, mra), "normal": (abi.TEX_RGBA8_UNORM, nmap), "sky": (abi.TEX_RGBA32F, sky)}
+
+
+def cornell_textured(seed: int = 1):
+    """The C1 Cornell box with textured materials and an HDR sky: left wall an sRGB checker,
+    back wall a float gradient, floor a GGX mixture with an MRA map and a normal map, the tall
+    box the checker and the normal map, the short box a metal with the gradient (textured
+    primary albedo on metallic paths), the ceiling an id with no texture (white). Texture ids:
+    checker 5, gradient 6, MRA 7, normal 8, missing 9, sky 2. The sky texture is on with a
+    rotation; the camera sits farther out so that camera rays and bounces reach the sky.
+    Returns (SceneArrays, Camera, Settings)."""
+    sc, cam, st = cornell(seed)
+    uv, tan = planar_attributes(sc.positions, sc.normals)
+    t = procedural_textures(seed + 2)
+    mats = sc.materials.copy()
+    mats[0]["diffuse_texture_id"] = 5
+    mats[2]["diffuse_texture_id"] = 6
+    mats[3] = mixture((0.8, 0.75, 0.7), 0.6)
+    mats[3]["mra_texture_id"] = 7
+    mats[3]["normal_texture_id"] = 8
+    mats[4]["diffuse_texture_id"] = 9
+    mats[5]["diffuse_texture_id"] = 5
+    mats[5]["normal_texture_id"] = 8
+    mats[6] = metallic((0.9, 0.8, 0.6), 0.3)
+    mats[6]["diffuse_texture_id"] = 6
+    textures = {5: t["checker"], 6: t["gradient"], 7: t["mra"], 8: t["normal"], 2: t["sky"]}
+    sc = abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, mats, sc.instances,
+                         lights=sc.lights, name="cornell-textured", texcoords=uv, tangents=tan, textures=textures)
+    cam = Camera(eye=(0.3, 0.6, 1.6), center=(0.0, 0.45, 0.0), fov_deg=42.0)
+    st.has_sky = True
+    st.sky_intensity = 0.7
+    st.sky_texture = 2
+    st.sky_rotation = 0.3
+    return sc, cam, st

@@ -1791,6 +1791,18 @@ static void output_fsr_o(const float* src, int W, int H, int P, uint32_t* out, i
 // ===================================== C API ==========================================
 extern "C" {
 
+float gko_atan2(float y, float x) { return atan2_(y, x); }
+float gko_acos(float x) { return acos_(x); }
+// The oracle's texture lookup and sky radiance, for their tests.
+void gko_tex_sample(void* h, int id, float u, float v, float* out) {
+    const f4 c = tex_sample(*static_cast<OScene*>(h), id, u, v);
+    out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
+}
+void gko_sky_dir(void* h, const GkrtFrameConstants* fc, const float* dir, float* out) {
+    const f4 c = sky_dir(*static_cast<OScene*>(h), *fc, f3{dir[0], dir[1], dir[2]});
+    out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
+}
+
 // Texture `id` of the oracle scene: texels as the sampler returns them (RGBA8 UNORM c / 255;
 // sRGB through the sRGB transfer function in double; RGBA32F as given). 0 on success.
 int gko_texture_upload(void* h, uint32_t id, uint32_t w, uint32_t ht, uint32_t format, const void* texels) {

@@ -75,6 +75,12 @@ def lib():
         L.gko_probe_bake.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_uint32, C.c_uint32,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.gko_texture_upload.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
+        L.gko_atan2.argtypes = [C.c_float, C.c_float]
+        L.gko_atan2.restype = C.c_float
+        L.gko_acos.argtypes = [C.c_float]
+        L.gko_acos.restype = C.c_float
+        L.gko_tex_sample.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_void_p]
+        L.gko_sky_dir.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_void_p, C.c_void_p]
         L.gko_exact_tri.restype = C.c_int
         L.gko_fp32_tri.restype = C.c_int
         _lib = L
@@ -118,6 +124,17 @@ class OracleScene:
             self.close()
         except Exception:
             pass
+
+    def tex_sample(self, texture_id: int, u: float, v: float) -> np.ndarray:
+        out = np.zeros(4, np.float32)
+        lib().gko_tex_sample(self.h, texture_id, C.c_float(u), C.c_float(v), out.ctypes.data)
+        return out
+
+    def sky_dir(self, fc, d) -> np.ndarray:
+        dd = np.ascontiguousarray(d, np.float32)
+        out = np.zeros(4, np.float32)
+        lib().gko_sky_dir(self.h, C.byref(fc), dd.ctypes.data, out.ctypes.data)
+        return out
 
     def trace_rays(self, rays: np.ndarray, mode: int = abi.TRACE_CLOSEST, brute: bool = False,
                    threads: int = 0) -> np.ndarray:
