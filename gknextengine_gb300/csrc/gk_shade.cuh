@@ -189,7 +189,7 @@ static __device__ __noinline__ HitAttr hit_attr(const ShadeScene& sc, f3 o, f3 d
 // the mesh's tangent frame (mikkTSpace, :74-80) carried to world space by the instance's
 // transform. The traced camera ray of the reference leaves the vertex's local normal and
 // tangent unset; here they are the barycentric mixes of the vertex attributes, as the
-// visibility-buffer caster computes them (GeneralFunc.slang:51-52).
+// visibility-buffer caster computes them (GeneralFunc.slang:49-51).
 struct GBufTex {
     f4 albedo;
     float rough;
@@ -233,6 +233,41 @@ struct ProbeLight {
     float area;
     int valid;
 };
+
+// The sky texture's nine-term spherical-harmonic projection per colour channel (ProjectHdrToSh,
+// Texture.cpp:180-254; computed by the host at texture upload, zero for 8-bit textures as the
+// reference projects HDR loads only), which the probe bake evaluates for its sky misses
+// (SampleIBLRough, Shading.slang:188-192). on = 0: the frame has no sky texture and the bake
+// sees the constant sky colour.
+struct SkySH {
+    float c[27];   // red terms 0..8, green 9..17, blue 18..26
+    int on;
+};
+// EvaluateSH (Shading.slang:150-186) at direction n with SampleIBLRough's rotation
+// 1 - SkyRotation about y, as (rgb, 1) times (HasSky ? SkyIntensity : 0).
+GK_D f4 sky_sh(const SkySH& s, const GkrtFrameConstants& fc, f3 n) {
+    float sn, cs;
+    sincos2pi((1.0f - fc.sky_rotation) * 0.5f, sn, cs);   // angle (1 - rotate) pi
+    const float rx = n.x * cs + n.z * sn, ry = n.y, rz = -n.x * sn + n.z * cs;
+    float b[9];
+    b[0] = 0.282095f;
+    b[1] = -0.488603f * ry;
+    b[2] = 0.488603f * rz;
+    b[3] = -0.488603f * rx;
+    b[4] = (1.092548f * rx) * ry;
+    b[5] = (-1.092548f * ry) * rz;
+    b[6] = 0.315392f * ((3.0f * ry) * ry - 1.0f);
+    b[7] = (-1.092548f * rx) * rz;
+    b[8] = 0.546274f * (rx * rx - rz * rz);
+    float r = 0.0f, g = 0.0f, bl = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        r = r + s.c[i] * b[i];
+        g = g + s.c[9 + i] * b[i];
+        bl = bl + s.c[18 + i] * b[i];
+    }
+    return F4(r, g, bl, 1.0f) * (fc.has_sky ? fc.sky_intensity : 0.0f);
+}
 GK_D f4 unpack10(uint32_t p) {
     float r = div_((float)(p & 0x3FFu), 1023.0f), g = div_((float)((p >> 10) & 0x3FFu), 1023.0f),
           b = div_((float)((p >> 20) & 0x3FFu), 1023.0f);

@@ -122,6 +122,9 @@ struct GkrtContext {
     // read (GKRT_MAX_TEXTURES entries, null texels for an id without a texture)
     std::vector<float4*> tex_buf;
     DevTex* d_tex = nullptr;
+    // per texture id the nine-term spherical-harmonic projection of an RGBA32F texture (27
+    // floats, see project_sky_sh), zero for 8-bit textures; empty until the first HDR upload
+    std::vector<float> tex_sh;
 
     Unet* unet = nullptr;                       // learned denoiser (gkrt_unet_init)
     unsigned long long* d_counters = nullptr;   // see Counters (gk_trace.cuh): 6 per-pass slots + total rays
@@ -761,6 +764,40 @@ float srgb8(uint8_t c) {
     return (float)(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
 }
 
+// ProjectHdrToSh (Texture.cpp:180-254): the equirectangular image projected on the nine real
+// spherical harmonics of bands 0-2, texel (x, y) at theta = (y + 1/2) pi / h, phi = (x + 1/2)
+// 2 pi / w, direction (sin theta cos phi, cos theta, sin theta sin phi), weighted by its solid
+// angle sin theta (pi / h)(2 pi / w), unnormalised. Accumulated in double in row-major texel
+// order and rounded to float once (the reference sums in float).
+void project_sky_sh(const float4* t, uint32_t w, uint32_t h, float out[27]) {
+    const double pi = 3.14159265358979323846;
+    const double c0 = 0.282095, c1 = 0.488603, c2 = 1.092548, c3 = 0.315392, c4 = 0.546274;
+    double acc[27] = {0.0};
+    std::vector<double> sp(w), cp(w);
+    for (uint32_t x = 0; x < w; ++x) {
+        const double phi = ((double)x + 0.5) / (double)w * (2.0 * pi);
+        sp[x] = std::sin(phi);
+        cp[x] = std::cos(phi);
+    }
+    for (uint32_t y = 0; y < h; ++y) {
+        const double theta = ((double)y + 0.5) / (double)h * pi;
+        const double st = std::sin(theta), ct = std::cos(theta);
+        const double wt = st * (pi / (double)h) * (2.0 * pi / (double)w);
+        for (uint32_t x = 0; x < w; ++x) {
+            const double dx = st * cp[x], dy = ct, dz = st * sp[x];
+            const double b[9] = {c0, -c1 * dy, c1 * dz, -c1 * dx, c2 * dx * dy, -c2 * dy * dz,
+                                 c3 * (3.0 * dy * dy - 1.0), -c2 * dx * dz, c4 * (dx * dx - dz * dz)};
+            const float4 v = t[(size_t)y * w + x];
+            for (int i = 0; i < 9; ++i) {
+                acc[i] += (double)v.x * b[i] * wt;
+                acc[9 + i] += (double)v.y * b[i] * wt;
+                acc[18 + i] += (double)v.z * b[i] * wt;
+            }
+        }
+    }
+    for (int k = 0; k < 27; ++k) out[k] = (float)acc[k];
+}
+
 int check_frame(GkrtContext* ctx, const GkrtFrameConstants* fc) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (!fc) return fail(ctx, GKRT_ERR_INVALID_ARG, "null frame constants");
@@ -1149,6 +1186,12 @@ int gkrt_texture_upload(GkrtContext* ctx, uint32_t texture_id, uint32_t width, u
     }
     dfree(ctx->tex_buf[texture_id]);
     ctx->tex_buf[texture_id] = d;
+    if (format == GKRT_TEX_RGBA32F || !ctx->tex_sh.empty()) {
+        if (ctx->tex_sh.empty()) ctx->tex_sh.assign((size_t)GKRT_MAX_TEXTURES * 27u, 0.0f);
+        float* c = ctx->tex_sh.data() + (size_t)texture_id * 27u;
+        if (format == GKRT_TEX_RGBA32F) project_sky_sh(t.data(), width, height, c);
+        else std::fill(c, c + 27, 0.0f);
+    }
     return GKRT_OK;
 }
 
@@ -1483,6 +1526,8 @@ int gkrt_probe_bake(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t fir
     if (!ctx->d_cubes || !ctx->d_voxels)
         return fail(ctx, GKRT_ERR_STATE, "no probe grid: upload one or call gkrt_probe_voxelize");
     if ((size_t)first + count > kProbeCount) return fail(ctx, GKRT_ERR_INVALID_ARG, "probe range outside the grid");
+    if ((fc->flags & GKRT_FRAME_SKY_TEXTURE) && fc->sky_index >= GKRT_MAX_TEXTURES)
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "sky_index outside the texture pool");
     DeviceGuard device_guard(ctx->device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = ensure_bvh(ctx, 0, st);
@@ -1505,7 +1550,14 @@ int gkrt_probe_bake(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32_t fir
         lt.valid = 1;
     }
     GK_CUDA(cudaMemsetAsync(ctx->d_counters, 0, 6 * sizeof(unsigned long long), st));
-    GK_CUDA(gkrt_launch_probe_bake(shade_scene(ctx), *fc, lt, first, count, ctx->d_cubes_prev, ctx->d_cubes,
+    SkySH sh;
+    std::memset(&sh, 0, sizeof(sh));
+    if (fc->flags & GKRT_FRAME_SKY_TEXTURE) {
+        sh.on = 1;
+        if (!ctx->tex_sh.empty())
+            std::memcpy(sh.c, ctx->tex_sh.data() + (size_t)fc->sky_index * 27u, sizeof(sh.c));
+    }
+    GK_CUDA(gkrt_launch_probe_bake(shade_scene(ctx), *fc, lt, sh, first, count, ctx->d_cubes_prev, ctx->d_cubes,
                                    (uint4*)ctx->d_voxels, ctx->d_counters, st));
     return GKRT_OK;
 }
@@ -1578,6 +1630,8 @@ static int adjoint_checks(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32
     if (fc->number_of_bounces > 16 || fc->max_number_of_bounces > 16)
         return fail(ctx, GKRT_ERR_UNSUPPORTED, "the adjoint records at most 16 bounces");
     if (ctx->nmat > 8192) return fail(ctx, GKRT_ERR_UNSUPPORTED, "the adjoint sums at most 8192 materials per block");
+    if (ctx->textured || (fc->flags & GKRT_FRAME_SKY_TEXTURE))
+        return fail(ctx, GKRT_ERR_UNSUPPORTED, "the adjoint covers untextured scenes under the constant sky");
     return GKRT_OK;
 }
 

@@ -14,6 +14,7 @@ struct SceneView;
 struct BvhNode;
 struct WideNode;
 struct ProbeLight;
+struct SkySH;
 
 // Launch-geometry and attribute caches of the launchers are kept per device (a process may
 // drive several GPUs): the current device's slot, or -1 past kMaxDevices.
@@ -193,7 +194,7 @@ cudaError_t gkrt_launch_trace_pass(const gk::ShadeScene& sc, const GkrtFrameCons
 cudaError_t gkrt_launch_probe_voxelize(const gk::ShadeScene& sc, uint32_t first, uint32_t count, uint4* voxels,
                                        unsigned long long* counters, cudaStream_t st);
 cudaError_t gkrt_launch_probe_bake(const gk::ShadeScene& sc, const GkrtFrameConstants& fc, const gk::ProbeLight& lt,
-                                   uint32_t first, uint32_t count, const uint32_t* cubes_prev, uint32_t* cubes,
+                                   const gk::SkySH& sh, uint32_t first, uint32_t count, const uint32_t* cubes_prev, uint32_t* cubes,
                                    uint4* voxels, unsigned long long* counters, cudaStream_t st);
 cudaError_t gkrt_launch_trace_rays(const gk::SceneView& S, const GkrtRay* rays, GkrtHit* hits, uint32_t n,
                                    uint32_t mode, unsigned long long* counters, cudaStream_t st);

@@ -68,6 +68,7 @@ struct ProbeHit {
     float t;
     uint32_t mat;
     Vtx v;
+    float tu, tv;   // texture coordinates at the hit (0 without texcoords)
 };
 
 // Closest hit over [EPS, tmax]: its float t, material, whether the ray met the triangle's
@@ -76,7 +77,7 @@ struct ProbeHit {
 GK_D ProbeHit probe_trace(const ShadeScene& sc, f3 o, f3 d, float tmax, bool want_vertex, uint32_t* stk, int stride,
                           Counters& cn) {
     ProbeHit r;
-    r.hit = false; r.back = false; r.t = 0.0f; r.mat = 0u;
+    r.hit = false; r.back = false; r.t = 0.0f; r.mat = 0u; r.tu = 0.0f; r.tv = 0.0f;
     ++cn.rays;
     const TraceOut t = traverse<kClosest, true>(sc.S, o, d, kTmin, tmax, stk, stride, cn);
     if (!t.hit) return r;
@@ -94,7 +95,14 @@ GK_D ProbeHit probe_trace(const ShadeScene& sc, f3 o, f3 d, float tmax, bool wan
     for (int k = 0; k < 12; ++k) w[k] = __ldg(&ip->winv[k]);
     const f3 dl = xvector(w, d);
     r.back = fmaf_(n.z, dl.z, fmaf_(n.y, dl.y, n.x * dl.x)) > 0.0f;
-    if (want_vertex) r.v = hit_vertex(sc, o, d, t.inst, t.prim, t.tri);
+    if (want_vertex) {
+        r.v = hit_vertex(sc, o, d, t.inst, t.prim, t.tri);
+        if (sc.uv) {
+            const HitAttr a = hit_attr(sc, o, d, t.inst, t.prim, t.tri);
+            r.tu = a.u;
+            r.tv = a.v;
+        }
+    }
     return r;
 }
 
@@ -215,7 +223,7 @@ __global__ void __launch_bounds__(kVoxThreads) k_probe_voxelize(ShadeScene sc, u
 
 // One bake step of probes [first, first + count): 8 lanes per probe, lane f < 6 bakes face f.
 __global__ void __launch_bounds__(kBakeThreads) k_probe_bake(ShadeScene sc, GkrtFrameConstants fc, ProbeLight lt,
-                                                             uint32_t first, uint32_t count,
+                                                             SkySH sh, uint32_t first, uint32_t count,
                                                              const uint32_t* cubes_prev, uint32_t* cubes,
                                                              uint4* voxels, unsigned long long* counters) {
     __shared__ uint32_t stack[kStackSize * kBakeThreads];
@@ -252,10 +260,13 @@ __global__ void __launch_bounds__(kBakeThreads) k_probe_bake(ShadeScene sc, Gkrt
             const f3 dir = align_normal(hv, basis);
             const ProbeHit h = probe_trace(sc, o, dir, kFastMaxTrace, true, stack + threadIdx.x, kBakeThreads, cn);
             if (h.hit) {
-                const f4 alb = load_mat(sc, h.v.mat).diffuse;
+                // the hit material's diffuse times its diffuse texture (AmbientCube.slang:504-510)
+                const MatV m = load_mat(sc, h.v.mat);
+                f4 alb = m.diffuse;
+                if (m.dtex >= 0) alb = alb * tex_sample(sc.tex, m.dtex, h.tu, h.tv);
                 bounce = bounce + (alb * probe_di(cubes_prev, sc.voxels, h.v.P, h.v.N)) * 1.25f;
             } else {
-                direct = direct + sky(fc);
+                direct = direct + (sh.on ? sky_sh(sh, fc, dir) : sky(fc));
                 skyv = skyv + 1.0f;
             }
         }
@@ -328,11 +339,11 @@ cudaError_t gkrt_launch_probe_voxelize(const ShadeScene& sc, uint32_t first, uin
 }
 
 cudaError_t gkrt_launch_probe_bake(const ShadeScene& sc, const GkrtFrameConstants& fc, const ProbeLight& lt,
-                                   uint32_t first, uint32_t count, const uint32_t* cubes_prev, uint32_t* cubes,
+                                   const SkySH& sh, uint32_t first, uint32_t count, const uint32_t* cubes_prev, uint32_t* cubes,
                                    uint4* voxels, unsigned long long* counters, cudaStream_t st) {
     if (count == 0) return cudaSuccess;
     const uint64_t threads = (uint64_t)count * 8u;
     k_probe_bake<<<(unsigned)((threads + kBakeThreads - 1) / kBakeThreads), kBakeThreads, 0, st>>>(
-        sc, fc, lt, first, count, cubes_prev, cubes, voxels, counters);
+        sc, fc, lt, sh, first, count, cubes_prev, cubes, voxels, counters);
     return cudaGetLastError();
 }

@@ -385,7 +385,9 @@ int  gkrt_upload_image(GkrtContext* ctx, int image_id, const void* src, size_t s
 /* Texture `texture_id` (< GKRT_MAX_TEXTURES) of width x height texels (rows first to last, 4
  * channels in `format`, bytes = width * height * texel size), replacing an earlier texture of
  * that id. Materials name textures by id (diffuse, MRA, normal map); the sky by
- * GkrtFrameConstants.sky_index. An id without a texture samples as opaque white. Synchronous.
+ * GkrtFrameConstants.sky_index. An id without a texture samples as opaque white. An RGBA32F
+ * texture is also projected on spherical harmonics for the probe bake's sky (ProjectHdrToSh,
+ * Texture.cpp:180-254). Synchronous.
  * (GlobalTexturePool::CreateTextureImage / TextureImage, src/Assets/Texture.cpp:380-620.) */
 int  gkrt_texture_upload(GkrtContext* ctx, uint32_t texture_id, uint32_t width, uint32_t height, uint32_t format,
                          const void* texels, size_t bytes);
@@ -423,8 +425,12 @@ int  gkrt_trace_rays_noalloc(GkrtContext* ctx, const GkrtRay* rays, GkrtHit* hit
  * of RayTraceBaseRenderer::PostRender, RayTraceBaseRenderer.cpp:225-274, running
  * RenderAmbientCubeOnly, AmbientCube.slang:656-690): probes within 2 m of a surface trace 16
  * jittered rays per face, add sky, light 0 and sun, and blend into their colours with weight
- * 1/8. The reference's schedule bakes slice (frame % F) of size (27648 / F) * 64 with F = 30,
- * 120 or 300. Neighbour probes are read as they were before the call.
+ * 1/8. A ray that meets a surface takes its material's diffuse times its diffuse texture; a
+ * sky miss takes, with GKRT_FRAME_SKY_TEXTURE, the spherical-harmonic projection of texture
+ * sky_index (computed by gkrt_texture_upload for RGBA32F textures, zero for 8-bit ones:
+ * SampleIBLRough, Shading.slang:188-192), else the constant sky colour. The reference's
+ * schedule bakes slice (frame % F) of size (27648 / F) * 64 with F = 30, 120 or 300.
+ * Neighbour probes are read as they were before the call.
  *
  * gkrt_probe_download: the grid to host memory (either pointer may be NULL); synchronous. */
 int  gkrt_probe_voxelize(GkrtContext* ctx, void* stream);
@@ -434,7 +440,8 @@ int  gkrt_probe_download(GkrtContext* ctx, uint32_t* cubes, uint32_t* voxels);
 /* Differentiable rendering (no counterpart in the reference): the pass's estimator with
  * `spp` samples per pixel from the primary hit, composed as the compose pass composes it
  * (diffuse x primary albedo + specular, no filter), and its path-replay adjoint.
- * Reference NEE mode without sun (else GKRT_ERR_UNSUPPORTED), at most 16 bounces.
+ * Reference NEE mode without sun, untextured materials and the constant sky (else
+ * GKRT_ERR_UNSUPPORTED), at most 16 bounces.
  * image / d_image: dense width x height float4 device arrays (the context's size).
  * sample_roughness: per material, the roughness GGX directions are sampled with (detached);
  * NULL samples with the current roughness. GGX bounces are weighted by the ratio of the

@@ -166,6 +166,7 @@ struct OScene {
     struct Tex {
         uint32_t w = 0, h = 0;
         std::vector<f4> t;
+        float sh[27] = {0.0f};   // spherical-harmonic projection of an RGBA32F texture, else zero
     };
     std::vector<Tex> tex;
 };
@@ -552,6 +553,33 @@ f4 sky_color(const GkrtFrameConstants& fc) {
     return scale4(c, fc.sky_intensity);
 }
 
+// SampleIBLRough (Shading.slang:188-192): EvaluateSH (Shading.slang:150-186) of the sky
+// texture's projection at direction n, rotated about y by (1 - SkyRotation) pi, as (rgb, 1)
+// times (HasSky ? SkyIntensity : 0). A texture without a projection (8-bit or absent) gives 0.
+f4 sky_rough(const OScene& S, const GkrtFrameConstants& fc, f3 n) {
+    static const float zero[27] = {0.0f};
+    const float* c = fc.sky_index < S.tex.size() ? S.tex[fc.sky_index].sh : zero;
+    float sn, cs;
+    sincos_2pi((1.0f - fc.sky_rotation) * 0.5f, &sn, &cs);
+    const float rx = n.x * cs + n.z * sn, ry = n.y, rz = -n.x * sn + n.z * cs;
+    const float b[9] = {0.282095f,
+                        -0.488603f * ry,
+                        0.488603f * rz,
+                        -0.488603f * rx,
+                        (1.092548f * rx) * ry,
+                        (-1.092548f * ry) * rz,
+                        0.315392f * ((3.0f * ry) * ry - 1.0f),
+                        (-1.092548f * rx) * rz,
+                        0.546274f * (rx * rx - rz * rz)};
+    float r = 0.0f, g = 0.0f, bl = 0.0f;
+    for (int i = 0; i < 9; ++i) {
+        r = r + c[i] * b[i];
+        g = g + c[9 + i] * b[i];
+        bl = bl + c[18 + i] * b[i];
+    }
+    return scale4(f4{r, g, bl, 1.0f}, fc.has_sky ? fc.sky_intensity : 0.0f);
+}
+
 // A sky miss in direction dir: SampleIBLV2 (Shading.slang:194-199) on texture sky_index when
 // the frame asks for it (d = normalize(dir), t = ((atan2(d.x, d.z) + pi rotate) / 2pi,
 // acos(d.y) / pi), min((10, 10, 10, 1), sample) x SkyIntensity), else the constant colour.
@@ -567,7 +595,7 @@ f4 sky_dir(const OScene& S, const GkrtFrameConstants& fc, f3 dir) {
 // FetchGBufferV2 (Shading.slang:82-112) for the primary vertex: albedo = diffuse x diffuse
 // texture, roughness = fuzziness x the MRA texture's green channel, and the normal map through
 // mikkTSpace (:74-80) on the vertex's local normal and tangent (the barycentric mixes the
-// visibility-buffer caster computes, GeneralFunc.slang:51-52), carried to world space by the
+// visibility-buffer caster computes, GeneralFunc.slang:49-51), carried to world space by the
 // instance transform and normalized.
 void fetch_gbuffer(const OScene& S, const GkrtMaterial& m, Vtx& v, f4& albedo, float& rough) {
     albedo = f4{m.diffuse[0], m.diffuse[1], m.diffuse[2], m.diffuse[3]};
@@ -1380,7 +1408,7 @@ struct ProbeHitO {
     bool hit = false, back = false;
     float t = 0.0f;
     uint32_t mat = 0;
-    Vtx v;
+    Vtx v;   // P, N, mat, inst and uv (the texture coordinates at the hit)
 };
 
 f3 probe_origin(uint32_t g) {
@@ -1422,6 +1450,11 @@ ProbeHitO probe_hit(const OScene& S, f3 o, f3 d, float tmax) {
     r.v.P = fma3(d, hh.t, o);
     r.v.mat = r.mat;
     r.v.inst = h.inst;
+    r.v.uv = f2{0.0f, 0.0f};
+    if (!S.uv.empty()) {
+        const f2 a = S.uv[vi[0]], b = S.uv[vi[1]], c = S.uv[vi[2]];
+        r.v.uv = f2{fma_(c.x - a.x, hh.b2, fma_(b.x - a.x, hh.b1, a.x)), fma_(c.y - a.y, hh.b2, fma_(b.y - a.y, hh.b1, a.y))};
+    }
     return r;
 }
 
@@ -1567,11 +1600,14 @@ void bake_probe(const OScene& S, const GkrtFrameConstants& fc, uint32_t g, const
             f3 dir = align_with_normal(hv, basis);
             ProbeHitO h = probe_hit(S, o, dir, 20.0f);
             if (h.hit) {
+                // the material's diffuse times its diffuse texture (AmbientCube.slang:504-510)
                 const GkrtMaterial& hm = get_mat(S, h.v.mat);
                 f4 alb{hm.diffuse[0], hm.diffuse[1], hm.diffuse[2], hm.diffuse[3]};
+                if (hm.diffuse_texture_id >= 0) alb = mul4(alb, tex_sample(S, hm.diffuse_texture_id, h.v.uv.x, h.v.uv.y));
                 bounce = add4(bounce, scale4(mul4(alb, probe_di(cubes_prev, voxels, h.v.P, h.v.N)), 1.25f));
             } else {
-                direct = add4(direct, sky_color(fc));
+                // (AmbientCube.slang:512-516) the sky texture's projection, or the constant sky
+                direct = add4(direct, (fc.flags & GKRT_FRAME_SKY_TEXTURE) ? sky_rough(S, fc, dir) : sky_color(fc));
                 skyv = skyv + 1.0f;
             }
         }
@@ -1798,9 +1834,51 @@ void gko_tex_sample(void* h, int id, float u, float v, float* out) {
     const f4 c = tex_sample(*static_cast<OScene*>(h), id, u, v);
     out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
 }
+// The projection of texture id (27 floats: red, green, blue terms) and the bake's sky lookup.
+int gko_texture_sh(void* h, uint32_t id, float* out) {
+    const OScene* S = static_cast<OScene*>(h);
+    if (id >= S->tex.size()) return -1;
+    std::memcpy(out, S->tex[id].sh, 27 * sizeof(float));
+    return 0;
+}
+void gko_sky_rough(void* h, const GkrtFrameConstants* fc, const float* dir, float* out) {
+    const f4 c = sky_rough(*static_cast<OScene*>(h), *fc, f3{dir[0], dir[1], dir[2]});
+    out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
+}
 void gko_sky_dir(void* h, const GkrtFrameConstants* fc, const float* dir, float* out) {
     const f4 c = sky_dir(*static_cast<OScene*>(h), *fc, f3{dir[0], dir[1], dir[2]});
     out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
+}
+
+// ProjectHdrToSh (Texture.cpp:180-254) of an equirectangular RGBA float image: per texel
+// (x, y) the direction at theta = (y + 1/2) pi / h, phi = (x + 1/2) 2 pi / w, i.e.
+// (sin theta cos phi, cos theta, sin theta sin phi), the nine real harmonics of bands 0-2 with
+// the shader's constants, and the solid-angle weight sin theta (pi / h)(2 pi / w); the sums are
+// not normalised. Summed in double, rows first to last and texels left to right, then rounded
+// to float (the reference sums in float).
+void project_sh(const f4* t, uint32_t w, uint32_t h, float out[27]) {
+    const double pi = 3.14159265358979323846;
+    const double k0 = 0.282095, k1 = 0.488603, k2 = 1.092548, k3 = 0.315392, k4 = 0.546274;
+    double sum[27];
+    for (int k = 0; k < 27; ++k) sum[k] = 0.0;
+    for (uint32_t y = 0; y < h; ++y) {
+        const double theta = ((double)y + 0.5) / (double)h * pi;
+        const double sth = std::sin(theta), cth = std::cos(theta);
+        const double wgt = sth * (pi / (double)h) * (2.0 * pi / (double)w);
+        for (uint32_t x = 0; x < w; ++x) {
+            const double phi = ((double)x + 0.5) / (double)w * (2.0 * pi);
+            const double dx = sth * std::cos(phi), dy = cth, dz = sth * std::sin(phi);
+            const double y9[9] = {k0, -k1 * dy, k1 * dz, -k1 * dx, k2 * dx * dy, -k2 * dy * dz,
+                                  k3 * (3.0 * dy * dy - 1.0), -k2 * dx * dz, k4 * (dx * dx - dz * dz)};
+            const f4 c = t[(size_t)y * w + x];
+            for (int i = 0; i < 9; ++i) {
+                sum[i] += (double)c.x * y9[i] * wgt;
+                sum[9 + i] += (double)c.y * y9[i] * wgt;
+                sum[18 + i] += (double)c.z * y9[i] * wgt;
+            }
+        }
+    }
+    for (int k = 0; k < 27; ++k) out[k] = (float)sum[k];
 }
 
 // Texture `id` of the oracle scene: texels as the sampler returns them (RGBA8 UNORM c / 255;
@@ -1814,8 +1892,10 @@ int gko_texture_upload(void* h, uint32_t id, uint32_t w, uint32_t ht, uint32_t f
     t.h = ht;
     const size_t n = (size_t)w * ht;
     t.t.resize(n);
+    std::fill(t.sh, t.sh + 27, 0.0f);
     if (format == GKRT_TEX_RGBA32F) {
         std::memcpy(t.t.data(), texels, n * 16);
+        project_sh(t.t.data(), w, ht, t.sh);
         return 0;
     }
     const uint8_t* b = static_cast<const uint8_t*>(texels);

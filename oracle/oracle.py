@@ -81,6 +81,9 @@ def lib():
         L.gko_acos.restype = C.c_float
         L.gko_tex_sample.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_void_p]
         L.gko_sky_dir.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_void_p, C.c_void_p]
+        L.gko_sky_rough.argtypes = [C.c_void_p, C.POINTER(abi.GkrtFrameConstants), C.c_void_p, C.c_void_p]
+        L.gko_texture_sh.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        L.gko_texture_sh.restype = C.c_int
         L.gko_exact_tri.restype = C.c_int
         L.gko_fp32_tri.restype = C.c_int
         _lib = L
@@ -135,6 +138,20 @@ class OracleScene:
         out = np.zeros(4, np.float32)
         lib().gko_sky_dir(self.h, C.byref(fc), dd.ctypes.data, out.ctypes.data)
         return out
+
+    def sky_rough(self, fc, d) -> np.ndarray:
+        """The probe bake's sky radiance in direction d (SampleIBLRough)."""
+        dd = np.ascontiguousarray(d, np.float32)
+        out = np.zeros(4, np.float32)
+        lib().gko_sky_rough(self.h, C.byref(fc), dd.ctypes.data, out.ctypes.data)
+        return out
+
+    def texture_sh(self, texture_id: int) -> np.ndarray:
+        """The spherical-harmonic projection of a texture, (3, 9): red, green, blue terms."""
+        out = np.zeros(27, np.float32)
+        if lib().gko_texture_sh(self.h, texture_id, out.ctypes.data) != 0:
+            raise ValueError(f"no texture {texture_id}")
+        return out.reshape(3, 9)
 
     def trace_rays(self, rays: np.ndarray, mode: int = abi.TRACE_CLOSEST, brute: bool = False,
                    threads: int = 0) -> np.ndarray:

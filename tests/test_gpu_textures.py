@@ -125,3 +125,80 @@ def test_texture_upload_errors_and_replacement():
         O.OracleScene(sc).trace_pass(fc, W, H, oim)
         np.testing.assert_allclose(b, oim[abi.IMG_ALBEDO], rtol=RTOL, atol=ATOL)
         assert not np.array_equal(a, b)
+
+
+def _scaled(sc, scale):
+    """The scene with every instance and light scaled by `scale` about the origin."""
+    inst = sc.instances.copy()
+    for i in range(len(inst)):
+        w = np.asarray(inst[i]["world"], np.float64).reshape(3, 4) * scale
+        inst[i]["world"] = w.astype(np.float32).reshape(12)
+        inst[i]["world_inv"] = scenes.affine_inverse(inst[i]["world"])
+    lights = sc.lights.copy()
+    for k in ("p0", "p1", "p3"):
+        lights[k][:, :3] *= scale
+    lights["normal_area"][:, 3] *= scale * scale
+    return abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, sc.materials, inst,
+                           lights=lights, name=sc.name + "-x4", texcoords=sc.texcoords, tangents=sc.tangents,
+                           textures=sc.textures)
+
+
+def test_textured_bake_matches_oracle():
+    """Two bake steps of the textured Cornell box (4 m) under the HDR sky: hits take the diffuse
+    texture (AmbientCube.slang:504-510), sky misses the sky texture's spherical-harmonic
+    projection (SampleIBLRough); GPU words equal the oracle's, and both inputs change them."""
+    from test_gpu_probes import ranges
+    sc, cam, st = scenes.cornell_textured()
+    sc = _scaled(sc, 4.0)
+    # bright enough for the packed colours (10 bits up to 512) to register a 1/8 blend step,
+    # the sun's light then as bounce light through the textured albedos
+    st.sky_intensity = 40.0
+    st.has_sun, st.sun_direction, st.sun_intensity = True, (0.3, 0.6, 1.0), 200.0
+    fc = camera.FrameBuilder(64, 64, st).build(cam, 0)
+    assert fc.flags & abi.FRAME_SKY_TEXTURE
+    first = ranges()[0][0]
+    count = ranges()[-1][0] + ranges()[-1][1] - first
+    osc = O.OracleScene(sc)
+    with PathTracingRenderer(0) as r:
+        r.load_scene(sc)
+        r.probe_voxelize()
+        r.synchronize()
+        for step in range(2):
+            prev, vox = r.probe_download()
+            r.probe_bake(fc, first, count)
+            r.synchronize()
+            cubes, _ = r.probe_download()
+            o, _ = osc.probe_bake(fc, first, count, prev, vox)
+            g = cubes[first:first + count]
+            bad = np.nonzero((g != o).any(axis=1))[0]
+            assert bad.size == 0, (step, bad[:5], g[bad[:2]], o[bad[:2]])
+        assert r.stats().device_error == 0
+    # the same step without the sky texture (constant sky) and without textures differs
+    surf = (vox[first:first + count, 2] & 0xFF) < 8
+    assert surf.sum() > 1000
+    st.sky_texture = None
+    fc_const = camera.FrameBuilder(64, 64, st).build(cam, 0)
+    o_const, _ = osc.probe_bake(fc_const, first, count, prev, vox)
+    assert ((o_const != o)[surf][:, 6:12]).any(axis=1).mean() > 0.05
+    mats = sc.materials.copy()
+    mats["diffuse_texture_id"] = -1
+    plain = abi.SceneArrays(sc.positions, sc.normals, sc.material_slots, sc.indices, sc.meshes, mats, sc.instances,
+                            lights=sc.lights, name="cornell-x4-untextured", texcoords=sc.texcoords,
+                            tangents=sc.tangents, textures=sc.textures)
+    o_plain, _ = O.OracleScene(plain).probe_bake(fc, first, count, prev, vox)
+    assert ((o_plain != o)[surf][:, 0:6]).any(axis=1).mean() > 0.01   # bounce light through textured albedo
+
+
+def test_adjoint_refuses_textures():
+    sc, cam, st = scenes.cornell_textured()
+    W = H = 32
+    with PathTracingRenderer(0) as r:
+        r.load_scene(sc)
+        r.create_swap_chain(W, H)
+        st.has_sun = False
+        fc = camera.FrameBuilder(W, H, st).build(cam, 0)
+        import torch
+        img = torch.zeros((H, W, 4), device="cuda")
+        with pytest.raises(GkrtError) as e:
+            r.adjoint_forward(fc, 1, img.data_ptr())
+        assert e.value.code == abi.GKRT_ERR_UNSUPPORTED

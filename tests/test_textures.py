@@ -128,6 +128,64 @@ def test_sky_lookup():
                                rtol=1e-6)
 
 
+def _sh_numpy(t):
+    """ProjectHdrToSh (Texture.cpp:180-254) in float64, vectorised: texel (x, y) at theta =
+    (y + 1/2) pi / h, phi = (x + 1/2) 2 pi / w, weight sin(theta) (pi / h)(2 pi / w)."""
+    h, w = t.shape[:2]
+    th = (np.arange(h) + 0.5) / h * np.pi
+    ph = (np.arange(w) + 0.5) / w * 2 * np.pi
+    st, ct = np.sin(th)[:, None], np.cos(th)[:, None]
+    dx, dy, dz = st * np.cos(ph)[None], np.broadcast_to(ct, (h, w)), st * np.sin(ph)[None]
+    basis = np.stack([np.full((h, w), 0.282095), -0.488603 * dy, 0.488603 * dz, -0.488603 * dx,
+                      1.092548 * dx * dy, -1.092548 * dy * dz, 0.315392 * (3 * dy * dy - 1),
+                      -1.092548 * dx * dz, 0.546274 * (dx * dx - dz * dz)])
+    wt = np.broadcast_to(st * (np.pi / h) * (2 * np.pi / w), (h, w))
+    return np.einsum("khw,hwc->ck", basis * wt, t[..., :3].astype(np.float64))
+
+
+def test_sky_sh_projection_and_the_bake_sky():
+    """The probe bake's sky (SampleIBLRough): the texture's projection against a float64
+    restatement, a constant sky evaluating to itself, skies linear in the direction evaluating
+    to the same linear function (band 1 holds them exactly), with the rotation 1 - SkyRotation
+    about y, 8-bit textures projecting to zero, and the frame's HasSky gate."""
+    rng = np.random.default_rng(8)
+    h, w = 32, 64
+    th = (np.arange(h) + 0.5) / h * np.pi
+    ph = (np.arange(w) + 0.5) / w * 2 * np.pi
+    dx = (np.sin(th)[:, None] * np.cos(ph)[None]).astype(np.float32)
+    dy = np.broadcast_to(np.cos(th)[:, None], (h, w)).astype(np.float32)
+    rnd = rng.uniform(0.0, 3.0, (h, w, 4)).astype(np.float32)
+    const = np.full((h, w, 4), 1.0, np.float32)
+    const[..., :3] = (0.5, 1.5, 2.5)
+    lin = np.ones((h, w, 4), np.float32)
+    lin[..., 0] = 2.0 + dy
+    lin[..., 1] = 2.0 + dx
+    lin[..., 2] = 1.0
+    rgba8 = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    osc = O.OracleScene(_scene_with({1: (abi.TEX_RGBA32F, rnd), 2: (abi.TEX_RGBA32F, const),
+                                     3: (abi.TEX_RGBA32F, lin), 4: (abi.TEX_RGBA8_SRGB, rgba8)}))
+    np.testing.assert_allclose(osc.texture_sh(1), _sh_numpy(rnd), rtol=1e-6, atol=1e-6)
+    assert not osc.texture_sh(4).any()
+
+    def frame(idx, rot, has_sky=True, intensity=1.0):
+        st = camera.Settings(has_sky=has_sky, sky_intensity=intensity, sky_texture=idx, sky_rotation=rot)
+        return camera.FrameBuilder(8, 8, st).build(camera.Camera(eye=(0, 0, 3), center=(0, 0, 0)), 0)
+
+    dirs = rng.normal(size=(64, 3))
+    dirs = (dirs / np.linalg.norm(dirs, axis=1, keepdims=True)).astype(np.float32)
+    for n in dirs:
+        # a constant sky: c0^2 4 pi = 1; the midpoint sums over 32 rows leak a few 1e-3 into
+        # band 0 and the zonal band-2 term
+        np.testing.assert_allclose(osc.sky_rough(frame(2, 0.4, intensity=2.0), n), [1.0, 3.0, 5.0, 2.0], rtol=4e-3)
+        # rotation angle (1 - SkyRotation) pi: SkyRotation 1 leaves directions alone, 0 turns x to -x
+        got = osc.sky_rough(frame(3, 1.0), n)
+        np.testing.assert_allclose(got[:3], [2.0 + n[1], 2.0 + n[0], 1.0], atol=1e-2)
+        got = osc.sky_rough(frame(3, 0.0), n)
+        np.testing.assert_allclose(got[:3], [2.0 + n[1], 2.0 - n[0], 1.0], atol=1e-2)
+    assert not osc.sky_rough(frame(2, 0.0, has_sky=False), dirs[0]).any()
+    np.testing.assert_array_equal(osc.sky_rough(frame(4, 0.0), dirs[0]), [0.0, 0.0, 0.0, 1.0])   # (rgb, 1)
+
+
 def test_rgbe_reader():
     rng = np.random.default_rng(4)
     rgbe = rng.integers(0, 256, (7, 40, 4)).astype(np.uint8)
