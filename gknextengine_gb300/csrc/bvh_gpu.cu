@@ -206,10 +206,14 @@ __global__ void k_init_idx(uint32_t* idx, uint32_t n) {
     if (t < n) idx[t] = t;
 }
 
-__global__ void k_clear(int* bins, int* tb, uint32_t ntask) {
+// Each device function below does one kernel's work for one item (a work item, a task, ...):
+// the per-round kernels call them once per block or thread, the instance-level build of
+// k_inst_level loops over them inside one cooperative launch.
+
+__device__ void clear_bins(int* bins, int* tb, uint32_t ntask, uint32_t first, uint32_t stride) {
     const uint32_t nb = ntask * (uint32_t)kBinWords, nt = ntask * 12u;
     const int pinf = f2o(INFINITY), ninf = f2o(-INFINITY);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb + nt; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = first; i < nb + nt; i += stride) {
         if (i < nb) {
             const uint32_t q = i % 7u;
             bins[i] = q == 6u ? 0 : (q < 3u ? pinf : ninf);
@@ -219,11 +223,14 @@ __global__ void k_clear(int* bins, int* tb, uint32_t ntask) {
         }
     }
 }
+__global__ void k_clear(int* bins, int* tb, uint32_t ntask) {
+    clear_bins(bins, tb, ntask, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
 
-__global__ void __launch_bounds__(kBt) k_bounds(Geo g, const uint32_t* idx, const uint32_t* wtask,
-                                                const uint32_t* wbeg, const uint32_t* wend, int* tb) {
+// (block of kBt threads) box and centroid bounds of work item w, merged into its task's
+__device__ void bounds_item(const Geo& g, const uint32_t* idx, const uint32_t* wtask, const uint32_t* wbeg,
+                            const uint32_t* wend, int* tb, uint32_t w) {
     __shared__ int s[12];
-    const uint32_t w = blockIdx.x;
     if (threadIdx.x < 12) s[threadIdx.x] = (threadIdx.x % 6) < 3 ? f2o(INFINITY) : f2o(-INFINITY);
     __syncthreads();
     float v[12];
@@ -257,6 +264,10 @@ __global__ void __launch_bounds__(kBt) k_bounds(Geo g, const uint32_t* idx, cons
         else atomicMax(d, s[threadIdx.x]);
     }
 }
+__global__ void __launch_bounds__(kBt) k_bounds(Geo g, const uint32_t* idx, const uint32_t* wtask,
+                                                const uint32_t* wbeg, const uint32_t* wend, int* tb) {
+    bounds_item(g, idx, wtask, wbeg, wend, tb, blockIdx.x);
+}
 
 __device__ __forceinline__ void axis_scale(const int* tbt, int k, float* clo, float* scale) {
     *clo = o2f(tbt[6 + k]);
@@ -264,10 +275,10 @@ __device__ __forceinline__ void axis_scale(const int* tbt, int k, float* clo, fl
     *scale = ext > 0.0f ? (float)kBins / ext : 0.0f;
 }
 
-__global__ void __launch_bounds__(kBt) k_bin(Geo g, const uint32_t* idx, const int* tb, const uint32_t* wtask,
-                                             const uint32_t* wbeg, const uint32_t* wend, int* bins) {
+// (block of kBt threads) the 3 x 16 bins of work item w, merged into its task's
+__device__ void bin_item(const Geo& g, const uint32_t* idx, const int* tb, const uint32_t* wtask,
+                         const uint32_t* wbeg, const uint32_t* wend, int* bins, uint32_t w) {
     __shared__ int sb[kBinWords];
-    const uint32_t w = blockIdx.x;
     const uint32_t t = wtask[w];
     const int pinf = f2o(INFINITY), ninf = f2o(-INFINITY);
     for (int i = threadIdx.x; i < kBinWords; i += kBt) {
@@ -300,6 +311,10 @@ __global__ void __launch_bounds__(kBt) k_bin(Geo g, const uint32_t* idx, const i
         else atomicMax(&gb[i], sb[i]);
     }
 }
+__global__ void __launch_bounds__(kBt) k_bin(Geo g, const uint32_t* idx, const int* tb, const uint32_t* wtask,
+                                             const uint32_t* wbeg, const uint32_t* wend, int* bins) {
+    bin_item(g, idx, tb, wtask, wbeg, wend, bins, blockIdx.x);
+}
 
 // SAH over one axis's bins (the host builder's sweep): best cost, boundary and left count.
 __device__ void sah_axis(const float (*bb)[6], const uint32_t* bc, int axis, float* best, int* best_axis,
@@ -325,10 +340,9 @@ __device__ void sah_axis(const float (*bb)[6], const uint32_t* bc, int axis, flo
     }
 }
 
-__global__ void k_split(const BigTask* tasks, uint32_t ntask, const int* bins, const int* tb, Split* split,
-                        BvhNode* nodes, float* root_box, uint32_t node_base) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntask) return;
+// task t: writes its box into its parent and picks the SAH split
+__device__ void split_task(const BigTask* tasks, uint32_t t, const int* bins, const int* tb, Split* split,
+                           BvhNode* nodes, float* root_box, uint32_t node_base) {
     const BigTask T = tasks[t];
     const int* tbt = tb + 12 * (size_t)t;
     float box[6];
@@ -354,17 +368,23 @@ __global__ void k_split(const BigTask* tasks, uint32_t ntask, const int* bins, c
     if (s.axis >= 0) { s.clo = clo[s.axis]; s.scale = scale[s.axis]; }
     split[t] = s;
 }
+__global__ void k_split(const BigTask* tasks, uint32_t ntask, const int* bins, const int* tb, Split* split,
+                        BvhNode* nodes, float* root_box, uint32_t node_base) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ntask) split_task(tasks, t, bins, tb, split, nodes, root_box, node_base);
+}
 
 __device__ __forceinline__ bool goes_left(const Geo& g, uint32_t p, uint32_t pos, const Split& s, uint32_t begin) {
     if (s.axis < 0) return pos - begin < s.nleft;
     return bin_of(g.cent[3 * (size_t)p + s.axis], s.clo, s.scale) < s.bin;
 }
 
-__global__ void __launch_bounds__(kBt) k_count_left(Geo g, const uint32_t* idx, const Split* split,
-                                                    const BigTask* tasks, const uint32_t* wtask, const uint32_t* wbeg,
-                                                    const uint32_t* wend, uint32_t* wleft) {
+// (block of kBt threads) how many primitives of work item w go left
+__device__ void count_left_item(const Geo& g, const uint32_t* idx, const Split* split, const BigTask* tasks,
+                                const uint32_t* wtask, const uint32_t* wbeg, const uint32_t* wend, uint32_t* wleft,
+                                uint32_t w) {
     __shared__ uint32_t red[kBt / 32];
-    const uint32_t w = blockIdx.x, t = wtask[w];
+    const uint32_t t = wtask[w];
     const Split s = split[t];
     const uint32_t begin = tasks[t].begin;
     uint32_t c = 0;
@@ -378,15 +398,19 @@ __global__ void __launch_bounds__(kBt) k_count_left(Geo g, const uint32_t* idx, 
         wleft[w] = tot;
     }
 }
+__global__ void __launch_bounds__(kBt) k_count_left(Geo g, const uint32_t* idx, const Split* split,
+                                                    const BigTask* tasks, const uint32_t* wtask, const uint32_t* wbeg,
+                                                    const uint32_t* wend, uint32_t* wleft) {
+    count_left_item(g, idx, split, tasks, wtask, wbeg, wend, wleft, blockIdx.x);
+}
 
 // Stable scatter into tmp: left side first. wleft_scan: exclusive scan of left counts over
 // work items; a task's work items are consecutive, the first being task_w0[t].
-__global__ void __launch_bounds__(kBt) k_scatter(Geo g, const uint32_t* idx, uint32_t* tmp, const Split* split,
-                                                 const BigTask* tasks, const uint32_t* wtask, const uint32_t* wbeg,
-                                                 const uint32_t* wend, const uint32_t* wleft_scan,
-                                                 const uint32_t* task_w0, uint32_t* info) {
+__device__ void scatter_item(const Geo& g, const uint32_t* idx, uint32_t* tmp, const Split* split,
+                             const BigTask* tasks, const uint32_t* wtask, const uint32_t* wbeg, const uint32_t* wend,
+                             const uint32_t* wleft_scan, const uint32_t* task_w0, uint32_t* info, uint32_t w) {
     __shared__ uint32_t wsum[kBt / 32];
-    const uint32_t w = blockIdx.x, t = wtask[w];
+    const uint32_t t = wtask[w];
     const BigTask T = tasks[t];
     const Split s = split[t];
     const uint32_t left_before = wleft_scan[w] - wleft_scan[task_w0[t]];
@@ -425,17 +449,24 @@ __global__ void __launch_bounds__(kBt) k_scatter(Geo g, const uint32_t* idx, uin
         __syncthreads();
     }
 }
+__global__ void __launch_bounds__(kBt) k_scatter(Geo g, const uint32_t* idx, uint32_t* tmp, const Split* split,
+                                                 const BigTask* tasks, const uint32_t* wtask, const uint32_t* wbeg,
+                                                 const uint32_t* wend, const uint32_t* wleft_scan,
+                                                 const uint32_t* task_w0, uint32_t* info) {
+    scatter_item(g, idx, tmp, split, tasks, wtask, wbeg, wend, wleft_scan, task_w0, info, blockIdx.x);
+}
 
+__device__ void copy_back_item(const uint32_t* tmp, uint32_t* idx, const uint32_t* wbeg, const uint32_t* wend,
+                               uint32_t w) {
+    for (uint32_t i = wbeg[w] + threadIdx.x; i < wend[w]; i += kBt) idx[i] = tmp[i];
+}
 __global__ void __launch_bounds__(kBt) k_copy_back(const uint32_t* tmp, uint32_t* idx, const uint32_t* wbeg,
                                                    const uint32_t* wend) {
-    const uint32_t w = blockIdx.x;
-    for (uint32_t i = wbeg[w] + threadIdx.x; i < wend[w]; i += kBt) idx[i] = tmp[i];
+    copy_back_item(tmp, idx, wbeg, wend, blockIdx.x);
 }
 
 // Per task: (big children, their work items, small children, node slots they reserve).
-__global__ void k_child_counts(const BigTask* tasks, uint32_t ntask, const Split* split, uint4* cc) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntask) return;
+__device__ void child_counts_task(const BigTask* tasks, uint32_t t, const Split* split, uint4* cc) {
     const BigTask T = tasks[t];
     const uint32_t m[2] = {split[t].nleft, (T.end - T.begin) - split[t].nleft};
     uint4 c = make_uint4(0u, 0u, 0u, 0u);
@@ -445,12 +476,14 @@ __global__ void k_child_counts(const BigTask* tasks, uint32_t ntask, const Split
     }
     cc[t] = c;
 }
-
-__global__ void k_emit(const BigTask* tasks, uint32_t ntask, const Split* split, const uint4* off, uint32_t node0,
-                       uint32_t res0, uint32_t small0, BigTask* next, uint32_t* nwtask, uint32_t* nwbeg,
-                       uint32_t* nwend, uint32_t* next_w0, SmallTask* small) {
+__global__ void k_child_counts(const BigTask* tasks, uint32_t ntask, const Split* split, uint4* cc) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntask) return;
+    if (t < ntask) child_counts_task(tasks, t, split, cc);
+}
+
+__device__ void emit_task(const BigTask* tasks, uint32_t t, const Split* split, const uint4* off, uint32_t node0,
+                          uint32_t res0, uint32_t small0, BigTask* next, uint32_t* nwtask, uint32_t* nwbeg,
+                          uint32_t* nwend, uint32_t* next_w0, SmallTask* small) {
     const BigTask T = tasks[t];
     uint4 o = off[t];
     const uint32_t mid = T.begin + split[t].nleft;
@@ -488,16 +521,21 @@ __global__ void k_emit(const BigTask* tasks, uint32_t ntask, const Split* split,
         }
     }
 }
+__global__ void k_emit(const BigTask* tasks, uint32_t ntask, const Split* split, const uint4* off, uint32_t node0,
+                       uint32_t res0, uint32_t small0, BigTask* next, uint32_t* nwtask, uint32_t* nwbeg,
+                       uint32_t* nwend, uint32_t* next_w0, SmallTask* small) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ntask)
+        emit_task(tasks, t, split, off, node0, res0, small0, next, nwtask, nwbeg, nwend, next_w0, small);
+}
 
 // One thread per small task: the rest of the subtree, depth first, with the host builder's
 // rules (triangle ranges of up to 2 are leaves, up to max_leaf when the SAH prefers a leaf;
 // instance leaves hold one instance). info[0] += nodes used, info[1] = max depth, info[2]
 // error bits.
-__global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, BvhNode* nodes, float* root_box,
-                        uint32_t max_leaf, int inst_leaf, const uint32_t* prim_map, uint32_t node_base,
-                        uint32_t* info) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ns) return;
+__device__ void small_task(const Geo& g, uint32_t* idx, const SmallTask* st, uint32_t i, BvhNode* nodes,
+                           float* root_box, uint32_t max_leaf, int inst_leaf, const uint32_t* prim_map,
+                           uint32_t node_base, uint32_t* info) {
     const SmallTask S = st[i];
     struct Item {
         uint32_t b, e;
@@ -611,6 +649,12 @@ __global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, 
     atomicAdd(&info[0], used);
     atomicMax(&info[1], (uint32_t)maxd);
 }
+__global__ void k_small(Geo g, uint32_t* idx, const SmallTask* st, uint32_t ns, BvhNode* nodes, float* root_box,
+                        uint32_t max_leaf, int inst_leaf, const uint32_t* prim_map, uint32_t node_base,
+                        uint32_t* info) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ns) small_task(g, idx, st, i, nodes, root_box, max_leaf, inst_leaf, prim_map, node_base, info);
+}
 
 // ---------------------------------------------------------------------------------------------
 // collapse into compressed 8-wide nodes (WideNode, gk_trace.cuh)
@@ -672,10 +716,25 @@ __device__ int wide_expand(const BvhNode* bin, int root, WEnt* e, const RefitLin
     return n;
 }
 
-// Per-axis scale 2^ex and origin k for the children's boxes, one step of margin on each side
-// (exact double arithmetic: x / 2^ex of a float is exact here, so are floor and ceil). The
-// exponent is capped at 38 so that 2^23 s |inv| stays finite for |inv| <= 1e20. Fails on
-// non-finite or out-of-range boxes.
+// floor and ceil of the exact product x 2^-ex (rs = 2^-ex, -100 <= ex <= 38) in float: a
+// product of magnitude >= 1 is a normal float and exact; below 1 only the sign of x matters
+// (a product that underflowed to a subnormal or to zero keeps the answer exact).
+__device__ __forceinline__ float floor_scaled(float x, float rs) {
+    const float y = x * rs;
+    if (fabsf(y) < 1.0f) return x < 0.0f ? -1.0f : 0.0f;
+    return floorf(y);
+}
+__device__ __forceinline__ float ceil_scaled(float x, float rs) {
+    const float y = x * rs;
+    if (fabsf(y) < 1.0f) return x > 0.0f ? 1.0f : 0.0f;
+    return ceilf(y);
+}
+
+// Per-axis scale 2^ex and origin k for the children's boxes, one step of margin on each side.
+// Exact: x / 2^ex of a float is floored or ceiled exactly (floor_scaled), and every count
+// below stays under 2^24, so the float arithmetic is that of exact integers. The exponent is
+// capped at 38 so that 2^23 s |inv| stays finite for |inv| <= 1e20. Fails on non-finite or
+// out-of-range boxes.
 __device__ bool wide_axis(const WEnt* e, int n, int ax, float& origin, uint32_t& ebyte, uint32_t* qlo,
                           uint32_t* qhi) {
     float lo = INFINITY, hi = -INFINITY;
@@ -689,18 +748,17 @@ __device__ bool wide_axis(const WEnt* e, int n, int ax, float& origin, uint32_t&
     if (range > 0.0) ex = max(ex, ilogb(range / 253.0));
     if (lo != 0.0f) ex = max(ex, ilogb(fabs((double)lo)) - 21);
     for (; ex <= 38; ++ex) {
-        // x / 2^ex as x * 2^-ex: exact for a float x and -100 <= ex <= 38 (no double underflow)
-        const double s = ldexp(1.0, ex), rs = ldexp(1.0, -ex);
-        const double k = floor((double)lo * rs) - 1.0;
-        if (fabs(k) >= 4194304.0) continue;   // |k| < 2^22
+        const float s = __int_as_float((127 + ex) << 23), rs = __int_as_float((127 - ex) << 23);   // 2^ex, 2^-ex
+        const float k = floor_scaled(lo, rs) - 1.0f;
+        if (fabsf(k) >= 4194304.0f) continue;   // |k| < 2^22
         bool ok = true;
-        for (int i = 0; i < n; ++i) ok = ok && (ceil((double)e[i].b[3 + ax] * rs) + 1.0 - k <= 255.0);
+        for (int i = 0; i < n; ++i) ok = ok && (ceil_scaled(e[i].b[3 + ax], rs) + 1.0f - k <= 255.0f);
         if (!ok) continue;
         for (int i = 0; i < n; ++i) {
-            qlo[i] = (uint32_t)(floor((double)e[i].b[ax] * rs) - 1.0 - k);
-            qhi[i] = (uint32_t)(ceil((double)e[i].b[3 + ax] * rs) + 1.0 - k);
+            qlo[i] = (uint32_t)(floor_scaled(e[i].b[ax], rs) - 1.0f - k);
+            qhi[i] = (uint32_t)(ceil_scaled(e[i].b[3 + ax], rs) + 1.0f - k);
         }
-        origin = (float)(k * s);
+        origin = k * s;
         ebyte = (uint32_t)(ex + 127);
         return true;
     }
@@ -708,29 +766,23 @@ __device__ bool wide_axis(const WEnt* e, int n, int ax, float& origin, uint32_t&
 }
 
 // items: x binary node, y wide index, z depth (1 at the roots)
-__global__ void k_wide_count(const BvhNode* bin, const int4* items, uint32_t n, uint32_t* cnt) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ void wide_count_item(const BvhNode* bin, const int4* items, uint32_t i, uint32_t* cnt) {
     WEnt e[8];
     const int m = wide_expand(bin, items[i].x, e);
     uint32_t c = 0;
     for (int j = 0; j < m; ++j) c += e[j].ref >= 0 ? 1u : 0u;
     cnt[i] = c;   // 0 for a malformed node: k_wide_emit reports it
 }
+__global__ void k_wide_count(const BvhNode* bin, const int4* items, uint32_t n, uint32_t* cnt) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) wide_count_item(bin, items, i, cnt);
+}
 
 // links (optional, links.parent null for none): refit links of the trees being collapsed
-__global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, const uint32_t* off, uint32_t next_base,
-                            WideNode* out, int4* next, uint32_t* err, RefitLinks links) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int4 it = items[i];
-    const RefitLinks* lk = links.parent ? &links : nullptr;
-    WEnt e[8];
-    int m = wide_expand(bin, it.x, e, lk);
-    if (m < 0) {
-        atomicOr(err, kBuildErrRange);
-        m = 0;
-    }
+// Wide node it.y from the m entries e: quantized boxes, refs (interior children become the
+// next level's items at next_base + off_i + rank), and the refit's source slots with links.
+__device__ void wide_write(const WEnt* e, int m, const int4& it, uint32_t off_i, uint32_t next_base, WideNode* out,
+                           int4* next, uint32_t* err, const RefitLinks* lk) {
     if (lk) {
         const uint32_t w = (uint32_t)it.y - lk->wbase;
         if (w < lk->wcap)
@@ -758,8 +810,8 @@ __global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, c
     uint32_t rank = 0;
     for (int j = 0; j < m; ++j) {   // interior children are still counted: the scan expects them
         if (e[j].ref >= 0) {
-            const uint32_t wi = next_base + off[i] + rank;
-            next[off[i] + rank] = make_int4(e[j].ref, (int)wi, it.z + 1, 0);
+            const uint32_t wi = next_base + off_i + rank;
+            next[off_i + rank] = make_int4(e[j].ref, (int)wi, it.z + 1, 0);
             ref[j] = (int)wi;
             ++rank;
         } else {
@@ -772,6 +824,23 @@ __global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, c
     w.ref[0] = make_int4(ref[0], ref[1], ref[2], ref[3]);
     w.ref[1] = make_int4(ref[4], ref[5], ref[6], ref[7]);
     out[it.y] = w;
+}
+__device__ void wide_emit_item(const BvhNode* bin, const int4* items, uint32_t i, const uint32_t* off,
+                               uint32_t next_base, WideNode* out, int4* next, uint32_t* err, const RefitLinks& links) {
+    const int4 it = items[i];
+    const RefitLinks* lk = links.parent ? &links : nullptr;
+    WEnt e[8];
+    int m = wide_expand(bin, it.x, e, lk);
+    if (m < 0) {
+        atomicOr(err, kBuildErrRange);
+        m = 0;
+    }
+    wide_write(e, m, it, off[i], next_base, out, next, err, lk);
+}
+__global__ void k_wide_emit(const BvhNode* bin, const int4* items, uint32_t n, const uint32_t* off, uint32_t next_base,
+                            WideNode* out, int4* next, uint32_t* err, RefitLinks links) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) wide_emit_item(bin, items, i, off, next_base, out, next, err, links);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -913,6 +982,565 @@ __global__ void __launch_bounds__(kScanB) k_scan_fix(const T* in, uint32_t n, T*
     out[i] = add_(sub_(out[i], in[i]), before);
 }
 
+// ---------------------------------------------------------------------------------------------
+// the instance level in one cooperative launch
+//
+// The same rounds, small tasks and collapse levels as the per-round kernels (so the same
+// trees), run by one persistent grid whose blocks are all resident (cooperative launch) and
+// meet at grid_sync between the steps of a round. Counts that the host reads back between
+// rounds elsewhere stay on the device: block 0 scans, every thread reads the totals after
+// the next barrier and updates its own copy of the round state, so every thread takes the
+// same branches. Buffers are sized from the instance count beforehand (a tree of n
+// single-instance leaves has n - 1 interior nodes), so nothing grows during the build. The
+// host waits once, for the result record.
+
+constexpr long long kSyncCycles = 1ll << 31;   // ~1 s at 2 GHz: a barrier gives up after this
+constexpr uint32_t kBuildErrSync = 4u;          // a barrier gave up
+constexpr uint32_t kBuildErrCap = 8u;           // a count exceeded the buffers sized beforehand
+constexpr uint32_t kBuildErrRounds = 16u;       // more than 64 rounds or collapse levels
+
+// Grid-wide barrier of the cooperative launch: sync[0] arrivals, sync[1] generation, sync[2]
+// error. Thread 0 of each block arrives; the last arrival resets the count and bumps the
+// generation, the others wait for the bump with a bounded wait. Returns false (for the whole
+// block) once any block gave up, so that every block leaves its loops.
+__device__ bool grid_sync(uint32_t* sync) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile uint32_t* vs = sync;
+        int good = vs[2] == 0u;
+        if (good) {
+            const uint32_t gen = vs[1];
+            __threadfence();
+            if (atomicAdd(&sync[0], 1u) == gridDim.x - 1u) {
+                atomicExch(&sync[0], 0u);
+                __threadfence();
+                atomicAdd(&sync[1], 1u);
+            } else {
+                const long long t0 = clock64();
+                while (vs[1] == gen) {
+                    if (vs[2] != 0u) { good = 0; break; }
+                    if (clock64() - t0 > kSyncCycles) { atomicOr(&sync[2], kBuildErrSync); good = 0; break; }
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+        }
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Exclusive scan of in[0, n) into out by one block of kBt threads; *total = the sum.
+template <class T>
+__device__ void block_scan_excl(const T* in, uint32_t n, T* out, T* total) {
+    __shared__ T s[kBt];
+    T carry = zero_<T>();
+    for (uint32_t base = 0; base < n; base += kBt) {
+        const uint32_t i = base + threadIdx.x;
+        const T v = i < n ? __ldcg(in + i) : zero_<T>();
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < kBt; o <<= 1) {
+            const T u = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : zero_<T>();
+            __syncthreads();
+            s[threadIdx.x] = add_(s[threadIdx.x], u);
+            __syncthreads();
+        }
+        if (i < n) out[i] = add_(carry, sub_(s[threadIdx.x], v));
+        carry = add_(carry, s[kBt - 1]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// ---- warp-wide forms for the instance level (few tasks, each on a 32-lane warp) ----
+
+struct WBox {
+    float b[6];   // lo xyz, hi xyz
+    uint32_t c;   // primitives
+};
+__device__ __forceinline__ WBox wbox_join(const WBox& x, const WBox& y) {
+    WBox r;
+    for (int j = 0; j < 3; ++j) { r.b[j] = fminf(x.b[j], y.b[j]); r.b[3 + j] = fmaxf(x.b[3 + j], y.b[3 + j]); }
+    r.c = x.c + y.c;
+    return r;
+}
+__device__ __forceinline__ WBox wbox_shfl_up(const WBox& x, int o) {
+    WBox r;
+    for (int j = 0; j < 6; ++j) r.b[j] = __shfl_up_sync(0xFFFFFFFFu, x.b[j], o, 16);
+    r.c = __shfl_up_sync(0xFFFFFFFFu, x.c, o, 16);
+    return r;
+}
+__device__ __forceinline__ WBox wbox_shfl_down(const WBox& x, int o) {
+    WBox r;
+    for (int j = 0; j < 6; ++j) r.b[j] = __shfl_down_sync(0xFFFFFFFFu, x.b[j], o, 16);
+    r.c = __shfl_down_sync(0xFFFFFFFFu, x.c, o, 16);
+    return r;
+}
+
+// sah_axis over two axes at once: lanes 0..15 hold the bins of axis `a0`, lanes 16..31 those
+// of axis `a1` (bin = lane & 15; an axis < 0 takes no part). Each half computes the cost at
+// its 15 bin boundaries from prefix and suffix unions; the warp keeps the candidate the
+// serial sweep over the axes in order would keep: the smallest cost, then the smaller axis,
+// then the first boundary, if that cost is below *best (NaN costs never win). Every lane
+// returns the same answer.
+__device__ void sah_pair_warp(const WBox& bin, int a0, int a1, float* best, int* best_axis, int* best_bin,
+                              uint32_t* best_left) {
+    const int lane = threadIdx.x & 31, l16 = lane & 15;
+    const int axis = lane < 16 ? a0 : a1;
+    WBox pre = bin, suf = bin;
+    for (int o = 1; o < 16; o <<= 1) {
+        const WBox u = wbox_shfl_up(pre, o), d = wbox_shfl_down(suf, o);
+        if (l16 >= o) pre = wbox_join(pre, u);
+        if (l16 + o < 16) suf = wbox_join(suf, d);
+    }
+    const WBox right = wbox_shfl_down(suf, 1);   // bins l16 + 1 .. 15 of the same half
+    bool ok = axis >= 0 && l16 < kBins - 1 && pre.c != 0u && right.c != 0u;
+    float cost = 0.0f;
+    if (ok) cost = area6(pre.b) * (float)pre.c + area6(right.b) * (float)right.c;
+    ok = ok && cost < *best;
+    float bc = ok ? cost : INFINITY;
+    int bk = ok ? (axis << 4) | l16 : 0x7FFFFFFF;   // (axis, boundary) order key
+    int bl = lane;
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oc = __shfl_xor_sync(0xFFFFFFFFu, bc, o);
+        const int ok2 = __shfl_xor_sync(0xFFFFFFFFu, bk, o);
+        const int ol = __shfl_xor_sync(0xFFFFFFFFu, bl, o);
+        if (ok2 != 0x7FFFFFFF && (bk == 0x7FFFFFFF || oc < bc || (oc == bc && ok2 < bk))) { bc = oc; bk = ok2; bl = ol; }
+    }
+    const uint32_t left = __shfl_sync(0xFFFFFFFFu, pre.c, bl);
+    if (bk != 0x7FFFFFFF) {
+        *best = bc;
+        *best_axis = bk >> 4;
+        *best_bin = (bk & 15) + 1;
+        *best_left = left;
+    }
+}
+
+// The bins of axis k (lanes 0..15 or 16..31 of a warp) from the task's global bins.
+__device__ __forceinline__ WBox load_bins(const int* b, int k, int l16) {
+    WBox w;
+    const int* q = &b[(k * kBins + l16) * 7];
+    for (int j = 0; j < 6; ++j) w.b[j] = o2f(q[j]);
+    w.c = (uint32_t)q[6];
+    return w;
+}
+__device__ __forceinline__ WBox empty_wbox() {
+    WBox w;
+    for (int j = 0; j < 3; ++j) { w.b[j] = INFINITY; w.b[3 + j] = -INFINITY; }
+    w.c = 0u;
+    return w;
+}
+
+// split_task with one warp per task: the same split (axes 0 and 1 in one pass, then axis 2).
+__device__ void split_task_warp(const BigTask* tasks, uint32_t t, const int* bins, const int* tb, Split* split,
+                                BvhNode* nodes, float* root_box, uint32_t node_base) {
+    const int lane = threadIdx.x & 31, l16 = lane & 15;
+    const BigTask T = tasks[t];
+    const int* tbt = tb + 12 * (size_t)t;
+    if (lane == 0) {
+        float box[6];
+        for (int j = 0; j < 6; ++j) box[j] = o2f(tbt[j]);
+        write_child(nodes, root_box, T.parent, T.side, box, (int)node_base + T.node);
+    }
+    const int* b = bins + (size_t)t * kBinWords;
+    Split sp;
+    sp.axis = -1; sp.bin = 0; sp.nleft = (T.end - T.begin) / 2u; sp.clo = 0.0f; sp.scale = 0.0f;
+    float best = INFINITY;
+    float clo[3], scale[3];
+    int use[3];
+    for (int k = 0; k < 3; ++k) {
+        axis_scale(tbt, k, &clo[k], &scale[k]);
+        use[k] = scale[k] > 0.0f ? k : -1;
+    }
+    {
+        const int k = lane < 16 ? use[0] : use[1];
+        sah_pair_warp(k >= 0 ? load_bins(b, k, l16) : empty_wbox(), use[0], use[1], &best, &sp.axis, &sp.bin,
+                      &sp.nleft);
+    }
+    if (use[2] >= 0)
+        sah_pair_warp(lane < 16 ? load_bins(b, 2, l16) : empty_wbox(), 2, -1, &best, &sp.axis, &sp.bin, &sp.nleft);
+    if (sp.axis >= 0) { sp.clo = clo[sp.axis]; sp.scale = scale[sp.axis]; }
+    if (lane == 0) split[t] = sp;
+}
+
+// small_task for instance leaves (one instance per leaf) with one warp per task. The task's
+// instances (at most kSmall = 32: lane q holds the range's q-th) are staged once in the warp's
+// shared memory with their boxes and centroids; per range: bounds by warp reductions, the bins
+// of all three axes in shared memory, the same binned-SAH choice as the serial sweep, and a
+// stable partition by ballots (the rounds' order) of the staged entries. The range stack is
+// warp-uniform.
+__device__ void small_task_warp(const Geo& g, uint32_t* idx, const SmallTask* st, uint32_t i, BvhNode* nodes,
+                                float* root_box, const uint32_t* prim_map, uint32_t node_base, uint32_t* info) {
+    constexpr int kW = kBt / 32;
+    __shared__ int sbins[kW][3][kBins * 7];
+    __shared__ float sbox[kW][9][32];   // lo xyz, hi xyz, centroid xyz of each staged entry
+    __shared__ uint32_t sprim[kW][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const SmallTask S = st[i];
+    const uint32_t m = S.end - S.begin;
+    if (m > 32u) {   // not produced by the rounds (ranges of more than kSmall are big tasks)
+        if (lane == 0) atomicOr(&info[2], kBuildErrRange);
+        return;
+    }
+    if ((uint32_t)lane < m) {
+        const uint32_t p = idx[S.begin + lane];
+        sprim[wid][lane] = p;
+        for (int k = 0; k < 6; ++k) sbox[wid][k][lane] = g.box[6 * (size_t)p + k];
+        for (int k = 0; k < 3; ++k) sbox[wid][6 + k][lane] = g.cent[3 * (size_t)p + k];
+    }
+    __syncwarp();
+    struct Item {
+        uint32_t b, e;   // positions relative to S.begin
+        int parent, side, depth;
+    };
+    Item stk[kSmallStack];
+    int sp = 0;
+    stk[sp++] = Item{0u, m, S.parent, S.side, S.depth};
+    uint32_t res = S.res0, used = 0;
+    int maxd = 0;
+    bool first = true;
+    const int pinf = f2o(INFINITY), ninf = f2o(-INFINITY);
+    while (sp > 0) {
+        const Item it = stk[--sp];
+        const uint32_t n = it.e - it.b;
+        const bool valid = (uint32_t)lane < n;
+        const uint32_t pos = it.b + (valid ? (uint32_t)lane : 0u);
+        const uint32_t p = sprim[wid][pos];
+        float box[6], cen[3], clo[3], chi[3], ubox[6];
+        for (int k = 0; k < 3; ++k) {
+            box[k] = valid ? sbox[wid][k][pos] : INFINITY;
+            box[3 + k] = valid ? sbox[wid][3 + k][pos] : -INFINITY;
+            cen[k] = sbox[wid][6 + k][pos];
+            clo[k] = valid ? cen[k] : INFINITY;
+            chi[k] = valid ? cen[k] : -INFINITY;
+        }
+        for (int k = 0; k < 6; ++k) ubox[k] = box[k];
+        for (int o = 16; o > 0; o >>= 1)
+            for (int k = 0; k < 3; ++k) {
+                ubox[k] = fminf(ubox[k], __shfl_xor_sync(0xFFFFFFFFu, ubox[k], o));
+                ubox[3 + k] = fmaxf(ubox[3 + k], __shfl_xor_sync(0xFFFFFFFFu, ubox[3 + k], o));
+                clo[k] = fminf(clo[k], __shfl_xor_sync(0xFFFFFFFFu, clo[k], o));
+                chi[k] = fmaxf(chi[k], __shfl_xor_sync(0xFFFFFFFFu, chi[k], o));
+            }
+        maxd = max(maxd, it.depth);
+        const bool leaf = n == 1u;
+        int best_axis = -1, best_bin = 0;
+        uint32_t best_left = 0;
+        float best = INFINITY, scale[3];
+        if (!leaf) {
+            int use[3];
+            for (int k = 0; k < 3; ++k) {
+                const float ext = chi[k] - clo[k];
+                use[k] = ext > 0.0f ? k : -1;
+                scale[k] = ext > 0.0f ? (float)kBins / ext : 0.0f;
+            }
+            for (int j = lane; j < 3 * kBins * 7; j += 32) {
+                const int q = j % 7;
+                (&sbins[wid][0][0])[j] = q == 6 ? 0 : (q < 3 ? pinf : ninf);
+            }
+            __syncwarp();
+            if (valid)
+                for (int k = 0; k < 3; ++k) {
+                    if (use[k] < 0) continue;
+                    int* c = &sbins[wid][k][bin_of(cen[k], clo[k], scale[k]) * 7];
+                    for (int j = 0; j < 3; ++j) {
+                        atomicMin(&c[j], f2o(box[j]));
+                        atomicMax(&c[3 + j], f2o(box[3 + j]));
+                    }
+                    atomicAdd(&c[6], 1);
+                }
+            __syncwarp();
+            WBox w = empty_wbox();
+            const int k01 = lane < 16 ? use[0] : use[1];
+            if (k01 >= 0) {
+                const int* q = &sbins[wid][k01][(lane & 15) * 7];
+                for (int j = 0; j < 6; ++j) w.b[j] = o2f(q[j]);
+                w.c = (uint32_t)q[6];
+            }
+            WBox w2 = empty_wbox();
+            if (lane < 16 && use[2] >= 0) {
+                const int* q = &sbins[wid][2][lane * 7];
+                for (int j = 0; j < 6; ++j) w2.b[j] = o2f(q[j]);
+                w2.c = (uint32_t)q[6];
+            }
+            __syncwarp();
+            sah_pair_warp(w, use[0], use[1], &best, &best_axis, &best_bin, &best_left);
+            if (use[2] >= 0) sah_pair_warp(w2, 2, -1, &best, &best_axis, &best_bin, &best_left);
+        }
+        if (leaf) {
+            if (lane == 0) {
+                const uint32_t payload = prim_map[p] << 3;
+                const int ref = (int)(~payload);
+                if (it.parent >= 0) {
+                    write_child(nodes, root_box, it.parent, it.side, ubox, ref);
+                } else {
+                    // a root that is a single leaf: interior root whose second child never intersects
+                    write_child(nodes, root_box, it.parent, it.side, ubox, 0);
+                    BvhNode nd;
+                    nd.a = make_float4(widen_lo(ubox[0]), widen_lo(ubox[1]), widen_lo(ubox[2]), widen_hi(ubox[3]));
+                    nd.b = make_float4(widen_hi(ubox[4]), widen_hi(ubox[5]), kFar, kFar);
+                    nd.c = make_float4(kFar, kFar, kFar, kFar);
+                    nd.d = make_int4(ref, kRefPop, 0, 0);
+                    nodes[S.root_node] = nd;
+                }
+            }
+            if (it.parent < 0) ++used;
+            first = false;
+            continue;
+        }
+        if (!(first && S.root_node >= 0) && res >= S.res0 + (m - 1u)) {
+            if (lane == 0) atomicOr(&info[2], kBuildErrRange);
+            break;
+        }
+        const int me = (first && S.root_node >= 0) ? S.root_node : (int)(res++);
+        first = false;
+        ++used;
+        if (lane == 0) write_child(nodes, root_box, it.parent, it.side, ubox, (int)node_base + me);
+        uint32_t mid;
+        if (best_axis < 0) {
+            mid = it.b + n / 2u;
+        } else {
+            const bool left = valid && bin_of(cen[best_axis], clo[best_axis], scale[best_axis]) < best_bin;
+            const unsigned ml = __ballot_sync(0xFFFFFFFFu, left), mv = __ballot_sync(0xFFFFFFFFu, valid);
+            const unsigned below = (1u << lane) - 1u;
+            const uint32_t nl = (uint32_t)__popc(ml);
+            const uint32_t to = it.b + (left ? (uint32_t)__popc(ml & below) : nl + (uint32_t)__popc(mv & ~ml & below));
+            __syncwarp();
+            if (valid) {
+                sprim[wid][to] = p;
+                for (int k = 0; k < 3; ++k) {
+                    sbox[wid][k][to] = box[k];
+                    sbox[wid][3 + k][to] = box[3 + k];
+                    sbox[wid][6 + k][to] = cen[k];
+                }
+            }
+            __syncwarp();
+            mid = it.b + nl;
+            if (mid == it.b || mid == it.e) mid = it.b + n / 2u;
+        }
+        if (sp + 2 > kSmallStack) {
+            if (lane == 0) atomicOr(&info[2], kBuildErrStack);
+            break;
+        }
+        stk[sp++] = Item{mid, it.e, me, 1, it.depth + 1};
+        stk[sp++] = Item{it.b, mid, me, 0, it.depth + 1};
+    }
+    if (lane == 0) {
+        atomicAdd(&info[0], used);
+        atomicMax(&info[1], (uint32_t)maxd);
+    }
+}
+
+// The collapse of the instance level with the expansion cached: the count step expands a
+// node (recording the refit links as it goes) and keeps its at most 8 entries, the emit step
+// quantizes and writes them without walking the two-child nodes again.
+__device__ void wide_count_cache_item(const BvhNode* bin, const int4* items, uint32_t i, uint32_t* cnt, WEnt* cache,
+                                      int* cache_n, const RefitLinks& links) {
+    const RefitLinks* lk = links.parent ? &links : nullptr;
+    WEnt e[8];
+    const int m = wide_expand(bin, items[i].x, e, lk);
+    uint32_t c = 0;
+    for (int j = 0; j < m; ++j) {
+        c += e[j].ref >= 0 ? 1u : 0u;
+        cache[8 * (size_t)i + j] = e[j];
+    }
+    cache_n[i] = m;
+    cnt[i] = c;   // 0 for a malformed node (m < 0): the emit step reports it
+}
+__device__ void wide_emit_cached_item(const WEnt* cache, const int* cache_n, const int4* items, uint32_t i,
+                                      const uint32_t* off, uint32_t next_base, WideNode* out, int4* next, uint32_t* err,
+                                      const RefitLinks& links) {
+    const int4 it = items[i];
+    const RefitLinks* lk = links.parent ? &links : nullptr;
+    WEnt e[8];
+    int m = cache_n[i];
+    if (m < 0 || m > 8) {
+        atomicOr(err, kBuildErrRange);
+        m = 0;
+    }
+    for (int j = 0; j < m; ++j) e[j] = cache[8 * (size_t)i + j];
+    wide_write(e, m, it, off[i], next_base, out, next, err, lk);
+}
+
+struct InstLevelArgs {
+    const GpuInstBox* inst;      // n instances of the tree (device)
+    uint32_t n;
+    const float* mesh_box;       // 6 per mesh
+    float *box, *cent;           // 6 / 3 per instance
+    uint32_t *idx, *tmp, *map;   // n each; map: instance index of each primitive
+    BigTask* tasks[2];
+    uint32_t *w0[2], *wtask[2], *wbeg[2], *wend[2];
+    int *bins, *tb;
+    Split* split;
+    uint32_t *wleft, *wleft_scan;
+    uint4 *cc, *cc_scan;
+    SmallTask* small;
+    uint32_t cap_t, cap_w, cap_s;   // task, work-item and small-task capacities
+    BvhNode* nodes;              // the two-child slots, relative index (bin + node_base)
+    const BvhNode* bin;          // the whole node array, for the collapse
+    uint32_t node_base, node_cap;
+    float* root_box;             // 6 floats
+    uint32_t* info;              // [0] nodes used by small tasks, [1] their depth, [2] build errors, [3] collapse errors
+    int4* witems[2];
+    uint32_t *wcnt, *woff, item_cap;
+    WEnt* wcache;                // 8 entries per collapse item of the level
+    int* wcache_n;
+    WideNode* wide;
+    uint32_t wide_base, wide_cap;
+    RefitLinks lk;
+    uint32_t* sync;              // grid_sync state, 3 words, zero at launch
+    uint4* tot4;
+    uint32_t* tot32;
+    uint32_t* result;            // node slots, nodes used, depth, wide nodes, wide levels, error bits
+};
+
+__global__ void __launch_bounds__(kBt) k_inst_level(InstLevelArgs a) {
+    const uint32_t gtid = blockIdx.x * kBt + threadIdx.x, gthreads = gridDim.x * kBt;
+    const uint32_t gwarp = gtid >> 5, gwarps = gthreads >> 5;
+    const Geo g{a.box, a.cent};
+    const uint32_t n = a.n;
+    uint32_t err = 0;
+    // instance boxes, the identity order and the root task
+    for (uint32_t i = gtid; i < n; i += gthreads) {
+        const GpuInstBox ib = a.inst[i];
+        float b[6];
+        inst_box(ib, a.mesh_box, b);
+        for (int r = 0; r < 3; ++r) {
+            a.box[6 * (size_t)i + r] = b[r];
+            a.box[6 * (size_t)i + 3 + r] = b[3 + r];
+            a.cent[3 * (size_t)i + r] = 0.5f * (b[r] + b[3 + r]);
+        }
+        a.idx[i] = i;
+        a.map[i] = ib.inst;
+    }
+    uint32_t ntask = 0, nwork = 0, nsmall = 0, next_node = 0, nodes_used = 0, rounds = 0;
+    int cur = 0;
+    if (n > kSmall) {
+        ntask = 1;
+        nwork = (n + kChunk - 1) / kChunk;
+        next_node = 1;
+        if (gtid == 0) {
+            a.tasks[0][0] = BigTask{0, -1, 0, 0, 0u, n};
+            a.w0[0][0] = 0;
+        }
+        for (uint32_t k = gtid; k < nwork; k += gthreads) {
+            a.wtask[0][k] = 0;
+            a.wbeg[0][k] = k * kChunk;
+            a.wend[0][k] = min((k + 1) * kChunk, n);
+        }
+        clear_bins(a.bins, a.tb, 1, gtid, gthreads);
+    } else if (n > 0) {
+        nsmall = 1;
+        next_node = n;   // the root and its n - 1 reserved slots
+        if (gtid == 0) a.small[0] = SmallTask{-1, 0, 0, 0, 0u, n, 1u, 0u};
+    }
+    if (gtid == 0)
+        for (int k = 0; k < 3; ++k) { a.root_box[k] = INFINITY; a.root_box[3 + k] = -INFINITY; }
+    bool live = grid_sync(a.sync);
+    while (live && ntask > 0) {
+        if (++rounds > 64) { err |= kBuildErrRounds; break; }
+        for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+            bounds_item(g, a.idx, a.wtask[cur], a.wbeg[cur], a.wend[cur], a.tb, w);
+            __syncthreads();
+        }
+        if (!(live = grid_sync(a.sync))) break;
+        for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+            bin_item(g, a.idx, a.tb, a.wtask[cur], a.wbeg[cur], a.wend[cur], a.bins, w);
+            __syncthreads();
+        }
+        if (!(live = grid_sync(a.sync))) break;
+        for (uint32_t t = gwarp; t < ntask; t += gwarps)
+            split_task_warp(a.tasks[cur], t, a.bins, a.tb, a.split, a.nodes, a.root_box, a.node_base);
+        if (!(live = grid_sync(a.sync))) break;
+        for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+            count_left_item(g, a.idx, a.split, a.tasks[cur], a.wtask[cur], a.wbeg[cur], a.wend[cur], a.wleft, w);
+            __syncthreads();
+        }
+        for (uint32_t t = gtid; t < ntask; t += gthreads) child_counts_task(a.tasks[cur], t, a.split, a.cc);
+        if (!(live = grid_sync(a.sync))) break;
+        if (blockIdx.x == 0) block_scan_excl<uint32_t>(a.wleft, nwork, a.wleft_scan, a.tot32);
+        if (blockIdx.x == (gridDim.x > 1u ? 1u : 0u)) block_scan_excl<uint4>(a.cc, ntask, a.cc_scan, a.tot4);
+        if (!(live = grid_sync(a.sync))) break;
+        const uint4 tot = __ldcg(a.tot4);
+        const uint32_t nbig = tot.x, nwork_next = tot.y, nsm = tot.z, nres = tot.w;
+        if (nbig > a.cap_t || nwork_next > a.cap_w || nsmall + nsm > a.cap_s ||
+            (uint64_t)next_node + nbig + nres > a.node_cap) {
+            err |= kBuildErrCap;
+            break;
+        }
+        const uint32_t node0 = next_node, res0 = next_node + nbig;
+        const int nx = cur ^ 1;
+        for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) {
+            scatter_item(g, a.idx, a.tmp, a.split, a.tasks[cur], a.wtask[cur], a.wbeg[cur], a.wend[cur],
+                         a.wleft_scan, a.w0[cur], a.info, w);
+            __syncthreads();
+        }
+        for (uint32_t t = gtid; t < ntask; t += gthreads)
+            emit_task(a.tasks[cur], t, a.split, a.cc_scan, node0, res0, nsmall, a.tasks[nx], a.wtask[nx], a.wbeg[nx],
+                      a.wend[nx], a.w0[nx], a.small);
+        if (!(live = grid_sync(a.sync))) break;
+        for (uint32_t w = blockIdx.x; w < nwork; w += gridDim.x) copy_back_item(a.tmp, a.idx, a.wbeg[cur], a.wend[cur], w);
+        clear_bins(a.bins, a.tb, nbig, gtid, gthreads);
+        nodes_used += ntask;
+        nsmall += nsm;
+        next_node += nbig + nres;
+        ntask = nbig;
+        nwork = nwork_next;
+        cur = nx;
+        live = grid_sync(a.sync);
+    }
+    if (live && err == 0u) {
+        for (uint32_t i = gwarp; i < nsmall; i += gwarps)
+            small_task_warp(g, a.idx, a.small, i, a.nodes, a.root_box, a.map, a.node_base, a.info);
+        live = grid_sync(a.sync);
+    }
+    // the collapse of the one tree into wide nodes [wide_base, ...)
+    uint32_t wn = 0, wnext = a.wide_base, levels = 0;
+    int wc = 0;
+    if (live && err == 0u && n > 0) {
+        if ((uint64_t)a.wide_base + 1u > a.wide_cap || a.item_cap < 1u) {
+            err |= kBuildErrCap;
+        } else {
+            wn = 1;
+            wnext = a.wide_base + 1u;
+            if (gtid == 0) a.witems[0][0] = make_int4((int)a.node_base, (int)a.wide_base, 1, 0);
+            live = grid_sync(a.sync);
+        }
+    }
+    while (live && err == 0u && wn > 0) {
+        if (++levels > 64) { err |= kBuildErrRounds; break; }
+        for (uint32_t i = gtid; i < wn; i += gthreads)
+            wide_count_cache_item(a.bin, a.witems[wc], i, a.wcnt, a.wcache, a.wcache_n, a.lk);
+        if (!(live = grid_sync(a.sync))) break;
+        if (blockIdx.x == 0) block_scan_excl<uint32_t>(a.wcnt, wn, a.woff, a.tot32);
+        if (!(live = grid_sync(a.sync))) break;
+        const uint32_t tot = __ldcg(a.tot32);
+        if ((uint64_t)wnext + tot > a.wide_cap || tot > a.item_cap) { err |= kBuildErrCap; break; }
+        for (uint32_t i = gtid; i < wn; i += gthreads)
+            wide_emit_cached_item(a.wcache, a.wcache_n, a.witems[wc], i, a.woff, wnext, a.wide, a.witems[wc ^ 1],
+                                  a.info + 3, a.lk);
+        if (!(live = grid_sync(a.sync))) break;
+        wnext += tot;
+        wn = tot;
+        wc ^= 1;
+    }
+    // every thread has the same err (it follows from values all threads read); the last
+    // barrier makes the small tasks' and the collapse's error words complete
+    if (live) live = grid_sync(a.sync);
+    if (gtid == 0) {
+        const uint32_t used_small = __ldcg(a.info), depth_small = __ldcg(a.info + 1);
+        a.result[0] = next_node;
+        a.result[1] = nodes_used + used_small;
+        a.result[2] = max(rounds, depth_small);
+        a.result[3] = wnext - a.wide_base;
+        a.result[4] = levels;
+        a.result[5] = err | __ldcg(a.info + 2) | __ldcg(a.info + 3) | __ldcg(a.sync + 2) | (live ? 0u : kBuildErrSync);
+    }
+}
+
 template <class T>
 struct DBuf {
     T* p = nullptr;
@@ -972,7 +1600,10 @@ struct GpuBvh {
     DBuf<MeshRange> ranges;
     DBuf<GpuInstBox> inst;
     DBuf<int4> witems[2];
-    DBuf<uint32_t> wcnt, woff, werr;
+    DBuf<uint32_t> wcnt, woff, werr, sync, result;
+    DBuf<WEnt> wcache;
+    DBuf<int> wcache_n;
+    uint32_t* result_host = nullptr;   // page-locked copy of the instance level's result record
     uint32_t launches = 0;   // kernels launched by all builds so far
 
     ~GpuBvh() {
@@ -984,6 +1615,8 @@ struct GpuBvh {
         cc.release(); cc_scan.release(); bsum4.release(); tot4.release(); bins.release(); tb.release();
         split.release(); small.release(); nodes.release(); ranges.release(); inst.release();
         witems[0].release(); witems[1].release(); wcnt.release(); woff.release(); werr.release();
+        sync.release(); result.release(); wcache.release(); wcache_n.release();
+        if (result_host) cudaFreeHost(result_host);
     }
 
     template <class T>
@@ -1245,6 +1878,97 @@ cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint
     const std::vector<uint32_t> rb(1, 0u), re(1, n);
     GK_TRY(B->build(n, rb, re, 1, true, B->map.p, node_base, out, st));
     return cudaStreamSynchronize(st);
+}
+
+cudaError_t gpu_bvh_build_instance_level(GpuBvh* B, const GpuInstBox* inst, uint32_t n, const float* mesh_box,
+                                        BvhNode* nodes, uint32_t node_base, uint32_t node_cap, WideNode* wide,
+                                        uint32_t wide_base, uint32_t wide_cap, const RefitLinks* links,
+                                        InstLevelResult* res, cudaStream_t st) {
+    *res = InstLevelResult();
+    if (n == 0) return cudaSuccess;
+    if ((uint64_t)node_cap < (uint64_t)n + 1u) return cudaErrorInvalidValue;
+    const uint32_t cap_t = n / (kSmall + 1u) + 2u, cap_w = cap_t + n / kChunk + 2u, cap_s = n + 1u;
+    GK_TRY(B->map.need(n));
+    GK_TRY(B->box.need(6 * (size_t)n));
+    GK_TRY(B->cent.need(3 * (size_t)n));
+    GK_TRY(B->idx.need(n));
+    GK_TRY(B->tmp.need(n));
+    for (int k = 0; k < 2; ++k) {
+        GK_TRY(B->tasks[k].need(cap_t));
+        GK_TRY(B->w0[k].need(cap_t));
+        GK_TRY(B->wtask[k].need(cap_w));
+        GK_TRY(B->wbeg[k].need(cap_w));
+        GK_TRY(B->wend[k].need(cap_w));
+        GK_TRY(B->witems[k].need(cap_s));
+    }
+    GK_TRY(B->bins.need((size_t)cap_t * kBinWords));
+    GK_TRY(B->tb.need((size_t)cap_t * 12));
+    GK_TRY(B->split.need(cap_t));
+    GK_TRY(B->wleft.need(cap_w));
+    GK_TRY(B->wleft_scan.need(cap_w));
+    GK_TRY(B->cc.need(cap_t));
+    GK_TRY(B->cc_scan.need(cap_t));
+    GK_TRY(B->small.need(cap_s));
+    GK_TRY(B->root_box.need(6));
+    GK_TRY(B->info.need(4));
+    GK_TRY(B->wcnt.need(cap_s));
+    GK_TRY(B->woff.need(cap_s));
+    GK_TRY(B->wcache.need(8 * (size_t)cap_s));
+    GK_TRY(B->wcache_n.need(cap_s));
+    GK_TRY(B->tot4.need(1));
+    GK_TRY(B->tot32.need(1));
+    GK_TRY(B->sync.need(3));
+    GK_TRY(B->result.need(8));
+    if (!B->result_host) GK_TRY(cudaMallocHost((void**)&B->result_host, 8 * sizeof(uint32_t)));
+    GK_TRY(cudaMemsetAsync(B->info.p, 0, 16, st));
+    GK_TRY(cudaMemsetAsync(B->sync.p, 0, 12, st));
+    GK_TRY(cudaMemsetAsync(nodes + node_base, 0, (size_t)node_cap * sizeof(BvhNode), st));
+    InstLevelArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.inst = inst; a.n = n; a.mesh_box = mesh_box;
+    a.box = B->box.p; a.cent = B->cent.p; a.idx = B->idx.p; a.tmp = B->tmp.p; a.map = B->map.p;
+    for (int k = 0; k < 2; ++k) {
+        a.tasks[k] = B->tasks[k].p; a.w0[k] = B->w0[k].p; a.wtask[k] = B->wtask[k].p;
+        a.wbeg[k] = B->wbeg[k].p; a.wend[k] = B->wend[k].p; a.witems[k] = B->witems[k].p;
+    }
+    a.bins = B->bins.p; a.tb = B->tb.p; a.split = B->split.p; a.wleft = B->wleft.p; a.wleft_scan = B->wleft_scan.p;
+    a.cc = B->cc.p; a.cc_scan = B->cc_scan.p; a.small = B->small.p;
+    a.cap_t = cap_t; a.cap_w = cap_w; a.cap_s = cap_s;
+    a.nodes = nodes + node_base; a.bin = nodes; a.node_base = node_base; a.node_cap = node_cap;
+    a.root_box = B->root_box.p; a.info = B->info.p;
+    a.wcnt = B->wcnt.p; a.woff = B->woff.p; a.item_cap = cap_s;
+    a.wcache = B->wcache.p; a.wcache_n = B->wcache_n.p;
+    a.wide = wide; a.wide_base = wide_base; a.wide_cap = wide_cap;
+    if (links) a.lk = *links;
+    a.sync = B->sync.p; a.tot4 = B->tot4.p; a.tot32 = B->tot32.p; a.result = B->result.p;
+    // one block per 256 instances, at most one per SM: every block is resident (cooperative
+    // launch), and a barrier costs one arrival per block
+    int dev = 0, sms = 1, per = 0;
+    GK_TRY(cudaGetDevice(&dev));
+    GK_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GK_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_inst_level, kBt, 0));
+    if (per < 1) return cudaErrorLaunchOutOfResources;
+    const uint32_t grid = std::max<uint32_t>(1u, std::min<uint32_t>((n + kBt - 1) / kBt, (uint32_t)sms));
+    void* params[] = {&a};
+    GK_TRY(cudaLaunchCooperativeKernel((const void*)k_inst_level, dim3(grid), dim3(kBt), params, 0, st));
+    ++B->launches;
+    GK_TRY(cudaMemcpyAsync(B->result_host, B->result.p, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GK_TRY(cudaStreamSynchronize(st));
+    const uint32_t* r = B->result_host;
+    res->node_count = r[0];
+    res->nodes_used = r[1];
+    res->depth = (int)r[2];
+    res->wide_count = r[3];
+    res->wide_depth = (int)r[4];
+    res->error = r[5];
+    return cudaSuccess;
+}
+
+bool gpu_bvh_cooperative_supported() {
+    int dev = 0, coop = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess) return false;
+    return coop != 0;
 }
 
 cudaError_t gpu_bvh_collapse(GpuBvh* B, const BvhNode* bin, const std::vector<int>& roots, uint32_t wide_base,

@@ -577,6 +577,52 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
     const uint32_t base = ctx->blas_node_count;
     int rc;
     if (!ctx->host_build) {
+        if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
+        // the instance tables first: their host work and uploads overlap the stream's earlier work
+        if ((rc = upload_instances(ctx, st)) != GKRT_OK) return rc;
+        if (gpu_bvh_cooperative_supported()) {
+            // the tree's members, staged in page-locked memory and uploaded into the refit's
+            // instance buffer (a refit rewrites it whole); one cooperative launch builds and
+            // collapses the level; the host waits once
+            uint32_t m = 0;
+            for (uint32_t i = 0; i < n; ++i) m += (ctx->inst[i].visible && ctx->blas_root[ctx->inst[i].mesh_id] >= 0);
+            const uint32_t slots = m + 1u;
+            if ((rc = ensure_node_cap(ctx, (size_t)base + slots)) != GKRT_OK) return rc;
+            if ((rc = ensure_wide_cap(ctx, (size_t)ctx->blas_wide_count + slots + 1, ctx->blas_wide_count)) != GKRT_OK)
+                return rc;
+            if ((rc = prepare_refit(ctx, slots, st)) != GKRT_OK) return rc;
+            tlas_members(ctx, ctx->tlas_members);
+            GpuInstBox* hb = static_cast<GpuInstBox*>(stage_buf(ctx, 5, sizeof(GpuInstBox) * (size_t)m + 16));
+            if (!hb) return fail(ctx, GKRT_ERR_OOM, "page-locked staging of the instance boxes");
+            uint32_t k = 0;
+            for (uint32_t i = 0; i < n; ++i) {
+                const GkrtInstance& in = ctx->inst[i];
+                if (!in.visible || ctx->blas_root[in.mesh_id] < 0) continue;
+                std::memcpy(hb[k].world, in.world, 48);
+                hb[k].mesh = in.mesh_id;
+                hb[k].inst = i;
+                hb[k].pad0 = hb[k].pad1 = 0;
+                ++k;
+            }
+            if ((rc = copy_staged(ctx, 5, ctx->d_refit_inst, sizeof(GpuInstBox) * (size_t)m, st)) != GKRT_OK) return rc;
+            InstLevelResult r;
+            GK_CUDA(gpu_bvh_build_instance_level(ctx->builder, ctx->d_refit_inst, m, ctx->d_blas_box, ctx->d_nodes, base,
+                                                 slots, ctx->d_wide, ctx->blas_wide_count, (uint32_t)ctx->d_wide_cap,
+                                                 &ctx->refit, &r, st));
+            if (r.error)
+                return fail(ctx, GKRT_ERR_INVALID_ARG,
+                            "instance BVH build failed (non-finite transforms or depth > 64), code " +
+                                std::to_string(r.error));
+            ctx->tlas_root = m ? (int)base : -1;
+            ctx->tlas_nodes = r.nodes_used;
+            ctx->tlas_bin_depth = r.depth;
+            ctx->tlas_wide_root = m ? (int)ctx->blas_wide_count : -1;
+            ctx->tlas_wide_count = r.wide_count;
+            ctx->tlas_wide_depth = r.wide_depth;
+            if ((rc = check_stack_bound(ctx)) != GKRT_OK) return rc;
+            ctx->tlas_ready = true;
+            return GKRT_OK;
+        }
         std::vector<GpuInstBox> ib;
         ib.reserve(n);
         for (uint32_t i = 0; i < n; ++i) {
@@ -589,9 +635,6 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
             b.pad0 = b.pad1 = 0;
             ib.push_back(b);
         }
-        if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
-        // the instance tables first: their host work and uploads overlap the stream's earlier work
-        if ((rc = upload_instances(ctx, st)) != GKRT_OK) return rc;
         GpuBvhResult r;
         GK_CUDA(gpu_bvh_build_instances(ctx->builder, ib.data(), (uint32_t)ib.size(), ctx->d_blas_box, base, &r, st));
         if ((rc = ensure_node_cap(ctx, (size_t)base + r.node_count)) != GKRT_OK) return rc;

@@ -145,6 +145,23 @@ cudaError_t gpu_bvh_build_meshes(GpuBvh* b, const float4* pos, const uint32_t* i
 // Instance-level tree; mesh_box: device, 6 floats per mesh.
 cudaError_t gpu_bvh_build_instances(GpuBvh* b, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
                                     uint32_t node_base, GpuBvhResult* out, cudaStream_t st);
+// The instance level in one cooperative launch and one host wait: a binned-SAH tree by the
+// rule of gpu_bvh_build_instances over the n records at `inst` (device), root node_base,
+// slots [node_base, node_base + node_count) of the
+// device array `nodes`, node_cap >= n + 1 slots zeroed first) collapsed into wide nodes
+// [wide_base, wide_base + wide_count) of `wide` (wide_cap nodes in all), links recorded when
+// non-null. res->error != 0: the build failed (non-finite transforms, more than 64 levels);
+// the nodes are then unusable.
+struct RefitLinks;
+struct InstLevelResult {
+    uint32_t node_count = 0, nodes_used = 0, wide_count = 0, error = 0;
+    int depth = 0, wide_depth = 0;
+};
+cudaError_t gpu_bvh_build_instance_level(GpuBvh* b, const GpuInstBox* inst, uint32_t n, const float* mesh_box,
+                                        BvhNode* nodes, uint32_t node_base, uint32_t node_cap, WideNode* wide,
+                                        uint32_t wide_base, uint32_t wide_cap, const RefitLinks* links,
+                                        InstLevelResult* res, cudaStream_t st);
+bool gpu_bvh_cooperative_supported();   // the current device takes cooperative launches
 // Collapse of two-child trees (device array bin, roots: node refs, -1 for none) into the
 // compressed 8-wide nodes the kernels traverse, at out[wide_base ...) of an array of out_cap
 // nodes. wroots: wide root per tree (-1 for none); count: wide nodes written; depth: levels.
