@@ -305,7 +305,7 @@ struct TraceOut {
     uint32_t inst, prim, tri;
 };
 
-enum { kClosest = 0, kAny = 1, kExact = 2 };
+enum { kClosest = 0, kAny = 1 };
 
 GK_D f3 tri_v(const float4* tris, uint32_t ti, int k, uint32_t* prim = nullptr) {
     float4 v = __ldg(&tris[3 * ti + k]);
@@ -325,7 +325,7 @@ struct Trav {
     uint32_t inst, prim, tri;   // current best
     uint32_t cur;               // instance being traversed
     int ref, sp, iter;
-    int mode;                   // kClosest / kAny / kExact
+    int mode;                   // kClosest / kAny
     uint32_t leaf;              // postponed triangle leaf (payload), valid when has_leaf
     bool hit, best_exact, inblas, done, ambiguous, has_leaf;
 };
@@ -382,19 +382,6 @@ GK_D bool trav_leaf(Trav& T, const SceneView& S, uint32_t first, uint32_t cnt, C
         ++cn.tris;
         const Fp32Hit f = fp32_test(T.o, sh, v0, v1, v2);
         if (f.kind == 0) continue;
-        if (T.mode == kExact) {
-            const ExactHit x = exact_test(T.o, T.d, sh, v0, v1, v2);
-            ++cn.fallbacks;
-            if (!x.hit || !(x.t >= tmind && x.t <= tmaxd)) continue;
-            const bool better = !T.hit || x.t < T.best_td ||
-                                (x.t == T.best_td && (T.cur < T.inst || (T.cur == T.inst && prim < T.prim)));
-            if (better) {
-                T.hit = true; T.inst = T.cur; T.prim = prim; T.tri = ti;
-                T.best_td = x.t;
-                T.tcull = (float)x.t * 1.000001f;
-            }
-            continue;
-        }
         float t, e;
         double td = 0.0;
         bool have_td = false;

@@ -7,7 +7,9 @@
 // zeros), N = cin and K = pixels. One CTA takes one tap and a run of pixels; both operands
 // are staged by the CTA's threads into the 64-byte-swizzled K-major layout (pixels along K)
 // straight from the NHWC tensors, made visible to the tensor core with a proxy fence, and
-// multiplied by one thread while the next pixels are staged (two buffers). The FP32
+// multiplied by one thread while the next pixels are staged (two buffers); a thread stages an
+// 8-pixel x 8-channel block with eight 16-byte loads and stores it transposed (byte permutes)
+// as eight 16-byte rows. The FP32
 // accumulator is added to dW with atomics. Every wait is bounded.
 #include "gk_umma.cuh"
 #include "gkrt_internal.h"
@@ -27,6 +29,26 @@ __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+__device__ __forceinline__ uint32_t word_of(const uint4& v, int i) {
+    return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// Stores the 8 x 8 block v (v[i]: 8 channels of pixel i) transposed: row r0 + c of the
+// 64-byte-swizzled K-major tile gets the 8 pixels' channel c as one 16-byte chunk at K
+// offset k0 (a multiple of 8).
+__device__ __forceinline__ void store_block_t(uint8_t* tile, int r0, int k0, const uint4* v) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        uint32_t w[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const uint32_t lo = word_of(v[2 * h], c >> 1), hi = word_of(v[2 * h + 1], c >> 1);
+            w[h] = (c & 1) ? __byte_perm(lo, hi, 0x7632) : __byte_perm(lo, hi, 0x5410);
+        }
+        *reinterpret_cast<uint4*>(tile + sw64_offset(r0 + c, k0)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
 __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -40,6 +62,7 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
     const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
     const long long npix = (long long)a.B * a.H * a.W;
     const long long p0 = (long long)blockIdx.x * a.chunk;
+    const long long pend = min(p0 + (long long)a.chunk, npix);   // pixels of this CTA: [p0, pend)
     const int nk = (int)((min((long long)a.chunk, npix - p0) + kWgStep - 1) / kWgStep);
     const uint32_t ncols = a.cin <= 32 ? 32u : a.cin <= 64 ? 64u : a.cin <= 128 ? 128u : 256u;
 
@@ -62,39 +85,73 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
     const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cin);
     bool ok = true;
     const int ga = a.cout / 8, gb = a.cin / 8;
+    // A[cout][pixel] = dP[pixel][cout] and B[cin][pixel] = X[pixel shifted by the tap][cin]
+    // (zero outside the image): per K step, one thread per block of 8 pixels x 8 channels
+    // (eight 16-byte loads, consecutive threads on consecutive channel groups), stored
+    // transposed as eight 16-byte rows. A thread has at most two blocks per step
+    // (4 (cout / 8 + cin / 8) <= 192); it loads its next step's blocks into registers before
+    // the barrier of the current one, so the loads are in flight during the barrier and the MMA.
+    const int na = (kWgStep / 8) * ga, nb = (kWgStep / 8) * gb;
+    uint4 v[2][8];
+    auto load_step = [&](int k) {
+        const long long qk = p0 + (long long)k * kWgStep;
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            const int it = tid + m * kWgThreads;
+            if (it >= na + nb) continue;
+            const bool is_a = it < na;
+            const int j = is_a ? it : it - na, gn = is_a ? ga : gb;
+            const int g = j % gn, jb = j / gn;
+            const long long q0 = qk + 8 * jb;
+            if (is_a) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    v[m][i] = q0 + i < pend
+                                  ? *reinterpret_cast<const uint4*>(a.dp + (q0 + i) * a.dp_c + a.dp_off + 8 * g)
+                                  : make_uint4(0u, 0u, 0u, 0u);
+            } else {
+                // coordinates of the block's first pixel, then stepped along the row
+                int x = 0, y = 0;
+                long long b = 0;
+                if (q0 < pend) {
+                    const long long row = q0 / a.W;
+                    x = (int)(q0 - row * a.W);
+                    y = (int)(row % a.H);
+                    b = row / a.H;
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    v[m][i] = make_uint4(0u, 0u, 0u, 0u);
+                    if (q0 + i < pend) {
+                        const int xs = x + dx, ys = y + dy;
+                        if (xs >= 0 && xs < a.W && ys >= 0 && ys < a.H)
+                            v[m][i] = *reinterpret_cast<const uint4*>(a.x + ((b * a.H + ys) * a.W + xs) * a.x_c +
+                                                                      a.x_off + 8 * g);
+                    }
+                    if (++x == a.W) {
+                        x = 0;
+                        if (++y == a.H) { y = 0; ++b; }
+                    }
+                }
+            }
+        }
+    };
+    if (nk > 0) load_step(0);
     for (int k = 0; k < nk && ok; ++k) {
         const int s = k & 1;
         if (k >= 2 && !mbar_wait_bounded(&done[s], (uint32_t)((k >> 1) - 1) & 1u, a.err)) ok = false;
         if (__syncthreads_or(!ok)) { ok = false; break; }
         uint8_t* sa = smem + s * stage_bytes;
         uint8_t* sb = sa + a_bytes;
-        // A[cout][pixel] = dP[pixel][cout]
-        for (int it = tid; it < kWgStep * ga; it += kWgThreads) {
-            const int pl = it / ga, g = it % ga;
-            const long long q = p0 + (long long)k * kWgStep + pl;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (q < p0 + a.chunk && q < npix)
-                v = *reinterpret_cast<const uint4*>(a.dp + q * a.dp_c + a.dp_off + 8 * g);
-            const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) *reinterpret_cast<uint16_t*>(sa + sw64_offset(8 * g + i, pl)) = e[i];
+        for (int m = 0; m < 2; ++m) {
+            const int it = tid + m * kWgThreads;
+            if (it >= na + nb) continue;
+            const bool is_a = it < na;
+            const int j = is_a ? it : it - na, gn = is_a ? ga : gb;
+            store_block_t(is_a ? sa : sb, 8 * (j % gn), 8 * (j / gn), v[m]);
         }
-        // B[cin][pixel] = X[pixel shifted by the tap][cin], zero outside the image
-        for (int it = tid; it < kWgStep * gb; it += kWgThreads) {
-            const int pl = it / gb, g = it % gb;
-            const long long q = p0 + (long long)k * kWgStep + pl;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (q < p0 + a.chunk && q < npix) {
-                const int x = (int)(q % a.W), y = (int)((q / a.W) % a.H);
-                const long long b = q / ((long long)a.W * a.H);
-                const int xs = x + dx, ys = y + dy;
-                if (xs >= 0 && xs < a.W && ys >= 0 && ys < a.H)
-                    v = *reinterpret_cast<const uint4*>(a.x + ((b * a.H + ys) * a.W + xs) * a.x_c + a.x_off + 8 * g);
-            }
-            const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
-#pragma unroll
-            for (int i = 0; i < 8; ++i) *reinterpret_cast<uint16_t*>(sb + sw64_offset(8 * g + i, pl)) = e[i];
-        }
+        if (k + 1 < nk) load_step(k + 1);
         fence_proxy_async();
         __syncthreads();
         if (tid == 0) {
