@@ -1712,7 +1712,7 @@ int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t w
     if (!x || !w || !y || batch == 0 || height == 0 || width == 0 || batch > 65535 || height > 65535 ||
         width > 65535 || cin > 4096 || flags > 3u)
         return GKRT_ERR_INVALID_ARG;
-    ConvArgs a;
+    ConvArgs a{};
     a.B = (int)batch; a.H = (int)height; a.W = (int)width; a.cin = (int)cin; a.cout = (int)cout;
     a.x_c = (int)cin; a.x_off = 0;
     a.bias = bias;

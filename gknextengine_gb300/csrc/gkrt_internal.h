@@ -89,6 +89,14 @@ struct ConvArgs {
     int n_store;                   // fp32 output: channels stored (<= cout)
     int flags;                     // kConvRelu | kConvF32Out
     uint32_t* err;                 // device error word
+    // optional outputs of the bf16 epilogue (null: none), channel strides and offsets multiples
+    // of 8: the 2 x 2 average of the stored values at half resolution (H / 2 x W / 2, blocks
+    // wholly inside the image; the denoiser's 2 x 2 average pooling), and every stored value at
+    // the four pixels of double resolution (2H x 2W; its nearest upsampling)
+    void* pool_out;
+    int pool_c, pool_off;
+    void* up_out;
+    int up_c, up_off;
 };
 
 // Host-side BVH build (binned SAH over boxes). Returns nodes in device layout and the leaf
@@ -242,12 +250,8 @@ struct WgradArgs {
 };
 }
 cudaError_t gkrt_launch_conv_wgrad(const gk::WgradArgs& a, cudaStream_t st);
-cudaError_t gkrt_launch_avgpool2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
-                                 int h, int w, int C, cudaStream_t st);
 cudaError_t gkrt_launch_avgpool2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
                                      int B, int H, int W, int C, int accumulate, cudaStream_t st);
-cudaError_t gkrt_launch_upsample2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
-                                  int H, int W, int C, cudaStream_t st);
 cudaError_t gkrt_launch_upsample2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
                                       int B, int h, int w, int C, cudaStream_t st);
 cudaError_t gkrt_launch_relu_bwd(void* dy, int dy_c, int dy_off, const void* y, int y_c, int y_off, long long npix,

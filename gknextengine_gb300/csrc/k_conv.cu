@@ -50,6 +50,50 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
+__device__ __forceinline__ void store_bf16x16(__nv_bfloat16* dst, const float* v) {
+    uint4* o = reinterpret_cast<uint4*>(dst);
+    o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                      pack_bf16x2(v[6], v[7]));
+    o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
+                      pack_bf16x2(v[14], v[15]));
+}
+
+// The bf16 epilogue of 16 channels (c0 .. c0 + 15) of pixel (x, y) of image img: the plain
+// store, and the optional pooled and upsampled outputs. Called by every lane of the warp
+// (the pool's 2 x 2 block is four lanes of one warp: x-neighbour lane ^ 1, y-neighbour lane ^
+// yl); the pooled average is ((v(x, y) + v(x + 1, y)) + v(x, y + 1)) + v(x + 1, y + 1) of the
+// stored (bf16-rounded) values, times 1/4, rounded to bf16.
+__device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float* v, int img, int x, int y, bool inside,
+                                              int c0, int yl) {
+    const size_t pix = ((size_t)img * a.H + y) * a.W + x;
+    if (inside) store_bf16x16(reinterpret_cast<__nv_bfloat16*>(a.out) + pix * a.out_c + a.out_off + c0, v);
+    if (a.up_out && inside) {
+        __nv_bfloat16* up = reinterpret_cast<__nv_bfloat16*>(a.up_out);
+        const size_t W2 = 2 * (size_t)a.W;
+        const size_t q = ((size_t)img * 2 * a.H + 2 * (size_t)y) * W2 + 2 * (size_t)x;
+        for (int k = 0; k < 4; ++k)
+            store_bf16x16(up + (q + (k >> 1) * W2 + (k & 1)) * a.up_c + a.up_off + c0, v);
+    }
+    if (a.pool_out) {
+        const int lane = threadIdx.x & 31;
+        float s[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float own = __bfloat162float(__float2bfloat16_rn(v[j]));
+            const float nx = __shfl_xor_sync(0xFFFFFFFFu, own, 1);
+            const float ny = __shfl_xor_sync(0xFFFFFFFFu, own, yl);
+            const float nxy = __shfl_xor_sync(0xFFFFFFFFu, own, yl ^ 1);
+            s[j] = (((0.0f + own) + nx) + ny) + nxy;
+            s[j] *= 0.25f;
+        }
+        const int h2 = a.H / 2, w2 = a.W / 2;
+        if (!(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2 && (lane & 1) == 0 && (lane & yl) == 0) {
+            const size_t pp = ((size_t)img * h2 + y / 2) * w2 + x / 2;
+            store_bf16x16(reinterpret_cast<__nv_bfloat16*>(a.pool_out) + pp * a.pool_c + a.pool_off + c0, s);
+        }
+    }
+}
+
 __device__ __forceinline__ void tile_origin(int t, int tiles_x, int tiles_y, int& x0, int& y0, int& img) {
     const int per_img = tiles_x * tiles_y;
     img = t / per_img;
@@ -187,7 +231,6 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                 uint32_t r[16];
                 tmem_ld16(base + (uint32_t)c0, r);
                 tmem_ld_wait();
-                if (!inside) continue;
                 float v[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
@@ -195,15 +238,11 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                     if (a.flags & kConvRelu) v[j] = fmaxf(v[j], 0.0f);
                 }
                 if (a.flags & kConvF32Out) {
+                    if (!inside) continue;
                     float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
                     for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
                 } else {
-                    uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + pix * a.out_c +
-                                                        a.out_off + c0);
-                    o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
-                                      pack_bf16x2(v[6], v[7]));
-                    o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
-                                      pack_bf16x2(v[14], v[15]));
+                    epilogue_bf16(a, v, img, x, y, inside, c0, 16);   // y-neighbour: lane ^ 16 (16-pixel rows)
                 }
             }
             tc_fence_before();
@@ -370,7 +409,6 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                 uint32_t rr[16];
                 tmem_ld16(base + (uint32_t)c0, rr);
                 tmem_ld_wait();
-                if (!inside) continue;
                 float v[16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
@@ -378,15 +416,11 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                     if (a.flags & kConvRelu) v[j] = fmaxf(v[j], 0.0f);
                 }
                 if (a.flags & kConvF32Out) {
+                    if (!inside) continue;
                     float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
                     for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
                 } else {
-                    uint4* o = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + pix * a.out_c +
-                                                        a.out_off + c0);
-                    o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
-                                      pack_bf16x2(v[6], v[7]));
-                    o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
-                                      pack_bf16x2(v[14], v[15]));
+                    epilogue_bf16(a, v, img, x, y, inside, c0, 8);   // y-neighbour: lane ^ 8 (8-pixel rows)
                 }
             }
             tc_fence_before();
@@ -446,6 +480,13 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         args.out_off + (f32 ? args.n_store : args.cout) > args.out_c || (f32 && args.n_store > args.cout) ||
         ((uintptr_t)x & 15u) || ((uintptr_t)w & 15u) || ((uintptr_t)args.out & 15u) || args.x_off % 8 ||
         (args.x_c > 0 && (args.x_c % 8 || args.x_off + args.cin > args.x_c)))
+        return cudaErrorInvalidValue;
+    if ((args.pool_out || args.up_out) && f32) return cudaErrorInvalidValue;
+    if (args.pool_out && (args.pool_c % 8 || args.pool_off % 8 || args.pool_off + args.cout > args.pool_c ||
+                          ((uintptr_t)args.pool_out & 15u)))
+        return cudaErrorInvalidValue;
+    if (args.up_out && (args.up_c % 8 || args.up_off % 8 || args.up_off + args.cout > args.up_c ||
+                        ((uintptr_t)args.up_out & 15u)))
         return cudaErrorInvalidValue;
     CUtensorMap mx, mw;
     const uint64_t xc = (uint64_t)(args.x_c > 0 ? args.x_c : args.cin);

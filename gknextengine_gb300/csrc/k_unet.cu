@@ -206,26 +206,6 @@ __device__ __forceinline__ void st8(__nv_bfloat16* p, const float* v) {
     *reinterpret_cast<uint4*>(p) = u;
 }
 
-__global__ void k_avgpool2(const __nv_bfloat16* in, int in_c, int in_off, __nv_bfloat16* out, int out_c, int out_off,
-                           int B, int h, int w, int C) {   // h, w: output size
-    const int g8 = C / 8;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= B * h * w * g8) return;
-    const int g = i % g8, p = i / g8;
-    const int x = p % w, y = (p / w) % h, b = p / (w * h);
-    const int W = 2 * w, H = 2 * h;
-    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0}, v[8];
-    for (int k = 0; k < 4; ++k) {
-        const size_t q = ((size_t)(b * H + 2 * y + (k >> 1)) * W + 2 * x + (k & 1));
-        ld8(in + q * in_c + in_off + 8 * g, v);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) s[j] += v[j];
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) s[j] *= 0.25f;
-    st8(out + (size_t)p * out_c + out_off + 8 * g, s);
-}
-
 // d_in (+)= d_out / 4 for each of the 2x2 inputs (accumulate: add to what is there)
 __global__ void k_avgpool2_bwd(const __nv_bfloat16* dout, int dout_c, int dout_off, __nv_bfloat16* din, int din_c,
                                int din_off, int B, int H, int W, int C, int accumulate) {   // H, W: input size
@@ -242,18 +222,6 @@ __global__ void k_avgpool2_bwd(const __nv_bfloat16* dout, int dout_c, int dout_o
 #pragma unroll
     for (int j = 0; j < 8; ++j) v[j] = 0.25f * v[j] + (accumulate ? d[j] : 0.0f);
     st8(dst, v);
-}
-
-__global__ void k_upsample2(const __nv_bfloat16* in, int in_c, int in_off, __nv_bfloat16* out, int out_c,
-                            int out_off, int B, int H, int W, int C) {   // H, W: output size
-    const int g8 = C / 8;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= B * H * W * g8) return;
-    const int g = i % g8, p = i / g8;
-    const int x = p % W, y = (p / W) % H, b = p / (W * H);
-    const size_t q = (size_t)(b * (H / 2) + y / 2) * (W / 2) + x / 2;
-    *reinterpret_cast<uint4*>(out + (size_t)p * out_c + out_off + 8 * g) =
-        *reinterpret_cast<const uint4*>(in + q * in_c + in_off + 8 * g);
 }
 
 // d_in = sum of the 2x2 output gradients it was copied to
@@ -355,23 +323,11 @@ cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
 
 static inline unsigned nblk(long long n) { return (unsigned)((n + 255) / 256); }
 
-cudaError_t gkrt_launch_avgpool2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
-                                 int h, int w, int C, cudaStream_t st) {
-    k_avgpool2<<<nblk((long long)B * h * w * (C / 8)), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
-                                                               (__nv_bfloat16*)out, out_c, out_off, B, h, w, C);
-    return cudaGetLastError();
-}
 cudaError_t gkrt_launch_avgpool2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,
                                      int B, int H, int W, int C, int accumulate, cudaStream_t st) {
     k_avgpool2_bwd<<<nblk((long long)B * H * W * (C / 8)), 256, 0, st>>>((const __nv_bfloat16*)dout, dout_c, dout_off,
                                                                    (__nv_bfloat16*)din, din_c, din_off, B, H, W, C,
                                                                    accumulate);
-    return cudaGetLastError();
-}
-cudaError_t gkrt_launch_upsample2(const void* in, int in_c, int in_off, void* out, int out_c, int out_off, int B,
-                                  int H, int W, int C, cudaStream_t st) {
-    k_upsample2<<<nblk((long long)B * H * W * (C / 8)), 256, 0, st>>>((const __nv_bfloat16*)in, in_c, in_off,
-                                                                (__nv_bfloat16*)out, out_c, out_off, B, H, W, C);
     return cudaGetLastError();
 }
 cudaError_t gkrt_launch_upsample2_bwd(const void* dout, int dout_c, int dout_off, void* din, int din_c, int din_off,

@@ -248,9 +248,13 @@ struct Unet {
         return cudaSuccess;
     }
 
+    // pool / up (optional): the epilogue also writes the 2 x 2 average of the output at half
+    // resolution, or the output at double resolution (nearest), at channel offset *_off of a
+    // tensor of *_c channels
     cudaError_t conv(int l, const __nv_bfloat16* in, int in_c, int in_off, void* out, int out_c, int out_off, int level,
-                     cudaStream_t st) {
-        ConvArgs a;
+                     cudaStream_t st, __nv_bfloat16* pool = nullptr, int pool_c = 0, int pool_off = 0,
+                     __nv_bfloat16* up = nullptr, int up_c = 0, int up_off = 0) {
+        ConvArgs a{};
         a.B = B; a.H = H >> level; a.W = W >> level;
         a.cin = kLayers[l].cin; a.cout = kLayers[l].cout;
         a.x_c = in_c; a.x_off = in_off;
@@ -259,6 +263,8 @@ struct Unet {
         a.n_store = kLayers[l].n_store;
         a.flags = (kLayers[l].relu ? kConvRelu : 0) | (l == OUT ? kConvF32Out : 0);
         a.err = err;
+        a.pool_out = pool; a.pool_c = pool_c; a.pool_off = pool_off;
+        a.up_out = up; a.up_c = up_c; a.up_off = up_off;
         return gkrt_launch_conv3x3(in, wb + wb_off[l], a, st);
     }
 
@@ -266,23 +272,19 @@ struct Unet {
         cudaError_t e;
 #define GK_T(x) if ((e = (x)) != cudaSuccess) return e
         GK_T(conv(E0A, x0, 32, 0, e0a, 32, 0, 0, st));
-        GK_T(conv(E0B, e0a, 32, 0, cat0, 96, 64, 0, st));
-        GK_T(gkrt_launch_avgpool2(cat0, 96, 64, p0, 32, 0, B, H >> 1, W >> 1, 32, st));
+        // the 2 x 2 pools and nearest upsamplings ride in the epilogues of the convolutions that
+        // produce their inputs: 2 x 2 means of the stored values, nearest copies
+        GK_T(conv(E0B, e0a, 32, 0, cat0, 96, 64, 0, st, p0, 32, 0));
         GK_T(conv(E1A, p0, 32, 0, e1a, 64, 0, 1, st));
-        GK_T(conv(E1B, e1a, 64, 0, cat1, 160, 96, 1, st));
-        GK_T(gkrt_launch_avgpool2(cat1, 160, 96, p1, 64, 0, B, H >> 2, W >> 2, 64, st));
+        GK_T(conv(E1B, e1a, 64, 0, cat1, 160, 96, 1, st, p1, 64, 0));
         GK_T(conv(E2A, p1, 64, 0, e2a, 96, 0, 2, st));
-        GK_T(conv(E2B, e2a, 96, 0, cat2, 224, 128, 2, st));
-        GK_T(gkrt_launch_avgpool2(cat2, 224, 128, p2, 96, 0, B, H >> 3, W >> 3, 96, st));
+        GK_T(conv(E2B, e2a, 96, 0, cat2, 224, 128, 2, st, p2, 96, 0));
         GK_T(conv(E3A, p2, 96, 0, e3a, 128, 0, 3, st));
-        GK_T(conv(E3B, e3a, 128, 0, e3b, 128, 0, 3, st));
-        GK_T(gkrt_launch_upsample2(e3b, 128, 0, cat2, 224, 0, B, H >> 2, W >> 2, 128, st));
+        GK_T(conv(E3B, e3a, 128, 0, e3b, 128, 0, 3, st, nullptr, 0, 0, cat2, 224, 0));
         GK_T(conv(D2A, cat2, 224, 0, d2a, 96, 0, 2, st));
-        GK_T(conv(D2B, d2a, 96, 0, d2b, 96, 0, 2, st));
-        GK_T(gkrt_launch_upsample2(d2b, 96, 0, cat1, 160, 0, B, H >> 1, W >> 1, 96, st));
+        GK_T(conv(D2B, d2a, 96, 0, d2b, 96, 0, 2, st, nullptr, 0, 0, cat1, 160, 0));
         GK_T(conv(D1A, cat1, 160, 0, d1a, 64, 0, 1, st));
-        GK_T(conv(D1B, d1a, 64, 0, d1b, 64, 0, 1, st));
-        GK_T(gkrt_launch_upsample2(d1b, 64, 0, cat0, 96, 0, B, H, W, 64, st));
+        GK_T(conv(D1B, d1a, 64, 0, d1b, 64, 0, 1, st, nullptr, 0, 0, cat0, 96, 0));
         GK_T(conv(D0A, cat0, 96, 0, d0a, 32, 0, 0, st));
         GK_T(conv(D0B, d0a, 32, 0, d0b, 32, 0, 0, st));
         GK_T(conv(OUT, d0b, 32, 0, y, 4, 0, 0, st));
@@ -309,7 +311,7 @@ struct Unet {
         GK_T(gkrt_launch_conv_wgrad(wa, st));
         GK_T(gkrt_launch_bias_grad(dy, dy_c, dy_off, npix, L.cout, g + boff[l], st));
         if (din) {
-            ConvArgs a;
+            ConvArgs a{};
             a.B = B; a.H = h; a.W = w;
             a.cin = L.cout; a.cout = L.cin;
             a.x_c = dy_c; a.x_off = dy_off;
