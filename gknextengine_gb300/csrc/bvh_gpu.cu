@@ -1604,6 +1604,7 @@ struct GpuBvh {
     DBuf<WEnt> wcache;
     DBuf<int> wcache_n;
     uint32_t* result_host = nullptr;   // page-locked copy of the instance level's result record
+    uint32_t inst_level_n = 0;         // instances of the instance-level build in flight
     uint32_t launches = 0;   // kernels launched by all builds so far
 
     ~GpuBvh() {
@@ -1880,11 +1881,11 @@ cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint
     return cudaStreamSynchronize(st);
 }
 
-cudaError_t gpu_bvh_build_instance_level(GpuBvh* B, const GpuInstBox* inst, uint32_t n, const float* mesh_box,
-                                        BvhNode* nodes, uint32_t node_base, uint32_t node_cap, WideNode* wide,
-                                        uint32_t wide_base, uint32_t wide_cap, const RefitLinks* links,
-                                        InstLevelResult* res, cudaStream_t st) {
-    *res = InstLevelResult();
+cudaError_t gpu_bvh_build_instance_level_launch(GpuBvh* B, const GpuInstBox* inst, uint32_t n, const float* mesh_box,
+                                               BvhNode* nodes, uint32_t node_base, uint32_t node_cap, WideNode* wide,
+                                               uint32_t wide_base, uint32_t wide_cap, const RefitLinks* links,
+                                               cudaStream_t st) {
+    B->inst_level_n = n;
     if (n == 0) return cudaSuccess;
     if ((uint64_t)node_cap < (uint64_t)n + 1u) return cudaErrorInvalidValue;
     const uint32_t cap_t = n / (kSmall + 1u) + 2u, cap_w = cap_t + n / kChunk + 2u, cap_s = n + 1u;
@@ -1952,7 +1953,12 @@ cudaError_t gpu_bvh_build_instance_level(GpuBvh* B, const GpuInstBox* inst, uint
     void* params[] = {&a};
     GK_TRY(cudaLaunchCooperativeKernel((const void*)k_inst_level, dim3(grid), dim3(kBt), params, 0, st));
     ++B->launches;
-    GK_TRY(cudaMemcpyAsync(B->result_host, B->result.p, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    return cudaMemcpyAsync(B->result_host, B->result.p, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+}
+
+cudaError_t gpu_bvh_build_instance_level_finish(GpuBvh* B, InstLevelResult* res, cudaStream_t st) {
+    *res = InstLevelResult();
+    if (B->inst_level_n == 0) return cudaSuccess;
     GK_TRY(cudaStreamSynchronize(st));
     const uint32_t* r = B->result_host;
     res->node_count = r[0];

@@ -572,15 +572,18 @@ int build_blas(GkrtContext* ctx, cudaStream_t st) {
     return ctx->host_build ? build_blas_host(ctx, st) : build_blas_gpu(ctx, st);
 }
 
-int build_tlas(GkrtContext* ctx, cudaStream_t st) {
+// during (optional): host work run while the GPU builds the level (else before the build).
+int build_tlas(GkrtContext* ctx, cudaStream_t st, int (*during)(GkrtContext*, cudaStream_t) = nullptr) {
     const uint32_t n = (uint32_t)ctx->inst.size();
     const uint32_t base = ctx->blas_node_count;
     int rc;
+    const bool coop = !ctx->host_build && gpu_bvh_cooperative_supported();
+    if (during && !coop && (rc = during(ctx, st)) != GKRT_OK) return rc;
     if (!ctx->host_build) {
         if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
         // the instance tables first: their host work and uploads overlap the stream's earlier work
         if ((rc = upload_instances(ctx, st)) != GKRT_OK) return rc;
-        if (gpu_bvh_cooperative_supported()) {
+        if (coop) {
             // the tree's members, staged in page-locked memory and uploaded into the refit's
             // instance buffer (a refit rewrites it whole); one cooperative launch builds and
             // collapses the level; the host waits once
@@ -605,10 +608,13 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
                 ++k;
             }
             if ((rc = copy_staged(ctx, 5, ctx->d_refit_inst, sizeof(GpuInstBox) * (size_t)m, st)) != GKRT_OK) return rc;
+            GK_CUDA(gpu_bvh_build_instance_level_launch(ctx->builder, ctx->d_refit_inst, m, ctx->d_blas_box, ctx->d_nodes,
+                                                        base, slots, ctx->d_wide, ctx->blas_wide_count,
+                                                        (uint32_t)ctx->d_wide_cap, &ctx->refit, st));
+            // host work of the caller's (the emitter table) while the build runs
+            const int rc_during = during ? during(ctx, st) : GKRT_OK;
             InstLevelResult r;
-            GK_CUDA(gpu_bvh_build_instance_level(ctx->builder, ctx->d_refit_inst, m, ctx->d_blas_box, ctx->d_nodes, base,
-                                                 slots, ctx->d_wide, ctx->blas_wide_count, (uint32_t)ctx->d_wide_cap,
-                                                 &ctx->refit, &r, st));
+            GK_CUDA(gpu_bvh_build_instance_level_finish(ctx->builder, &r, st));
             if (r.error)
                 return fail(ctx, GKRT_ERR_INVALID_ARG,
                             "instance BVH build failed (non-finite transforms or depth > 64), code " +
@@ -621,7 +627,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st) {
             ctx->tlas_wide_depth = r.wide_depth;
             if ((rc = check_stack_bound(ctx)) != GKRT_OK) return rc;
             ctx->tlas_ready = true;
-            return GKRT_OK;
+            return rc_during;
         }
         std::vector<GpuInstBox> ib;
         ib.reserve(n);
@@ -1123,11 +1129,14 @@ int gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances,
     DeviceGuard device_guard(ctx->device);
     const PassScope scope(ctx, kPassTlas, (cudaStream_t)stream);
     ctx->inst.assign(instances, instances + count);
-    // host work first (emitter table, then the instance tables inside build_tlas), uploaded
-    // asynchronously, so that it overlaps the stream's earlier frames; the GPU build follows
-    if ((rc = build_emitters(ctx, (cudaStream_t)stream)) != GKRT_OK) return rc;
-    if (!ctx->blas_ready) return ensure_bvh(ctx, 0, (cudaStream_t)stream);
-    return build_tlas(ctx, (cudaStream_t)stream);
+    // host work first (the instance tables inside build_tlas), uploaded asynchronously, so that
+    // it overlaps the stream's earlier frames; the emitter table is built on the host while the
+    // GPU builds the instance level
+    if (!ctx->blas_ready) {
+        if ((rc = build_emitters(ctx, (cudaStream_t)stream)) != GKRT_OK) return rc;
+        return ensure_bvh(ctx, 0, (cudaStream_t)stream);
+    }
+    return build_tlas(ctx, (cudaStream_t)stream, build_emitters);
 }
 
 int gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count, void* stream) {

@@ -165,10 +165,13 @@ struct InstLevelResult {
     uint32_t node_count = 0, nodes_used = 0, wide_count = 0, error = 0;
     int depth = 0, wide_depth = 0;
 };
-cudaError_t gpu_bvh_build_instance_level(GpuBvh* b, const GpuInstBox* inst, uint32_t n, const float* mesh_box,
-                                        BvhNode* nodes, uint32_t node_base, uint32_t node_cap, WideNode* wide,
-                                        uint32_t wide_base, uint32_t wide_cap, const RefitLinks* links,
-                                        InstLevelResult* res, cudaStream_t st);
+// _launch enqueues the build on st; _finish waits for it (the one host wait) and returns its
+// result. Host work in between overlaps the build.
+cudaError_t gpu_bvh_build_instance_level_launch(GpuBvh* b, const GpuInstBox* inst, uint32_t n, const float* mesh_box,
+                                               BvhNode* nodes, uint32_t node_base, uint32_t node_cap, WideNode* wide,
+                                               uint32_t wide_base, uint32_t wide_cap, const RefitLinks* links,
+                                               cudaStream_t st);
+cudaError_t gpu_bvh_build_instance_level_finish(GpuBvh* b, InstLevelResult* res, cudaStream_t st);
 bool gpu_bvh_cooperative_supported();   // the current device takes cooperative launches
 // Collapse of two-child trees (device array bin, roots: node refs, -1 for none) into the
 // compressed 8-wide nodes the kernels traverse, at out[wide_base ...) of an array of out_cap
