@@ -617,6 +617,31 @@ def run_gkrt(args):
         ms_a = ra0.elapsed_time(ra1)
         all_levels = {"mrays_s": (s1a.rays_total - s0a.rays_total) / (ms_a * 1e-3) / 1e6, "ms_per_frame": ms_a / K,
                       "update_span_ms": sum(a.elapsed_time(b) for a, b in fa) / K}
+        # the refit-or-rebuild policy over the same frames (growth limit 1.25)
+        fp = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(K)]
+        rp0, rp1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r.update_instances(insts[Wm], stream)
+        r.synchronize(stream)
+        s0p = r.stats()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            rp0.record(stream)
+            for k in range(K):
+                fc = fcs[Wm + k]
+                fp[k][0].record(stream)
+                r.update_instances_auto(insts[Wm + k], 1.25, stream)
+                fp[k][1].record(stream)
+                r.trace_pass(fc, stream)
+                r.reproject_pass(fc, stream)
+                r.denoise_pass(fc, stream)
+                r.end_frame(stream)
+            rp1.record(stream)
+            torch.cuda.synchronize()
+        s1p = r.stats()
+        ms_p = rp0.elapsed_time(rp1)
+        auto = {"mrays_s": (s1p.rays_total - s0p.rays_total) / (ms_p * 1e-3) / 1e6, "ms_per_frame": ms_p / K,
+                "update_span_ms": float(np.median([a.elapsed_time(b) for a, b in fp])),
+                "refits": s1p.tlas_refits - s0p.tlas_refits, "rebuilds": s1p.tlas_rebuilds - s0p.tlas_rebuilds}
         refit = {"mrays_s": (s1r.rays_total - s0r.rays_total) / (ms_r * 1e-3) / 1e6,
                  "ms_per_frame": ms_r / K,
                  "trace_ms": sum(a.elapsed_time(b) for _, a, b in fe) / K,
@@ -626,7 +651,7 @@ def run_gkrt(args):
                  "refits": s1r.tlas_refits - s0r.tlas_refits,
                  "node_visits_last_frame": s1r.node_visits,
                  "node_visits_last_frame_rebuilt": st_last.node_visits,
-                 "all_levels_rebuilt_each_frame": all_levels}
+                 "all_levels_rebuilt_each_frame": all_levels, "auto_policy": auto}
 
     # ---- probe grid (after the timed frames: a baked grid changes path termination) ----
     probe_ms = None

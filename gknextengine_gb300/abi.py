@@ -174,7 +174,7 @@ class GkrtStats(C.Structure):
                 ("device_error", C.c_uint32), ("bvh_nodes", C.c_uint32), ("bvh_leaf_tris", C.c_uint32),
                 ("tlas_nodes", C.c_uint32), ("emitters", C.c_uint32), ("build_launches", C.c_uint32),
                 ("wide_nodes", C.c_uint32), ("wide_depth", C.c_uint32), ("tlas_refits", C.c_uint32),
-                ("hit_fetches", C.c_uint32)]
+                ("hit_fetches", C.c_uint32), ("tlas_rebuilds", C.c_uint32), ("pad", C.c_uint32)]
 
 
 def fptr(a: np.ndarray, ctype=C.c_float):

@@ -117,6 +117,15 @@ struct GkrtContext {
     size_t refit_ncap = 0, refit_wcap = 0, refit_icap = 0;
     std::vector<uint8_t> tlas_members;
     uint32_t tlas_refits = 0;
+    uint32_t tlas_rebuilds = 0;
+    // the refit-or-rebuild policy (gkrt_scene_update_instances_auto): each trace pass copies its
+    // counters into one of two page-locked records (by pass parity) with an event after it
+    unsigned long long* h_trace_counters = nullptr;   // 2 x 7, the Counters slots of d_counters
+    cudaEvent_t trace_ev[2] = {};
+    uint64_t trace_seq = 0;        // trace passes recorded
+    uint64_t trace_seq_read = 0;   // passes the policy has read (their sequence numbers + 1)
+    uint64_t base_after = 0;       // the baseline comes from a pass with this sequence number or later
+    double visits_base = -1.0, visits_last = -1.0;   // node visits per ray; -1: none yet
 
     // the texture pool: one RGBA-float buffer per uploaded id and the device table the kernels
     // read (GKRT_MAX_TEXTURES entries, null texels for an id without a texture)
@@ -627,6 +636,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st, int (*during)(GkrtContext*, cu
             ctx->tlas_wide_depth = r.wide_depth;
             if ((rc = check_stack_bound(ctx)) != GKRT_OK) return rc;
             ctx->tlas_ready = true;
+            ++ctx->tlas_rebuilds;
             return rc_during;
         }
         std::vector<GpuInstBox> ib;
@@ -653,6 +663,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st, int (*during)(GkrtContext*, cu
         ctx->tlas_bin_depth = r.depth;
         if ((rc = finish_tlas(ctx, r.node_count, st)) != GKRT_OK) return rc;
         ctx->tlas_ready = true;
+        ++ctx->tlas_rebuilds;
         return GKRT_OK;
     }
     std::vector<float> boxes;
@@ -703,6 +714,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st, int (*during)(GkrtContext*, cu
     ctx->tlas_bin_depth = hb.depth;
     if ((rc = finish_tlas(ctx, (uint32_t)hb.nodes.size(), st)) != GKRT_OK) return rc;
     ctx->tlas_ready = true;
+    ++ctx->tlas_rebuilds;
     return upload_instances(ctx, st);
 }
 
@@ -1015,6 +1027,9 @@ int gkrt_context_destroy(GkrtContext* ctx) {
     for (auto& pe : ctx->pass_ev)
         for (cudaEvent_t& ev : pe)
             if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t& ev : ctx->trace_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->h_trace_counters) cudaFreeHost(ctx->h_trace_counters);
     delete ctx;
     return GKRT_OK;
 }
@@ -1157,6 +1172,68 @@ int gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances, 
     return refit_tlas(ctx, (cudaStream_t)stream);
 }
 
+// The newest trace pass whose counters have reached the host (without waiting): node visits
+// per ray into visits_last, and into visits_base when none is set and the pass came after the
+// last rebuild.
+static void poll_trace_counters(GkrtContext* ctx) {
+    if (!ctx->h_trace_counters) return;
+    for (uint64_t back = 1; back <= 2 && back <= ctx->trace_seq; ++back) {
+        const uint64_t seq = ctx->trace_seq - back;
+        if (seq < ctx->trace_seq_read) break;
+        if (cudaEventQuery(ctx->trace_ev[seq & 1]) != cudaSuccess) continue;
+        const unsigned long long* c = ctx->h_trace_counters + 7 * (seq & 1);
+        if (c[0] > 0) {
+            ctx->visits_last = (double)c[3] / (double)c[0];
+            if (ctx->visits_base < 0.0 && seq >= ctx->base_after) ctx->visits_base = ctx->visits_last;
+        }
+        ctx->trace_seq_read = seq + 1;
+        break;
+    }
+    cudaGetLastError();   // a not-ready query leaves no error behind
+}
+
+int gkrt_scene_update_instances_auto(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count,
+                                     float growth_limit, void* stream) {
+    if (!ctx) return GKRT_ERR_INVALID_ARG;
+    if (!(growth_limit >= 1.0f) || !std::isfinite(growth_limit))
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "growth_limit must be a finite number >= 1");
+    if (!ctx->has_scene) return fail(ctx, GKRT_ERR_STATE, "no scene uploaded");
+    if (!instances || count != ctx->inst.size())
+        return fail(ctx, GKRT_ERR_INVALID_ARG, "instance update must keep the instance count");
+    int rc = validate_instances(ctx, instances, count, (uint32_t)ctx->meshes.size(), ctx->nmat);
+    if (rc != GKRT_OK) return rc;
+    DeviceGuard device_guard(ctx->device);
+    if (!ctx->h_trace_counters) {   // first use: trace passes start recording their counters
+        for (cudaEvent_t& ev : ctx->trace_ev)
+            if (!ev) GK_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        GK_CUDA(cudaMallocHost((void**)&ctx->h_trace_counters, 14 * sizeof(unsigned long long)));
+    }
+    const PassScope scope(ctx, kPassTlas, (cudaStream_t)stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    ctx->inst.assign(instances, instances + count);
+    poll_trace_counters(ctx);
+    bool refit = ctx->blas_ready && ctx->tlas_ready;
+    if (refit) {
+        std::vector<uint8_t> m;
+        tlas_members(ctx, m);
+        refit = m == ctx->tlas_members;
+    }
+    if (refit && ctx->visits_base > 0.0 && ctx->visits_last > 0.0)
+        refit = ctx->visits_last < (double)growth_limit * ctx->visits_base;
+    if (refit) {
+        if ((rc = build_emitters(ctx, st)) != GKRT_OK) return rc;
+        return refit_tlas(ctx, st);
+    }
+    // rebuild: the next completed pass traced on the new tree sets the baseline
+    ctx->visits_base = -1.0;
+    ctx->base_after = ctx->trace_seq;
+    if (!ctx->blas_ready) {
+        if ((rc = build_emitters(ctx, st)) != GKRT_OK) return rc;
+        return ensure_bvh(ctx, 0, st);
+    }
+    return build_tlas(ctx, st, build_emitters);
+}
+
 int gkrt_build_bvh(GkrtContext* ctx, uint32_t flags, void* stream) {
     if (!ctx) return GKRT_ERR_INVALID_ARG;
     if (flags & ~(GKRT_BUILD_ALL | GKRT_BUILD_ON_HOST)) return fail(ctx, GKRT_ERR_INVALID_ARG, "unknown build flags");
@@ -1197,6 +1274,13 @@ int gkrt_trace_pass(GkrtContext* ctx, const GkrtFrameConstants* fc, void* stream
     const int stack_words = std::max(8, std::min(kStackSize, ctx->blas_bin_depth + ctx->tlas_bin_depth + 3));
     GK_CUDA(gkrt_launch_trace_pass(sc, *fc, (int)ctx->W, (int)ctx->H, (int)ctx->P, im, ctx->d_counters, ctx->d_work,
                                    ctx->num_sms, stack_words, ctx->textured, st));
+    if (ctx->h_trace_counters) {   // the refit-or-rebuild policy is in use: this pass's counters
+        const int k = (int)(ctx->trace_seq & 1);
+        GK_CUDA(cudaMemcpyAsync(ctx->h_trace_counters + 7 * k, ctx->d_counters, 7 * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, st));
+        GK_CUDA(cudaEventRecord(ctx->trace_ev[k], st));
+        ++ctx->trace_seq;
+    }
     return GKRT_OK;
 }
 
@@ -1649,6 +1733,7 @@ int gkrt_get_stats(GkrtContext* ctx, GkrtStats* out) {
     out->wide_nodes = ctx->blas_wide_count + ctx->tlas_wide_count;
     out->wide_depth = (uint32_t)(ctx->blas_wide_depth + ctx->tlas_wide_depth);
     out->tlas_refits = ctx->tlas_refits;
+    out->tlas_rebuilds = ctx->tlas_rebuilds;
     return GKRT_OK;
 }
 

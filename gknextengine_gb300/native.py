@@ -43,6 +43,7 @@ def load(path: str | None = None):
     L.gkrt_scene_upload.argtypes = [vp, C.POINTER(abi.GkrtSceneDesc)]
     L.gkrt_scene_update_instances.argtypes = [vp, vp, C.c_uint32, vp]
     L.gkrt_scene_refit_instances.argtypes = [vp, vp, C.c_uint32, vp]
+    L.gkrt_scene_update_instances_auto.argtypes = [vp, vp, C.c_uint32, C.c_float, vp]
     L.gkrt_build_bvh.argtypes = [vp, C.c_uint32, vp]
     for n in ("gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_render_frame"):
         getattr(L, n).argtypes = [vp, C.POINTER(abi.GkrtFrameConstants), vp]
@@ -93,6 +94,7 @@ def load(path: str | None = None):
 EXPORTED = [
     "gkrt_context_create", "gkrt_context_destroy", "gkrt_last_error_message", "gkrt_abi_version",
     "gkrt_resize", "gkrt_scene_upload", "gkrt_scene_update_instances", "gkrt_scene_refit_instances",
+    "gkrt_scene_update_instances_auto",
     "gkrt_build_bvh",
     "gkrt_trace_pass", "gkrt_reproject_pass", "gkrt_denoise_pass", "gkrt_end_frame", "gkrt_render_frame",
     "gkrt_output_resize", "gkrt_output_pass", "gkrt_get_output", "gkrt_copy_output_to_host",

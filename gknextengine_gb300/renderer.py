@@ -104,6 +104,13 @@ class PathTracingRenderer:
         self._check(self._lib.gkrt_scene_refit_instances(self._h, inst.ctypes.data, inst.shape[0],
                                                          self._stream(stream)))
 
+    def update_instances_auto(self, instances: np.ndarray, growth_limit: float = 1.25, stream=None):
+        """The same update, refit while the node visits per ray of the newest finished trace pass
+        stay below growth_limit times those right after the last rebuild, else rebuilt."""
+        inst = np.ascontiguousarray(instances, dtype=abi.INSTANCE_DTYPE)
+        self._check(self._lib.gkrt_scene_update_instances_auto(self._h, inst.ctypes.data, inst.shape[0],
+                                                               C.c_float(growth_limit), self._stream(stream)))
+
     def build_bvh(self, flags: int = abi.BUILD_ALL, stream=None):
         self._check(self._lib.gkrt_build_bvh(self._h, flags, self._stream(stream)))
 

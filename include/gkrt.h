@@ -284,6 +284,8 @@ typedef struct GkrtStats {
     uint32_t tlas_refits;       /* instance-level refits since creation                   */
     uint32_t hit_fetches;       /* closest hits whose vertex, normal, material and instance
                                    data were read (hit reconstruction), last pass          */
+    uint32_t tlas_rebuilds;     /* instance-level builds since creation (uploads included) */
+    uint32_t pad;
 } GkrtStats;
 
 typedef struct GkrtContext GkrtContext;
@@ -314,6 +316,16 @@ int  gkrt_scene_update_instances(GkrtContext* ctx, const GkrtInstance* instances
  * (visibility, or a mesh without triangles) it rebuilds instead. */
 int  gkrt_scene_refit_instances(GkrtContext* ctx, const GkrtInstance* instances,
                                 uint32_t count, void* stream);
+/* The same update, refit or rebuild by the traversal cost the refits have cost so far: it refits
+ * while the tree keeps its instances and the node visits per ray of the latest completed trace
+ * pass are below growth_limit times those of the first completed pass after the last rebuild,
+ * and rebuilds otherwise (then the next completed pass sets the new baseline). Each trace pass
+ * copies its counters to page-locked memory without a host wait; the policy reads the newest
+ * pass that has finished, so it may act one frame late. growth_limit >= 1 (1: rebuild every
+ * time); gkrt_scene_update_instances and _refit_instances do not consult it. Counts of both
+ * outcomes in GkrtStats (tlas_refits, tlas_rebuilds). */
+int  gkrt_scene_update_instances_auto(GkrtContext* ctx, const GkrtInstance* instances, uint32_t count,
+                                      float growth_limit, void* stream);
 
 /* Acceleration structures (RayTraceBaseRenderer::CreateBottomLevelStructures /
  * CreateTopLevelStructures, RayTraceBaseRenderer.cpp:276-386; TLAS update :205-218).

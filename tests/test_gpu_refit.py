@@ -187,3 +187,49 @@ def test_refit_of_a_host_built_tree_and_mesh_changes(env):
         assert a.stats().device_error == 0
     finally:
         a.build_bvh(abi.BUILD_ALL)
+
+
+def test_auto_policy_refits_then_rebuilds():
+    """gkrt_scene_update_instances_auto: small motions keep the tree (refits, no rebuild); once
+    the spheres are scattered across the city the node visits per ray grow past the limit and
+    the call rebuilds, after which visits fall back. Every frame's hits equal the oracle's."""
+    sc, cam, st, motion = small_city()
+    st.flags = abi.FRAME_PRIMARY_IDS
+    fb = camera.FrameBuilder(W, H, st)
+    rng = np.random.default_rng(7)
+    rays = random_rays(rng, 4000, (-20.0, 0.0, -20.0), (140.0, 60.0, 140.0))
+    with PathTracingRenderer(0) as r:
+        r.load_scene(sc)
+        r.create_swap_chain(W, H)
+        s0 = r.stats()
+        visits = []
+
+        def frame(k, inst, limit):
+            r.update_instances_auto(inst, limit)
+            r.trace_pass(fb.build(cam, k))
+            r.synchronize()
+            visits.append(r.stats().node_visits / max(r.stats().rays_traced, 1))
+
+        for k in range(1, 5):   # small motions: refit
+            frame(k, motion.instances(k), 1.25)
+        s1 = r.stats()
+        assert s1.tlas_refits - s0.tlas_refits == 4 and s1.tlas_rebuilds == s0.tlas_rebuilds
+        # scatter the spheres across the whole city: the refit tree's boxes balloon
+        inst = motion.instances(5)
+        sph = slice(motion.first, motion.first + motion.radius.shape[0])
+        w = inst["world"][sph].astype(np.float64)
+        w[:, 3] = rng.uniform(0.0, 120.0, w.shape[0])
+        w[:, 11] = rng.uniform(0.0, 120.0, w.shape[0])
+        inst["world"][sph] = w.astype(np.float32)
+        inst["world_inv"][sph] = np.stack([scenes.affine_inverse(x) for x in inst["world"][sph]])
+        for k in range(5, 9):
+            frame(k, inst, 1.25)
+            assert_hits_equal(gpu_trace_rays(r, rays), O.OracleScene(with_instances(sc, inst)).trace_rays(rays))
+        s2 = r.stats()
+        assert s2.tlas_rebuilds > s1.tlas_rebuilds, visits   # the growth triggered a rebuild
+        assert visits[-1] < max(visits[4:6]), visits          # and the rebuilt tree is cheaper
+        assert s2.device_error == 0
+        # growth_limit below 1 is refused
+        from gknextengine_gb300.native import GkrtError
+        with pytest.raises(GkrtError):
+            r.update_instances_auto(inst, 0.5)
