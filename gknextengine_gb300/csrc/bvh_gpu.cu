@@ -18,7 +18,9 @@
 //   emit      children with more than kSmall primitives become the next round's big tasks
 //             (with their work items); the others become small tasks with a reserved run of
 //             m - 1 node slots (the most a subtree of m primitives can use).
-// The host reads back one group of counts per round. Small tasks are finished at the end by
+// For the mesh level the host reads back one group of counts per round; the instance level
+// runs the same steps in one cooperative launch (k_inst_level, below). Small tasks are finished
+// at the end by
 // one thread each, sequentially and with the host builder's leaf rule (SAH leaf test for
 // up to max_leaf triangles). Node indices are deterministic; reserved slots that a small
 // subtree does not use stay zero and are never referenced.
@@ -1598,7 +1600,6 @@ struct GpuBvh {
     DBuf<SmallTask> small;
     DBuf<BvhNode> nodes;
     DBuf<MeshRange> ranges;
-    DBuf<GpuInstBox> inst;
     DBuf<int4> witems[2];
     DBuf<uint32_t> wcnt, woff, werr, sync, result;
     DBuf<WEnt> wcache;
@@ -1614,7 +1615,7 @@ struct GpuBvh {
         }
         wleft.release(); wleft_scan.release(); bsum32.release(); tot32.release(); info.release(); map.release();
         cc.release(); cc_scan.release(); bsum4.release(); tot4.release(); bins.release(); tb.release();
-        split.release(); small.release(); nodes.release(); ranges.release(); inst.release();
+        split.release(); small.release(); nodes.release(); ranges.release();
         witems[0].release(); witems[1].release(); wcnt.release(); woff.release(); werr.release();
         sync.release(); result.release(); wcache.release(); wcache_n.release();
         if (result_host) cudaFreeHost(result_host);
@@ -1856,28 +1857,6 @@ cudaError_t gpu_bvh_build_meshes(GpuBvh* B, const float4* pos, const uint32_t* i
         ++B->launches;
     }
     GK_TRY(cudaGetLastError());
-    return cudaStreamSynchronize(st);
-}
-
-cudaError_t gpu_bvh_build_instances(GpuBvh* B, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
-                                    uint32_t node_base, GpuBvhResult* out, cudaStream_t st) {
-    GK_TRY(B->inst.need(std::max<uint32_t>(n, 1u)));
-    GK_TRY(B->map.need(std::max<uint32_t>(n, 1u)));
-    std::vector<uint32_t> map(n);
-    for (uint32_t i = 0; i < n; ++i) map[i] = inst_host[i].inst;
-    if (n) {
-        GK_TRY(cudaMemcpyAsync(B->inst.p, inst_host, n * sizeof(GpuInstBox), cudaMemcpyHostToDevice, st));
-        GK_TRY(cudaMemcpyAsync(B->map.p, map.data(), n * 4ull, cudaMemcpyHostToDevice, st));
-    }
-    GK_TRY(B->box.need(6 * (size_t)std::max<uint32_t>(n, 1u)));
-    GK_TRY(B->cent.need(3 * (size_t)std::max<uint32_t>(n, 1u)));
-    if (n) {
-        k_inst_boxes<<<(n + 255) / 256, 256, 0, st>>>(B->inst.p, n, mesh_box, B->box.p, B->cent.p);
-        ++B->launches;
-    }
-    GK_TRY(cudaGetLastError());
-    const std::vector<uint32_t> rb(1, 0u), re(1, n);
-    GK_TRY(B->build(n, rb, re, 1, true, B->map.p, node_base, out, st));
     return cudaStreamSynchronize(st);
 }
 

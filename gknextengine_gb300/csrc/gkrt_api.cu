@@ -587,7 +587,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st, int (*during)(GkrtContext*, cu
     const uint32_t base = ctx->blas_node_count;
     int rc;
     const bool coop = !ctx->host_build && gpu_bvh_cooperative_supported();
-    if (during && !coop && (rc = during(ctx, st)) != GKRT_OK) return rc;
+    if (during && !coop && (rc = during(ctx, st)) != GKRT_OK) return rc;   // the host builder
     if (!ctx->host_build) {
         if ((rc = get_builder(ctx)) != GKRT_OK) return rc;
         // the instance tables first: their host work and uploads overlap the stream's earlier work
@@ -639,32 +639,7 @@ int build_tlas(GkrtContext* ctx, cudaStream_t st, int (*during)(GkrtContext*, cu
             ++ctx->tlas_rebuilds;
             return rc_during;
         }
-        std::vector<GpuInstBox> ib;
-        ib.reserve(n);
-        for (uint32_t i = 0; i < n; ++i) {
-            const GkrtInstance& in = ctx->inst[i];
-            if (!in.visible || ctx->blas_root[in.mesh_id] < 0) continue;
-            GpuInstBox b;
-            std::memcpy(b.world, in.world, 48);
-            b.mesh = in.mesh_id;
-            b.inst = i;
-            b.pad0 = b.pad1 = 0;
-            ib.push_back(b);
-        }
-        GpuBvhResult r;
-        GK_CUDA(gpu_bvh_build_instances(ctx->builder, ib.data(), (uint32_t)ib.size(), ctx->d_blas_box, base, &r, st));
-        if ((rc = ensure_node_cap(ctx, (size_t)base + r.node_count)) != GKRT_OK) return rc;
-        if (r.node_count)
-            GK_CUDA(cudaMemcpyAsync(ctx->d_nodes + base, r.nodes, (size_t)r.node_count * sizeof(BvhNode),
-                                    cudaMemcpyDeviceToDevice, st));
-        GK_CUDA(cudaStreamSynchronize(st));
-        ctx->tlas_root = ib.empty() ? -1 : r.root_node[0];
-        ctx->tlas_nodes = r.nodes_used;
-        ctx->tlas_bin_depth = r.depth;
-        if ((rc = finish_tlas(ctx, r.node_count, st)) != GKRT_OK) return rc;
-        ctx->tlas_ready = true;
-        ++ctx->tlas_rebuilds;
-        return GKRT_OK;
+        return fail(ctx, GKRT_ERR_NO_DEVICE, "the GPU instance-level build needs cooperative launches");
     }
     std::vector<float> boxes;
     std::vector<uint32_t> map;

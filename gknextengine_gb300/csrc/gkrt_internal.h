@@ -150,13 +150,10 @@ uint32_t gpu_bvh_launches(const GpuBvh* b);   // kernels launched by all its bui
 cudaError_t gpu_bvh_build_meshes(GpuBvh* b, const float4* pos, const uint32_t* indices, const GkrtMesh* meshes,
                                  uint32_t nmesh, uint32_t node_base, float4* tris_out, GpuBvhResult* out,
                                  cudaStream_t st);
-// Instance-level tree; mesh_box: device, 6 floats per mesh.
-cudaError_t gpu_bvh_build_instances(GpuBvh* b, const GpuInstBox* inst_host, uint32_t n, const float* mesh_box,
-                                    uint32_t node_base, GpuBvhResult* out, cudaStream_t st);
-// The instance level in one cooperative launch and one host wait: a binned-SAH tree by the
-// rule of gpu_bvh_build_instances over the n records at `inst` (device), root node_base,
-// slots [node_base, node_base + node_count) of the
-// device array `nodes`, node_cap >= n + 1 slots zeroed first) collapsed into wide nodes
+// The instance level in one cooperative launch and one host wait: a binned-SAH tree (the
+// builder's rule, one instance per leaf) over the n records at `inst` (device; mesh_box: 6
+// floats per mesh), root node_base, slots [node_base, node_base + node_count) of the device
+// array `nodes` (node_cap >= n + 1 slots, zeroed first), collapsed into wide nodes
 // [wide_base, wide_base + wide_count) of `wide` (wide_cap nodes in all), links recorded when
 // non-null. res->error != 0: the build failed (non-finite transforms, more than 64 levels);
 // the nodes are then unusable.
