@@ -20,9 +20,8 @@
 //             m - 1 node slots (the most a subtree of m primitives can use).
 // For the mesh level the host reads back one group of counts per round; the instance level
 // runs the same steps in one cooperative launch (k_inst_level, below). Small tasks are finished
-// at the end by
-// one thread each, sequentially and with the host builder's leaf rule (SAH leaf test for
-// up to max_leaf triangles). Node indices are deterministic; reserved slots that a small
+// at the end by one thread each (one warp each at the instance level), sequentially and with
+// the host builder's leaf rule (SAH leaf test for up to max_leaf triangles). Node indices are deterministic; reserved slots that a small
 // subtree does not use stay zero and are never referenced.
 // Node layout and leaf encoding are those of gk_trace.cuh.
 #include <algorithm>
