@@ -873,11 +873,11 @@ cudaError_t gkrt_encode_tmap_2d(CUtensorMap* map, const void* base, uint32_t ele
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// cuTensorMapEncodeTiled for bf16 tensors of rank 2..5; zeros outside the tensor. swizzle64:
-// the 64-byte swizzle of the tensor-core kernels' K-major operands (inner box <= 64 bytes),
-// else no swizzle (dense boxes).
+// cuTensorMapEncodeTiled for bf16 tensors of rank 2..5; zeros outside the tensor. swizzle: 0
+// none (dense boxes), 64 or 128 bytes (the tensor-core kernels' operand layouts; the inner box
+// at most that many bytes).
 static cudaError_t encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
-                                    const uint64_t* strides_bytes, const uint32_t* box, bool swizzle64) {
+                                    const uint64_t* strides_bytes, const uint32_t* box, int swizzle) {
     typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -890,7 +890,8 @@ static cudaError_t encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t
         if (q != cudaDriverEntryPointSuccess || !p) return cudaErrorNotSupported;
         fn = (EncodeFn)p;
     }
-    if (rank < 2 || rank > 5 || ((uintptr_t)base & 15u) || (box[0] * 2u) % 16u || (swizzle64 && box[0] * 2u > 64u))
+    if (rank < 2 || rank > 5 || ((uintptr_t)base & 15u) || (box[0] * 2u) % 16u ||
+        (swizzle != 0 && swizzle != 64 && swizzle != 128) || (swizzle && box[0] * 2u > (uint32_t)swizzle))
         return cudaErrorInvalidValue;
     cuuint64_t d[5], s[4];
     cuuint32_t b[5], es[5];
@@ -905,18 +906,24 @@ static cudaError_t encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t
         if (s[i] % 16u) return cudaErrorInvalidValue;
     }
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, const_cast<void*>(base), d, s, b, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    swizzle == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                   : (swizzle == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_NONE),
                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                   const uint64_t* strides_bytes, const uint32_t* box) {
-    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, true);
+    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, 64);
+}
+cudaError_t gkrt_encode_tmap_bf16_sw128(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                        const uint64_t* strides_bytes, const uint32_t* box) {
+    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, 128);
 }
 cudaError_t gkrt_encode_tmap_bf16_dense(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                         const uint64_t* strides_bytes, const uint32_t* box) {
-    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, false);
+    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, 0);
 }
 
 int gkrt_internal_ready_view(GkrtContext* ctx, SceneView* view, unsigned long long** counters, int* device) {
@@ -1914,12 +1921,11 @@ int gkrt_conv3x3_wgrad_bf16(const void* dy, const void* x, uint32_t batch, uint3
         return GKRT_ERR_INVALID_ARG;
     uint32_t* d_err = standalone_err_word();
     if (!d_err) return GKRT_ERR_OOM;
-    WgradArgs a;
+    WgradArgs a{};
     a.B = (int)batch; a.H = (int)height; a.W = (int)width;
     a.dp = (const __nv_bfloat16*)dy; a.dp_c = (int)cout; a.dp_off = 0; a.cout = (int)cout;
     a.x = (const __nv_bfloat16*)x; a.x_c = (int)cin; a.x_off = 0; a.cin = (int)cin;
     a.dw = dw;
-    a.chunk = 2048;
     a.err = d_err;
     cudaError_t e = gkrt_launch_conv_wgrad(a, (cudaStream_t)stream);
     if (e == cudaErrorInvalidValue) return GKRT_ERR_INVALID_ARG;

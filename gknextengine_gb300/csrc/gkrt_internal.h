@@ -245,7 +245,6 @@ struct WgradArgs {
     const __nv_bfloat16* x;
     int x_c, x_off, cin;
     float* dw;
-    int chunk;                     // pixels per CTA, a multiple of 32
     uint32_t* err;
 };
 }

@@ -2,15 +2,11 @@
 // convolution (k_conv.cu): weight gradients on the tensor cores, and the element-wise,
 // pooling, loss and optimiser kernels.
 //
-// Weight gradient of a 3x3 convolution, dW[cout][tap][cin] = sum over pixels of
-// dP[p][cout] * X[p + tap offset][cin], is a GEMM with M = cout (padded to 128 rows of
-// zeros), N = cin and K = pixels. One CTA takes one tap and a run of pixels; both operands
-// are staged by the CTA's threads into the 64-byte-swizzled K-major layout (pixels along K)
-// straight from the NHWC tensors, made visible to the tensor core with a proxy fence, and
-// multiplied by one thread while the next pixels are staged (two buffers); a thread stages an
-// 8-pixel x 8-channel block with eight 16-byte loads and stores it transposed (byte permutes)
-// as eight 16-byte rows. The FP32
-// accumulator is added to dW with atomics. Every wait is bounded.
+// The weight gradient of a 3x3 convolution, dW[cout][tap][cin] = sum over pixels of
+// dP[p][cout] * X[p + tap offset][cin], is a GEMM with K = pixels whose operands TMA loads
+// straight from the NHWC tensors in the MN-major layout (k_conv_wgrad_tma, below).
+#include <algorithm>
+
 #include "gk_umma.cuh"
 #include "gkrt_internal.h"
 
@@ -18,63 +14,71 @@ namespace gk {
 
 namespace {
 
-constexpr int kWgThreads = 128;
-constexpr int kWgStep = 32;   // pixels per K step
+// ---- weight gradient with TMA-fed MN-major operands ----
+// The same GEMM, dW[cout][tap][cin] = sum over pixels of dP[p][cout] X[p + tap][cin], with K =
+// pixels: NHWC rows hold the channels of one pixel contiguously, which is the MN-major layout
+// of both operands for K along pixels, so TMA loads them unchanged. A K step is a run of
+// kWtK pixels of one image row; per 64-channel group one box {64 channels, kWtK pixels} lands
+// 128-byte swizzled (an atom of 8 pixel rows x 128 bytes, atoms 1024 bytes apart along K). X's
+// box starts at the tap's shift, and TMA's zero fill outside the tensor is the padding. The CTA
+// takes one tap and a run of image rows: warp 0 issues the loads into a ring of stages, warp 1
+// the MMAs (M = 128 rows of dP's channels, zero past cout; N = cin), and all four warps the
+// epilogue (atomics into dW). Every wait is bounded.
 
-__device__ __forceinline__ uint32_t sw64_offset(int r, int k) {   // byte offset of element (row r, k) in a tile
-    return (uint32_t)((r >> 3) * 512 + (r & 7) * 64 + ((((k >> 3) ^ (r >> 1)) & 3) << 4) + (k & 7) * 2);
+constexpr int kWtThreads = 128;
+constexpr int kWtK = 32;                        // pixels per K step
+constexpr int kWtAtom = kWtK * 128;             // one 64-channel box of a step: 4096 bytes
+constexpr int kWtStages = 4;
+constexpr int kWtGuard = 4096;                  // shared memory after the last stage, never written
+
+// Descriptor of an MN-major, 128-byte-swizzled operand: the leading byte offset is the stride
+// between 64-channel atoms along M (or N), 4096 bytes here, and the stride byte offset the one
+// between 8-row groups along K, 1024 bytes (the weight-gradient test against torch holds this
+// assignment; the swapped one gives wrong sums).
+__device__ __forceinline__ uint64_t wt_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)(((uint32_t)kWtAtom >> 4) & 0x3FFFu) << 16;   // leading byte offset
+    d |= (uint64_t)((1024u >> 4) & 0x3FFFu) << 32;               // stride byte offset
+    d |= (uint64_t)1u << 46;   // version
+    d |= (uint64_t)2u << 61;   // SWIZZLE_128B
+    return d;
 }
 
-__device__ __forceinline__ void fence_proxy_async() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ uint32_t word_of(const uint4& v, int i) {
-    return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
-}
-
-// Stores the 8 x 8 block v (v[i]: 8 channels of pixel i) transposed: row r0 + c of the
-// 64-byte-swizzled K-major tile gets the 8 pixels' channel c as one 16-byte chunk at K
-// offset k0 (a multiple of 8).
-__device__ __forceinline__ void store_block_t(uint8_t* tile, int r0, int k0, const uint4* v) {
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        uint32_t w[4];
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            const uint32_t lo = word_of(v[2 * h], c >> 1), hi = word_of(v[2 * h + 1], c >> 1);
-            w[h] = (c & 1) ? __byte_perm(lo, hi, 0x7632) : __byte_perm(lo, hi, 0x5410);
-        }
-        *reinterpret_cast<uint4*>(tile + sw64_offset(r0 + c, k0)) = make_uint4(w[0], w[1], w[2], w[3]);
-    }
-}
-
-__global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
+__global__ void __launch_bounds__(kWtThreads) k_conv_wgrad_tma(const __grid_constant__ CUtensorMap mdp,
+                                                               const __grid_constant__ CUtensorMap mx, WgradArgs a,
+                                                               int rows_per_cta, int nb) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    const int a_bytes = 128 * 64;
-    const int b_bytes = ((a.cin * 64) + 1023) & ~1023;
-    const int stage_bytes = a_bytes + b_bytes;
-    uint64_t* done = reinterpret_cast<uint64_t*>(smem + 2 * stage_bytes);
-    uint64_t* accb = done + 2;
+    const int stage_bytes = (2 + nb) * kWtAtom;   // A: 2 atoms (M = 128), B: nb atoms (N = cin)
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kWtStages * stage_bytes + kWtGuard);
+    uint64_t* empty = full + kWtStages;
+    uint64_t* accb = empty + kWtStages;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const long long npix = (long long)a.B * a.H * a.W;
-    const long long p0 = (long long)blockIdx.x * a.chunk;
-    const long long pend = min(p0 + (long long)a.chunk, npix);   // pixels of this CTA: [p0, pend)
-    const int nk = (int)((min((long long)a.chunk, npix - p0) + kWgStep - 1) / kWgStep);
+    const int rows = a.B * a.H;
+    const int r0 = blockIdx.x * rows_per_cta, r1 = min(r0 + rows_per_cta, rows);
+    const int xsteps = (a.W + kWtK - 1) / kWtK;
+    const int nk = r1 > r0 ? (r1 - r0) * xsteps : 0;
+    const bool a_two = a.cout > 64;   // dP's second 64-channel atom is loaded, else it stays zero
     const uint32_t ncols = a.cin <= 32 ? 32u : a.cin <= 64 ? 64u : a.cin <= 128 ? 128u : 256u;
 
-    for (int i = tid; i < 2 * stage_bytes / 16; i += kWgThreads)   // zero rows stay zero (M padding)
-        reinterpret_cast<uint4*>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (!a_two)   // the second A atom of every stage: zero rows of M
+        for (int st = 0; st < kWtStages; ++st)
+            for (int i = tid; i < kWtAtom / 16; i += kWtThreads)
+                reinterpret_cast<uint4*>(smem + st * stage_bytes + kWtAtom)[i] = make_uint4(0u, 0u, 0u, 0u);
     if (tid == 0) {
-        mbar_init(&done[0], 1);
-        mbar_init(&done[1], 1);
+        for (int st = 0; st < kWtStages; ++st) {
+            mbar_init(&full[st], 1);
+            mbar_init(&empty[st], 1);
+        }
         mbar_init(accb, 1);
+        *abort_flag = 0;
         mbar_fence_init();
     }
-    if (warp == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the zeroed atoms, for the tensor core
+    if (warp == 1) {
         tmem_alloc(tslot, ncols);
         tmem_relinquish();
     }
@@ -82,88 +86,50 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cin);
-    bool ok = true;
-    const int ga = a.cout / 8, gb = a.cin / 8;
-    // A[cout][pixel] = dP[pixel][cout] and B[cin][pixel] = X[pixel shifted by the tap][cin]
-    // (zero outside the image): per K step, one thread per block of 8 pixels x 8 channels
-    // (eight 16-byte loads, consecutive threads on consecutive channel groups), stored
-    // transposed as eight 16-byte rows. A thread has at most two blocks per step
-    // (4 (cout / 8 + cin / 8) <= 192); it loads its next step's blocks into registers before
-    // the barrier of the current one, so the loads are in flight during the barrier and the MMA.
-    const int na = (kWgStep / 8) * ga, nb = (kWgStep / 8) * gb;
-    uint4 v[2][8];
-    auto load_step = [&](int k) {
-        const long long qk = p0 + (long long)k * kWgStep;
-#pragma unroll
-        for (int m = 0; m < 2; ++m) {
-            const int it = tid + m * kWgThreads;
-            if (it >= na + nb) continue;
-            const bool is_a = it < na;
-            const int j = is_a ? it : it - na, gn = is_a ? ga : gb;
-            const int g = j % gn, jb = j / gn;
-            const long long q0 = qk + 8 * jb;
-            if (is_a) {
-#pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    v[m][i] = q0 + i < pend
-                                  ? *reinterpret_cast<const uint4*>(a.dp + (q0 + i) * a.dp_c + a.dp_off + 8 * g)
-                                  : make_uint4(0u, 0u, 0u, 0u);
-            } else {
-                // coordinates of the block's first pixel, then stepped along the row
-                int x = 0, y = 0;
-                long long b = 0;
-                if (q0 < pend) {
-                    const long long row = q0 / a.W;
-                    x = (int)(q0 - row * a.W);
-                    y = (int)(row % a.H);
-                    b = row / a.H;
+
+    if (warp == 0) {
+        if (lane == 0) {   // producer
+            const uint32_t bytes = (uint32_t)((a_two ? 2 : 1) + nb) * (uint32_t)kWtAtom;
+            for (int k = 0; k < nk && !*abort_flag; ++k) {
+                const int s = k % kWtStages;
+                const uint32_t use = (uint32_t)(k / kWtStages);
+                if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1u) & 1u, a.err)) {
+                    *abort_flag = 1;
+                    break;
                 }
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    v[m][i] = make_uint4(0u, 0u, 0u, 0u);
-                    if (q0 + i < pend) {
-                        const int xs = x + dx, ys = y + dy;
-                        if (xs >= 0 && xs < a.W && ys >= 0 && ys < a.H)
-                            v[m][i] = *reinterpret_cast<const uint4*>(a.x + ((b * a.H + ys) * a.W + xs) * a.x_c +
-                                                                      a.x_off + 8 * g);
-                    }
-                    if (++x == a.W) {
-                        x = 0;
-                        if (++y == a.H) { y = 0; ++b; }
-                    }
-                }
+                const int row = r0 + k / xsteps, x0 = (k % xsteps) * kWtK;
+                const int img = row / a.H, y = row - img * a.H;
+                uint8_t* st = smem + s * stage_bytes;
+                mbar_expect_tx(&full[s], bytes);
+                tma_load_4d(st, &mdp, 0, x0, y, img, &full[s]);
+                if (a_two) tma_load_4d(st + kWtAtom, &mdp, 64, x0, y, img, &full[s]);
+                for (int j = 0; j < nb; ++j)
+                    tma_load_4d(st + (2 + j) * kWtAtom, &mx, 64 * j, x0 + dx, y + dy, img, &full[s]);
             }
         }
-    };
-    if (nk > 0) load_step(0);
-    for (int k = 0; k < nk && ok; ++k) {
-        const int s = k & 1;
-        if (k >= 2 && !mbar_wait_bounded(&done[s], (uint32_t)((k >> 1) - 1) & 1u, a.err)) ok = false;
-        if (__syncthreads_or(!ok)) { ok = false; break; }
-        uint8_t* sa = smem + s * stage_bytes;
-        uint8_t* sb = sa + a_bytes;
-#pragma unroll
-        for (int m = 0; m < 2; ++m) {
-            const int it = tid + m * kWgThreads;
-            if (it >= na + nb) continue;
-            const bool is_a = it < na;
-            const int j = is_a ? it : it - na, gn = is_a ? ga : gb;
-            store_block_t(is_a ? sa : sb, 8 * (j % gn), 8 * (j / gn), v[m]);
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer
+            const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cin) | (1u << 15) | (1u << 16);   // MN-major A, B
+            bool ok = true;
+            for (int k = 0; k < nk && ok; ++k) {
+                const int s = k % kWtStages;
+                if (!mbar_wait_bounded(&full[s], (uint32_t)(k / kWtStages) & 1u, a.err)) {
+                    *abort_flag = 1;
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t sa = smem_u32(smem + s * stage_bytes), sb = sa + 2u * (uint32_t)kWtAtom;
+                for (int kk = 0; kk < kWtK / 16; ++kk)   // 16 pixels (two 8-row groups) per MMA
+                    umma_bf16(tmem, wt_desc(sa + 2048u * kk), wt_desc(sb + 2048u * kk), idesc,
+                              (k | kk) != 0 ? 1u : 0u);
+                umma_commit(&empty[s]);
+            }
         }
-        if (k + 1 < nk) load_step(k + 1);
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            tc_fence_after();
-            const uint32_t ua = smem_u32(sa), ub = smem_u32(sb);
-            umma_bf16(tmem, umma_desc_sw64(ua), umma_desc_sw64(ub), idesc, k != 0 ? 1u : 0u);
-            umma_bf16(tmem, umma_desc_sw64(ua + 32u), umma_desc_sw64(ub + 32u), idesc, 1u);
-            umma_commit(&done[s]);
-        }
+        if (lane == 0) umma_commit(accb);
     }
-    if (tid == 0) umma_commit(accb);
-    const bool ready = mbar_wait_bounded(accb, 0u, a.err) && ok && nk > 0;
+    __syncwarp();
+    const bool ready = mbar_wait_bounded(accb, 0u, a.err) && nk > 0 && !*abort_flag;
     __syncwarp();
     tc_fence_after();
     const int r = warp * 32 + lane;   // TMEM lane = cout row
@@ -181,7 +147,7 @@ __global__ void __launch_bounds__(kWgThreads) k_conv_wgrad(WgradArgs a) {
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, ncols);
+    if (warp == 1) tmem_dealloc(tmem, ncols);
 }
 
 // ---- element-wise kernels (NHWC bf16 with channel stride/offset) ----
@@ -297,27 +263,49 @@ __global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16* dp, int 
 
 using namespace gk;
 
-size_t gkrt_wgrad_smem_bytes(int cin) {
-    return 2 * (size_t)(128 * 64 + (((cin * 64) + 1023) & ~1023)) + 64 + 1024;
+cudaError_t gkrt_encode_tmap_bf16_sw128(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                        const uint64_t* strides_bytes, const uint32_t* box);
+
+static size_t wgrad_tma_smem(int nb) {
+    return (size_t)kWtStages * (size_t)(2 + nb) * kWtAtom + kWtGuard + 256 + 1024;
 }
 
 cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
-    if (a.cin % 16 || a.cin < 16 || a.cin > 256 || a.cout % 8 || a.cout > 128 || a.chunk % kWgStep || a.chunk <= 0 ||
-        a.dp_c % 8 || a.dp_off % 8 || a.x_c % 8 || a.x_off % 8 || ((uintptr_t)a.dp & 15u) || ((uintptr_t)a.x & 15u))
+    if (a.cin % 16 || a.cin < 16 || a.cin > 256 || a.cout % 8 || a.cout < 8 || a.cout > 128 || a.dp_c % 8 ||
+        a.dp_off % 8 || a.x_c % 8 || a.x_off % 8 || a.dp_off + a.cout > a.dp_c || a.x_off + a.cin > a.x_c ||
+        ((uintptr_t)a.dp & 15u) || ((uintptr_t)a.x & 15u) || a.B < 1 || a.H < 1 || a.W < 1)
         return cudaErrorInvalidValue;
-    const long long npix = (long long)a.B * a.H * a.W;
-    const size_t smem = gkrt_wgrad_smem_bytes(a.cin);
+    static int sms_dev[kMaxDevices] = {};
     static bool attr_set[kMaxDevices] = {};   // set once per device for the largest operand (cin = 256)
     const int dev = current_device_slot();
     if (dev < 0) return cudaErrorInvalidDevice;
+    if (!sms_dev[dev]) {
+        cudaError_t e = cudaDeviceGetAttribute(&sms_dev[dev], cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+    }
     if (!attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)gkrt_wgrad_smem_bytes(256));
+        cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)wgrad_tma_smem(4));
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
-    const dim3 grid((unsigned)((npix + a.chunk - 1) / a.chunk), 9);
-    k_conv_wgrad<<<grid, kWgThreads, smem, st>>>(a);
+    const uint64_t W = (uint64_t)a.W, H = (uint64_t)a.H, B = (uint64_t)a.B;
+    const uint32_t box[4] = {64u, (uint32_t)kWtK, 1u, 1u};
+    CUtensorMap mdp, mx;
+    const uint64_t dd[4] = {(uint64_t)a.cout, W, H, B};
+    const uint64_t ds[3] = {(uint64_t)a.dp_c * 2, W * a.dp_c * 2, H * W * a.dp_c * 2};
+    cudaError_t e = gkrt_encode_tmap_bf16_sw128(&mdp, a.dp + a.dp_off, 4, dd, ds, box);
+    if (e != cudaSuccess) return e;
+    const uint64_t xd[4] = {(uint64_t)a.cin, W, H, B};
+    const uint64_t xs[3] = {(uint64_t)a.x_c * 2, W * a.x_c * 2, H * W * a.x_c * 2};
+    if ((e = gkrt_encode_tmap_bf16_sw128(&mx, a.x + a.x_off, 4, xd, xs, box)) != cudaSuccess) return e;
+    const int nb = (a.cin + 63) / 64;
+    // about two CTAs per SM over the nine taps, each a run of image rows
+    const long long rows = (long long)a.B * a.H;
+    const long long target = 2LL * sms_dev[dev];
+    const int rows_per_cta = (int)std::max(1LL, (rows * 9 + target - 1) / target);
+    const dim3 grid((unsigned)((rows + rows_per_cta - 1) / rows_per_cta), 9);
+    k_conv_wgrad_tma<<<grid, kWtThreads, wgrad_tma_smem(nb), st>>>(mdp, mx, a, rows_per_cta, nb);
     return cudaGetLastError();
 }
 

@@ -301,12 +301,11 @@ struct Unet {
         const long long npix = (long long)B * h * w;
         const LayerDef& L = kLayers[l];
         if (L.relu) GK_T(gkrt_launch_relu_bwd(dy, dy_c, dy_off, y_act, y_c, y_off, npix, L.cout, st));
-        WgradArgs wa;
+        WgradArgs wa{};
         wa.B = B; wa.H = h; wa.W = w;
         wa.dp = dy; wa.dp_c = dy_c; wa.dp_off = dy_off; wa.cout = L.cout;
         wa.x = x; wa.x_c = x_c; wa.x_off = x_off; wa.cin = L.cin;
         wa.dw = g + woff[l];
-        wa.chunk = 2048;
         wa.err = err;
         GK_T(gkrt_launch_conv_wgrad(wa, st));
         GK_T(gkrt_launch_bias_grad(dy, dy_c, dy_off, npix, L.cout, g + boff[l], st));

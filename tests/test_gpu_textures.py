@@ -43,6 +43,28 @@ def test_textured_cornell_matches_oracle(W, H):
         assert np.unique(np.round(gim[abi.IMG_NORMAL][hit][:, 3], 4)).size > 10
 
 
+def test_textured_cornell_emissive_nee_matches_oracle():
+    """The textured scene under emissive-triangle NEE (the instantiation with both the alias
+    table and the texture fetches): three frames equal to the oracle's, ids exact."""
+    sc, cam, st = scenes.cornell_textured()
+    st.nee_mode = abi.NEE_EMISSIVE
+    st.flags = abi.FRAME_PRIMARY_IDS
+    W, H = 80, 56
+    osc = O.OracleScene(sc)
+    oim = O.new_images(W, H)
+    fb = camera.FrameBuilder(W, H, st)
+    with PathTracingRenderer(0) as r:
+        r.load_scene(sc)
+        r.create_swap_chain(W, H)
+        assert r.stats().emitters > 0
+        for f in range(3):
+            fc = fb.build(cam.orbit(1.5 * f), f)
+            r.render(fc)
+            r.synchronize()
+            O.render_frame(osc, fc, W, H, oim)
+            _compare_trace_images(r.images(), oim)
+
+
 def test_textured_render_differs_from_untextured():
     """The same frame with the textures, and with the materials' texture ids set to -1 and no
     sky texture, differ (both equal the oracle's own renderings)."""
