@@ -82,7 +82,9 @@ struct AtrousArgs {
 constexpr int kConvRelu = 1, kConvF32Out = 2;
 struct ConvArgs {
     int B, H, W, cin, cout;        // cin % 32 == 0; cout % 16 == 0, 16..256 (MMA N)
-    int x_c, x_off;                // input: channel stride (>= cin) and first channel (multiple of 8)
+    int x_c, x_off;                // input: channel stride and first channel (multiple of 8)
+    int x_valid;                   // channels the input holds at x_off (multiple of 8, <= cin; 0: cin);
+                                   // the rest read as zeros
     const float* bias;             // cout floats or null
     void* out;
     int out_c, out_off;            // multiples of 16 (bf16 output)
@@ -244,6 +246,7 @@ struct WgradArgs {
     int dp_c, dp_off, cout;
     const __nv_bfloat16* x;
     int x_c, x_off, cin;
+    int x_valid;                   // channels X holds at x_off (multiple of 8, <= cin; 0: cin), the rest zero
     float* dw;
     uint32_t* err;
 };

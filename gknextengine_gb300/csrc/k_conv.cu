@@ -479,8 +479,10 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         args.H < 1 || args.W < 1 || (!f32 && (args.out_c % 16 || args.out_off % 16)) ||
         args.out_off + (f32 ? args.n_store : args.cout) > args.out_c || (f32 && args.n_store > args.cout) ||
         ((uintptr_t)x & 15u) || ((uintptr_t)w & 15u) || ((uintptr_t)args.out & 15u) || args.x_off % 8 ||
-        (args.x_c > 0 && (args.x_c % 8 || args.x_off + args.cin > args.x_c)))
+        args.x_valid < 0 || args.x_valid > args.cin || args.x_valid % 8)
         return cudaErrorInvalidValue;
+    const int xv = args.x_valid > 0 ? args.x_valid : args.cin;   // channels present; the rest are zeros
+    if (args.x_c > 0 && (args.x_c % 8 || args.x_off + xv > args.x_c)) return cudaErrorInvalidValue;
     if ((args.pool_out || args.up_out) && f32) return cudaErrorInvalidValue;
     if (args.pool_out && (args.pool_c % 8 || args.pool_off % 8 || args.pool_off + args.cout > args.pool_c ||
                           ((uintptr_t)args.pool_out & 15u)))
@@ -489,7 +491,7 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
                         ((uintptr_t)args.up_out & 15u)))
         return cudaErrorInvalidValue;
     CUtensorMap mx, mw;
-    const uint64_t xc = (uint64_t)(args.x_c > 0 ? args.x_c : args.cin);
+    const uint64_t xc = (uint64_t)(args.x_c > 0 ? args.x_c : xv);
     // per device: SM count, the attributes set, resident CTAs per output width
     static int sms_dev[kMaxDevices] = {};
     static bool halo_attr[kMaxDevices] = {};
@@ -503,7 +505,8 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     }
     const int sms = sms_dev[dev];
     if (conv_halo(args.cin, args.cout)) {
-        const uint64_t xd[4] = {(uint64_t)args.cin, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
+        // channels past xv lie outside the map: TMA fills them with zeros
+        const uint64_t xd[4] = {(uint64_t)xv, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
         const uint64_t xs[3] = {xc * 2, (uint64_t)args.W * xc * 2, (uint64_t)args.H * args.W * xc * 2};
         const uint32_t xb[4] = {8, kHaloBoxX, kHaloBoxY, 1};
         const void* xbase = static_cast<const uint8_t*>(x) + (size_t)args.x_off * 2;
@@ -533,7 +536,7 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         k_conv3x3_halo<<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles);
         return cudaGetLastError();
     }
-    const uint64_t xd[4] = {(uint64_t)args.cin, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
+    const uint64_t xd[4] = {(uint64_t)xv, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
     const uint64_t xs[3] = {xc * 2, (uint64_t)args.W * xc * 2, (uint64_t)args.H * args.W * xc * 2};
     const bool rows = conv_rows(args.cout);
     const uint32_t xb[4] = {32, kTileX, (uint32_t)(rows ? kTileY + 2 : kTileY), 1};

@@ -271,9 +271,11 @@ static size_t wgrad_tma_smem(int nb) {
 }
 
 cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
+    const int xv = a.x_valid > 0 ? a.x_valid : a.cin;   // X's channels present; the rest are zeros
     if (a.cin % 16 || a.cin < 16 || a.cin > 256 || a.cout % 8 || a.cout < 8 || a.cout > 128 || a.dp_c % 8 ||
-        a.dp_off % 8 || a.x_c % 8 || a.x_off % 8 || a.dp_off + a.cout > a.dp_c || a.x_off + a.cin > a.x_c ||
-        ((uintptr_t)a.dp & 15u) || ((uintptr_t)a.x & 15u) || a.B < 1 || a.H < 1 || a.W < 1)
+        a.dp_off % 8 || a.x_c % 8 || a.x_off % 8 || a.dp_off + a.cout > a.dp_c || a.x_valid < 0 ||
+        a.x_valid > a.cin || a.x_valid % 8 || a.x_off + xv > a.x_c || ((uintptr_t)a.dp & 15u) ||
+        ((uintptr_t)a.x & 15u) || a.B < 1 || a.H < 1 || a.W < 1)
         return cudaErrorInvalidValue;
     static int sms_dev[kMaxDevices] = {};
     static bool attr_set[kMaxDevices] = {};   // set once per device for the largest operand (cin = 256)
@@ -296,7 +298,7 @@ cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
     const uint64_t ds[3] = {(uint64_t)a.dp_c * 2, W * a.dp_c * 2, H * W * a.dp_c * 2};
     cudaError_t e = gkrt_encode_tmap_bf16_sw128(&mdp, a.dp + a.dp_off, 4, dd, ds, box);
     if (e != cudaSuccess) return e;
-    const uint64_t xd[4] = {(uint64_t)a.cin, W, H, B};
+    const uint64_t xd[4] = {(uint64_t)xv, W, H, B};   // channels past xv: TMA's zero fill
     const uint64_t xs[3] = {(uint64_t)a.x_c * 2, W * a.x_c * 2, H * W * a.x_c * 2};
     if ((e = gkrt_encode_tmap_bf16_sw128(&mx, a.x + a.x_off, 4, xd, xs, box)) != cudaSuccess) return e;
     const int nb = (a.cin + 63) / 64;

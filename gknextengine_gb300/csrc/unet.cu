@@ -37,20 +37,24 @@ constexpr LayerDef kLayers[kUnetLayers] = {
     {160, 64, 1, 64},  {64, 64, 1, 64},   {96, 32, 1, 32},  {32, 32, 1, 32},  {32, 32, 0, 3}};
 enum { E0A, E0B, E1A, E1B, E2A, E2B, E3A, E3B, D2A, D2B, D1A, D1B, D0A, D0B, OUT };
 
+// The network input x0: kXc channels per pixel (the 10 inputs, then zeros); the first layer's
+// 32 input channels read the ones past kXc as zeros (its tensor map ends there).
+constexpr int kXc = 16;
+
 __global__ void k_pack_input(const float* in, long long npix, __nv_bfloat16* x0) {
     const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;   // one pixel
     if (p >= npix) return;
-    float v[32];
+    float v[kXc];
 #pragma unroll
-    for (int c = 0; c < 32; ++c) v[c] = 0.0f;
+    for (int c = 0; c < kXc; ++c) v[c] = 0.0f;
 #pragma unroll
     for (int c = 0; c < 10; ++c) v[c] = in[p * 10 + c];
 #pragma unroll
     for (int c = 0; c < 3; ++c) v[c] = log1pf(fmaxf(v[c], 0.0f));
     v[9] = fminf(fmaxf(v[9], 0.0f), 1.0f);   // depth; misses carry 100000
-    uint4* o = reinterpret_cast<uint4*>(x0 + p * 32);
+    uint4* o = reinterpret_cast<uint4*>(x0 + p * kXc);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < kXc / 8; ++k) {
         __nv_bfloat162 h[4];
         for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(v[8 * k + 2 * j], v[8 * k + 2 * j + 1]);
         o[k] = *reinterpret_cast<uint4*>(h);
@@ -66,18 +70,18 @@ __global__ void k_pack_frame(const float4* sd, const float4* ss, const float4* a
     const int x = (int)(i % W), y = (int)(i / W);
     const size_t q = (size_t)y * P + x;
     const float4 d = sd[q], s = ss[q], a = alb[q], n = nrm[q];
-    float v[32];
+    float v[kXc];
 #pragma unroll
-    for (int c = 0; c < 32; ++c) v[c] = 0.0f;
+    for (int c = 0; c < kXc; ++c) v[c] = 0.0f;
     v[0] = log1pf(fmaxf(fmaf(d.x, a.x, s.x), 0.0f));
     v[1] = log1pf(fmaxf(fmaf(d.y, a.y, s.y), 0.0f));
     v[2] = log1pf(fmaxf(fmaf(d.z, a.z, s.z), 0.0f));
     v[3] = a.x; v[4] = a.y; v[5] = a.z;
     v[6] = n.x; v[7] = n.y; v[8] = n.z;
     v[9] = fminf(fmaxf(depth[q], 0.0f), 1.0f);   // misses carry 100000
-    uint4* o = reinterpret_cast<uint4*>(x0 + i * 32);
+    uint4* o = reinterpret_cast<uint4*>(x0 + i * kXc);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < kXc / 8; ++k) {
         __nv_bfloat162 h[4];
         for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(v[8 * k + 2 * j], v[8 * k + 2 * j + 1]);
         o[k] = *reinterpret_cast<uint4*>(h);
@@ -218,7 +222,7 @@ struct Unet {
             __nv_bfloat16** ptr;
             int level, ch;
         };
-        const Req reqs[] = {{&x0, 0, 32},    {&e0a, 0, 32},   {&cat0, 0, 96},   {&p0, 1, 32},    {&e1a, 1, 64},
+        const Req reqs[] = {{&x0, 0, kXc},    {&e0a, 0, 32},   {&cat0, 0, 96},   {&p0, 1, 32},    {&e1a, 1, 64},
                             {&cat1, 1, 160}, {&p1, 2, 64},    {&e2a, 2, 96},    {&cat2, 2, 224}, {&p2, 3, 96},
                             {&e3a, 3, 128},  {&e3b, 3, 128},  {&d2a, 2, 96},    {&d2b, 2, 96},   {&d1a, 1, 64},
                             {&d1b, 1, 64},   {&d0a, 0, 32},   {&d0b, 0, 32},    {&gy, 0, 32},    {&g_d0b, 0, 32},
@@ -258,6 +262,7 @@ struct Unet {
         a.B = B; a.H = H >> level; a.W = W >> level;
         a.cin = kLayers[l].cin; a.cout = kLayers[l].cout;
         a.x_c = in_c; a.x_off = in_off;
+        a.x_valid = in_c - in_off < a.cin ? in_c - in_off : 0;   // x0 holds fewer channels than E0A's 32
         a.bias = p + boff[l];
         a.out = out; a.out_c = out_c; a.out_off = out_off;
         a.n_store = kLayers[l].n_store;
@@ -271,7 +276,7 @@ struct Unet {
     cudaError_t forward(cudaStream_t st) {
         cudaError_t e;
 #define GK_T(x) if ((e = (x)) != cudaSuccess) return e
-        GK_T(conv(E0A, x0, 32, 0, e0a, 32, 0, 0, st));
+        GK_T(conv(E0A, x0, kXc, 0, e0a, 32, 0, 0, st));
         // the 2 x 2 pools and nearest upsamplings ride in the epilogues of the convolutions that
         // produce their inputs: 2 x 2 means of the stored values, nearest copies
         GK_T(conv(E0B, e0a, 32, 0, cat0, 96, 64, 0, st, p0, 32, 0));
@@ -305,6 +310,7 @@ struct Unet {
         wa.B = B; wa.H = h; wa.W = w;
         wa.dp = dy; wa.dp_c = dy_c; wa.dp_off = dy_off; wa.cout = L.cout;
         wa.x = x; wa.x_c = x_c; wa.x_off = x_off; wa.cin = L.cin;
+        wa.x_valid = x_c - x_off < L.cin ? x_c - x_off : 0;
         wa.dw = g + woff[l];
         wa.err = err;
         GK_T(gkrt_launch_conv_wgrad(wa, st));
@@ -347,7 +353,7 @@ struct Unet {
         GK_T(layer_bwd(E1A, g_e1a, 64, 0, e1a, 64, 0, p0, 32, 0, g_p0, 1, st));
         GK_T(gkrt_launch_avgpool2_bwd(g_p0, 32, 0, g_cat0, 96, 64, B, H, W, 32, 1, st));
         GK_T(layer_bwd(E0B, g_cat0, 96, 64, cat0, 96, 64, e0a, 32, 0, g_e0a, 0, st));
-        GK_T(layer_bwd(E0A, g_e0a, 32, 0, e0a, 32, 0, x0, 32, 0, nullptr, 0, st));
+        GK_T(layer_bwd(E0A, g_e0a, 32, 0, e0a, 32, 0, x0, kXc, 0, nullptr, 0, st));
         return cudaSuccess;
     }
 #undef GK_T
