@@ -44,25 +44,30 @@ __device__ __forceinline__ uint64_t wt_desc(uint32_t saddr) {
     return d;
 }
 
+// kTaps = 1: one tap per CTA (blockIdx.y), N = cin in nb atoms. kTaps = 9: all nine taps in one
+// CTA for cin <= 32 (one B atom per tap, nine accumulators of 32 columns in 512 TMEM columns),
+// so that dP is loaded once per step instead of once per tap.
+template <int kTaps>
 __global__ void __launch_bounds__(kWtThreads) k_conv_wgrad_tma(const __grid_constant__ CUtensorMap mdp,
                                                                const __grid_constant__ CUtensorMap mx, WgradArgs a,
                                                                int rows_per_cta, int nb) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-    const int stage_bytes = (2 + nb) * kWtAtom;   // A: 2 atoms (M = 128), B: nb atoms (N = cin)
+    const int nbt = kTaps == 1 ? nb : 9;           // B atoms per stage
+    const int stage_bytes = (2 + nbt) * kWtAtom;   // A: 2 atoms (M = 128), then the B atoms
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + kWtStages * stage_bytes + kWtGuard);
     uint64_t* empty = full + kWtStages;
     uint64_t* accb = empty + kWtStages;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(accb + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int tap0 = kTaps == 1 ? (int)blockIdx.y : 0;
     const int rows = a.B * a.H;
     const int r0 = blockIdx.x * rows_per_cta, r1 = min(r0 + rows_per_cta, rows);
     const int xsteps = (a.W + kWtK - 1) / kWtK;
     const int nk = r1 > r0 ? (r1 - r0) * xsteps : 0;
     const bool a_two = a.cout > 64;   // dP's second 64-channel atom is loaded, else it stays zero
-    const uint32_t ncols = a.cin <= 32 ? 32u : a.cin <= 64 ? 64u : a.cin <= 128 ? 128u : 256u;
+    const uint32_t ncols = kTaps == 9 ? 512u : a.cin <= 32 ? 32u : a.cin <= 64 ? 64u : a.cin <= 128 ? 128u : 256u;
 
     if (!a_two)   // the second A atom of every stage: zero rows of M
         for (int st = 0; st < kWtStages; ++st)
@@ -89,7 +94,7 @@ __global__ void __launch_bounds__(kWtThreads) k_conv_wgrad_tma(const __grid_cons
 
     if (warp == 0) {
         if (lane == 0) {   // producer
-            const uint32_t bytes = (uint32_t)((a_two ? 2 : 1) + nb) * (uint32_t)kWtAtom;
+            const uint32_t bytes = (uint32_t)((a_two ? 2 : 1) + nbt) * (uint32_t)kWtAtom;
             for (int k = 0; k < nk && !*abort_flag; ++k) {
                 const int s = k % kWtStages;
                 const uint32_t use = (uint32_t)(k / kWtStages);
@@ -103,8 +108,14 @@ __global__ void __launch_bounds__(kWtThreads) k_conv_wgrad_tma(const __grid_cons
                 mbar_expect_tx(&full[s], bytes);
                 tma_load_4d(st, &mdp, 0, x0, y, img, &full[s]);
                 if (a_two) tma_load_4d(st + kWtAtom, &mdp, 64, x0, y, img, &full[s]);
-                for (int j = 0; j < nb; ++j)
-                    tma_load_4d(st + (2 + j) * kWtAtom, &mx, 64 * j, x0 + dx, y + dy, img, &full[s]);
+                if (kTaps == 1) {
+                    const int dy = tap0 / 3 - 1, dx = tap0 % 3 - 1;
+                    for (int j = 0; j < nb; ++j)
+                        tma_load_4d(st + (2 + j) * kWtAtom, &mx, 64 * j, x0 + dx, y + dy, img, &full[s]);
+                } else {
+                    for (int t = 0; t < 9; ++t)
+                        tma_load_4d(st + (2 + t) * kWtAtom, &mx, 0, x0 + t % 3 - 1, y + t / 3 - 1, img, &full[s]);
+                }
             }
         }
     } else if (warp == 1) {
@@ -120,9 +131,10 @@ __global__ void __launch_bounds__(kWtThreads) k_conv_wgrad_tma(const __grid_cons
                 }
                 tc_fence_after();
                 const uint32_t sa = smem_u32(smem + s * stage_bytes), sb = sa + 2u * (uint32_t)kWtAtom;
-                for (int kk = 0; kk < kWtK / 16; ++kk)   // 16 pixels (two 8-row groups) per MMA
-                    umma_bf16(tmem, wt_desc(sa + 2048u * kk), wt_desc(sb + 2048u * kk), idesc,
-                              (k | kk) != 0 ? 1u : 0u);
+                for (int t = 0; t < (kTaps == 1 ? 1 : 9); ++t)
+                    for (int kk = 0; kk < kWtK / 16; ++kk)   // 16 pixels (two 8-row groups) per MMA
+                        umma_bf16(tmem + (uint32_t)(t * 32), wt_desc(sa + 2048u * kk),
+                                  wt_desc(sb + (uint32_t)(t * kWtAtom) + 2048u * kk), idesc, (k | kk) != 0 ? 1u : 0u);
                 umma_commit(&empty[s]);
             }
         }
@@ -133,18 +145,19 @@ __global__ void __launch_bounds__(kWtThreads) k_conv_wgrad_tma(const __grid_cons
     __syncwarp();
     tc_fence_after();
     const int r = warp * 32 + lane;   // TMEM lane = cout row
-    for (int c0 = 0; c0 < a.cin; c0 += 16) {
-        uint32_t v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        tmem_ld_wait();
-        if (!ready || r >= a.cout) continue;
-        float* d = a.dw + ((size_t)r * 9 + tap) * a.cin + c0;
+    for (int t = 0; t < (kTaps == 1 ? 1 : 9); ++t)
+        for (int c0 = 0; c0 < a.cin; c0 += 16) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * 32 + c0), v);
+            tmem_ld_wait();
+            if (!ready || r >= a.cout) continue;
+            float* d = a.dw + ((size_t)r * 9 + (kTaps == 1 ? tap0 : t)) * a.cin + c0;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const float f = __uint_as_float(v[j]);
-            if (f != 0.0f) atomicAdd(d + j, f);
+            for (int j = 0; j < 16; ++j) {
+                const float f = __uint_as_float(v[j]);
+                if (f != 0.0f) atomicAdd(d + j, f);
+            }
         }
-    }
     tc_fence_before();
     __syncthreads();
     if (warp == 1) tmem_dealloc(tmem, ncols);
@@ -266,8 +279,8 @@ using namespace gk;
 cudaError_t gkrt_encode_tmap_bf16_sw128(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                         const uint64_t* strides_bytes, const uint32_t* box);
 
-static size_t wgrad_tma_smem(int nb) {
-    return (size_t)kWtStages * (size_t)(2 + nb) * kWtAtom + kWtGuard + 256 + 1024;
+static size_t wgrad_tma_smem(int nbt) {   // nbt: B atoms per stage
+    return (size_t)kWtStages * (size_t)(2 + nbt) * kWtAtom + kWtGuard + 256 + 1024;
 }
 
 cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
@@ -278,7 +291,7 @@ cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
         ((uintptr_t)a.x & 15u) || a.B < 1 || a.H < 1 || a.W < 1)
         return cudaErrorInvalidValue;
     static int sms_dev[kMaxDevices] = {};
-    static bool attr_set[kMaxDevices] = {};   // set once per device for the largest operand (cin = 256)
+    static bool attr_set[kMaxDevices] = {};   // set once per device for the largest stage
     const int dev = current_device_slot();
     if (dev < 0) return cudaErrorInvalidDevice;
     if (!sms_dev[dev]) {
@@ -286,8 +299,11 @@ cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
         if (e != cudaSuccess) return e;
     }
     if (!attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad_tma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)wgrad_tma_smem(4));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_conv_wgrad_tma<9>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)wgrad_tma_smem(9));
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
@@ -302,12 +318,19 @@ cudaError_t gkrt_launch_conv_wgrad(const WgradArgs& a, cudaStream_t st) {
     const uint64_t xs[3] = {(uint64_t)a.x_c * 2, W * a.x_c * 2, H * W * a.x_c * 2};
     if ((e = gkrt_encode_tmap_bf16_sw128(&mx, a.x + a.x_off, 4, xd, xs, box)) != cudaSuccess) return e;
     const int nb = (a.cin + 63) / 64;
-    // about two CTAs per SM over the nine taps, each a run of image rows
     const long long rows = (long long)a.B * a.H;
+    if (a.cin <= 32) {   // all taps per CTA (512 TMEM columns: one CTA per SM), a run of image rows each
+        const long long target = sms_dev[dev];
+        const int rows_per_cta = (int)std::max(1LL, (rows + target - 1) / target);
+        const dim3 grid((unsigned)((rows + rows_per_cta - 1) / rows_per_cta), 1);
+        k_conv_wgrad_tma<9><<<grid, kWtThreads, wgrad_tma_smem(9), st>>>(mdp, mx, a, rows_per_cta, 1);
+        return cudaGetLastError();
+    }
+    // about two CTAs per SM over the nine taps, each a run of image rows
     const long long target = 2LL * sms_dev[dev];
     const int rows_per_cta = (int)std::max(1LL, (rows * 9 + target - 1) / target);
     const dim3 grid((unsigned)((rows + rows_per_cta - 1) / rows_per_cta), 9);
-    k_conv_wgrad_tma<<<grid, kWtThreads, wgrad_tma_smem(nb), st>>>(mdp, mx, a, rows_per_cta, nb);
+    k_conv_wgrad_tma<1><<<grid, kWtThreads, wgrad_tma_smem(nb), st>>>(mdp, mx, a, rows_per_cta, nb);
     return cudaGetLastError();
 }
 
