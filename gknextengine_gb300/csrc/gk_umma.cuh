@@ -37,6 +37,19 @@ __device__ __forceinline__ uint64_t umma_desc_dense(uint32_t saddr, uint32_t lbo
     return d;
 }
 
+// Descriptor of a K-major operand with 32- or 64-byte swizzle: rows of rb bytes (16 or 32
+// bf16 along K), 8-row groups sbo bytes apart (512 / 256 for dense atoms; any multiple of 16).
+// The tensor core applies the swizzle on the absolute address bits, as the TMA does when it
+// writes a box, so the operand may start at any row of a box (base offset 0).
+__device__ __forceinline__ uint64_t umma_desc_swz(uint32_t saddr, uint32_t rb, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1u << 16;                      // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;                      // version
+    d |= (uint64_t)(rb == 64u ? 4u : 6u) << 61;   // SWIZZLE_64B or SWIZZLE_32B
+    return d;
+}
+
 // Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16 (bits 7-9, 10-12 = 1),
 // both K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 __host__ __device__ constexpr uint32_t umma_idesc_bf16(uint32_t M, uint32_t N) {

@@ -874,8 +874,8 @@ cudaError_t gkrt_encode_tmap_2d(CUtensorMap* map, const void* base, uint32_t ele
 }
 
 // cuTensorMapEncodeTiled for bf16 tensors of rank 2..5; zeros outside the tensor. swizzle: 0
-// none (dense boxes), 64 or 128 bytes (the tensor-core kernels' operand layouts; the inner box
-// at most that many bytes).
+// none (dense boxes), 32, 64 or 128 bytes (the tensor-core kernels' operand layouts; the inner
+// box at most that many bytes).
 static cudaError_t encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                     const uint64_t* strides_bytes, const uint32_t* box, int swizzle) {
     typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -891,7 +891,8 @@ static cudaError_t encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t
         fn = (EncodeFn)p;
     }
     if (rank < 2 || rank > 5 || ((uintptr_t)base & 15u) || (box[0] * 2u) % 16u ||
-        (swizzle != 0 && swizzle != 64 && swizzle != 128) || (swizzle && box[0] * 2u > (uint32_t)swizzle))
+        (swizzle != 0 && swizzle != 32 && swizzle != 64 && swizzle != 128) ||
+        (swizzle && box[0] * 2u > (uint32_t)swizzle))
         return cudaErrorInvalidValue;
     cuuint64_t d[5], s[4];
     cuuint32_t b[5], es[5];
@@ -907,8 +908,10 @@ static cudaError_t encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t
     }
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, const_cast<void*>(base), d, s, b, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    swizzle == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
-                                   : (swizzle == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_NONE),
+                    swizzle == 128  ? CU_TENSOR_MAP_SWIZZLE_128B
+                    : swizzle == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                    : swizzle == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                                    : CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -920,6 +923,10 @@ cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t r
 cudaError_t gkrt_encode_tmap_bf16_sw128(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                         const uint64_t* strides_bytes, const uint32_t* box) {
     return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, 128);
+}
+cudaError_t gkrt_encode_tmap_bf16_sw32(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                       const uint64_t* strides_bytes, const uint32_t* box) {
+    return encode_tmap_bf16(map, base, rank, dims, strides_bytes, box, 32);
 }
 cudaError_t gkrt_encode_tmap_bf16_dense(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                         const uint64_t* strides_bytes, const uint32_t* box) {

@@ -83,8 +83,8 @@ constexpr int kConvRelu = 1, kConvF32Out = 2;
 struct ConvArgs {
     int B, H, W, cin, cout;        // cin % 32 == 0; cout % 16 == 0, 16..256 (MMA N)
     int x_c, x_off;                // input: channel stride and first channel (multiple of 8)
-    int x_valid;                   // channels the input holds at x_off (multiple of 8, <= cin; 0: cin);
-                                   // the rest read as zeros
+    int x_valid;                   // channels the input holds at x_off (a multiple of 32 <= cin, or 16
+                                   // for cin == 32 with Cout <= 32; 0: cin); the rest read as zeros
     const float* bias;             // cout floats or null
     void* out;
     int out_c, out_off;            // multiples of 16 (bf16 output)

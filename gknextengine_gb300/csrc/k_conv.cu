@@ -102,15 +102,18 @@ __device__ __forceinline__ void tile_origin(int t, int tiles_x, int tiles_y, int
     x0 = (r % tiles_x) * kTileX;
 }
 
+// kRows: row-box stages (three vertical taps per stage) or one tap per stage. The MMA issuer
+// adds each operand's offset to the descriptors' start fields as a constant.
+template <bool kRows>
 __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant__ CUtensorMap mx,
                                                           const __grid_constant__ CUtensorMap mw, ConvArgs a,
-                                                          int tiles_x, int tiles_y, int ntiles, int stages,
-                                                          int rows) {
+                                                          int tiles_x, int tiles_y, int ntiles, int stages) {
+    constexpr bool rows = kRows;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const int a_bytes = kTileX * (rows ? kTileY + 2 : kTileY) * 64;
     const int b_bytes = a.cout * 64;
-    const int nb = rows ? 3 : 1;   // weight boxes per stage
+    constexpr int nb = rows ? 3 : 1;   // weight boxes per stage
     const int stage_bytes = (a_bytes + nb * b_bytes + 1023) & ~1023;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + stages * stage_bytes);
     uint64_t* empty = full + stages;
@@ -178,6 +181,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
     } else if (warp == 1) {
         if (lane == 0) {   // MMA issuer
             const uint32_t idesc = umma_idesc_bf16(128u, (uint32_t)a.cout);
+            const int b_step = b_bytes >> 4;   // one weight box in 16-byte units
             int kg = 0, i = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
@@ -197,11 +201,14 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t sa = smem_u32(smem + s * stage_bytes), sb = sa + (uint32_t)a_bytes;
+                    const uint32_t sa = smem_u32(smem + s * stage_bytes);
+                    // start fields (16-byte units) stay below 2^14: shared memory < 256 KB
+                    const uint64_t a0 = umma_desc_sw64(sa), b0 = umma_desc_sw64(sa + (uint32_t)a_bytes);
+#pragma unroll
                     for (int dy = 0; dy < nb; ++dy) {
-                        const uint32_t ta = sa + (uint32_t)(dy * kTileX * 64), tb = sb + (uint32_t)(dy * b_bytes);
-                        umma_bf16(d, umma_desc_sw64(ta), umma_desc_sw64(tb), idesc, (k | dy) != 0 ? 1u : 0u);
-                        umma_bf16(d, umma_desc_sw64(ta + 32u), umma_desc_sw64(tb + 32u), idesc, 1u);
+                        const uint64_t ta = a0 + (uint64_t)(dy * kTileX * 4), tb = b0 + (uint64_t)(dy * b_step);
+                        umma_bf16(d, ta, tb, idesc, (k | dy) != 0 ? 1u : 0u);
+                        umma_bf16(d, ta + 2u, tb + 2u, idesc, 1u);
                     }
                     umma_commit(&empty[s]);
                 }
@@ -257,24 +264,38 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
 // Halo tiles: outputs of up to 32 channels whose weights fit in shared memory (the
 // full-resolution layers). Tiles of 8 x 16 pixels (x by y, M = 128). The CTA loads all weights
 // once ({32 Cin, Cout} boxes per tap and input chunk, 64-byte swizzled) and keeps them; per
-// 32-channel input chunk a stage holds the chunk's 10 x 18-pixel halo box as four 8-channel
-// planes without swizzle (180 pixel rows of 16 bytes each, planes 2944 bytes apart: a TMA
-// destination must be 128-byte aligned), so that the A operand of tap (dy, dx) is that box at
-// start offset (10 dy + dx) x 16 bytes: core matrices of 8 pixels (one tile row) are 160 bytes
-// apart, K halves one plane pair apart. Each input chunk is read
-// once per tile (with its halo, 1.4x) instead of three times, and no weights per tile.
+// 32-channel input chunk a stage holds the chunk's 10 x 18-pixel halo box (180 pixel rows), so
+// that the A operand of tap (dy, dx) is that box at start offset (10 dy + dx) rows, 8-row groups
+// (one tile row) 10 rows apart. Each input chunk is read once per tile (with its halo, 1.4x),
+// and no weights per tile. Two layouts of the box, chosen by the input's pixel stride:
+//  * rows (rb = 64, or 32 for an input of 16 channels), when the chunk is the whole pixel: one
+//    TMA box of rb-byte pixel rows in the K-major layout with rb-byte swizzle. The tensor core
+//    applies the swizzle on the absolute shared-memory address bits, as the TMA does when it
+//    writes the box, so an operand may start at any row of it (descriptor base offset 0).
+//  * planes (rb = 16), when the chunk is part of a wider pixel: four 8-channel planes without
+//    swizzle (180 rows of 16 bytes each, planes 2944 bytes apart: a TMA destination must be
+//    128-byte aligned), core matrices of 8 pixels 160 bytes apart, K halves one plane pair apart.
+// Measured on the 1080p denoiser layers (ncu, cold): 32 -> 32 layers 110 -> 95 us with rows;
+// the 96-channel input (192-byte pixels read 64 bytes at a time) 211 us with planes, 281 with
+// rows; the 16-channel input 111 -> 85 us (rows of 32 bytes: half the MMAs).
 
 constexpr int kHaloX = 8, kHaloY = 16;
 constexpr int kHaloBoxX = kHaloX + 2, kHaloBoxY = kHaloY + 2;
-constexpr int kHaloPlane = kHaloBoxX * kHaloBoxY * 16;             // 8 channels: 2880 bytes
+constexpr int kHaloRows = kHaloBoxX * kHaloBoxY;                   // 180 pixel rows
+constexpr int kHaloPlane = kHaloRows * 16;                         // 8 channels: 2880 bytes
 constexpr int kHaloPlaneStride = (kHaloPlane + 127) & ~127;        // 2944
-constexpr int kHaloStage = (4 * kHaloPlaneStride + 1023) & ~1023;  // 32 channels
+constexpr int kHaloStage = (4 * kHaloPlaneStride + 1023) & ~1023;  // 12288 (>= 180 x 64): 1024-byte aligned
 constexpr int kHaloStages = 4;
 constexpr int kHaloWeightMax = 96 * 1024;
 
+// kRb: 16 (planes), 32 or 64 (rows of that many bytes). The MMA issuer's loop over the nine taps
+// is unrolled with the operand offsets as constants added to the descriptors' start fields: with
+// up to 54 MMAs per tile a single issuing thread must not fall behind the tensor core.
+template <int kRb>
 __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_constant__ CUtensorMap mx,
                                                                const __grid_constant__ CUtensorMap mw, ConvArgs a,
                                                                int tiles_x, int tiles_y, int ntiles) {
+    constexpr int rb = kRb;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const int kc = a.cin / 32;
@@ -336,14 +357,21 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                         break;
                     }
                     uint8_t* sa = stage0 + s * kHaloStage;
-                    if (smem_u32(sa) & 127u) {   // every plane starts 128-byte aligned (stride 2944)
+                    if (smem_u32(sa) & 1023u) {   // stages start 1024-byte aligned (weights: 1024-byte boxes)
+                        // (planes then start 128-byte aligned)
                         atomicOr(a.err, kErrTmaWait);
                         *abort_flag = 1;
                         break;
                     }
-                    mbar_expect_tx(&full[s], (uint32_t)(4 * kHaloPlane));
-                    for (int j = 0; j < 4; ++j)
-                        tma_load_4d(sa + j * kHaloPlaneStride, &mx, c * 32 + j * 8, x0 - 1, y0 - 1, img, &full[s]);
+                    if (kRb == 16) {
+                        mbar_expect_tx(&full[s], (uint32_t)(4 * kHaloPlane));
+                        for (int j = 0; j < 4; ++j)
+                            tma_load_4d(sa + j * kHaloPlaneStride, &mx, c * 32 + j * 8, x0 - 1, y0 - 1, img,
+                                        &full[s]);
+                    } else {
+                        mbar_expect_tx(&full[s], (uint32_t)(kHaloRows * rb));
+                        tma_load_4d(sa, &mx, c * 32, x0 - 1, y0 - 1, img, &full[s]);
+                    }
                 }
             }
         }
@@ -354,6 +382,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
             if (!ok) *abort_flag = 1;
             tc_fence_after();
             const uint32_t wb0 = smem_u32(wsm);
+            const int b_step = b_bytes >> 4;   // one tap's weight box in 16-byte units
             int kg = 0, i = 0;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++i) {
                 const int acc = i & 1;
@@ -373,14 +402,20 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                     }
                     tc_fence_after();
                     const uint32_t sa = smem_u32(stage0 + s * kHaloStage);
-                    const uint32_t wb = wb0 + (uint32_t)(9 * c * b_bytes);
+                    // descriptors of the tap-(0, 0) operands; a tap adds its offset (16-byte
+                    // units) to the start field, which stays below 2^14 (shared memory < 256 KB)
+                    const uint64_t a0 = kRb == 16 ? umma_desc_dense(sa, (uint32_t)kHaloPlaneStride, kHaloBoxX * 16u)
+                                                  : umma_desc_swz(sa, (uint32_t)kRb, (uint32_t)(kHaloBoxX * kRb));
+                    const uint64_t b0 = umma_desc_sw64(wb0 + (uint32_t)(9 * c * b_bytes));
+                    constexpr int nkk = kRb == 32 ? 1 : 2;
+#pragma unroll
                     for (int tap = 0; tap < 9; ++tap) {
-                        const uint32_t off = (uint32_t)(((tap / 3) * kHaloBoxX + tap % 3) * 16);
-                        for (int kk = 0; kk < 2; ++kk) {
-                            const uint64_t ad = umma_desc_dense(sa + (uint32_t)(2 * kk * kHaloPlaneStride) + off,
-                                                                (uint32_t)kHaloPlaneStride, (uint32_t)(kHaloBoxX * 16));
-                            const uint64_t bd = umma_desc_sw64(wb + (uint32_t)(tap * b_bytes + kk * 32));
-                            umma_bf16(d, ad, bd, idesc, (c | tap | kk) != 0 ? 1u : 0u);
+                        const int off = ((tap / 3) * kHaloBoxX + tap % 3) * kRb;
+#pragma unroll
+                        for (int kk = 0; kk < nkk; ++kk) {
+                            const int aoff = kRb == 16 ? 2 * kk * kHaloPlaneStride + off : off + kk * 32;
+                            umma_bf16(d, a0 + (uint64_t)(aoff >> 4), b0 + (uint64_t)(tap * b_step + kk * 2), idesc,
+                                      (c | tap | kk) != 0 ? 1u : 0u);
                         }
                     }
                     umma_commit(&empty[s]);
@@ -439,6 +474,8 @@ using namespace gk;
 
 cudaError_t gkrt_encode_tmap_bf16(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                   const uint64_t* strides_bytes, const uint32_t* box);
+cudaError_t gkrt_encode_tmap_bf16_sw32(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
+                                       const uint64_t* strides_bytes, const uint32_t* box);
 cudaError_t gkrt_encode_tmap_bf16_dense(CUtensorMap* map, const void* base, uint32_t rank, const uint64_t* dims,
                                         const uint64_t* strides_bytes, const uint32_t* box);
 
@@ -479,9 +516,13 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         args.H < 1 || args.W < 1 || (!f32 && (args.out_c % 16 || args.out_off % 16)) ||
         args.out_off + (f32 ? args.n_store : args.cout) > args.out_c || (f32 && args.n_store > args.cout) ||
         ((uintptr_t)x & 15u) || ((uintptr_t)w & 15u) || ((uintptr_t)args.out & 15u) || args.x_off % 8 ||
-        args.x_valid < 0 || args.x_valid > args.cin || args.x_valid % 8)
+        args.x_valid < 0 || args.x_valid > args.cin || (args.x_valid % 32 && args.x_valid != 16))
         return cudaErrorInvalidValue;
     const int xv = args.x_valid > 0 ? args.x_valid : args.cin;   // channels present; the rest are zeros
+    // the 32-channel boxes end inside the map, except 16 channels of a 32-channel input (halo
+    // tiles with 32-byte rows)
+    const bool halo = conv_halo(args.cin, args.cout);
+    if (xv % 32 && !(halo && args.cin == 32)) return cudaErrorInvalidValue;
     if (args.x_c > 0 && (args.x_c % 8 || args.x_off + xv > args.x_c)) return cudaErrorInvalidValue;
     if ((args.pool_out || args.up_out) && f32) return cudaErrorInvalidValue;
     if (args.pool_out && (args.pool_c % 8 || args.pool_off % 8 || args.pool_off + args.cout > args.pool_c ||
@@ -504,13 +545,18 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         if (e0 != cudaSuccess) return e0;
     }
     const int sms = sms_dev[dev];
-    if (conv_halo(args.cin, args.cout)) {
-        // channels past xv lie outside the map: TMA fills them with zeros
+    if (halo) {
+        // rows when a chunk is the whole pixel (64 bytes, or 32 for an input of 16 channels),
+        // planes when the pixel is wider than the chunk
+        const int rb = (int)xc * 2 == std::min(xv, 32) * 2 ? (xv == 16 ? 32 : 64) : 16;
+        if (rb == 16 && xv % 32) return cudaErrorInvalidValue;
         const uint64_t xd[4] = {(uint64_t)xv, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
         const uint64_t xs[3] = {xc * 2, (uint64_t)args.W * xc * 2, (uint64_t)args.H * args.W * xc * 2};
-        const uint32_t xb[4] = {8, kHaloBoxX, kHaloBoxY, 1};
+        const uint32_t xb[4] = {(uint32_t)(rb == 16 ? 8 : rb / 2), kHaloBoxX, kHaloBoxY, 1};
         const void* xbase = static_cast<const uint8_t*>(x) + (size_t)args.x_off * 2;
-        cudaError_t e = gkrt_encode_tmap_bf16_dense(&mx, xbase, 4, xd, xs, xb);
+        cudaError_t e = rb == 64   ? gkrt_encode_tmap_bf16(&mx, xbase, 4, xd, xs, xb)
+                        : rb == 32 ? gkrt_encode_tmap_bf16_sw32(&mx, xbase, 4, xd, xs, xb)
+                                   : gkrt_encode_tmap_bf16_dense(&mx, xbase, 4, xd, xs, xb);
         if (e != cudaSuccess) return e;
         const uint64_t wd[2] = {(uint64_t)9 * args.cin, (uint64_t)args.cout};
         const uint64_t ws[1] = {(uint64_t)9 * args.cin * 2};
@@ -519,12 +565,14 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         const size_t smem = conv_halo_smem(args.cin, args.cout);
         if (!halo_attr[dev]) {
             const int mx_smem = (int)(kHaloWeightMax + kHaloStages * kHaloStage + 4096);
-            if ((e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, mx_smem)) !=
-                cudaSuccess)
-                return e;
-            if ((e = cudaFuncSetAttribute(k_conv3x3_halo, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                          (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
-                return e;
+            for (const void* f : {(const void*)k_conv3x3_halo<16>, (const void*)k_conv3x3_halo<32>,
+                                  (const void*)k_conv3x3_halo<64>}) {
+                if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, mx_smem)) != cudaSuccess)
+                    return e;
+                if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                              (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
+                    return e;
+            }
             halo_attr[dev] = true;
         }
         const int ncols = 2 * (args.cout <= 32 ? 32 : 64);
@@ -533,7 +581,12 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         const int tiles_x = (args.W + kHaloX - 1) / kHaloX, tiles_y = (args.H + kHaloY - 1) / kHaloY;
         const int ntiles = tiles_x * tiles_y * args.B;
         const int grid = std::min(ntiles, sms * per_sm);
-        k_conv3x3_halo<<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles);
+        if (rb == 64)
+            k_conv3x3_halo<64><<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles);
+        else if (rb == 32)
+            k_conv3x3_halo<32><<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles);
+        else
+            k_conv3x3_halo<16><<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles);
         return cudaGetLastError();
     }
     const uint64_t xd[4] = {(uint64_t)xv, (uint64_t)args.W, (uint64_t)args.H, (uint64_t)args.B};
@@ -552,12 +605,14 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     // launch geometry per output width, computed once per device (host calls kept off the
     // per-launch path)
     if (smem > smem_set[dev]) {
-        if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)conv_smem_max())) !=
-            cudaSuccess)
-            return e;
-        if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                      (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
-            return e;
+        for (const void* f : {(const void*)k_conv3x3<true>, (const void*)k_conv3x3<false>}) {
+            if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)conv_smem_max())) !=
+                cudaSuccess)
+                return e;
+            if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          (int)cudaSharedmemCarveoutMaxShared)) != cudaSuccess)
+                return e;
+        }
         smem_set[dev] = conv_smem_max();
     }
     int per_sm = per_sm_cache[dev][args.cout];
@@ -572,7 +627,10 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     const int tiles_x = (args.W + kTileX - 1) / kTileX, tiles_y = (args.H + kTileY - 1) / kTileY;
     const int ntiles = tiles_x * tiles_y * args.B;
     const int grid = std::min(ntiles, sms * per_sm);
-    k_conv3x3<<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles, conv_stages(args.cout),
-                                                rows ? 1 : 0);
+    if (rows)
+        k_conv3x3<true><<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles, conv_stages(args.cout));
+    else
+        k_conv3x3<false><<<grid, kConvThreads, smem, st>>>(mx, mw, args, tiles_x, tiles_y, ntiles,
+                                                           conv_stages(args.cout));
     return cudaGetLastError();
 }
