@@ -58,24 +58,56 @@ __device__ __forceinline__ void store_bf16x16(__nv_bfloat16* dst, const float* v
                       pack_bf16x2(v[14], v[15]));
 }
 
+// Shared memory of the bf16 epilogue: 1 KB per epilogue warp (16-byte aligned).
+constexpr int kEpiBuf = 4 * 1024 + 16;
+
+__device__ __forceinline__ size_t shfl_size(size_t v, int src) {
+    const uint32_t lo = __shfl_sync(0xFFFFFFFFu, (uint32_t)v, src);
+    const uint32_t hi = __shfl_sync(0xFFFFFFFFu, (uint32_t)((uint64_t)v >> 32), src);
+    return (size_t)(((uint64_t)hi << 32) | lo);
+}
+
 // The bf16 epilogue of 16 channels (c0 .. c0 + 15) of pixel (x, y) of image img: the plain
 // store, and the optional pooled and upsampled outputs. Called by every lane of the warp
 // (the pool's 2 x 2 block is four lanes of one warp: x-neighbour lane ^ 1, y-neighbour lane ^
 // yl); the pooled average is ((v(x, y) + v(x + 1, y)) + v(x, y + 1)) + v(x + 1, y + 1) of the
-// stored (bf16-rounded) values, times 1/4, rounded to bf16.
+// stored (bf16-rounded) values, times 1/4, rounded to bf16. The warp's 32 pixels pass their
+// 32 bytes through ebuf (this warp's 1 KB of shared memory; 16-byte chunks swizzled by lane bit
+// 2, so that neither side has bank conflicts), and each 32-byte sector of the output is then
+// written whole by two lanes of one store instruction: lane-per-pixel stores wrote every sector
+// in two 16-byte halves from separate instructions, twice the L2 write requests.
 __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float* v, int img, int x, int y, bool inside,
-                                              int c0, int yl) {
+                                              int c0, int yl, uint4* ebuf) {
+    const int lane = threadIdx.x & 31;
     const size_t pix = ((size_t)img * a.H + y) * a.W + x;
-    if (inside) store_bf16x16(reinterpret_cast<__nv_bfloat16*>(a.out) + pix * a.out_c + a.out_off + c0, v);
-    if (a.up_out && inside) {
-        __nv_bfloat16* up = reinterpret_cast<__nv_bfloat16*>(a.up_out);
-        const size_t W2 = 2 * (size_t)a.W;
-        const size_t q = ((size_t)img * 2 * a.H + 2 * (size_t)y) * W2 + 2 * (size_t)x;
-        for (int k = 0; k < 4; ++k)
-            store_bf16x16(up + (q + (k >> 1) * W2 + (k & 1)) * a.up_c + a.up_off + c0, v);
+    const int sw = (lane >> 2) & 1;
+    ebuf[2 * lane + sw] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
+                                     pack_bf16x2(v[6], v[7]));
+    ebuf[2 * lane + (sw ^ 1)] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]),
+                                           pack_bf16x2(v[12], v[13]), pack_bf16x2(v[14], v[15]));
+    __syncwarp();
+    const size_t W2 = 2 * (size_t)a.W;
+    const size_t uq = ((size_t)img * 2 * a.H + 2 * (size_t)y) * W2 + 2 * (size_t)x;
+    const int h = lane & 1;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const int src = (lane >> 1) + 16 * i;
+        const uint4 val = ebuf[2 * src + (h ^ ((src >> 2) & 1))];
+        const size_t spix = shfl_size(pix, src);
+        const bool sin = __shfl_sync(0xFFFFFFFFu, inside ? 1 : 0, src) != 0;
+        if (sin)
+            *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + spix * a.out_c + a.out_off + c0 +
+                                      8 * h) = val;
+        if (a.up_out) {
+            const size_t sq = shfl_size(uq, src);
+            __nv_bfloat16* up = reinterpret_cast<__nv_bfloat16*>(a.up_out) + a.up_off + c0 + 8 * h;
+            if (sin)
+                for (int k = 0; k < 4; ++k)
+                    *reinterpret_cast<uint4*>(up + (sq + (k >> 1) * W2 + (k & 1)) * a.up_c) = val;
+        }
     }
+    __syncwarp();   // the next group rewrites ebuf
     if (a.pool_out) {
-        const int lane = threadIdx.x & 31;
         float s[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -122,6 +154,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
     uint64_t* fin = acce + 2;          // every MMA of this CTA completed
     uint32_t* tslot = reinterpret_cast<uint32_t*>(fin + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+    uint4* ebuf = reinterpret_cast<uint4*>((reinterpret_cast<uintptr_t>(tslot + 2) + 15) & ~(uintptr_t)15);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int kc = a.cin / 32, nk = (rows ? 3 : 9) * kc;
@@ -249,7 +282,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                     float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
                     for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
                 } else {
-                    epilogue_bf16(a, v, img, x, y, inside, c0, 16);   // y-neighbour: lane ^ 16 (16-pixel rows)
+                    // y-neighbour: lane ^ 16 (16-pixel rows)
+                    epilogue_bf16(a, v, img, x, y, inside, c0, 16, ebuf + 64 * q);
                 }
             }
             tc_fence_before();
@@ -311,6 +345,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
     uint64_t* fin = acce + 2;
     uint32_t* tslot = reinterpret_cast<uint32_t*>(fin + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+    uint4* ebuf = reinterpret_cast<uint4*>((reinterpret_cast<uintptr_t>(tslot + 2) + 15) & ~(uintptr_t)15);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t ncols1 = a.cout <= 32 ? 32u : 64u;
@@ -455,7 +490,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                     float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
                     for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
                 } else {
-                    epilogue_bf16(a, v, img, x, y, inside, c0, 8);   // y-neighbour: lane ^ 8 (8-pixel rows)
+                    // y-neighbour: lane ^ 8 (8-pixel rows)
+                    epilogue_bf16(a, v, img, x, y, inside, c0, 8, ebuf + 64 * q);
                 }
             }
             tc_fence_before();
@@ -485,7 +521,7 @@ cudaError_t gkrt_encode_tmap_bf16_dense(CUtensorMap* map, const void* base, uint
 // (the 64 -> 64 layers then run one CTA per SM behind 72 KB of weights).
 static bool conv_halo(int cin, int cout) { return cout <= 32 && 9 * cin * cout * 2 <= kHaloWeightMax; }
 static size_t conv_halo_smem(int cin, int cout) {
-    return (size_t)9 * cin * cout * 2 + kHaloStages * kHaloStage + (2 * kHaloStages + 6) * 8 + 8 + 1024;
+    return (size_t)9 * cin * cout * 2 + kHaloStages * kHaloStage + (2 * kHaloStages + 6) * 8 + 8 + kEpiBuf + 1024;
 }
 
 // Outputs of up to 128 channels use the row-box stages (three vertical taps per box); the
@@ -501,7 +537,7 @@ static int conv_stages(int cout) { return conv_rows(cout) ? 3 : 4; }
 size_t gkrt_conv_smem_bytes(int cout) {
     const bool rows = conv_rows(cout);
     const int stage = (kTileX * (rows ? kTileY + 2 : kTileY) * 64 + (rows ? 3 : 1) * cout * 64 + 1023) & ~1023;
-    return (size_t)conv_stages(cout) * stage + 2 * conv_stages(cout) * 8 + 5 * 8 + 8 + 1024;
+    return (size_t)conv_stages(cout) * stage + 2 * conv_stages(cout) * 8 + 5 * 8 + 8 + kEpiBuf + 1024;
 }
 
 static size_t conv_smem_max() {
@@ -564,7 +600,7 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
         if ((e = gkrt_encode_tmap_bf16(&mw, w, 2, wd, ws, wb)) != cudaSuccess) return e;
         const size_t smem = conv_halo_smem(args.cin, args.cout);
         if (!halo_attr[dev]) {
-            const int mx_smem = (int)(kHaloWeightMax + kHaloStages * kHaloStage + 4096);
+            const int mx_smem = (int)(kHaloWeightMax + kHaloStages * kHaloStage + 2048 + kEpiBuf);
             for (const void* f : {(const void*)k_conv3x3_halo<16>, (const void*)k_conv3x3_halo<32>,
                                   (const void*)k_conv3x3_halo<64>}) {
                 if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, mx_smem)) != cudaSuccess)
