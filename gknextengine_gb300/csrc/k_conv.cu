@@ -118,12 +118,41 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float* v,
             s[j] = (((0.0f + own) + nx) + ny) + nxy;
             s[j] *= 0.25f;
         }
+        // the block's top-left lane (even x, even y: lane bits 0 and log2(yl) clear) owns the
+        // average; the warp's 8 owners pass it through ebuf, and 16 lanes store 8 whole sectors
         const int h2 = a.H / 2, w2 = a.W / 2;
-        if (!(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2 && (lane & 1) == 0 && (lane & yl) == 0) {
-            const size_t pp = ((size_t)img * h2 + y / 2) * w2 + x / 2;
-            store_bf16x16(reinterpret_cast<__nv_bfloat16*>(a.pool_out) + pp * a.pool_c + a.pool_off + c0, s);
+        const int b = yl == 16 ? 4 : 3;
+        const bool owner = (lane & 1) == 0 && (lane & yl) == 0;
+        const int k = ((lane >> (b + 1)) << (b - 1)) | ((lane & (yl - 1)) >> 1);
+        const size_t pp = ((size_t)img * h2 + y / 2) * w2 + x / 2;
+        const bool pvalid = owner && !(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2;
+        if (owner) {
+            const int ks = (k >> 2) & 1;
+            ebuf[2 * k + ks] = make_uint4(pack_bf16x2(s[0], s[1]), pack_bf16x2(s[2], s[3]), pack_bf16x2(s[4], s[5]),
+                                          pack_bf16x2(s[6], s[7]));
+            ebuf[2 * k + (ks ^ 1)] = make_uint4(pack_bf16x2(s[8], s[9]), pack_bf16x2(s[10], s[11]),
+                                                pack_bf16x2(s[12], s[13]), pack_bf16x2(s[14], s[15]));
         }
+        __syncwarp();
+        const int src = (lane >> 1) & 7;   // lanes 0-15 store; the source owner's lane:
+        const int src_lane = ((src >> (b - 1)) << (b + 1)) | ((src & ((1 << (b - 1)) - 1)) << 1);
+        const size_t spp = shfl_size(pp, src_lane);
+        const bool sv = __shfl_sync(0xFFFFFFFFu, pvalid ? 1 : 0, src_lane) != 0;
+        if (lane < 16 && sv) {
+            const uint4 val = ebuf[2 * src + (h ^ ((src >> 2) & 1))];
+            *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.pool_out) + spp * a.pool_c + a.pool_off +
+                                      c0 + 8 * h) = val;
+        }
+        __syncwarp();
     }
+}
+
+// fp32 output of channels c0 .. c0 + n - 1 (n <= 16) at o: 16-byte stores where o allows.
+__device__ __forceinline__ void store_f32(float* o, const float* v, int n) {
+    int j = 0;
+    if (!(reinterpret_cast<uintptr_t>(o) & 15u))
+        for (; j + 4 <= n; j += 4) *reinterpret_cast<float4*>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+    for (; j < n; ++j) o[j] = v[j];
 }
 
 __device__ __forceinline__ void tile_origin(int t, int tiles_x, int tiles_y, int& x0, int& y0, int& img) {
@@ -279,8 +308,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                 }
                 if (a.flags & kConvF32Out) {
                     if (!inside) continue;
-                    float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
-                    for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
+                    store_f32(reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0, v,
+                              min(16, a.n_store - c0));
                 } else {
                     // y-neighbour: lane ^ 16 (16-pixel rows)
                     epilogue_bf16(a, v, img, x, y, inside, c0, 16, ebuf + 64 * q);
@@ -487,8 +516,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                 }
                 if (a.flags & kConvF32Out) {
                     if (!inside) continue;
-                    float* o = reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0;
-                    for (int j = 0; j < 16 && c0 + j < a.n_store; ++j) o[j] = v[j];
+                    store_f32(reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0, v,
+                              min(16, a.n_store - c0));
                 } else {
                     // y-neighbour: lane ^ 8 (8-pixel rows)
                     epilogue_bf16(a, v, img, x, y, inside, c0, 8, ebuf + 64 * q);

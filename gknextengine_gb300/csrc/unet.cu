@@ -3,7 +3,10 @@
 // denoiser is the closed OIDN library, PathTracingRenderer.cpp:33-64, 234-269).
 //
 // Inputs, 10 channels per pixel: 1-spp linear radiance (as log(1 + x)), albedo, normal,
-// depth (NDC, clamped to [0, 1]: camera misses carry 100000); padded with zeros to 32 channels. Output: log(1 + radiance), 3 channels.
+// depth (NDC, clamped to [0, 1]: camera misses carry 100000); stored as 16 channels (zeros
+// after the 10), the first layer reads 32 (the rest as zeros). Output: log(1 + radiance), 3
+// channels, stored with a fourth (an unused network output) so that each pixel is one 16-byte
+// store.
 //   level 0 (full)   enc0a 32->32, enc0b 32->32 ............ dec0a 96->32, dec0b 32->32, out 32->3
 //   level 1 (1/2)    enc1a 32->64, enc1b 64->64 ............ dec1a 160->64, dec1b 64->64
 //   level 2 (1/4)    enc2a 64->96, enc2b 96->96 ............ dec2a 224->96, dec2b 96->96
@@ -34,7 +37,7 @@ struct LayerDef {
 constexpr LayerDef kLayers[kUnetLayers] = {
     {32, 32, 1, 32},   {32, 32, 1, 32},   {32, 64, 1, 64},  {64, 64, 1, 64},  {64, 96, 1, 96},
     {96, 96, 1, 96},   {96, 128, 1, 128}, {128, 128, 1, 128}, {224, 96, 1, 96}, {96, 96, 1, 96},
-    {160, 64, 1, 64},  {64, 64, 1, 64},   {96, 32, 1, 32},  {32, 32, 1, 32},  {32, 32, 0, 3}};
+    {160, 64, 1, 64},  {64, 64, 1, 64},   {96, 32, 1, 32},  {32, 32, 1, 32},  {32, 32, 0, 4}};
 enum { E0A, E0B, E1A, E1B, E2A, E2B, E3A, E3B, D2A, D2B, D1A, D1B, D0A, D0B, OUT };
 
 // The network input x0: kXc channels per pixel (the 10 inputs, then zeros); the first layer's

@@ -495,7 +495,8 @@ int  gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t 
  * 1-spp linear radiance rgb, albedo rgb, normal xyz, NDC depth (clamped to [0, 1]); target:
  * [..][3] linear radiance.
  * out_linear: [..][4] denoised linear radiance (w = 1); out_raw: [..][4] the network's
- * log(1 + radiance) output, the quantity gkrt_unet_backward's d_raw differentiates. Sizes
+ * log(1 + radiance) output in x, y, z (w: an unused fourth output), the quantity
+ * gkrt_unet_backward's d_raw differentiates (its w is ignored). Sizes
  * are multiples of 8 from 16 to 8192, batch 1..64. Parameters: gkrt_unet_param_count floats,
  * per layer the weights [cout][3][3][cin] then the biases; set_params resets Adam's state.
  * The denoise pass uses it with GKRT_DENOISE_UNET. */
