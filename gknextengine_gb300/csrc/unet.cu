@@ -44,51 +44,76 @@ enum { E0A, E0B, E1A, E1B, E2A, E2B, E3A, E3B, D2A, D2B, D1A, D1B, D0A, D0B, OUT
 // 32 input channels read the ones past kXc as zeros (its tensor map ends there).
 constexpr int kXc = 16;
 
-__global__ void k_pack_input(const float* in, long long npix, __nv_bfloat16* x0) {
-    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;   // one pixel
-    if (p >= npix) return;
+// 256 pixels per block: their 10 KB of input are read as whole 16-byte words into shared
+// memory (pixel-per-thread loads of 40-byte records touch every line ten times).
+__global__ void __launch_bounds__(256) k_pack_input(const float* in, long long npix, __nv_bfloat16* x0) {
+    __shared__ __align__(16) float rec[256 * 10];
+    const long long p0 = blockIdx.x * 256LL;
+    const int n = (int)(npix - p0 < 256 ? npix - p0 : 256);
+    const float* src = in + p0 * 10;
+    if (n == 256 && !(reinterpret_cast<uintptr_t>(src) & 15u)) {
+        for (int i = threadIdx.x; i < 640; i += 256)
+            reinterpret_cast<float4*>(rec)[i] = __ldcs(reinterpret_cast<const float4*>(src) + i);
+    } else {
+        for (int i = threadIdx.x; i < n * 10; i += 256) rec[i] = src[i];
+    }
+    __syncthreads();
     float v[kXc];
 #pragma unroll
     for (int c = 0; c < kXc; ++c) v[c] = 0.0f;
+    if ((int)threadIdx.x < n) {   // one pixel
 #pragma unroll
-    for (int c = 0; c < 10; ++c) v[c] = in[p * 10 + c];
+        for (int c = 0; c < 10; ++c) v[c] = rec[threadIdx.x * 10 + c];
+    }
 #pragma unroll
     for (int c = 0; c < 3; ++c) v[c] = log1pf(fmaxf(v[c], 0.0f));
     v[9] = fminf(fmaxf(v[9], 0.0f), 1.0f);   // depth; misses carry 100000
-    uint4* o = reinterpret_cast<uint4*>(x0 + p * kXc);
+    __syncthreads();   // rec now holds the packed pixels (32 bytes each), stored as whole lines
+    uint4* packed = reinterpret_cast<uint4*>(rec);
 #pragma unroll
     for (int k = 0; k < kXc / 8; ++k) {
         __nv_bfloat162 h[4];
         for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(v[8 * k + 2 * j], v[8 * k + 2 * j + 1]);
-        o[k] = *reinterpret_cast<uint4*>(h);
+        packed[threadIdx.x * (kXc / 8) + k] = *reinterpret_cast<uint4*>(h);
     }
+    __syncthreads();
+    uint4* o = reinterpret_cast<uint4*>(x0 + p0 * kXc);
+    for (int i = threadIdx.x; i < n * (kXc / 8); i += 256) o[i] = packed[i];
 }
 
 // From the pass's images (pitched float4 / float): composed 1-spp radiance
 // (diffuse x albedo + specular), albedo, normal, depth.
-__global__ void k_pack_frame(const float4* sd, const float4* ss, const float4* alb, const float4* nrm,
-                             const float* depth, int W, int H, int P, __nv_bfloat16* x0) {
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= (long long)W * H) return;
-    const int x = (int)(i % W), y = (int)(i / W);
-    const size_t q = (size_t)y * P + x;
-    const float4 d = sd[q], s = ss[q], a = alb[q], n = nrm[q];
+// (256 pixels per block, their packed 32-byte records stored as whole lines through shared memory)
+__global__ void __launch_bounds__(256) k_pack_frame(const float4* sd, const float4* ss, const float4* alb,
+                                                    const float4* nrm, const float* depth, int W, int H, int P,
+                                                    __nv_bfloat16* x0) {
+    __shared__ __align__(16) uint4 packed[256 * (kXc / 8)];
+    const long long i0 = blockIdx.x * 256LL, i = i0 + threadIdx.x;
+    const long long npix = (long long)W * H;
+    const int n = (int)(npix - i0 < 256 ? npix - i0 : 256);
     float v[kXc];
 #pragma unroll
     for (int c = 0; c < kXc; ++c) v[c] = 0.0f;
-    v[0] = log1pf(fmaxf(fmaf(d.x, a.x, s.x), 0.0f));
-    v[1] = log1pf(fmaxf(fmaf(d.y, a.y, s.y), 0.0f));
-    v[2] = log1pf(fmaxf(fmaf(d.z, a.z, s.z), 0.0f));
-    v[3] = a.x; v[4] = a.y; v[5] = a.z;
-    v[6] = n.x; v[7] = n.y; v[8] = n.z;
-    v[9] = fminf(fmaxf(depth[q], 0.0f), 1.0f);   // misses carry 100000
-    uint4* o = reinterpret_cast<uint4*>(x0 + i * kXc);
+    if (i < npix) {
+        const int x = (int)(i % W), y = (int)(i / W);
+        const size_t q = (size_t)y * P + x;
+        const float4 d = sd[q], s = ss[q], a = alb[q], n4 = nrm[q];
+        v[0] = log1pf(fmaxf(fmaf(d.x, a.x, s.x), 0.0f));
+        v[1] = log1pf(fmaxf(fmaf(d.y, a.y, s.y), 0.0f));
+        v[2] = log1pf(fmaxf(fmaf(d.z, a.z, s.z), 0.0f));
+        v[3] = a.x; v[4] = a.y; v[5] = a.z;
+        v[6] = n4.x; v[7] = n4.y; v[8] = n4.z;
+        v[9] = fminf(fmaxf(depth[q], 0.0f), 1.0f);   // misses carry 100000
+    }
 #pragma unroll
     for (int k = 0; k < kXc / 8; ++k) {
         __nv_bfloat162 h[4];
         for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(v[8 * k + 2 * j], v[8 * k + 2 * j + 1]);
-        o[k] = *reinterpret_cast<uint4*>(h);
+        packed[threadIdx.x * (kXc / 8) + k] = *reinterpret_cast<uint4*>(h);
     }
+    __syncthreads();
+    uint4* o = reinterpret_cast<uint4*>(x0 + i0 * kXc);
+    for (int j = threadIdx.x; j < n * (kXc / 8); j += 256) o[j] = packed[j];
 }
 
 // gradient of the loss in log space; loss sum in FP64
