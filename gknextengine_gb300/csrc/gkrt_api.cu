@@ -1789,11 +1789,13 @@ int gkrt_adjoint_backward(GkrtContext* ctx, const GkrtFrameConstants* fc, uint32
     return GKRT_OK;
 }
 
-int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin, const void* w,
-                      const float* bias, uint32_t cout, void* y, uint32_t y_channels, uint32_t y_offset,
-                      uint32_t y_store, uint32_t flags, void* stream) {
+static int conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin, const void* w,
+                        const float* bias, uint32_t cout, void* y, uint32_t y_channels, uint32_t y_offset,
+                        uint32_t y_store, uint32_t flags, void* pool, uint32_t pool_channels, uint32_t pool_offset,
+                        void* up, uint32_t up_channels, uint32_t up_offset, void* stream) {
     if (!x || !w || !y || batch == 0 || height == 0 || width == 0 || batch > 65535 || height > 65535 ||
-        width > 65535 || cin > 4096 || flags > 3u)
+        width > 65535 || cin > 4096 || flags > 3u || pool_channels > 4096 || pool_offset > 4096 ||
+        up_channels > 4096 || up_offset > 4096)
         return GKRT_ERR_INVALID_ARG;
     ConvArgs a{};
     a.B = (int)batch; a.H = (int)height; a.W = (int)width; a.cin = (int)cin; a.cout = (int)cout;
@@ -1804,12 +1806,30 @@ int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t w
     a.out_off = (int)y_offset;
     a.n_store = (int)y_store;
     a.flags = (int)flags;
+    a.pool_out = pool; a.pool_c = (int)pool_channels; a.pool_off = (int)pool_offset;
+    a.up_out = up; a.up_c = (int)up_channels; a.up_off = (int)up_offset;
     uint32_t* d_err = standalone_err_word();   // the standalone kernels' error word (this device's)
     if (!d_err) return GKRT_ERR_OOM;
     a.err = d_err;
     cudaError_t e = gkrt_launch_conv3x3(x, w, a, (cudaStream_t)stream);
     if (e == cudaErrorInvalidValue) return GKRT_ERR_INVALID_ARG;
     return e == cudaSuccess ? GKRT_OK : GKRT_ERR_CUDA;
+}
+
+int gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin, const void* w,
+                      const float* bias, uint32_t cout, void* y, uint32_t y_channels, uint32_t y_offset,
+                      uint32_t y_store, uint32_t flags, void* stream) {
+    return conv3x3_bf16(x, batch, height, width, cin, w, bias, cout, y, y_channels, y_offset, y_store, flags, nullptr,
+                        0, 0, nullptr, 0, 0, stream);
+}
+
+int gkrt_conv3x3_bf16_fused(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin,
+                            const void* w, const float* bias, uint32_t cout, void* y, uint32_t y_channels,
+                            uint32_t y_offset, uint32_t flags, void* pool, uint32_t pool_channels,
+                            uint32_t pool_offset, void* up, uint32_t up_channels, uint32_t up_offset, void* stream) {
+    if (flags & GKRT_CONV_F32) return GKRT_ERR_INVALID_ARG;
+    return conv3x3_bf16(x, batch, height, width, cin, w, bias, cout, y, y_channels, y_offset, 0, flags, pool,
+                        pool_channels, pool_offset, up, up_channels, up_offset, stream);
 }
 
 // ---- learned denoiser ----

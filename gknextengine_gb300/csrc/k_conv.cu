@@ -70,8 +70,8 @@ __device__ __forceinline__ size_t shfl_size(size_t v, int src) {
 // The bf16 epilogue of 16 channels (c0 .. c0 + 15) of pixel (x, y) of image img: the plain
 // store, and the optional pooled and upsampled outputs. Called by every lane of the warp
 // (the pool's 2 x 2 block is four lanes of one warp: x-neighbour lane ^ 1, y-neighbour lane ^
-// yl); the pooled average is ((v(x, y) + v(x + 1, y)) + v(x, y + 1)) + v(x + 1, y + 1) of the
-// stored (bf16-rounded) values, times 1/4, rounded to bf16. The warp's 32 pixels pass their
+// yl); the pooled average is (((0 + v(x, y)) + v(x + 1, y)) + v(x, y + 1)) + v(x + 1, y + 1) of
+// the stored (bf16-rounded) values, times 1/4, rounded to bf16. The warp's 32 pixels pass their
 // 32 bytes through ebuf (this warp's 1 KB of shared memory; 16-byte chunks swizzled by lane bit
 // 2, so that neither side has bank conflicts), and each 32-byte sector of the output is then
 // written whole by two lanes of one store instruction: lane-per-pixel stores wrote every sector
@@ -108,21 +108,31 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float* v,
     }
     __syncwarp();   // the next group rewrites ebuf
     if (a.pool_out) {
-        float s[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const float own = __bfloat162float(__float2bfloat16_rn(v[j]));
-            const float nx = __shfl_xor_sync(0xFFFFFFFFu, own, 1);
-            const float ny = __shfl_xor_sync(0xFFFFFFFFu, own, yl);
-            const float nxy = __shfl_xor_sync(0xFFFFFFFFu, own, yl ^ 1);
-            s[j] = (((0.0f + own) + nx) + ny) + nxy;
-            s[j] *= 0.25f;
-        }
         // the block's top-left lane (even x, even y: lane bits 0 and log2(yl) clear) owns the
-        // average; the warp's 8 owners pass it through ebuf, and 16 lanes store 8 whole sectors
+        // average; it reads the block's four stored values from ebuf, and the warp's 8 owners
+        // pass the averages back through ebuf, where 16 lanes store 8 whole sectors
         const int h2 = a.H / 2, w2 = a.W / 2;
         const int b = yl == 16 ? 4 : 3;
         const bool owner = (lane & 1) == 0 && (lane & yl) == 0;
+        float s[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) s[j] = 0.0f;
+        if (owner) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {   // own, x-neighbour, y-neighbour, diagonal
+                const int nl = lane ^ (t & 1) ^ (t & 2 ? yl : 0), ns = (nl >> 2) & 1;
+                const uint4 lo = ebuf[2 * nl + ns], hi = ebuf[2 * nl + (ns ^ 1)];
+                const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    s[2 * j] = s[2 * j] + __uint_as_float(w[j] << 16);
+                    s[2 * j + 1] = s[2 * j + 1] + __uint_as_float(w[j] & 0xFFFF0000u);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) s[j] *= 0.25f;
+        }
+        __syncwarp();   // the block values are read before the averages overwrite ebuf
         const int k = ((lane >> (b + 1)) << (b - 1)) | ((lane & (yl - 1)) >> 1);
         const size_t pp = ((size_t)img * h2 + y / 2) * w2 + x / 2;
         const bool pvalid = owner && !(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2;

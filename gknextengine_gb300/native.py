@@ -69,6 +69,9 @@ def load(path: str | None = None):
     L.gkrt_affine_inverse.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.gkrt_conv3x3_bf16.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp,
                                     C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp]
+    L.gkrt_conv3x3_bf16_fused.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32,
+                                          vp, C.c_uint32, C.c_uint32, C.c_uint32, vp, C.c_uint32, C.c_uint32, vp,
+                                          C.c_uint32, C.c_uint32, vp]
     L.gkrt_conv3x3_wgrad_bf16.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp]
     L.gkrt_unet_init.argtypes = [vp, C.c_uint64]
     L.gkrt_unet_param_count.argtypes = [vp, C.POINTER(C.c_uint32)]
@@ -103,7 +106,8 @@ EXPORTED = [
     "gkrt_texture_upload",
     "gkrt_get_stats", "gkrt_get_pass_times", "gkrt_probe_voxelize", "gkrt_probe_bake", "gkrt_probe_download",
     "gkrt_synchronize", "gkrt_affine_inverse",
-    "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16", "gkrt_conv3x3_wgrad_bf16",
+    "gkrt_set_material_params", "gkrt_adjoint_forward", "gkrt_adjoint_backward", "gkrt_conv3x3_bf16", "gkrt_conv3x3_bf16_fused",
+    "gkrt_conv3x3_wgrad_bf16",
     "gkrt_unet_init", "gkrt_unet_param_count", "gkrt_unet_get_params", "gkrt_unet_set_params", "gkrt_unet_get_state", "gkrt_unet_set_state", "gkrt_unet_forward",
     "gkrt_unet_backward", "gkrt_unet_zero_grad", "gkrt_unet_train_step",
 ]

@@ -487,6 +487,16 @@ int  gkrt_conv3x3_wgrad_bf16(const void* dy, const void* x, uint32_t batch, uint
 int  gkrt_conv3x3_bf16(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin,
                        const void* w, const float* bias, uint32_t cout, void* y, uint32_t y_channels,
                        uint32_t y_offset, uint32_t y_store, uint32_t flags, void* stream);
+/* The same convolution (bf16 output) with the two extra outputs its epilogue can write, as the
+ * denoiser's skip tensors use them (either pointer may be null): pool, NHWC bf16 at
+ * (height / 2) x (width / 2) with pool_channels channels, at pool_offset the 2x2 average
+ * (((0 + y00) + y01) + y10) + y11, times 1/4, of the stored bf16 outputs; up, NHWC bf16 at
+ * (2 height) x (2 width) with up_channels channels, at up_offset each output repeated over its
+ * 2x2 block (nearest upsampling). Channel counts and offsets multiples of 8. */
+int  gkrt_conv3x3_bf16_fused(const void* x, uint32_t batch, uint32_t height, uint32_t width, uint32_t cin,
+                             const void* w, const float* bias, uint32_t cout, void* y, uint32_t y_channels,
+                             uint32_t y_offset, uint32_t flags, void* pool, uint32_t pool_channels,
+                             uint32_t pool_offset, void* up, uint32_t up_channels, uint32_t up_offset, void* stream);
 
 /* Learned denoiser (no counterpart in the reference, whose learned denoiser is the closed
  * OIDN library): a 4-level 3x3-convolution U-Net (32/64/96/128 channels) in bf16 with FP32

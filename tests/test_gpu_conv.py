@@ -54,6 +54,41 @@ def test_conv_matches_torch(B, H, W, cin, cout, relu):
     assert bool((out[..., :off].float() == 7.0).all()) and bool((out[..., off + cout:].float() == 7.0).all())
 
 
+@pytest.mark.parametrize("B,H,W,cin,cout", [(2, 37, 45, 32, 32), (1, 19, 23, 96, 32), (1, 24, 40, 64, 64),
+                                            (2, 17, 33, 32, 48)])
+def test_conv_fused_pool_and_upsample(B, H, W, cin, cout):
+    """The epilogue's extra outputs (the denoiser's skip tensors) equal the same values computed
+    from the convolution's own bf16 output: the 2x2 average ((a + b) + c) + d times 1/4 rounded to
+    bf16, bit for bit, and the nearest upsampling; neighbouring channels stay untouched."""
+    torch = _torch()
+    L = native.load()
+    g = torch.Generator(device="cuda").manual_seed(B * 7 + cin + cout + H)
+    x = torch.randn((B, H, W, cin), device="cuda", generator=g).bfloat16()
+    w = (torch.randn((cout, 3, 3, cin), device="cuda", generator=g) / (3 * cin ** 0.5)).bfloat16()
+    bias = torch.randn(cout, device="cuda", generator=g) * 0.1
+    out_c, off, pc, po, uc, uo = cout + 32, 16, cout + 24, 16, cout + 8, 8
+    out = torch.full((B, H, W, out_c), 3.0, device="cuda").bfloat16()
+    pool = torch.full((B, H // 2, W // 2, pc), 5.0, device="cuda").bfloat16()
+    up = torch.full((B, 2 * H, 2 * W, uc), 6.0, device="cuda").bfloat16()
+    rc = L.gkrt_conv3x3_bf16_fused(C.c_void_p(x.data_ptr()), B, H, W, cin, C.c_void_p(w.data_ptr()),
+                                   C.c_void_p(bias.data_ptr()), cout, C.c_void_p(out.data_ptr()), out_c, off, 1,
+                                   C.c_void_p(pool.data_ptr()), pc, po, C.c_void_p(up.data_ptr()), uc, uo, None)
+    assert rc == abi.GKRT_OK, rc
+    torch.cuda.synchronize()
+    y = out[..., off:off + cout]
+    ref = torch.relu(torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), w.float().permute(0, 3, 1, 2), bias,
+                                                padding=1)).permute(0, 2, 3, 1)
+    torch.testing.assert_close(y.float(), ref.bfloat16().float(), rtol=2e-2, atol=2e-2)
+    yf = y.float()[:, :2 * (H // 2), :2 * (W // 2)]
+    avg = ((((yf[:, 0::2, 0::2] + yf[:, 0::2, 1::2]) + yf[:, 1::2, 0::2]) + yf[:, 1::2, 1::2]) * 0.25).bfloat16()
+    assert torch.equal(pool[..., po:po + cout], avg)
+    rep = y.repeat_interleave(2, dim=1).repeat_interleave(2, dim=2)
+    assert torch.equal(up[..., uo:uo + cout], rep)
+    assert bool((pool[..., :po].float() == 5.0).all()) and bool((pool[..., po + cout:].float() == 5.0).all())
+    assert bool((up[..., :uo].float() == 6.0).all()) and bool((up[..., uo + cout:].float() == 6.0).all())
+    assert bool((out[..., :off].float() == 3.0).all()) and bool((out[..., off + cout:].float() == 3.0).all())
+
+
 def test_conv_f32_output_subset():
     torch = _torch()
     g = torch.Generator(device="cuda").manual_seed(3)
