@@ -1915,6 +1915,7 @@ int gkrt_unet_backward(GkrtContext* ctx, const float* d_raw, void* stream) {
     int rc = unet_ready(ctx);
     if (rc != GKRT_OK) return rc;
     if (!d_raw) return fail(ctx, GKRT_ERR_INVALID_ARG, "null gradient");
+    if (!gkrt_unet_has_forward(ctx->unet)) return fail(ctx, GKRT_ERR_STATE, "gkrt_unet_forward was not called");
     GK_CUDA(gkrt_unet_backward_dev(ctx->unet, d_raw, (cudaStream_t)stream));
     return GKRT_OK;
 }

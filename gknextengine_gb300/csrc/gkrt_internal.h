@@ -99,6 +99,13 @@ struct ConvArgs {
     int pool_c, pool_off;
     void* up_out;
     int up_c, up_off;
+    // optional addend of the bf16 epilogue (null: none), added to the sum before ReLU: at half
+    // resolution (H / 2 x W / 2, H and W even), add_c channels per pixel (a multiple of 8, at
+    // least 4 cout), output pixel (x, y) reading channels ((y & 1) 2 + (x & 1)) cout + c of
+    // pixel (x / 2, y / 2): the four sub-pixel parities of a convolution over nearest-upsampled
+    // input, computed at half resolution
+    const void* add_par;
+    int add_c;
 };
 
 // Host-side BVH build (binned SAH over boxes). Returns nodes in device layout and the leaf
@@ -279,6 +286,7 @@ cudaError_t gkrt_unet_zero_grad(gk::Unet* u, cudaStream_t st);
 cudaError_t gkrt_unet_forward_dev(gk::Unet* u, const float* input, int b, int h, int w, float* out_linear,
                                   float* out_raw, cudaStream_t st);
 cudaError_t gkrt_unet_backward_dev(gk::Unet* u, const float* d_raw, cudaStream_t st);
+bool gkrt_unet_has_forward(const gk::Unet* u);   // a forward ran (the backward's size and input)
 cudaError_t gkrt_unet_train_step_dev(gk::Unet* u, const float* input, const float* target, int b, int h, int w,
                                      float lr, double* loss_host, cudaStream_t st);
 cudaError_t gkrt_unet_denoise_frame(gk::Unet* u, const float4* sd, const float4* ss, const float4* alb,

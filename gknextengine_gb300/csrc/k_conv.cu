@@ -76,7 +76,7 @@ __device__ __forceinline__ size_t shfl_size(size_t v, int src) {
 // 2, so that neither side has bank conflicts), and each 32-byte sector of the output is then
 // written whole by two lanes of one store instruction: lane-per-pixel stores wrote every sector
 // in two 16-byte halves from separate instructions, twice the L2 write requests.
-__device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float* v, int img, int x, int y, bool inside,
+__device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v)[16], int img, int x, int y, bool inside,
                                               int c0, int yl, uint4* ebuf) {
     const int lane = threadIdx.x & 31;
     const size_t pix = ((size_t)img * a.H + y) * a.W + x;
@@ -157,12 +157,37 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float* v,
     }
 }
 
+// The addend's 16 channels for output channels c0 .. c0 + 15 of pixel (x, y) (add_par): q is
+// the element index of the half-resolution pixel's parity group.
+__device__ __forceinline__ size_t pix_add(const ConvArgs& a, int img, int x, int y) {
+    const size_t hp = ((size_t)img * (a.H >> 1) + (y >> 1)) * (a.W >> 1) + (x >> 1);
+    return hp * a.add_c + (size_t)(((y & 1) << 1) | (x & 1)) * a.cout;
+}
+__device__ __forceinline__ void add_parity(const ConvArgs& a, float (&v)[16], size_t q, int c0) {
+    const uint4* s = reinterpret_cast<const uint4*>(reinterpret_cast<const __nv_bfloat16*>(a.add_par) + q + c0);
+    const uint4 lo = __ldg(s), hi = __ldg(s + 1);
+    const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        v[2 * j] += __uint_as_float(w[j] << 16);
+        v[2 * j + 1] += __uint_as_float(w[j] & 0xFFFF0000u);
+    }
+}
+
 // fp32 output of channels c0 .. c0 + n - 1 (n <= 16) at o: 16-byte stores where o allows.
-__device__ __forceinline__ void store_f32(float* o, const float* v, int n) {
-    int j = 0;
-    if (!(reinterpret_cast<uintptr_t>(o) & 15u))
-        for (; j + 4 <= n; j += 4) *reinterpret_cast<float4*>(o + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-    for (; j < n; ++j) o[j] = v[j];
+// Unrolled with constant indices, so that v stays in registers.
+__device__ __forceinline__ void store_f32(float* o, const float (&v)[16], int n) {
+    const bool al = !(reinterpret_cast<uintptr_t>(o) & 15u);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (al && 4 * q + 4 <= n) {
+            *reinterpret_cast<float4*>(o + 4 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int j = 4 * q; j < 4 * q + 4; ++j)
+                if (j < n) o[j] = v[j];
+        }
+    }
 }
 
 __device__ __forceinline__ void tile_origin(int t, int tiles_x, int tiles_y, int& x0, int& y0, int& img) {
@@ -312,10 +337,11 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                 tmem_ld_wait();
                 float v[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                if (a.add_par && inside) add_parity(a, v, pix_add(a, img, x, y), c0);
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
                     if (a.flags & kConvRelu) v[j] = fmaxf(v[j], 0.0f);
-                }
                 if (a.flags & kConvF32Out) {
                     if (!inside) continue;
                     store_f32(reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0, v,
@@ -520,10 +546,11 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                 tmem_ld_wait();
                 float v[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    v[j] = __uint_as_float(rr[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(rr[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                if (a.add_par && inside) add_parity(a, v, pix_add(a, img, x, y), c0);
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
                     if (a.flags & kConvRelu) v[j] = fmaxf(v[j], 0.0f);
-                }
                 if (a.flags & kConvF32Out) {
                     if (!inside) continue;
                     store_f32(reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0, v,
@@ -599,7 +626,10 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     const bool halo = conv_halo(args.cin, args.cout);
     if (xv % 32 && !(halo && args.cin == 32)) return cudaErrorInvalidValue;
     if (args.x_c > 0 && (args.x_c % 8 || args.x_off + xv > args.x_c)) return cudaErrorInvalidValue;
-    if ((args.pool_out || args.up_out) && f32) return cudaErrorInvalidValue;
+    if ((args.pool_out || args.up_out || args.add_par) && f32) return cudaErrorInvalidValue;
+    if (args.add_par && ((args.H | args.W) & 1 || args.add_c % 8 || args.add_c < 4 * args.cout ||
+                         ((uintptr_t)args.add_par & 15u)))
+        return cudaErrorInvalidValue;
     if (args.pool_out && (args.pool_c % 8 || args.pool_off % 8 || args.pool_off + args.cout > args.pool_c ||
                           ((uintptr_t)args.pool_out & 15u)))
         return cudaErrorInvalidValue;

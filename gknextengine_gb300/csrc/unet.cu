@@ -180,6 +180,35 @@ __global__ void k_weights_bf16(const float* w, int cin, int cout, __nv_bfloat16*
     wf[((long long)ci * 9 + (8 - tap)) * cout + co] = h;
 }
 
+// dec0a's weights (fp32 [32][9][96]; input channels 0-63 the nearest-upsampled dec1b, 64-95
+// enc0b) as the inference forward's two convolutions. A 3x3 tap (dy, dx) of output pixel
+// (2i + a, 2j + b) reads the upsampled input at half-resolution offset (floor((a + dy) / 2),
+// floor((b + dx) / 2)), so over the upsampled channels the layer is, per parity (a, b), a 3x3
+// convolution at half resolution whose tap weights are the sums of the full-resolution taps
+// reading that offset (zero padding agrees, H and W being even):
+//   wup[(2a + b) 32 + co][3 (dyl + 1) + dxl + 1][ci] = sum of w[co][3 (dy + 1) + dx + 1][ci]
+//     over dy, dx in -1..1 (ascending) with floor((a + dy) / 2) = dyl, floor((b + dx) / 2) = dxl,
+// summed in FP32 and rounded to bf16; we0b[co][tap][ci] = w[co][tap][64 + ci].
+__device__ __forceinline__ int floor_half(int v) { return (v + 2) / 2 - 1; }   // v in -1..2
+__global__ void k_weights_subpixel(const float* w, __nv_bfloat16* wup, __nv_bfloat16* we0b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 128 * 9 * 64) {
+        const int ci = i % 64, lt = (i / 64) % 9, n = i / (64 * 9);
+        const int a = (n / 32) >> 1, b = (n / 32) & 1, co = n % 32;
+        const int dyl = lt / 3 - 1, dxl = lt % 3 - 1;
+        float acc = 0.0f;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx)
+                if (floor_half(a + dy) == dyl && floor_half(b + dx) == dxl)
+                    acc = acc + w[((size_t)co * 9 + 3 * (dy + 1) + dx + 1) * 96 + ci];
+        wup[i] = __float2bfloat16_rn(acc);
+    }
+    if (i < 32 * 9 * 32) {
+        const int ci = i % 32, tap = (i / 32) % 9, co = i / (32 * 9);
+        we0b[i] = __float2bfloat16_rn(w[((size_t)co * 9 + tap) * 96 + 64 + ci]);
+    }
+}
+
 inline unsigned nb(long long n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
@@ -189,6 +218,8 @@ struct Unet {
     size_t nparams = 0, nweights_bf16 = 0;
     float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
     __nv_bfloat16 *wb = nullptr, *wf = nullptr;
+    __nv_bfloat16 *wup = nullptr, *we0b = nullptr;   // dec0a as the inference forward's convolutions
+    bool train_acts = false;   // the activations are the training forward's (backward may run)
     int step = 0;
     int B = 0, H = 0, W = 0;
     void* arena = nullptr;
@@ -216,7 +247,8 @@ struct Unet {
         nweights_bf16 = wo;
     }
     ~Unet() {
-        for (void* q : {(void*)p, (void*)g, (void*)m, (void*)v, (void*)wb, (void*)wf, arena, (void*)d_loss, (void*)err})
+        for (void* q : {(void*)p, (void*)g, (void*)m, (void*)v, (void*)wb, (void*)wf, (void*)wup, (void*)we0b, arena,
+                        (void*)d_loss, (void*)err})
             if (q) cudaFree(q);
     }
 
@@ -226,6 +258,8 @@ struct Unet {
             if ((e = cudaMalloc((void**)q, nparams * sizeof(float))) != cudaSuccess) return e;
         if ((e = cudaMalloc((void**)&wb, nweights_bf16 * 2)) != cudaSuccess) return e;
         if ((e = cudaMalloc((void**)&wf, nweights_bf16 * 2)) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&wup, 128 * 9 * 64 * 2)) != cudaSuccess) return e;
+        if ((e = cudaMalloc((void**)&we0b, 32 * 9 * 32 * 2)) != cudaSuccess) return e;
         if ((e = cudaMalloc((void**)&d_loss, sizeof(double))) != cudaSuccess) return e;
         if ((e = cudaMalloc((void**)&err, 4)) != cudaSuccess) return e;
         return cudaMemset(err, 0, 4);
@@ -238,6 +272,7 @@ struct Unet {
             k_weights_bf16<<<nb(n), 256, 0, st>>>(p + woff[l], kLayers[l].cin, kLayers[l].cout, wb + wb_off[l],
                                                   wf + wb_off[l]);
         }
+        k_weights_subpixel<<<nb(128 * 9 * 64), 256, 0, st>>>(p + woff[D0A], wup, we0b);
         return cudaGetLastError();
     }
 
@@ -301,13 +336,23 @@ struct Unet {
         return gkrt_launch_conv3x3(in, wb + wb_off[l], a, st);
     }
 
-    cudaError_t forward(cudaStream_t st) {
+    // train: the forward whose activations the backward reads (the upsampled copies in the
+    // concatenations). Otherwise dec1b's upsampled copy is not written: dec0a runs as the
+    // sub-pixel convolution of dec1b at half resolution (the four parities, 128 channels, into
+    // the unused gradient buffer g_cat0) and a convolution over enc0b (dense in g_e0a) that adds
+    // them.
+    cudaError_t forward(cudaStream_t st, bool train) {
         cudaError_t e;
+        train_acts = train;
 #define GK_T(x) if ((e = (x)) != cudaSuccess) return e
         GK_T(conv(E0A, x0, kXc, 0, e0a, 32, 0, 0, st));
         // the 2 x 2 pools and nearest upsamplings ride in the epilogues of the convolutions that
         // produce their inputs: 2 x 2 means of the stored values, nearest copies
-        GK_T(conv(E0B, e0a, 32, 0, cat0, 96, 64, 0, st, p0, 32, 0));
+        // inference: enc0b dense in the unused gradient buffer g_e0a (the sub-pixel dec0a reads it
+        // alone); training: into its concatenation
+        __nv_bfloat16* e0b = train ? cat0 : g_e0a;
+        const int e0b_c = train ? 96 : 32, e0b_off = train ? 64 : 0;
+        GK_T(conv(E0B, e0a, 32, 0, e0b, e0b_c, e0b_off, 0, st, p0, 32, 0));
         GK_T(conv(E1A, p0, 32, 0, e1a, 64, 0, 1, st));
         GK_T(conv(E1B, e1a, 64, 0, cat1, 160, 96, 1, st, p1, 64, 0));
         GK_T(conv(E2A, p1, 64, 0, e2a, 96, 0, 2, st));
@@ -317,8 +362,28 @@ struct Unet {
         GK_T(conv(D2A, cat2, 224, 0, d2a, 96, 0, 2, st));
         GK_T(conv(D2B, d2a, 96, 0, d2b, 96, 0, 2, st, nullptr, 0, 0, cat1, 160, 0));
         GK_T(conv(D1A, cat1, 160, 0, d1a, 64, 0, 1, st));
-        GK_T(conv(D1B, d1a, 64, 0, d1b, 64, 0, 1, st, nullptr, 0, 0, cat0, 96, 0));
-        GK_T(conv(D0A, cat0, 96, 0, d0a, 32, 0, 0, st));
+        if (train) {
+            GK_T(conv(D1B, d1a, 64, 0, d1b, 64, 0, 1, st, nullptr, 0, 0, cat0, 96, 0));
+            GK_T(conv(D0A, cat0, 96, 0, d0a, 32, 0, 0, st));
+        } else {
+            GK_T(conv(D1B, d1a, 64, 0, d1b, 64, 0, 1, st));
+            __nv_bfloat16* par = g_cat0;   // B x H/2 x W/2 x 128 fits in B x H x W x 96
+            ConvArgs a{};
+            a.B = B; a.H = H >> 1; a.W = W >> 1; a.cin = 64; a.cout = 128;
+            a.x_c = 64;
+            a.out = par; a.out_c = 128; a.n_store = 128;
+            a.err = err;
+            GK_T(gkrt_launch_conv3x3(d1b, wup, a, st));
+            ConvArgs c{};
+            c.B = B; c.H = H; c.W = W; c.cin = 32; c.cout = 32;
+            c.x_c = e0b_c; c.x_off = e0b_off;
+            c.bias = p + boff[D0A];
+            c.out = d0a; c.out_c = 32; c.n_store = 32;
+            c.flags = kConvRelu;
+            c.err = err;
+            c.add_par = par; c.add_c = 128;
+            GK_T(gkrt_launch_conv3x3(e0b, we0b, c, st));
+        }
         GK_T(conv(D0B, d0a, 32, 0, d0b, 32, 0, 0, st));
         GK_T(conv(OUT, d0b, 32, 0, y, 4, 0, 0, st));
         return cudaSuccess;
@@ -447,27 +512,36 @@ cudaError_t gkrt_unet_set_state_host(Unet* u, const float* m, const float* v, ui
 
 cudaError_t gkrt_unet_zero_grad(Unet* u, cudaStream_t st) { return cudaMemsetAsync(u->g, 0, u->nparams * 4, st); }
 
-cudaError_t gkrt_unet_forward_dev(Unet* u, const float* input, int b, int h, int w, float* out_linear, float* out_raw,
-                                  cudaStream_t st) {
+static cudaError_t forward_dev(Unet* u, const float* input, int b, int h, int w, float* out_linear, float* out_raw,
+                               bool train, cudaStream_t st) {
     cudaError_t e = u->ensure_size(b, h, w);
     if (e != cudaSuccess) return e;
     const long long npix = (long long)b * h * w;
     if (input) k_pack_input<<<nb(npix), 256, 0, st>>>(input, npix, u->x0);
-    if ((e = u->forward(st)) != cudaSuccess) return e;
+    if ((e = u->forward(st, train)) != cudaSuccess) return e;
     if (out_linear) k_out_linear<<<nb(npix), 256, 0, st>>>(u->y, npix, out_linear);
     if (out_raw) e = cudaMemcpyAsync(out_raw, u->y, npix * 16, cudaMemcpyDeviceToDevice, st);
     return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
+// Inference: the sub-pixel form of dec0a. A backward after it runs the training forward again
+// on the same packed input (x0) for the activations it reads.
+cudaError_t gkrt_unet_forward_dev(Unet* u, const float* input, int b, int h, int w, float* out_linear, float* out_raw,
+                                  cudaStream_t st) {
+    return forward_dev(u, input, b, h, w, out_linear, out_raw, false, st);
+}
+
 cudaError_t gkrt_unet_backward_dev(Unet* u, const float* d_raw, cudaStream_t st) {
     const long long npix = (long long)u->B * u->H * u->W;
+    cudaError_t e;
+    if (!u->train_acts && (e = u->forward(st, true)) != cudaSuccess) return e;
     k_grad_in<<<nb(npix * 32), 256, 0, st>>>(d_raw, npix, u->gy);
     return u->backward(st);
 }
 
 cudaError_t gkrt_unet_train_step_dev(Unet* u, const float* input, const float* target, int b, int h, int w, float lr,
                                      double* loss_host, cudaStream_t st) {
-    cudaError_t e = gkrt_unet_forward_dev(u, input, b, h, w, nullptr, nullptr, st);
+    cudaError_t e = forward_dev(u, input, b, h, w, nullptr, nullptr, true, st);
     if (e != cudaSuccess) return e;
     const long long npix = (long long)b * h * w;
     if ((e = cudaMemsetAsync(u->d_loss, 0, sizeof(double), st)) != cudaSuccess) return e;
@@ -498,10 +572,11 @@ cudaError_t gkrt_unet_denoise_frame(Unet* u, const float4* sd, const float4* ss,
     cudaError_t e = u->ensure_size(1, H, W);
     if (e != cudaSuccess) return e;
     k_pack_frame<<<nb((long long)W * H), 256, 0, st>>>(sd, ss, alb, nrm, depth, W, H, P, u->x0);
-    if ((e = u->forward(st)) != cudaSuccess) return e;
+    if ((e = u->forward(st, false)) != cudaSuccess) return e;
     (void)y_out_raw;
     return cudaGetLastError();
 }
 
 const float* gkrt_unet_output(const Unet* u) { return u->y; }
+bool gkrt_unet_has_forward(const Unet* u) { return u->B > 0; }
 uint32_t* gkrt_unet_error_word(const Unet* u) { return u->err; }

@@ -506,7 +506,11 @@ int  gkrt_conv3x3_bf16_fused(const void* x, uint32_t batch, uint32_t height, uin
  * [..][3] linear radiance.
  * out_linear: [..][4] denoised linear radiance (w = 1); out_raw: [..][4] the network's
  * log(1 + radiance) output in x, y, z (w: an unused fourth output), the quantity
- * gkrt_unet_backward's d_raw differentiates (its w is ignored). Sizes
+ * gkrt_unet_backward's d_raw differentiates (its w is ignored). gkrt_unet_forward is the
+ * inference forward: the first decoder convolution runs in its sub-pixel form at half
+ * resolution (its taps over the upsampled input summed per output parity, the sums rounded to
+ * bf16), within bf16 rounding of the training forward; gkrt_unet_backward re-runs the training
+ * forward on the same input for the activations it needs (GKRT_ERR_STATE without a forward). Sizes
  * are multiples of 8 from 16 to 8192, batch 1..64. Parameters: gkrt_unet_param_count floats,
  * per layer the weights [cout][3][3][cin] then the biases; set_params resets Adam's state.
  * The denoise pass uses it with GKRT_DENOISE_UNET. */
