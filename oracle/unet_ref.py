@@ -93,8 +93,39 @@ def pack_input(inp):
     return bf16(x)
 
 
-def forward(params, inp):
-    """Returns (y raw log-space output (B, H, W, 3), cache)."""
+def subpixel_weights(W):
+    """dec0a's weights over its upsampled input channels (W (32, 3, 3, 96), channels 0-63) as a
+    half-resolution convolution with 128 outputs, one group of 32 per output parity (a, b): the
+    taps (dy, dx) of output pixel (2i + a, 2j + b) read the upsampled input at half-resolution
+    offset (floor((a + dy) / 2), floor((b + dx) / 2)), so each half-resolution tap's weight is
+    the sum of the full-resolution taps that read it (unet.cu, k_weights_subpixel)."""
+    Wup = np.zeros((128, 3, 3, 64))
+    for a in range(2):
+        for b in range(2):
+            for dy in (-1, 0, 1):
+                for dx in (-1, 0, 1):
+                    dyl, dxl = (a + dy) // 2, (b + dx) // 2
+                    Wup[(2 * a + b) * 32:(2 * a + b + 1) * 32, dyl + 1, dxl + 1, :] += W[:, dy + 1, dx + 1, :64]
+    return Wup
+
+
+def subpixel_conv(x_half, Wup, cout=32):
+    """The full-resolution output of the parity convolution: pixel (2i + a, 2j + b) takes
+    channels (2a + b) cout .. of conv(x_half, Wup) at (i, j)."""
+    U = conv(x_half, Wup)
+    B, h, w, _ = U.shape
+    out = np.zeros((B, 2 * h, 2 * w, cout))
+    for a in range(2):
+        for b in range(2):
+            out[:, a::2, b::2, :] = U[..., (2 * a + b) * cout:(2 * a + b + 1) * cout]
+    return out, U
+
+
+def forward(params, inp, inference=False):
+    """Returns (y raw log-space output (B, H, W, 3), cache). inference: dec0a as the library's
+    inference forward computes it (unet.cu, Unet::forward without train): the parity
+    convolution of dec1b with bf16 sums of the weights, its output stored in bf16, added to the
+    convolution over enc0b before the bias and ReLU."""
     P = [(bf16(W), b.astype(np.float64)) for W, b in unpack(params)]
 
     def layer(l, x, store=True):
@@ -124,7 +155,15 @@ def forward(params, inp):
     c["d1a"] = layer(10, c["cat1"])
     c["d1b"] = layer(11, c["d1a"])
     c["cat0"] = np.concatenate([up(c["d1b"]), c["e0b"]], -1)
-    c["d0a"] = layer(12, c["cat0"])
+    if inference:
+        W32 = unpack(params)[12][0].astype(np.float32).astype(np.float64)
+        u_full, _ = subpixel_conv(c["d1b"], bf16(subpixel_weights(W32)))
+        # the parity outputs are stored in bf16: take the rounding per half-resolution value
+        u_full = bf16(u_full)
+        o = conv(c["e0b"], bf16(W32[..., 64:])) + P[12][1] + u_full
+        c["d0a"] = bf16(np.maximum(o, 0.0))
+    else:
+        c["d0a"] = layer(12, c["cat0"])
     c["d0b"] = layer(13, c["d0a"])
     y = layer(14, c["d0b"], store=False)
     c["P"] = P

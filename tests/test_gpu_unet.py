@@ -42,9 +42,14 @@ def test_unet_matches_cpu_oracle():
         net.forward(x, out_raw=raw)
         torch.cuda.synchronize()
         y_ref, cache = unet_ref.forward(p, inp.astype(np.float64))
+        # gkrt_unet_forward is the inference forward (sub-pixel dec0a); its oracle, and the
+        # training forward's, which the backward below runs again
+        y_inf, _ = unet_ref.forward(p, inp.astype(np.float64), inference=True)
         y = raw.cpu().numpy()[..., :3]
-        print("forward relative error", np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref))
-        assert np.linalg.norm(y - y_ref) < 2e-2 * np.linalg.norm(y_ref)
+        e_inf = np.linalg.norm(y - y_inf) / np.linalg.norm(y_inf)
+        e_train = np.linalg.norm(y - y_ref) / np.linalg.norm(y_ref)
+        print("forward relative error: inference oracle", e_inf, "training oracle", e_train)
+        assert e_inf < 2e-2 and e_train < 2e-2
         d = rng.normal(size=(B, H, W, 3)) / (B * H * W)
         d4 = np.zeros((B, H, W, 4), np.float32)
         d4[..., :3] = d
