@@ -17,11 +17,13 @@
 namespace gk {
 
 constexpr int kPtThreads = 128;
-// resident blocks per SM (at most 102 registers; ptxas uses 96): with stacks sized to the
-// scene the fifth block fits in shared memory, and the latency-bound traversal gains more from
-// it than it loses to spills (1080p bricks trace pass: 3 blocks 4.43 ms, 4 blocks 4.04 ms,
-// 5 blocks 3.78 ms, 6 blocks 3.82 ms, 8 blocks 3.80 ms)
-constexpr int kPtMinBlocks = 5;
+// Resident blocks per SM, per instantiation: 4 (128 registers, few spills) without emissive
+// NEE, 5 (96 registers, spills) with it, whose shadow rays add a second traversal per vertex
+// that more warps hide better. Same box, current kernel: the 1080p brick trace pass (no NEE)
+// 3 / 4 / 5 / 6 blocks 3.94 / 3.43 / 3.56 / 3.54 ms; the 4K city (alias-table NEE) 116.4 /
+// 102.9 / 97.0 ms for 3 / 4 / 5 blocks.
+template <bool kNee>
+constexpr int pt_blocks() { return kNee ? 5 : 4; }
 constexpr int kRefillBelow = 1;    // shade and refill once every lane of the warp has finished its ray
 constexpr float kCosCone = 0.999990482f;   // cos(0.25 deg), Shading.slang:897
 
@@ -409,7 +411,7 @@ __device__ void start_pixel(Lane& L, Trav& T, const Ctx& c, int x, int y) {
 // leaves the rest of the SM's 256 KB to L1, which serves the node fetches (measured on 1080p
 // bricks: 72-word stacks 4.15 ms, 36-word 4.01 ms).
 template <bool kNee, bool kTex>
-__global__ void __launch_bounds__(kPtThreads, kPtMinBlocks) k_trace_pass(ShadeScene sc, GkrtFrameConstants fc, int W, int H,
+__global__ void __launch_bounds__(kPtThreads, pt_blocks<kNee>()) k_trace_pass(ShadeScene sc, GkrtFrameConstants fc, int W, int H,
                                                            int P, PixelImages im, unsigned long long* counters,
                                                            unsigned int* work, int stack_words) {
     extern __shared__ uint32_t dyn_smem[];
