@@ -50,14 +50,6 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-__device__ __forceinline__ void store_bf16x16(__nv_bfloat16* dst, const float* v) {
-    uint4* o = reinterpret_cast<uint4*>(dst);
-    o[0] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
-                      pack_bf16x2(v[6], v[7]));
-    o[1] = make_uint4(pack_bf16x2(v[8], v[9]), pack_bf16x2(v[10], v[11]), pack_bf16x2(v[12], v[13]),
-                      pack_bf16x2(v[14], v[15]));
-}
-
 // Shared memory of the bf16 epilogue: 1 KB per epilogue warp (16-byte aligned).
 constexpr int kEpiBuf = 4 * 1024 + 16;
 
