@@ -100,52 +100,34 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v
     }
     __syncwarp();   // the next group rewrites ebuf
     if (a.pool_out) {
-        // the block's top-left lane (even x, even y: lane bits 0 and log2(yl) clear) owns the
-        // average; it reads the block's four stored values from ebuf, and the warp's 8 owners
-        // pass the averages back through ebuf, where 16 lanes store 8 whole sectors
+        // The warp's 8 pooled pixels x 16 channels: lane l averages channels 4 (l & 3) .. + 3 of
+        // pooled pixel l >> 2 from the block's four stored values in ebuf (the block's top-left
+        // lane, even x and even y, has lane bits 0 and log2(yl) clear; then its x-, y- and
+        // diagonal neighbours, in that order) and stores them: 4 lanes per 32-byte sector.
         const int h2 = a.H / 2, w2 = a.W / 2;
         const int b = yl == 16 ? 4 : 3;
-        const bool owner = (lane & 1) == 0 && (lane & yl) == 0;
-        float s[16];
+        const int k = lane >> 2, qd = lane & 3;
+        const int tl = ((k >> (b - 1)) << (b + 1)) | ((k & ((1 << (b - 1)) - 1)) << 1);   // top-left lane
+        float s4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int j = 0; j < 16; ++j) s[j] = 0.0f;
-        if (owner) {
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {   // own, x-neighbour, y-neighbour, diagonal
-                const int nl = lane ^ (t & 1) ^ (t & 2 ? yl : 0), ns = (nl >> 2) & 1;
-                const uint4 lo = ebuf[2 * nl + ns], hi = ebuf[2 * nl + (ns ^ 1)];
-                const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    s[2 * j] = s[2 * j] + __uint_as_float(w[j] << 16);
-                    s[2 * j + 1] = s[2 * j + 1] + __uint_as_float(w[j] & 0xFFFF0000u);
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < 16; ++j) s[j] *= 0.25f;
+        for (int t = 0; t < 4; ++t) {
+            const int nl = tl ^ (t & 1) ^ (t & 2 ? yl : 0);
+            const uint2 w = *reinterpret_cast<const uint2*>(reinterpret_cast<const uint8_t*>(ebuf) +
+                                                            (2 * nl + ((qd >> 1) ^ ((nl >> 2) & 1))) * 16 +
+                                                            (qd & 1) * 8);
+            s4[0] = s4[0] + __uint_as_float(w.x << 16);
+            s4[1] = s4[1] + __uint_as_float(w.x & 0xFFFF0000u);
+            s4[2] = s4[2] + __uint_as_float(w.y << 16);
+            s4[3] = s4[3] + __uint_as_float(w.y & 0xFFFF0000u);
         }
-        __syncwarp();   // the block values are read before the averages overwrite ebuf
-        const int k = ((lane >> (b + 1)) << (b - 1)) | ((lane & (yl - 1)) >> 1);
         const size_t pp = ((size_t)img * h2 + y / 2) * w2 + x / 2;
-        const bool pvalid = owner && !(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2;
-        if (owner) {
-            const int ks = (k >> 2) & 1;
-            ebuf[2 * k + ks] = make_uint4(pack_bf16x2(s[0], s[1]), pack_bf16x2(s[2], s[3]), pack_bf16x2(s[4], s[5]),
-                                          pack_bf16x2(s[6], s[7]));
-            ebuf[2 * k + (ks ^ 1)] = make_uint4(pack_bf16x2(s[8], s[9]), pack_bf16x2(s[10], s[11]),
-                                                pack_bf16x2(s[12], s[13]), pack_bf16x2(s[14], s[15]));
-        }
-        __syncwarp();
-        const int src = (lane >> 1) & 7;   // lanes 0-15 store; the source owner's lane:
-        const int src_lane = ((src >> (b - 1)) << (b + 1)) | ((src & ((1 << (b - 1)) - 1)) << 1);
-        const size_t spp = shfl_size(pp, src_lane);
-        const bool sv = __shfl_sync(0xFFFFFFFFu, pvalid ? 1 : 0, src_lane) != 0;
-        if (lane < 16 && sv) {
-            const uint4 val = ebuf[2 * src + (h ^ ((src >> 2) & 1))];
-            *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.pool_out) + spp * a.pool_c + a.pool_off +
-                                      c0 + 8 * h) = val;
-        }
-        __syncwarp();
+        const bool pvalid = !(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2;
+        const size_t spp = shfl_size(pp, tl);
+        if (__shfl_sync(0xFFFFFFFFu, pvalid ? 1 : 0, tl))
+            *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(a.pool_out) + spp * a.pool_c + a.pool_off + c0 +
+                                      4 * qd) =
+                make_uint2(pack_bf16x2(s4[0] * 0.25f, s4[1] * 0.25f), pack_bf16x2(s4[2] * 0.25f, s4[3] * 0.25f));
+        __syncwarp();   // the next group rewrites ebuf
     }
 }
 
