@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid
     __shared__ __align__(128) float4 t_nrm[kRpT * kRpT];
     __shared__ __align__(128) uint32_t t_id[kRpT * kRpIdX];
     __shared__ __align__(128) float2 t_mv[kRpMv * kRpMv];
+    __shared__ float t_mvl[kRpMv * kRpMv];   // |motion| of each staged pixel (the taps' mir terms)
     __shared__ __align__(8) uint64_t bar;
     const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -119,7 +120,13 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid
         tma_load_2d(t_id, &m_id, x0 - 4, y0 - kRpHalo, &bar);
         tma_load_2d(t_mv, &m_mv, 2 * (x0 - 4), y0 - 4, &bar);
     }
-    if (!tl.wait(a.err)) return;
+    // the block agrees on the load's outcome before the barrier below
+    if (!__syncthreads_and(tl.wait(a.err) ? 1 : 0)) return;
+    for (int i = threadIdx.x; i < kRpMv * kRpMv; i += 256) {
+        const float2 m2 = t_mv[i];
+        t_mvl[i] = sqrt_(fmaf_(m2.y, m2.y, m2.x * m2.x));
+    }
+    __syncthreads();
     if (x >= a.W || y >= a.H) return;
     const size_t pix = (size_t)y * a.P + x;
     // tile-local coordinates of (x, y)
@@ -161,8 +168,7 @@ __global__ void __launch_bounds__(256) k_reproject(ReprojectArgs a, const __grid
             sd = sd + tf4(t_sd, kRpT, cx + ox, cy + oy) * w;
             ss = ss + tf4(t_ss, kRpT, cx + ox, cy + oy) * w;
             tw = tw + w;
-            const float2 m2 = t_mv[(ty + 4 + 2 * oy) * kRpMv + (tx + 4 + 2 * ox)];
-            mir = mir + sqrt_(fmaf_(m2.y, m2.y, m2.x * m2.x));
+            mir = mir + t_mvl[(ty + 4 + 2 * oy) * kRpMv + (tx + 4 + 2 * ox)];
         }
     }
     sd = F4(div_(sd.x, tw), div_(sd.y, tw), div_(sd.z, tw), div_(sd.w, tw));
