@@ -317,7 +317,7 @@ GK_D f3 tri_v(const float4* tris, uint32_t ti, int k, uint32_t* prim = nullptr) 
 // strided); everything else is here, so a ray can be advanced one step at a time and a
 // lane can leave the traversal loop and come back.
 struct Trav {
-    f3 wo, wd;            // world ray
+    f3 wo, wd, winv;      // world ray and its safe reciprocal direction (restored on leaving an instance)
     f3 o, d, inv;         // ray in the current space (world or instance)
     float tmin;           // read by the ray-query kernels (kRayTmin); the rt pass uses kTmin
     float tmax, tcull, best_lo, best_hi;
@@ -338,6 +338,7 @@ template <bool kWide = false>
 GK_D void trav_init(Trav& T, const SceneView& S, f3 wo, f3 wd, float tmax, int mode, float tmin = kTmin) {
     T.wo = wo; T.wd = wd; T.o = wo; T.d = wd;
     T.inv = safe_inv(wd);
+    T.winv = T.inv;
     T.tmin = tmin;
     T.tmax = tmax;
     T.tcull = tmax * 1.000001f;
@@ -470,7 +471,7 @@ GK_D bool trav_node_step(Trav& T, const SceneView& S, uint32_t* stk, int stride,
     }
     if (ref == kRefMarker) {
         if (T.has_leaf) { T.ref = kRefMarker; return false; }   // the postponed leaf needs this instance's ray
-        T.o = T.wo; T.d = T.wd; T.inv = safe_inv(T.wd);
+        T.o = T.wo; T.d = T.wd; T.inv = T.winv;
         T.inblas = false;
         if (T.sp == 0) { T.done = true; T.ref = kRefPop; return false; }
         --T.sp;
@@ -536,7 +537,7 @@ GK_D void wide_sort_cx(uint32_t& a, uint32_t& b) {
 }
 
 GK_D void trav_to_world(Trav& T) {
-    T.o = T.wo; T.d = T.wd; T.inv = safe_inv(T.wd);
+    T.o = T.wo; T.d = T.wd; T.inv = T.winv;
     T.inblas = false;
 }
 
