@@ -131,6 +131,17 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v
     }
 }
 
+// v[j] += bias[c0 + j] (bias null: nothing) as four 16-byte loads (the bias is 16-byte aligned).
+__device__ __forceinline__ void add_bias16(const float* bias, int c0, float (&v)[16]) {
+    if (!bias) return;
+    const float4* b4 = reinterpret_cast<const float4*>(bias + c0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float4 b = __ldg(b4 + k);
+        v[4 * k] += b.x; v[4 * k + 1] += b.y; v[4 * k + 2] += b.z; v[4 * k + 3] += b.w;
+    }
+}
+
 // The addend's 16 channels for output channels c0 .. c0 + 15 of pixel (x, y) (add_par): q is
 // the element index of the half-resolution pixel's parity group.
 __device__ __forceinline__ size_t pix_add(const ConvArgs& a, int img, int x, int y) {
@@ -311,7 +322,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                 tmem_ld_wait();
                 float v[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+                add_bias16(a.bias, c0, v);
                 if (a.add_par && inside) add_parity(a, v, pix_add(a, img, x, y), c0);
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
@@ -520,7 +532,8 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                 tmem_ld_wait();
                 float v[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(rr[j]) + (a.bias ? __ldg(&a.bias[c0 + j]) : 0.0f);
+                for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(rr[j]);
+                add_bias16(a.bias, c0, v);
                 if (a.add_par && inside) add_parity(a, v, pix_add(a, img, x, y), c0);
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
@@ -591,7 +604,8 @@ cudaError_t gkrt_launch_conv3x3(const void* x, const void* w, const ConvArgs& ar
     if (args.cin % 32 || args.cin < 32 || args.cout % 16 || args.cout < 16 || args.cout > 256 || args.B < 1 ||
         args.H < 1 || args.W < 1 || (!f32 && (args.out_c % 16 || args.out_off % 16)) ||
         args.out_off + (f32 ? args.n_store : args.cout) > args.out_c || (f32 && args.n_store > args.cout) ||
-        ((uintptr_t)x & 15u) || ((uintptr_t)w & 15u) || ((uintptr_t)args.out & 15u) || args.x_off % 8 ||
+        ((uintptr_t)x & 15u) || ((uintptr_t)w & 15u) || ((uintptr_t)args.out & 15u) ||
+        ((uintptr_t)args.bias & 15u) || args.x_off % 8 ||
         args.x_valid < 0 || args.x_valid > args.cin || (args.x_valid % 32 && args.x_valid != 16))
         return cudaErrorInvalidValue;
     const int xv = args.x_valid > 0 ? args.x_valid : args.cin;   // channels present; the rest are zeros
