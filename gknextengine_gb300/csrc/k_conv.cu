@@ -68,10 +68,53 @@ __device__ __forceinline__ size_t shfl_size(size_t v, int src) {
 // 2, so that neither side has bank conflicts), and each 32-byte sector of the output is then
 // written whole by two lanes of one store instruction: lane-per-pixel stores wrote every sector
 // in two 16-byte halves from separate instructions, twice the L2 write requests.
-__device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v)[16], int img, int x, int y, bool inside,
-                                              int c0, int yl, uint4* ebuf) {
-    const int lane = threadIdx.x & 31;
+// Where a lane's stores of one tile go, the same for every channel group (computed once per
+// tile): the two pixels whose 16-byte halves it stores (element offsets into out and, for the
+// nearest upsampling, of the top-left of the 2 x 2 block in up), and the pooled pixel whose
+// four channels it stores.
+struct EpiDst {
+    size_t o[2], u[2], p;
+    bool in[2], pin;
+};
+__device__ __forceinline__ EpiDst epi_dst(const ConvArgs& a, int img, int x, int y, bool inside, int yl) {
+    const int lane = threadIdx.x & 31, h = lane & 1;
     const size_t pix = ((size_t)img * a.H + y) * a.W + x;
+    const size_t uq = ((size_t)img * 2 * a.H + 2 * (size_t)y) * (2 * (size_t)a.W) + 2 * (size_t)x;
+    EpiDst d;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const int src = (lane >> 1) + 16 * i;
+        d.o[i] = shfl_size(pix, src) * a.out_c + a.out_off + 8 * h;
+        d.in[i] = __shfl_sync(0xFFFFFFFFu, inside ? 1 : 0, src) != 0;
+        d.u[i] = a.up_out ? shfl_size(uq, src) * a.up_c + a.up_off + 8 * h : 0;
+    }
+    d.p = 0;
+    d.pin = false;
+    if (a.pool_out) {
+        const int h2 = a.H / 2, w2 = a.W / 2;
+        const int b = yl == 16 ? 4 : 3;
+        const int k = lane >> 2;
+        const int tl = ((k >> (b - 1)) << (b + 1)) | ((k & ((1 << (b - 1)) - 1)) << 1);   // top-left lane
+        const size_t pp = ((size_t)img * h2 + y / 2) * w2 + x / 2;
+        const bool pvalid = !(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2;
+        d.p = shfl_size(pp, tl) * a.pool_c + a.pool_off + 4 * (lane & 3);
+        d.pin = __shfl_sync(0xFFFFFFFFu, pvalid ? 1 : 0, tl) != 0;
+    }
+    return d;
+}
+
+// The bf16 epilogue of 16 channels (c0 .. c0 + 15) of the warp's 32 pixels: the plain store,
+// and the optional pooled and upsampled outputs. Called by every lane of the warp (the pool's
+// 2 x 2 block is four lanes of one warp: x-neighbour lane ^ 1, y-neighbour lane ^ yl); the
+// pooled average is (((0 + v(x, y)) + v(x + 1, y)) + v(x, y + 1)) + v(x + 1, y + 1) of the
+// stored (bf16-rounded) values, times 1/4, rounded to bf16. The warp's 32 pixels pass their
+// 32 bytes through ebuf (this warp's 1 KB of shared memory; 16-byte chunks swizzled by lane bit
+// 2, so that neither side has bank conflicts), and each 32-byte sector of the output is then
+// written whole by two lanes of one store instruction: lane-per-pixel stores wrote every sector
+// in two 16-byte halves from separate instructions, twice the L2 write requests.
+__device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v)[16], const EpiDst& d, int c0,
+                                              int yl, uint4* ebuf) {
+    const int lane = threadIdx.x & 31;
     const int sw = (lane >> 2) & 1;
     ebuf[2 * lane + sw] = make_uint4(pack_bf16x2(v[0], v[1]), pack_bf16x2(v[2], v[3]), pack_bf16x2(v[4], v[5]),
                                      pack_bf16x2(v[6], v[7]));
@@ -79,23 +122,16 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v
                                            pack_bf16x2(v[12], v[13]), pack_bf16x2(v[14], v[15]));
     __syncwarp();
     const size_t W2 = 2 * (size_t)a.W;
-    const size_t uq = ((size_t)img * 2 * a.H + 2 * (size_t)y) * W2 + 2 * (size_t)x;
     const int h = lane & 1;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
         const int src = (lane >> 1) + 16 * i;
         const uint4 val = ebuf[2 * src + (h ^ ((src >> 2) & 1))];
-        const size_t spix = shfl_size(pix, src);
-        const bool sin = __shfl_sync(0xFFFFFFFFu, inside ? 1 : 0, src) != 0;
-        if (sin)
-            *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + spix * a.out_c + a.out_off + c0 +
-                                      8 * h) = val;
-        if (a.up_out) {
-            const size_t sq = shfl_size(uq, src);
-            __nv_bfloat16* up = reinterpret_cast<__nv_bfloat16*>(a.up_out) + a.up_off + c0 + 8 * h;
-            if (sin)
-                for (int k = 0; k < 4; ++k)
-                    *reinterpret_cast<uint4*>(up + (sq + (k >> 1) * W2 + (k & 1)) * a.up_c) = val;
+        if (d.in[i]) *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(a.out) + d.o[i] + c0) = val;
+        if (a.up_out && d.in[i]) {
+            __nv_bfloat16* up = reinterpret_cast<__nv_bfloat16*>(a.up_out) + d.u[i] + c0;
+            for (int k = 0; k < 4; ++k)
+                *reinterpret_cast<uint4*>(up + ((k >> 1) * W2 + (k & 1)) * a.up_c) = val;
         }
     }
     __syncwarp();   // the next group rewrites ebuf
@@ -104,7 +140,6 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v
         // pooled pixel l >> 2 from the block's four stored values in ebuf (the block's top-left
         // lane, even x and even y, has lane bits 0 and log2(yl) clear; then its x-, y- and
         // diagonal neighbours, in that order) and stores them: 4 lanes per 32-byte sector.
-        const int h2 = a.H / 2, w2 = a.W / 2;
         const int b = yl == 16 ? 4 : 3;
         const int k = lane >> 2, qd = lane & 3;
         const int tl = ((k >> (b - 1)) << (b + 1)) | ((k & ((1 << (b - 1)) - 1)) << 1);   // top-left lane
@@ -120,12 +155,8 @@ __device__ __forceinline__ void epilogue_bf16(const ConvArgs& a, const float (&v
             s4[2] = s4[2] + __uint_as_float(w.y << 16);
             s4[3] = s4[3] + __uint_as_float(w.y & 0xFFFF0000u);
         }
-        const size_t pp = ((size_t)img * h2 + y / 2) * w2 + x / 2;
-        const bool pvalid = !(x & 1) && !(y & 1) && x / 2 < w2 && y / 2 < h2;
-        const size_t spp = shfl_size(pp, tl);
-        if (__shfl_sync(0xFFFFFFFFu, pvalid ? 1 : 0, tl))
-            *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(a.pool_out) + spp * a.pool_c + a.pool_off + c0 +
-                                      4 * qd) =
+        if (d.pin)
+            *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(a.pool_out) + d.p + c0) =
                 make_uint2(pack_bf16x2(s4[0] * 0.25f, s4[1] * 0.25f), pack_bf16x2(s4[2] * 0.25f, s4[3] * 0.25f));
         __syncwarp();   // the next group rewrites ebuf
     }
@@ -316,6 +347,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
             const bool inside = y < a.H && x < a.W;
             const size_t pix = ((size_t)img * a.H + y) * a.W + x;
             const uint32_t base = tmem + (uint32_t)acc * ncols1 + ((uint32_t)(q * 32) << 16);
+            const EpiDst dst = epi_dst(a, img, x, y, inside, 16);   // y-neighbour: lane ^ 16 (16-pixel rows)
             for (int c0 = 0; c0 < a.cout; c0 += 16) {
                 uint32_t r[16];
                 tmem_ld16(base + (uint32_t)c0, r);
@@ -333,8 +365,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3(const __grid_constant_
                     store_f32(reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0, v,
                               min(16, a.n_store - c0));
                 } else {
-                    // y-neighbour: lane ^ 16 (16-pixel rows)
-                    epilogue_bf16(a, v, img, x, y, inside, c0, 16, ebuf + 64 * q);
+                    epilogue_bf16(a, v, dst, c0, 16, ebuf + 64 * q);
                 }
             }
             tc_fence_before();
@@ -526,6 +557,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
             const bool inside = y < a.H && x < a.W;
             const size_t pix = ((size_t)img * a.H + y) * a.W + x;
             const uint32_t base = tmem + (uint32_t)acc * ncols1 + ((uint32_t)(q * 32) << 16);
+            const EpiDst dst = epi_dst(a, img, x, y, inside, 8);   // y-neighbour: lane ^ 8 (8-pixel rows)
             for (int c0 = 0; c0 < a.cout; c0 += 16) {
                 uint32_t rr[16];
                 tmem_ld16(base + (uint32_t)c0, rr);
@@ -543,8 +575,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv3x3_halo(const __grid_cons
                     store_f32(reinterpret_cast<float*>(a.out) + pix * a.out_c + a.out_off + c0, v,
                               min(16, a.n_store - c0));
                 } else {
-                    // y-neighbour: lane ^ 8 (8-pixel rows)
-                    epilogue_bf16(a, v, img, x, y, inside, c0, 8, ebuf + 64 * q);
+                    epilogue_bf16(a, v, dst, c0, 8, ebuf + 64 * q);
                 }
             }
             tc_fence_before();
