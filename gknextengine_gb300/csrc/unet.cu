@@ -324,6 +324,9 @@ struct Unet {
         ConvArgs a{};
         a.B = B; a.H = H >> level; a.W = W >> level;
         a.cin = kLayers[l].cin; a.cout = kLayers[l].cout;
+        // the output layer stores 4 of its 32 channels: its first 16 weight rows (an MMA of
+        // N = 16) compute them; the gradients of the others are zero (their loss gradient is)
+        if (l == OUT) a.cout = 16;
         a.x_c = in_c; a.x_off = in_off;
         a.x_valid = in_c - in_off < a.cin ? in_c - in_off : 0;   // x0 holds fewer channels than E0A's 32
         a.bias = p + boff[l];
