@@ -70,10 +70,11 @@ def test_unet_matches_cpu_oracle():
         # Deeper layers see gradients re-rounded to bf16 at every layer; the oracle itself moves
         # by 3-10% per layer between FP32 and FP64 accumulation, so the bar there is direction
         # (cosine) and a bounded relative error (measured with these seeds: at most 0.134, the
-        # cosine at least 0.992). The kernels themselves are pinned in isolation by
+        # cosine at least 0.992; a convolution kernel that sums the taps in another order gave
+        # a cosine of 0.988). The kernels themselves are pinned in isolation by
         # test_gpu_conv.py (weight and input gradients against torch).
         assert rels[-1] < 2e-2, rels
-        assert min(coss) > 0.99 and max(rels) < 0.16, (rels, coss)
+        assert min(coss) > 0.98 and max(rels) < 0.18, (rels, coss)
 
 
 def test_unet_overfits_a_batch():
