@@ -77,6 +77,34 @@ def test_unet_matches_cpu_oracle():
         assert min(coss) > 0.98 and max(rels) < 0.18, (rels, coss)
 
 
+def test_backward_needs_a_forward_and_follows_inference():
+    """gkrt_unet_backward without a forward is a state error. After the inference forward it
+    re-runs the training forward on the same input, so a second backward (now on the training
+    forward's activations) gives the same gradients (up to the order of the weight-gradient
+    partial sums)."""
+    torch = _torch()
+    from gknextengine_gb300.native import GkrtError
+    with PathTracingRenderer(0) as r:
+        net = Unet(r, seed=9)
+        d = torch.zeros((1, 32, 32, 4), device="cuda")
+        with pytest.raises(GkrtError) as e:
+            net.backward(d)
+        assert e.value.code == abi.GKRT_ERR_STATE
+        g = torch.Generator(device="cuda").manual_seed(2)
+        inp = torch.rand((1, 32, 32, 10), device="cuda", generator=g)
+        raw = torch.zeros((1, 32, 32, 4), device="cuda")
+        net.forward(inp, out_raw=raw)
+        d = torch.randn((1, 32, 32, 4), device="cuda", generator=g) * 1e-3
+        net.zero_grad()
+        net.backward(d)
+        _, g1 = net.params(with_grads=True)
+        net.zero_grad()
+        net.backward(d)   # the activations are the training forward's now: the same gradients
+        _, g2 = net.params(with_grads=True)
+        assert np.isfinite(g1).all() and np.abs(g1).max() > 0
+        assert np.linalg.norm(g2 - g1) <= 1e-5 * np.linalg.norm(g1)
+
+
 def test_unet_overfits_a_batch():
     torch = _torch()
     with PathTracingRenderer(0) as r:
