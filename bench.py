@@ -47,7 +47,7 @@ NODE_BYTES, TRI_BYTES, RAY_BYTES = 64, 48, 32
 # warp instructions issued (sm__inst_executed.sum), thread instructions
 # (smsp__thread_inst_executed.sum), DRAM bytes read + written, and the rays of that launch.
 # The node and triangle reads of the algorithmic bytes are served by L1/L2.
-TRACE_NCU_1080P = {"inst": 1878357723, "thread_inst": 23367915045, "dram_bytes": 7472384 + 116647424,
+TRACE_NCU_1080P = {"inst": 1876796969, "thread_inst": 23252036915, "dram_bytes": 7515904 + 116706048,
                    "rays": 4483043}
 ISSUE_PER_SM_PER_CLOCK = 4   # four schedulers per SM, one warp instruction each per cycle
 
