@@ -5,8 +5,8 @@
 // are multiples of 32; weights are [Cout][3][3][Cin] bf16; accumulation is FP32 in tensor
 // memory.
 //
-// Persistent, warp-specialised CTAs loop over tiles of 8 x 16 pixels (M = 128) times all Cout
-// (N <= 256) of one image:
+// Persistent, warp-specialised CTAs loop over tiles of 16 x 8 pixels (x by y, M = 128) times
+// all Cout (N <= 256) of one image (outputs of up to 32 channels use the halo-tile kernel below):
 //   K loop   9 taps x Cin / 32 chunks. For tap (dy, dx) and chunk c the A operand is the
 //            4D TMA box {32 channels, 16 x, 8 y, 1 image} of the input shifted by the tap;
 //            coordinates outside the image read zeros, which is the zero padding. The B
@@ -24,9 +24,11 @@
 //            tile's accumulator; two accumulators in TMEM alternate between tiles, so the
 //            epilogue of one tile runs under the MMAs of the next.
 //   epilogue warps 2-5 (one per TMEM lane quarter) read their 32 lanes (pixels) 16 columns at
-//            a time, add the bias, apply ReLU, store bf16 (or fp32) NHWC at a channel offset of
-//            a wider tensor (skip connections are concatenated without copies), and release
-//            the accumulator.
+//            a time, add the bias (and an optional half-resolution parity addend), apply ReLU,
+//            store bf16 (or fp32) NHWC at a channel offset of a wider tensor (skip connections
+//            are concatenated without copies; bf16 through the warp's shared-memory exchange,
+//            whole 32-byte sectors per store), optionally with the 2 x 2 average and the
+//            nearest upsampling, and release the accumulator.
 // The grid holds as many CTAs per SM as shared memory and the 512 TMEM columns allow.
 // Every barrier wait is bounded; a wait that runs out records the wait error bit in the
 // device error word and the CTA skips its stores.
